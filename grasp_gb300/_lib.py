@@ -1,0 +1,134 @@
+"""ctypes bindings of libgraspgpu (the C ABI in include/grasp_gpu.h) and
+libgraspsynth (include/grasp_synth.h).
+
+The libraries are built in-tree (grasp_gb300/_build). Loading fails loudly
+when they are missing: there is no CPU fallback for the GPU path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+_d = C.POINTER(C.c_double)
+_i32 = C.POINTER(C.c_int32)
+_i64 = C.POINTER(C.c_int64)
+_int = C.POINTER(C.c_int)
+_u8 = C.POINTER(C.c_uint8)
+
+_gpu = None
+_synth = None
+
+
+class GGList(C.Structure):
+    _fields_ = [("nlab", C.c_int64), ("lab", _i32), ("start", _i64), ("loc", _i32), ("coeff", _d)]
+
+
+class GGDvdParams(C.Structure):
+    _fields_ = [
+        ("flavour", C.c_int), ("precision", C.c_int), ("lim", C.c_int), ("maxiter", C.c_int),
+        ("critr", C.c_double), ("critc", C.c_double), ("crite", C.c_double), ("robust", C.c_int),
+    ]
+
+
+class GSBlockSpec(C.Structure):
+    _fields_ = [
+        ("nw", C.c_int), ("np", _int), ("nak", _int), ("frozen", _u8), ("nref", C.c_int), ("refs", _u8),
+        ("max_rank", C.c_int), ("two_j", C.c_int), ("parity", C.c_int), ("kmaxf", C.c_int),
+        ("max_ncf", C.c_int64), ("density", C.c_double), ("coeff_scale", C.c_double), ("seed", C.c_uint64),
+    ]
+
+
+# symbol name -> (restype, argtypes); every symbol include/grasp_gpu.h declares
+GPU_SYMBOLS = {
+    "gg_last_error": (C.c_char_p, []),
+    "gg_version": (C.c_int, []),
+    "gg_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "gg_ctx_destroy": (C.c_int, [C.c_void_p]),
+    "gg_ctx_synchronize": (C.c_int, [C.c_void_p]),
+    "gg_set_grid": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, _d, _d, _d, _d]),
+    "gg_get_grid": (C.c_int, [C.c_void_p, _d, _d, _d]),
+    "gg_set_orbitals": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _int, _int, _d, _d]),
+    "gg_genintrk": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _i64, _int]),
+    "gg_get_rk_table": (C.c_int, [C.c_void_p, _i32, _d, _i32]),
+    "gg_rkintc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
+    "gg_slater": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
+    "gg_rinti": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _d]),
+    "gg_iabint_table": (C.c_int, [C.c_void_p, _d]),
+    "gg_hmat_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, _i64, _i32, C.POINTER(C.c_void_p)]),
+    "gg_hmat_destroy": (C.c_int, [C.c_void_p]),
+    "gg_setham_upload": (C.c_int, [C.c_void_p, C.c_void_p, _u8, C.POINTER(GGList), C.c_int, C.POINTER(GGList)]),
+    "gg_setham_assemble": (C.c_int, [C.c_void_p, C.c_void_p, _d]),
+    "gg_setham": (C.c_int, [C.c_void_p, C.c_void_p, _u8, C.POINTER(GGList), C.c_int, C.POINTER(GGList), _d]),
+    "gg_hmat_get_emt": (C.c_int, [C.c_void_p, _d]),
+    "gg_hmat_set_emt": (C.c_int, [C.c_void_p, _d]),
+    "gg_spicmv2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, _d, _d, C.c_int]),
+    "gg_maneig": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(GGDvdParams), _d, _d, _int, _int, _int]),
+    "gg_stage_stat": (C.c_double, [C.c_void_p, C.c_int]),
+}
+
+SYNTH_SYMBOLS = {
+    "gs_dcbsrw": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, _d, C.c_int, C.c_double, _d, _d, _d, _d, _int]),
+    "gs_screenpar": (C.c_int, [C.c_int, _int, C.c_int, _d]),
+    "gs_block_generate": (C.c_int, [C.POINTER(GSBlockSpec), C.POINTER(C.c_void_p)]),
+    "gs_block_free": (None, [C.c_void_p]),
+    "gs_block_sizes": (C.c_int, [C.c_void_p, _int, _i64, _int, _int, _i64, _i64]),
+    "gs_block_structure": (C.c_int, [C.c_void_p, _i64, _i32, _u8]),
+    "gs_block_list": (C.c_int, [C.c_void_p, C.c_int, _i32, _i64, _i32, _i32, _d]),
+}
+
+
+def _bind(lib, table):
+    for name, (res, args) in table.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+def lib_paths():
+    return _build.LIB_GPU, _build.LIB_SYNTH
+
+
+def ensure_built():
+    if not (os.path.exists(_build.LIB_GPU) and os.path.exists(_build.LIB_SYNTH)):
+        _build.build()
+
+
+def gpu():
+    """libgraspgpu, loaded on first use. Raises if it is missing."""
+    global _gpu
+    if _gpu is None:
+        if not os.path.exists(_build.LIB_GPU):
+            raise RuntimeError(
+                f"libgraspgpu.so not found at {_build.LIB_GPU}: build it with `python -m grasp_gb300.build` "
+                "(there is no CPU fallback)")
+        _gpu = _bind(C.CDLL(_build.LIB_GPU), GPU_SYMBOLS)
+    return _gpu
+
+
+def synth():
+    global _synth
+    if _synth is None:
+        if not os.path.exists(_build.LIB_SYNTH):
+            _build.build()
+        _synth = _bind(C.CDLL(_build.LIB_SYNTH), SYNTH_SYMBOLS)
+    return _synth
+
+
+class GGError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+def check(status):
+    if status != 0:
+        msg = gpu().gg_last_error()
+        raise GGError(status, msg.decode() if msg else "")
+    return status
+
+
+def ptr(a, t):
+    return a.ctypes.data_as(t)

@@ -1,0 +1,191 @@
+"""Python mirror of the reference's interface for the CI hot path, over the
+C ABI of libgraspgpu (include/grasp_gpu.h).
+
+Names follow the reference: :meth:`Context.genintrk` (rci90/genintrk.f90),
+:meth:`Context.slater` (lib9290/slater.f90), :meth:`Context.rinti`
+(lib9290/rinti.f90), :meth:`Context.rkintc` (rci90/rkintc.f90),
+:meth:`HMatrix.setham` (rmcdhf90/setham.f90), :meth:`HMatrix.spicmv2`
+(lib9290/spicmv2.f90), :meth:`HMatrix.maneig` (rci90/maneig.f90 /
+rmcdhf90/maneig.f90). Errors the reference turns into STOP raise GGError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import GGDvdParams, GGList, _d, _i32, _i64, _int, _u8, check, ptr
+
+FP64 = 0
+SPLIT = 1
+
+
+class Context:
+    """One GPU context: grid (grid_C), orbitals (wave_C), R^k and I(ab) tables."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        check(_lib.gpu().gg_ctx_create(device, C.byref(self._h)))
+        self.nw = 0
+        self.n = 0
+
+    def close(self):
+        if self._h:
+            _lib.gpu().gg_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # grid_C / npot_C
+    def set_grid(self, n, rnt, h, c, zz, r=None, rp=None, rpor=None):
+        zz = np.ascontiguousarray(zz, np.float64)
+        args = [None, None, None]
+        if r is not None:
+            self._r = [np.ascontiguousarray(x, np.float64) for x in (r, rp, rpor)]
+            args = [ptr(x, _d) for x in self._r]
+        check(_lib.gpu().gg_set_grid(self._h, n, rnt, h, c, *args, ptr(zz, _d)))
+        self.n = n
+
+    def grid(self):
+        r = np.zeros(self.n + 10); rp = np.zeros(self.n + 10); rpor = np.zeros(self.n + 10)
+        check(_lib.gpu().gg_get_grid(self._h, ptr(r, _d), ptr(rp, _d), ptr(rpor, _d)))
+        return r, rp, rpor
+
+    # wave_C
+    def set_orbitals(self, nak, mf, pf, qf):
+        nak = np.ascontiguousarray(nak, np.int32); mf = np.ascontiguousarray(mf, np.int32)
+        pf = np.ascontiguousarray(pf, np.float64); qf = np.ascontiguousarray(qf, np.float64)
+        nw, ld = pf.shape
+        check(_lib.gpu().gg_set_orbitals(self._h, nw, ld, ptr(nak, _int), ptr(mf, _int), ptr(pf, _d), ptr(qf, _d)))
+        self.nw = nw
+
+    def genintrk(self, kmax=-1, precision=FP64):
+        n = C.c_int64(); j2 = C.c_int()
+        check(_lib.gpu().gg_genintrk(self._h, kmax, precision, C.byref(n), C.byref(j2)))
+        self.n_rk = n.value
+        self.kloop = j2.value if kmax < 0 else kmax
+        return n.value, j2.value
+
+    def rk_table(self):
+        ind = np.zeros(self.n_rk, np.int32); val = np.zeros(self.n_rk); ks = np.zeros(self.kloop + 2, np.int32)
+        check(_lib.gpu().gg_get_rk_table(self._h, ptr(ind, _i32), ptr(val, _d), ptr(ks, _i32)))
+        return ind, val, ks
+
+    def rkintc(self, a, b, c, d, k):
+        out = C.c_double()
+        check(_lib.gpu().gg_rkintc(self._h, a, b, c, d, k, C.byref(out)))
+        return out.value
+
+    def slater(self, a, b, c, d, k):
+        out = C.c_double()
+        check(_lib.gpu().gg_slater(self._h, a, b, c, d, k, C.byref(out)))
+        return out.value
+
+    def rinti(self, j, k, mode=0):
+        out = C.c_double()
+        check(_lib.gpu().gg_rinti(self._h, j, k, mode, C.byref(out)))
+        return out.value
+
+    def iabint_table(self):
+        t = np.zeros(self.nw * self.nw)
+        check(_lib.gpu().gg_iabint_table(self._h, ptr(t, _d)))
+        return t.reshape(self.nw, self.nw)
+
+    def stage_stat(self, which):
+        return _lib.gpu().gg_stage_stat(self._h, which)
+
+    def synchronize(self):
+        check(_lib.gpu().gg_ctx_synchronize(self._h))
+
+
+def _mklist(d, keep):
+    lab = np.ascontiguousarray(d["lab"], np.int32); st = np.ascontiguousarray(d["start"], np.int64)
+    loc = np.ascontiguousarray(d["loc"], np.int32); co = np.ascontiguousarray(d["coeff"], np.float64)
+    keep.extend([lab, st, loc, co])
+    return GGList(lab.size, ptr(lab, _i32), ptr(st, _i64), ptr(loc, _i32), ptr(co, _d))
+
+
+class HMatrix:
+    """One Hamiltonian block on the device (hmat_C: EMT, IROW, IENDC)."""
+
+    def __init__(self, ctx: Context, ncf, iendc, irow):
+        self.ctx = ctx
+        self.ncf = int(ncf)
+        self.iendc = np.ascontiguousarray(iendc, np.int64)
+        self.irow = np.ascontiguousarray(irow, np.int32)
+        self.nnz = int(self.iendc[-1])
+        self._h = C.c_void_p()
+        check(_lib.gpu().gg_hmat_create(ctx._h, self.ncf, self.nnz, ptr(self.iendc, _i64), ptr(self.irow, _i32),
+                                        C.byref(self._h)))
+        self.eav = None
+
+    def close(self):
+        if self._h:
+            _lib.gpu().gg_hmat_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def setham_upload(self, iq, tlist, vlists):
+        keep = []
+        iq = np.ascontiguousarray(iq, np.uint8)
+        tl = _mklist(tlist, keep)
+        vl = (GGList * max(1, len(vlists)))(*[_mklist(v, keep) for v in vlists])
+        check(_lib.gpu().gg_setham_upload(self.ctx._h, self._h, ptr(iq, _u8), C.byref(tl), len(vlists) - 1, vl))
+
+    def setham_assemble(self):
+        eav = C.c_double()
+        check(_lib.gpu().gg_setham_assemble(self.ctx._h, self._h, C.byref(eav)))
+        self.eav = eav.value
+        return self.eav
+
+    def setham(self, iq, tlist, vlists):
+        """SETHAM + the EAV shift of MATRIX; returns EAV. EMT stays on the device."""
+        self.setham_upload(iq, tlist, vlists)
+        return self.setham_assemble()
+
+    def emt(self):
+        out = np.zeros(self.nnz)
+        check(_lib.gpu().gg_hmat_get_emt(self._h, ptr(out, _d)))
+        return out
+
+    def set_emt(self, emt):
+        emt = np.ascontiguousarray(emt, np.float64)
+        check(_lib.gpu().gg_hmat_set_emt(self._h, ptr(emt, _d)))
+
+    def spicmv2(self, b, precision=FP64):
+        b = np.asfortranarray(np.asarray(b, np.float64).reshape(self.ncf, -1))
+        c = np.zeros_like(b, order="F")
+        check(_lib.gpu().gg_spicmv2(self.ctx._h, self._h, b.shape[1], ptr(b, _d), ptr(c, _d), precision))
+        return c
+
+    def maneig(self, nvec, flavour=0, precision=FP64, lim=0, maxiter=0, critr=0.0, critc=0.0, crite=0.0,
+               robust=False, raise_on_maxiter=True):
+        p = GGDvdParams(flavour, precision, lim, maxiter, critr, critc, crite, int(robust))
+        ev = np.zeros(nvec); vec = np.zeros((nvec, self.ncf))
+        nl, nm, ie = C.c_int(), C.c_int(), C.c_int()
+        st = _lib.gpu().gg_maneig(self.ctx._h, self._h, nvec, C.byref(p), ptr(ev, _d), ptr(vec, _d), C.byref(nl),
+                                  C.byref(nm), C.byref(ie))
+        info = dict(nloops=nl.value, nmv=nm.value, ierr=ie.value, status=st)
+        if st != 0 and (raise_on_maxiter or st != _lib_status("GG_ERR_CONVERGE")):
+            check(st)
+        return ev, vec.T.copy(), info
+
+
+def _lib_status(name):
+    return {"GG_ERR_CONVERGE": -7}[name]

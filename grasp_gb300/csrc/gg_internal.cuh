@@ -1,0 +1,161 @@
+// gg_internal.cuh - shared state and helpers of libgraspgpu (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/grasp_gpu.h"
+
+namespace gg {
+
+void set_error(const std::string &msg);
+int fail(int status, const std::string &msg);
+
+#define GG_CUDA(call)                                                                   \
+  do {                                                                                  \
+    cudaError_t e_ = (call);                                                            \
+    if (e_ != cudaSuccess)                                                              \
+      return ::gg::fail(GG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define GG_TRY(call)             \
+  do {                           \
+    int s_ = (call);             \
+    if (s_ != GG_OK) return s_;  \
+  } while (0)
+
+constexpr int KLIMIT = 20;   // yzk.f90:54 (KLIMIT), kkstart_C KMAX
+constexpr int KEYORB = 215;  // parameter_def_M.f90:22
+constexpr int GPAD = 16;     // padding slots after NNN1 in device grid arrays
+
+// Device buffer with RAII.
+template <class T> struct DBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  DBuf(const DBuf &) = delete;
+  DBuf &operator=(const DBuf &) = delete;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  int alloc(size_t count) {
+    if (count <= n && p) return GG_OK;
+    release();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(GG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    n = count;
+    return GG_OK;
+  }
+};
+
+// Grid constants passed by value to kernels (SETQIC results, DEF_C values).
+struct QuadConst {
+  double C1, C2, C3, C4;
+  double CNC5C[4][3];  // CNC5C(i=2..5, j=2..4) -> [i-2][j-2]
+  double A13[13][13];  // LIC13_C A(13,13), row-major [i-1][j-1]
+  double accy;         // ACCY = H**6
+  double h, c;         // H, speed of light C
+  int n;               // N
+};
+
+struct Grid {
+  int n = 0;
+  double rnt = 0, h = 0, c = 0;
+  std::vector<double> R, RP, RPOR, ZZ;  // host, 1-based, size n + GPAD + 10
+  QuadConst q{};
+  DBuf<double> dR, dRP, dRPOR, dZZ;     // device, 1-based like the host copies
+  DBuf<double> dPow;                    // [4][KLIMIT+1][np]: RTTK, RTTKM, RTTK1, RTTKM1 ; k = 0 row holds RM
+  int np = 0;                           // row pitch of dPow (>= n + GPAD)
+};
+
+struct Orbitals {
+  int nw = 0, ld = 0;
+  std::vector<int> nak, mf, nkl, nkj;   // 1-based host copies
+  DBuf<double> dPF, dQF;                // [nw][ld]
+  DBuf<int> dMF, dNAK;                  // 1-based
+};
+
+struct RkTable {
+  int kloop = -1, j2max = 0;
+  int64_t n = 0;
+  std::vector<int32_t> kstart;          // KSTART(0:kloop+1)
+  std::vector<int32_t> hInd;            // host copy of INDTEIRK
+  DBuf<int32_t> dInd;
+  DBuf<double> dVal;
+  bool valid = false;
+};
+
+struct Lists {  // device copies of one block's T/V lists, concatenated in SETHAM order
+  int kmaxf = -1;
+  int64_t nlab = 0, ncontr = 0;
+  std::vector<int64_t> list_lab0;       // first label of each list (T, V0..Vkmaxf), size kmaxf + 3
+  DBuf<int32_t> dLab;                   // [nlab]
+  DBuf<int64_t> dStart;                 // [nlab + 1], global contribution offsets
+  DBuf<int32_t> dLoc;                   // [ncontr]
+  DBuf<double> dCoeff;                  // [ncontr]
+  DBuf<uint8_t> dIq;                    // [ncf][nw]
+  bool valid = false;
+};
+
+}  // namespace gg
+
+struct gg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  gg::Grid grid;
+  gg::Orbitals orb;
+  gg::RkTable rk;
+  gg::DBuf<double> dIab;                // [nw * nw]
+  bool iab_valid = false;
+  double stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+struct gg_hmat {
+  gg_ctx *ctx = nullptr;
+  int ncf = 0;
+  int64_t nnz = 0;
+  std::vector<int64_t> hIendc;          // IENDC(0:ncf)
+  gg::DBuf<int64_t> dIendc;             // [ncf + 1]
+  gg::DBuf<int32_t> dIrow;              // [nnz]
+  gg::DBuf<double> dEmt;                // [nnz]
+  gg::DBuf<double> dDiag;               // [ncf]
+  bool emt_valid = false;
+  double eav = 0.0;
+  gg::Lists lists;
+  // full symmetric CSR used by the matvec (both triangles, diagonal first)
+  bool sym_valid = false;
+  int64_t sym_nnz = 0;
+  gg::DBuf<int64_t> dSymPtr;            // [ncf + 1]
+  gg::DBuf<int32_t> dSymCol;            // [sym_nnz]
+  gg::DBuf<int64_t> dSymSrc;            // [sym_nnz] index into EMT
+  gg::DBuf<double> dSymVal;             // [sym_nnz] FP64 values
+  gg::DBuf<float> dSymHi, dSymLo;       // [sym_nnz] split values
+  gg::DBuf<float2> dXs;                 // [ncf] split copy of the input vector
+  bool sym_vals_valid = false;
+};
+
+namespace gg {
+// radial.cu
+int ensure_grid(gg_ctx *ctx);
+int ensure_orbitals(gg_ctx *ctx);
+// timing helpers (ctx.cu)
+int timer_start(gg_ctx *ctx);
+int timer_stop(gg_ctx *ctx, double *ms);
+// spmv.cu
+int build_sym(gg_hmat *h);
+int refresh_sym_values(gg_hmat *h);
+int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s);
+double spmv_bytes(const gg_hmat *h, int precision, int m);
+// hosteig.cpp: lowest m eigenpairs of a packed-upper symmetric matrix
+int sym_eig_lowest(int n, const double *ap, int m, double *w, double *z);
+}  // namespace gg

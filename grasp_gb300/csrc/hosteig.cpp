@@ -1,0 +1,257 @@
+// hosteig.cpp - lowest eigenpairs of the small Rayleigh-Ritz matrix S
+// (DVDSON's DSPEVX('V','I','U') call, libdvd90/dvdson.f90:724) on the host.
+//
+// S is at most LIM x LIM (LIM = 2 NVEC + 60 for rci): a few hundred
+// kilo-flops of dependent FP64 work per Davidson iteration. A Grace core runs
+// this several times faster than one GB300 SM (whose FP64 pipe is narrow),
+// so the N-length work stays on the GPU and this k x k problem runs here,
+// in FP64, once per iteration.
+//
+// Algorithm (the one DSPEVX uses): Householder reduction to tridiagonal form,
+// eigenvalues by the implicit QL method with Wilkinson shifts, eigenvectors of
+// the wanted eigenvalues by inverse iteration (re-orthogonalised within
+// clusters), back-transformed by the stored reflectors. References:
+// Golub & Van Loan, Matrix Computations (4th ed.), Alg. 8.3.1, 8.3.3, 8.2.2.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+namespace gg {
+
+namespace {
+
+struct Tri {
+  int n;
+  std::vector<double> d, e, v, beta;  // e[i] = T(i+1, i); v: reflector k in column k
+};
+
+void tridiag(int n, std::vector<double> &A, Tri &T) {  // A: full, column-major, lower used
+  T.n = n;
+  T.d.assign(n, 0.0);
+  T.e.assign(std::max(1, n - 1), 0.0);
+  T.v.assign((size_t)n * n, 0.0);
+  T.beta.assign(n, 0.0);
+  std::vector<double> p(n), w(n);
+  for (int k = 0; k + 2 < n; ++k) {
+    const int m = n - k - 1, o = k + 1;
+    double *x = &A[(size_t)k * n + o];
+    double sig = 0.0;
+    for (int i = 1; i < m; ++i) sig += x[i] * x[i];
+    double *vk = &T.v[(size_t)k * n];
+    vk[0] = 1.0;
+    for (int i = 1; i < m; ++i) vk[i] = x[i];
+    T.d[k] = A[(size_t)k * n + k];
+    if (sig == 0.0) {
+      T.e[k] = x[0];
+      T.beta[k] = 0.0;
+      continue;
+    }
+    const double mu = std::sqrt(x[0] * x[0] + sig);
+    const double v0 = (x[0] <= 0.0) ? x[0] - mu : -sig / (x[0] + mu);
+    const double beta = 2.0 * v0 * v0 / (sig + v0 * v0);
+    for (int i = 1; i < m; ++i) vk[i] /= v0;
+    T.e[k] = mu;
+    T.beta[k] = beta;
+    for (int i = 0; i < m; ++i) p[i] = 0.0;
+    for (int j = 0; j < m; ++j) {
+      const double *col = &A[(size_t)(o + j) * n + o];
+      const double vj = vk[j];
+      double acc = col[j] * vj;
+      for (int i = j + 1; i < m; ++i) {
+        p[i] += col[i] * vj;
+        acc += col[i] * vk[i];
+      }
+      p[j] += acc;
+    }
+    double pv = 0.0;
+    for (int i = 0; i < m; ++i) {
+      p[i] *= beta;
+      pv += p[i] * vk[i];
+    }
+    const double half = 0.5 * beta * pv;
+    for (int i = 0; i < m; ++i) w[i] = p[i] - half * vk[i];
+    for (int j = 0; j < m; ++j) {
+      double *col = &A[(size_t)(o + j) * n + o];
+      const double vj = vk[j], wj = w[j];
+      for (int i = j; i < m; ++i) col[i] -= vk[i] * wj + w[i] * vj;
+    }
+  }
+  if (n >= 2) {
+    T.d[n - 2] = A[(size_t)(n - 2) * n + (n - 2)];
+    T.e[n - 2] = A[(size_t)(n - 2) * n + (n - 1)];
+  }
+  T.d[n - 1] = A[(size_t)(n - 1) * n + (n - 1)];
+}
+
+// eigenvalues of the tridiagonal (d, e) by implicit QL; returns false on no convergence
+bool ql_values(int n, std::vector<double> d, std::vector<double> e, std::vector<double> &out) {
+  e.resize(n, 0.0);
+  // e[i] couples i and i+1; shift to the QL convention e[i] couples i-1, i
+  std::vector<double> ee(n, 0.0);
+  for (int i = 1; i < n; ++i) ee[i - 1] = e[i - 1];
+  for (int l = 0; l < n; ++l) {
+    int iter = 0, m;
+    do {
+      for (m = l; m < n - 1; ++m) {
+        const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(ee[m]) <= 2.220446049250313e-16 * dd) break;
+      }
+      if (m != l) {
+        if (iter++ == 60) return false;
+        double g = (d[l + 1] - d[l]) / (2.0 * ee[l]);
+        double r = std::hypot(g, 1.0);
+        g = d[m] - d[l] + ee[l] / (g + (g >= 0 ? std::fabs(r) : -std::fabs(r)));
+        double s = 1.0, c = 1.0, p = 0.0;
+        int i;
+        for (i = m - 1; i >= l; --i) {
+          double f = s * ee[i], b = c * ee[i];
+          ee[i + 1] = (r = std::hypot(f, g));
+          if (r == 0.0) {
+            d[i + 1] -= p;
+            ee[m] = 0.0;
+            break;
+          }
+          s = f / r;
+          c = g / r;
+          g = d[i + 1] - p;
+          r = (d[i] - g) * s + 2.0 * c * b;
+          d[i + 1] = g + (p = s * r);
+          g = c * r - b;
+        }
+        if (r == 0.0 && i >= l) continue;
+        d[l] -= p;
+        ee[l] = g;
+        ee[m] = 0.0;
+      }
+    } while (m != l);
+  }
+  out = d;
+  std::sort(out.begin(), out.end());
+  return true;
+}
+
+void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector<double>> &orth, unsigned seed,
+              double tnorm) {
+  const int n = T.n;
+  if (n == 1) {
+    x[0] = 1.0;
+    return;
+  }
+  const double tiny = 2.220446049250313e-16 * std::max(tnorm, 1e-300);
+  std::vector<double> u0(n), u1(n), u2(n), l(n);
+  std::vector<char> piv(n);
+  double a0 = T.d[0] - lam, a1 = T.e[0];
+  for (int i = 0; i < n; ++i) {
+    double sub = 0, b0 = 0, b1 = 0;
+    if (i + 1 < n) {
+      sub = T.e[i];
+      b0 = T.d[i + 1] - lam;
+      b1 = (i + 2 < n) ? T.e[i + 1] : 0.0;
+    }
+    if (i + 1 < n && std::fabs(sub) > std::fabs(a0)) {
+      piv[i] = 1;
+      const double m = a0 / sub;
+      l[i] = m;
+      u0[i] = sub;
+      u1[i] = b0;
+      u2[i] = b1;
+      const double n0 = a1 - m * b0, n1 = -m * b1;
+      a0 = n0;
+      a1 = n1;
+    } else {
+      piv[i] = 0;
+      if (a0 == 0.0) a0 = tiny;
+      const double m = (i + 1 < n) ? sub / a0 : 0.0;
+      l[i] = m;
+      u0[i] = a0;
+      u1[i] = a1;
+      u2[i] = 0.0;
+      a0 = b0 - m * a1;
+      a1 = b1;
+    }
+  }
+  unsigned s = 2463534242u ^ (seed * 2654435761u);
+  for (int i = 0; i < n; ++i) {
+    s ^= s << 13;
+    s ^= s >> 17;
+    s ^= s << 5;
+    x[i] = (double)(s & 0xffff) / 65536.0 - 0.5 + 1e-3;
+  }
+  for (int it = 0; it < 4; ++it) {
+    for (int i = 0; i + 1 < n; ++i) {
+      if (piv[i]) std::swap(x[i], x[i + 1]);
+      x[i + 1] -= l[i] * x[i];
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double v = x[i];
+      if (i + 1 < n) v -= u1[i] * x[i + 1];
+      if (i + 2 < n) v -= u2[i] * x[i + 2];
+      double d = u0[i];
+      if (std::fabs(d) < tiny) d = d < 0 ? -tiny : tiny;
+      x[i] = v / d;
+    }
+    for (const auto &q : orth) {
+      double dot = 0.0;
+      for (int i = 0; i < n; ++i) dot += q[i] * x[i];
+      for (int i = 0; i < n; ++i) x[i] -= dot * q[i];
+    }
+    double nrm = 0.0;
+    for (int i = 0; i < n; ++i) nrm += x[i] * x[i];
+    nrm = std::sqrt(nrm);
+    if (nrm == 0.0) nrm = 1.0;
+    const double inv = 1.0 / nrm;
+    for (int i = 0; i < n; ++i) x[i] *= inv;
+  }
+}
+
+}  // namespace
+
+// Lowest m eigenpairs of the symmetric n x n matrix given in packed upper
+// storage (AP(i + j(j-1)/2) = A(i,j), i <= j). w[m] ascending, z[n x m].
+int sym_eig_lowest(int n, const double *ap, int m, double *w, double *z) {
+  if (n <= 0 || m <= 0 || m > n) return -1;
+  std::vector<double> A((size_t)n * n);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i <= j; ++i) {
+      const double v = ap[i + (size_t)j * (j + 1) / 2];
+      A[(size_t)j * n + i] = v;
+      A[(size_t)i * n + j] = v;
+    }
+  Tri T;
+  tridiag(n, A, T);
+  std::vector<double> ev;
+  if (!ql_values(n, T.d, T.e, ev)) return -2;
+  double tnorm = 0.0;
+  for (int i = 0; i < n; ++i)
+    tnorm = std::max(tnorm, std::fabs(T.d[i]) + (i > 0 ? std::fabs(T.e[i - 1]) : 0.0) +
+                                (i + 1 < n ? std::fabs(T.e[i]) : 0.0));
+  const double ortol = 1e-3 * tnorm, eps = 2.220446049250313e-16;
+  std::vector<std::vector<double>> cluster;
+  std::vector<double> x(n);
+  double prev = 0.0;
+  for (int j = 0; j < m; ++j) {
+    double lam = ev[j];
+    w[j] = lam;
+    if (j > 0 && lam - prev > ortol) cluster.clear();
+    if (j > 0 && lam - prev < 10.0 * eps * std::fabs(lam)) lam = prev + 10.0 * eps * std::fabs(lam);
+    inv_iter(T, lam, x.data(), cluster, (unsigned)j + 1u, tnorm);
+    cluster.push_back(x);
+    prev = lam;
+    double *zj = z + (size_t)j * n;
+    for (int i = 0; i < n; ++i) zj[i] = x[i];
+    for (int k = n - 3; k >= 0; --k) {
+      const double beta = T.beta[k];
+      if (beta == 0.0) continue;
+      const double *vk = &T.v[(size_t)k * n];
+      const int mm = n - k - 1;
+      double *zz = zj + k + 1;
+      double dot = 0.0;
+      for (int i = 0; i < mm; ++i) dot += vk[i] * zz[i];
+      dot *= beta;
+      for (int i = 0; i < mm; ++i) zz[i] -= dot * vk[i];
+    }
+  }
+  return 0;
+}
+
+}  // namespace gg

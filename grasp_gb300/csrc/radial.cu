@@ -1,0 +1,794 @@
+// radial.cu - R^k table (GENINTRK/SLATER/YZK/QUAD) and one-body I(ab)
+// (RINTI/DPBDT) on the GPU.
+//
+// Compiled with -fmad=false: every multiply and add below is rounded on its
+// own, as in the reference's FP64 loops, so that the Y^k functions and the
+// per-integral quadratures reproduce the reference's arithmetic step by
+// step. The R^k contraction uses explicit fma() and is not bit-exact.
+//
+// Layout in HBM (all FP64):
+//   Y buffer   [nY][np]  Y^k_bd(r_i) at [f*np + i] (1-based i), zero beyond
+//                        the integration limit MTP(b,d) of SLATER.
+//   A buffer   [nP][KC]  w(i) * (P_a P_c + Q_a Q_c)(r_i) * RPOR(r_i) for
+//                        every pair a <= c, zero outside 2 <= i <= min(MF).
+//   VALTEIRK   [N_Rk]    written by the contraction epilogue in GENINTRK order.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "gg_internal.cuh"
+
+namespace gg {
+
+namespace {
+
+constexpr int KC_TILE = 16;  // contraction depth per shared-memory stage
+constexpr int BM = 32, BN = 64;
+
+struct YDesc {
+  int k, b, d;  // Y^k_{bd}
+  int mtp;      // min(MF(b), MF(d)) (YZK's MTP)
+  int mtpb;     // last point kept in the Y buffer (N when k == 0 and b == d)
+  int cs;       // first function index with the same (k, b)
+  int nd;       // number of functions with the same (k, b) = |D(b,k)|
+};
+
+struct RkTile {
+  int k, a;
+  int ncA;        // |C(a,k)|: rows of the (k,a) problem
+  int r0;         // first row of this tile
+  int rowpair0;   // offset into the row-pair list of the (k,a) problem
+  int cs_a;       // first column (Y function) of the (k,a) problem
+  int c0, c1;     // column range [c0, c1) of this tile
+  long long base; // 0-based VALTEIRK position of the (k,a) problem
+};
+
+struct QuadItem {  // one integral evaluated with the general QUAD
+  int a, c, f, mtp;
+  long long pos;
+};
+
+__device__ __forceinline__ double pf(const double *P, int ld, int i, int j) {
+  return P[(size_t)(j - 1) * ld + (i - 1)];
+}
+
+// QUAD (lib9290/quad.f90:52-103) on a 1-based array TA with room for
+// TA(MTP+3). Sequential, in the reference's order.
+__device__ double quad_seq(double *TA, int mtp, const double *R, const double *RP, const QuadConst &q) {
+  const int mtpm1 = mtp - 1;
+  for (int i = 2; i <= mtpm1; ++i) {
+    const double tai = TA[i];
+    if (fabs(tai) <= 0.0) continue;
+    const int ip1 = i + 1;
+    const double taip1 = TA[ip1];
+    const double quott = taip1 / tai;
+    if (quott <= 0.0) continue;
+    const double frip1 = taip1 / RP[ip1];
+    double fri = tai / RP[i];
+    const double ratio = frip1 / fri;
+    const double rip1 = R[ip1], ri = R[i];
+    const double sigma = log(ratio) / log(rip1 / ri);
+    fri = ri * fri;
+    double result = fri / (sigma + 1.0);
+    TA[mtp + 1] = 0.0;
+    TA[mtp + 2] = 0.0;
+    TA[mtp + 3] = 0.0;
+    result = result + q.C1 * tai;
+    double s = 0.0;
+    for (int j = ip1; j <= mtp; j += 4) s = s + (q.C2 * (TA[j] + TA[j + 2]) + q.C3 * TA[j + 1] + q.C4 * TA[j + 3]);
+    result = result + s;
+    if ((mtp - i) % 4 == 0) result = result - q.C1 * TA[mtp];
+    return result;
+  }
+  return 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// YZK part 1 (yzk.f90:105-126, 190-201): RHOP and the two TEMP arrays.
+//   TZ(i) = r^k RHOP(i), TW(i) = RHOP(i) / r^(k+1) on 2 <= i <= MTP, else 0.
+// ---------------------------------------------------------------------------
+__global__ void k_ytemp(const YDesc *__restrict__ yd, int nf, const double *__restrict__ PF,
+                        const double *__restrict__ QF, int ld, const double *__restrict__ RP,
+                        const double *__restrict__ pw, int np, double *__restrict__ TZ, double *__restrict__ TW) {
+  const int f = blockIdx.y;
+  if (f >= nf) return;
+  const YDesc y = yd[f];
+  const double *RTTK = pw + (size_t)(0 * (KLIMIT + 1) + y.k) * np;
+  const double *RTTKM1 = pw + (size_t)(3 * (KLIMIT + 1) + y.k) * np;
+  const double *RM = pw;  // row k = 0 of table 0
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    double tz = 0.0, tw = 0.0;
+    if (i >= 2 && i <= y.mtp) {
+      const double rhop =
+          RP[i] * (pf(PF, ld, i, y.b) * pf(PF, ld, i, y.d) + pf(QF, ld, i, y.b) * pf(QF, ld, i, y.d));
+      if (y.k == 0) {
+        tz = rhop;
+        tw = rhop * RM[i];
+      } else {
+        tz = RTTK[i] * rhop;
+        tw = rhop * RTTKM1[i];
+      }
+    }
+    TZ[(size_t)f * np + i] = tz;
+    TW[(size_t)f * np + i] = tw;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// YZK part 2 (yzk.f90:128-224): the four interleaved stride-4 Newton-Cotes
+// recurrences for Z (forward) and W (backward). One thread per (function,
+// residue class mod 4); the four threads of a function are adjacent lanes.
+// ---------------------------------------------------------------------------
+__global__ void k_ychain(const YDesc *__restrict__ yd, int nf, const double *__restrict__ TZ,
+                         const double *__restrict__ TW, const double *__restrict__ R,
+                         const double *__restrict__ pw, int np, QuadConst q, double *__restrict__ Y) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = t >> 2, c = t & 3;
+  const bool active = f < nf;
+  YDesc y = active ? yd[f] : yd[0];
+  const int K = y.k, MTP = y.mtp, MTPP3 = MTP + 3, N = q.n;
+  const double *T = TZ + (size_t)(active ? f : 0) * np;
+  const double *Tw = TW + (size_t)(active ? f : 0) * np;
+  double *Yf = Y + (size_t)(active ? f : 0) * np;
+  const int s = c + 2;  // chain start: 2, 3, 4, 5
+  double z = 0.0;
+  if (active) {
+    if (s <= 4) {
+      double sum = 0.0;
+      for (int kk = 2; kk <= 5; ++kk) sum = sum + q.CNC5C[kk - 2][s - 2] * T[kk];
+      z = sum;
+    } else {  // ZK(5) = ZK(1) + RTMP(5), ZK(1) = 0
+      const double rtmp = q.C1 * (T[1] + T[5]) + q.C2 * (T[2] + T[4]) + q.C3 * T[3];
+      z = 0.0 + rtmp;
+    }
+    Yf[s] = z;
+    for (int i = s + 4; i <= MTPP3; i += 4) {
+      const double rtmp = q.C1 * (T[i - 4] + T[i]) + q.C2 * (T[i - 3] + T[i - 1]) + q.C3 * T[i - 2];
+      z = z + rtmp;
+      Yf[i] = z;
+    }
+  }
+  // asymptotic value (yzk.f90:150-171)
+  const int owner = (MTPP3 - 2) & 3;
+  const double z_top = __shfl_sync(0xffffffffu, z, (threadIdx.x & ~3) + owner);
+  if (!active) return;
+  double zklim, dif = 0.0;
+  if (K == 0) {
+    zklim = (y.b == y.d) ? 1.0 : 0.0;
+    const double d0 = z - zklim;  // this chain's value at its last point (in [MTP, MTP+3])
+    if (fabs(d0) > q.accy) dif = d0;
+  } else {
+    zklim = z_top;
+  }
+  const double *RTTKM = pw + (size_t)(1 * (KLIMIT + 1) + K) * np;
+  const double *RTTK1 = pw + (size_t)(2 * (KLIMIT + 1) + K) * np;
+  // backward pass: W recurrence on i <= MTP, assembly of Y = Z + W on 2..N
+  int top = s;
+  while (top + 4 < np) top += 4;
+  double wk_next = 0.0;
+  for (int i = top; i >= s; i -= 4) {
+    if (i > N) {
+      Yf[i] = 0.0;
+      continue;
+    }
+    double zf;
+    if (K == 0) {
+      if (i <= MTPP3)
+        zf = (dif != 0.0) ? Yf[i] - dif : Yf[i];
+      else
+        zf = zklim;
+    } else {
+      zf = (i <= MTPP3) ? Yf[i] * RTTKM[i] : zklim * RTTKM[i];
+    }
+    double wkf = 0.0;
+    if (i <= MTP) {
+      const double wk = wk_next + q.C1 * (Tw[i] + Tw[i + 4]) + q.C2 * (Tw[i + 1] + Tw[i + 3]) + q.C3 * Tw[i + 2];
+      wk_next = wk;
+      wkf = (K == 0) ? wk * R[i] : wk * RTTK1[i];
+    }
+    double yv = zf + wkf;
+    if (i > y.mtpb) yv = 0.0;
+    Yf[i] = yv;
+  }
+}
+
+// A rows: w(i) (P_a P_c + Q_a Q_c) RPOR on 2 <= i <= min(MF(a), MF(c)).
+// w is the closed Newton-Cotes weight pattern of QUAD started at i = 2:
+// C1 at 2, then C2, C3, C2, C4 repeating.
+__global__ void k_apairs(const int2 *__restrict__ pairs, int npairs, const double *__restrict__ PF,
+                         const double *__restrict__ QF, int ld, const int *__restrict__ MF,
+                         const double *__restrict__ RPOR, int KC, QuadConst q, double *__restrict__ A) {
+  const int p = blockIdx.y;
+  if (p >= npairs) return;
+  const int a = pairs[p].x, c = pairs[p].y;
+  const int m = min(MF[a], MF[c]);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < KC; i += gridDim.x * blockDim.x) {
+    double v = 0.0;
+    if (i >= 2 && i <= m) {
+      const double rho = (pf(PF, ld, i, a) * pf(PF, ld, i, c) + pf(QF, ld, i, a) * pf(QF, ld, i, c)) * RPOR[i];
+      const int ph = (i - 2) & 3;
+      const double w = (i == 2) ? q.C1 : (ph == 1 || ph == 3) ? q.C2 : (ph == 2) ? q.C3 : q.C4;
+      v = w * rho;
+    }
+    A[(size_t)p * KC + i] = v;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// R^k contraction: for each (k, a) the GEMM  O[c, f] = sum_i A[(a,c), i] Y[f, i]
+// over the rows c in C(a,k) and the Y functions f = (b,d) with b >= a, then
+// QUAD's power-law head term and end-panel correction per entry. Output
+// positions follow GENINTRK's loop order (k, a, b, c, d).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_rk_gemm(const RkTile *__restrict__ tiles, const int *__restrict__ rowpair,
+                                                 const int2 *__restrict__ pairs, const double *__restrict__ A,
+                                                 const double *__restrict__ Y, const YDesc *__restrict__ yd, int KC,
+                                                 int np, const double *__restrict__ PF, const double *__restrict__ QF,
+                                                 int ld, const int *__restrict__ MF, const double *__restrict__ R,
+                                                 const double *__restrict__ RP, const double *__restrict__ RPOR,
+                                                 QuadConst q, double *__restrict__ val, long long nval,
+                                                 QuadItem *__restrict__ fb, int *__restrict__ nfb) {
+  __shared__ double As[2][KC_TILE][BM];
+  __shared__ double Bs[2][KC_TILE][BN + 1];
+  __shared__ int rowp[BM];
+  const RkTile T = tiles[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int nrow = min(BM, T.ncA - T.r0);
+  const int ncol = T.c1 - T.c0;
+  if (tid < BM) rowp[tid] = (tid < nrow) ? rowpair[T.rowpair0 + T.r0 + tid] : -1;
+  __syncthreads();
+  double acc[2][4];
+#pragma unroll
+  for (int u = 0; u < 2; ++u)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) acc[u][v] = 0.0;
+
+  auto load = [&](int buf, int k0) {
+    // A: BM rows x KC_TILE ; 256 threads -> 2 elements each
+    for (int e = tid; e < BM * KC_TILE; e += 256) {
+      const int r = e / KC_TILE, kk = e % KC_TILE;
+      const int p = rowp[r];
+      As[buf][kk][r] = (p >= 0) ? A[(size_t)p * KC + k0 + kk] : 0.0;
+    }
+    for (int e = tid; e < BN * KC_TILE; e += 256) {
+      const int j = e / KC_TILE, kk = e % KC_TILE;
+      Bs[buf][kk][j] = (j < ncol) ? Y[(size_t)(T.c0 + j) * np + k0 + kk] : 0.0;
+    }
+  };
+  const int nk = KC / KC_TILE;
+  load(0, 0);
+  __syncthreads();
+  for (int s = 0; s < nk; ++s) {
+    const int buf = s & 1;
+    if (s + 1 < nk) load(buf ^ 1, (s + 1) * KC_TILE);
+#pragma unroll
+    for (int kk = 0; kk < KC_TILE; ++kk) {
+      const double a0 = As[buf][kk][ty * 2 + 0], a1 = As[buf][kk][ty * 2 + 1];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double b = Bs[buf][kk][tx * 4 + v];
+        acc[0][v] = fma(a0, b, acc[0][v]);
+        acc[1][v] = fma(a1, b, acc[1][v]);
+      }
+    }
+    __syncthreads();
+  }
+  // epilogue
+  const int a = T.a;
+#pragma unroll
+  for (int u = 0; u < 2; ++u) {
+    const int r = ty * 2 + u;
+    if (r >= nrow) continue;
+    const int p = rowp[r];
+    const int c = pairs[p].y;
+    const int idx_c = T.r0 + r;
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const int j = tx * 4 + v;
+      if (j >= ncol) continue;
+      const int f = T.c0 + j;
+      const YDesc y = yd[f];
+      const long long pos =
+          T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)idx_c * y.nd + (long long)(f - y.cs);
+      if (pos < 0 || pos >= nval) {  // position outside the table: report, never write
+        atomicExch(nfb + 1, 1);
+        continue;
+      }
+      int mtp;
+      if (T.k == 0 && y.b == y.d)
+        mtp = min(MF[a], MF[c]);
+      else
+        mtp = min(min(y.mtp, MF[a]), MF[c]);
+      const double *Yf = Y + (size_t)f * np;
+      auto ta = [&](int i) {
+        return ((pf(PF, ld, i, a) * pf(PF, ld, i, c) + pf(QF, ld, i, a) * pf(QF, ld, i, c)) * RPOR[i]) * Yf[i];
+      };
+      bool ok = mtp >= 3;
+      double res = 0.0;
+      if (ok) {
+        const double tai = ta(2), taip1 = ta(3);
+        ok = !(fabs(tai) <= 0.0) && (taip1 / tai > 0.0);
+        if (ok) {
+          const double frip1 = taip1 / RP[3];
+          double fri = tai / RP[2];
+          const double ratio = frip1 / fri;
+          const double sigma = log(ratio) / log(R[3] / R[2]);
+          fri = R[2] * fri;
+          res = fri / (sigma + 1.0) + acc[u][v];
+          if ((mtp - 2) % 4 == 0) res = res - q.C1 * ta(mtp);
+        }
+      }
+      if (ok) {
+        val[pos] = res;
+      } else {
+        const int slot = atomicAdd(nfb, 1);
+        fb[slot] = QuadItem{a, c, f, mtp, pos};
+      }
+    }
+  }
+}
+
+// General per-integral QUAD: TA(i) = ((P_a P_c + Q_a Q_c) RPOR) Y_f(i),
+// one warp per integral, sequential reference-order sum on lane 0.
+__global__ void k_quad_items(const QuadItem *__restrict__ items, const int *__restrict__ nitems_p, int nitems_max,
+                             const double *__restrict__ Y, int np, const double *__restrict__ PF,
+                             const double *__restrict__ QF, int ld, const double *__restrict__ R,
+                             const double *__restrict__ RP, const double *__restrict__ RPOR, QuadConst q,
+                             double *__restrict__ out) {
+  extern __shared__ double sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  double *TA = sm + (size_t)warp * np;
+  const int nitems = nitems_p ? min(*nitems_p, nitems_max) : nitems_max;
+  for (int it = blockIdx.x * wpb + warp; it < nitems; it += gridDim.x * wpb) {
+    const QuadItem w = items[it];
+    const double *Yf = Y + (size_t)w.f * np;
+    for (int i = lane; i < np; i += 32) {
+      double v = 0.0;
+      if (i >= 2 && i <= w.mtp)
+        v = ((pf(PF, ld, i, w.a) * pf(PF, ld, i, w.c) + pf(QF, ld, i, w.a) * pf(QF, ld, i, w.c)) * RPOR[i]) * Yf[i];
+      TA[i] = v;
+    }
+    __syncwarp();
+    if (lane == 0) out[w.pos] = quad_seq(TA, w.mtp, R, RP, q);
+    __syncwarp();
+  }
+}
+
+// DPBDT (lib9290/dpbdt.f90:39-99): 13-point derivative of orbital J (per
+// grid index) into dP, dQ (1-based).
+__device__ void dpbdt_warp(const double *PF, const double *QF, int ld, int J, const QuadConst &q, double *dP,
+                           double *dQ, int lane) {
+  const int N = q.n;
+  const double A1 = q.A13[6][0], A2 = q.A13[6][1], A3 = q.A13[6][2], A4 = q.A13[6][3], A5 = q.A13[6][4],
+               A6 = q.A13[6][5];
+  for (int i = 1 + lane; i <= N; i += 32) {
+    double hp = 0.0, hq = 0.0;
+    if (i <= 6) {
+      for (int k = 1; k <= 13; ++k) hp = hp + q.A13[i - 1][k - 1] * pf(PF, ld, k, J);
+      for (int k = 1; k <= 13; ++k) hq = hq + q.A13[i - 1][k - 1] * pf(QF, ld, k, J);
+    } else if (i <= N - 6) {
+      hp = A1 * (pf(PF, ld, i - 6, J) - pf(PF, ld, i + 6, J)) + A2 * (pf(PF, ld, i - 5, J) - pf(PF, ld, i + 5, J)) +
+           A3 * (pf(PF, ld, i - 4, J) - pf(PF, ld, i + 4, J)) + A4 * (pf(PF, ld, i - 3, J) - pf(PF, ld, i + 3, J)) +
+           A5 * (pf(PF, ld, i - 2, J) - pf(PF, ld, i + 2, J)) + A6 * (pf(PF, ld, i - 1, J) - pf(PF, ld, i + 1, J));
+      hq = A1 * (pf(QF, ld, i - 6, J) - pf(QF, ld, i + 6, J)) + A2 * (pf(QF, ld, i - 5, J) - pf(QF, ld, i + 5, J)) +
+           A3 * (pf(QF, ld, i - 4, J) - pf(QF, ld, i + 4, J)) + A4 * (pf(QF, ld, i - 3, J) - pf(QF, ld, i + 3, J)) +
+           A5 * (pf(QF, ld, i - 2, J) - pf(QF, ld, i + 2, J)) + A6 * (pf(QF, ld, i - 1, J) - pf(QF, ld, i + 1, J));
+    } else {
+      const int irow = i - N + 13;
+      for (int k = 1; k <= 13; ++k) hp = hp + q.A13[irow - 1][k - 1] * pf(PF, ld, N - 13 + k, J);
+      for (int k = 1; k <= 13; ++k) hq = hq + q.A13[irow - 1][k - 1] * pf(QF, ld, N - 13 + k, J);
+    }
+    dP[i] = hp;
+    dQ[i] = hq;
+  }
+}
+
+// RINTI (lib9290/rinti.f90:53-100) for a list of (J, K) pairs: one warp each.
+__global__ void k_rinti(const int2 *__restrict__ jk, int npairs, int mode, const double *__restrict__ PF,
+                        const double *__restrict__ QF, int ld, const int *__restrict__ MF,
+                        const int *__restrict__ NAK, const double *__restrict__ R, const double *__restrict__ RP,
+                        const double *__restrict__ RPOR, const double *__restrict__ ZZ, int np, QuadConst q,
+                        double *__restrict__ out, const int *__restrict__ outidx) {
+  extern __shared__ double sm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  double *dP = sm + (size_t)warp * 3 * np;
+  double *dQ = dP + np;
+  double *TA = dQ + np;
+  for (int it = blockIdx.x * wpb + warp; it < npairs; it += gridDim.x * wpb) {
+    const int J = jk[it].x, K = jk[it].y;
+    const int mtp = max(MF[J], MF[K]);
+    const double C = q.c;
+    dpbdt_warp(PF, QF, ld, K, q, dP, dQ, lane);
+    __syncwarp();
+    for (int i = lane; i < np; i += 32) TA[i] = (i >= 2 && i <= mtp) ? pf(QF, ld, i, J) * dP[i] - pf(PF, ld, i, J) * dQ[i] : 0.0;
+    __syncwarp();
+    double piece1 = 0.0, piece2 = 0.0, piece3 = 0.0, piece4 = 0.0;
+    if (lane == 0) {
+      piece1 = quad_seq(TA, mtp, R, RP, q);
+      piece1 = C * piece1 / q.h;
+    }
+    __syncwarp();
+    for (int i = lane; i < np; i += 32)
+      TA[i] = (i >= 2 && i <= mtp) ? RP[i] * pf(QF, ld, i, J) * pf(QF, ld, i, K) : 0.0;
+    __syncwarp();
+    if (lane == 0) {
+      piece2 = quad_seq(TA, mtp, R, RP, q);
+      piece2 = -2.0 * C * C * piece2;
+    }
+    __syncwarp();
+    for (int i = lane; i < np; i += 32)
+      TA[i] = (i >= 2 && i <= mtp)
+                  ? RPOR[i] * (pf(PF, ld, i, J) * pf(QF, ld, i, K) + pf(QF, ld, i, J) * pf(PF, ld, i, K))
+                  : 0.0;
+    __syncwarp();
+    if (lane == 0) {
+      piece3 = quad_seq(TA, mtp, R, RP, q);
+      piece3 = piece3 * C * (double)NAK[K];
+    }
+    __syncwarp();
+    if (mode == 0) {
+      for (int i = lane; i < np; i += 32)
+        TA[i] = (i >= 2 && i <= mtp)
+                    ? RPOR[i] * ZZ[i] * (pf(PF, ld, i, J) * pf(PF, ld, i, K) + pf(QF, ld, i, J) * pf(QF, ld, i, K))
+                    : 0.0;
+      __syncwarp();
+      if (lane == 0) {
+        piece4 = quad_seq(TA, mtp, R, RP, q);
+        piece4 = -piece4;
+      }
+      __syncwarp();
+    }
+    if (lane == 0) out[outidx ? outidx[it] : it] = piece1 + piece2 + piece3 + piece4;
+    __syncwarp();
+  }
+}
+
+__global__ void k_fill(double *p, size_t n, double v) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+bool triangrk(int la, int k, int lb) {  // rci90/triangrk.f90:27-37
+  if ((k + la + lb) % 2 != 0) return false;
+  if (std::abs(la - lb) > k) return false;
+  if (la + lb < k) return false;
+  return true;
+}
+
+// Builds Y functions for the descriptor list on the device: TZ/TW scratch
+// then the chains. Y must hold nf * np doubles.
+int build_y(gg_ctx *ctx, const YDesc *d_yd, int nf, double *dY, DBuf<double> &scratch) {
+  Grid &g = ctx->grid;
+  Orbitals &o = ctx->orb;
+  const int np = g.np;
+  GG_TRY(scratch.alloc((size_t)2 * nf * np));
+  double *TZ = scratch.p, *TW = scratch.p + (size_t)nf * np;
+  dim3 grid1((np + 127) / 128, nf);
+  k_ytemp<<<grid1, 128, 0, ctx->stream>>>(d_yd, nf, o.dPF.p, o.dQF.p, o.ld, g.dRP.p, g.dPow.p, np, TZ, TW);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemsetAsync(dY, 0, (size_t)nf * np * sizeof(double), ctx->stream));
+  const int nthr = nf * 4;
+  k_ychain<<<(nthr + 127) / 128, 128, 0, ctx->stream>>>(d_yd, nf, TZ, TW, g.dR.p, g.dPow.p, np, g.q, dY);
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+template <class T> int upload(DBuf<T> &b, const std::vector<T> &h, cudaStream_t s) {
+  GG_TRY(b.alloc(h.size()));
+  if (!h.empty()) GG_CUDA(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return GG_OK;
+}
+
+}  // namespace
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max_out) {
+  GG_TRY(ensure_orbitals(ctx));
+  if (precision != GG_FP64) return fail(GG_ERR_ARG, "gg_genintrk: only GG_FP64 is implemented");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  Grid &g = ctx->grid;
+  Orbitals &o = ctx->orb;
+  RkTable &rk = ctx->rk;
+  const int NW = o.nw, KEY = NW + 1;
+  int j2max = o.nkj[1];
+  for (int i = 2; i <= NW; ++i) j2max = std::max(j2max, o.nkj[i]);
+  if (j2max > KLIMIT) return fail(GG_ERR_ARG, "genintrk: KMAX too small");
+  const int kloop = kmax < 0 ? j2max : kmax;
+  if (kloop > KLIMIT) return fail(GG_ERR_ARG, "genintrk: k beyond KLIMIT = 20");
+  GG_TRY(timer_start(ctx));
+
+  // Y functions, ordered (k, b, d): D(b,k) = {d >= b : TRIANGRK(l_b, k, l_d)}
+  std::vector<YDesc> yd;
+  std::vector<std::vector<int>> cs(kloop + 1, std::vector<int>(NW + 2, -1)), nd(kloop + 1, std::vector<int>(NW + 2, 0));
+  std::vector<int> kend(kloop + 1, 0);
+  for (int k = 0; k <= kloop; ++k) {
+    for (int b = 1; b <= NW; ++b) {
+      cs[k][b] = (int)yd.size();
+      for (int d = b; d <= NW; ++d)
+        if (triangrk(o.nkl[b], k, o.nkl[d])) {
+          YDesc y;
+          y.k = k;
+          y.b = b;
+          y.d = d;
+          y.mtp = std::min(o.mf[b], o.mf[d]);
+          y.mtpb = (k == 0 && b == d) ? g.n : y.mtp;
+          y.cs = cs[k][b];
+          y.nd = 0;
+          yd.push_back(y);
+        }
+      nd[k][b] = (int)yd.size() - cs[k][b];
+      for (int f = cs[k][b]; f < (int)yd.size(); ++f) yd[f].nd = nd[k][b];
+    }
+    kend[k] = (int)yd.size();
+  }
+  // pair list for the A rows (a <= c), k-independent
+  std::vector<int2> pairs;
+  std::vector<int> pidx((size_t)(NW + 1) * (NW + 1), -1);
+  for (int a = 1; a <= NW; ++a)
+    for (int c = a; c <= NW; ++c) {
+      pidx[(size_t)a * (NW + 1) + c] = (int)pairs.size();
+      pairs.push_back(make_int2(a, c));
+    }
+  // INDTEIRK and KSTART in GENINTRK order (rci90/genintrk.f90:64-86) and the
+  // contraction problems (k, a); each problem's entries are contiguous.
+  rk.kstart.assign(kloop + 2, 0);
+  rk.hInd.clear();
+  std::vector<RkTile> tiles;
+  std::vector<int> rowpair;
+  int64_t N = 0;
+  rk.kstart[0] = 1;
+  for (int k = 0; k <= kloop; ++k) {
+    for (int a = 1; a <= NW; ++a) {
+      const int ncA = nd[k][a];
+      if (ncA == 0) continue;
+      const int c0 = cs[k][a], c1 = kend[k];
+      const long long base = N;
+      // integer index list in reference order
+      for (int b = a; b <= NW; ++b)
+        for (int ic = 0; ic < ncA; ++ic) {
+          const int c = yd[cs[k][a] + ic].d;
+          for (int id = 0; id < nd[k][b]; ++id) {
+            const int d = yd[cs[k][b] + id].d;
+            rk.hInd.push_back(((a * KEY + b) * KEY + c) * KEY + d);
+          }
+        }
+      N = (int64_t)rk.hInd.size();
+      const int rp0 = (int)rowpair.size();
+      for (int ic = 0; ic < ncA; ++ic) rowpair.push_back(pidx[(size_t)a * (NW + 1) + yd[cs[k][a] + ic].d]);
+      for (int r0 = 0; r0 < ncA; r0 += BM)
+        for (int cc = c0; cc < c1; cc += BN) {
+          RkTile t;
+          t.k = k;
+          t.a = a;
+          t.ncA = ncA;
+          t.r0 = r0;
+          t.rowpair0 = rp0;
+          t.cs_a = c0;
+          t.c0 = cc;
+          t.c1 = std::min(c1, cc + BN);
+          t.base = base;
+          tiles.push_back(t);
+        }
+    }
+    rk.kstart[k + 1] = (int32_t)(N + 1);
+  }
+  if (N > INT32_MAX) return fail(GG_ERR_RANGE, "genintrk: table too large");
+  rk.n = N;
+  rk.kloop = kloop;
+  rk.j2max = j2max;
+  // device work
+  const int nf = (int)yd.size();
+  const int np = g.np;
+  const int KC = ((g.n + 1 + KC_TILE - 1) / KC_TILE) * KC_TILE;
+  if (KC > np) return fail(GG_ERR_ARG, "genintrk: grid padding too small");
+  DBuf<YDesc> dYd;
+  DBuf<int2> dPairs;
+  DBuf<RkTile> dTiles;
+  DBuf<int> dRowpair, dNfb;
+  DBuf<double> dY, dA, scratch;
+  DBuf<QuadItem> dFb;
+  GG_TRY(upload(dYd, yd, ctx->stream));
+  GG_TRY(upload(dPairs, pairs, ctx->stream));
+  GG_TRY(upload(dTiles, tiles, ctx->stream));
+  GG_TRY(upload(dRowpair, rowpair, ctx->stream));
+  GG_TRY(rk.dInd.alloc(std::max<int64_t>(N, 1)));
+  GG_TRY(rk.dVal.alloc(std::max<int64_t>(N, 1)));
+  if (N > 0)
+    GG_CUDA(cudaMemcpyAsync(rk.dInd.p, rk.hInd.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+  GG_TRY(dY.alloc((size_t)std::max(nf, 1) * np));
+  if (nf > 0) GG_TRY(build_y(ctx, dYd.p, nf, dY.p, scratch));
+  const int npairs = (int)pairs.size();
+  GG_TRY(dA.alloc((size_t)npairs * KC));
+  {
+    dim3 gr((KC + 127) / 128, npairs);
+    k_apairs<<<gr, 128, 0, ctx->stream>>>(dPairs.p, npairs, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dRPOR.p, KC, g.q, dA.p);
+    GG_CUDA(cudaGetLastError());
+  }
+  GG_TRY(dFb.alloc(std::max<int64_t>(N, 1)));
+  GG_TRY(dNfb.alloc(2));  // [0] fallback count, [1] position error flag
+  GG_CUDA(cudaMemsetAsync(dNfb.p, 0, 2 * sizeof(int), ctx->stream));
+  if (!tiles.empty()) {
+    k_rk_gemm<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(dTiles.p, dRowpair.p, dPairs.p, dA.p, dY.p, dYd.p, KC,
+                                                              np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p,
+                                                              g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p);
+    GG_CUDA(cudaGetLastError());
+  }
+  int hfb[2] = {0, 0};
+  GG_CUDA(cudaMemcpyAsync(hfb, dNfb.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (hfb[1]) return fail(GG_ERR_STATE, "genintrk: contraction produced a table position out of range");
+  const int nfb = hfb[0];
+  if (nfb > 0) {
+    const int wpb = 4;
+    const size_t smem = (size_t)wpb * np * sizeof(double);
+    const int blocks = std::min((nfb + wpb - 1) / wpb, 4096);
+    k_quad_items<<<blocks, 32 * wpb, smem, ctx->stream>>>(dFb.p, dNfb.p, nfb, dY.p, np, o.dPF.p, o.dQF.p, o.ld, g.dR.p,
+                                                          g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p);
+    GG_CUDA(cudaGetLastError());
+  }
+  double ms = 0;
+  GG_TRY(timer_stop(ctx, &ms));
+  ctx->stats[0] = ms;
+  rk.valid = true;
+  if (n_out) *n_out = N;
+  if (j2max_out) *j2max_out = j2max;
+  return GG_OK;
+}
+
+int gg_get_rk_table(gg_ctx *ctx, int32_t *indteirk, double *valteirk, int32_t *kstart) {
+  if (!ctx || !ctx->rk.valid) return fail(GG_ERR_STATE, "gg_get_rk_table: no table (call gg_genintrk)");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  const RkTable &rk = ctx->rk;
+  if (indteirk && rk.n) std::memcpy(indteirk, rk.hInd.data(), rk.n * sizeof(int32_t));
+  if (valteirk && rk.n) {
+    GG_CUDA(cudaMemcpyAsync(valteirk, rk.dVal.p, rk.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  if (kstart) std::memcpy(kstart, rk.kstart.data(), rk.kstart.size() * sizeof(int32_t));
+  return GG_OK;
+}
+
+int gg_rkintc(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *tegral) {
+  if (!ctx || !ctx->rk.valid) return fail(GG_ERR_STATE, "gg_rkintc: no table");
+  const RkTable &rk = ctx->rk;
+  const int nw = ctx->orb.nw, KEY = nw + 1;
+  if (k < 0 || k > rk.kloop || ia < 1 || ib < 1 || ic < 1 || id < 1 || ia > nw || ib > nw || ic > nw || id > nw)
+    return fail(GG_ERR_ARG, "gg_rkintc: index out of range");
+  // canonical order (rci90/rkintc.f90:45-62)
+  if (ia > ic) std::swap(ia, ic);
+  if (ib > id) std::swap(ib, id);
+  if (ia > ib) {
+    std::swap(ia, ib);
+    std::swap(ic, id);
+  }
+  const int32_t index = ((ia * KEY + ib) * KEY + ic) * KEY + id;
+  int64_t jl = rk.kstart[k], ju = rk.kstart[k + 1] - 1;
+  if (ju < jl || index < rk.hInd[jl - 1] || index > rk.hInd[ju - 1])
+    return fail(GG_ERR_NOTFOUND, "Something wrong in rkintc");
+  while (ju - jl > 1) {
+    const int64_t jm = (ju + jl) / 2;
+    if (rk.hInd[jm - 1] > index)
+      ju = jm;
+    else
+      jl = jm;
+  }
+  int64_t loc;
+  if (index == rk.hInd[ju - 1])
+    loc = ju;
+  else if (index == rk.hInd[jl - 1])
+    loc = jl;
+  else
+    return fail(GG_ERR_NOTFOUND, "Rkintc Integral not found");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_CUDA(cudaMemcpyAsync(tegral, rk.dVal.p + (loc - 1), sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GG_OK;
+}
+
+int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out) {
+  GG_TRY(ensure_orbitals(ctx));
+  Orbitals &o = ctx->orb;
+  Grid &g = ctx->grid;
+  const int nw = o.nw;
+  if (!out || k < 0 || k > KLIMIT || ia < 1 || ib < 1 || ic < 1 || id < 1 || ia > nw || ib > nw || ic > nw ||
+      id > nw)
+    return fail(GG_ERR_ARG, "gg_slater: bad arguments");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  YDesc y;
+  y.k = k;
+  y.b = ib;
+  y.d = id;
+  y.mtp = std::min(o.mf[ib], o.mf[id]);
+  y.mtpb = (k == 0 && ib == id) ? g.n : y.mtp;
+  y.cs = 0;
+  y.nd = 1;
+  // SLATER's integration limit (slater.f90:56-60)
+  QuadItem it;
+  it.a = ia;
+  it.c = ic;
+  it.f = 0;
+  it.mtp = (k == 0 && ib == id) ? std::min(o.mf[ia], o.mf[ic]) : std::min(std::min(y.mtp, o.mf[ia]), o.mf[ic]);
+  it.pos = 0;
+  std::vector<YDesc> hy{y};
+  std::vector<QuadItem> hi{it};
+  DBuf<YDesc> dy;
+  DBuf<QuadItem> di;
+  DBuf<double> dY, scratch, dout;
+  GG_TRY(upload(dy, hy, ctx->stream));
+  GG_TRY(upload(di, hi, ctx->stream));
+  GG_TRY(dY.alloc(g.np));
+  GG_TRY(dout.alloc(1));
+  GG_TRY(build_y(ctx, dy.p, 1, dY.p, scratch));
+  k_quad_items<<<1, 32, g.np * sizeof(double), ctx->stream>>>(di.p, nullptr, 1, dY.p, g.np, o.dPF.p, o.dQF.p, o.ld,
+                                                             g.dR.p, g.dRP.p, g.dRPOR.p, g.q, dout.p);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GG_OK;
+}
+
+static int run_rinti(gg_ctx *ctx, const std::vector<int2> &jk, int mode, double *dOut, const std::vector<int> *outidx) {
+  Orbitals &o = ctx->orb;
+  Grid &g = ctx->grid;
+  DBuf<int2> djk;
+  DBuf<int> didx;
+  GG_TRY(upload(djk, jk, ctx->stream));
+  if (outidx) GG_TRY(upload(didx, *outidx, ctx->stream));
+  const int wpb = 2;
+  const size_t smem = (size_t)wpb * 3 * g.np * sizeof(double);
+  const int blocks = std::max(1, std::min(((int)jk.size() + wpb - 1) / wpb, 2048));
+  k_rinti<<<blocks, 32 * wpb, smem, ctx->stream>>>(djk.p, (int)jk.size(), mode, o.dPF.p, o.dQF.p, o.ld, o.dMF.p,
+                                                   o.dNAK.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.dZZ.p, g.np, g.q, dOut,
+                                                   outidx ? didx.p : nullptr);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GG_OK;
+}
+
+int gg_rinti(gg_ctx *ctx, int j, int k, int mode, double *out) {
+  GG_TRY(ensure_orbitals(ctx));
+  const Orbitals &o = ctx->orb;
+  if (!out || j < 1 || k < 1 || j > o.nw || k > o.nw) return fail(GG_ERR_ARG, "gg_rinti: bad arguments");
+  if (o.nak[j] != o.nak[k]) return fail(GG_ERR_KAPPA, "RINTI: Attempt to calculate I(a,b) with kappa(a) != kappa(b)");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  DBuf<double> d;
+  GG_TRY(d.alloc(1));
+  GG_TRY(run_rinti(ctx, {make_int2(j, k)}, mode, d.p, nullptr));
+  GG_CUDA(cudaMemcpy(out, d.p, sizeof(double), cudaMemcpyDeviceToHost));
+  return GG_OK;
+}
+
+int gg_iabint_table(gg_ctx *ctx, double *iab) {
+  GG_TRY(ensure_orbitals(ctx));
+  GG_CUDA(cudaSetDevice(ctx->device));
+  const Orbitals &o = ctx->orb;
+  const int nw = o.nw;
+  GG_TRY(timer_start(ctx));
+  GG_TRY(ctx->dIab.alloc((size_t)nw * nw));
+  k_fill<<<64, 256, 0, ctx->stream>>>(ctx->dIab.p, (size_t)nw * nw, nan(""));
+  GG_CUDA(cudaGetLastError());
+  std::vector<int2> jk;
+  std::vector<int> idx;
+  for (int a = 1; a <= nw; ++a)
+    for (int b = 1; b <= nw; ++b)
+      if (o.nak[a] == o.nak[b]) {
+        jk.push_back(make_int2(a, b));
+        idx.push_back((a - 1) * nw + (b - 1));
+      }
+  if (!jk.empty()) GG_TRY(run_rinti(ctx, jk, 0, ctx->dIab.p, &idx));
+  double ms = 0;
+  GG_TRY(timer_stop(ctx, &ms));
+  ctx->stats[1] = ms;
+  ctx->iab_valid = true;
+  if (iab) GG_CUDA(cudaMemcpy(iab, ctx->dIab.p, (size_t)nw * nw * sizeof(double), cudaMemcpyDeviceToHost));
+  return GG_OK;
+}
+
+}  // extern "C"

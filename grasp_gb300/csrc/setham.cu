@@ -1,0 +1,639 @@
+// setham.cu - Hamiltonian assembly from rangular's T/V lists on the GPU
+// (rmcdhf90/setham.f90:3-352, the EAV shift of rmcdhf90/matrix.f90:178-203).
+//
+// Compiled with -fmad=false: EMT(LOC) = EMT(LOC) + TEGRAL*COEFF is rounded
+// twice, as the reference does.
+//
+// Method. The reference scatters, label by label, EMT(LOC) += I * COEFF.
+// Here every contribution is first given the slot of its integral in one
+// device array [VALTEIRK | I(ab) table]; the contributions are then
+// transposed into per-element segments (a counting sort by LOC whose
+// segments are sorted back into list order), so that one thread per matrix
+// element adds its contributions in exactly the reference's order (T list,
+// then V^0 .. V^kmaxf, labels in file order). No floating-point atomics: the
+// result is deterministic and equals the reference's sequence of roundings
+// given the same integrals.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "gg_internal.cuh"
+
+namespace gg {
+namespace {
+
+struct DiagTerm {
+  int type;    // 0 I(aa) IQ ; 1 F0(aa) ; 2 Fk(aa) ; 3 F0(ab) ; 4 Gk(ab)
+  int a, b;    // 0-based orbital indices
+  int full_a, full_b;  // 2j+1 of a, b
+  double fac;  // CLRX(...) for types 2 and 4
+  long long slot;
+};
+
+// GAM(I) = log((I-1)!) (lib9290/factt.f90)
+struct Gam {
+  double g[512];
+  Gam() {
+    g[0] = 0.0;
+    g[1] = 1.0;
+    g[2] = 1.0;
+    double x = 2.0;
+    for (int i = 3; i <= 30; ++i) {
+      g[i] = g[i - 1] * x;
+      x = x + 1.0;
+    }
+    for (int i = 1; i <= 30; ++i) g[i] = std::log(g[i]);
+    x = 30.0;
+    for (int i = 31; i < 512; ++i) {
+      g[i] = g[i - 1] + std::log(x);
+      x = x + 1.0;
+    }
+  }
+};
+
+// CLRX (lib9290/clrx.f90): the 3j symbol (ja k jb; 1/2 0 -1/2) up to sign
+// conventions, from log-factorials.
+double clrx(int kappaa, int k, int kappab) {
+  static const Gam G;
+  const double *GAM = G.g;
+  const int ka = std::abs(kappaa), kb = std::abs(kappab);
+  if (std::abs(ka - kb) <= k && ka + kb - 1 >= k) {
+    double exptrm = -std::log((double)(ka * kb));
+    const int kapkb = ka + kb, kabkp = kapkb + k, kamkb = ka - kb, kbmka = kb - ka;
+    exptrm = 0.5 * (exptrm + GAM[kapkb - k] + GAM[kamkb + k + 1] + GAM[kbmka + k + 1] - GAM[kabkp + 1]);
+    double r;
+    if (kabkp % 2 == 0) {
+      r = ((3 * kabkp / 2) % 2 == 0) ? 1.0 : -1.0;
+      exptrm = exptrm + GAM[(kabkp + 2) / 2] - GAM[(kapkb - k) / 2] - GAM[(kamkb + k + 2) / 2] -
+               GAM[(kbmka + k + 2) / 2];
+    } else {
+      r = (((3 * kabkp - 1) / 2) % 2 == 0) ? 1.0 : -1.0;
+      exptrm = exptrm + GAM[(kabkp + 1) / 2] - GAM[(kapkb - k + 1) / 2] - GAM[(kamkb + k + 1) / 2] -
+               GAM[(kbmka + k + 1) / 2];
+    }
+    return r * std::exp(exptrm);
+  }
+  return 0.0;
+}
+
+// canonical RKINTC position of R^k(abcd) in the device table; -1 if absent
+__device__ long long rk_lookup(const int32_t *ind, const int32_t *kstart, int kloop, int key, int ia, int ib, int ic,
+                               int id, int k) {
+  if (k < 0 || k > kloop) return -1;
+  if (ia > ic) {
+    const int t = ia;
+    ia = ic;
+    ic = t;
+  }
+  if (ib > id) {
+    const int t = ib;
+    ib = id;
+    id = t;
+  }
+  if (ia > ib) {
+    int t = ia;
+    ia = ib;
+    ib = t;
+    t = ic;
+    ic = id;
+    id = t;
+  }
+  const int32_t index = ((ia * key + ib) * key + ic) * key + id;
+  long long jl = kstart[k], ju = (long long)kstart[k + 1] - 1;
+  if (ju < jl) return -1;
+  if (index < ind[jl - 1] || index > ind[ju - 1]) return -1;
+  while (ju - jl > 1) {
+    const long long jm = (ju + jl) / 2;
+    if (ind[jm - 1] > index)
+      ju = jm;
+    else
+      jl = jm;
+  }
+  if (index == ind[ju - 1]) return ju - 1;
+  if (index == ind[jl - 1]) return jl - 1;
+  return -1;
+}
+
+// Label -> integral slot, and the slot of each contribution (one warp per label).
+__global__ void k_label_slots(const int32_t *__restrict__ lab, const int64_t *__restrict__ start, int64_t nlab,
+                              const int64_t *__restrict__ list_lab0, int nlists, int nw, const int *__restrict__ nak,
+                              const int32_t *__restrict__ ind, const int32_t *__restrict__ kstart, int kloop,
+                              long long nrk, int32_t *__restrict__ cslot, int *__restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  for (long long l = wid; l < nlab; l += nwarps) {
+    int list = 0;
+    while (list + 1 < nlists && l >= list_lab0[list + 1]) ++list;
+    int32_t L = lab[l];
+    long long slot = -1;
+    if (list == 0) {  // T list: IA = MOD(LAB,KEY), IB = LAB/KEY (setham.f90:244-245)
+      const int ia = L % KEYORB, ib = L / KEYORB;
+      if (ia >= 1 && ib >= 1 && ia <= nw && ib <= nw && nak[ia] == nak[ib]) slot = nrk + (long long)(ia - 1) * nw + (ib - 1);
+    } else {  // V^k list (setham.f90:305-310)
+      const int k = list - 1;
+      const int id = L % KEYORB;
+      L = L / KEYORB;
+      const int ib = L % KEYORB;
+      L = L / KEYORB;
+      const int ic = L % KEYORB;
+      const int ia = L / KEYORB;
+      if (ia >= 1 && ib >= 1 && ic >= 1 && id >= 1 && ia <= nw && ib <= nw && ic <= nw && id <= nw)
+        slot = rk_lookup(ind, kstart, kloop, nw + 1, ia, ib, ic, id, k);
+    }
+    if (slot < 0) {
+      if (lane == 0) atomicExch(err, 1);
+      slot = 0;
+    }
+    for (long long j = start[l] + lane; j < start[l + 1]; j += 32) cslot[j] = (int32_t)slot;
+  }
+}
+
+__global__ void k_count_loc(const int32_t *__restrict__ loc, int64_t n, int64_t nnz, int *__restrict__ cnt,
+                            int *__restrict__ err) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t L = loc[j];
+    if (L < 1 || (int64_t)L > nnz) {
+      atomicExch(err, 2);
+      continue;
+    }
+    atomicAdd(&cnt[L - 1], 1);
+  }
+}
+
+// exclusive scan of cnt[n] into off[n+1] (int64), three phases
+__global__ void k_scan_blocks(const int *__restrict__ cnt, int64_t n, int64_t *__restrict__ part, int64_t chunk) {
+  __shared__ long long s[1024];
+  const int64_t b = blockIdx.x;
+  const int64_t lo = b * chunk, hi = min(n, lo + chunk);
+  long long acc = 0;
+  for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) acc += cnt[i];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] += s[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[b] = s[0];
+}
+__global__ void k_scan_parts(int64_t *part, int64_t nparts) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    long long acc = 0;
+    for (int64_t i = 0; i < nparts; ++i) {
+      const long long v = part[i];
+      part[i] = acc;
+      acc += v;
+    }
+    part[nparts] = acc;
+  }
+}
+__global__ void k_scan_final(const int *__restrict__ cnt, int64_t n, const int64_t *__restrict__ part, int64_t chunk,
+                             int64_t *__restrict__ off) {
+  // one block per chunk; serial over warps-sized pieces with a block scan
+  __shared__ long long s[1024];
+  const int64_t b = blockIdx.x;
+  const int64_t lo = b * chunk, hi = min(n, lo + chunk);
+  long long base = part[b];
+  for (int64_t i0 = lo; i0 < hi; i0 += blockDim.x) {
+    const int64_t i = i0 + threadIdx.x;
+    const long long v = (i < hi) ? cnt[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = 1; w < (int)blockDim.x; w <<= 1) {
+      long long t = ((int)threadIdx.x >= w) ? s[threadIdx.x - w] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < hi) off[i] = base + s[threadIdx.x] - v;
+    const long long tot = s[blockDim.x - 1];
+    __syncthreads();
+    base += tot;
+  }
+  if (b == gridDim.x - 1 && threadIdx.x == 0) off[n] = part[gridDim.x];
+}
+
+__global__ void k_scatter_perm(const int32_t *__restrict__ loc, int64_t n, const int64_t *__restrict__ off,
+                               int *__restrict__ fill, int32_t *__restrict__ perm) {
+  for (int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; j < n; j += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t L = loc[j];
+    const int r = atomicAdd(&fill[L - 1], 1);
+    perm[off[L - 1] + r] = (int32_t)j;
+  }
+}
+
+// sort each element's segment back into list order, then gather the
+// coefficient and integral slot of each contribution
+__global__ void k_sort_gather(const int64_t *__restrict__ off, int64_t nnz, int32_t *__restrict__ perm,
+                              const double *__restrict__ coeff, const int32_t *__restrict__ cslot,
+                              double *__restrict__ coeff_s, int32_t *__restrict__ slot_s) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t lo = off[e], hi = off[e + 1];
+    for (int64_t i = lo + 1; i < hi; ++i) {
+      const int32_t v = perm[i];
+      int64_t j = i - 1;
+      while (j >= lo && perm[j] > v) {
+        perm[j + 1] = perm[j];
+        --j;
+      }
+      perm[j + 1] = v;
+    }
+    for (int64_t i = lo; i < hi; ++i) {
+      const int32_t p = perm[i];
+      coeff_s[i] = coeff[p];
+      slot_s[i] = cslot[p];
+    }
+  }
+}
+
+// Diagonal pieces without MCP coefficients (setham.f90:83-219), one thread
+// per CSF, terms in the reference's loop order, zero coefficients skipped.
+__global__ void k_diag_terms(const DiagTerm *__restrict__ terms, int nterms, const uint8_t *__restrict__ iq, int nw,
+                             int ncf, const int64_t *__restrict__ iendc, const double *__restrict__ integ,
+                             double *__restrict__ emt) {
+  const int ir = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ir >= ncf) return;
+  const uint8_t *q = iq + (size_t)ir * nw;
+  double acc = 0.0;
+  for (int t = 0; t < nterms; ++t) {
+    const DiagTerm T = terms[t];
+    const int qa = q[T.a];
+    double coef = 0.0;
+    switch (T.type) {
+      case 0:  // IQ(a) I(aa)
+        if (qa <= 0) continue;
+        coef = (double)qa;
+        break;
+      case 1:  // FCO(0,a,a) = (q(q-1))/2 (fco.f90)
+        coef = (double)((qa * (qa - 1)) / 2);
+        break;
+      case 2:  // FCO(k,a,a) for a full subshell
+        if (qa == T.full_a) {
+          const double fac = T.fac * (double)qa;
+          coef = -0.5 * fac * fac;
+        }
+        break;
+      case 3:  // FCO(0,a,b) = q_a q_b
+        coef = (double)(qa * (int)q[T.b]);
+        break;
+      case 4: {  // GCO(k,a,b) (gco.f90)
+        const int qb = q[T.b];
+        if (qa == T.full_a || qb == T.full_b) coef = -(double)(qa * qb) * T.fac * T.fac;
+        break;
+      }
+    }
+    if (coef == 0.0) continue;
+    acc = acc + coef * integ[T.slot];
+  }
+  emt[iendc[ir + 1] - 1] = acc;
+}
+
+// EMT(LOC) = EMT(LOC) + I * COEFF over the element's contributions, in order
+__global__ void k_assemble(const int64_t *__restrict__ off, int64_t nnz, const double *__restrict__ coeff_s,
+                           const int32_t *__restrict__ slot_s, const double *__restrict__ integ,
+                           double *__restrict__ emt) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t lo = off[e], hi = off[e + 1];
+    if (lo == hi) continue;
+    double acc = emt[e];
+    for (int64_t i = lo; i < hi; ++i) acc = acc + integ[slot_s[i]] * coeff_s[i];
+    emt[e] = acc;
+  }
+}
+
+// EAV = sum of diagonals / NCF (deterministic tree), then H - EAV I
+__global__ void k_eav(const int64_t *__restrict__ iendc, int ncf, double *__restrict__ emt, double *__restrict__ diag,
+                      double *__restrict__ eav_out) {
+  __shared__ double s[1024];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < ncf; i += blockDim.x) acc = acc + emt[iendc[i + 1] - 1];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) s[threadIdx.x] = s[threadIdx.x] + s[threadIdx.x + w];
+    __syncthreads();
+  }
+  const double eav = s[0] / (double)ncf;
+  for (int i = threadIdx.x; i < ncf; i += blockDim.x) {
+    const int64_t p = iendc[i + 1] - 1;
+    const double v = emt[p] - eav;
+    emt[p] = v;
+    diag[i] = v;
+  }
+  if (threadIdx.x == 0) *eav_out = eav;
+}
+
+template <class T> int upload(DBuf<T> &b, const T *h, size_t n, cudaStream_t s) {
+  GG_TRY(b.alloc(n));
+  if (n) GG_CUDA(cudaMemcpyAsync(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  return GG_OK;
+}
+
+// host-side RKINTC position (0-based) in the context table, -1 if absent
+long long host_rk_pos(const RkTable &rk, int nw, int ia, int ib, int ic, int id, int k) {
+  if (k > rk.kloop) return -1;
+  const int KEY = nw + 1;
+  if (ia > ic) std::swap(ia, ic);
+  if (ib > id) std::swap(ib, id);
+  if (ia > ib) {
+    std::swap(ia, ib);
+    std::swap(ic, id);
+  }
+  const int32_t index = ((ia * KEY + ib) * KEY + ic) * KEY + id;
+  const int32_t *b = rk.hInd.data() + (rk.kstart[k] - 1);
+  const int32_t *e = rk.hInd.data() + (rk.kstart[k + 1] - 1);
+  const int32_t *p = std::lower_bound(b, e, index);
+  if (p == e || *p != index) return -1;
+  return p - rk.hInd.data();
+}
+
+}  // namespace
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_hmat_create(gg_ctx *ctx, int ncf, int64_t nnz, const int64_t *iendc, const int32_t *irow, gg_hmat **out) {
+  if (!ctx || !out || !iendc || !irow || ncf < 1 || nnz < ncf) return fail(GG_ERR_ARG, "gg_hmat_create: bad arguments");
+  *out = nullptr;
+  if (iendc[0] != 0 || iendc[ncf] != nnz) return fail(GG_ERR_ARG, "gg_hmat_create: IENDC(0) must be 0, IENDC(NCF) = NNZ");
+  for (int i = 1; i <= ncf; ++i) {
+    if (iendc[i] <= iendc[i - 1]) return fail(GG_ERR_ARG, "gg_hmat_create: empty row (the diagonal is required)");
+    // diagonal last in each row (lower-triangle-by-rows mode, spicmv2.f90)
+    if (irow[iendc[i] - 1] != i) return fail(GG_ERR_ARG, "gg_hmat_create: row does not end with its diagonal");
+    for (int64_t p = iendc[i - 1]; p < iendc[i] - 1; ++p)
+      if (irow[p] < 1 || irow[p] >= i) return fail(GG_ERR_ARG, "gg_hmat_create: IROW outside the lower triangle");
+  }
+  GG_CUDA(cudaSetDevice(ctx->device));
+  gg_hmat *h = new gg_hmat;
+  h->ctx = ctx;
+  h->ncf = ncf;
+  h->nnz = nnz;
+  h->hIendc.assign(iendc, iendc + ncf + 1);
+  int s = upload(h->dIendc, iendc, (size_t)ncf + 1, ctx->stream);
+  if (s == GG_OK) s = upload(h->dIrow, irow, (size_t)nnz, ctx->stream);
+  if (s == GG_OK) s = h->dEmt.alloc(nnz);
+  if (s == GG_OK) s = h->dDiag.alloc(ncf);
+  if (s == GG_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess) s = fail(GG_ERR_CUDA, "gg_hmat_create: copy failed");
+  if (s != GG_OK) {
+    delete h;
+    return s;
+  }
+  *out = h;
+  return GG_OK;
+}
+
+int gg_hmat_destroy(gg_hmat *h) {
+  if (!h) return GG_OK;
+  cudaSetDevice(h->ctx->device);
+  cudaStreamSynchronize(h->ctx->stream);
+  delete h;
+  return GG_OK;
+}
+
+int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *tlist, int kmaxf,
+                     const gg_list *vlists) {
+  if (!ctx || !h || h->ctx != ctx || !iq || !tlist || kmaxf < -1 || (kmaxf >= 0 && !vlists))
+    return fail(GG_ERR_ARG, "gg_setham_upload: bad arguments");
+  GG_TRY(ensure_orbitals(ctx));
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_TRY(timer_start(ctx));
+  Lists &L = h->lists;
+  const int nlists = kmaxf + 2;
+  std::vector<const gg_list *> ls;
+  ls.push_back(tlist);
+  for (int k = 0; k <= kmaxf; ++k) ls.push_back(&vlists[k]);
+  int64_t nlab = 0, ncontr = 0;
+  L.list_lab0.assign(nlists + 1, 0);
+  for (int i = 0; i < nlists; ++i) {
+    const gg_list *x = ls[i];
+    if (x->nlab < 0 || (x->nlab > 0 && (!x->lab || !x->start || !x->loc || !x->coeff)))
+      return fail(GG_ERR_ARG, "gg_setham_upload: bad list");
+    if (x->nlab > 0 && x->start[0] != 0) return fail(GG_ERR_ARG, "gg_setham_upload: start[0] must be 0");
+    for (int64_t l = 0; l < x->nlab; ++l)
+      if (x->start[l + 1] < x->start[l]) return fail(GG_ERR_ARG, "gg_setham_upload: decreasing start[]");
+    L.list_lab0[i] = nlab;
+    nlab += x->nlab;
+    ncontr += x->nlab ? x->start[x->nlab] : 0;
+  }
+  L.list_lab0[nlists] = nlab;
+  if (ncontr > INT32_MAX) return fail(GG_ERR_RANGE, "gg_setham_upload: more than 2^31-1 contributions in one block");
+  L.kmaxf = kmaxf;
+  L.nlab = nlab;
+  L.ncontr = ncontr;
+  const int nw = ctx->orb.nw;
+  GG_TRY(L.dIq.alloc((size_t)h->ncf * nw));
+  GG_CUDA(cudaMemcpyAsync(L.dIq.p, iq, (size_t)h->ncf * nw, cudaMemcpyHostToDevice, ctx->stream));
+  GG_TRY(L.dLab.alloc(nlab));
+  GG_TRY(L.dStart.alloc(nlab + 1));
+  GG_TRY(L.dLoc.alloc(ncontr));
+  GG_TRY(L.dCoeff.alloc(ncontr));
+  // concatenate lists; label starts are shifted to global contribution offsets
+  std::vector<int64_t> st;
+  st.reserve(nlab + 1);
+  int64_t c0 = 0, l0 = 0;
+  for (int i = 0; i < nlists; ++i) {
+    const gg_list *x = ls[i];
+    if (x->nlab == 0) continue;
+    const int64_t nc = x->start[x->nlab];
+    for (int64_t l = 0; l < x->nlab; ++l) st.push_back(c0 + x->start[l]);
+    GG_CUDA(cudaMemcpyAsync(L.dLab.p + l0, x->lab, x->nlab * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    if (nc) {
+      GG_CUDA(cudaMemcpyAsync(L.dLoc.p + c0, x->loc, nc * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+      GG_CUDA(cudaMemcpyAsync(L.dCoeff.p + c0, x->coeff, nc * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    c0 += nc;
+    l0 += x->nlab;
+  }
+  st.push_back(c0);
+  GG_CUDA(cudaMemcpyAsync(L.dStart.p, st.data(), st.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+  double ms = 0;
+  GG_TRY(timer_stop(ctx, &ms));  // synchronises: the host vector st may go
+  ctx->stats[7] = ms;
+  L.valid = true;
+  h->emt_valid = false;
+  h->sym_vals_valid = false;
+  return GG_OK;
+}
+
+int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
+  if (!ctx || !h || h->ctx != ctx) return fail(GG_ERR_ARG, "gg_setham_assemble: bad arguments");
+  Lists &L = h->lists;
+  if (!L.valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no lists (call gg_setham_upload)");
+  if (!ctx->rk.valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no R^k table (call gg_genintrk)");
+  if (!ctx->iab_valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no I(ab) table (call gg_iabint_table)");
+  if (L.kmaxf > ctx->rk.kloop) return fail(GG_ERR_STATE, "gg_setham_assemble: R^k table does not reach KMAXF");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const Orbitals &o = ctx->orb;
+  const RkTable &rk = ctx->rk;
+  const int nw = o.nw, ncf = h->ncf;
+  const int64_t nnz = h->nnz, ncontr = L.ncontr;
+  GG_TRY(timer_start(ctx));
+  // combined integral array [VALTEIRK | I(ab)]
+  DBuf<double> integ;
+  const long long nrk = rk.n;
+  GG_TRY(integ.alloc((size_t)nrk + (size_t)nw * nw));
+  if (nrk) GG_CUDA(cudaMemcpyAsync(integ.p, rk.dVal.p, nrk * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  GG_CUDA(cudaMemcpyAsync(integ.p + nrk, ctx->dIab.p, (size_t)nw * nw * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  // diagonal term list in the loop order of setham.f90:83-219
+  std::vector<DiagTerm> terms;
+  auto iab_slot = [&](int a) { return (long long)nrk + (long long)(a - 1) * nw + (a - 1); };
+  auto add = [&](int type, int a, int b, int k, double fac) -> int {
+    DiagTerm t;
+    t.type = type;
+    t.a = a - 1;
+    t.b = b - 1;
+    t.full_a = o.nkj[a] + 1;
+    t.full_b = o.nkj[b] + 1;
+    t.fac = fac;
+    if (type == 0)
+      t.slot = iab_slot(a);
+    else if (type == 1 || type == 2)
+      t.slot = host_rk_pos(rk, nw, a, a, a, a, k);
+    else if (type == 3)
+      t.slot = host_rk_pos(rk, nw, a, b, a, b, 0);
+    else
+      t.slot = host_rk_pos(rk, nw, a, b, b, a, k);
+    if (t.slot < 0) return fail(GG_ERR_STATE, "setham: diagonal integral missing from the R^k table");
+    terms.push_back(t);
+    return GG_OK;
+  };
+  for (int a = 1; a <= nw; ++a) GG_TRY(add(0, a, a, 0, 0.0));
+  for (int a = 1; a <= nw; ++a) GG_TRY(add(1, a, a, 0, 0.0));
+  {
+    int km = 0, K = 0;
+    do {
+      K = K + 2;
+      for (int a = 1; a <= nw; ++a) {
+        const int k0 = o.nkj[a] - 1;
+        km = std::max(k0, km);
+        if (K > k0) continue;
+        GG_TRY(add(2, a, a, K, clrx(o.nak[a], K, o.nak[a])));
+      }
+    } while (K < km);
+  }
+  for (int a = 1; a <= nw - 1; ++a)
+    for (int b = a + 1; b <= nw; ++b) GG_TRY(add(3, a, b, 0, 0.0));
+  {
+    int km = 0, K = -1;
+    do {
+      K = K + 1;
+      for (int a = 1; a <= nw - 1; ++a)
+        for (int b = a + 1; b <= nw; ++b) {
+          const int nja = o.nkj[a], njb = o.nkj[b];
+          const int kmin = (o.nak[a] * o.nak[b] > 0) ? std::abs((nja - njb) / 2) : std::abs((nja - njb) / 2) + 1;
+          if ((K - kmin) % 2 != 0) continue;
+          const int kmx = (nja + njb) / 2;
+          km = std::max(kmx, km);
+          if (K < kmin || K > kmx) continue;
+          GG_TRY(add(4, a, b, K, clrx(o.nak[a], K, o.nak[b])));
+        }
+    } while (K < km);
+  }
+  DBuf<DiagTerm> dTerms;
+  GG_TRY(upload(dTerms, terms.data(), terms.size(), s));
+  DBuf<int32_t> cslot, perm, slot_s;
+  DBuf<int> cnt, fill, err;
+  DBuf<int64_t> off, part;
+  DBuf<double> coeff_s;
+  GG_TRY(cslot.alloc(ncontr));
+  GG_TRY(perm.alloc(ncontr));
+  GG_TRY(slot_s.alloc(ncontr));
+  GG_TRY(coeff_s.alloc(ncontr));
+  GG_TRY(cnt.alloc(nnz));
+  GG_TRY(fill.alloc(nnz));
+  GG_TRY(off.alloc(nnz + 1));
+  GG_TRY(err.alloc(1));
+  GG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
+  GG_CUDA(cudaMemsetAsync(cnt.p, 0, nnz * sizeof(int), s));
+  GG_CUDA(cudaMemsetAsync(fill.p, 0, nnz * sizeof(int), s));
+  DBuf<int64_t> dLab0;
+  GG_TRY(upload(dLab0, L.list_lab0.data(), L.list_lab0.size(), s));
+  DBuf<int32_t> dKstart;
+  GG_TRY(upload(dKstart, rk.kstart.data(), rk.kstart.size(), s));
+  const int nlists = L.kmaxf + 2;
+  if (L.nlab) {
+    const int blocks = (int)std::min<int64_t>((L.nlab * 32 + 255) / 256, 65535);
+    k_label_slots<<<blocks, 256, 0, s>>>(L.dLab.p, L.dStart.p, L.nlab, dLab0.p, nlists, nw, o.dNAK.p, rk.dInd.p,
+                                         dKstart.p, rk.kloop, nrk, cslot.p, err.p);
+    GG_CUDA(cudaGetLastError());
+  }
+  const int gblocks = 152 * 8;
+  if (ncontr) {
+    k_count_loc<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, nnz, cnt.p, err.p);
+    GG_CUDA(cudaGetLastError());
+  }
+  int herr = 0;
+  GG_CUDA(cudaMemcpyAsync(&herr, err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  if (herr == 1) return fail(GG_ERR_RANGE, "SETHAM: a list label has no integral (bad label or R^k not in the table)");
+  if (herr == 2) return fail(GG_ERR_RANGE, "SETHAM: Error in computing contribution: LOC > NELMNT");
+  {
+    const int64_t chunk = 1 << 16;
+    const int64_t nparts = (nnz + chunk - 1) / chunk;
+    GG_TRY(part.alloc(nparts + 1));
+    k_scan_blocks<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk);
+    k_scan_parts<<<1, 32, 0, s>>>(part.p, nparts);
+    k_scan_final<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk, off.p);
+    GG_CUDA(cudaGetLastError());
+  }
+  if (ncontr) {
+    k_scatter_perm<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, off.p, fill.p, perm.p);
+    k_sort_gather<<<gblocks, 256, 0, s>>>(off.p, nnz, perm.p, L.dCoeff.p, cslot.p, coeff_s.p, slot_s.p);
+    GG_CUDA(cudaGetLastError());
+  }
+  // EMT = 0 ; diagonal pieces ; list contributions ; EAV shift
+  GG_CUDA(cudaMemsetAsync(h->dEmt.p, 0, nnz * sizeof(double), s));
+  k_diag_terms<<<(ncf + 127) / 128, 128, 0, s>>>(dTerms.p, (int)terms.size(), L.dIq.p, nw, ncf, h->dIendc.p, integ.p,
+                                                 h->dEmt.p);
+  GG_CUDA(cudaGetLastError());
+  k_assemble<<<gblocks, 256, 0, s>>>(off.p, nnz, coeff_s.p, slot_s.p, integ.p, h->dEmt.p);
+  GG_CUDA(cudaGetLastError());
+  DBuf<double> deav;
+  GG_TRY(deav.alloc(1));
+  k_eav<<<1, 1024, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dDiag.p, deav.p);
+  GG_CUDA(cudaGetLastError());
+  double eav = 0;
+  GG_CUDA(cudaMemcpyAsync(&eav, deav.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  double ms = 0;
+  GG_TRY(timer_stop(ctx, &ms));
+  ctx->stats[2] = ms;
+  h->eav = eav;
+  h->emt_valid = true;
+  h->sym_vals_valid = false;
+  if (eav_out) *eav_out = eav;
+  return GG_OK;
+}
+
+int gg_setham(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *tlist, int kmaxf, const gg_list *vlists,
+              double *eav_out) {
+  GG_TRY(gg_setham_upload(ctx, h, iq, tlist, kmaxf, vlists));
+  return gg_setham_assemble(ctx, h, eav_out);
+}
+
+int gg_hmat_get_emt(gg_hmat *h, double *emt) {
+  if (!h || !emt) return fail(GG_ERR_ARG, "gg_hmat_get_emt: bad arguments");
+  if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_hmat_get_emt: EMT not assembled");
+  GG_CUDA(cudaSetDevice(h->ctx->device));
+  GG_CUDA(cudaMemcpyAsync(emt, h->dEmt.p, h->nnz * sizeof(double), cudaMemcpyDeviceToHost, h->ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(h->ctx->stream));
+  return GG_OK;
+}
+
+int gg_hmat_set_emt(gg_hmat *h, const double *emt) {
+  if (!h || !emt) return fail(GG_ERR_ARG, "gg_hmat_set_emt: bad arguments");
+  GG_CUDA(cudaSetDevice(h->ctx->device));
+  GG_CUDA(cudaMemcpyAsync(h->dEmt.p, emt, h->nnz * sizeof(double), cudaMemcpyHostToDevice, h->ctx->stream));
+  std::vector<double> d(h->ncf);
+  for (int i = 0; i < h->ncf; ++i) d[i] = emt[h->hIendc[i + 1] - 1];
+  GG_CUDA(cudaMemcpyAsync(h->dDiag.p, d.data(), h->ncf * sizeof(double), cudaMemcpyHostToDevice, h->ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(h->ctx->stream));
+  h->emt_valid = true;
+  h->sym_vals_valid = false;
+  h->eav = 0.0;
+  return GG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,322 @@
+// spmv.cu - the Davidson matrix-vector product (SPICMV2, lib9290/spicmv2.f90)
+// on the GPU.
+//
+// The reference keeps the lower triangle by rows (diagonal last) and does,
+// row by row, C(i) += H(i,i) B(i) + sum_j H(i,j) B(j) and C(j) += H(i,j) B(i)
+// (DMERGE). On the GPU the scattered second update would need atomics, whose
+// order (and rounding) changes from run to run. Instead the structure is
+// expanded once into a full symmetric CSR (own row, then the transposed
+// entries in increasing source row), built by a deterministic chunked
+// transpose; each row is then one warp-reduced dot product, so the result is
+// reproducible bit for bit.
+//
+// Precision modes:
+//   GG_FP64   y = H x in FP64 (one DFMA per stored entry).
+//   GG_SPLIT  off-diagonal H stored as hi + lo FP32 pairs, x split the same
+//             way, products and sums in double-float arithmetic on the FP32
+//             pipe (about 2^-44 relative), the diagonal term in FP64. GB300's
+//             FP64 pipe issues roughly 1/64 of its FP32 rate, so FP64 SpMV is
+//             issue-bound at about the HBM rate; the split form is not.
+#include <algorithm>
+#include <vector>
+
+#include "gg_internal.cuh"
+
+namespace gg {
+namespace {
+
+constexpr int NCHUNK = 128;
+
+// counts of transposed entries per (chunk, column)
+__global__ void k_tcount(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow,
+                         const int *__restrict__ chunk_r0, int ncf, int *__restrict__ cnt) {
+  const int ch = blockIdx.x;
+  const int r0 = chunk_r0[ch], r1 = chunk_r0[ch + 1];
+  int *c = cnt + (size_t)ch * ncf;
+  for (int r = r0; r < r1; ++r) {
+    const int64_t lo = iendc[r], hi = iendc[r + 1] - 1;  // last entry is the diagonal
+    for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) atomicAdd(&c[irow[p] - 1], 1);
+  }
+}
+
+// cursor(chunk, col) = start of col's transposed part + entries of earlier chunks
+__global__ void k_cursor(const int *__restrict__ cnt, int ncf, int nch, const int64_t *__restrict__ symptr,
+                         const int64_t *__restrict__ iendc, int64_t *__restrict__ cursor) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncf; c += gridDim.x * blockDim.x) {
+    int64_t pos = symptr[c] + (iendc[c + 1] - iendc[c]);
+    for (int ch = 0; ch < nch; ++ch) {
+      cursor[(size_t)ch * ncf + c] = pos;
+      pos += cnt[(size_t)ch * ncf + c];
+    }
+  }
+}
+
+__global__ void k_tcol_total(const int *__restrict__ cnt, int ncf, int nch, const int64_t *__restrict__ iendc,
+                             int64_t *__restrict__ rowlen) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncf; c += gridDim.x * blockDim.x) {
+    int64_t t = iendc[c + 1] - iendc[c];
+    for (int ch = 0; ch < nch; ++ch) t += cnt[(size_t)ch * ncf + c];
+    rowlen[c] = t;
+  }
+}
+
+// transposed placement: rows of a chunk in order; within one row the columns
+// are distinct, so the cursors need no atomics
+__global__ void k_tplace(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow,
+                         const int *__restrict__ chunk_r0, int ncf, int64_t *__restrict__ cursor,
+                         int32_t *__restrict__ scol, int64_t *__restrict__ ssrc) {
+  const int ch = blockIdx.x;
+  const int r0 = chunk_r0[ch], r1 = chunk_r0[ch + 1];
+  int64_t *cur = cursor + (size_t)ch * ncf;
+  for (int r = r0; r < r1; ++r) {
+    const int64_t lo = iendc[r], hi = iendc[r + 1] - 1;
+    for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+      const int c = irow[p] - 1;
+      const int64_t pos = cur[c];
+      cur[c] = pos + 1;
+      scol[pos] = r;
+      ssrc[pos] = p;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_own(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow, int ncf,
+                      const int64_t *__restrict__ symptr, int32_t *__restrict__ scol, int64_t *__restrict__ ssrc) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= ncf) return;
+  const int64_t lo = iendc[warp], hi = iendc[warp + 1];
+  const int64_t base = symptr[warp];
+  for (int64_t p = lo + lane; p < hi; p += 32) {
+    scol[base + (p - lo)] = irow[p] - 1;
+    ssrc[base + (p - lo)] = p;
+  }
+}
+
+__global__ void k_rowlen_scan(const int64_t *__restrict__ rowlen, int n, int64_t *__restrict__ ptr) {
+  // single block scan (n up to a few million rows is fine for a one-time build)
+  __shared__ long long s[1024];
+  long long base = 0;
+  for (int i0 = 0; i0 < n; i0 += blockDim.x) {
+    const int i = i0 + threadIdx.x;
+    const long long v = (i < n) ? rowlen[i] : 0;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int w = 1; w < (int)blockDim.x; w <<= 1) {
+      const long long t = ((int)threadIdx.x >= w) ? s[threadIdx.x - w] : 0;
+      __syncthreads();
+      s[threadIdx.x] += t;
+      __syncthreads();
+    }
+    if (i < n) ptr[i] = base + s[threadIdx.x] - v;
+    const long long tot = s[blockDim.x - 1];
+    __syncthreads();
+    base += tot;
+  }
+  if (threadIdx.x == 0) ptr[n] = base;
+}
+
+// values: FP64 copy and the hi/lo split (diagonal excluded from the split)
+__global__ void k_symvals(const int64_t *__restrict__ symptr, const int32_t *__restrict__ scol,
+                          const int64_t *__restrict__ ssrc, const double *__restrict__ emt, int ncf,
+                          double *__restrict__ sval, float *__restrict__ shi, float *__restrict__ slo) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= ncf) return;
+  for (int64_t p = symptr[warp] + lane; p < symptr[warp + 1]; p += 32) {
+    const double v = emt[ssrc[p]];
+    sval[p] = v;
+    if (scol[p] == warp) {
+      shi[p] = 0.f;
+      slo[p] = 0.f;
+    } else {
+      const float h = __double2float_rn(v);
+      shi[p] = h;
+      slo[p] = __double2float_rn(v - (double)h);
+    }
+  }
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// y = H x, FP64, one warp per row
+__global__ void __launch_bounds__(256) k_spmv64(const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                                const double *__restrict__ val, const double *__restrict__ x,
+                                                double *__restrict__ y, int n) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const int64_t lo = ptr[row], hi = ptr[row + 1];
+  double acc = 0.0;
+  for (int64_t p = lo + lane; p < hi; p += 32) acc = fma(__ldg(val + p), __ldg(x + __ldg(col + p)), acc);
+  acc = warp_sum(acc);
+  if (lane == 0) y[row] = acc;
+}
+
+// double-float helpers (Dekker / Knuth error-free transformations)
+struct df {
+  float h, l;
+};
+__device__ __forceinline__ df two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  const float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__device__ __forceinline__ df df_add(df a, df b) {
+  df s = two_sum(a.h, b.h);
+  const float t = s.l + a.l + b.l;
+  const float h = s.h + t;
+  return {h, t - (h - s.h)};
+}
+
+__global__ void k_split_x(const double *__restrict__ x, float2 *__restrict__ xs, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = x[i];
+    const float h = __double2float_rn(v);
+    xs[i] = make_float2(h, __double2float_rn(v - (double)h));
+  }
+}
+
+// y = H x with H_offdiag = hi + lo (FP32 pair), x = xh + xl; double-float
+// accumulation; FP64 diagonal
+__global__ void __launch_bounds__(256) k_spmv_split(const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                                    const float *__restrict__ hi, const float *__restrict__ lo,
+                                                    const float2 *__restrict__ xs, const double *__restrict__ diag,
+                                                    const double *__restrict__ x, double *__restrict__ y, int n) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const int64_t p0 = ptr[row], p1 = ptr[row + 1];
+  df acc = {0.f, 0.f};
+  for (int64_t p = p0 + lane; p < p1; p += 32) {
+    const float ah = __ldg(hi + p), al = __ldg(lo + p);
+    const float2 xv = __ldg(xs + __ldg(col + p));
+    const float ph = ah * xv.x;
+    const float pe = fmaf(ah, xv.x, -ph);               // exact low part of ah*xh
+    const float cross = fmaf(ah, xv.y, fmaf(al, xv.x, pe));
+    acc = df_add(acc, two_sum(ph, cross));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    df other;
+    other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
+    other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
+    acc = df_add(acc, other);
+  }
+  if (lane == 0) y[row] = ((double)acc.h + (double)acc.l) + diag[row] * x[row];
+}
+
+}  // namespace
+
+int build_sym(gg_hmat *h) {
+  if (h->sym_valid) return GG_OK;
+  gg_ctx *ctx = h->ctx;
+  cudaStream_t s = ctx->stream;
+  const int ncf = h->ncf;
+  // row chunks balanced by stored entries
+  const int nch = std::min(NCHUNK, ncf);
+  std::vector<int> r0(nch + 1, ncf);
+  r0[0] = 0;
+  {
+    const double per = (double)h->nnz / nch;
+    int c = 1;
+    for (int r = 0; r < ncf && c < nch; ++r)
+      if ((double)h->hIendc[r + 1] >= per * c) r0[c++] = r + 1;
+    for (; c < nch; ++c) r0[c] = ncf;
+    r0[nch] = ncf;
+    for (int i = 1; i <= nch; ++i) r0[i] = std::max(r0[i], r0[i - 1]);
+  }
+  DBuf<int> dr0, cnt;
+  DBuf<int64_t> rowlen, cursor;
+  GG_TRY(dr0.alloc(nch + 1));
+  GG_CUDA(cudaMemcpyAsync(dr0.p, r0.data(), (nch + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
+  GG_TRY(cnt.alloc((size_t)nch * ncf));
+  GG_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)nch * ncf * sizeof(int), s));
+  k_tcount<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cnt.p);
+  GG_CUDA(cudaGetLastError());
+  GG_TRY(rowlen.alloc(ncf));
+  k_tcol_total<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dIendc.p, rowlen.p);
+  GG_TRY(h->dSymPtr.alloc(ncf + 1));
+  k_rowlen_scan<<<1, 1024, 0, s>>>(rowlen.p, ncf, h->dSymPtr.p);
+  GG_CUDA(cudaGetLastError());
+  int64_t total = 0;
+  GG_CUDA(cudaMemcpyAsync(&total, h->dSymPtr.p + ncf, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  if (total != 2 * h->nnz - ncf) return fail(GG_ERR_STATE, "build_sym: inconsistent structure");
+  h->sym_nnz = total;
+  GG_TRY(h->dSymCol.alloc(total));
+  GG_TRY(h->dSymSrc.alloc(total));
+  GG_TRY(cursor.alloc((size_t)nch * ncf));
+  k_cursor<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dSymPtr.p, h->dIendc.p, cursor.p);
+  k_own<<<(ncf * 32 + 255) / 256, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, ncf, h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p);
+  k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cursor.p, h->dSymCol.p, h->dSymSrc.p);
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaStreamSynchronize(s));
+  h->sym_valid = true;
+  h->sym_vals_valid = false;
+  return GG_OK;
+}
+
+int refresh_sym_values(gg_hmat *h) {
+  GG_TRY(build_sym(h));
+  if (h->sym_vals_valid) return GG_OK;
+  cudaStream_t s = h->ctx->stream;
+  GG_TRY(h->dSymVal.alloc(h->sym_nnz));
+  GG_TRY(h->dSymHi.alloc(h->sym_nnz));
+  GG_TRY(h->dSymLo.alloc(h->sym_nnz));
+  k_symvals<<<(h->ncf * 32 + 255) / 256, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p, h->dEmt.p, h->ncf,
+                                                      h->dSymVal.p, h->dSymHi.p, h->dSymLo.p);
+  GG_CUDA(cudaGetLastError());
+  h->sym_vals_valid = true;
+  return GG_OK;
+}
+
+// y[:, v] = H x[:, v] for v < m (column-major [ncf x m]); stream-ordered
+int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s) {
+  const int n = h->ncf;
+  const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
+  for (int v = 0; v < m; ++v) {
+    const double *x = dx + (size_t)v * n;
+    double *y = dy + (size_t)v * n;
+    if (precision == GG_SPLIT) {
+      GG_TRY(h->dXs.alloc(n));
+      k_split_x<<<(n + 255) / 256, 256, 0, s>>>(x, h->dXs.p, n);
+      k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p, h->dDiag.p, x,
+                                          y, n);
+    } else {
+      k_spmv64<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, x, y, n);
+    }
+    GG_CUDA(cudaGetLastError());
+  }
+  return GG_OK;
+}
+
+// Algorithmic bytes of one y = H x in the reference's storage (lower
+// triangle once): nnz_l (8 + 4) + (ncf + 1) 8 + 3 ncf 8 m for FP64 (hi+lo is
+// the same byte count).
+double spmv_bytes(const gg_hmat *h, int precision, int m) {
+  (void)precision;
+  return (double)h->nnz * 12.0 + (double)(h->ncf + 1) * 8.0 + 3.0 * h->ncf * 8.0 * m;
+}
+
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" int gg_spicmv2(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c, int precision) {
+  if (!ctx || !h || h->ctx != ctx || m < 1 || !b || !c) return fail(GG_ERR_ARG, "gg_spicmv2: bad arguments");
+  if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_spicmv2: EMT not set");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_TRY(refresh_sym_values(h));
+  DBuf<double> db, dc;
+  const size_t n = (size_t)h->ncf * m;
+  GG_TRY(db.alloc(n));
+  GG_TRY(dc.alloc(n));
+  GG_CUDA(cudaMemcpyAsync(db.p, b, n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  GG_TRY(spmv(h, precision, db.p, dc.p, m, ctx->stream));
+  GG_CUDA(cudaMemcpyAsync(c, dc.p, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GG_OK;
+}

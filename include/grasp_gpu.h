@@ -1,0 +1,187 @@
+/*
+ * grasp_gpu.h - C ABI of the GB300 (sm_103a) CI hot path for GRASP.
+ *
+ * This library replaces one stage of GRASP's rci / rmcdhf: the radial
+ * integral tables (GENINTRK / SLATER / RINTI), the Hamiltonian assembly from
+ * rangular's T/V angular-coefficient lists (SETHAM) and the Davidson
+ * eigensolver (MANEIG -> GDVD/DVDSON with SPICMV2 as the matrix-vector
+ * product). Everything runs on one GPU; there is no CPU fallback.
+ *
+ * Conventions (the reference's own):
+ *  - orbital, CSF and sparse-position indices are 1-based;
+ *  - PF/QF are column-major [ld x nw] (PF(NNNP, NW), wave_C);
+ *  - the Hamiltonian is the lower triangle stored by rows with the diagonal
+ *    last in each row: IENDC(0:NCF) row ends, IROW column indices, EMT values
+ *    (hmat_C; mcp.30 record layout). IENDC is int64 here so that blocks above
+ *    2^31-1 non-zeros are representable; IROW stays int32.
+ *  - every entry point returns 0 on success and a negative gg_status on
+ *    failure; gg_last_error() gives the message. No entry point aborts the
+ *    process (the reference STOPs; the caller decides what to do).
+ *
+ * Device memory is owned by the context and its handles. All work is issued
+ * on the context's CUDA stream; calls are synchronous unless documented.
+ */
+#ifndef GRASP_GPU_H
+#define GRASP_GPU_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gg_ctx gg_ctx;
+typedef struct gg_hmat gg_hmat;
+
+enum gg_status {
+  GG_OK = 0,
+  GG_ERR_ARG = -1,       /* invalid argument */
+  GG_ERR_CUDA = -2,      /* CUDA runtime error */
+  GG_ERR_STATE = -3,     /* call order (e.g. no orbitals yet) */
+  GG_ERR_NOTFOUND = -4,  /* RKINTC: integral not in the table */
+  GG_ERR_RANGE = -5,     /* SETHAM: LOC beyond NELMNT, label out of range */
+  GG_ERR_KAPPA = -6,     /* RINTI: orbitals with different kappa */
+  GG_ERR_CONVERGE = -7,  /* DVDSON: MAXITER reached (ierr has bit 2048) */
+  GG_ERR_NOMEM = -8
+};
+
+/* Precision of the R^k contraction and of the Davidson matvec. */
+enum gg_precision {
+  GG_FP64 = 0,       /* FP64 everywhere */
+  GG_SPLIT = 1       /* hi+lo FP32 split of the off-diagonal matvec; FP64
+                        diagonal, Rayleigh-Ritz, Gram-Schmidt and residuals */
+};
+
+const char *gg_last_error(void);
+int gg_version(void);
+
+/* ---- context --------------------------------------------------------- */
+int gg_ctx_create(int device, gg_ctx **out);
+int gg_ctx_destroy(gg_ctx *ctx);
+/* Blocks until all work on the context's stream has finished. */
+int gg_ctx_synchronize(gg_ctx *ctx);
+
+/* ---- grid (grid_C, npot_C, def_C) ---------------------------------------
+ * Replaces RADGRD (lib9290/radgrd.f90:3) + SETQIC (lib9290/setqic.f90:3) as
+ * called from GETCID (rci90/getcid.f90:233-237). r/rp/rpor may be NULL: the
+ * exponential grid (HP = 0) is then generated as RADGRD does. zz[n] is the
+ * nuclear potential r*V(r) (ZZ). c is the speed of light (C).            */
+int gg_set_grid(gg_ctx *ctx, int n, double rnt, double h, double c, const double *r, const double *rp,
+                const double *rpor, const double *zz);
+/* Copies of R, RP, RPOR (n + 10 values each). */
+int gg_get_grid(gg_ctx *ctx, double *r, double *rp, double *rpor);
+
+/* ---- orbitals (wave_C: PF, QF, MF; orb_C: NAK) ----------------------------
+ * Replaces the state LODRWF (lib9290/lodrwf.f90:100-134) leaves behind.
+ * Values beyond MF(j) must be zero, as LODRWF leaves them.               */
+int gg_set_orbitals(gg_ctx *ctx, int nw, int ld, const int *nak, const int *mf, const double *pf,
+                    const double *qf);
+
+/* ---- R^k table ------------------------------------------------------------
+ * GENINTRK (rci90/genintrk.f90:3, loop :67-86): all R^k(ab;cd) with
+ * a<=b, a<=c, b<=d and TRIANGRK(l_a,k,l_c) & TRIANGRK(l_b,k,l_d), for
+ * k = 0..J2MAX (kmax < 0) or k = 0..kmax. The table stays on the device.
+ * precision: GG_FP64 (FP64 contraction).                                   */
+int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max_out);
+/* Copies INDTEIRK (int32, packed ((a*KEY+b)*KEY+c)*KEY+d, KEY = NW+1),
+ * VALTEIRK (double) and KSTART(0:kloop+1) (1-based positions). Any pointer
+ * may be NULL.                                                              */
+int gg_get_rk_table(gg_ctx *ctx, int32_t *indteirk, double *valteirk, int32_t *kstart);
+/* RKINTC (rci90/rkintc.f90:3): canonicalise, then look the integral up in
+ * the device table. Returns GG_ERR_NOTFOUND where the reference STOPs.     */
+int gg_rkintc(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *tegral);
+/* SLATER (lib9290/slater.f90:3): one R^k(ab;cd) evaluated on the device. */
+int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out);
+
+/* ---- one-body integrals ----------------------------------------------------
+ * RINTI (lib9290/rinti.f90:3) with DPBDT (dpbdt.f90:3): I(ab), mode 0
+ * includes the nuclear potential. GG_ERR_KAPPA where NAK(a) != NAK(b).      */
+int gg_rinti(gg_ctx *ctx, int j, int k, int mode, double *out);
+/* IABINT's cache (rci90/iabint.f90:3) as a dense table: iab[(a-1)*nw+(b-1)]
+ * = I(ab) for NAK(a) == NAK(b), NaN otherwise. iab may be NULL (the table
+ * is kept on the device for SETHAM).                                         */
+int gg_iabint_table(gg_ctx *ctx, double *iab);
+
+/* ---- Hamiltonian block (hmat_C) -------------------------------------------
+ * Structure of one block as MATRIX reads it from mcp.30
+ * (rmcdhf90/matrix.f90:123-140): iendc[0..ncf] (IENDC(0) = 0), irow[nnz]. */
+int gg_hmat_create(gg_ctx *ctx, int ncf, int64_t nnz, const int64_t *iendc, const int32_t *irow,
+                   gg_hmat **out);
+int gg_hmat_destroy(gg_hmat *h);
+
+/* One rangular coefficient list (mcp.31 or mcp.32+k, one block), as
+ * SORTMEM writes it (rangular90/sortmem.f90:232-284): nlab labels; label l
+ * owns contributions start[l] .. start[l+1]-1 of loc[] (the sparse INDEX,
+ * 1-based into EMT) and coeff[]. T labels pack min(a,b)*215+max(a,b);
+ * V labels pack ((a*215+c)*215+b)*215+d (rmcdhf90/setham.f90:244, 305-310). */
+typedef struct {
+  int64_t nlab;
+  const int32_t *lab;
+  const int64_t *start; /* nlab + 1 entries, start[0] = 0 */
+  const int32_t *loc;
+  const double *coeff;
+} gg_list;
+
+/* SETHAM (rmcdhf90/setham.f90:3) for one block, followed by the average
+ * energy shift of MATRIX (rmcdhf90/matrix.f90:178-203).
+ * iq[(ir-1)*nw + (a-1)] = IQ(a, ir), the subshell occupations of the block's
+ * CSFs (used for the diagonal FCO/GCO pieces, setham.f90:83-219).
+ * vlists has kmaxf + 1 entries (k = 0..kmaxf). Needs gg_genintrk (with
+ * kloop >= kmaxf) and gg_iabint_table first. On return EMT holds H - EAV*I
+ * on the device and *eav_out = EAV.
+ * gg_setham_upload copies the lists to the device; gg_setham_assemble
+ * builds the per-element gather index and assembles EMT from the device
+ * copies. gg_setham does both.                                              */
+int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *tlist, int kmaxf,
+                     const gg_list *vlists);
+int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out);
+int gg_setham(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *tlist, int kmaxf,
+              const gg_list *vlists, double *eav_out);
+/* Copies EMT (nnz values) back to the host. */
+int gg_hmat_get_emt(gg_hmat *h, double *emt);
+/* Replaces EMT by caller values (for a matrix assembled elsewhere, e.g. the
+ * rows rci writes to rci.res, setham_gg.f90:378). */
+int gg_hmat_set_emt(gg_hmat *h, const double *emt);
+
+/* SPICMV2 (lib9290/spicmv2.f90:2): C = H B for m host vectors [ncf x m]. */
+int gg_spicmv2(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c, int precision);
+
+/* ---- eigen-solve ------------------------------------------------------------
+ * MANEIG (rci90/maneig.f90:3 when flavour = 0, rmcdhf90/maneig.f90:3 when
+ * flavour = 1): lowest nvec eigenpairs of the block's H - EAV, dominant
+ * component of each eigenvector made positive (rci90/maneig.f90:532-555).
+ * The Davidson solver follows GDVD/DVDSON (libdvd90/gdvd.f90:4,
+ * dvdson.f90:1) with the reference's constants: CRITE 1e-17, CRITC = CRITR
+ * = 1e-9, MBLOCK 1, LIM/MAXITR per flavour. Where the reference uses dense
+ * DSPEVX (rci, ncf <= 2000), this library runs the same Davidson to the
+ * same tolerances. Initial estimates follow INIEST2
+ * (lib9290/iniest2.f90:3): the lowest eigenvectors of the leading
+ * min(nmax, ncf) block.
+ * eval[nvec] (relative to EAV), evec[ncf x nvec] column-major.             */
+typedef struct {
+  int flavour;    /* 0 = rci, 1 = rmcdhf */
+  int precision;  /* gg_precision of the matvec */
+  int lim;        /* <= 0: reference default */
+  int maxiter;    /* <= 0: reference default */
+  double critr;   /* <= 0: 1e-9 */
+  double critc;   /* <= 0: 1e-9 */
+  double crite;   /* <= 0: 1e-17 */
+  int robust;     /* 0: DVDSON exactly. 1: the first pass's robust shift uses
+                     DL = 0 where the reference uses |1e30 - lambda| (its
+                     OLDVAL sentinel, dvdson.f90:703), which otherwise wastes
+                     the first correction vector and can let the coefficient
+                     test stop the solver early. */
+} gg_dvd_params;
+
+int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double *eval, double *evec,
+              int *nloops, int *nmv, int *ierr);
+
+/* ---- timing --------------------------------------------------------------
+ * Device time (ms, CUDA events on the context stream) of the named stage of
+ * the last call: 0 genintrk, 1 iabint, 2 setham assemble, 3 maneig total,
+ * 4 matvec (sum over the last maneig), 5 number of matvec launches,
+ * 6 bytes moved by one matvec (algorithmic), 7 setham upload.              */
+double gg_stage_stat(gg_ctx *ctx, int which);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,248 @@
+"""CPU FP64 oracle for GRASP's CI hot path (test infrastructure only).
+
+This package is the checker for the CUDA path. Only ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline legs of ``bench.py`` may
+import it; the product library never does.
+
+The C++ restatement lives in ``oracle.cpp`` (built by ``oracle/Makefile``
+into ``oracle/_build/liboracle.so``). This module loads it with ctypes and
+offers numpy-friendly wrappers whose names follow the reference subroutines
+(QUAD, YZK, SLATER, RINTI, GENINTRK, RKINTC, SETHAM, SPICMV2, DSPEVX, GDVD,
+INIEST2, MANEIG).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
+_lib = None
+
+_d = C.POINTER(C.c_double)
+_i32 = C.POINTER(C.c_int32)
+_i64 = C.POINTER(C.c_int64)
+_int = C.POINTER(C.c_int)
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with its Makefile (g++, a few seconds)."""
+    if force or not os.path.exists(_LIB_PATH) or (
+        os.path.getmtime(_LIB_PATH) < os.path.getmtime(os.path.join(_HERE, "oracle.cpp"))
+    ):
+        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    return _LIB_PATH
+
+
+class OrList(C.Structure):
+    _fields_ = [
+        ("nlab", C.c_int64),
+        ("lab", _i32),
+        ("start", _i64),
+        ("loc", _i32),
+        ("coeff", _d),
+    ]
+
+
+class OrDvdParams(C.Structure):
+    _fields_ = [
+        ("lim", C.c_int), ("ilow", C.c_int), ("ihigh", C.c_int), ("niv", C.c_int),
+        ("mblock", C.c_int), ("maxiter", C.c_int),
+        ("crite", C.c_double), ("critc", C.c_double), ("critr", C.c_double), ("ortho", C.c_double),
+        ("robust", C.c_int),
+    ]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(_LIB_PATH)
+        L.or_create.restype = C.c_void_p
+        L.or_create.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, _d]
+        L.or_destroy.argtypes = [C.c_void_p]
+        L.or_get_grid.argtypes = [C.c_void_p, _d, _d, _d]
+        L.or_get_qic.argtypes = [C.c_void_p, _d, _d]
+        L.or_set_orbitals.argtypes = [C.c_void_p, C.c_int, C.c_int, _int, _int, _d, _d]
+        L.or_quad.restype = C.c_double
+        L.or_quad.argtypes = [C.c_void_p, C.c_int, _d]
+        L.or_yzk.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _d]
+        L.or_slater.restype = C.c_double
+        L.or_slater.argtypes = [C.c_void_p] + [C.c_int] * 5
+        L.or_rinti.restype = C.c_double
+        L.or_rinti.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _int]
+        L.or_triangrk.argtypes = [C.c_int] * 3
+        L.or_genintrk.restype = C.c_int64
+        L.or_genintrk.argtypes = [C.c_void_p, C.c_int, _i32, _d, _i32, _int, C.c_int]
+        L.or_rkintc.argtypes = [C.c_int, _i32, _d, _i32] + [C.c_int] * 5 + [_d]
+        L.or_clrx.restype = C.c_double
+        L.or_clrx.argtypes = [C.c_int] * 3
+        L.or_setham.argtypes = [C.c_void_p, C.c_int, C.c_int64, _i64, C.POINTER(C.c_uint8),
+                                C.POINTER(OrList), C.c_int, C.POINTER(OrList), _d]
+        L.or_shift_eav.restype = C.c_double
+        L.or_shift_eav.argtypes = [C.c_int, _i64, _d]
+        L.or_spicmv2.argtypes = [C.c_int, C.c_int, _i64, _i32, _d, _d, _d]
+        L.or_dspevx.argtypes = [C.c_int, _d, C.c_int, C.c_int, _d, _d]
+        L.or_iniest2.argtypes = [C.c_int, C.c_int, C.c_int, _d, _d, _i64, _i32]
+        L.or_gdvd.argtypes = [C.c_int, _i64, _i32, _d, _d, C.POINTER(OrDvdParams), _d, C.c_int64,
+                              _int, _int, _int, C.c_int]
+        L.or_maneig.argtypes = [C.c_int, C.c_int, C.c_int, _i64, _i32, _d, _d, _d, _int, _int, _int, C.c_int,
+                                C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class Oracle:
+    """One radial grid + orbital set, like the reference's grid_C/wave_C globals."""
+
+    def __init__(self, n=590, rnt=None, h=0.05, c=137.035999139, zz=None, z=None):
+        if rnt is None:
+            rnt = 2.0e-6 / z if z else 2.0e-6
+        self.n, self.rnt, self.h, self.c = n, rnt, h, c
+        if zz is None:
+            zz = np.full(n, float(z) if z else 0.0)
+        self.zz = np.ascontiguousarray(zz, dtype=np.float64)
+        self._h = lib().or_create(n, rnt, h, c, _p(self.zz, _d))
+        if not self._h:
+            raise ValueError("or_create failed")
+        self.nw = 0
+
+    def __del__(self):
+        if getattr(self, "_h", None) and _lib is not None:
+            _lib.or_destroy(self._h)
+            self._h = None
+
+    def grid(self):
+        r = np.zeros(self.n + 10); rp = np.zeros(self.n + 10); rpor = np.zeros(self.n + 10)
+        lib().or_get_grid(self._h, _p(r, _d), _p(rp, _d), _p(rpor, _d))
+        return r, rp, rpor
+
+    def qic(self):
+        c = np.zeros(4); cnc = np.zeros(12)
+        lib().or_get_qic(self._h, _p(c, _d), _p(cnc, _d))
+        return c, cnc.reshape(3, 4)
+
+    def set_orbitals(self, nak, mf, pf, qf):
+        """pf, qf: arrays [nw, ld] (row = orbital); stored column-major like PF(NNNP, NW)."""
+        self.nak = np.ascontiguousarray(nak, dtype=np.int32)
+        self.mf = np.ascontiguousarray(mf, dtype=np.int32)
+        self.pf = np.ascontiguousarray(pf, dtype=np.float64)
+        self.qf = np.ascontiguousarray(qf, dtype=np.float64)
+        nw, ld = self.pf.shape
+        rc = lib().or_set_orbitals(self._h, nw, ld, _p(self.nak, _int), _p(self.mf, _int),
+                                   _p(self.pf, _d), _p(self.qf, _d))
+        if rc != 0:
+            raise ValueError(f"or_set_orbitals failed: {rc}")
+        self.nw = nw
+
+    def quad(self, ta, mtp):
+        ta = np.array(ta, dtype=np.float64)
+        if ta.size < mtp + 3:
+            ta = np.concatenate([ta, np.zeros(mtp + 3 - ta.size)])
+        return lib().or_quad(self._h, mtp, _p(ta, _d))
+
+    def yzk(self, k, i, j):
+        yk = np.zeros(self.n)
+        mtp = lib().or_yzk(self._h, k, i, j, _p(yk, _d))
+        return yk, mtp
+
+    def slater(self, a, b, c, d, k):
+        return lib().or_slater(self._h, a, b, c, d, k)
+
+    def rinti(self, j, k, mode=0):
+        err = C.c_int(0)
+        v = lib().or_rinti(self._h, j, k, mode, C.byref(err))
+        if err.value:
+            raise ValueError("RINTI: orbitals have different kappa")
+        return v
+
+    def genintrk(self, kmax=-1, nthreads=1):
+        j2 = C.c_int(0)
+        n = lib().or_genintrk(self._h, kmax, None, None, None, C.byref(j2), 1)
+        if n < 0:
+            raise ValueError("GENINTRK: k beyond KLIMIT")
+        kloop = j2.value if kmax < 0 else kmax
+        ind = np.zeros(n, np.int32); val = np.zeros(n); ks = np.zeros(kloop + 2, np.int32)
+        lib().or_genintrk(self._h, kmax, _p(ind, _i32), _p(val, _d), _p(ks, _i32), C.byref(j2), nthreads)
+        return ind, val, ks, j2.value
+
+    def rkintc(self, table, a, b, c, d, k):
+        ind, val, ks = table[:3]
+        out = C.c_double(0)
+        rc = lib().or_rkintc(self.nw, _p(ind, _i32), _p(val, _d), _p(ks, _i32), a, b, c, d, k, C.byref(out))
+        if rc != 0:
+            raise KeyError("Rkintc Integral not found")
+        return out.value
+
+    def setham(self, ncf, nelmnt, iendc, iq, tlist, vlists):
+        """tlist / vlists: dicts with 'lab', 'start', 'loc', 'coeff' numpy arrays."""
+        keep = []
+
+        def mk(d):
+            lab = np.ascontiguousarray(d["lab"], np.int32); st = np.ascontiguousarray(d["start"], np.int64)
+            loc = np.ascontiguousarray(d["loc"], np.int32); co = np.ascontiguousarray(d["coeff"], np.float64)
+            keep.extend([lab, st, loc, co])
+            return OrList(lab.size, _p(lab, _i32), _p(st, _i64), _p(loc, _i32), _p(co, _d))
+
+        tl = mk(tlist)
+        vl = (OrList * len(vlists))(*[mk(v) for v in vlists])
+        emt = np.zeros(nelmnt)
+        iendc = np.ascontiguousarray(iendc, np.int64)
+        iq = np.ascontiguousarray(iq, np.uint8)
+        rc = lib().or_setham(self._h, ncf, nelmnt, _p(iendc, _i64), _p(iq, C.POINTER(C.c_uint8)),
+                             C.byref(tl), len(vlists) - 1, vl, _p(emt, _d))
+        if rc != 0:
+            raise ValueError("SETHAM: LOC beyond NELMNT")
+        return emt
+
+
+def shift_eav(ncf, iendc, emt):
+    iendc = np.ascontiguousarray(iendc, np.int64)
+    return lib().or_shift_eav(ncf, _p(iendc, _i64), _p(emt, _d))
+
+
+def spicmv2(n, iendc, irow, emt, b):
+    b = np.asfortranarray(b.reshape(n, -1), dtype=np.float64)
+    m = b.shape[1]
+    c = np.zeros((n, m), order="F")
+    iendc = np.ascontiguousarray(iendc, np.int64); irow = np.ascontiguousarray(irow, np.int32)
+    emt = np.ascontiguousarray(emt, np.float64)
+    lib().or_spicmv2(n, m, _p(iendc, _i64), _p(irow, _i32), _p(emt, _d), _p(b, _d), _p(c, _d))
+    return c
+
+
+def dspevx(ap, n, il, iu):
+    ap = np.ascontiguousarray(ap, np.float64)
+    m = iu - il + 1
+    w = np.zeros(m); z = np.zeros((m, n))
+    rc = lib().or_dspevx(n, _p(ap, _d), il, iu, _p(w, _d), _p(z, _d))
+    if rc:
+        raise ValueError("dspevx failed")
+    return w, z.T
+
+
+def maneig(flavour, ncf, nvec, iendc, irow, emt, nthreads=1, robust=False):
+    iendc = np.ascontiguousarray(iendc, np.int64); irow = np.ascontiguousarray(irow, np.int32)
+    emt = np.ascontiguousarray(emt, np.float64)
+    ev = np.zeros(nvec); vec = np.zeros((nvec, ncf))
+    nl, nm, ie = C.c_int(0), C.c_int(0), C.c_int(0)
+    rc = lib().or_maneig(flavour, ncf, nvec, _p(iendc, _i64), _p(irow, _i32), _p(emt, _d), _p(ev, _d),
+                         _p(vec, _d), C.byref(nl), C.byref(nm), C.byref(ie), nthreads, int(robust))
+    if rc < 0:
+        raise RuntimeError(f"MANEIG failed rc={rc} ierr={ie.value}")
+    return ev, vec.T, dict(nloops=nl.value, nmv=nm.value, ierr=ie.value)
+
+
+def clrx(ka, k, kb):
+    return lib().or_clrx(ka, k, kb)
+
+
+def triangrk(la, k, lb):
+    return bool(lib().or_triangrk(la, k, lb))
