@@ -324,8 +324,11 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
     *ierr_out = IERR;
     return fail(GG_ERR_ARG, "DVDSON: inconsistent LIM / NUME / MBLOCK / NIV (IERR " + std::to_string(IERR) + ")");
   }
-  std::vector<double> S((size_t)LIM * (LIM + 1) / 2, 0.0), SVEC((size_t)LIM * LIM, 0.0), EIGVAL(LIM, 0.0),
-      OLDVAL(NUME + 2, 0.0), SCRA1(8 * LIM, 0.0);
+  // OLDVAL receives IFIND = min(KPASS, REST) values each pass (dvdson.f90:722),
+  // more than its declared NUME + 1 (the reference's copy runs into the slack
+  // at the end of WORK): size it LIM.
+  std::vector<double> S((size_t)LIM * (LIM + 1) / 2, 0.0), SVEC((size_t)LIM * LIM, 0.0), EIGVAL(LIM + 2, 0.0),
+      OLDVAL(LIM + 2, 0.0), SCRA1(8 * LIM, 0.0);
   std::vector<int> INCV(LIM + 2, 0), ICV(NUME + 2, 0), IND(LIM + 2, 0);
   std::vector<double> ROWLAST(LIM + 2, 0.0);
   // INITDVD (dvdson.f90:848-948) with NUME + 1
