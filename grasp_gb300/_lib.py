@@ -66,6 +66,12 @@ GPU_SYMBOLS = {
     "gg_spicmv2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, _d, _d, C.c_int]),
     "gg_maneig": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(GGDvdParams), _d, _d, _int, _int, _int]),
     "gg_stage_stat": (C.c_double, [C.c_void_p, C.c_int]),
+    "gg_launch_count": (C.c_longlong, []),
+    "gg_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "gg_host_unregister": (C.c_int, [C.c_void_p]),
+    "gg_event_record": (C.c_int, [C.c_void_p, C.c_int]),
+    "gg_event_elapsed": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _d]),
+    "gg_matvec_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _d, _d]),
 }
 
 SYNTH_SYMBOLS = {

@@ -105,6 +105,16 @@ class Context:
     def stage_stat(self, which):
         return _lib.gpu().gg_stage_stat(self._h, which)
 
+    def mark(self, slot):
+        """Record a CUDA event (slot 0..7) on the context stream."""
+        check(_lib.gpu().gg_event_record(self._h, slot))
+
+    def elapsed(self, a, b):
+        """Milliseconds between two marks (synchronises on b)."""
+        ms = C.c_double()
+        check(_lib.gpu().gg_event_elapsed(self._h, a, b, C.byref(ms)))
+        return ms.value
+
     def synchronize(self):
         check(_lib.gpu().gg_ctx_synchronize(self._h))
 
@@ -187,5 +197,33 @@ class HMatrix:
         return ev, vec.T.copy(), info
 
 
+    def matvec_timing(self, precision=FP64, iters=20):
+        """(ms per y = H x launch, algorithmic bytes per launch)."""
+        ms = C.c_double(); by = C.c_double()
+        check(_lib.gpu().gg_matvec_timing(self.ctx._h, self._h, precision, iters, C.byref(ms), C.byref(by)))
+        return ms.value, by.value
+
+
 def _lib_status(name):
     return {"GG_ERR_CONVERGE": -7}[name]
+
+
+def launch_count():
+    """Kernels libgraspgpu has launched in this process."""
+    return int(_lib.gpu().gg_launch_count())
+
+
+class pinned:
+    """Context manager that page-locks numpy arrays for the duration."""
+
+    def __init__(self, *arrays):
+        self.arrays = [a for a in arrays if a is not None and a.nbytes > 0]
+
+    def __enter__(self):
+        for a in self.arrays:
+            check(_lib.gpu().gg_host_register(C.c_void_p(a.ctypes.data), a.nbytes))
+        return self
+
+    def __exit__(self, *exc):
+        for a in self.arrays:
+            _lib.gpu().gg_host_unregister(C.c_void_p(a.ctypes.data))

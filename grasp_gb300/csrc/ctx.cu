@@ -1,4 +1,5 @@
 // ctx.cu - context, grid (RADGRD/SETQIC) and orbital state of libgraspgpu.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -7,7 +8,9 @@
 namespace gg {
 
 static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
 
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int status, const std::string &msg) {
   g_last_error = msg;
@@ -72,6 +75,8 @@ int gg_ctx_destroy(gg_ctx *ctx) {
   if (!ctx) return GG_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  for (cudaEvent_t &e : ctx->marks)
+    if (e) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -263,8 +268,40 @@ int gg_set_orbitals(gg_ctx *ctx, int nw, int ld, const int *nak, const int *mf, 
 }
 
 double gg_stage_stat(gg_ctx *ctx, int which) {
-  if (!ctx || which < 0 || which >= 8) return -1.0;
+  if (!ctx || which < 0 || which >= 16) return -1.0;
   return ctx->stats[which];
+}
+
+long long gg_launch_count(void) { return g_launches.load(); }
+
+int gg_host_register(void *p, size_t bytes) {
+  if (!p || bytes == 0) return fail(GG_ERR_ARG, "gg_host_register: bad arguments");
+  GG_CUDA(cudaHostRegister(p, bytes, cudaHostRegisterDefault));
+  return GG_OK;
+}
+
+int gg_host_unregister(void *p) {
+  if (!p) return fail(GG_ERR_ARG, "gg_host_unregister: null pointer");
+  GG_CUDA(cudaHostUnregister(p));
+  return GG_OK;
+}
+
+int gg_event_record(gg_ctx *ctx, int slot) {
+  if (!ctx || slot < 0 || slot >= 8) return fail(GG_ERR_ARG, "gg_event_record: bad slot");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  if (!ctx->marks[slot]) GG_CUDA(cudaEventCreate(&ctx->marks[slot]));
+  GG_CUDA(cudaEventRecord(ctx->marks[slot], ctx->stream));
+  return GG_OK;
+}
+
+int gg_event_elapsed(gg_ctx *ctx, int a, int b, double *ms) {
+  if (!ctx || a < 0 || a >= 8 || b < 0 || b >= 8 || !ctx->marks[a] || !ctx->marks[b] || !ms)
+    return fail(GG_ERR_ARG, "gg_event_elapsed: bad slots");
+  GG_CUDA(cudaEventSynchronize(ctx->marks[b]));
+  float f = 0.f;
+  GG_CUDA(cudaEventElapsedTime(&f, ctx->marks[a], ctx->marks[b]));
+  *ms = f;
+  return GG_OK;
 }
 
 }  // extern "C"

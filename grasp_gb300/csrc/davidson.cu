@@ -20,6 +20,7 @@
 //    precision.
 //  - Dot products are blocked reductions, not sequential sums.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -200,6 +201,9 @@ struct Dvd {
   int nmv = 0;
   double mv_ms = 0;
   int mv_count = 0;
+  double t_eig = 0, t_wait = 0;  // host seconds: projected eigenproblem, device-to-host waits
+  std::vector<cudaEvent_t> evs;   // matvec start/stop pairs, read once at the end
+  size_t ev_used = 0;
   cudaEvent_t e0 = nullptr, e1 = nullptr;
 
   int init(gg_ctx *c, gg_hmat *hm, int prec, int nn, int lm) {
@@ -227,30 +231,46 @@ struct Dvd {
   ~Dvd() {
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
+    for (cudaEvent_t e : evs) cudaEventDestroy(e);
   }
   double *col(DBuf<double> &X, int j) { return X.p + (size_t)j * ld; }
 
-  // OP (gdvd.f90:137-142): AB[:, j0:j0+m) = H BASIS[:, j0:j0+m)
+  // OP (gdvd.f90:137-142): AB[:, j0:j0+m) = H BASIS[:, j0:j0+m); each launch
+  // is bracketed by events that are read after the solve (no extra sync)
   int op(int j0, int m) {
     for (int v = 0; v < m; ++v) {
-      GG_CUDA(cudaEventRecord(e0, s));
+      if (ev_used + 2 > evs.size()) {
+        for (int q = 0; q < 64; ++q) {
+          cudaEvent_t e;
+          GG_CUDA(cudaEventCreate(&e));
+          evs.push_back(e);
+        }
+      }
+      GG_CUDA(cudaEventRecord(evs[ev_used], s));
       GG_TRY(spmv(h, precision, col(B, j0 + v), col(AB, j0 + v), 1, s));
-      GG_CUDA(cudaEventRecord(e1, s));
-      GG_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      GG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      mv_ms += ms;
+      GG_CUDA(cudaEventRecord(evs[ev_used + 1], s));
+      ev_used += 2;
       ++mv_count;
     }
     nmv += m;
+    return GG_OK;
+  }
+  int collect_matvec_time() {
+    GG_CUDA(cudaStreamSynchronize(s));
+    for (size_t q = 0; q + 1 < ev_used; q += 2) {
+      float ms = 0.f;
+      GG_CUDA(cudaEventElapsedTime(&ms, evs[q], evs[q + 1]));
+      mv_ms += ms;
+    }
+    ev_used = 0;
     return GG_OK;
   }
   // out[0:k] = BASIS[:, 0:k]^T w  (device)
   int dots_dev(const DBuf<double> &X, int k, const double *w, double *out) {
     if (k <= 0) return GG_OK;
     dim3 g(nrb, (k + CG - 1) / CG);
-    k_dots_part<<<g, TPB, 0, s>>>(X.p, ld, k, w, n, part.p);
-    k_dots_reduce<<<(k + 127) / 128, 128, 0, s>>>(part.p, nrb, k, out);
+    k_dots_part<<<g, TPB, 0, s>>>(X.p, ld, k, w, n, part.p); ::gg::note_launch();
+    k_dots_reduce<<<(k + 127) / 128, 128, 0, s>>>(part.p, nrb, k, out); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
@@ -262,10 +282,10 @@ struct Dvd {
     for (int pass = 0; pass < 2; ++pass) {
       if (j > 0) {
         GG_TRY(dots_dev(B, j, w, dots.p));
-        k_sub_gemv<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(w, B.p, ld, j, dots.p, n);
+        k_sub_gemv<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(w, B.p, ld, j, dots.p, n); ::gg::note_launch();
       }
-      k_sq_part<<<nb, TPB, 0, s>>>(w, n, part.p);
-      k_normalize<<<nb, TPB, 0, s>>>(w, n, part.p, nb);
+      k_sq_part<<<nb, TPB, 0, s>>>(w, n, part.p); ::gg::note_launch();
+      k_normalize<<<nb, TPB, 0, s>>>(w, n, part.p, nb); ::gg::note_launch();
       GG_CUDA(cudaGetLastError());
     }
     return GG_OK;
@@ -275,7 +295,9 @@ struct Dvd {
     GG_TRY(dots_dev(B, kp + 1, col(AB, kp), dots.p));
     std::vector<double> hcol(kp + 1);
     GG_CUDA(cudaMemcpyAsync(hcol.data(), dots.p, (kp + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const auto t0 = std::chrono::steady_clock::now();
     GG_CUDA(cudaStreamSynchronize(s));
+    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     const size_t off = (size_t)kp * (kp + 1) / 2;
     for (int i = 0; i <= kp; ++i) S[off + i] = hcol[i];
     return GG_OK;
@@ -286,7 +308,7 @@ struct Dvd {
     GG_CUDA(cudaMemcpyAsync(small.p, hC, (size_t)k * m * sizeof(double), cudaMemcpyHostToDevice, s));
     const size_t sm = (size_t)k * m * sizeof(double);
     if (sm > 48 * 1024) GG_CUDA(cudaFuncSetAttribute(k_multbc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_multbc<<<(n + TPB - 1) / TPB, TPB, sm, s>>>(X.p, ld, k, small.p, m, T.p, n);
+    k_multbc<<<(n + TPB - 1) / TPB, TPB, sm, s>>>(X.p, ld, k, small.p, m, T.p, n); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaMemcpy2DAsync(X.p, ld * 8, T.p, ld * 8, (size_t)n * 8, m, cudaMemcpyDeviceToDevice, s));
     return GG_OK;
@@ -294,7 +316,9 @@ struct Dvd {
   double host_sum_sqrt(int np) {
     std::vector<double> hp(np);
     cudaMemcpyAsync(hp.data(), part.p, np * sizeof(double), cudaMemcpyDeviceToHost, s);
+    const auto t0 = std::chrono::steady_clock::now();
     cudaStreamSynchronize(s);
+    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     double a = 0.0;
     for (int i = 0; i < np; ++i) a += hp[i];
     return std::sqrt(a);
@@ -365,10 +389,16 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
     const int IFIND = std::min(KPASS, REST);
     for (int i = 0; i < IFIND; ++i) OLDVAL[i] = EIGVAL[i];
     w.assign(IFIND, 0.0);
-    if (sym_eig_lowest(KPASS, S.data(), IFIND, w.data(), SVEC.data()) != 0) {
+    // DSPEVX returns IFIND eigenpairs; only the first NUME eigenvectors are
+    // read afterwards (TSTSEL, NEWVEC, MULTBC), all IFIND = REST when the
+    // basis is full and OVFLOW collapses onto them.
+    const int nvecs = (KPASS == LIM) ? IFIND : std::min(IFIND, NUME);
+    const auto te0 = std::chrono::steady_clock::now();
+    if (sym_eig_lowest(KPASS, S.data(), IFIND, nvecs, w.data(), SVEC.data()) != 0) {
       *ierr_out = -1;
       return fail(GG_ERR_CONVERGE, "DVDSON: projected eigenproblem failed");
     }
+    D.t_eig += std::chrono::duration<double>(std::chrono::steady_clock::now() - te0).count();
     for (int i = 0; i < IFIND; ++i) EIGVAL[i] = w[i];
     // TSTSEL (dvdson.f90:1260-1413)
     {
@@ -436,7 +466,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
         const int nb = (n + TPB - 1) / TPB;
         // ICUR = column KPASS + NADDED (a converged target is overwritten)
         k_ritz<<<nb, TPB, 0, D.s>>>(D.B.p, D.AB.p, D.ld, KPASS, D.small.p, EIGVAL[indx - 1],
-                                    D.col(D.B, KPASS + nadded), D.col(D.AB, KPASS + nadded), n, D.part.p);
+                                    D.col(D.B, KPASS + nadded), D.col(D.AB, KPASS + nadded), n, D.part.p); ::gg::note_launch();
         GG_CUDA(cudaGetLastError());
         const double res = D.host_sum_sqrt(nb);
         SCRA1[indx - 1] = res;
@@ -470,7 +500,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
         // shift + preconditioner for this column now (MBLOCK columns at most)
         k_precond<<<(n + TPB - 1) / TPB, TPB, 0, D.s>>>(D.col(D.AB, KPASS + nadded - 1), D.col(D.B, KPASS + nadded - 1),
                                                         rhseps_added, lam_added, D.diag.p, D.col(D.B, KPASS + nadded - 1),
-                                                        n);
+                                                        n); ::gg::note_launch();
         GG_CUDA(cudaGetLastError());
         if (nadded + KPASS == limadd) break;
       }
@@ -496,14 +526,14 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   resid_out.assign(NUME, 0.0);
   for (int i = 0; i < NUME; ++i) {
     const int nb = std::min((n + TPB - 1) / TPB, 1024);
-    k_final_res_part<<<nb, TPB, 0, D.s>>>(D.B.p, D.AB.p, D.ld, i, EIGVAL[i], n, D.part.p);
+    k_final_res_part<<<nb, TPB, 0, D.s>>>(D.B.p, D.AB.p, D.ld, i, EIGVAL[i], n, D.part.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
     resid_out[i] = D.host_sum_sqrt(nb);
   }
   eigval_out.assign(EIGVAL.begin(), EIGVAL.begin() + NUME);
   *nloops_out = NLOOPS;
   *ierr_out = IERR;
-  return GG_OK;
+  return D.collect_matvec_time();
 }
 
 // Leading ns x ns block of a matrix as its own hmat (INIEST2's sub-matrix).
@@ -630,6 +660,9 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     // coefficient test) from a sane first shift
     P1.robust = 1;
     P1.critc = 0.0;
+    // block Davidson: up to NUME correction vectors per pass, so far fewer
+    // projected eigenproblems than one vector per pass
+    P1.mblock = nvec;
     P1.lim = std::min(ns, P.lim);
     if (ns < ncf && P1.lim < P.nume + 1) P1.lim = ns;
     GG_TRY(D1.init(ctx, blk, precision, ns, P1.lim));
@@ -642,6 +675,9 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     nmv_total += D1.nmv;
     nl_total += nl;
     *ierr = ie;
+    ctx->stats[8] = nl;      // stage-1 (leading block) loops
+    ctx->stats[9] = 0;       // stage-2 loops
+    ctx->stats[10] = D1.mv_ms;
   }
   Dvd *Dout = &D1;
   Dvd D2;
@@ -659,6 +695,9 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     nl_total += nl;
     *ierr = ie;
     Dout = &D2;
+    ctx->stats[9] = nl;
+    ctx->stats[11] = D2.mv_ms;
+    ctx->stats[12] = D2.mv_count;
   }
   for (int j = 0; j < nvec; ++j) eval[j] = ev[j];
   std::vector<double> hv;
@@ -686,6 +725,8 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   ctx->stats[3] = ms;
   ctx->stats[4] = mv_ms;
   ctx->stats[5] = mv_count;
+  ctx->stats[13] = 1e3 * (D1.t_eig + D2.t_eig);    // host projected eigenproblem ms
+  ctx->stats[14] = 1e3 * (D1.t_wait + D2.t_wait);  // host waits on device results ms
   *nloops = nl_total;
   *nmv = nmv_total;
   if (*ierr & 2048) return fail(GG_ERR_CONVERGE, "DVDSON: maximum number of iterations reached (IERR 2048)");

@@ -12,6 +12,8 @@ namespace gg {
 
 void set_error(const std::string &msg);
 int fail(int status, const std::string &msg);
+// counts this library's kernel launches (reported by gg_launch_count)
+void note_launch();
 
 #define GG_CUDA(call)                                                                   \
   do {                                                                                  \
@@ -116,8 +118,9 @@ struct gg_ctx {
   gg::RkTable rk;
   gg::DBuf<double> dIab;                // [nw * nw]
   bool iab_valid = false;
-  double stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  double stats[16] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t marks[8] = {};  // gg_event_record slots
 };
 
 struct gg_hmat {
@@ -156,6 +159,7 @@ int build_sym(gg_hmat *h);
 int refresh_sym_values(gg_hmat *h);
 int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s);
 double spmv_bytes(const gg_hmat *h, int precision, int m);
-// hosteig.cpp: lowest m eigenpairs of a packed-upper symmetric matrix
-int sym_eig_lowest(int n, const double *ap, int m, double *w, double *z);
+// hosteig.cpp: lowest m eigenvalues of a packed-upper symmetric matrix and
+// the eigenvectors of the lowest mvec <= m of them
+int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *z);
 }  // namespace gg

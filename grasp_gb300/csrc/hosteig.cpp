@@ -206,10 +206,11 @@ void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector
 
 }  // namespace
 
-// Lowest m eigenpairs of the symmetric n x n matrix given in packed upper
-// storage (AP(i + j(j-1)/2) = A(i,j), i <= j). w[m] ascending, z[n x m].
-int sym_eig_lowest(int n, const double *ap, int m, double *w, double *z) {
-  if (n <= 0 || m <= 0 || m > n) return -1;
+// Lowest m eigenvalues of the symmetric n x n matrix given in packed upper
+// storage (AP(i + j(j-1)/2) = A(i,j), i <= j), w[m] ascending, and the
+// eigenvectors of the lowest mvec of them, z[n x mvec].
+int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *z) {
+  if (n <= 0 || m <= 0 || m > n || mvec < 0 || mvec > m) return -1;
   std::vector<double> A((size_t)n * n);
   for (int j = 0; j < n; ++j)
     for (int i = 0; i <= j; ++i) {
@@ -229,9 +230,9 @@ int sym_eig_lowest(int n, const double *ap, int m, double *w, double *z) {
   std::vector<std::vector<double>> cluster;
   std::vector<double> x(n);
   double prev = 0.0;
-  for (int j = 0; j < m; ++j) {
+  for (int j = 0; j < m; ++j) w[j] = ev[j];
+  for (int j = 0; j < mvec; ++j) {
     double lam = ev[j];
-    w[j] = lam;
     if (j > 0 && lam - prev > ortol) cluster.clear();
     if (j > 0 && lam - prev < 10.0 * eps * std::fabs(lam)) lam = prev + 10.0 * eps * std::fabs(lam);
     inv_iter(T, lam, x.data(), cluster, (unsigned)j + 1u, tnorm);

@@ -466,11 +466,11 @@ int build_y(gg_ctx *ctx, const YDesc *d_yd, int nf, double *dY, DBuf<double> &sc
   GG_TRY(scratch.alloc((size_t)2 * nf * np));
   double *TZ = scratch.p, *TW = scratch.p + (size_t)nf * np;
   dim3 grid1((np + 127) / 128, nf);
-  k_ytemp<<<grid1, 128, 0, ctx->stream>>>(d_yd, nf, o.dPF.p, o.dQF.p, o.ld, g.dRP.p, g.dPow.p, np, TZ, TW);
+  k_ytemp<<<grid1, 128, 0, ctx->stream>>>(d_yd, nf, o.dPF.p, o.dQF.p, o.ld, g.dRP.p, g.dPow.p, np, TZ, TW); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaMemsetAsync(dY, 0, (size_t)nf * np * sizeof(double), ctx->stream));
   const int nthr = nf * 4;
-  k_ychain<<<(nthr + 127) / 128, 128, 0, ctx->stream>>>(d_yd, nf, TZ, TW, g.dR.p, g.dPow.p, np, g.q, dY);
+  k_ychain<<<(nthr + 127) / 128, 128, 0, ctx->stream>>>(d_yd, nf, TZ, TW, g.dR.p, g.dPow.p, np, g.q, dY); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
@@ -608,7 +608,7 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   GG_TRY(dA.alloc((size_t)npairs * KC));
   {
     dim3 gr((KC + 127) / 128, npairs);
-    k_apairs<<<gr, 128, 0, ctx->stream>>>(dPairs.p, npairs, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dRPOR.p, KC, g.q, dA.p);
+    k_apairs<<<gr, 128, 0, ctx->stream>>>(dPairs.p, npairs, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dRPOR.p, KC, g.q, dA.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   GG_TRY(dFb.alloc(std::max<int64_t>(N, 1)));
@@ -617,7 +617,7 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   if (!tiles.empty()) {
     k_rk_gemm<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(dTiles.p, dRowpair.p, dPairs.p, dA.p, dY.p, dYd.p, KC,
                                                               np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p,
-                                                              g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p);
+                                                              g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   int hfb[2] = {0, 0};
@@ -630,7 +630,7 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
     const size_t smem = (size_t)wpb * np * sizeof(double);
     const int blocks = std::min((nfb + wpb - 1) / wpb, 4096);
     k_quad_items<<<blocks, 32 * wpb, smem, ctx->stream>>>(dFb.p, dNfb.p, nfb, dY.p, np, o.dPF.p, o.dQF.p, o.ld, g.dR.p,
-                                                          g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p);
+                                                          g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   double ms = 0;
@@ -727,7 +727,7 @@ int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out) {
   GG_TRY(dout.alloc(1));
   GG_TRY(build_y(ctx, dy.p, 1, dY.p, scratch));
   k_quad_items<<<1, 32, g.np * sizeof(double), ctx->stream>>>(di.p, nullptr, 1, dY.p, g.np, o.dPF.p, o.dQF.p, o.ld,
-                                                             g.dR.p, g.dRP.p, g.dRPOR.p, g.q, dout.p);
+                                                             g.dR.p, g.dRP.p, g.dRPOR.p, g.q, dout.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -746,7 +746,7 @@ static int run_rinti(gg_ctx *ctx, const std::vector<int2> &jk, int mode, double 
   const int blocks = std::max(1, std::min(((int)jk.size() + wpb - 1) / wpb, 2048));
   k_rinti<<<blocks, 32 * wpb, smem, ctx->stream>>>(djk.p, (int)jk.size(), mode, o.dPF.p, o.dQF.p, o.ld, o.dMF.p,
                                                    o.dNAK.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.dZZ.p, g.np, g.q, dOut,
-                                                   outidx ? didx.p : nullptr);
+                                                   outidx ? didx.p : nullptr); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   return GG_OK;
@@ -772,7 +772,7 @@ int gg_iabint_table(gg_ctx *ctx, double *iab) {
   const int nw = o.nw;
   GG_TRY(timer_start(ctx));
   GG_TRY(ctx->dIab.alloc((size_t)nw * nw));
-  k_fill<<<64, 256, 0, ctx->stream>>>(ctx->dIab.p, (size_t)nw * nw, nan(""));
+  k_fill<<<64, 256, 0, ctx->stream>>>(ctx->dIab.p, (size_t)nw * nw, nan("")); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   std::vector<int2> jk;
   std::vector<int> idx;

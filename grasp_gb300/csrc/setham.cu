@@ -557,12 +557,12 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
   if (L.nlab) {
     const int blocks = (int)std::min<int64_t>((L.nlab * 32 + 255) / 256, 65535);
     k_label_slots<<<blocks, 256, 0, s>>>(L.dLab.p, L.dStart.p, L.nlab, dLab0.p, nlists, nw, o.dNAK.p, rk.dInd.p,
-                                         dKstart.p, rk.kloop, nrk, cslot.p, err.p);
+                                         dKstart.p, rk.kloop, nrk, cslot.p, err.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   const int gblocks = 152 * 8;
   if (ncontr) {
-    k_count_loc<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, nnz, cnt.p, err.p);
+    k_count_loc<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, nnz, cnt.p, err.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   int herr = 0;
@@ -574,26 +574,26 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
     const int64_t chunk = 1 << 16;
     const int64_t nparts = (nnz + chunk - 1) / chunk;
     GG_TRY(part.alloc(nparts + 1));
-    k_scan_blocks<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk);
-    k_scan_parts<<<1, 32, 0, s>>>(part.p, nparts);
-    k_scan_final<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk, off.p);
+    k_scan_blocks<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk); ::gg::note_launch();
+    k_scan_parts<<<1, 32, 0, s>>>(part.p, nparts); ::gg::note_launch();
+    k_scan_final<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk, off.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   if (ncontr) {
-    k_scatter_perm<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, off.p, fill.p, perm.p);
-    k_sort_gather<<<gblocks, 256, 0, s>>>(off.p, nnz, perm.p, L.dCoeff.p, cslot.p, coeff_s.p, slot_s.p);
+    k_scatter_perm<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, off.p, fill.p, perm.p); ::gg::note_launch();
+    k_sort_gather<<<gblocks, 256, 0, s>>>(off.p, nnz, perm.p, L.dCoeff.p, cslot.p, coeff_s.p, slot_s.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   // EMT = 0 ; diagonal pieces ; list contributions ; EAV shift
   GG_CUDA(cudaMemsetAsync(h->dEmt.p, 0, nnz * sizeof(double), s));
   k_diag_terms<<<(ncf + 127) / 128, 128, 0, s>>>(dTerms.p, (int)terms.size(), L.dIq.p, nw, ncf, h->dIendc.p, integ.p,
-                                                 h->dEmt.p);
+                                                 h->dEmt.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
-  k_assemble<<<gblocks, 256, 0, s>>>(off.p, nnz, coeff_s.p, slot_s.p, integ.p, h->dEmt.p);
+  k_assemble<<<gblocks, 256, 0, s>>>(off.p, nnz, coeff_s.p, slot_s.p, integ.p, h->dEmt.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   DBuf<double> deav;
   GG_TRY(deav.alloc(1));
-  k_eav<<<1, 1024, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dDiag.p, deav.p);
+  k_eav<<<1, 1024, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dDiag.p, deav.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   double eav = 0;
   GG_CUDA(cudaMemcpyAsync(&eav, deav.p, sizeof(double), cudaMemcpyDeviceToHost, s));

@@ -234,12 +234,12 @@ int build_sym(gg_hmat *h) {
   GG_CUDA(cudaMemcpyAsync(dr0.p, r0.data(), (nch + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
   GG_TRY(cnt.alloc((size_t)nch * ncf));
   GG_CUDA(cudaMemsetAsync(cnt.p, 0, (size_t)nch * ncf * sizeof(int), s));
-  k_tcount<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cnt.p);
+  k_tcount<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cnt.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   GG_TRY(rowlen.alloc(ncf));
-  k_tcol_total<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dIendc.p, rowlen.p);
+  k_tcol_total<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dIendc.p, rowlen.p); ::gg::note_launch();
   GG_TRY(h->dSymPtr.alloc(ncf + 1));
-  k_rowlen_scan<<<1, 1024, 0, s>>>(rowlen.p, ncf, h->dSymPtr.p);
+  k_rowlen_scan<<<1, 1024, 0, s>>>(rowlen.p, ncf, h->dSymPtr.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   int64_t total = 0;
   GG_CUDA(cudaMemcpyAsync(&total, h->dSymPtr.p + ncf, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -249,9 +249,9 @@ int build_sym(gg_hmat *h) {
   GG_TRY(h->dSymCol.alloc(total));
   GG_TRY(h->dSymSrc.alloc(total));
   GG_TRY(cursor.alloc((size_t)nch * ncf));
-  k_cursor<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dSymPtr.p, h->dIendc.p, cursor.p);
-  k_own<<<(ncf * 32 + 255) / 256, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, ncf, h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p);
-  k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cursor.p, h->dSymCol.p, h->dSymSrc.p);
+  k_cursor<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dSymPtr.p, h->dIendc.p, cursor.p); ::gg::note_launch();
+  k_own<<<(ncf * 32 + 255) / 256, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, ncf, h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p); ::gg::note_launch();
+  k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cursor.p, h->dSymCol.p, h->dSymSrc.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaStreamSynchronize(s));
   h->sym_valid = true;
@@ -267,7 +267,7 @@ int refresh_sym_values(gg_hmat *h) {
   GG_TRY(h->dSymHi.alloc(h->sym_nnz));
   GG_TRY(h->dSymLo.alloc(h->sym_nnz));
   k_symvals<<<(h->ncf * 32 + 255) / 256, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p, h->dEmt.p, h->ncf,
-                                                      h->dSymVal.p, h->dSymHi.p, h->dSymLo.p);
+                                                      h->dSymVal.p, h->dSymHi.p, h->dSymLo.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   h->sym_vals_valid = true;
   return GG_OK;
@@ -282,11 +282,11 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
     double *y = dy + (size_t)v * n;
     if (precision == GG_SPLIT) {
       GG_TRY(h->dXs.alloc(n));
-      k_split_x<<<(n + 255) / 256, 256, 0, s>>>(x, h->dXs.p, n);
+      k_split_x<<<(n + 255) / 256, 256, 0, s>>>(x, h->dXs.p, n); ::gg::note_launch();
       k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p, h->dDiag.p, x,
-                                          y, n);
+                                          y, n); ::gg::note_launch();
     } else {
-      k_spmv64<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, x, y, n);
+      k_spmv64<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, x, y, n); ::gg::note_launch();
     }
     GG_CUDA(cudaGetLastError());
   }
@@ -304,6 +304,29 @@ double spmv_bytes(const gg_hmat *h, int precision, int m) {
 }  // namespace gg
 
 using namespace gg;
+
+extern "C" int gg_matvec_timing(gg_ctx *ctx, gg_hmat *h, int precision, int iters, double *ms_per_launch,
+                                double *alg_bytes) {
+  if (!ctx || !h || h->ctx != ctx || iters < 1 || !ms_per_launch) return fail(GG_ERR_ARG, "gg_matvec_timing: bad args");
+  if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_matvec_timing: EMT not set");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_TRY(refresh_sym_values(h));
+  DBuf<double> x, y;
+  const int n = h->ncf;
+  GG_TRY(x.alloc(n));
+  GG_TRY(y.alloc(n));
+  std::vector<double> hx(n);
+  for (int i = 0; i < n; ++i) hx[i] = 1.0 / (1.0 + (i % 97));
+  GG_CUDA(cudaMemcpyAsync(x.p, hx.data(), n * 8, cudaMemcpyHostToDevice, ctx->stream));
+  GG_TRY(spmv(h, precision, x.p, y.p, 1, ctx->stream));  // warm-up
+  GG_TRY(timer_start(ctx));
+  for (int it = 0; it < iters; ++it) GG_TRY(spmv(h, precision, x.p, y.p, 1, ctx->stream));
+  double ms = 0;
+  GG_TRY(timer_stop(ctx, &ms));
+  *ms_per_launch = ms / iters;
+  if (alg_bytes) *alg_bytes = spmv_bytes(h, precision, 1);
+  return GG_OK;
+}
 
 extern "C" int gg_spicmv2(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c, int precision) {
   if (!ctx || !h || h->ctx != ctx || m < 1 || !b || !c) return fail(GG_ERR_ARG, "gg_spicmv2: bad arguments");

@@ -178,8 +178,26 @@ int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double 
  * Device time (ms, CUDA events on the context stream) of the named stage of
  * the last call: 0 genintrk, 1 iabint, 2 setham assemble, 3 maneig total,
  * 4 matvec (sum over the last maneig), 5 number of matvec launches,
- * 6 bytes moved by one matvec (algorithmic), 7 setham upload.              */
+ * 6 bytes moved by one matvec (algorithmic), 7 setham upload,
+ * 8 / 9 Davidson loops of the leading-block (INIEST2) / full-block stage,
+ * 10 / 11 their matvec ms, 12 full-block matvec launches, 13 host ms in the
+ * projected eigenproblems, 14 host ms waiting for device results.          */
 double gg_stage_stat(gg_ctx *ctx, int which);
+
+/* ---- measurement helpers (no counterpart in the reference) ------------------
+ * gg_launch_count: kernels this library has launched in this process.
+ * gg_event_record / gg_event_elapsed: CUDA events (8 slots) on the context
+ * stream; elapsed synchronises on slot b.
+ * gg_matvec_timing: average device time of one y = H x launch (after a
+ * warm-up) over iters launches, and its algorithmic bytes.                  */
+long long gg_launch_count(void);
+/* Page-locks (pins) caller memory so that uploads from it run at full link
+ * rate; unregister before freeing it. */
+int gg_host_register(void *p, size_t bytes);
+int gg_host_unregister(void *p);
+int gg_event_record(gg_ctx *ctx, int slot);
+int gg_event_elapsed(gg_ctx *ctx, int a, int b, double *ms);
+int gg_matvec_timing(gg_ctx *ctx, gg_hmat *h, int precision, int iters, double *ms_per_launch, double *alg_bytes);
 
 #ifdef __cplusplus
 }

@@ -90,7 +90,7 @@ def lib():
         L.or_gdvd.argtypes = [C.c_int, _i64, _i32, _d, _d, C.POINTER(OrDvdParams), _d, C.c_int64,
                               _int, _int, _int, C.c_int]
         L.or_maneig.argtypes = [C.c_int, C.c_int, C.c_int, _i64, _i32, _d, _d, _d, _int, _int, _int, C.c_int,
-                                C.c_int]
+                                C.c_int, C.c_int, _d]
         _lib = L
     return _lib
 
@@ -228,16 +228,18 @@ def dspevx(ap, n, il, iu):
     return w, z.T
 
 
-def maneig(flavour, ncf, nvec, iendc, irow, emt, nthreads=1, robust=False):
+def maneig(flavour, ncf, nvec, iendc, irow, emt, nthreads=1, robust=False, maxiter=0):
     iendc = np.ascontiguousarray(iendc, np.int64); irow = np.ascontiguousarray(irow, np.int32)
     emt = np.ascontiguousarray(emt, np.float64)
     ev = np.zeros(nvec); vec = np.zeros((nvec, ncf))
     nl, nm, ie = C.c_int(0), C.c_int(0), C.c_int(0)
+    secs = np.zeros(2)
     rc = lib().or_maneig(flavour, ncf, nvec, _p(iendc, _i64), _p(irow, _i32), _p(emt, _d), _p(ev, _d),
-                         _p(vec, _d), C.byref(nl), C.byref(nm), C.byref(ie), nthreads, int(robust))
+                         _p(vec, _d), C.byref(nl), C.byref(nm), C.byref(ie), nthreads, int(robust), int(maxiter),
+                         _p(secs, _d))
     if rc < 0:
         raise RuntimeError(f"MANEIG failed rc={rc} ierr={ie.value}")
-    return ev, vec.T, dict(nloops=nl.value, nmv=nm.value, ierr=ie.value)
+    return ev, vec.T, dict(nloops=nl.value, nmv=nm.value, ierr=ie.value, t_iniest2=secs[0], t_dvdson=secs[1])
 
 
 def clrx(ka, k, kb):

@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -1401,7 +1402,11 @@ int or_gdvd(int n, const int64_t *iendc, const int32_t *irow, const double *emt,
 }
 
 int or_maneig(int flavour, int ncf, int nvec, const int64_t *iendc, const int32_t *irow, const double *emt,
-              double *eval, double *evec, int *nloops, int *nmv, int *ierr, int nthreads, int robust) {
+              double *eval, double *evec, int *nloops, int *nmv, int *ierr, int nthreads, int robust,
+              int maxiter_override, double *seconds) {
+  using clk = std::chrono::steady_clock;
+  const auto t_start = clk::now();
+  if (seconds) seconds[0] = seconds[1] = 0.0;
   *nloops = 0;
   *nmv = 0;
   *ierr = 0;
@@ -1437,6 +1442,9 @@ int or_maneig(int flavour, int ncf, int nvec, const int64_t *iendc, const int32_
     for (int ic = 1; ic <= ncf; ++ic) diag[ic - 1] = emt[iendc[ic] - 1];
     const int nmax = (flavour == 0) ? 2000 : N1000;
     or_iniest2(nmax, ncf, niv, work.data(), emt, iendc, irow);
+    const auto t_ini = clk::now();
+    if (seconds) seconds[0] = std::chrono::duration<double>(t_ini - t_start).count();
+    if (maxiter_override > 0) maxitr = maxiter_override;
     if (flavour == 0 || ncf > N1000) {
       or_dvd_params p;
       p.lim = lim;
@@ -1453,6 +1461,7 @@ int or_maneig(int flavour, int ncf, int nvec, const int64_t *iendc, const int32_
       int rc = or_gdvd(ncf, iendc, irow, emt, diag.data(), &p, work.data(), lwork, nloops, nmv, ierr, nthreads);
       if (rc < 0) return rc;
     }
+    if (seconds) seconds[1] = std::chrono::duration<double>(clk::now() - t_ini).count();
     const int64_t nend = (int64_t)ncf * niv;
     for (int j = 0; j < nvec; ++j) {
       eval[j] = work[nend + j];

@@ -73,11 +73,10 @@ double or_clrx(int kappaa, int k, int kappab);
  * CSFs as [nw x ncf] column-major bytes: iq[(ir-1)*nw + (ia-1)].
  * nkj: 2j of each orbital is derived from NAK.
  * iendc[0..ncf] (IENDC(0:NCF), 1-based positions, diagonal last per row).
- * The T list and each V^k list are given as flattened label groups:
+ * The T list and each V^k list are given as label groups (or_list):
  *   nlab labels; lab[l]; start[l]..start[l+1]-1 index the contribution arrays
  *   loc[] (1-based INDEX into EMT) and coeff[].
- * v lists are given for k = 0..kmaxf; vk_* arrays are concatenations, with
- * vk_nlab[k] labels each and vk_labofs[k] the first label of list k.
+ * vlists has kmaxf + 1 entries (k = 0..kmaxf).
  * emt[nelmnt] is accumulated (the caller zeroes it, as MATRIX does).
  * Returns 0, or -1 when a LOC exceeds nelmnt (the reference ERROR STOPs).
  * ------------------------------------------------------------------- */
@@ -131,11 +130,13 @@ int or_iniest2(int nmax, int ncf, int niv, double *basis, const double *emt,
  * The matrix already has EAV subtracted from its diagonal. Computes the
  * lowest nvec eigenpairs (IVEC = 1..nvec) with the reference's dispatch
  * (dense DSPEVX or Davidson), and the reference's sign convention.
- * eval[nvec], evec[ncf x nvec]. */
+ * eval[nvec], evec[ncf x nvec]. maxiter_override > 0 replaces MAXITR (for
+ * timing a bounded number of Davidson loops); seconds (may be NULL) gets
+ * [INIEST2 wall time, DVDSON wall time]. */
 int or_maneig(int flavour, int ncf, int nvec, const int64_t *iendc,
               const int32_t *irow, const double *emt, double *eval,
               double *evec, int *nloops, int *nmv, int *ierr, int nthreads,
-              int robust);
+              int robust, int maxiter_override, double *seconds);
 
 #ifdef __cplusplus
 }
