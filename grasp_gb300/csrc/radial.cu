@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 #include "gg_internal.cuh"
 
@@ -733,6 +734,111 @@ int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out) {
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   return GG_OK;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// gg_slater_noalloc: SLATER without any device allocation.
+//
+// Some callers cannot allocate device memory when they need one integral: a
+// host code that has handed the whole device to a memory pool or to the
+// Hamiltonian and Davidson basis of a large block (where a cudaMalloc would
+// fail or fragment the pool), or code whose error handling cannot recover
+// from an allocation failure in the middle of a loop (the Fortran callers
+// STOP). For them this entry point evaluates R^k(ab;cd) exactly like
+// gg_slater, but its working arrays (the two TEMP arrays and Y^k of YZK, the
+// integral's descriptors and its result) live in one file-scope device array
+// of fixed size, reserved when the library is loaded and held by every GPU
+// that loads it until the process exits.
+//
+// Limit: the grid must satisfy N + 26 <= NOALLOC_NP (N <= 2022 points; GRASP
+// uses 590). The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress) with that device current; make that first call
+// before any stream capture. All calls share the array and it keeps the last
+// call's contents (Y^k is cleared at the start of each call): calls that can
+// overlap on the GPU -- several host threads, or several contexts on one
+// device -- race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+namespace gg {
+namespace {
+constexpr int NOALLOC_NP = 2048;              // doubles per working array
+constexpr int NOALLOC_DESC = 64;              // doubles reserved for descriptors and the result
+static __device__ __align__(256) double g_noalloc_scratch[3 * NOALLOC_NP + NOALLOC_DESC];
+
+struct NoallocAddr {
+  std::mutex mu;
+  double *ptr[64] = {};
+};
+NoallocAddr &noalloc_addr() {
+  static NoallocAddr a;
+  return a;
+}
+}  // namespace
+}  // namespace gg
+
+extern "C" int gg_slater_noalloc(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out) {
+  GG_TRY(ensure_orbitals(ctx));
+  Orbitals &o = ctx->orb;
+  Grid &g = ctx->grid;
+  const int nw = o.nw;
+  if (!out || k < 0 || k > KLIMIT || ia < 1 || ib < 1 || ic < 1 || id < 1 || ia > nw || ib > nw || ic > nw ||
+      id > nw)
+    return fail(GG_ERR_ARG, "gg_slater_noalloc: bad arguments");
+  if (g.np > NOALLOC_NP)
+    return fail(GG_ERR_ARG, "gg_slater_noalloc: grid of " + std::to_string(g.n) +
+                                " points exceeds the fixed scratch (at most " + std::to_string(NOALLOC_NP - GPAD - 10) +
+                                " points); use gg_slater");
+  if (ctx->device < 0 || ctx->device >= 64) return fail(GG_ERR_ARG, "gg_slater_noalloc: device index above 63");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  double *base = nullptr;
+  {
+    NoallocAddr &A = noalloc_addr();
+    std::lock_guard<std::mutex> lock(A.mu);
+    if (!A.ptr[ctx->device]) {
+      void *p = nullptr;
+      GG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+      A.ptr[ctx->device] = static_cast<double *>(p);
+    }
+    base = A.ptr[ctx->device];
+  }
+  double *TZ = base, *TW = base + NOALLOC_NP, *Y = base + 2 * NOALLOC_NP;
+  double *tail = base + 3 * NOALLOC_NP;  // 256-byte aligned: 3 * 2048 doubles = 192 * 256 bytes
+  YDesc *dyd = reinterpret_cast<YDesc *>(tail);
+  QuadItem *ditem = reinterpret_cast<QuadItem *>(tail + 8);
+  double *dout = tail + 16;
+  YDesc y;
+  y.k = k;
+  y.b = ib;
+  y.d = id;
+  y.mtp = std::min(o.mf[ib], o.mf[id]);
+  y.mtpb = (k == 0 && ib == id) ? g.n : y.mtp;
+  y.cs = 0;
+  y.nd = 1;
+  QuadItem it;
+  it.a = ia;
+  it.c = ic;
+  it.f = 0;
+  it.mtp = (k == 0 && ib == id) ? std::min(o.mf[ia], o.mf[ic]) : std::min(std::min(y.mtp, o.mf[ia]), o.mf[ic]);
+  it.pos = 0;
+  const int np = g.np;
+  GG_CUDA(cudaMemcpyAsync(dyd, &y, sizeof(YDesc), cudaMemcpyHostToDevice, ctx->stream));
+  GG_CUDA(cudaMemcpyAsync(ditem, &it, sizeof(QuadItem), cudaMemcpyHostToDevice, ctx->stream));
+  dim3 grid1((np + 127) / 128, 1);
+  k_ytemp<<<grid1, 128, 0, ctx->stream>>>(dyd, 1, o.dPF.p, o.dQF.p, o.ld, g.dRP.p, g.dPow.p, np, TZ, TW);
+  ::gg::note_launch();
+  GG_CUDA(cudaMemsetAsync(Y, 0, (size_t)np * sizeof(double), ctx->stream));
+  k_ychain<<<1, 128, 0, ctx->stream>>>(dyd, 1, TZ, TW, g.dR.p, g.dPow.p, np, g.q, Y);
+  ::gg::note_launch();
+  k_quad_items<<<1, 32, np * sizeof(double), ctx->stream>>>(ditem, nullptr, 1, Y, np, o.dPF.p, o.dQF.p, o.ld, g.dR.p,
+                                                            g.dRP.p, g.dRPOR.p, g.q, dout);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(out, dout, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GG_OK;
+}
+
+extern "C" {
 
 static int run_rinti(gg_ctx *ctx, const std::vector<int2> &jk, int mode, double *dOut, const std::vector<int> *outidx) {
   Orbitals &o = ctx->orb;

@@ -90,6 +90,17 @@ int gg_get_rk_table(gg_ctx *ctx, int32_t *indteirk, double *valteirk, int32_t *k
 int gg_rkintc(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *tegral);
 /* SLATER (lib9290/slater.f90:3): one R^k(ab;cd) evaluated on the device. */
 int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out);
+/* gg_slater without any device allocation. No counterpart in the reference:
+ * for callers that cannot allocate device memory at the point where they
+ * need an integral (device memory fully handed to a pool or to a large
+ * block's Hamiltonian and basis; callers that cannot recover from a failed
+ * allocation inside a loop). Same result as gg_slater. Its working arrays
+ * sit in one fixed device array that every GPU loading this library holds
+ * until exit; grids up to 2022 points (N + 26 <= 2048), larger ones are
+ * rejected with GG_ERR_ARG. The first call on a device looks up that
+ * array's address with the device current: make it before any stream
+ * capture. Calls share the array: calls that overlap on the GPU race.      */
+int gg_slater_noalloc(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out);
 
 /* ---- one-body integrals ----------------------------------------------------
  * RINTI (lib9290/rinti.f90:3) with DPBDT (dpbdt.f90:3): I(ab), mode 0
