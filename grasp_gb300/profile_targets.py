@@ -1,0 +1,55 @@
+"""Small, fixed command lines for the profiler (ncu) runs whose summaries sit
+in profiles/. Each target builds the Fe XV workload once and runs only the
+kernel family it is named for, a few times:
+
+  python -m grasp_gb300.profile_targets spmv     # 3 full-size y = H x launches per precision
+  python -m grasp_gb300.profile_targets solve    # one full CI solve (launch list)
+  python -m grasp_gb300.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
+"""
+from __future__ import annotations
+
+import sys
+
+
+def _fe15_context():
+    from . import Context, HMatrix, workloads
+    w = workloads.fe15()
+    b = w.block
+    ctx = Context(0)
+    ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
+    ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    ctx.genintrk()
+    ctx.iabint_table()
+    H = HMatrix(ctx, b.ncf, b.iendc, b.irow)
+    H.setham(b.iq, b.tlist, b.vlists)
+    return w, ctx, H
+
+
+def spmv():
+    from . import FP64, SPLIT
+    w, ctx, H = _fe15_context()
+    for prec in (FP64, SPLIT):
+        ms, by = H.matvec_timing(prec, 3)
+        print(f"precision {prec}: {ms * 1e3:.1f} us per launch, {by / 1e6:.1f} MB algorithmic")
+
+
+def solve():
+    from . import SPLIT
+    w, ctx, H = _fe15_context()
+    ev, vec, info = H.maneig(w.nroots, flavour=0, precision=SPLIT)
+    print("loops", info["nloops"], "E0", ev[0])
+
+
+def rk():
+    from . import Context, workloads
+    w = workloads.rk40()
+    ctx = Context(0)
+    ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
+    ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    for _ in range(3):
+        n, _ = ctx.genintrk(kmax=8)
+    print("R^k integrals", n, "ms", ctx.stage_stat(0))
+
+
+if __name__ == "__main__":
+    {"spmv": spmv, "solve": solve, "rk": rk}[sys.argv[1]]()

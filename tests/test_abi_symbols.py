@@ -1,0 +1,60 @@
+"""The C-ABI libraries load on a machine without a GPU and export every
+function their headers (include/grasp_gpu.h, include/grasp_synth.h) declare.
+No compute calls here."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:gg|gs)_\w+)\s*\(", src, flags=re.M)
+    return sorted(set(names))
+
+
+def exported(path):
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True, check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if " T " in line}
+
+
+@pytest.fixture(scope="module")
+def libs():
+    from grasp_gb300 import build
+    return build.build()
+
+
+def test_gpu_header_symbols_exported(libs):
+    names = declared("grasp_gpu.h")
+    assert len(names) >= 30
+    syms = exported(libs[0])
+    missing = [n for n in names if n not in syms]
+    assert not missing, missing
+
+
+def test_synth_header_symbols_exported(libs):
+    names = declared("grasp_synth.h")
+    syms = exported(libs[1])
+    assert not [n for n in names if n not in syms]
+
+
+def test_gpu_library_loads_and_reports_errors(libs):
+    lib = ctypes.CDLL(libs[0])
+    lib.gg_version.restype = ctypes.c_int
+    assert lib.gg_version() == 1
+    lib.gg_last_error.restype = ctypes.c_char_p
+    # argument checks run before any device call
+    h = ctypes.c_void_p()
+    assert lib.gg_ctx_create(-1, ctypes.byref(h)) != 0
+    assert lib.gg_last_error()
+
+
+def test_python_bindings_cover_header(libs):
+    from grasp_gb300 import _lib
+    assert set(declared("grasp_gpu.h")) <= set(_lib.GPU_SYMBOLS)
+    assert set(declared("grasp_synth.h")) <= set(_lib.SYNTH_SYMBOLS)
