@@ -29,9 +29,18 @@ class Context:
         check(_lib.gpu().gg_ctx_create(device, C.byref(self._h)))
         self.nw = 0
         self.n = 0
+        # handle boxes of the matrices made on this context: closing the
+        # context destroys them first (finalisers of objects collected
+        # together run in no particular order)
+        self._children = []
 
     def close(self):
         if self._h:
+            for box in self._children:
+                if box[0]:
+                    _lib.gpu().gg_hmat_destroy(box[0])
+                    box[0] = C.c_void_p()
+            self._children = []
             _lib.gpu().gg_ctx_destroy(self._h)
             self._h = C.c_void_p()
 
@@ -135,15 +144,20 @@ class HMatrix:
         self.iendc = np.ascontiguousarray(iendc, np.int64)
         self.irow = np.ascontiguousarray(irow, np.int32)
         self.nnz = int(self.iendc[-1])
-        self._h = C.c_void_p()
+        self._box = [C.c_void_p()]
         check(_lib.gpu().gg_hmat_create(ctx._h, self.ncf, self.nnz, ptr(self.iendc, _i64), ptr(self.irow, _i32),
-                                        C.byref(self._h)))
+                                        C.byref(self._box[0])))
+        ctx._children.append(self._box)
         self.eav = None
 
+    @property
+    def _h(self):
+        return self._box[0]
+
     def close(self):
-        if self._h:
-            _lib.gpu().gg_hmat_destroy(self._h)
-            self._h = C.c_void_p()
+        if self._box[0] and self.ctx._h:
+            _lib.gpu().gg_hmat_destroy(self._box[0])
+            self._box[0] = C.c_void_p()
 
     def __del__(self):
         try:

@@ -11,6 +11,7 @@ static thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void note_launches(long long m) { g_launches.fetch_add(m, std::memory_order_relaxed); }
 void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int status, const std::string &msg) {
   g_last_error = msg;
@@ -268,7 +269,7 @@ int gg_set_orbitals(gg_ctx *ctx, int nw, int ld, const int *nak, const int *mf, 
 }
 
 double gg_stage_stat(gg_ctx *ctx, int which) {
-  if (!ctx || which < 0 || which >= 16) return -1.0;
+  if (!ctx || which < 0 || which >= 24) return -1.0;
   return ctx->stats[which];
 }
 

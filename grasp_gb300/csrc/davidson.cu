@@ -14,6 +14,14 @@
 // copies per iteration (a residual norm and one column of S) synchronise
 // the two.
 //
+// The N-length kernels are tall-skinny FP64 products (N ~ 1e4..1e6 rows,
+// k <= LIM columns). GB300 issues FP64 at a small fraction of its FP32 rate,
+// so they are laid out for FP64 issue: transposed products give each thread
+// 16 independent FMA chains (16 columns) and reduce through warp shuffles;
+// row products tile 32 rows x 8 column chunks per block so that all SMs hold
+// enough independent chains. All reductions run in a fixed order: results are
+// reproducible run to run.
+//
 // Differences from the reference, all at rounding level:
 //  - Gram-Schmidt is two-pass classical (CGS2), the reference's mgs_nrm is
 //    two-pass modified; both leave the new vector orthonormal to working
@@ -22,6 +30,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -31,143 +40,316 @@ namespace gg {
 namespace {
 
 constexpr int TPB = 256;
-constexpr int RB = 1024;  // rows per block in the partial-dot kernels
-constexpr int CG = 8;     // columns per block in the partial-dot kernels
+constexpr int RT = 128;        // threads (= rows) per block of the row kernels
+constexpr int CD_T = 256;      // threads of the column-dot kernel (8 warps)
+constexpr int CD_G = 4;        // columns per warp group of the column-dot kernel
+constexpr int CD_MAXR = 1024;  // rows per block of the column-dot kernel, at most
+constexpr int SV_MAX = 1024;   // LIM bound: shared copies of s and of the coefficients
+constexpr int RC = 32;         // rows per block of MULTBC (one per lane)
+constexpr int NCH = 8;         // warps of MULTBC
 
-// partial dots part[rb * k + j] = sum_{i in row block rb} B[i, j] w[i], j < k
-__global__ void k_dots_part(const double *__restrict__ B, int64_t ld, int k, const double *__restrict__ w, int n,
-                            double *__restrict__ part) {
-  __shared__ double s[CG][TPB];
-  const int rb = blockIdx.x, j0 = blockIdx.y * CG;
-  double acc[CG];
+// device scalars of one pass (slots of Dvd::scal)
+constexpr int SC_RN2 = 0;   // |r|^2 of the last Ritz residual
+constexpr int SC_RHS = 1;   // RHSEPS of the robust shift
+constexpr int SC_CONV = 2;  // 1.0 when |r| < CRITR
+constexpr int SC_F1 = 3;    // 1/|w| after Gram-Schmidt pass 1
+constexpr int SC_F2 = 4;    // 1/|w| after pass 2
+constexpr int SC_N = 16;
+
+__device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
-  for (int c = 0; c < CG; ++c) acc[c] = 0.0;
-  const int i0 = rb * RB, i1 = min(n, i0 + RB);
-  for (int i = i0 + threadIdx.x; i < i1; i += TPB) {
-    const double wi = w[i];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum of one value per thread over a block of NT threads, in a fixed order;
+// the result is valid in thread 0.
+template <int NT> __device__ __forceinline__ double block_sum(double v, double *red) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
 #pragma unroll
-    for (int c = 0; c < CG; ++c)
-      if (j0 + c < k) acc[c] = fma(B[(size_t)(j0 + c) * ld + i], wi, acc[c]);
-  }
-#pragma unroll
-  for (int c = 0; c < CG; ++c) s[c][threadIdx.x] = acc[c];
-  __syncthreads();
-  for (int st = TPB / 2; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st)
-#pragma unroll
-      for (int c = 0; c < CG; ++c) s[c][threadIdx.x] += s[c][threadIdx.x + st];
-    __syncthreads();
-  }
-  if (threadIdx.x < CG && j0 + (int)threadIdx.x < k) part[(size_t)rb * k + j0 + threadIdx.x] = s[threadIdx.x][0];
+    for (int q = 0; q < NT / 32; ++q) t += red[q];
+  return t;
 }
 
-// out[j] = sum over row blocks of part (fixed order)
-__global__ void k_dots_reduce(const double *__restrict__ part, int nrb, int k, double *__restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= k) return;
-  double s = 0.0;
-  for (int r = 0; r < nrb; ++r) s += part[(size_t)r * k + j];
-  out[j] = s;
+// ---------------------------------------------------------------------------
+// The parameters of one Davidson pass. Graph replays read them from device
+// memory (written by the graph's first node from pinned host memory); the
+// launch-by-launch path passes them by value. The kernels are the same.
+// ---------------------------------------------------------------------------
+struct IterParams {
+  int c;         // column written by this pass
+  int k;         // basis columns the Ritz vector is built from
+  double lam;    // EIGVAL(INDX)
+  double gap;    // NEWVEC's GAP for INDX
+  double dl;     // NEWVEC's DL for INDX
+  double critr;  // CRITR
+};
+struct PSrc {
+  const IterParams *dp;
+  IterParams hv;
+  __device__ __forceinline__ IterParams get() const { return dp ? *dp : hv; }
+};
+
+// Last block of a grid to arrive (after its own partial was written):
+// true in every thread of that block.
+__device__ __forceinline__ bool arrive_last(unsigned *counter, bool *flag) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) *flag = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  return *flag;
 }
 
-// w -= B[:, 0:k] coef  (coef on the device)
-__global__ void k_sub_gemv(double *__restrict__ w, const double *__restrict__ B, int64_t ld, int k,
-                           const double *__restrict__ coef, int n) {
-  __shared__ double c[1024];
-  for (int j = threadIdx.x; j < k; j += blockDim.x) c[j] = coef[j];
+// Ritz vector and residual (NEWVEC, dvdson.f90:1100-1111), one row per thread:
+//   b = BASIS s ; a = AB s ; r = a - lambda b -> BASIS(:, c), AB(:, c).
+// The last block adds the per-block |r|^2 in order and derives NEWVEC's
+// robust shift (dvdson.f90:1139-1160) and the convergence flag.
+__global__ void __launch_bounds__(RT) k_ritz(double *B, double *AB, int64_t ld, PSrc ps,
+                                             const double *__restrict__ s, int n, double *__restrict__ part,
+                                             unsigned *__restrict__ counter, double *__restrict__ scal) {
+  const IterParams P = ps.get();
+  const int k = P.k, c = P.c;
+  __shared__ double sv[SV_MAX];
+  __shared__ double red[RT / 32];
+  __shared__ bool last;
+  for (int j = threadIdx.x; j < k; j += RT) sv[j] = s[j];
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  double acc = 0.0;
-  for (int j = 0; j < k; ++j) acc = fma(B[(size_t)j * ld + i], c[j], acc);
-  w[i] -= acc;
-}
-
-// partial sums of squares
-__global__ void k_sq_part(const double *__restrict__ w, int n, double *__restrict__ part) {
-  __shared__ double s[TPB];
-  double acc = 0.0;
-  for (int i = blockIdx.x * TPB + threadIdx.x; i < n; i += gridDim.x * TPB) acc = fma(w[i], w[i], acc);
-  s[threadIdx.x] = acc;
-  __syncthreads();
-  for (int st = TPB / 2; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st) s[threadIdx.x] += s[threadIdx.x + st];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) part[blockIdx.x] = s[0];
-}
-
-// w *= 1/sqrt(sum(part)); every block reduces the partials in the same order
-__global__ void k_normalize(double *__restrict__ w, int n, const double *__restrict__ part, int np) {
-  __shared__ double sc;
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int i = 0; i < np; ++i) s += part[i];
-    const double dnm = sqrt(s);
-    sc = 1.0 / dnm;
-  }
-  __syncthreads();
-  const double f = sc;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) w[i] *= f;
-}
-
-// Ritz vector and residual (NEWVEC, dvdson.f90:1100-1111):
-//   b = BASIS s ; a = AB s ; r = a - lambda b ; part = partial sums of r^2
-__global__ void k_ritz(const double *__restrict__ B, const double *__restrict__ AB, int64_t ld, int k,
-                       const double *__restrict__ s, double lam, double *__restrict__ bout, double *__restrict__ rout,
-                       int n, double *__restrict__ part) {
-  __shared__ double sv[1024];
-  __shared__ double red[TPB];
-  for (int j = threadIdx.x; j < k; j += blockDim.x) sv[j] = s[j];
-  __syncthreads();
-  const int i = blockIdx.x * TPB + threadIdx.x;
-  double r2 = 0.0;
+  const int i = blockIdx.x * RT + threadIdx.x;
+  double r = 0.0;
   if (i < n) {
-    double b = 0.0, a = 0.0;
-    for (int j = 0; j < k; ++j) {
-      b = fma(B[(size_t)j * ld + i], sv[j], b);
-      a = fma(AB[(size_t)j * ld + i], sv[j], a);
+    const double *pb = B + i, *pa = AB + i;
+    double b0 = 0.0, b1 = 0.0, b2 = 0.0, b3 = 0.0, a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    int j = 0;
+    for (; j + 3 < k; j += 4) {
+      const size_t o = (size_t)j * ld;
+      b0 = fma(pb[o], sv[j], b0);
+      a0 = fma(pa[o], sv[j], a0);
+      b1 = fma(pb[o + ld], sv[j + 1], b1);
+      a1 = fma(pa[o + ld], sv[j + 1], a1);
+      b2 = fma(pb[o + 2 * ld], sv[j + 2], b2);
+      a2 = fma(pa[o + 2 * ld], sv[j + 2], a2);
+      b3 = fma(pb[o + 3 * ld], sv[j + 3], b3);
+      a3 = fma(pa[o + 3 * ld], sv[j + 3], a3);
     }
-    const double r = a + (-lam) * b;
-    bout[i] = b;
-    rout[i] = r;
-    r2 = r * r;
+    for (; j < k; ++j) {
+      b0 = fma(pb[(size_t)j * ld], sv[j], b0);
+      a0 = fma(pa[(size_t)j * ld], sv[j], a0);
+    }
+    const double b = (b0 + b1) + (b2 + b3), a = (a0 + a1) + (a2 + a3);
+    r = fma(-P.lam, b, a);
+    B[(size_t)c * ld + i] = b;
+    AB[(size_t)c * ld + i] = r;
   }
-  red[threadIdx.x] = r2;
+  const double t = block_sum<RT>(r * r, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+  if (!arrive_last(counter, &last)) return;
+  double u = 0.0;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + q);
   __syncthreads();
-  for (int st = TPB / 2; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st) red[threadIdx.x] += red[threadIdx.x + st];
-    __syncthreads();
+  u = block_sum<RT>(u, red);
+  if (threadIdx.x == 0) {
+    const double res = sqrt(u);
+    scal[SC_RN2] = u;
+    scal[SC_RHS] = (P.gap > res) ? sqrt(P.dl * res) : fmin(P.dl, sqrt(P.dl));
+    scal[SC_CONV] = (res < P.critr) ? 1.0 : 0.0;
+    *counter = 0u;
   }
-  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-// robust shift + GDVD diagonal preconditioner (gdvd.f90:114-129):
+// robust shift + GDVD diagonal preconditioner (gdvd.f90:114-129) of column c:
 //   r <- r - rhseps b ; DIAG <- DIAG - lambda ; w = r/DIAG (|DIAG| > 1e-6)
 //   or r*1e6 ; DIAG <- DIAG + lambda ; BASIS column <- w
-__global__ void k_precond(double *__restrict__ r, const double *__restrict__ b, double rhseps, double lam,
-                          double *__restrict__ diag, double *__restrict__ w, int n) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const double rr = r[i] + (-rhseps) * b[i];
-  r[i] = rr;
+__device__ __forceinline__ double precond_row(double *bc, double *rc, double *diag, int i, double rhseps, double lam) {
+  const double rr = fma(-rhseps, bc[i], rc[i]);
+  rc[i] = rr;
   const double d = diag[i] - lam;
-  w[i] = (fabs(d) > 1.0e-06) ? rr / d : rr * 1.0e06;
+  const double w = (fabs(d) > 1.0e-06) ? rr / d : rr * 1.0e06;
+  bc[i] = w;
   diag[i] = d + lam;
+  return w;
 }
 
-// out[:, j] = sum_{i<k} B[:, i] C[i + j k], j < m   (MULTBC)
-__global__ void k_multbc(const double *__restrict__ B, int64_t ld, int k, const double *__restrict__ C, int m,
-                         double *__restrict__ out, int n) {
-  extern __shared__ double cs[];
-  for (int t = threadIdx.x; t < k * m; t += blockDim.x) cs[t] = C[t];
-  __syncthreads();
+__global__ void k_precond(double *B, double *AB, int64_t ld, PSrc ps, const double *__restrict__ scal,
+                          double *__restrict__ diag, int n) {
+  const IterParams P = ps.get();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  for (int j = 0; j < m; ++j) {
-    double acc = 0.0;
-    for (int q = 0; q < k; ++q) acc = fma(B[(size_t)q * ld + i], cs[(size_t)j * k + q], acc);
-    out[(size_t)j * ld + i] = acc;
+  precond_row(B + (size_t)P.c * ld, AB + (size_t)P.c * ld, diag, i, scal[SC_RHS], P.lam);
+}
+
+// out[j] = f sum_i X[i, j] w[i] for j < k = c + kofs, w = column c of W
+// (c from the pass parameters; f = scal[fslot], or 1 when fslot < 0).
+// PRE = true first applies the shift and preconditioner to column c (W is
+// then BASIS; AB and DIAG are updated too). Skipped entirely when skip
+// points to a non-zero flag.
+//
+// Layout: block b owns rows [b R, b R + R); it stages w for them in shared
+// memory, then warp g takes column groups g, g + 8, ... of 4 columns: lanes
+// stride the rows (coalesced 256-byte loads, 4 independent FMA chains) and
+// a transpose butterfly reduces the 4 sums over the 32 lanes with 6 adds per
+// lane. The last block adds the per-block partials in block order.
+template <bool PRE>
+__global__ void __launch_bounds__(CD_T) k_cdots(const double *X, int64_t ld, PSrc ps, int kofs, double *W, double *AB,
+                                                double *diag, const double *scal, const double *skip, int fslot,
+                                                int n, int rows, int kp, double *__restrict__ part,
+                                                unsigned *__restrict__ counter, double *__restrict__ out) {
+  if (skip && *skip != 0.0) return;
+  const IterParams P = ps.get();
+  const int c = P.c, k = c + kofs;
+  __shared__ double ws[CD_MAXR];
+  __shared__ bool last;
+  const int r0 = blockIdx.x * rows;
+  const int nr = min(rows, n - r0);
+  double *wc = W + (size_t)c * ld;
+  if (PRE) {
+    const double rhseps = scal[SC_RHS];
+    double *rc = AB + (size_t)c * ld;
+    for (int t = threadIdx.x; t < nr; t += CD_T) ws[t] = precond_row(wc, rc, diag, r0 + t, rhseps, P.lam);
+  } else {
+    for (int t = threadIdx.x; t < nr; t += CD_T) ws[t] = wc[r0 + t];
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int ngrp = (k + CD_G - 1) / CD_G;
+  const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
+  for (int g = wid; g < ngrp; g += CD_T / 32) {
+    const int j0 = g * CD_G;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    const double *x0 = X + (size_t)j0 * ld + r0;
+    if (j0 + CD_G <= k) {
+      for (int t = lane; t < nr; t += 32) {
+        const double wv = ws[t];
+        a0 = fma(x0[t], wv, a0);
+        a1 = fma(x0[t + ld], wv, a1);
+        a2 = fma(x0[t + 2 * ld], wv, a2);
+        a3 = fma(x0[t + 3 * ld], wv, a3);
+      }
+    } else {
+      const int m = k - j0;
+      for (int t = lane; t < nr; t += 32) {
+        const double wv = ws[t];
+        a0 = fma(x0[t], wv, a0);
+        if (m > 1) a1 = fma(x0[t + ld], wv, a1);
+        if (m > 2) a2 = fma(x0[t + 2 * ld], wv, a2);
+      }
+    }
+    // lanes with bit 4 clear keep columns 0, 1; set: 2, 3
+    const double s0 = hi16 ? a0 : a2, s1 = hi16 ? a1 : a3;
+    const double k0 = (hi16 ? a2 : a0) + __shfl_xor_sync(0xffffffffu, s0, 16);
+    const double k1 = (hi16 ? a3 : a1) + __shfl_xor_sync(0xffffffffu, s1, 16);
+    // bit 3 clear keeps the first of the pair
+    double v = (hi8 ? k1 : k0) + __shfl_xor_sync(0xffffffffu, hi8 ? k0 : k1, 8);
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    const int q = (lane >> 3) & 3;  // column of v
+    if ((lane & 7) == 0 && j0 + q < k) part[(size_t)blockIdx.x * kp + j0 + q] = v;
+  }
+  if (!arrive_last(counter, &last)) return;
+  const double f = (fslot >= 0) ? scal[fslot] : 1.0;
+  for (int j = wid; j < k; j += CD_T / 32) {
+    double u = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) u += __ldcg(part + (size_t)b * kp + j);
+    u = warp_sum(u);
+    if (lane == 0) out[j] = (fslot >= 0) ? f * u : u;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// Gram-Schmidt update of column c, one row per thread:
+//   w <- f w - sum_{j<c} X[:, j] coef[j]   (f = scal[fin], or 1 when fin < 0)
+// and scal[fout] = 1/|w| (the last block adds the block partials in order).
+__global__ void __launch_bounds__(RT) k_csub(double *X, int64_t ld, PSrc ps, const double *__restrict__ coef,
+                                             const double *skip, int fin, int fout, int n,
+                                             double *__restrict__ part, unsigned *__restrict__ counter,
+                                             double *scal) {
+  if (skip && *skip != 0.0) return;
+  const IterParams P = ps.get();
+  const int k = P.c;
+  __shared__ double cs[SV_MAX];
+  __shared__ double red[RT / 32];
+  __shared__ bool last;
+  for (int j = threadIdx.x; j < k; j += RT) cs[j] = coef[j];
+  __syncthreads();
+  const int i = blockIdx.x * RT + threadIdx.x;
+  double wn = 0.0;
+  if (i < n) {
+    const double *px = X + i;
+    double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+    int j = 0;
+    for (; j + 3 < k; j += 4) {
+      const size_t o = (size_t)j * ld;
+      t0 = fma(px[o], cs[j], t0);
+      t1 = fma(px[o + ld], cs[j + 1], t1);
+      t2 = fma(px[o + 2 * ld], cs[j + 2], t2);
+      t3 = fma(px[o + 3 * ld], cs[j + 3], t3);
+    }
+    for (; j < k; ++j) t0 = fma(px[(size_t)j * ld], cs[j], t0);
+    const double t = (t0 + t1) + (t2 + t3);
+    double *w = X + (size_t)k * ld + i;
+    const double w0 = (fin >= 0) ? scal[fin] * (*w) : *w;
+    wn = w0 - t;
+    *w = wn;
+  }
+  const double sq = block_sum<RT>(wn * wn, red);
+  if (threadIdx.x == 0) part[blockIdx.x] = sq;
+  if (!arrive_last(counter, &last)) return;
+  double u = 0.0;
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + q);
+  __syncthreads();
+  u = block_sum<RT>(u, red);
+  if (threadIdx.x == 0) {
+    scal[fout] = 1.0 / sqrt(u);
+    *counter = 0u;
+  }
+}
+
+// column c <- scal[fslot] * column c; with xs, also its hi+lo split for the matvec
+__global__ void k_cscale(double *X, int64_t ld, PSrc ps, const double *skip, const double *__restrict__ scal,
+                         int fslot, int n, float2 *__restrict__ xs) {
+  if (skip && *skip != 0.0) return;
+  const IterParams P = ps.get();
+  const double f = scal[fslot];
+  double *w = X + (size_t)P.c * ld;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double v = f * w[i];
+    w[i] = v;
+    if (xs) {
+      const float hv = __double2float_rn(v);
+      xs[i] = make_float2(hv, __double2float_rn(v - (double)hv));
+    }
+  }
+}
+
+// out[:, j] = sum_{q<k} X[:, q] C[q + j k], j < m   (MULTBC)
+// Block = 32 rows x 8 warps; warp w computes output columns w, w+8, ... with
+// up to 8 accumulators each pass; C is read through the read-only cache.
+__global__ void __launch_bounds__(TPB) k_multbc(const double *__restrict__ X, int64_t ld, int k,
+                                                const double *__restrict__ C, int m, double *__restrict__ out, int n) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int i = blockIdx.x * RC + lane;
+  if (i >= n) return;
+  for (int jb = wid; jb < m; jb += NCH * 8) {
+    double acc[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[u] = 0.0;
+    for (int q = 0; q < k; ++q) {
+      const double x = X[(size_t)q * ld + i];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int j = jb + u * NCH;
+        if (j < m) acc[u] = fma(x, __ldg(C + (size_t)j * k + q), acc[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int j = jb + u * NCH;
+      if (j < m) out[(size_t)j * ld + i] = acc[u];
+    }
   }
 }
 
@@ -196,17 +378,36 @@ struct Dvd {
   int n, lim;
   int64_t ld;
   cudaStream_t s;
-  DBuf<double> B, AB, T, diag, part, small, dots;
-  int nrb;
+  DBuf<double> B, AB, T, diag, part, small;
+  DBuf<double> dots;              // [0, lim + 8) dot products, then SC_N pass scalars
+  DBuf<double> dup;               // [0, 8) IterParams, [8, 8 + lim) Ritz coefficients
+  DBuf<unsigned> counters;        // last-block counters, one per kernel kind
+  int nrow = 0;                   // blocks of the row kernels
+  int cd_rows = 0, cd_blocks = 0, kp = 0;  // column-dot layout: rows per block, blocks, partial pitch
   int nmv = 0;
   double mv_ms = 0;
   int mv_count = 0;
-  double t_eig = 0, t_wait = 0;  // host seconds: projected eigenproblem, device-to-host waits
+  double t_eig = 0, t_wait = 0;   // host seconds: projected eigenproblem, device-to-host waits
+  double t_total = 0;             // host seconds in dvdson
   std::vector<cudaEvent_t> evs;   // matvec start/stop pairs, read once at the end
   size_t ev_used = 0;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double *hup = nullptr;          // pinned, layout of dup
+  double *hdown = nullptr;        // pinned, layout of dots
+  cudaGraph_t graph = nullptr;    // single-vector pass (MBLOCK = 1)
+  cudaGraphExec_t gexec = nullptr;
+  cudaEvent_t gev0 = nullptr, gev1 = nullptr;
+  cudaEvent_t pev0 = nullptr, pev1 = nullptr;  // around each single-vector pass
+  double pass_ms = 0;             // device ms of the single-vector passes
+  int graph_kernels = 0;
+  bool use_graph = true;          // GRASP_GPU_DVD_GRAPH=0 launches the same pass kernel by kernel
+
+  double *scal() { return dots.p + lim + 8; }
+  IterParams *dpar() { return reinterpret_cast<IterParams *>(dup.p); }
+  IterParams *hpar() { return reinterpret_cast<IterParams *>(hup); }
+  double *col(DBuf<double> &X, int j) { return X.p + (size_t)j * ld; }
 
   int init(gg_ctx *c, gg_hmat *hm, int prec, int nn, int lm) {
+    static_assert(sizeof(IterParams) <= 8 * sizeof(double), "IterParams slot");
     ctx = c;
     h = hm;
     precision = prec;
@@ -214,26 +415,178 @@ struct Dvd {
     lim = lm;
     s = c->stream;
     ld = ((int64_t)n + 31) / 32 * 32;
-    nrb = (n + RB - 1) / RB;
+    nrow = (n + RT - 1) / RT;
+    // about two column-dot blocks per SM, rows a multiple of 32
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+    cd_rows = (int)std::min<int64_t>(CD_MAXR, std::max<int64_t>(32, ((n + 2 * sms - 1) / (2 * sms) + 31) / 32 * 32));
+    cd_blocks = (n + cd_rows - 1) / cd_rows;
+    kp = lim + 8;
     GG_TRY(B.alloc((size_t)ld * lim));
     GG_TRY(AB.alloc((size_t)ld * lim));
     GG_TRY(T.alloc((size_t)ld * lim));
     GG_TRY(diag.alloc(n));
-    GG_TRY(part.alloc((size_t)std::max(nrb * lim, (n + TPB - 1) / TPB + 1024)));
+    GG_TRY(part.alloc((size_t)std::max(cd_blocks * kp, nrow) + 1024));
     GG_TRY(small.alloc(4096));
-    GG_TRY(dots.alloc(lim + 8));
+    GG_TRY(dots.alloc(lim + 8 + SC_N));
+    GG_TRY(dup.alloc(8 + lim));
+    GG_TRY(counters.alloc(16));
+    GG_CUDA(cudaMemsetAsync(counters.p, 0, 16 * sizeof(unsigned), s));
+    GG_CUDA(cudaMemsetAsync(dots.p, 0, (lim + 8 + SC_N) * sizeof(double), s));
+    GG_CUDA(cudaMallocHost(&hup, (size_t)(8 + lim) * sizeof(double)));
+    GG_CUDA(cudaMallocHost(&hdown, (size_t)(lim + 8 + SC_N) * sizeof(double)));
+    std::memset(hup, 0, (size_t)(8 + lim) * sizeof(double));
     GG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)ld * lim * 8, s));
     GG_CUDA(cudaMemsetAsync(AB.p, 0, (size_t)ld * lim * 8, s));
-    GG_CUDA(cudaEventCreate(&e0));
-    GG_CUDA(cudaEventCreate(&e1));
+    if (precision == GG_SPLIT) GG_TRY(h->dXs.alloc(n));
+    const char *e = std::getenv("GRASP_GPU_DVD_GRAPH");
+    use_graph = !(e && e[0] == '0');
     return GG_OK;
   }
   ~Dvd() {
-    if (e0) cudaEventDestroy(e0);
-    if (e1) cudaEventDestroy(e1);
     for (cudaEvent_t e : evs) cudaEventDestroy(e);
+    if (hup) cudaFreeHost(hup);
+    if (hdown) cudaFreeHost(hdown);
+    if (gexec) cudaGraphExecDestroy(gexec);
+    if (graph) cudaGraphDestroy(graph);
+    if (gev0) cudaEventDestroy(gev0);
+    if (gev1) cudaEventDestroy(gev1);
+    if (pev0) cudaEventDestroy(pev0);
+    if (pev1) cudaEventDestroy(pev1);
   }
-  double *col(DBuf<double> &X, int j) { return X.p + (size_t)j * ld; }
+
+  // ---- kernel launchers (counters: 0 ritz, 1 column dots, 2 csub) ----
+  void launch_ritz(const PSrc &ps) {
+    k_ritz<<<nrow, RT, 0, s>>>(B.p, AB.p, ld, ps, dup.p + 8, n, part.p, counters.p + 0, scal());
+    note_launch();
+  }
+  void launch_dots(bool pre, const PSrc &ps, int kofs, double *W, const double *skip, int fslot) {
+    if (pre)
+      k_cdots<true><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, fslot, n, cd_rows,
+                                               kp, part.p, counters.p + 1, dots.p);
+    else
+      k_cdots<false><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, fslot, n, cd_rows,
+                                                kp, part.p, counters.p + 1, dots.p);
+    note_launch();
+  }
+  void launch_csub(const PSrc &ps, const double *skip, int fin, int fout) {
+    k_csub<<<nrow, RT, 0, s>>>(B.p, ld, ps, dots.p, skip, fin, fout, n, part.p, counters.p + 2, scal());
+    note_launch();
+  }
+  void launch_cscale(const PSrc &ps, const double *skip, int fslot, float2 *xs) {
+    k_cscale<<<std::min((n + TPB - 1) / TPB, 4 * 152), TPB, 0, s>>>(B.p, ld, ps, skip, scal(), fslot, n, xs);
+    note_launch();
+  }
+  // two-pass classical Gram-Schmidt of column ps.c against columns
+  // 0..c-1 with normalisation (mgs_nrm, dvdson.f90:1417-1508); the first
+  // pass optionally applies the preconditioner to the column first. The
+  // normalisation after pass 1 is carried as a factor into pass 2.
+  void cgs2(const PSrc &ps, bool pre, const double *skip, float2 *xs) {
+    launch_dots(pre, ps, 0, B.p, skip, -1);
+    launch_csub(ps, skip, -1, SC_F1);
+    launch_dots(false, ps, 0, B.p, skip, SC_F1);
+    launch_csub(ps, skip, SC_F1, SC_F2);
+    launch_cscale(ps, skip, SC_F2, xs);
+  }
+
+  // One single-vector pass (MBLOCK = 1) for target parameters ps, with the
+  // Ritz coefficients already in dup: Ritz vector and residual; shift,
+  // preconditioner and CGS2 of column c; y = H x; S(0:c, c); results down.
+  // Everything after the Ritz kernel is skipped on the device when the
+  // target has converged.
+  int enqueue_single(const PSrc &ps, const int *dcol, bool in_capture) {
+    const double *skip = scal() + SC_CONV;
+    GG_CUDA(cudaMemcpyAsync(dup.p, hup, (size_t)(8 + lim) * sizeof(double), cudaMemcpyHostToDevice, s));
+    launch_ritz(ps);
+    cgs2(ps, true, skip, precision == GG_SPLIT ? h->dXs.p : nullptr);
+    if (in_capture) {
+      GG_CUDA(cudaEventRecordWithFlags(gev0, s, cudaEventRecordExternal));
+    } else {
+      GG_CUDA(cudaEventRecord(gev0, s));
+    }
+    GG_TRY(spmv_col(h, precision, B.p, AB.p, ld, dcol, skip, s));
+    if (in_capture) {
+      GG_CUDA(cudaEventRecordWithFlags(gev1, s, cudaEventRecordExternal));
+    } else {
+      GG_CUDA(cudaEventRecord(gev1, s));
+    }
+    launch_dots(false, ps, 1, AB.p, skip, -1);
+    GG_CUDA(cudaMemcpyAsync(hdown, dots.p, (size_t)(lim + 8 + SC_N) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    return GG_OK;
+  }
+
+  int build_graph() {
+    if (!gev0) GG_CUDA(cudaEventCreate(&gev0));
+    if (!gev1) GG_CUDA(cudaEventCreate(&gev1));
+    PSrc ps{dpar(), IterParams{}};
+    const int *dcol = reinterpret_cast<const int *>(reinterpret_cast<const char *>(dup.p) + offsetof(IterParams, c));
+    GG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const long long before = gg_launch_count();
+    const int st = enqueue_single(ps, dcol, true);
+    const long long captured = gg_launch_count() - before;
+    note_launches(-captured);  // counted per replay instead
+    cudaGraph_t gcap = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(s, &gcap);
+    if (st != GG_OK) {
+      if (gcap) cudaGraphDestroy(gcap);
+      return st;
+    }
+    if (ce != cudaSuccess) return fail(GG_ERR_CUDA, std::string("Davidson graph capture: ") + cudaGetErrorString(ce));
+    graph = gcap;
+    GG_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
+    graph_kernels = (int)captured;
+    return GG_OK;
+  }
+
+  // One single-vector pass for basis size kpass and the target with Ritz
+  // coefficients svec. Returns |r|; when |r| >= critr the new column kpass of
+  // S is written into S (packed upper).
+  int single_pass(int kpass, const double *svec, double lam, double gap, double dl, double critr, double *res,
+                  std::vector<double> &S) {
+    IterParams &hp = *hpar();
+    hp.c = kpass;
+    hp.k = kpass;
+    hp.lam = lam;
+    hp.gap = gap;
+    hp.dl = dl;
+    hp.critr = critr;
+    std::memcpy(hup + 8, svec, (size_t)kpass * sizeof(double));
+    if (!pev0) GG_CUDA(cudaEventCreate(&pev0));
+    if (!pev1) GG_CUDA(cudaEventCreate(&pev1));
+    GG_CUDA(cudaEventRecord(pev0, s));
+    if (use_graph) {
+      if (!gexec) GG_TRY(build_graph());
+      GG_CUDA(cudaGraphLaunch(gexec, s));
+      note_launches(graph_kernels);
+    } else {
+      if (!gev0) GG_CUDA(cudaEventCreate(&gev0));
+      if (!gev1) GG_CUDA(cudaEventCreate(&gev1));
+      PSrc ps{nullptr, hp};
+      const int *dcol = reinterpret_cast<const int *>(reinterpret_cast<const char *>(dup.p) + offsetof(IterParams, c));
+      GG_TRY(enqueue_single(ps, dcol, false));
+    }
+    GG_CUDA(cudaEventRecord(pev1, s));
+    const auto t0 = std::chrono::steady_clock::now();
+    GG_CUDA(cudaStreamSynchronize(s));
+    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    {
+      float pms = 0.f;
+      GG_CUDA(cudaEventElapsedTime(&pms, pev0, pev1));
+      pass_ms += pms;
+    }
+    const double *sc = hdown + lim + 8;
+    *res = std::sqrt(sc[SC_RN2]);
+    if (sc[SC_CONV] == 0.0) {
+      const size_t off = (size_t)kpass * (kpass + 1) / 2;
+      std::memcpy(S.data() + off, hdown, (size_t)(kpass + 1) * sizeof(double));
+      float ms = 0.f;
+      GG_CUDA(cudaEventElapsedTime(&ms, gev0, gev1));
+      mv_ms += ms;
+      ++mv_count;
+      ++nmv;
+    }
+    return GG_OK;
+  }
 
   // OP (gdvd.f90:137-142): AB[:, j0:j0+m) = H BASIS[:, j0:j0+m); each launch
   // is bracketed by events that are read after the solve (no extra sync)
@@ -265,52 +618,69 @@ struct Dvd {
     ev_used = 0;
     return GG_OK;
   }
-  // out[0:k] = BASIS[:, 0:k]^T w  (device)
-  int dots_dev(const DBuf<double> &X, int k, const double *w, double *out) {
-    if (k <= 0) return GG_OK;
-    dim3 g(nrb, (k + CG - 1) / CG);
-    k_dots_part<<<g, TPB, 0, s>>>(X.p, ld, k, w, n, part.p); ::gg::note_launch();
-    k_dots_reduce<<<(k + 127) / 128, 128, 0, s>>>(part.p, nrb, k, out); ::gg::note_launch();
+  static PSrc by_value(int c, int k = 0, double lam = 0, double gap = 0, double dl = 0, double critr = 0) {
+    IterParams p{};
+    p.c = c;
+    p.k = k;
+    p.lam = lam;
+    p.gap = gap;
+    p.dl = dl;
+    p.critr = critr;
+    return PSrc{nullptr, p};
+  }
+  // column j orthonormalised against columns 0..j-1
+  int orthonormalize(int j) {
+    const PSrc ps = by_value(j);
+    if (j > 0) {
+      cgs2(ps, false, nullptr, nullptr);
+    } else {
+      launch_csub(ps, nullptr, -1, SC_F2);
+      launch_cscale(ps, nullptr, SC_F2, nullptr);
+    }
     GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
-  // two-pass classical Gram-Schmidt of column j against columns 0..j-1,
-  // normalised after each pass (mgs_nrm, dvdson.f90:1417-1508)
-  int orthonormalize(int j) {
-    double *w = col(B, j);
-    const int nb = std::min((n + TPB - 1) / TPB, 1024);
-    for (int pass = 0; pass < 2; ++pass) {
-      if (j > 0) {
-        GG_TRY(dots_dev(B, j, w, dots.p));
-        k_sub_gemv<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(w, B.p, ld, j, dots.p, n); ::gg::note_launch();
-      }
-      k_sq_part<<<nb, TPB, 0, s>>>(w, n, part.p); ::gg::note_launch();
-      k_normalize<<<nb, TPB, 0, s>>>(w, n, part.p, nb); ::gg::note_launch();
-      GG_CUDA(cudaGetLastError());
-    }
-    return GG_OK;
-  }
-  // S(1:kp+1, kp+1) for new column kp (0-based) of AB, into host Sp (packed upper)
-  int adds(int kp, std::vector<double> &S) {
-    GG_TRY(dots_dev(B, kp + 1, col(AB, kp), dots.p));
-    std::vector<double> hcol(kp + 1);
-    GG_CUDA(cudaMemcpyAsync(hcol.data(), dots.p, (kp + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+  // S(1:kp+1, kp+1) for new column kp (0-based) of AB, into host S (packed upper)
+  int adds(int kp_, std::vector<double> &S) {
+    launch_dots(false, by_value(kp_), 1, AB.p, nullptr, -1);
+    GG_CUDA(cudaGetLastError());
+    const size_t off = (size_t)kp_ * (kp_ + 1) / 2;
+    GG_CUDA(cudaMemcpyAsync(hdown, dots.p, (kp_ + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
     const auto t0 = std::chrono::steady_clock::now();
     GG_CUDA(cudaStreamSynchronize(s));
     t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    const size_t off = (size_t)kp * (kp + 1) / 2;
-    for (int i = 0; i <= kp; ++i) S[off + i] = hcol[i];
+    std::memcpy(S.data() + off, hdown, (kp_ + 1) * sizeof(double));
     return GG_OK;
   }
-  // X[:, 0:m) = X[:, 0:k) C (k x m)
+  // X[:, 0:m) = X[:, 0:k) C (k x m): computed into T, copied back (BASIS and
+  // AB keep their addresses, which the iteration graph holds)
   int multbc(DBuf<double> &X, int k, int m, const double *hC) {
     if ((size_t)k * m > small.n) GG_TRY(small.alloc((size_t)k * m));
     GG_CUDA(cudaMemcpyAsync(small.p, hC, (size_t)k * m * sizeof(double), cudaMemcpyHostToDevice, s));
-    const size_t sm = (size_t)k * m * sizeof(double);
-    if (sm > 48 * 1024) GG_CUDA(cudaFuncSetAttribute(k_multbc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_multbc<<<(n + TPB - 1) / TPB, TPB, sm, s>>>(X.p, ld, k, small.p, m, T.p, n); ::gg::note_launch();
+    k_multbc<<<(n + RC - 1) / RC, TPB, 0, s>>>(X.p, ld, k, small.p, m, T.p, n);
+    note_launch();
     GG_CUDA(cudaGetLastError());
-    GG_CUDA(cudaMemcpy2DAsync(X.p, ld * 8, T.p, ld * 8, (size_t)n * 8, m, cudaMemcpyDeviceToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(X.p, T.p, (size_t)m * ld * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return GG_OK;
+  }
+  // Block pass (MBLOCK > 1): Ritz vector and residual of one target into
+  // column c; returns |r| (the preconditioner follows when not converged)
+  int ritz(int k, const double *hsvec, double lam, double gap, double dl, double critr, int c, double *res) {
+    std::memcpy(hup + 8, hsvec, k * sizeof(double));
+    GG_CUDA(cudaMemcpyAsync(dup.p + 8, hup + 8, k * sizeof(double), cudaMemcpyHostToDevice, s));
+    launch_ritz(by_value(c, k, lam, gap, dl, critr));
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(hdown + lim + 8, scal(), SC_N * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const auto t0 = std::chrono::steady_clock::now();
+    GG_CUDA(cudaStreamSynchronize(s));
+    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    *res = std::sqrt(hdown[lim + 8 + SC_RN2]);
+    return GG_OK;
+  }
+  int precond(int c, double lam) {
+    k_precond<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(B.p, AB.p, ld, by_value(c, 0, lam), scal(), diag.p, n);
+    note_launch();
+    GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
   double host_sum_sqrt(int np) {
@@ -339,6 +709,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   const int n = D.n, LIM = P.lim, NUME = P.nume, MBLOCK = P.mblock, MAXITER = P.maxiter;
   int NIV = P.niv;
   int IERR = 0;
+  const auto t_begin = std::chrono::steady_clock::now();
   if (LIM > n) IERR += 1;
   if (LIM <= 0) IERR += 2;
   if (NUME > LIM || (NUME == LIM && NUME != n)) IERR += 128;
@@ -384,7 +755,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   int REST = std::max(LIM / 2, 2 * NUME);
   REST = std::min(REST, LIM - 3);
   bool DONE = false;
-  std::vector<double> tmpS, w, z;
+  std::vector<double> w;
   for (;;) {
     const int IFIND = std::min(KPASS, REST);
     for (int i = 0; i < IFIND; ++i) OLDVAL[i] = EIGVAL[i];
@@ -455,20 +826,33 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
     }
     // NEWVEC (dvdson.f90:1002-1172)
     int nadded = 0, icvc = 0;
-    double lam_added = 0.0, rhseps_added = 0.0;
-    {
-      const int limadd = std::min(LIM, MBLOCK + KPASS);
+    // GAP and DL of target indx (dvdson.f90:1128-1138). On the first pass
+    // OLDVAL still holds DVDRVR's 1e30 sentinel (dvdson.f90:703): the
+    // reference then shifts by RHSEPS ~ 1e13 and its first correction vector
+    // carries no new direction, after which the coefficient test (CRITC) can
+    // end the iteration early. robust = 1 uses DL = 0 on that pass instead.
+    auto gap_dl = [&](int indx, double *gap, double *dl) {
+      if (indx == 1) {
+        *gap = std::fabs(EIGVAL[1] - EIGVAL[0]);
+      } else {
+        const double gaplow = std::fabs(EIGVAL[indx - 1] - EIGVAL[indx - 2]);
+        const double gapup = std::fabs(EIGVAL[indx] - EIGVAL[indx - 1]);
+        *gap = std::min(gaplow, gapup);
+      }
+      *dl = std::fabs(OLDVAL[indx - 1] - EIGVAL[indx - 1]);
+      if (P.robust && OLDVAL[indx - 1] >= 1.0e29) *dl = 0.0;
+    };
+    if (MBLOCK == 1) {
+      // one device pass per target: Ritz vector, shift, preconditioner,
+      // Gram-Schmidt, OP and ADDS of column KPASS; a converged target's pass
+      // stops after the residual and the next target takes the column
       DONE = false;
       for (int i = 1; i <= NNCV; ++i) {
         const int indx = INCV[i];
-        GG_CUDA(cudaMemcpyAsync(D.small.p, SVEC.data() + (size_t)(indx - 1) * KPASS, KPASS * sizeof(double),
-                                cudaMemcpyHostToDevice, D.s));
-        const int nb = (n + TPB - 1) / TPB;
-        // ICUR = column KPASS + NADDED (a converged target is overwritten)
-        k_ritz<<<nb, TPB, 0, D.s>>>(D.B.p, D.AB.p, D.ld, KPASS, D.small.p, EIGVAL[indx - 1],
-                                    D.col(D.B, KPASS + nadded), D.col(D.AB, KPASS + nadded), n, D.part.p); ::gg::note_launch();
-        GG_CUDA(cudaGetLastError());
-        const double res = D.host_sum_sqrt(nb);
+        double gap, dl, res = 0.0;
+        gap_dl(indx, &gap, &dl);
+        GG_TRY(D.single_pass(KPASS, SVEC.data() + (size_t)(indx - 1) * KPASS, EIGVAL[indx - 1], gap, dl, P.critr,
+                             &res, S));
         SCRA1[indx - 1] = res;
         if (res < P.critr) {
           ++icvc;
@@ -477,31 +861,42 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
           DONE = true;
           break;
         }
-        double gap;
-        if (indx == 1) {
-          gap = std::fabs(EIGVAL[1] - EIGVAL[0]);
-        } else {
-          const double gaplow = std::fabs(EIGVAL[indx - 1] - EIGVAL[indx - 2]);
-          const double gapup = std::fabs(EIGVAL[indx] - EIGVAL[indx - 1]);
-          gap = std::min(gaplow, gapup);
+        nadded = 1;
+        INCV[1] = indx;
+        break;
+      }
+      if (DONE) break;
+      NNCV = nadded;
+      KPASS += NNCV;
+      ++NLOOPS;
+      if (NLOOPS <= MAXITER) continue;
+      IERR += 2048;
+      --NLOOPS;
+      KPASS -= NNCV;
+      break;
+    }
+    {
+      const int limadd = std::min(LIM, MBLOCK + KPASS);
+      DONE = false;
+      for (int i = 1; i <= NNCV; ++i) {
+        const int indx = INCV[i];
+        // ICUR = column KPASS + NADDED (a converged target is overwritten)
+        double gap, dl, res = 0.0;
+        gap_dl(indx, &gap, &dl);
+        const int c = KPASS + nadded;
+        GG_TRY(D.ritz(KPASS, SVEC.data() + (size_t)(indx - 1) * KPASS, EIGVAL[indx - 1], gap, dl, P.critr, c, &res));
+        SCRA1[indx - 1] = res;
+        if (res < P.critr) {
+          ++icvc;
+          ICV[indx] = 1;
+          if (icvc < NNCV) continue;
+          DONE = true;
+          break;
         }
-        double dl = std::fabs(OLDVAL[indx - 1] - EIGVAL[indx - 1]);
-        // On the first pass OLDVAL still holds DVDRVR's 1e30 sentinel
-        // (dvdson.f90:703): the reference then shifts by RHSEPS ~ 1e13 and its
-        // first correction vector carries no new direction, after which the
-        // coefficient test (CRITC) can end the iteration early. robust = 1
-        // uses DL = 0 on that pass instead.
-        if (P.robust && OLDVAL[indx - 1] >= 1.0e29) dl = 0.0;
-        const double rhseps = (gap > res) ? std::sqrt(dl * res) : std::min(dl, std::sqrt(dl));
         ++nadded;
         INCV[nadded] = indx;
-        lam_added = EIGVAL[indx - 1];
-        rhseps_added = rhseps;
         // shift + preconditioner for this column now (MBLOCK columns at most)
-        k_precond<<<(n + TPB - 1) / TPB, TPB, 0, D.s>>>(D.col(D.AB, KPASS + nadded - 1), D.col(D.B, KPASS + nadded - 1),
-                                                        rhseps_added, lam_added, D.diag.p, D.col(D.B, KPASS + nadded - 1),
-                                                        n); ::gg::note_launch();
-        GG_CUDA(cudaGetLastError());
+        GG_TRY(D.precond(c, EIGVAL[indx - 1]));
         if (nadded + KPASS == limadd) break;
       }
       if (DONE) break;
@@ -533,6 +928,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   eigval_out.assign(EIGVAL.begin(), EIGVAL.begin() + NUME);
   *nloops_out = NLOOPS;
   *ierr_out = IERR;
+  D.t_total += std::chrono::duration<double>(std::chrono::steady_clock::now() - t_begin).count();
   return D.collect_matvec_time();
 }
 
@@ -675,8 +1071,8 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     nmv_total += D1.nmv;
     nl_total += nl;
     *ierr = ie;
-    ctx->stats[8] = nl;      // stage-1 (leading block) loops
-    ctx->stats[9] = 0;       // stage-2 loops
+    ctx->stats[8] = nl;  // stage-1 (leading block) loops
+    ctx->stats[9] = 0;   // stage-2 loops
     ctx->stats[10] = D1.mv_ms;
   }
   Dvd *Dout = &D1;
@@ -700,7 +1096,6 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     ctx->stats[12] = D2.mv_count;
   }
   for (int j = 0; j < nvec; ++j) eval[j] = ev[j];
-  std::vector<double> hv;
   if (evec) {
     GG_CUDA(cudaMemcpy2DAsync(evec, (size_t)ncf * 8, Dout->B.p, Dout->ld * 8, (size_t)ncf * 8, nvec,
                               cudaMemcpyDeviceToHost, ctx->stream));
@@ -727,6 +1122,11 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   ctx->stats[5] = mv_count;
   ctx->stats[13] = 1e3 * (D1.t_eig + D2.t_eig);    // host projected eigenproblem ms
   ctx->stats[14] = 1e3 * (D1.t_wait + D2.t_wait);  // host waits on device results ms
+  ctx->stats[15] = 1e3 * (D1.t_total + D2.t_total);  // host ms inside the two Davidson runs
+  ctx->stats[16] = D2.pass_ms;
+  ctx->stats[17] = 1e3 * D1.t_total;
+  ctx->stats[18] = 1e3 * D2.t_total;
+  ctx->stats[19] = 1e3 * D2.t_eig;
   *nloops = nl_total;
   *nmv = nmv_total;
   if (*ierr & 2048) return fail(GG_ERR_CONVERGE, "DVDSON: maximum number of iterations reached (IERR 2048)");

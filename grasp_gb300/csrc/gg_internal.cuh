@@ -14,6 +14,8 @@ void set_error(const std::string &msg);
 int fail(int status, const std::string &msg);
 // counts this library's kernel launches (reported by gg_launch_count)
 void note_launch();
+// adds m (possibly negative: launches recorded while a graph was captured)
+void note_launches(long long m);
 
 #define GG_CUDA(call)                                                                   \
   do {                                                                                  \
@@ -118,7 +120,7 @@ struct gg_ctx {
   gg::RkTable rk;
   gg::DBuf<double> dIab;                // [nw * nw]
   bool iab_valid = false;
-  double stats[16] = {};
+  double stats[24] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t marks[8] = {};  // gg_event_record slots
 };
@@ -158,6 +160,8 @@ int timer_stop(gg_ctx *ctx, double *ms);
 int build_sym(gg_hmat *h);
 int refresh_sym_values(gg_hmat *h);
 int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s);
+int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
+             const double *skip, cudaStream_t s);
 double spmv_bytes(const gg_hmat *h, int precision, int m);
 // hosteig.cpp: lowest m eigenvalues of a packed-upper symmetric matrix and
 // the eigenvectors of the lowest mvec <= m of them

@@ -208,7 +208,75 @@ __global__ void __launch_bounds__(256) k_spmv_split(const int64_t *__restrict__ 
   if (lane == 0) y[row] = ((double)acc.h + (double)acc.l) + diag[row] * x[row];
 }
 
+// Column-indexed forms for the Davidson iteration graph: x = Bbase + c ld,
+// y = ABbase + c ld with c read from device memory at run time; nothing is
+// done when skip points to a non-zero flag. The split form reads x from its
+// hi+lo copy, which the caller prepared.
+__global__ void __launch_bounds__(256) k_spmv64_col(const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                                    const double *__restrict__ val, const double *__restrict__ Bbase,
+                                                    double *__restrict__ ABbase, int64_t ld,
+                                                    const int *__restrict__ pc, const double *skip, int n) {
+  if (skip && *skip != 0.0) return;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const size_t off = (size_t)(*pc) * ld;
+  const double *x = Bbase + off;
+  const int64_t lo = ptr[row], hi = ptr[row + 1];
+  double acc = 0.0;
+  for (int64_t p = lo + lane; p < hi; p += 32) acc = fma(__ldg(val + p), x[__ldg(col + p)], acc);
+  acc = warp_sum(acc);
+  if (lane == 0) ABbase[off + row] = acc;
+}
+
+__global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+                                                        const float *__restrict__ hi, const float *__restrict__ lo,
+                                                        const float2 *__restrict__ xs, const double *__restrict__ diag,
+                                                        const double *__restrict__ Bbase, double *__restrict__ ABbase,
+                                                        int64_t ld, const int *__restrict__ pc, const double *skip,
+                                                        int n) {
+  if (skip && *skip != 0.0) return;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const size_t off = (size_t)(*pc) * ld;
+  const int64_t p0 = ptr[row], p1 = ptr[row + 1];
+  df acc = {0.f, 0.f};
+  for (int64_t p = p0 + lane; p < p1; p += 32) {
+    const float ah = __ldg(hi + p), al = __ldg(lo + p);
+    const float2 xv = xs[__ldg(col + p)];
+    const float ph = ah * xv.x;
+    const float pe = fmaf(ah, xv.x, -ph);
+    const float cross = fmaf(ah, xv.y, fmaf(al, xv.x, pe));
+    acc = df_add(acc, two_sum(ph, cross));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    df other;
+    other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
+    other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
+    acc = df_add(acc, other);
+  }
+  if (lane == 0) ABbase[off + row] = ((double)acc.h + (double)acc.l) + diag[row] * Bbase[off + row];
+}
+
 }  // namespace
+
+// y = H x with x = Bbase + c ld, y = ABbase + c ld, c = *dcol on the device;
+// GG_SPLIT reads x from h->dXs (the caller's split copy of the same column)
+int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
+             const double *skip, cudaStream_t s) {
+  const int n = h->ncf;
+  const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
+  if (precision == GG_SPLIT) {
+    if (h->dXs.n < (size_t)n) return fail(GG_ERR_STATE, "spmv_col: split copy of x not allocated");
+    k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
+                                            h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n); ::gg::note_launch();
+  } else {
+    k_spmv64_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, Bbase, ABbase, ld, dcol, skip, n);
+    ::gg::note_launch();
+  }
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
 
 int build_sym(gg_hmat *h) {
   if (h->sym_valid) return GG_OK;

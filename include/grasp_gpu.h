@@ -192,7 +192,10 @@ int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double 
  * 6 bytes moved by one matvec (algorithmic), 7 setham upload,
  * 8 / 9 Davidson loops of the leading-block (INIEST2) / full-block stage,
  * 10 / 11 their matvec ms, 12 full-block matvec launches, 13 host ms in the
- * projected eigenproblems, 14 host ms waiting for device results.          */
+ * projected eigenproblems, 14 host ms waiting for device results, 15 host ms
+ * inside both Davidson runs, 16 device ms of the full-block single-vector
+ * passes, 17 / 18 host ms of the leading-block / full-block Davidson run,
+ * 19 host ms of the full-block projected eigenproblems.                    */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* ---- measurement helpers (no counterpart in the reference) ------------------

@@ -126,3 +126,32 @@ def test_maneig_davidson_path(gpu_ready, oracle_mod):
             assert info0["ierr"] == 0 and info["ierr"] == 0
             assert np.abs(ev - ev0).max() <= 1e-9, (robust, precision, ev, ev0)
             assert np.abs(vec - vec0).max() <= 1e-7, (robust, precision, np.abs(vec - vec0).max())
+
+
+def test_maneig_graph_pass_matches_launch_path(gpu_ready, monkeypatch):
+    """The single-vector pass replayed as a CUDA graph and the same pass
+    launched kernel by kernel do the same arithmetic in the same order."""
+    from grasp_gb300 import Context, HMatrix
+    from grasp_gb300 import synth as S
+    orbs = S.orbital_set(6, 3)
+    case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
+    occ = lambda d: S.occupation(orbs, d)  # noqa: E731
+    refs = [occ({(1, -1): 2, (2, -1): 2}), occ({(1, -1): 2, (2, 1): 2}), occ({(1, -1): 2, (2, -2): 2})]
+    blk = S.ci_block(orbs, refs, [0] * len(orbs), two_j=2, parity=0, density=0.05, seed=9)
+    ctx = Context(0)
+    ctx.set_grid(case["n"], case["rnt"], case["h"], case["c"], case["zz"])
+    ob = case["orb"]
+    ctx.set_orbitals(ob.nak, ob.mf, ob.pf, ob.qf)
+    ctx.genintrk()
+    ctx.iabint_table()
+    H = HMatrix(ctx, blk.ncf, blk.iendc, blk.irow)
+    H.setham(blk.iq, blk.tlist, blk.vlists)
+    for precision in (0, 1):
+        for robust in (False, True):
+            monkeypatch.setenv("GRASP_GPU_DVD_GRAPH", "0")
+            ev0, vec0, info0 = H.maneig(3, flavour=0, precision=precision, robust=robust)
+            monkeypatch.setenv("GRASP_GPU_DVD_GRAPH", "1")
+            ev, vec, info = H.maneig(3, flavour=0, precision=precision, robust=robust)
+            assert info["nloops"] == info0["nloops"]
+            assert np.array_equal(ev, ev0), (ev, ev0)
+            assert np.array_equal(vec, vec0)
