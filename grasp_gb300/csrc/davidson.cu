@@ -308,6 +308,91 @@ __global__ void __launch_bounds__(RT) k_csub(double *X, int64_t ld, PSrc ps, con
   }
 }
 
+// ---------------------------------------------------------------------------
+// Block passes (MBLOCK > 1): the Ritz vectors and residuals of all targets
+// in one sweep over BASIS and AB, then the shifts and preconditioners of the
+// targets NEWVEC keeps, in NEWVEC's order.
+// ---------------------------------------------------------------------------
+constexpr int MT_MAX = 16;     // targets per sweep
+constexpr int MT_SMEM = 4096;  // doubles of Ritz coefficients held in shared memory
+
+// For targets t < nt: b_t = BASIS s_t -> T(:, 2t), r_t = AB s_t - lambda_t b_t
+// -> T(:, 2t + 1), rn2[t] = |r_t|^2 (block partials added in order by the
+// last block). s_t = S + t k.
+__global__ void __launch_bounds__(RT) k_ritz_multi(const double *__restrict__ B, const double *__restrict__ AB,
+                                                   int64_t ld, int k, int nt, const double *__restrict__ S,
+                                                   const double *__restrict__ lam, double *__restrict__ T, int n,
+                                                   double *__restrict__ part, unsigned *__restrict__ counter,
+                                                   double *__restrict__ rn2) {
+  __shared__ double sv[MT_SMEM];
+  __shared__ double red[RT / 32];
+  __shared__ bool last;
+  for (int q = threadIdx.x; q < nt * k; q += RT) sv[q] = S[q];
+  __syncthreads();
+  const int i = blockIdx.x * RT + threadIdx.x;
+  double bacc[MT_MAX], aacc[MT_MAX];
+#pragma unroll
+  for (int t = 0; t < MT_MAX; ++t) bacc[t] = aacc[t] = 0.0;
+  if (i < n) {
+    for (int j = 0; j < k; ++j) {
+      const double bj = B[(size_t)j * ld + i], aj = AB[(size_t)j * ld + i];
+#pragma unroll
+      for (int t = 0; t < MT_MAX; ++t)
+        if (t < nt) {
+          bacc[t] = fma(bj, sv[t * k + j], bacc[t]);
+          aacc[t] = fma(aj, sv[t * k + j], aacc[t]);
+        }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < MT_MAX; ++t) {
+    if (t >= nt) break;
+    double r = 0.0;
+    if (i < n) {
+      r = fma(-lam[t], bacc[t], aacc[t]);
+      T[(size_t)(2 * t) * ld + i] = bacc[t];
+      T[(size_t)(2 * t + 1) * ld + i] = r;
+    }
+    const double sq = block_sum<RT>(r * r, red);
+    if (threadIdx.x == 0) part[(size_t)t * gridDim.x + blockIdx.x] = sq;
+    __syncthreads();
+  }
+  if (!arrive_last(counter, &last)) return;
+  for (int t = 0; t < nt; ++t) {
+    double u = 0.0;
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + (size_t)t * gridDim.x + q);
+    u = block_sum<RT>(u, red);
+    if (threadIdx.x == 0) rn2[t] = u;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+struct PrecList {
+  int m;
+  int col[MT_MAX];      // BASIS column of the new vector
+  int t[MT_MAX];        // its target (columns 2t, 2t+1 of T)
+  double lam[MT_MAX];   // EIGVAL(INDX)
+  double rhs[MT_MAX];   // RHSEPS
+};
+
+// shifts and GDVD preconditioners (gdvd.f90:114-129) of the kept targets in
+// NEWVEC's order, DIAG updated after each as in the reference
+__global__ void k_precond_multi(double *__restrict__ B, const double *__restrict__ T, int64_t ld, PrecList L,
+                                double *__restrict__ diag, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double dg = diag[i];
+  for (int q = 0; q < L.m; ++q) {
+    const double b = T[(size_t)(2 * L.t[q]) * ld + i], r = T[(size_t)(2 * L.t[q] + 1) * ld + i];
+    const double rr = fma(-L.rhs[q], b, r);
+    const double d = dg - L.lam[q];
+    B[(size_t)L.col[q] * ld + i] = (fabs(d) > 1.0e-06) ? rr / d : rr * 1.0e06;
+    dg = d + L.lam[q];
+  }
+  diag[i] = dg;
+}
+
 // column c <- scal[fslot] * column c; with xs, also its hi+lo split for the matvec
 __global__ void k_cscale(double *X, int64_t ld, PSrc ps, const double *skip, const double *__restrict__ scal,
                          int fslot, int n, float2 *__restrict__ xs) {
@@ -393,6 +478,10 @@ struct Dvd {
   size_t ev_used = 0;
   double *hup = nullptr;          // pinned, layout of dup
   double *hdown = nullptr;        // pinned, layout of dots
+  DBuf<double> dS;                // staging of new columns of S (packed upper, like S)
+  double *hS = nullptr;           // pinned, layout of dS
+  DBuf<double> dmt;               // block pass: [MT_MAX lim] coefficients, [MT_MAX] lambda, [MT_MAX] |r|^2
+  double *hmt = nullptr;          // pinned, layout of dmt
   cudaGraph_t graph = nullptr;    // single-vector pass (MBLOCK = 1)
   cudaGraphExec_t gexec = nullptr;
   cudaEvent_t gev0 = nullptr, gev1 = nullptr;
@@ -426,7 +515,11 @@ struct Dvd {
     GG_TRY(AB.alloc((size_t)ld * lim));
     GG_TRY(T.alloc((size_t)ld * lim));
     GG_TRY(diag.alloc(n));
-    GG_TRY(part.alloc((size_t)std::max(cd_blocks * kp, nrow) + 1024));
+    GG_TRY(part.alloc((size_t)std::max(cd_blocks * kp, nrow * MT_MAX) + 1024));
+    GG_TRY(dS.alloc((size_t)lim * (lim + 1) / 2));
+    GG_TRY(dmt.alloc((size_t)MT_MAX * lim + 2 * MT_MAX));
+    GG_CUDA(cudaMallocHost(&hS, (size_t)lim * (lim + 1) / 2 * sizeof(double)));
+    GG_CUDA(cudaMallocHost(&hmt, ((size_t)MT_MAX * lim + 2 * MT_MAX) * sizeof(double)));
     GG_TRY(small.alloc(4096));
     GG_TRY(dots.alloc(lim + 8 + SC_N));
     GG_TRY(dup.alloc(8 + lim));
@@ -447,6 +540,8 @@ struct Dvd {
     for (cudaEvent_t e : evs) cudaEventDestroy(e);
     if (hup) cudaFreeHost(hup);
     if (hdown) cudaFreeHost(hdown);
+    if (hS) cudaFreeHost(hS);
+    if (hmt) cudaFreeHost(hmt);
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     if (gev0) cudaEventDestroy(gev0);
@@ -460,13 +555,15 @@ struct Dvd {
     k_ritz<<<nrow, RT, 0, s>>>(B.p, AB.p, ld, ps, dup.p + 8, n, part.p, counters.p + 0, scal());
     note_launch();
   }
-  void launch_dots(bool pre, const PSrc &ps, int kofs, double *W, const double *skip, int fslot) {
+  void launch_dots(bool pre, const PSrc &ps, int kofs, double *W, const double *skip, int fslot,
+                   double *out = nullptr) {
+    if (!out) out = dots.p;
     if (pre)
       k_cdots<true><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, fslot, n, cd_rows,
-                                               kp, part.p, counters.p + 1, dots.p);
+                                               kp, part.p, counters.p + 1, out);
     else
       k_cdots<false><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, fslot, n, cd_rows,
-                                                kp, part.p, counters.p + 1, dots.p);
+                                                kp, part.p, counters.p + 1, out);
     note_launch();
   }
   void launch_csub(const PSrc &ps, const double *skip, int fin, int fout) {
@@ -640,16 +737,48 @@ struct Dvd {
     GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
-  // S(1:kp+1, kp+1) for new column kp (0-based) of AB, into host S (packed upper)
-  int adds(int kp_, std::vector<double> &S) {
-    launch_dots(false, by_value(kp_), 1, AB.p, nullptr, -1);
+  // ADDS (dvdson.f90:960-1000): S(1:kp+1, kp+1) for the new columns
+  // kp0..kp0+m-1 of AB, staged at their packed offsets and read back with
+  // one copy into host S (packed upper)
+  int adds(int kp0, int m, std::vector<double> &S) {
+    for (int v = 0; v < m; ++v) {
+      const int kp_ = kp0 + v;
+      launch_dots(false, by_value(kp_), 1, AB.p, nullptr, -1, dS.p + (size_t)kp_ * (kp_ + 1) / 2);
+    }
     GG_CUDA(cudaGetLastError());
-    const size_t off = (size_t)kp_ * (kp_ + 1) / 2;
-    GG_CUDA(cudaMemcpyAsync(hdown, dots.p, (kp_ + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const size_t o0 = (size_t)kp0 * (kp0 + 1) / 2, o1 = (size_t)(kp0 + m) * (kp0 + m + 1) / 2;
+    GG_CUDA(cudaMemcpyAsync(hS + o0, dS.p + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, s));
     const auto t0 = std::chrono::steady_clock::now();
     GG_CUDA(cudaStreamSynchronize(s));
     t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    std::memcpy(S.data() + off, hdown, (kp_ + 1) * sizeof(double));
+    std::memcpy(S.data() + o0, hS + o0, (o1 - o0) * sizeof(double));
+    return GG_OK;
+  }
+  // Block pass: Ritz vectors and residual norms of nt targets (coefficient
+  // vectors svec[t], length k; eigenvalues lam[t]) in one sweep; rn2[t] = |r_t|^2
+  bool ritz_multi_fits(int k, int nt) const { return nt <= MT_MAX && nt * k <= MT_SMEM && 2 * nt <= lim; }
+  int ritz_multi(int k, int nt, const double *const *svec, const double *lam, double *rn2) {
+    for (int t = 0; t < nt; ++t) std::memcpy(hmt + (size_t)t * k, svec[t], k * sizeof(double));
+    double *hl = hmt + (size_t)MT_MAX * lim;
+    for (int t = 0; t < nt; ++t) hl[t] = lam[t];
+    GG_CUDA(cudaMemcpyAsync(dmt.p, hmt, (size_t)nt * k * sizeof(double), cudaMemcpyHostToDevice, s));
+    GG_CUDA(cudaMemcpyAsync(dmt.p + (size_t)MT_MAX * lim, hl, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
+    k_ritz_multi<<<nrow, RT, 0, s>>>(B.p, AB.p, ld, k, nt, dmt.p, dmt.p + (size_t)MT_MAX * lim, T.p, n, part.p,
+                                     counters.p + 3, drn);
+    note_launch();
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(hl + MT_MAX, drn, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const auto t0 = std::chrono::steady_clock::now();
+    GG_CUDA(cudaStreamSynchronize(s));
+    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int t = 0; t < nt; ++t) rn2[t] = hl[MT_MAX + t];
+    return GG_OK;
+  }
+  int precond_multi(const PrecList &L) {
+    k_precond_multi<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(B.p, T.p, ld, L, diag.p, n);
+    note_launch();
+    GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
   // X[:, 0:m) = X[:, 0:k) C (k x m): computed into T, copied back (BASIS and
@@ -744,7 +873,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
       break;
     }
     NIV = IEND;
-    for (int j = 0; j < NIV; ++j) GG_TRY(D.adds(j, S));
+    GG_TRY(D.adds(0, NIV, S));
   }
   int NLOOPS = 1;
   for (int i = 0; i < NUME; ++i) {
@@ -875,7 +1004,46 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
       KPASS -= NNCV;
       break;
     }
-    {
+    if (D.ritz_multi_fits(KPASS, NNCV)) {
+      // every candidate target's Ritz vector and residual in one sweep;
+      // NEWVEC's sequential decisions then run on the residual norms
+      const int limadd = std::min(LIM, MBLOCK + KPASS);
+      std::vector<int> tl(INCV.begin() + 1, INCV.begin() + 1 + NNCV);
+      std::vector<const double *> sv(NNCV);
+      std::vector<double> lam(NNCV), rn2(NNCV);
+      for (int t = 0; t < NNCV; ++t) {
+        sv[t] = SVEC.data() + (size_t)(tl[t] - 1) * KPASS;
+        lam[t] = EIGVAL[tl[t] - 1];
+      }
+      GG_TRY(D.ritz_multi(KPASS, NNCV, sv.data(), lam.data(), rn2.data()));
+      PrecList L{};
+      DONE = false;
+      for (int i = 1; i <= NNCV; ++i) {
+        const int indx = tl[i - 1];
+        double gap, dl;
+        gap_dl(indx, &gap, &dl);
+        const double res = std::sqrt(rn2[i - 1]);
+        SCRA1[indx - 1] = res;
+        if (res < P.critr) {
+          ++icvc;
+          ICV[indx] = 1;
+          if (icvc < NNCV) continue;
+          DONE = true;
+          break;
+        }
+        ++nadded;
+        INCV[nadded] = indx;
+        L.col[L.m] = KPASS + nadded - 1;
+        L.t[L.m] = i - 1;
+        L.lam[L.m] = EIGVAL[indx - 1];
+        L.rhs[L.m] = (gap > res) ? std::sqrt(dl * res) : std::min(dl, std::sqrt(dl));
+        ++L.m;
+        if (nadded + KPASS == limadd) break;
+      }
+      if (DONE) break;
+      NNCV = nadded;
+      GG_TRY(D.precond_multi(L));
+    } else {
       const int limadd = std::min(LIM, MBLOCK + KPASS);
       DONE = false;
       for (int i = 1; i <= NNCV; ++i) {
@@ -905,7 +1073,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
     // Gram-Schmidt of the new vectors, OP, ADDS
     for (int v = 0; v < NNCV; ++v) GG_TRY(D.orthonormalize(KPASS + v));
     GG_TRY(D.op(KPASS, NNCV));
-    for (int v = 0; v < NNCV; ++v) GG_TRY(D.adds(KPASS + v, S));
+    GG_TRY(D.adds(KPASS, NNCV, S));
     KPASS += NNCV;
     ++NLOOPS;
     if (NLOOPS <= MAXITER) continue;

@@ -99,13 +99,13 @@ bool ql_values(int n, std::vector<double> d, std::vector<double> e, std::vector<
       if (m != l) {
         if (iter++ == 60) return false;
         double g = (d[l + 1] - d[l]) / (2.0 * ee[l]);
-        double r = std::hypot(g, 1.0);
+        double r = std::sqrt(g * g + 1.0);  // |g| is bounded: e[l] is not negligible here
         g = d[m] - d[l] + ee[l] / (g + (g >= 0 ? std::fabs(r) : -std::fabs(r)));
         double s = 1.0, c = 1.0, p = 0.0;
         int i;
         for (i = m - 1; i >= l; --i) {
           double f = s * ee[i], b = c * ee[i];
-          ee[i + 1] = (r = std::hypot(f, g));
+          ee[i + 1] = (r = std::sqrt(f * f + g * g));
           if (r == 0.0) {
             d[i + 1] -= p;
             ee[m] = 0.0;

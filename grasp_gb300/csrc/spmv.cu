@@ -190,6 +190,9 @@ __global__ void __launch_bounds__(256) k_spmv_split(const int64_t *__restrict__ 
   if (row >= n) return;
   const int64_t p0 = ptr[row], p1 = ptr[row + 1];
   df acc = {0.f, 0.f};
+  // unrolled so that several iterations' loads (and the dependent x gathers)
+  // are in flight together; the additions keep their order
+#pragma unroll 4
   for (int64_t p = p0 + lane; p < p1; p += 32) {
     const float ah = __ldg(hi + p), al = __ldg(lo + p);
     const float2 xv = __ldg(xs + __ldg(col + p));
@@ -240,6 +243,7 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
   const size_t off = (size_t)(*pc) * ld;
   const int64_t p0 = ptr[row], p1 = ptr[row + 1];
   df acc = {0.f, 0.f};
+#pragma unroll 4
   for (int64_t p = p0 + lane; p < p1; p += 32) {
     const float ah = __ldg(hi + p), al = __ldg(lo + p);
     const float2 xv = xs[__ldg(col + p)];
