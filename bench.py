@@ -272,9 +272,14 @@ def run_ours(a):
     l0 = launch_count()
     times = []
     ev = None
+    mv_ms = mv_n = 0.0
     for _ in range(a.steps):
         t, ev, vec, info = solve_resident(ctx, H, w.nroots, SPLIT)
         times.append(t)
+        # full-block matvecs of this solve, timed with CUDA events on the
+        # context stream around each launch
+        mv_ms += ctx.stage_stat(11)
+        mv_n += ctx.stage_stat(12)
     l1 = launch_count()
     clk = clocks.stop()
     _barrier(pg)
@@ -288,11 +293,16 @@ def run_ours(a):
         times64.append(t)
     t_fp64 = _max_over_ranks(pg, statistics.median(times64))
     dE = float(np.abs(ev - ev64).max())
-    # matvec roofline (dominant kernel of the Davidson loop)
-    ms_split, alg_bytes = H.matvec_timing(SPLIT, 50)
+    # matvec roofline (dominant kernel of the Davidson loop): algorithmic
+    # bytes of one y = H x over the full block (the reference's lower-triangle
+    # storage, stage_stat 6) / the average in-solve launch time of the timed
+    # steps; the standalone cold-L2 timings are reported beside it
+    alg_bytes = ctx.stage_stat(6)
+    ms_insolve = mv_ms / max(mv_n, 1.0)
+    ms_split, _ = H.matvec_timing(SPLIT, 50)
     ms_64, _ = H.matvec_timing(FP64, 50)
     peak, peak_kind = _peaks()
-    achieved = alg_bytes / (ms_split * 1e-3) / 1e9
+    achieved = alg_bytes / (ms_insolve * 1e-3) / 1e9
     # e2e through the public API from pinned host buffers
     arrays = [b.iendc, b.irow, b.iq, w.orb.pf, w.orb.qf, b.tlist["lab"], b.tlist["start"], b.tlist["loc"],
               b.tlist["coeff"]]
@@ -322,10 +332,13 @@ def run_ours(a):
                        parallelism="replicas" if ws > 1 else "single", l2="inputs > L2 (129 MB): no flush"),
         "fp64_ci_solve_s": t_fp64,
         "max_abs_dE_split_vs_fp64_Eh": dE,
-        "matvec": {"split_us": ms_split * 1e3, "fp64_us": ms_64 * 1e3, "alg_bytes": alg_bytes,
-                   "split_gbs": achieved, "fp64_gbs": alg_bytes / (ms_64 * 1e-3) / 1e9},
+        "matvec": {"in_solve_split_us": ms_insolve * 1e3, "in_solve_launches": int(mv_n),
+                   "standalone_split_us": ms_split * 1e3, "standalone_fp64_us": ms_64 * 1e3,
+                   "alg_bytes": alg_bytes, "standalone_split_gbs": alg_bytes / (ms_split * 1e-3) / 1e9,
+                   "standalone_fp64_gbs": alg_bytes / (ms_64 * 1e-3) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": _ncu_traffic(), "kernel": "k_spmv_split", "peak_kind": peak_kind},
+                     "traffic": _ncu_traffic(), "kernel": "k_spmv_split_col (in the Davidson pass)",
+                     "peak_kind": peak_kind},
         "stages": stage,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(l1 - l0),
