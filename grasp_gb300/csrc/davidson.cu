@@ -40,10 +40,14 @@ namespace gg {
 namespace {
 
 constexpr int TPB = 256;
-constexpr int RT = 128;        // threads (= rows) per block of the row kernels
+constexpr int RT = 128;        // threads (= rows) per block of the block-pass Ritz kernel
+constexpr int RR = 64;         // rows per block of the row kernels (k_ritz, k_csub)
+constexpr int RCH = 4;         // column chunks per row: threads per row of the row kernels
+constexpr int RTH = RR * RCH;  // threads per block of the row kernels
 constexpr int CD_T = 256;      // threads of the column-dot kernel (8 warps)
 constexpr int CD_G = 4;        // columns per warp group of the column-dot kernel
 constexpr int CD_MAXR = 1024;  // rows per block of the column-dot kernel, at most
+constexpr int CS_T = 256;      // threads of the column-sum kernel
 constexpr int SV_MAX = 1024;   // LIM bound: shared copies of s and of the coefficients
 constexpr int RC = 32;         // rows per block of MULTBC (one per lane)
 constexpr int NCH = 8;         // warps of MULTBC
@@ -104,53 +108,73 @@ __device__ __forceinline__ bool arrive_last(unsigned *counter, bool *flag) {
   return *flag;
 }
 
-// Ritz vector and residual (NEWVEC, dvdson.f90:1100-1111), one row per thread:
+
+// Row products of the row kernels: thread (row rl, chunk ch) of a block of
+// RR rows x RCH chunks sums X[i, j] v[j] over its chunk of columns with four
+// independent chains (loads of several columns in flight); the chunk sums
+// are combined in chunk order through shared memory by the caller.
+__device__ __forceinline__ double chunk_dot(const double *__restrict__ px, int64_t ld, const double *v, int jb,
+                                            int je) {
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
+  int j = jb;
+#pragma unroll 2
+  for (; j + 3 < je; j += 4) {
+    const size_t o = (size_t)j * ld;
+    const double x0 = px[o], x1 = px[o + ld], x2 = px[o + 2 * ld], x3 = px[o + 3 * ld];
+    t0 = fma(x0, v[j], t0);
+    t1 = fma(x1, v[j + 1], t1);
+    t2 = fma(x2, v[j + 2], t2);
+    t3 = fma(x3, v[j + 3], t3);
+  }
+  for (; j < je; ++j) t0 = fma(px[(size_t)j * ld], v[j], t0);
+  return (t0 + t1) + (t2 + t3);
+}
+
+// Ritz vector and residual (NEWVEC, dvdson.f90:1100-1111):
 //   b = BASIS s ; a = AB s ; r = a - lambda b -> BASIS(:, c), AB(:, c).
 // The last block adds the per-block |r|^2 in order and derives NEWVEC's
 // robust shift (dvdson.f90:1139-1160) and the convergence flag.
-__global__ void __launch_bounds__(RT) k_ritz(double *B, double *AB, int64_t ld, PSrc ps,
-                                             const double *__restrict__ s, int n, double *__restrict__ part,
-                                             unsigned *__restrict__ counter, double *__restrict__ scal) {
+__global__ void __launch_bounds__(RTH) k_ritz(double *B, double *AB, int64_t ld, PSrc ps,
+                                              const double *__restrict__ s, int n, double *__restrict__ part,
+                                              unsigned *__restrict__ counter, double *__restrict__ scal) {
   const IterParams P = ps.get();
   const int k = P.k, c = P.c;
   __shared__ double sv[SV_MAX];
-  __shared__ double red[RT / 32];
+  __shared__ double pb[RCH][RR], pa[RCH][RR];
+  __shared__ double red[RTH / 32];
   __shared__ bool last;
-  for (int j = threadIdx.x; j < k; j += RT) sv[j] = s[j];
+  for (int j = threadIdx.x; j < k; j += RTH) sv[j] = s[j];
   __syncthreads();
-  const int i = blockIdx.x * RT + threadIdx.x;
-  double r = 0.0;
+  const int rl = threadIdx.x % RR, ch = threadIdx.x / RR;
+  const int i = blockIdx.x * RR + rl;
+  const int per = (k + RCH - 1) / RCH, jb = min(k, ch * per), je = min(k, jb + per);
+  double bs = 0.0, as = 0.0;
   if (i < n) {
-    const double *pb = B + i, *pa = AB + i;
-    double b0 = 0.0, b1 = 0.0, b2 = 0.0, b3 = 0.0, a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    int j = 0;
-    for (; j + 3 < k; j += 4) {
-      const size_t o = (size_t)j * ld;
-      b0 = fma(pb[o], sv[j], b0);
-      a0 = fma(pa[o], sv[j], a0);
-      b1 = fma(pb[o + ld], sv[j + 1], b1);
-      a1 = fma(pa[o + ld], sv[j + 1], a1);
-      b2 = fma(pb[o + 2 * ld], sv[j + 2], b2);
-      a2 = fma(pa[o + 2 * ld], sv[j + 2], a2);
-      b3 = fma(pb[o + 3 * ld], sv[j + 3], b3);
-      a3 = fma(pa[o + 3 * ld], sv[j + 3], a3);
+    bs = chunk_dot(B + i, ld, sv, jb, je);
+    as = chunk_dot(AB + i, ld, sv, jb, je);
+  }
+  pb[ch][rl] = bs;
+  pa[ch][rl] = as;
+  __syncthreads();
+  double r = 0.0;
+  if (ch == 0 && i < n) {
+    double bb = pb[0][rl], aa = pa[0][rl];
+#pragma unroll
+    for (int q = 1; q < RCH; ++q) {
+      bb += pb[q][rl];
+      aa += pa[q][rl];
     }
-    for (; j < k; ++j) {
-      b0 = fma(pb[(size_t)j * ld], sv[j], b0);
-      a0 = fma(pa[(size_t)j * ld], sv[j], a0);
-    }
-    const double b = (b0 + b1) + (b2 + b3), a = (a0 + a1) + (a2 + a3);
-    r = fma(-P.lam, b, a);
-    B[(size_t)c * ld + i] = b;
+    r = fma(-P.lam, bb, aa);
+    B[(size_t)c * ld + i] = bb;
     AB[(size_t)c * ld + i] = r;
   }
-  const double t = block_sum<RT>(r * r, red);
+  const double t = block_sum<RTH>(r * r, red);
   if (threadIdx.x == 0) part[blockIdx.x] = t;
   if (!arrive_last(counter, &last)) return;
   double u = 0.0;
-  for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + q);
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += RTH) u += __ldcg(part + q);
   __syncthreads();
-  u = block_sum<RT>(u, red);
+  u = block_sum<RTH>(u, red);
   if (threadIdx.x == 0) {
     const double res = sqrt(u);
     scal[SC_RN2] = u;
@@ -194,14 +218,12 @@ __global__ void k_precond(double *B, double *AB, int64_t ld, PSrc ps, const doub
 // lane. The last block adds the per-block partials in block order.
 template <bool PRE>
 __global__ void __launch_bounds__(CD_T) k_cdots(const double *X, int64_t ld, PSrc ps, int kofs, double *W, double *AB,
-                                                double *diag, const double *scal, const double *skip, int fslot,
-                                                int n, int rows, int kp, double *__restrict__ part,
-                                                unsigned *__restrict__ counter, double *__restrict__ out) {
+                                                double *diag, const double *scal, const double *skip, int n,
+                                                int rows, int pitch, double *__restrict__ part) {
   if (skip && *skip != 0.0) return;
   const IterParams P = ps.get();
   const int c = P.c, k = c + kofs;
   __shared__ double ws[CD_MAXR];
-  __shared__ bool last;
   const int r0 = blockIdx.x * rows;
   const int nr = min(rows, n - r0);
   double *wc = W + (size_t)c * ld;
@@ -247,61 +269,68 @@ __global__ void __launch_bounds__(CD_T) k_cdots(const double *X, int64_t ld, PSr
     v += __shfl_xor_sync(0xffffffffu, v, 2);
     v += __shfl_xor_sync(0xffffffffu, v, 1);
     const int q = (lane >> 3) & 3;  // column of v
-    if ((lane & 7) == 0 && j0 + q < k) part[(size_t)blockIdx.x * kp + j0 + q] = v;
+    if ((lane & 7) == 0 && j0 + q < k) part[(size_t)(j0 + q) * pitch + blockIdx.x] = v;
   }
-  if (!arrive_last(counter, &last)) return;
-  const double f = (fslot >= 0) ? scal[fslot] : 1.0;
-  for (int j = wid; j < k; j += CD_T / 32) {
-    double u = 0.0;
-    for (int b = lane; b < (int)gridDim.x; b += 32) u += __ldcg(part + (size_t)b * kp + j);
-    u = warp_sum(u);
-    if (lane == 0) out[j] = (fslot >= 0) ? f * u : u;
-  }
-  if (threadIdx.x == 0) *counter = 0u;
 }
 
-// Gram-Schmidt update of column c, one row per thread:
+// out[j] = f sum_b part[j pitch + b] over the nb block partials of k_cdots,
+// j < k = c + kofs; one block per column, partials added in a fixed order
+// (f = scal[fslot], or 1 when fslot < 0). packed: out is a packed upper
+// matrix and the sums go to its column c.
+__global__ void __launch_bounds__(CS_T) k_colsum(const double *__restrict__ part, int pitch, int nb, PSrc ps, int kofs,
+                                                 const double *skip, const double *__restrict__ scal, int fslot,
+                                                 double *__restrict__ out, int packed) {
+  if (skip && *skip != 0.0) return;
+  const IterParams P = ps.get();
+  const int j = blockIdx.x;
+  if (j >= P.c + kofs) return;
+  if (packed) out += (size_t)P.c * (P.c + 1) / 2;  // column c of a packed upper matrix
+  __shared__ double red[CS_T / 32];
+  const double *pj = part + (size_t)j * pitch;
+  double u = 0.0;
+  for (int b = threadIdx.x; b < nb; b += CS_T) u += pj[b];
+  u = block_sum<CS_T>(u, red);
+  if (threadIdx.x == 0) out[j] = (fslot >= 0) ? scal[fslot] * u : u;
+}
+
+// Gram-Schmidt update of column c:
 //   w <- f w - sum_{j<c} X[:, j] coef[j]   (f = scal[fin], or 1 when fin < 0)
 // and scal[fout] = 1/|w| (the last block adds the block partials in order).
-__global__ void __launch_bounds__(RT) k_csub(double *X, int64_t ld, PSrc ps, const double *__restrict__ coef,
-                                             const double *skip, int fin, int fout, int n,
-                                             double *__restrict__ part, unsigned *__restrict__ counter,
-                                             double *scal) {
+__global__ void __launch_bounds__(RTH) k_csub(double *X, int64_t ld, PSrc ps, const double *__restrict__ coef,
+                                              const double *skip, int fin, int fout, int n,
+                                              double *__restrict__ part, unsigned *__restrict__ counter,
+                                              double *scal) {
   if (skip && *skip != 0.0) return;
   const IterParams P = ps.get();
   const int k = P.c;
   __shared__ double cs[SV_MAX];
-  __shared__ double red[RT / 32];
+  __shared__ double pt[RCH][RR];
+  __shared__ double red[RTH / 32];
   __shared__ bool last;
-  for (int j = threadIdx.x; j < k; j += RT) cs[j] = coef[j];
+  for (int j = threadIdx.x; j < k; j += RTH) cs[j] = coef[j];
   __syncthreads();
-  const int i = blockIdx.x * RT + threadIdx.x;
+  const int rl = threadIdx.x % RR, ch = threadIdx.x / RR;
+  const int i = blockIdx.x * RR + rl;
+  const int per = (k + RCH - 1) / RCH, jb = min(k, ch * per), je = min(k, jb + per);
+  pt[ch][rl] = (i < n) ? chunk_dot(X + i, ld, cs, jb, je) : 0.0;
+  __syncthreads();
   double wn = 0.0;
-  if (i < n) {
-    const double *px = X + i;
-    double t0 = 0.0, t1 = 0.0, t2 = 0.0, t3 = 0.0;
-    int j = 0;
-    for (; j + 3 < k; j += 4) {
-      const size_t o = (size_t)j * ld;
-      t0 = fma(px[o], cs[j], t0);
-      t1 = fma(px[o + ld], cs[j + 1], t1);
-      t2 = fma(px[o + 2 * ld], cs[j + 2], t2);
-      t3 = fma(px[o + 3 * ld], cs[j + 3], t3);
-    }
-    for (; j < k; ++j) t0 = fma(px[(size_t)j * ld], cs[j], t0);
-    const double t = (t0 + t1) + (t2 + t3);
+  if (ch == 0 && i < n) {
+    double t = pt[0][rl];
+#pragma unroll
+    for (int q = 1; q < RCH; ++q) t += pt[q][rl];
     double *w = X + (size_t)k * ld + i;
     const double w0 = (fin >= 0) ? scal[fin] * (*w) : *w;
     wn = w0 - t;
     *w = wn;
   }
-  const double sq = block_sum<RT>(wn * wn, red);
+  const double sq = block_sum<RTH>(wn * wn, red);
   if (threadIdx.x == 0) part[blockIdx.x] = sq;
   if (!arrive_last(counter, &last)) return;
   double u = 0.0;
-  for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + q);
+  for (int q = threadIdx.x; q < (int)gridDim.x; q += RTH) u += __ldcg(part + q);
   __syncthreads();
-  u = block_sum<RT>(u, red);
+  u = block_sum<RTH>(u, red);
   if (threadIdx.x == 0) {
     scal[fout] = 1.0 / sqrt(u);
     *counter = 0u;
@@ -467,7 +496,8 @@ struct Dvd {
   DBuf<double> dots;              // [0, lim + 8) dot products, then SC_N pass scalars
   DBuf<double> dup;               // [0, 8) IterParams, [8, 8 + lim) Ritz coefficients
   DBuf<unsigned> counters;        // last-block counters, one per kernel kind
-  int nrow = 0;                   // blocks of the row kernels
+  int nrow = 0;                   // blocks of the block-pass Ritz kernel (RT rows each)
+  int nrr = 0;                    // blocks of the row kernels (RR rows each)
   int cd_rows = 0, cd_blocks = 0, kp = 0;  // column-dot layout: rows per block, blocks, partial pitch
   int nmv = 0;
   double mv_ms = 0;
@@ -488,6 +518,12 @@ struct Dvd {
   cudaEvent_t pev0 = nullptr, pev1 = nullptr;  // around each single-vector pass
   double pass_ms = 0;             // device ms of the single-vector passes
   int graph_kernels = 0;
+  // block pass (MBLOCK > 1): new columns c_v = KPASS + v, v < m, each
+  // Gram-Schmidt -> OP -> ADDS, as one graph per m; parameters in dpv[v]
+  DBuf<IterParams> dpv;
+  IterParams *hpv = nullptr;      // pinned
+  std::vector<cudaGraphExec_t> bexec;
+  std::vector<int> bkernels;
   bool use_graph = true;          // GRASP_GPU_DVD_GRAPH=0 launches the same pass kernel by kernel
 
   double *scal() { return dots.p + lim + 8; }
@@ -505,6 +541,7 @@ struct Dvd {
     s = c->stream;
     ld = ((int64_t)n + 31) / 32 * 32;
     nrow = (n + RT - 1) / RT;
+    nrr = (n + RR - 1) / RR;
     // about two column-dot blocks per SM, rows a multiple of 32
     int sms = 152;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
@@ -515,7 +552,7 @@ struct Dvd {
     GG_TRY(AB.alloc((size_t)ld * lim));
     GG_TRY(T.alloc((size_t)ld * lim));
     GG_TRY(diag.alloc(n));
-    GG_TRY(part.alloc((size_t)std::max(cd_blocks * kp, nrow * MT_MAX) + 1024));
+    GG_TRY(part.alloc((size_t)std::max(std::max(cd_blocks * kp, nrow * MT_MAX), nrr) + 1024));
     GG_TRY(dS.alloc((size_t)lim * (lim + 1) / 2));
     GG_TRY(dmt.alloc((size_t)MT_MAX * lim + 2 * MT_MAX));
     GG_CUDA(cudaMallocHost(&hS, (size_t)lim * (lim + 1) / 2 * sizeof(double)));
@@ -543,6 +580,9 @@ struct Dvd {
     if (hS) cudaFreeHost(hS);
     if (hmt) cudaFreeHost(hmt);
     if (gexec) cudaGraphExecDestroy(gexec);
+    for (cudaGraphExec_t e : bexec)
+      if (e) cudaGraphExecDestroy(e);
+    if (hpv) cudaFreeHost(hpv);
     if (graph) cudaGraphDestroy(graph);
     if (gev0) cudaEventDestroy(gev0);
     if (gev1) cudaEventDestroy(gev1);
@@ -552,22 +592,25 @@ struct Dvd {
 
   // ---- kernel launchers (counters: 0 ritz, 1 column dots, 2 csub) ----
   void launch_ritz(const PSrc &ps) {
-    k_ritz<<<nrow, RT, 0, s>>>(B.p, AB.p, ld, ps, dup.p + 8, n, part.p, counters.p + 0, scal());
+    k_ritz<<<nrr, RTH, 0, s>>>(B.p, AB.p, ld, ps, dup.p + 8, n, part.p, counters.p + 0, scal());
     note_launch();
   }
+  // column dots (partials per block, then one block per column adds them)
   void launch_dots(bool pre, const PSrc &ps, int kofs, double *W, const double *skip, int fslot,
-                   double *out = nullptr) {
+                   double *out = nullptr, int packed = 0) {
     if (!out) out = dots.p;
     if (pre)
-      k_cdots<true><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, fslot, n, cd_rows,
-                                               kp, part.p, counters.p + 1, out);
+      k_cdots<true><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, n, cd_rows,
+                                               cd_blocks, part.p);
     else
-      k_cdots<false><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, fslot, n, cd_rows,
-                                                kp, part.p, counters.p + 1, out);
+      k_cdots<false><<<cd_blocks, CD_T, 0, s>>>(B.p, ld, ps, kofs, W, AB.p, diag.p, scal(), skip, n, cd_rows,
+                                                cd_blocks, part.p);
+    k_colsum<<<lim + 1, CS_T, 0, s>>>(part.p, cd_blocks, cd_blocks, ps, kofs, skip, scal(), fslot, out, packed);
+    note_launch();
     note_launch();
   }
   void launch_csub(const PSrc &ps, const double *skip, int fin, int fout) {
-    k_csub<<<nrow, RT, 0, s>>>(B.p, ld, ps, dots.p, skip, fin, fout, n, part.p, counters.p + 2, scal());
+    k_csub<<<nrr, RTH, 0, s>>>(B.p, ld, ps, dots.p, skip, fin, fout, n, part.p, counters.p + 2, scal());
     note_launch();
   }
   void launch_cscale(const PSrc &ps, const double *skip, int fslot, float2 *xs) {
@@ -632,6 +675,71 @@ struct Dvd {
     graph = gcap;
     GG_CUDA(cudaGraphInstantiate(&gexec, graph, 0));
     graph_kernels = (int)captured;
+    return GG_OK;
+  }
+
+  // Gram-Schmidt, OP and ADDS of new columns P[v].c, v < m, in that order per
+  // column (each column needs only the columns before it); the S columns go
+  // to dS at their packed offsets
+  int enqueue_block(int m) {
+    for (int v = 0; v < m; ++v) {
+      const PSrc ps{dpv.p + v, IterParams{}};
+      const int *dcol = reinterpret_cast<const int *>(reinterpret_cast<const char *>(dpv.p + v) +
+                                                      offsetof(IterParams, c));
+      cgs2(ps, false, nullptr, precision == GG_SPLIT ? h->dXs.p : nullptr);
+      GG_TRY(spmv_col(h, precision, B.p, AB.p, ld, dcol, nullptr, s));
+      launch_dots(false, ps, 1, AB.p, nullptr, -1, dS.p, 1);
+    }
+    return GG_OK;
+  }
+  // the block pass for columns kpass .. kpass+m-1: one graph launch, one copy
+  // of the new S columns back
+  int block_pass(int kpass, int m, std::vector<double> &S) {
+    if (m <= 0) return GG_OK;
+    if (m > MT_MAX) return fail(GG_ERR_ARG, "block pass: more new vectors than supported");
+    if (!dpv.p) {
+      GG_TRY(dpv.alloc(MT_MAX));
+      GG_CUDA(cudaMallocHost(&hpv, MT_MAX * sizeof(IterParams)));
+      bexec.assign(MT_MAX + 1, nullptr);
+      bkernels.assign(MT_MAX + 1, 0);
+    }
+    for (int v = 0; v < m; ++v) {
+      hpv[v] = IterParams{};
+      hpv[v].c = kpass + v;
+    }
+    GG_CUDA(cudaMemcpyAsync(dpv.p, hpv, m * sizeof(IterParams), cudaMemcpyHostToDevice, s));
+    if (use_graph) {
+      if (!bexec[m]) {
+        GG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        const long long before = gg_launch_count();
+        const int st = enqueue_block(m);
+        const long long captured = gg_launch_count() - before;
+        note_launches(-captured);
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(s, &g);
+        if (st != GG_OK) {
+          if (g) cudaGraphDestroy(g);
+          return st;
+        }
+        if (ce != cudaSuccess) return fail(GG_ERR_CUDA, std::string("block pass capture: ") + cudaGetErrorString(ce));
+        const cudaError_t ie = cudaGraphInstantiate(&bexec[m], g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess) return fail(GG_ERR_CUDA, std::string("block pass graph: ") + cudaGetErrorString(ie));
+        bkernels[m] = (int)captured;
+      }
+      GG_CUDA(cudaGraphLaunch(bexec[m], s));
+      note_launches(bkernels[m]);
+    } else {
+      GG_TRY(enqueue_block(m));
+    }
+    nmv += m;
+    mv_count += m;
+    const size_t o0 = (size_t)kpass * (kpass + 1) / 2, o1 = (size_t)(kpass + m) * (kpass + m + 1) / 2;
+    GG_CUDA(cudaMemcpyAsync(hS + o0, dS.p + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const auto t0 = std::chrono::steady_clock::now();
+    GG_CUDA(cudaStreamSynchronize(s));
+    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::memcpy(S.data() + o0, hS + o0, (o1 - o0) * sizeof(double));
     return GG_OK;
   }
 
@@ -884,22 +992,43 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   int REST = std::max(LIM / 2, 2 * NUME);
   REST = std::min(REST, LIM - 3);
   bool DONE = false;
-  std::vector<double> w;
+  std::vector<double> w, hlo, hhi;
+  int kprev = -1, mprev = 0;  // size of S and number of eigenvalues at the previous solve
   for (;;) {
     const int IFIND = std::min(KPASS, REST);
     for (int i = 0; i < IFIND; ++i) OLDVAL[i] = EIGVAL[i];
-    w.assign(IFIND, 0.0);
-    // DSPEVX returns IFIND eigenpairs; only the first NUME eigenvectors are
-    // read afterwards (TSTSEL, NEWVEC, MULTBC), all IFIND = REST when the
-    // basis is full and OVFLOW collapses onto them.
-    const int nvecs = (KPASS == LIM) ? IFIND : std::min(IFIND, NUME);
+    // DSPEVX returns IFIND eigenpairs. Read afterwards are EIGVAL(1:NUME+1)
+    // (TSTSEL, NEWVEC's GAP) and the first NUME eigenvectors (TSTSEL,
+    // NEWVEC, MULTBC), except when the basis is full: OVFLOW then collapses
+    // onto all IFIND = REST pairs. Only those are computed.
+    const bool full = (KPASS == LIM);
+    const int mneed = full ? IFIND : std::min(IFIND, NUME + 1);
+    const int nvecs = full ? IFIND : std::min(IFIND, NUME);
+    w.assign(mneed, 0.0);
+    // interlacing: S grew by p columns since the last solve (whose leading
+    // block had eigenvalues OLDVAL), so lambda_j lies in
+    // [OLDVAL(j-p), OLDVAL(j)]
+    const double *blo = nullptr, *bhi = nullptr;
+    if (kprev > 0 && KPASS > kprev) {
+      const int pcols = KPASS - kprev;
+      hlo.assign(mneed, -1e300);
+      hhi.assign(mneed, 1e300);
+      for (int j = 0; j < mneed; ++j) {
+        if (j < mprev) hhi[j] = OLDVAL[j];
+        if (j - pcols >= 0 && j - pcols < mprev) hlo[j] = OLDVAL[j - pcols];
+      }
+      blo = hlo.data();
+      bhi = hhi.data();
+    }
     const auto te0 = std::chrono::steady_clock::now();
-    if (sym_eig_lowest(KPASS, S.data(), IFIND, nvecs, w.data(), SVEC.data()) != 0) {
+    if (sym_eig_lowest(KPASS, S.data(), mneed, nvecs, w.data(), SVEC.data(), blo, bhi) != 0) {
       *ierr_out = -1;
       return fail(GG_ERR_CONVERGE, "DVDSON: projected eigenproblem failed");
     }
     D.t_eig += std::chrono::duration<double>(std::chrono::steady_clock::now() - te0).count();
-    for (int i = 0; i < IFIND; ++i) EIGVAL[i] = w[i];
+    for (int i = 0; i < mneed; ++i) EIGVAL[i] = w[i];
+    kprev = KPASS;
+    mprev = mneed;
     // TSTSEL (dvdson.f90:1260-1413)
     {
       int NNCE = 0;
@@ -952,6 +1081,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
         ind += i;
       }
       KPASS = REST;
+      kprev = REST;  // S is now diag(EIGVAL(1:REST)): its eigenvalues are known
     }
     // NEWVEC (dvdson.f90:1002-1172)
     int nadded = 0, icvc = 0;
@@ -1071,9 +1201,13 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
       NNCV = nadded;
     }
     // Gram-Schmidt of the new vectors, OP, ADDS
-    for (int v = 0; v < NNCV; ++v) GG_TRY(D.orthonormalize(KPASS + v));
-    GG_TRY(D.op(KPASS, NNCV));
-    GG_TRY(D.adds(KPASS, NNCV, S));
+    if (NNCV <= MT_MAX) {
+      GG_TRY(D.block_pass(KPASS, NNCV, S));
+    } else {
+      for (int v = 0; v < NNCV; ++v) GG_TRY(D.orthonormalize(KPASS + v));
+      GG_TRY(D.op(KPASS, NNCV));
+      GG_TRY(D.adds(KPASS, NNCV, S));
+    }
     KPASS += NNCV;
     ++NLOOPS;
     if (NLOOPS <= MAXITER) continue;

@@ -164,6 +164,8 @@ int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int
              const double *skip, cudaStream_t s);
 double spmv_bytes(const gg_hmat *h, int precision, int m);
 // hosteig.cpp: lowest m eigenvalues of a packed-upper symmetric matrix and
-// the eigenvectors of the lowest mvec <= m of them
-int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *z);
+// the eigenvectors of the lowest mvec <= m of them; blo/bhi (may be null)
+// bound eigenvalue j from below/above
+int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *z, const double *blo = nullptr,
+                   const double *bhi = nullptr);
 }  // namespace gg

@@ -130,6 +130,122 @@ bool ql_values(int n, std::vector<double> d, std::vector<double> e, std::vector<
   return true;
 }
 
+// Lowest m eigenvalues (ascending) of the tridiagonal (d, e) by Sturm-count
+// bisection until each is isolated, then Newton's method on det(T - x I)
+// kept inside the isolating bracket (Wilkinson, The Algebraic Eigenvalue
+// Problem, ch. 5, sec. 37-38: the LDL^T pivots q_i of T - x I count the
+// eigenvalues below x, and f'/f = sum q_i'/q_i with one division per step).
+// blo/bhi, when given, are brackets known to hold eigenvalue j (the
+// interlacing bounds from the previous, smaller projected matrix); they are
+// padded by the rounding bound. The active searches are kept in contiguous
+// arrays so that the recurrence vectorises across them. Returns false if a
+// search does not finish.
+bool tri_lowest(int n, const std::vector<double> &d, const std::vector<double> &e, int m, double *w,
+                const double *blo = nullptr, const double *bhi = nullptr) {
+  const double eps = 2.220446049250313e-16;
+  std::vector<double> e2(n, 0.0);
+  double gl = d[0], gu = d[0], tnorm = 0.0, emax2 = 0.0;
+  for (int i = 0; i < n; ++i) {
+    const double el = (i > 0) ? std::fabs(e[i - 1]) : 0.0, er = (i + 1 < n) ? std::fabs(e[i]) : 0.0;
+    gl = std::min(gl, d[i] - el - er);
+    gu = std::max(gu, d[i] + el + er);
+    tnorm = std::max(tnorm, std::fabs(d[i]) + el + er);
+    if (i + 1 < n) {
+      e2[i] = e[i] * e[i];
+      emax2 = std::max(emax2, e2[i]);
+    }
+  }
+  const double pivmin = 2.2250738585072014e-308 * std::max(1.0, emax2) / eps;
+  const double pad = 2.0 * eps * n * std::max(tnorm, 1e-300) + 2.0 * pivmin;
+  gl -= pad;
+  gu += pad;
+  const double atol = 4.0 * eps * std::max(tnorm, 1e-300);
+  std::vector<double> lo(m, gl), hi(m, gu), xj(m);
+  std::vector<int> clo(m, 0), chi(m, n), newton(m, 0), iters(m, 0);
+  if (blo && bhi)
+    for (int j = 0; j < m; ++j) {
+      // a hint is only a bound; an unusable one is ignored
+      const double l = std::max(gl, blo[j] - 8.0 * pad), h = std::min(gu, bhi[j] + 8.0 * pad);
+      if (l < h) {
+        lo[j] = l;
+        hi[j] = h;
+        clo[j] = (l == gl) ? 0 : -1;  // counts at hinted ends are not known yet
+        chi[j] = (h == gu) ? n : -1;
+      }
+    }
+  // compacted state of the active searches
+  std::vector<int> act(m);
+  std::vector<double> x(m), inv(m), qp(m), S(m);
+  std::vector<int> cnt(m);
+  for (int j = 0; j < m; ++j) act[j] = j;
+  int na = m;
+  auto small = [&](int j) {
+    return hi[j] - lo[j] <= atol + 2.0 * eps * std::max(std::fabs(lo[j]), std::fabs(hi[j]));
+  };
+  while (na > 0) {
+    for (int a = 0; a < na; ++a) {
+      const int j = act[a];
+      x[a] = newton[j] ? xj[j] : 0.5 * (lo[j] + hi[j]);
+      double q = d[0] - x[a];
+      if (std::fabs(q) < pivmin) q = -pivmin;
+      const double iv = 1.0 / q;
+      cnt[a] = (q < 0.0);
+      qp[a] = -1.0;
+      S[a] = -iv;
+      inv[a] = iv;
+    }
+    for (int i = 1; i < n; ++i) {
+      const double di = d[i], ei2 = e2[i - 1];
+      for (int a = 0; a < na; ++a) {
+        const double ivp = inv[a];
+        double q = (di - x[a]) - ei2 * ivp;
+        q = (std::fabs(q) < pivmin) ? -pivmin : q;
+        const double dq = -1.0 + ei2 * qp[a] * ivp * ivp;
+        const double iv = 1.0 / q;
+        cnt[a] += (q < 0.0);
+        S[a] += dq * iv;
+        qp[a] = dq;
+        inv[a] = iv;
+      }
+    }
+    int keep = 0;
+    for (int a = 0; a < na; ++a) {
+      const int j = act[a];
+      if (++iters[j] > 300) return false;
+      // keep lambda_j in [lo, hi): count(lo) <= j < count(hi)
+      if (cnt[a] <= j) {
+        lo[j] = x[a];
+        clo[j] = cnt[a];
+      } else {
+        hi[j] = x[a];
+        chi[j] = cnt[a];
+      }
+      bool done = small(j);
+      if (!done && !newton[j] && clo[j] == j && chi[j] == j + 1) {
+        newton[j] = 1;  // isolated: Newton from the middle of the bracket
+        xj[j] = 0.5 * (lo[j] + hi[j]);
+      } else if (!done && newton[j]) {
+        const double step = (S[a] != 0.0) ? -1.0 / S[a] : 0.0;
+        const double xn = x[a] + step;
+        if (std::fabs(step) <= 2.0 * eps * std::fabs(x[a]) + pivmin) {
+          done = true;
+          xj[j] = (xn > lo[j] && xn < hi[j]) ? xn : x[a];
+        } else {
+          xj[j] = (xn > lo[j] && xn < hi[j]) ? xn : 0.5 * (lo[j] + hi[j]);
+        }
+      }
+      if (done) {
+        w[j] = newton[j] ? xj[j] : 0.5 * (lo[j] + hi[j]);
+      } else {
+        act[keep++] = j;
+      }
+    }
+    na = keep;
+  }
+  for (int j = 1; j < m; ++j) w[j] = std::max(w[j], w[j - 1]);
+  return true;
+}
+
 void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector<double>> &orth, unsigned seed,
               double tnorm) {
   const int n = T.n;
@@ -208,8 +324,10 @@ void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector
 
 // Lowest m eigenvalues of the symmetric n x n matrix given in packed upper
 // storage (AP(i + j(j-1)/2) = A(i,j), i <= j), w[m] ascending, and the
-// eigenvectors of the lowest mvec of them, z[n x mvec].
-int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *z) {
+// eigenvectors of the lowest mvec of them, z[n x mvec]. blo/bhi (may be
+// null): bounds known to hold eigenvalue j, used when 2m <= n.
+int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *z, const double *blo,
+                   const double *bhi) {
   if (n <= 0 || m <= 0 || m > n || mvec < 0 || mvec > m) return -1;
   std::vector<double> A((size_t)n * n);
   for (int j = 0; j < n; ++j)
@@ -221,7 +339,13 @@ int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *
   Tri T;
   tridiag(n, A, T);
   std::vector<double> ev;
-  if (!ql_values(n, T.d, T.e, ev)) return -2;
+  if (2 * m <= n) {
+    // the lowest few: isolate and refine each (the DSTEBZ route of DSPEVX)
+    ev.assign(m, 0.0);
+    if (!tri_lowest(n, T.d, T.e, m, ev.data(), blo, bhi)) return -2;
+  } else if (!ql_values(n, T.d, T.e, ev)) {
+    return -2;
+  }
   double tnorm = 0.0;
   for (int i = 0; i < n; ++i)
     tnorm = std::max(tnorm, std::fabs(T.d[i]) + (i > 0 ? std::fabs(T.e[i - 1]) : 0.0) +
