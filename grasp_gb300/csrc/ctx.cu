@@ -61,6 +61,7 @@ int gg_ctx_create(int device, gg_ctx **out) {
   GG_CUDA(cudaSetDevice(device));
   gg_ctx *c = new gg_ctx;
   c->device = device;
+  cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);

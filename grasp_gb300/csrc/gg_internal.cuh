@@ -110,10 +110,26 @@ struct Lists {  // device copies of one block's T/V lists, concatenated in SETHA
   bool valid = false;
 };
 
+constexpr int LT_TW = 1024;  // tile width of the tiled lower-triangle matvec
+
+// Tiled lower-triangle layout of the split matvec (ltile.cu)
+struct LTile {
+  bool built = false, usable = false, vals_valid = false;
+  int nj = 0, nchunks = 0, nitems = 0;
+  int64_t nslots = 0;
+  size_t smem = 0;
+  DBuf<unsigned char> blob, chunks, items;
+  DBuf<long long> slot0;
+  DBuf<int64_t> src;                    // EMT index of every slot
+  DBuf<int> jptr, jlist;                // items per column tile
+  DBuf<double> pg, ps;                  // row partials [nj][ncf], column partials [items][LT_TW]
+};
+
 }  // namespace gg
 
 struct gg_ctx {
   int device = 0;
+  int sms = 152;                        // multiprocessors of the device
   cudaStream_t stream = nullptr;
   gg::Grid grid;
   gg::Orbitals orb;
@@ -147,6 +163,7 @@ struct gg_hmat {
   gg::DBuf<float> dSymHi, dSymLo;       // [sym_nnz] split values
   gg::DBuf<float2> dXs;                 // [ncf] split copy of the input vector
   bool sym_vals_valid = false;
+  gg::LTile lt;                         // tiled lower-triangle layout (split matvec)
 };
 
 namespace gg {
@@ -163,6 +180,12 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
 int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
              const double *skip, cudaStream_t s);
 double spmv_bytes(const gg_hmat *h, int precision, int m);
+// ltile.cu
+int build_ltile(gg_hmat *h);
+int refresh_ltile_values(gg_hmat *h);
+int spmv_ltile(gg_hmat *h, const float2 *xs, const double *Xbase, double *Ybase, int64_t ld, const int *dcol,
+               const double *skip, cudaStream_t s);
+double ltile_bytes(const gg_hmat *h);
 // hosteig.cpp: lowest m eigenvalues of a packed-upper symmetric matrix and
 // the eigenvectors of the lowest mvec <= m of them; blo/bhi (may be null)
 // bound eigenvalue j from below/above

@@ -18,6 +18,8 @@
 //             FP64 pipe issues roughly 1/64 of its FP32 rate, so FP64 SpMV is
 //             issue-bound at about the HBM rate; the split form is not.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "gg_internal.cuh"
@@ -272,6 +274,7 @@ int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int
   const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
   if (precision == GG_SPLIT) {
     if (h->dXs.n < (size_t)n) return fail(GG_ERR_STATE, "spmv_col: split copy of x not allocated");
+    if (h->lt.usable) return spmv_ltile(h, h->dXs.p, Bbase, ABbase, ld, dcol, skip, s);
     k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
                                             h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n); ::gg::note_launch();
   } else {
@@ -331,8 +334,20 @@ int build_sym(gg_hmat *h) {
   return GG_OK;
 }
 
+// The tiled lower-triangle split matvec (ltile.cu) reads each stored value
+// once but is slower than the full symmetric kernel at present; it is used
+// when GRASP_GPU_MATVEC=ltile.
+static bool want_ltile() {
+  const char *e = std::getenv("GRASP_GPU_MATVEC");
+  return e && std::strcmp(e, "ltile") == 0;
+}
+
 int refresh_sym_values(gg_hmat *h) {
   GG_TRY(build_sym(h));
+  if (want_ltile()) {
+    GG_TRY(build_ltile(h));
+    GG_TRY(refresh_ltile_values(h));
+  }
   if (h->sym_vals_valid) return GG_OK;
   cudaStream_t s = h->ctx->stream;
   GG_TRY(h->dSymVal.alloc(h->sym_nnz));
@@ -355,8 +370,12 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
     if (precision == GG_SPLIT) {
       GG_TRY(h->dXs.alloc(n));
       k_split_x<<<(n + 255) / 256, 256, 0, s>>>(x, h->dXs.p, n); ::gg::note_launch();
-      k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p, h->dDiag.p, x,
-                                          y, n); ::gg::note_launch();
+      if (h->lt.usable) {
+        GG_TRY(spmv_ltile(h, h->dXs.p, x, y, 0, nullptr, nullptr, s));
+      } else {
+        k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p, h->dDiag.p,
+                                            x, y, n); ::gg::note_launch();
+      }
     } else {
       k_spmv64<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, x, y, n); ::gg::note_launch();
     }
