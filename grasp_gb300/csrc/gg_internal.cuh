@@ -158,6 +158,8 @@ struct gg_hmat {
   int64_t sym_nnz = 0;
   gg::DBuf<int64_t> dSymPtr;            // [ncf + 1]
   gg::DBuf<int32_t> dSymCol;            // [sym_nnz]
+  gg::DBuf<unsigned short> dSymCol16;   // [sym_nnz] when ncf <= 65536
+  bool sym_col16 = false;
   gg::DBuf<int64_t> dSymSrc;            // [sym_nnz] index into EMT
   gg::DBuf<double> dSymVal;             // [sym_nnz] FP64 values
   gg::DBuf<float> dSymHi, dSymLo;       // [sym_nnz] split values

@@ -184,7 +184,8 @@ __global__ void k_split_x(const double *__restrict__ x, float2 *__restrict__ xs,
 
 // y = H x with H_offdiag = hi + lo (FP32 pair), x = xh + xl; double-float
 // accumulation; FP64 diagonal
-__global__ void __launch_bounds__(256) k_spmv_split(const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+template <typename CI>
+__global__ void __launch_bounds__(256) k_spmv_split(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
                                                     const float *__restrict__ hi, const float *__restrict__ lo,
                                                     const float2 *__restrict__ xs, const double *__restrict__ diag,
                                                     const double *__restrict__ x, double *__restrict__ y, int n) {
@@ -233,7 +234,8 @@ __global__ void __launch_bounds__(256) k_spmv64_col(const int64_t *__restrict__ 
   if (lane == 0) ABbase[off + row] = acc;
 }
 
-__global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restrict__ ptr, const int32_t *__restrict__ col,
+template <typename CI>
+__global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
                                                         const float *__restrict__ hi, const float *__restrict__ lo,
                                                         const float2 *__restrict__ xs, const double *__restrict__ diag,
                                                         const double *__restrict__ Bbase, double *__restrict__ ABbase,
@@ -264,6 +266,13 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
   if (lane == 0) ABbase[off + row] = ((double)acc.h + (double)acc.l) + diag[row] * Bbase[off + row];
 }
 
+// 16-bit copy of the column indices (blocks of at most 65,536 CSFs): the
+// split matvec then reads 10 bytes per stored entry instead of 12
+__global__ void k_col16(const int32_t *__restrict__ col, int64_t nnz, unsigned short *__restrict__ c16) {
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nnz; p += (int64_t)gridDim.x * blockDim.x)
+    c16[p] = (unsigned short)col[p];
+}
+
 }  // namespace
 
 // y = H x with x = Bbase + c ld, y = ABbase + c ld, c = *dcol on the device;
@@ -275,8 +284,13 @@ int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int
   if (precision == GG_SPLIT) {
     if (h->dXs.n < (size_t)n) return fail(GG_ERR_STATE, "spmv_col: split copy of x not allocated");
     if (h->lt.usable) return spmv_ltile(h, h->dXs.p, Bbase, ABbase, ld, dcol, skip, s);
-    k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
-                                            h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n); ::gg::note_launch();
+    if (h->sym_col16)
+      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
+                                              h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
+    else
+      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
+                                              h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
+    ::gg::note_launch();
   } else {
     k_spmv64_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, Bbase, ABbase, ld, dcol, skip, n);
     ::gg::note_launch();
@@ -328,6 +342,13 @@ int build_sym(gg_hmat *h) {
   k_own<<<(ncf * 32 + 255) / 256, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, ncf, h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p); ::gg::note_launch();
   k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cursor.p, h->dSymCol.p, h->dSymSrc.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
+  if (ncf <= 65536) {
+    GG_TRY(h->dSymCol16.alloc(h->sym_nnz));
+    k_col16<<<1024, 256, 0, s>>>(h->dSymCol.p, h->sym_nnz, h->dSymCol16.p);
+    ::gg::note_launch();
+    h->sym_col16 = true;
+  }
+  GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaStreamSynchronize(s));
   h->sym_valid = true;
   h->sym_vals_valid = false;
@@ -373,8 +394,13 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
       if (h->lt.usable) {
         GG_TRY(spmv_ltile(h, h->dXs.p, x, y, 0, nullptr, nullptr, s));
       } else {
-        k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p, h->dDiag.p,
-                                            x, y, n); ::gg::note_launch();
+        if (h->sym_col16)
+          k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
+                                              h->dDiag.p, x, y, n);
+        else
+          k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
+                                              h->dDiag.p, x, y, n);
+        ::gg::note_launch();
       }
     } else {
       k_spmv64<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, x, y, n); ::gg::note_launch();
