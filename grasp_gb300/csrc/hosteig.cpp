@@ -56,12 +56,24 @@ void tridiag(int n, std::vector<double> &A, Tri &T) {  // A: full, column-major,
     for (int j = 0; j < m; ++j) {
       const double *col = &A[(size_t)(o + j) * n + o];
       const double vj = vk[j];
-      double acc = col[j] * vj;
-      for (int i = j + 1; i < m; ++i) {
+      // four partial sums: independent chains instead of one dependent one
+      double a0 = col[j] * vj, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      int i = j + 1;
+      for (; i + 3 < m; i += 4) {
         p[i] += col[i] * vj;
-        acc += col[i] * vk[i];
+        p[i + 1] += col[i + 1] * vj;
+        p[i + 2] += col[i + 2] * vj;
+        p[i + 3] += col[i + 3] * vj;
+        a0 += col[i] * vk[i];
+        a1 += col[i + 1] * vk[i + 1];
+        a2 += col[i + 2] * vk[i + 2];
+        a3 += col[i + 3] * vk[i + 3];
       }
-      p[j] += acc;
+      for (; i < m; ++i) {
+        p[i] += col[i] * vj;
+        a0 += col[i] * vk[i];
+      }
+      p[j] += (a0 + a1) + (a2 + a3);
     }
     double pv = 0.0;
     for (int i = 0; i < m; ++i) {
@@ -353,6 +365,9 @@ int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *
   const double ortol = 1e-3 * tnorm, eps = 2.220446049250313e-16;
   std::vector<std::vector<double>> cluster;
   std::vector<double> x(n);
+  // eigenvectors of T, row-major [n][mvec] so that the back-transformation
+  // below runs all vectors together
+  std::vector<double> Y((size_t)n * std::max(mvec, 1));
   double prev = 0.0;
   for (int j = 0; j < m; ++j) w[j] = ev[j];
   for (int j = 0; j < mvec; ++j) {
@@ -362,20 +377,32 @@ int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *
     inv_iter(T, lam, x.data(), cluster, (unsigned)j + 1u, tnorm);
     cluster.push_back(x);
     prev = lam;
-    double *zj = z + (size_t)j * n;
-    for (int i = 0; i < n; ++i) zj[i] = x[i];
-    for (int k = n - 3; k >= 0; --k) {
-      const double beta = T.beta[k];
-      if (beta == 0.0) continue;
-      const double *vk = &T.v[(size_t)k * n];
-      const int mm = n - k - 1;
-      double *zz = zj + k + 1;
-      double dot = 0.0;
-      for (int i = 0; i < mm; ++i) dot += vk[i] * zz[i];
-      dot *= beta;
-      for (int i = 0; i < mm; ++i) zz[i] -= dot * vk[i];
+    for (int i = 0; i < n; ++i) Y[(size_t)i * mvec + j] = x[i];
+  }
+  // z = H_0 H_1 ... H_{n-3} y: reflectors applied last to first, to every
+  // vector at once (dots over rows, vectorised across the vectors)
+  std::vector<double> dots(std::max(mvec, 1));
+  for (int k = n - 3; k >= 0 && mvec > 0; --k) {
+    const double beta = T.beta[k];
+    if (beta == 0.0) continue;
+    const double *vk = &T.v[(size_t)k * n];
+    const int mm = n - k - 1;
+    double *Yk = &Y[(size_t)(k + 1) * mvec];
+    for (int j = 0; j < mvec; ++j) dots[j] = 0.0;
+    for (int i = 0; i < mm; ++i) {
+      const double vi = vk[i];
+      const double *yi = Yk + (size_t)i * mvec;
+      for (int j = 0; j < mvec; ++j) dots[j] += vi * yi[j];
+    }
+    for (int j = 0; j < mvec; ++j) dots[j] *= beta;
+    for (int i = 0; i < mm; ++i) {
+      const double vi = vk[i];
+      double *yi = Yk + (size_t)i * mvec;
+      for (int j = 0; j < mvec; ++j) yi[j] -= dots[j] * vi;
     }
   }
+  for (int j = 0; j < mvec; ++j)
+    for (int i = 0; i < n; ++i) z[(size_t)j * n + i] = Y[(size_t)i * mvec + j];
   return 0;
 }
 

@@ -1,0 +1,338 @@
+"""GRASP's file formats at the boundary of the CI stage, read and written
+byte-compatibly (Fortran unformatted sequential records: each record framed
+by its int32 byte length before and after; little-endian; default INTEGER is
+int32, REAL*8 is float64, LOGICAL is 4 bytes).
+
+  mcp.30        angular structure: file header, then per block the CSR-lower
+                structure MATRIX reads (rmcdhf90/matrix.f90:123-140)
+  mcp.31        one-body (T) coefficient lists, sorted by label
+  mcp.32+k      two-body (V^k) coefficient lists, k = 0..KMAXF
+                (record layouts: rangular90/setmcp.f90:80-82, setmcp2.f90:49-50,
+                sortmem.f90:232-284; read by rmcdhf90/setmcp.f90:78-137 and
+                rmcdhf90/setham.f90:223-341)
+  rwfn          radial wavefunctions (lib9290/lodrwf.f90:100-108)
+  .cm / .mix    mixing coefficients (rci90/matrix.f90:209-212, lodmix.f90:75)
+
+The coefficient lists convert to and from the label-grouped arrays that
+:meth:`grasp_gb300.HMatrix.setham` takes (dicts of lab/start/loc/coeff).
+"""
+from __future__ import annotations
+
+import os
+import struct
+from dataclasses import dataclass, field
+
+import numpy as np
+
+_I4 = np.dtype("<i4")
+_F8 = np.dtype("<f8")
+
+
+class FortranFile:
+    """Sequential unformatted records with 4-byte length markers."""
+
+    def __init__(self, path, mode="rb"):
+        self.f = open(path, mode)
+
+    def close(self):
+        self.f.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def read_record(self) -> bytes:
+        head = self.f.read(4)
+        if len(head) < 4:
+            raise EOFError
+        (n,) = struct.unpack("<i", head)
+        data = self.f.read(n)
+        (m,) = struct.unpack("<i", self.f.read(4))
+        if m != n or len(data) != n:
+            raise ValueError("corrupt record markers")
+        return data
+
+    def write_record(self, *parts):
+        data = b"".join(p if isinstance(p, (bytes, bytearray)) else np.ascontiguousarray(p).tobytes()
+                        for p in parts)
+        self.f.write(struct.pack("<i", len(data)))
+        self.f.write(data)
+        self.f.write(struct.pack("<i", len(data)))
+
+
+def _i4(*v):
+    return np.array(v, dtype=_I4)
+
+
+def _chars(s, n):
+    b = s.encode("ascii")
+    return b[:n].ljust(n, b" ")
+
+
+# ---------------------------------------------------------------------------
+# mcp files
+# ---------------------------------------------------------------------------
+
+@dataclass
+class McpBlock:
+    """One J/parity block: structure (mcp.30) and coefficient lists."""
+    ncf: int
+    iendc: np.ndarray                   # int64 [ncf + 1], IENDC(0) = 0
+    irow: np.ndarray                    # int32 [nnz], 1-based
+    tlist: dict = None                  # lab/start/loc/coeff (+ iclmn)
+    vlists: list = field(default_factory=list)
+
+
+@dataclass
+class McpSet:
+    ncore: int
+    nelec: int
+    ncf: int                            # NCF of the file header (all blocks)
+    nw: int
+    kmaxf: int
+    idblk: list
+    blocks: list
+    diag: bool = False
+    iccut: int = 0
+    lfordr: bool = False
+    myid: int = 0
+    nprocs: int = 1
+
+
+def _write_common_header(ff, s: McpSet):
+    ff.write_record(_chars("MCP", 3), _i4(len(s.blocks), s.myid, s.nprocs))
+    ff.write_record(_i4(s.nelec, s.ncf, s.nw))
+    ff.write_record(_i4(int(s.diag), s.iccut, int(s.lfordr)))
+
+
+def _read_common_header(ff):
+    r = ff.read_record()
+    lab = r[:3].decode("ascii")
+    nb, myid, nprocs = np.frombuffer(r[3:15], _I4)
+    if lab != "MCP":
+        raise ValueError("not a sorted GRASP92 MCP file")
+    nelec, ncf, nw = np.frombuffer(ff.read_record(), _I4)
+    diag, iccut, lfordr = np.frombuffer(ff.read_record(), _I4)
+    return int(nb), int(myid), int(nprocs), int(nelec), int(ncf), int(nw), bool(diag), int(iccut), bool(lfordr)
+
+
+def _write_list(ff, jblock, ncf, lst):
+    lab = np.asarray(lst["lab"], _I4)
+    start = np.asarray(lst["start"], np.int64)
+    loc = np.asarray(lst["loc"], _I4)
+    coeff = np.asarray(lst["coeff"], _F8)
+    iclmn = np.asarray(lst.get("iclmn", np.zeros(loc.size, _I4)), _I4)
+    ff.write_record(_chars("MCP", 3), _i4(jblock, ncf, loc.size))
+    rec = np.dtype([("iclmn", _I4), ("index", _I4), ("coeff", _F8)])
+    for l in range(lab.size):
+        a, b = int(start[l]), int(start[l + 1])
+        ff.write_record(_i4(lab[l], b - a))
+        data = np.empty(b - a, rec)
+        data["iclmn"], data["index"], data["coeff"] = iclmn[a:b], loc[a:b], coeff[a:b]
+        ff.write_record(data)
+    ff.write_record(_i4(0, 0))
+
+
+def _read_list(ff, jblock, ncf):
+    r = ff.read_record()
+    if r[:3].decode("ascii") != "MCP":
+        raise ValueError("list block header missing")
+    jb, ncft, ncoeff = np.frombuffer(r[3:15], _I4)
+    if jb != jblock or ncft != ncf:
+        raise ValueError(f"list block {jb}/{ncft} where block {jblock}/{ncf} expected")
+    rec = np.dtype([("iclmn", _I4), ("index", _I4), ("coeff", _F8)])
+    labs, starts, parts = [], [0], []
+    while True:
+        lab, ncontr = np.frombuffer(ff.read_record(), _I4)
+        if lab == 0 and ncontr == 0:
+            break
+        d = np.frombuffer(ff.read_record(), rec)
+        if d.size != ncontr:
+            raise ValueError("contribution record of the wrong length")
+        labs.append(int(lab))
+        parts.append(d)
+        starts.append(starts[-1] + int(ncontr))
+    d = np.concatenate(parts) if parts else np.zeros(0, rec)
+    return dict(lab=np.array(labs, np.int32), start=np.array(starts, np.int64),
+                loc=np.ascontiguousarray(d["index"]), coeff=np.ascontiguousarray(d["coeff"]),
+                iclmn=np.ascontiguousarray(d["iclmn"]))
+
+
+def write_mcp(filehead, s: McpSet):
+    """Writes filehead.30, filehead.31 and filehead.32 .. filehead.(32+kmaxf)."""
+    nb = len(s.blocks)
+    with FortranFile(f"{filehead}.30", "wb") as ff:
+        ff.write_record(_i4(s.ncore, nb, s.kmaxf))
+        ff.write_record(np.array([b.ncf for b in s.blocks], _I4))
+        ff.write_record(b"".join(_chars(x, 8) for x in s.idblk))
+        _write_common_header(ff, s)
+        for j, b in enumerate(s.blocks, start=1):
+            nnz = int(b.iendc[-1])
+            ff.write_record(_chars("MCP", 3), _i4(j, b.ncf))
+            ff.write_record(_i4(nnz))
+            ff.write_record(np.asarray(b.iendc[1:], _I4), np.asarray(b.irow, _I4))
+    for k in range(31, 33 + s.kmaxf):
+        with FortranFile(f"{filehead}.{k}", "wb") as ff:
+            _write_common_header(ff, s)
+            for j, b in enumerate(s.blocks, start=1):
+                lst = b.tlist if k == 31 else b.vlists[k - 32]
+                _write_list(ff, j, b.ncf, lst)
+
+
+def read_mcp(filehead) -> McpSet:
+    """Reads the mcp files the way SETMCP, MATRIX and SETHAM do (one process)."""
+    with FortranFile(f"{filehead}.30") as ff:
+        ncore, nblock, kmaxf = (int(x) for x in np.frombuffer(ff.read_record(), _I4))
+        ncfblk = np.frombuffer(ff.read_record(), _I4).copy()
+        raw = ff.read_record()
+        idblk = [raw[8 * i:8 * i + 8].decode("ascii") for i in range(nblock)]
+        nb, myid, nprocs, nelec, ncf, nw, diag, iccut, lfordr = _read_common_header(ff)
+        if nprocs != 1:
+            raise ValueError("mcp files written for several processes")
+        blocks = []
+        for j in range(1, nblock + 1):
+            r = ff.read_record()
+            jb, ncfb = np.frombuffer(r[3:11], _I4)
+            if jb != j or ncfb != ncfblk[j - 1]:
+                raise ValueError("matrx: jblockt .NE. jblock .OR. ncf1 .NE. ncf2")
+            (nnz,) = np.frombuffer(ff.read_record(), _I4)
+            d = np.frombuffer(ff.read_record(), _I4)
+            iendc = np.concatenate([[0], d[:ncfb]]).astype(np.int64)
+            irow = d[ncfb:ncfb + nnz].copy()
+            blocks.append(McpBlock(int(ncfb), iendc, irow))
+    for k in range(31, 33 + kmaxf):
+        with FortranFile(f"{filehead}.{k}") as ff:
+            _read_common_header(ff)
+            for j, b in enumerate(blocks, start=1):
+                lst = _read_list(ff, j, b.ncf)
+                if k == 31:
+                    b.tlist = lst
+                else:
+                    b.vlists.append(lst)
+    return McpSet(ncore, nelec, ncf, nw, kmaxf, idblk, blocks, diag, iccut, lfordr, myid, nprocs)
+
+
+# ---------------------------------------------------------------------------
+# rwfn (radial wavefunctions)
+# ---------------------------------------------------------------------------
+
+@dataclass
+class Orbital:
+    np: int
+    nak: int
+    e: float
+    pz: float
+    p: np.ndarray
+    q: np.ndarray
+    r: np.ndarray
+
+
+def read_rwfn(path) -> list:
+    out = []
+    with FortranFile(path) as ff:
+        if ff.read_record()[:6] != b"G92RWF":
+            raise ValueError("not a G92RWF file")
+        while True:
+            try:
+                r = ff.read_record()
+            except EOFError:
+                break
+            npy, naky = np.frombuffer(r[:8], _I4)
+            (ey,) = np.frombuffer(r[8:16], _F8)
+            (my,) = np.frombuffer(r[16:20], _I4)
+            d = np.frombuffer(ff.read_record(), _F8)
+            rr = np.frombuffer(ff.read_record(), _F8)
+            out.append(Orbital(int(npy), int(naky), float(ey), float(d[0]), d[1:1 + my].copy(),
+                               d[1 + my:1 + 2 * my].copy(), rr[:my].copy()))
+    return out
+
+
+def write_rwfn(path, orbitals):
+    with FortranFile(path, "wb") as ff:
+        ff.write_record(b"G92RWF")
+        for o in orbitals:
+            my = o.p.size
+            ff.write_record(_i4(o.np, o.nak), np.array([o.e], _F8), _i4(my))
+            ff.write_record(np.array([o.pz], _F8), np.asarray(o.p, _F8), np.asarray(o.q, _F8))
+            ff.write_record(np.asarray(o.r, _F8))
+
+
+def orbitals_on_grid(orbitals, n, ld=None):
+    """PF/QF [ld x nw] (column-major, zero beyond MF) and NAK/MF as the C ABI
+    takes them, from rwfn records (the orbitals' grid must be the run's)."""
+    nw = len(orbitals)
+    ld = ld or n
+    pf = np.zeros((nw, ld))
+    qf = np.zeros((nw, ld))
+    mf = np.zeros(nw, np.int32)
+    nak = np.array([o.nak for o in orbitals], np.int32)
+    for j, o in enumerate(orbitals):
+        m = min(o.p.size, n)
+        pf[j, :m], qf[j, :m] = o.p[:m], o.q[:m]
+        mf[j] = m
+    return nak, mf, pf, qf
+
+
+# ---------------------------------------------------------------------------
+# mixing coefficients (.cm)
+# ---------------------------------------------------------------------------
+
+@dataclass
+class MixBlock:
+    jblock: int
+    ncf: int
+    nvec: int
+    two_j_plus_1: int
+    parity: int
+    ivec: np.ndarray
+    eav: float
+    eval: np.ndarray
+    evec: np.ndarray                    # [ncf x nvec], column j = vector j
+
+
+@dataclass
+class MixFile:
+    nelec: int
+    ncftot: int
+    nw: int
+    nvectot: int
+    nvecsiz: int
+    blocks: list
+
+
+def read_mix(path) -> MixFile:
+    with FortranFile(path) as ff:
+        if ff.read_record()[:6] != b"G92MIX":
+            raise ValueError("not a G92MIX file")
+        nelec, ncftot, nw, nvectot, nvecsiz, nblock = (int(x) for x in np.frombuffer(ff.read_record(), _I4))
+        blocks = []
+        for _ in range(nblock):
+            jb, ncf, nvec, jj, par = (int(x) for x in np.frombuffer(ff.read_record(), _I4))
+            if nvec <= 0:  # a block without vectors: its header only (rci90/matrix.f90:164-165)
+                blocks.append(MixBlock(jb, ncf, nvec, jj, par, np.zeros(0, np.int32), 0.0, np.zeros(0),
+                                       np.zeros((ncf, 0))))
+                continue
+            ivec = np.frombuffer(ff.read_record(), _I4).copy()
+            d = np.frombuffer(ff.read_record(), _F8)
+            ev = np.frombuffer(ff.read_record(), _F8).reshape(nvec, ncf).T.copy()
+            blocks.append(MixBlock(jb, ncf, nvec, jj, par, ivec, float(d[0]), d[1:1 + nvec].copy(), ev))
+    return MixFile(nelec, ncftot, nw, nvectot, nvecsiz, blocks)
+
+
+def write_mix(path, m: MixFile):
+    with FortranFile(path, "wb") as ff:
+        ff.write_record(b"G92MIX")
+        ff.write_record(_i4(m.nelec, m.ncftot, m.nw, m.nvectot, m.nvecsiz, len(m.blocks)))
+        for b in m.blocks:
+            ff.write_record(_i4(b.jblock, b.ncf, b.nvec, b.two_j_plus_1, b.parity))
+            if b.nvec <= 0:
+                continue
+            ff.write_record(np.asarray(b.ivec, _I4))
+            ff.write_record(np.concatenate([[b.eav], np.asarray(b.eval, _F8)]).astype(_F8))
+            ff.write_record(np.asarray(b.evec, _F8).T.copy())
+
+
+def exists(path):
+    return os.path.exists(path)

@@ -1,0 +1,163 @@
+"""GRASP file formats (grasp_gb300/formats.py): round trips of mcp.30/31/32+k,
+rwfn and .cm, and checks against the reference's own example data
+(src/appl/rhfszeeman95/examples: rwfn and mixing files written by GRASP runs,
+and their text summaries), when the reference tree is present.
+
+The reference-data checks also pin the oracle's grid and quadrature on
+orbitals GRASP produced: RADGRD reproduces the stored grid, QUAD finds the
+orbitals normalised, and the moments <r^-1>, <r>, <r^2> agree with the
+values the reference printed (6 digits)."""
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from grasp_gb300 import formats as F
+from tests.common import hydrogenic_case, ne7_block, oracle_for
+
+REF = "/root/reference/src/appl/rhfszeeman95/examples"
+ref_data = pytest.mark.skipif(not os.path.isdir(REF), reason="reference example data not present")
+
+
+def test_mcp_round_trip_and_setham(tmp_path, oracle_mod):
+    case = hydrogenic_case(nmax=4, lmax=3, z=10.0)
+    _, blk = ne7_block()
+    s = F.McpSet(ncore=0, nelec=4, ncf=blk.ncf, nw=case["orb"].nw, kmaxf=len(blk.vlists) - 1, idblk=["  0+    "],
+                 blocks=[F.McpBlock(blk.ncf, blk.iendc, blk.irow, blk.tlist, list(blk.vlists))])
+    head = str(tmp_path / "mcp")
+    F.write_mcp(head, s)
+    assert sorted(os.listdir(tmp_path)) == sorted(f"mcp.{k}" for k in range(30, 33 + s.kmaxf))
+    r = F.read_mcp(head)
+    assert (r.ncore, r.nelec, r.nw, r.kmaxf, r.idblk) == (0, 4, s.nw, s.kmaxf, s.idblk)
+    b = r.blocks[0]
+    np.testing.assert_array_equal(b.iendc, blk.iendc)
+    np.testing.assert_array_equal(b.irow, blk.irow)
+    for got, want in zip([b.tlist] + b.vlists, [blk.tlist] + list(blk.vlists)):
+        for key in ("lab", "start", "loc", "coeff"):
+            np.testing.assert_array_equal(got[key], want[key])
+    # SETHAM from the lists read back is the SETHAM of the originals
+    o = oracle_for(case)
+    o.genintrk()
+    e0 = o.setham(blk.ncf, blk.nnz, blk.iendc, blk.iq, blk.tlist, blk.vlists)
+    e1 = o.setham(b.ncf, int(b.iendc[-1]), b.iendc, blk.iq, b.tlist, b.vlists)
+    np.testing.assert_array_equal(e0, e1)
+
+
+def test_mcp_record_framing(tmp_path):
+    """Each record is framed by its byte length (int32) on both sides."""
+    p = tmp_path / "x.bin"
+    with F.FortranFile(p, "wb") as ff:
+        ff.write_record(np.array([1, 2, 3], "<i4"))
+    raw = p.read_bytes()
+    assert raw[:4] == (12).to_bytes(4, "little") and raw[-4:] == (12).to_bytes(4, "little") and len(raw) == 20
+
+
+def test_rwfn_round_trip(tmp_path):
+    case = hydrogenic_case(nmax=2, lmax=1, z=10.0)
+    ob = case["orb"]
+    r = np.arange(case["n"]) * 0.01
+    orbs = [F.Orbital(n, k, -e, 1.5, ob.pf[j, :ob.mf[j]], ob.qf[j, :ob.mf[j]], r[:ob.mf[j]])
+            for j, ((n, k), e) in enumerate(zip(case["orbs"], ob.e))]
+    F.write_rwfn(tmp_path / "w", orbs)
+    back = F.read_rwfn(tmp_path / "w")
+    assert [(o.np, o.nak, o.e, o.pz) for o in back] == [(o.np, o.nak, o.e, o.pz) for o in orbs]
+    for a, b in zip(back, orbs):
+        np.testing.assert_array_equal(a.p, b.p)
+        np.testing.assert_array_equal(a.q, b.q)
+
+
+def test_mix_round_trip(tmp_path):
+    rng = np.random.default_rng(1)
+    blocks = [F.MixBlock(1, 5, 2, 1, -1, np.array([1, 2], np.int32), -3.5, np.array([-1.0, -0.5]),
+                         rng.normal(size=(5, 2))),
+              F.MixBlock(2, 3, 0, 999, 999, np.zeros(0, np.int32), 0.0, np.zeros(0), np.zeros((3, 0)))]
+    m = F.MixFile(2, 8, 4, 2, 5, blocks)
+    F.write_mix(tmp_path / "cm", m)
+    back = F.read_mix(tmp_path / "cm")
+    assert (back.nelec, back.ncftot, back.nw, back.nvectot, back.nvecsiz) == (2, 8, 4, 2, 5)
+    np.testing.assert_array_equal(back.blocks[0].evec, blocks[0].evec)
+    assert back.blocks[0].eav == -3.5 and back.blocks[1].nvec == 0
+
+
+def _grid_from_rwfn(orbs):
+    r = max((o.r for o in orbs), key=len)
+    h = round(float(np.log(r[2] / r[1] - 1.0)), 10)   # the run's H, printed with 13 digits
+    rnt = r[1] / (np.exp(h) - 1.0)
+    return r, h, rnt
+
+
+@ref_data
+@pytest.mark.parametrize("name", ["data_He/3Pn6", "data_Ge/2Fn5"])
+def test_reference_rwfn_grid_and_norms(oracle_mod, name):
+    orbs = F.read_rwfn(f"{REF}/{name}.w")
+    r, h, rnt = _grid_from_rwfn(orbs)
+    n = len(r)
+    o = oracle_mod.Oracle(n=n, rnt=rnt, h=h, zz=np.ones(n))
+    R, RP, _ = o.grid()
+    assert np.max(np.abs(R[1:n] - r[1:]) / r[1:]) < 1e-13       # RADGRD
+    for orb in orbs:
+        my = orb.p.size
+        ta = np.zeros(n + 10)
+        ta[:my] = RP[:my] * (orb.p ** 2 + orb.q ** 2)
+        assert abs(o.quad(ta, my) - 1.0) < 1e-12                # QUAD: GRASP's orbitals are normalised
+
+
+@ref_data
+def test_reference_rwfn_moments_match_summary(oracle_mod):
+    name = "data_He/3Pn6"
+    orbs = F.read_rwfn(f"{REF}/{name}.w")
+    r, h, rnt = _grid_from_rwfn(orbs)
+    n = len(r)
+    o = oracle_mod.Oracle(n=n, rnt=rnt, h=h, zz=np.ones(n))
+    R, RP, _ = o.grid()
+    text = open(f"{REF}/{name}.sum").read()
+    block = text.split("Generalised")[1].split("Eigenenergies")[0]
+    rows = re.findall(r"^\s+(\d+[a-z]-?)\s+(\S+)\s+(\S+)\s+(\S+)\s+\S+$", block, re.M)
+    assert len(rows) == len(orbs)
+    for orb, (lab, m1, p1, p2) in zip(orbs, rows):
+        my = orb.p.size
+        rho = orb.p ** 2 + orb.q ** 2
+        got = []
+        for k in (-1, 1, 2):
+            ta = np.zeros(n + 10)
+            ta[:my] = RP[:my] * rho * R[:my] ** k if k > 0 else 0.0
+            if k < 0:
+                ta[1:my] = RP[1:my] * rho[1:] / R[1:my]
+            got.append(o.quad(ta, my))
+        want = [float(x.replace("D", "E")) for x in (m1, p1, p2)]
+        for g, w in zip(got, want):
+            assert abs(g - w) <= 6e-6 * abs(w), (lab, got, want)
+
+
+@ref_data
+@pytest.mark.parametrize("name", ["data_He/3Pn6", "data_Ge/2Fn5"])
+def test_reference_mix_energies_match_summary(name):
+    """EAV + EVAL of the rci mixing file equal the energies rci printed in
+    its summary (.csum, one 'Eigenenergies' table per block)."""
+    m = F.read_mix(f"{REF}/{name}.cm")
+    text = open(f"{REF}/{name}.csum").read()
+    hartrees = []
+    for part in text.split("Eigenenergies:")[1:]:
+        hartrees += [float(x.replace("D", "E")) for x in
+                     re.findall(r"^\s+\d+\s+\S+\s+[+-]\s+(\S+)", part.split("Weights")[0], re.M)]
+    mine = [b.eav + e for b in m.blocks for e in b.eval]
+    # the summary also prints excitation energies and a combined table:
+    # every level of the mixing file must appear among its numbers
+    for e in mine:
+        assert min(abs(e - h) for h in hartrees) <= 1e-11, (e, hartrees)
+    for b in m.blocks:
+        np.testing.assert_allclose(np.linalg.norm(b.evec, axis=0), 1.0, atol=1e-12)
+
+
+@ref_data
+def test_reference_files_round_trip_bytes(tmp_path):
+    """Reading then writing a GRASP-written file gives back the same bytes."""
+    for path in sorted(glob.glob(f"{REF}/data_*/*.w")) + sorted(glob.glob(f"{REF}/data_*/*.cm")):
+        out = tmp_path / os.path.basename(path)
+        if path.endswith(".w"):
+            F.write_rwfn(out, F.read_rwfn(path))
+        else:
+            F.write_mix(out, F.read_mix(path))
+        assert out.read_bytes() == open(path, "rb").read(), path
