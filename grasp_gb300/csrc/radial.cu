@@ -215,6 +215,58 @@ __global__ void k_apairs(const int2 *__restrict__ pairs, int npairs, const doubl
   }
 }
 
+// Completes one R^k(ab;cd) from its contraction sum: QUAD's power-law head
+// term at i = 2 and the end-panel correction at MTP (quad.f90), written at
+// its GENINTRK position; entries whose QUAD head index is not 2 go to the
+// general per-integral QUAD instead.
+__device__ __forceinline__ void rk_finish(const RkTile &T, int p, int idx_c, int f, double sum,
+                                          const int2 *__restrict__ pairs, const YDesc *__restrict__ yd,
+                                          const double *__restrict__ Y, int np, const double *__restrict__ PF,
+                                          const double *__restrict__ QF, int ld, const int *__restrict__ MF,
+                                          const double *__restrict__ R, const double *__restrict__ RP,
+                                          const double *__restrict__ RPOR, const QuadConst &q,
+                                          double *__restrict__ val, long long nval, QuadItem *__restrict__ fb,
+                                          int *__restrict__ nfb) {
+  const int a = T.a;
+  const int c = pairs[p].y;
+  const YDesc y = yd[f];
+  const long long pos = T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)idx_c * y.nd + (long long)(f - y.cs);
+  if (pos < 0 || pos >= nval) {  // position outside the table: report, never write
+    atomicExch(nfb + 1, 1);
+    return;
+  }
+  int mtp;
+  if (T.k == 0 && y.b == y.d)
+    mtp = min(MF[a], MF[c]);
+  else
+    mtp = min(min(y.mtp, MF[a]), MF[c]);
+  const double *Yf = Y + (size_t)f * np;
+  auto ta = [&](int i) {
+    return ((pf(PF, ld, i, a) * pf(PF, ld, i, c) + pf(QF, ld, i, a) * pf(QF, ld, i, c)) * RPOR[i]) * Yf[i];
+  };
+  bool ok = mtp >= 3;
+  double res = 0.0;
+  if (ok) {
+    const double tai = ta(2), taip1 = ta(3);
+    ok = !(fabs(tai) <= 0.0) && (taip1 / tai > 0.0);
+    if (ok) {
+      const double frip1 = taip1 / RP[3];
+      double fri = tai / RP[2];
+      const double ratio = frip1 / fri;
+      const double sigma = log(ratio) / log(R[3] / R[2]);
+      fri = R[2] * fri;
+      res = fri / (sigma + 1.0) + sum;
+      if ((mtp - 2) % 4 == 0) res = res - q.C1 * ta(mtp);
+    }
+  }
+  if (ok) {
+    val[pos] = res;
+  } else {
+    const int slot = atomicAdd(nfb, 1);
+    fb[slot] = QuadItem{a, c, f, mtp, pos};
+  }
+}
+
 // ---------------------------------------------------------------------------
 // R^k contraction: for each (k, a) the GEMM  O[c, f] = sum_i A[(a,c), i] Y[f, i]
 // over the rows c in C(a,k) and the Y functions f = (b,d) with b >= a, then
@@ -276,58 +328,147 @@ __global__ void __launch_bounds__(256) k_rk_gemm(const RkTile *__restrict__ tile
     __syncthreads();
   }
   // epilogue
-  const int a = T.a;
 #pragma unroll
   for (int u = 0; u < 2; ++u) {
     const int r = ty * 2 + u;
     if (r >= nrow) continue;
-    const int p = rowp[r];
-    const int c = pairs[p].y;
-    const int idx_c = T.r0 + r;
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
       const int j = tx * 4 + v;
       if (j >= ncol) continue;
-      const int f = T.c0 + j;
-      const YDesc y = yd[f];
-      const long long pos =
-          T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)idx_c * y.nd + (long long)(f - y.cs);
-      if (pos < 0 || pos >= nval) {  // position outside the table: report, never write
-        atomicExch(nfb + 1, 1);
-        continue;
-      }
-      int mtp;
-      if (T.k == 0 && y.b == y.d)
-        mtp = min(MF[a], MF[c]);
-      else
-        mtp = min(min(y.mtp, MF[a]), MF[c]);
-      const double *Yf = Y + (size_t)f * np;
-      auto ta = [&](int i) {
-        return ((pf(PF, ld, i, a) * pf(PF, ld, i, c) + pf(QF, ld, i, a) * pf(QF, ld, i, c)) * RPOR[i]) * Yf[i];
-      };
-      bool ok = mtp >= 3;
-      double res = 0.0;
-      if (ok) {
-        const double tai = ta(2), taip1 = ta(3);
-        ok = !(fabs(tai) <= 0.0) && (taip1 / tai > 0.0);
-        if (ok) {
-          const double frip1 = taip1 / RP[3];
-          double fri = tai / RP[2];
-          const double ratio = frip1 / fri;
-          const double sigma = log(ratio) / log(R[3] / R[2]);
-          fri = R[2] * fri;
-          res = fri / (sigma + 1.0) + acc[u][v];
-          if ((mtp - 2) % 4 == 0) res = res - q.C1 * ta(mtp);
-        }
-      }
-      if (ok) {
-        val[pos] = res;
-      } else {
-        const int slot = atomicAdd(nfb, 1);
-        fb[slot] = QuadItem{a, c, f, mtp, pos};
-      }
+      rk_finish(T, rowp[r], T.r0 + r, T.c0 + j, acc[u][v], pairs, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val,
+                nval, fb, nfb);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// The same contraction on the tensor cores, split-precision (Ozaki): each row
+// of A and of Y is scaled by a power of two 2^e (|row| < 2^e) and cut into
+// OZ_S slices of 7 bits, x = 2^e sum_s q_s 2^(-7(s+1)) with q_s in [-127, 127]
+// (truncation toward zero; every step is exact in FP64). The products of
+// slice pairs (s, t) with s + t < OZ_S are exact int8 x int8 -> int32 tensor
+// products; pairs with the same q = s + t share one int32 accumulator
+// (at most OZ_S x KC x 127^2 < 2^31). The sum over q is then
+// sum_q acc_q 2^(eA + eY - 7(q + 2)) in FP64. With OZ_S = 10 the result
+// agrees with the FP64 contraction to a few 1e-13 relative on R^k data.
+// ---------------------------------------------------------------------------
+constexpr int OZ_S = 10;
+
+// slices[s][row][i] for rows < nrows (row nrows: zeros), exps[row]
+__global__ void k_oz_split(const double *__restrict__ M, int nrows, int pitch, int K, int KP,
+                           signed char *__restrict__ slices, int *__restrict__ exps) {
+  const int row = blockIdx.x;
+  __shared__ double red[128];
+  double mx = 0.0;
+  if (row < nrows)
+    for (int i = threadIdx.x; i < K; i += blockDim.x) mx = fmax(mx, fabs(M[(size_t)row * pitch + i]));
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int st = 64; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
+  }
+  mx = red[0];
+  const int e = (mx > 0.0) ? ilogb(mx) + 1 : 0;  // mx < 2^e
+  if (threadIdx.x == 0) exps[row] = e;
+  const size_t plane = (size_t)(nrows + 1) * KP;
+  for (int i = threadIdx.x; i < KP; i += blockDim.x) {
+    double x = (row < nrows && i < K) ? scalbn(M[(size_t)row * pitch + i], -e) : 0.0;
+#pragma unroll
+    for (int q = 0; q < OZ_S; ++q) {
+      x *= 128.0;
+      const double t = trunc(x);
+      slices[q * plane + (size_t)row * KP + i] = (signed char)(int)t;
+      x -= t;
+    }
+  }
+}
+
+__device__ __forceinline__ void mma_s8(int (&c)[4], int a0, int a1, int a2, int a3, int b0, int b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+r"(c[0]), "+r"(c[1]), "+r"(c[2]), "+r"(c[3])
+      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// Tiles as k_rk_gemm (BM x BN); warp w computes rows (w & 1) 16 .. +16 and
+// columns (w >> 1) 16 .. +16 (two m16n8k32 tiles).
+__global__ void __launch_bounds__(256) k_rk_ozaki(const RkTile *__restrict__ tiles, const int *__restrict__ rowpair,
+                                                  const int2 *__restrict__ pairs, const signed char *__restrict__ As,
+                                                  const int *__restrict__ eA, int npairs,
+                                                  const signed char *__restrict__ Ys, const int *__restrict__ eY,
+                                                  int nf, int KP, const double *__restrict__ Y,
+                                                  const YDesc *__restrict__ yd, int np, const double *__restrict__ PF,
+                                                  const double *__restrict__ QF, int ld, const int *__restrict__ MF,
+                                                  const double *__restrict__ R, const double *__restrict__ RP,
+                                                  const double *__restrict__ RPOR, QuadConst q,
+                                                  double *__restrict__ val, long long nval,
+                                                  QuadItem *__restrict__ fb, int *__restrict__ nfb) {
+  const RkTile T = tiles[blockIdx.x];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int gid = lane >> 2, tig = lane & 3;
+  const int nrow = min(BM, T.ncA - T.r0), ncol = T.c1 - T.c0;
+  const int rb = (w & 1) * 16, cb = (w >> 1) * 16;
+  // rows of this warp's fragments (pair index, or the zero row)
+  const int r_lo = rb + gid, r_hi = rb + gid + 8;
+  const int p_lo = (r_lo < nrow) ? rowpair[T.rowpair0 + T.r0 + r_lo] : npairs;
+  const int p_hi = (r_hi < nrow) ? rowpair[T.rowpair0 + T.r0 + r_hi] : npairs;
+  int fcol[2];
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt) {
+    const int j = cb + nt * 8 + gid;
+    fcol[nt] = (j < ncol) ? T.c0 + j : nf;
+  }
+  const size_t aplane = (size_t)(npairs + 1) * KP, yplane = (size_t)(nf + 1) * KP;
+  int acc[OZ_S][2][4];
+#pragma unroll
+  for (int qq = 0; qq < OZ_S; ++qq)
+#pragma unroll
+    for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+      for (int e = 0; e < 4; ++e) acc[qq][nt][e] = 0;
+  for (int k0 = 0; k0 < KP; k0 += 32) {
+    int bf[OZ_S][2][2];
+#pragma unroll
+    for (int t = 0; t < OZ_S; ++t)
+#pragma unroll
+      for (int nt = 0; nt < 2; ++nt) {
+        const signed char *yb = Ys + t * yplane + (size_t)fcol[nt] * KP + k0 + tig * 4;
+        bf[t][nt][0] = __ldg(reinterpret_cast<const int *>(yb));
+        bf[t][nt][1] = __ldg(reinterpret_cast<const int *>(yb + 16));
+      }
+#pragma unroll
+    for (int sa = 0; sa < OZ_S; ++sa) {
+      const signed char *alo = As + sa * aplane + (size_t)p_lo * KP + k0 + tig * 4;
+      const signed char *ahi = As + sa * aplane + (size_t)p_hi * KP + k0 + tig * 4;
+      const int a0 = __ldg(reinterpret_cast<const int *>(alo));
+      const int a1 = __ldg(reinterpret_cast<const int *>(ahi));
+      const int a2 = __ldg(reinterpret_cast<const int *>(alo + 16));
+      const int a3 = __ldg(reinterpret_cast<const int *>(ahi + 16));
+#pragma unroll
+      for (int t = 0; t < OZ_S - sa; ++t)
+#pragma unroll
+        for (int nt = 0; nt < 2; ++nt) mma_s8(acc[sa + t][nt], a0, a1, a2, a3, bf[t][nt][0], bf[t][nt][1]);
+    }
+  }
+  // fold the q sums in FP64, then QUAD's head/end terms and the table position
+  const int ea_lo = eA[p_lo], ea_hi = eA[p_hi];
+#pragma unroll
+  for (int nt = 0; nt < 2; ++nt)
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const int r = (e < 2) ? r_lo : r_hi;
+      const int j = cb + nt * 8 + tig * 2 + (e & 1);
+      if (r >= nrow || j >= ncol) continue;
+      const int f = T.c0 + j;
+      const int ex = ((e < 2) ? ea_lo : ea_hi) + eY[f];
+      double sum = 0.0;
+#pragma unroll
+      for (int qq = OZ_S - 1; qq >= 0; --qq) sum += scalbn((double)acc[qq][nt][e], ex - 7 * (qq + 2));
+      rk_finish(T, (e < 2) ? p_lo : p_hi, T.r0 + r, f, sum, pairs, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val,
+                nval, fb, nfb);
+    }
 }
 
 // General per-integral QUAD: TA(i) = ((P_a P_c + Q_a Q_c) RPOR) Y_f(i),
@@ -354,6 +495,68 @@ __global__ void k_quad_items(const QuadItem *__restrict__ items, const int *__re
     __syncwarp();
     if (lane == 0) out[w.pos] = quad_seq(TA, w.mtp, R, RP, q);
     __syncwarp();
+  }
+}
+
+// The same QUAD for the table's items, one warp per integral with the work
+// spread over the lanes: the head index (first i in [2, MTP-1] with
+// TA(i) != 0 and TA(i+1)/TA(i) > 0) by ballot, the 4-point panel sums
+// (quad.f90:94-99) split over the lanes and combined by a fixed butterfly,
+// so the result is deterministic. Only the order of the panel sum differs
+// from quad_seq (a few ulps of the sum of |terms|). TA values are formed
+// where they are used, so no grid size limit comes from shared memory.
+__global__ void k_quad_table(const QuadItem *__restrict__ items, const int *__restrict__ nitems_p, int nitems_max,
+                             const double *__restrict__ Y, int np, const double *__restrict__ PF,
+                             const double *__restrict__ QF, int ld, const double *__restrict__ R,
+                             const double *__restrict__ RP, const double *__restrict__ RPOR, QuadConst q,
+                             double *__restrict__ out) {
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const int nitems = min(*nitems_p, nitems_max);
+  for (int it = blockIdx.x * wpb + (threadIdx.x >> 5); it < nitems; it += gridDim.x * wpb) {
+    const QuadItem w = items[it];
+    const int mtp = w.mtp;
+    const double *Yf = Y + (size_t)w.f * np;
+    const double *Pa = PF + (size_t)(w.a - 1) * ld, *Pc = PF + (size_t)(w.c - 1) * ld;
+    const double *Qa = QF + (size_t)(w.a - 1) * ld, *Qc = QF + (size_t)(w.c - 1) * ld;
+    // TA(i) of quad.f90, zero outside [2, MTP] (the pads TA(MTP+1..MTP+3))
+    auto ta = [&](int i) -> double {
+      if (i < 2 || i > mtp) return 0.0;
+      return ((Pa[i - 1] * Pc[i - 1] + Qa[i - 1] * Qc[i - 1]) * RPOR[i]) * Yf[i];
+    };
+    int head = -1;
+    for (int i0 = 2; i0 <= mtp - 1 && head < 0; i0 += 32) {
+      const int i = i0 + lane;
+      bool hit = false;
+      if (i <= mtp - 1) {
+        const double tai = ta(i);
+        hit = !(fabs(tai) <= 0.0) && (ta(i + 1) / tai > 0.0);
+      }
+      const unsigned b = __ballot_sync(0xffffffffu, hit);
+      if (b) head = i0 + __ffs(b) - 1;
+    }
+    double s = 0.0;
+    if (head >= 0)
+      for (int j = head + 1 + 4 * lane; j <= mtp; j += 128)
+        s += q.C2 * (ta(j) + ta(j + 2)) + q.C3 * ta(j + 1) + q.C4 * ta(j + 3);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) {
+      double result = 0.0;
+      if (head >= 0) {
+        const int i = head, ip1 = i + 1;
+        const double tai = ta(i), taip1 = ta(ip1);
+        const double frip1 = taip1 / RP[ip1];
+        double fri = tai / RP[i];
+        const double sigma = log(frip1 / fri) / log(R[ip1] / R[i]);
+        fri = R[i] * fri;
+        result = fri / (sigma + 1.0);
+        result = result + q.C1 * tai;
+        result = result + s;
+        if ((mtp - i) % 4 == 0) result = result - q.C1 * ta(mtp);
+      }
+      out[w.pos] = result;
+    }
   }
 }
 
@@ -492,7 +695,7 @@ extern "C" {
 
 int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max_out) {
   GG_TRY(ensure_orbitals(ctx));
-  if (precision != GG_FP64) return fail(GG_ERR_ARG, "gg_genintrk: only GG_FP64 is implemented");
+  if (precision != GG_FP64 && precision != GG_SPLIT) return fail(GG_ERR_ARG, "gg_genintrk: unknown precision");
   GG_CUDA(cudaSetDevice(ctx->device));
   Grid &g = ctx->grid;
   Orbitals &o = ctx->orb;
@@ -615,7 +818,22 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   GG_TRY(dFb.alloc(std::max<int64_t>(N, 1)));
   GG_TRY(dNfb.alloc(2));  // [0] fallback count, [1] position error flag
   GG_CUDA(cudaMemsetAsync(dNfb.p, 0, 2 * sizeof(int), ctx->stream));
-  if (!tiles.empty()) {
+  DBuf<signed char> dAs, dYs;
+  DBuf<int> dEA, dEY;
+  if (!tiles.empty() && precision == GG_SPLIT) {
+    // tensor-core contraction on int8 slices of A and Y (k_oz_split, k_rk_ozaki)
+    const int KP = (KC + 31) / 32 * 32;
+    GG_TRY(dAs.alloc((size_t)OZ_S * (npairs + 1) * KP));
+    GG_TRY(dYs.alloc((size_t)OZ_S * (nf + 1) * KP));
+    GG_TRY(dEA.alloc(npairs + 1));
+    GG_TRY(dEY.alloc(nf + 1));
+    k_oz_split<<<npairs + 1, 128, 0, ctx->stream>>>(dA.p, npairs, KC, KC, KP, dAs.p, dEA.p); ::gg::note_launch();
+    k_oz_split<<<nf + 1, 128, 0, ctx->stream>>>(dY.p, nf, np, KC, KP, dYs.p, dEY.p); ::gg::note_launch();
+    k_rk_ozaki<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(
+        dTiles.p, dRowpair.p, dPairs.p, dAs.p, dEA.p, npairs, dYs.p, dEY.p, nf, KP, dY.p, dYd.p, np, o.dPF.p, o.dQF.p,
+        o.ld, o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p); ::gg::note_launch();
+    GG_CUDA(cudaGetLastError());
+  } else if (!tiles.empty()) {
     k_rk_gemm<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(dTiles.p, dRowpair.p, dPairs.p, dA.p, dY.p, dYd.p, KC,
                                                               np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p,
                                                               g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p); ::gg::note_launch();
@@ -626,11 +844,11 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (hfb[1]) return fail(GG_ERR_STATE, "genintrk: contraction produced a table position out of range");
   const int nfb = hfb[0];
+  ctx->stats[20] = nfb;
   if (nfb > 0) {
-    const int wpb = 4;
-    const size_t smem = (size_t)wpb * np * sizeof(double);
-    const int blocks = std::min((nfb + wpb - 1) / wpb, 4096);
-    k_quad_items<<<blocks, 32 * wpb, smem, ctx->stream>>>(dFb.p, dNfb.p, nfb, dY.p, np, o.dPF.p, o.dQF.p, o.ld, g.dR.p,
+    const int wpb = 8;
+    const int blocks = std::min((nfb + wpb - 1) / wpb, 8 * ctx->sms);
+    k_quad_table<<<blocks, 32 * wpb, 0, ctx->stream>>>(dFb.p, dNfb.p, nfb, dY.p, np, o.dPF.p, o.dQF.p, o.ld, g.dR.p,
                                                           g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }

@@ -5,6 +5,7 @@ kernel family it is named for, a few times:
   python -m grasp_gb300.profile_targets spmv     # 3 full-size y = H x launches per precision
   python -m grasp_gb300.profile_targets solve    # one full CI solve (launch list)
   python -m grasp_gb300.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
+  python -m grasp_gb300.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
 """
 from __future__ import annotations
 
@@ -40,16 +41,20 @@ def solve():
     print("loops", info["nloops"], "E0", ev[0])
 
 
-def rk():
+def rk(precision=0):
     from . import Context, workloads
     w = workloads.rk40()
     ctx = Context(0)
     ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
     ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
     for _ in range(3):
-        n, _ = ctx.genintrk(kmax=8)
+        n, _ = ctx.genintrk(kmax=8, precision=precision)
     print("R^k integrals", n, "ms", ctx.stage_stat(0))
 
 
+def rk_split():
+    rk(precision=1)
+
+
 if __name__ == "__main__":
-    {"spmv": spmv, "solve": solve, "rk": rk}[sys.argv[1]]()
+    {"spmv": spmv, "solve": solve, "rk": rk, "rk_split": rk_split}[sys.argv[1]]()

@@ -79,7 +79,11 @@ int gg_set_orbitals(gg_ctx *ctx, int nw, int ld, const int *nak, const int *mf, 
  * GENINTRK (rci90/genintrk.f90:3, loop :67-86): all R^k(ab;cd) with
  * a<=b, a<=c, b<=d and TRIANGRK(l_a,k,l_c) & TRIANGRK(l_b,k,l_d), for
  * k = 0..J2MAX (kmax < 0) or k = 0..kmax. The table stays on the device.
- * precision: GG_FP64 (FP64 contraction).                                   */
+ * precision: GG_FP64: FP64 contraction on the CUDA cores; GG_SPLIT: the
+ * contraction on the int8 tensor cores, A and Y each split into 10 signed
+ * 7-bit slices under a per-row power-of-two scale (Ozaki scheme), the exact
+ * int32 slice products summed in FP64 (relative error ~1e-13 of the row
+ * scales' product); the QUAD head term and end correction stay FP64.     */
 int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max_out);
 /* Copies INDTEIRK (int32, packed ((a*KEY+b)*KEY+c)*KEY+d, KEY = NW+1),
  * VALTEIRK (double) and KSTART(0:kloop+1) (1-based positions). Any pointer
@@ -195,7 +199,9 @@ int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double 
  * projected eigenproblems, 14 host ms waiting for device results, 15 host ms
  * inside both Davidson runs, 16 device ms of the full-block single-vector
  * passes, 17 / 18 host ms of the leading-block / full-block Davidson run,
- * 19 host ms of the full-block projected eigenproblems.                    */
+ * 19 host ms of the full-block projected eigenproblems, 20 number of R^k
+ * table entries the last genintrk evaluated with the general QUAD (head
+ * index above 2).                                                          */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* ---- measurement helpers (no counterpart in the reference) ------------------

@@ -60,11 +60,34 @@ def test_genintrk_kmax8_40orbitals(gpu_ready, oracle_mod):
     ind0, val0, ks0, _ = o.genintrk(kmax=8, nthreads=16)
     ctx = gpu_ctx(case)
     n, _ = ctx.genintrk(kmax=8)
+    # entries whose QUAD head index is above 2 take the warp-parallel general
+    # QUAD (k_quad_table); this workload has thousands of them
+    assert ctx.stage_stat(20) > 1000
     ind, val, ks = ctx.rk_table()
     np.testing.assert_array_equal(ind, ind0)
     err = np.abs(val - val0)
     rel = err / np.maximum(np.abs(val0), RK_ATOL / RK_RTOL)
     assert rel.max() <= RK_RTOL, (float(rel.max()), int(np.argmax(rel)))
+
+
+@pytest.mark.parametrize("nmax,lmax,z,sig,kmax,kapmax", [(4, 3, 10.0, None, -1, None),
+                                                         (5, 3, 26.0, "random", -1, None),
+                                                         (7, 4, 26.0, "random", 8, 4)])
+def test_genintrk_tensor_core_split(gpu_ready, oracle_mod, nmax, lmax, z, sig, kmax, kapmax):
+    """GG_SPLIT: the contraction on int8 slices with int32 tensor-core sums
+    (Ozaki split, 10 slices of 7 bits per row) meets the same bar as FP64:
+    <= 1e-12 relative with a 1e-14 absolute floor; indices bit-exact."""
+    case = hydrogenic_case(nmax=nmax, lmax=lmax, z=z, sigma=sig, seed=2024, kappa_max=kapmax)
+    o = oracle_for(case)
+    ind0, val0, ks0, _ = o.genintrk(kmax=kmax, nthreads=16)
+    ctx = gpu_ctx(case)
+    ctx.genintrk(kmax=kmax, precision=1)
+    ind, val, ks = ctx.rk_table()
+    np.testing.assert_array_equal(ind, ind0)
+    np.testing.assert_array_equal(ks, ks0)
+    err = np.abs(val - val0)
+    bad = err > RK_RTOL * np.abs(val0) + RK_ATOL
+    assert not bad.any(), (int(bad.sum()), float((err / np.maximum(np.abs(val0), 1e-300)).max()))
 
 
 def test_slater_rkintc_rinti(gpu_ready, oracle_mod):
