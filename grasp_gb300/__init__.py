@@ -9,7 +9,7 @@ Layout:
   formats.py  GRASP file formats (Fortran unformatted records)
   build.py    nvcc build recipe (sm_103a)
 """
-from .core import FP64, SPLIT, Context, HMatrix  # noqa: F401
+from .core import FP64, SPLIT, Context, HMatrix, maneig_batched  # noqa: F401
 from ._lib import GGError  # noqa: F401
 
-__all__ = ["Context", "HMatrix", "GGError", "FP64", "SPLIT"]
+__all__ = ["Context", "HMatrix", "GGError", "FP64", "SPLIT", "maneig_batched"]

@@ -66,6 +66,8 @@ GPU_SYMBOLS = {
     "gg_hmat_set_emt": (C.c_int, [C.c_void_p, _d]),
     "gg_spicmv2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, _d, _d, C.c_int]),
     "gg_maneig": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(GGDvdParams), _d, _d, _int, _int, _int]),
+    "gg_maneig_batched": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), _int, C.POINTER(GGDvdParams), _d,
+                                    _d, _int, _int, _int]),
     "gg_stage_stat": (C.c_double, [C.c_void_p, C.c_int]),
     "gg_launch_count": (C.c_longlong, []),
     "gg_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),

@@ -218,6 +218,36 @@ class HMatrix:
         return ms.value, by.value
 
 
+def maneig_batched(ctx, hmats, nvec, precision=FP64, lim=0, maxiter=0, critr=0.0, raise_on_maxiter=True):
+    """MANEIG for many blocks in one batched GPU Davidson (gg_maneig_batched).
+
+    The reference calls MANEIG once per J/parity block from its block loop
+    (rci90/matrix.f90:177-187). ``hmats`` are assembled HMatrix objects (any
+    contexts of one device), ``nvec`` the roots per block (an int or one per
+    block). Returns ``[(eval, evec), ...]`` per block (evec columns are the
+    eigenvectors, dominant component positive) and the per-block
+    ``nloops``, ``nmv`` and ``ierr`` arrays."""
+    nb = len(hmats)
+    nv = np.full(nb, nvec, np.int32) if np.isscalar(nvec) else np.ascontiguousarray(nvec, np.int32)
+    ncf = np.array([h.ncf for h in hmats], np.int64)
+    ev = np.zeros(int(nv.sum()))
+    vec = np.zeros(int((ncf * nv).sum()))
+    hs = (C.c_void_p * nb)(*[h._h.value for h in hmats])
+    nl, nm, ie = (np.zeros(nb, np.int32) for _ in range(3))
+    p = GGDvdParams(0, precision, lim, maxiter, critr, 0.0, 0.0, 0)
+    st = _lib.gpu().gg_maneig_batched(ctx._h, nb, hs, ptr(nv, _int), C.byref(p), ptr(ev, _d), ptr(vec, _d),
+                                      ptr(nl, _int), ptr(nm, _int), ptr(ie, _int))
+    if st != 0 and (raise_on_maxiter or st != _lib_status("GG_ERR_CONVERGE")):
+        check(st)
+    out, eo, vo = [], 0, 0
+    for b in range(nb):
+        r, n = int(nv[b]), int(ncf[b])
+        out.append((ev[eo:eo + r].copy(), vec[vo:vo + n * r].reshape(r, n).T.copy()))
+        eo += r
+        vo += n * r
+    return out, dict(nloops=nl, nmv=nm, ierr=ie, status=st)
+
+
 def _lib_status(name):
     return {"GG_ERR_CONVERGE": -7}[name]
 

@@ -6,6 +6,7 @@ kernel family it is named for, a few times:
   python -m grasp_gb300.profile_targets solve    # one full CI solve (launch list)
   python -m grasp_gb300.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
   python -m grasp_gb300.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
+  python -m grasp_gb300.profile_targets batch    # two batched solves of the 310-block workload (split)
 """
 from __future__ import annotations
 
@@ -56,5 +57,15 @@ def rk_split():
     rk(precision=1)
 
 
+def batch():
+    from . import SPLIT, Context, maneig_batched, workloads
+    w = workloads.batch()
+    ctx = Context(0)
+    hs = workloads.assemble_batch(w, ctx)
+    for _ in range(2):
+        res, info = maneig_batched(ctx, hs, w.nroots, precision=SPLIT)
+    print("blocks", len(hs), "iterations", ctx.stage_stat(21), "ms", ctx.stage_stat(3))
+
+
 if __name__ == "__main__":
-    {"spmv": spmv, "solve": solve, "rk": rk, "rk_split": rk_split}[sys.argv[1]]()
+    {"spmv": spmv, "solve": solve, "rk": rk, "rk_split": rk_split, "batch": batch}[sys.argv[1]]()

@@ -18,6 +18,11 @@ Sizes versus the workload descriptions they stand in for:
         (2 % by default).
   rk40  The R^k table workload: n <= 7, |kappa| <= 4 (40 orbitals), Z = 26,
         screening drawn U[0, Z-1] from the seed, k = 0..8.
+  batch The ne7 expansion for every ion Z = 10..40 (31 ions) and every
+        2J = 0, 2, 4, 6, 8 of both parities: 310 blocks of 321-1007 CSFs
+        (7,027 CSFs and 1.04 M stored elements per ion), 3 roots each. The
+        angular lists depend on the CSFs only, so each (J, parity) block's
+        T/V lists are generated once and assembled with every ion's orbitals.
 """
 from __future__ import annotations
 
@@ -96,3 +101,56 @@ def rk40(seed=2024):
     sig = np.random.default_rng(seed).uniform(0.0, z - 1.0, size=len(orbs))
     n, rnt, ob = _orbitals(orbs, z, sig)
     return Workload("rk_table_40orb_k8", z, orbs, n, rnt, 0.05, S.CVAC, np.full(n, z), ob, None, 0, kmax=8)
+
+
+@dataclass
+class BatchWorkload:
+    name: str
+    zs: list
+    orbs: list
+    blocks: list        # [(two_j, parity, CIBlock)] shared by every ion
+    nroots: int
+
+    def describe(self):
+        ncf = [b.ncf for _, _, b in self.blocks]
+        return dict(workload=self.name, ions=len(self.zs), blocks=len(self.zs) * len(self.blocks),
+                    ncf_min=min(ncf), ncf_max=max(ncf), ncf_total=len(self.zs) * sum(ncf),
+                    nnz_total=len(self.zs) * sum(b.nnz for _, _, b in self.blocks), nroots=self.nroots)
+
+    def ion(self, z):
+        """(n, rnt, orbitals) of ion Z on its own grid (RNT = 2e-6/Z)."""
+        return _orbitals(self.orbs, float(z), S.screenpar([k for _, k in self.orbs], 1))
+
+
+def batch(zs=tuple(range(10, 41)), two_js=(0, 2, 4, 6, 8), parities=(0, 1), max_ncf=0, seed=3, nroots=3):
+    orbs = S.orbital_set(4, 3)
+
+    def occ(d):
+        return S.occupation(orbs, d)
+    refs = [occ({(1, -1): 2, (2, -1): 2}), occ({(1, -1): 2, (2, 1): 2}), occ({(1, -1): 2, (2, 1): 1, (2, -2): 1}),
+            occ({(1, -1): 2, (2, -2): 2})]
+    blocks = []
+    for par in parities:
+        for tj in two_js:
+            blocks.append((tj, par, S.ci_block(orbs, refs, [0] * len(orbs), two_j=tj, parity=par, max_ncf=max_ncf,
+                                               seed=seed)))
+    return BatchWorkload(f"ne_like_{len(zs)}ions_{len(zs) * len(blocks)}blocks", list(zs), orbs, blocks, nroots)
+
+
+def assemble_batch(w, ctx):
+    """All blocks of all ions on one context: per ion the grid, orbitals,
+    R^k and I(ab) tables, then SETHAM of each block. Returns the HMatrix
+    objects in (ion, block) order."""
+    from . import HMatrix
+    hs = []
+    for z in w.zs:
+        n, rnt, ob = w.ion(z)
+        ctx.set_grid(n, rnt, 0.05, S.CVAC, np.full(n, float(z)))
+        ctx.set_orbitals(ob.nak, ob.mf, ob.pf, ob.qf)
+        ctx.genintrk()
+        ctx.iabint_table()
+        for _, _, b in w.blocks:
+            H = HMatrix(ctx, b.ncf, b.iendc, b.irow)
+            H.setham(b.iq, b.tlist, b.vlists)
+            hs.append(H)
+    return hs

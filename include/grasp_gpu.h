@@ -189,6 +189,27 @@ typedef struct {
 int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double *eval, double *evec,
               int *nloops, int *nmv, int *ierr);
 
+/* ---- MANEIG over many blocks ---------------------------------------------
+ * Replaces the per-block MANEIG calls of rci's block loop
+ * (rci90/matrix.f90:177-187 -> rci90/maneig.f90:3) for nblocks blocks at
+ * once: all blocks run one batched Davidson on the device (every step of the
+ * iteration, including the projected eigenproblems, is a GPU kernel over all
+ * blocks; the iteration is one CUDA graph). Block b asks for its lowest
+ * nvec[b] (1..16, <= NCF) eigenpairs of its assembled matrix (EMT - EAV, as
+ * MANEIG). p (may be NULL): precision (GG_FP64 / GG_SPLIT matvec), lim (LIM,
+ * default min(NCF, 2 NVEC + 60), at most 128), maxiter (default
+ * max(200 NVEC, NCF/10)), critr (residual norm, default 1e-9); flavour,
+ * critc, crite and robust are not used. Blocks may come from different
+ * contexts of the same device.
+ * eval: all blocks' eigenvalues, concatenated (sum of nvec). evec (may be
+ * NULL): all blocks' eigenvectors, concatenated, block b column-major
+ * NCF_b x nvec[b], dominant component positive (rci90/maneig.f90:532-555).
+ * nloops, nmv, ierr (may be NULL): per block; ierr bit 2048 = MAXITER
+ * reached, then GG_ERR_CONVERGE is returned (results are still written).
+ * Blocks with NCF <= LIM are solved exactly in the full unit basis.         */
+int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nvec, const gg_dvd_params *p,
+                      double *eval, double *evec, int *nloops, int *nmv, int *ierr);
+
 /* ---- timing --------------------------------------------------------------
  * Device time (ms, CUDA events on the context stream) of the named stage of
  * the last call: 0 genintrk, 1 iabint, 2 setham assemble, 3 maneig total,
@@ -201,7 +222,9 @@ int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double 
  * passes, 17 / 18 host ms of the leading-block / full-block Davidson run,
  * 19 host ms of the full-block projected eigenproblems, 20 number of R^k
  * table entries the last genintrk evaluated with the general QUAD (head
- * index above 2).                                                          */
+ * index above 2), 21 iterations of the last gg_maneig_batched (all blocks
+ * together), 22 kernels per batched iteration (stage 3 is the batched
+ * solve's total ms).                                                       */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* ---- measurement helpers (no counterpart in the reference) ------------------
