@@ -172,7 +172,7 @@ __device__ void inv_iter_dev(int n, const double *d, const double *e, double lam
     s ^= s << 5;
     x[i] = (double)(s & 0xffff) / 65536.0 - 0.5 + 1e-3;
   }
-  for (int it = 0; it < 3; ++it) {
+  for (int it = 0; it < 2; ++it) {
     for (int i = 0; i + 1 < n; ++i) {
       if (piv[i]) {
         const double t = x[i];
@@ -214,7 +214,7 @@ __device__ __forceinline__ int sturm64(int m, const double *dd, const double *e2
   int cnt = (q < 0.0);
   for (int i = 1; i < m; ++i) {
     const double ei2 = e2[i - 1];
-    double qi = (dd[i] - x) - ei2 * inv;
+    double qi = fma(-ei2, inv, dd[i] - x);
     qi = (fabs(qi) < pivmin) ? -pivmin : qi;
     const double dq = fma(ei2 * qp, inv * inv, -1.0);
     const double iv = 1.0 / qi;
@@ -553,6 +553,52 @@ __global__ void __launch_bounds__(EIG_T) k_b_eig(const BDesc *__restrict__ desc,
 // Tall-skinny kernels over row tiles of all blocks.
 // ---------------------------------------------------------------------------
 
+// One thread per row: x_j = V(i, 0:m) y_j, u_j = W(i, 0:m) y_j, the residual
+// u_j - theta_j x_j, and the tile's |R_j|^2 partials in a fixed order. NR is
+// r rounded up to an instantiated size; GB300 issues FP64 slowly, so no FMA
+// is spent on unused columns.
+template <int NR>
+__device__ __forceinline__ void ritz_rows(const BDesc &D, const BTile &T, const BState &S, bool row,
+                                          const double *__restrict__ V, const double *__restrict__ W,
+                                          const double *Ys, double *__restrict__ X, double *__restrict__ R,
+                                          double *red, double *__restrict__ part, int r) {
+  const int m = S.m, n = D.n, i = T.r0 + threadIdx.x;
+  double x[NR], u[NR];
+#pragma unroll
+  for (int j = 0; j < NR; ++j) x[j] = u[j] = 0.0;
+  if (row) {
+    const double *Vi = V + D.voff + i, *Wi = W + D.voff + i;
+#pragma unroll 4
+    for (int k = 0; k < m; ++k) {
+      const double v = Vi[(size_t)k * n], w = Wi[(size_t)k * n];
+#pragma unroll
+      for (int j = 0; j < NR; ++j)
+        if (j < r) {
+          x[j] = fma(v, Ys[k * r + j], x[j]);
+          u[j] = fma(w, Ys[k * r + j], u[j]);
+        }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < NR; ++j) {
+    if (j >= r) break;
+    double res = 0.0;
+    if (row) {
+      res = fma(-S.theta[j], x[j], u[j]);
+      X[D.xoff + (size_t)j * n + i] = x[j];
+      R[D.xoff + (size_t)j * n + i] = res;
+    }
+    red[threadIdx.x] = res * res;
+    __syncthreads();
+    for (int h = RT / 2; h > 0; h >>= 1) {
+      if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[j] = red[0];
+    __syncthreads();
+  }
+}
+
 // Ritz vectors and residuals of the r targets, |R_j|^2 partials per tile
 __global__ void __launch_bounds__(RT) k_b_ritz(const BTile *__restrict__ tiles, const BDesc *__restrict__ desc,
                                                const BState *__restrict__ st, const double *__restrict__ V,
@@ -563,7 +609,7 @@ __global__ void __launch_bounds__(RT) k_b_ritz(const BTile *__restrict__ tiles, 
   const BState &S = st[T.b];
   if (!S.active) return;
   const BDesc D = desc[T.b];
-  const int m = S.m, r = D.r, n = D.n, L = D.lim;
+  const int m = S.m, r = D.r, L = D.lim;
   __shared__ double Ys[MAXL * MAXR];
   __shared__ double red[RT];
   const double *Yb = Ypool + D.soff;
@@ -572,41 +618,17 @@ __global__ void __launch_bounds__(RT) k_b_ritz(const BTile *__restrict__ tiles, 
     Ys[idx] = Yb[(size_t)j * L + k];  // Ys[k * r + j]
   }
   __syncthreads();
-  const int i = T.r0 + threadIdx.x;
   const bool row = threadIdx.x < T.nr;
-  double x[MAXR], u[MAXR];
-#pragma unroll
-  for (int j = 0; j < MAXR; ++j) x[j] = u[j] = 0.0;
-  if (row) {
-    const double *Vi = V + D.voff + i, *Wi = W + D.voff + i;
-#pragma unroll 4
-    for (int k = 0; k < m; ++k) {
-      const double v = Vi[(size_t)k * n], w = Wi[(size_t)k * n];
-#pragma unroll
-      for (int j = 0; j < MAXR; ++j)
-        if (j < r) {
-          x[j] = fma(v, Ys[k * r + j], x[j]);
-          u[j] = fma(w, Ys[k * r + j], u[j]);
-        }
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < MAXR; ++j) {
-    if (j >= r) break;
-    double res = 0.0;
-    if (row) {
-      res = u[j] - S.theta[j] * x[j];
-      X[D.xoff + (size_t)j * n + i] = x[j];
-      R[D.xoff + (size_t)j * n + i] = res;
-    }
-    red[threadIdx.x] = res * res;
-    __syncthreads();
-    for (int h = RT / 2; h > 0; h >>= 1) {
-      if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) part[(size_t)blockIdx.x * ps + j] = red[0];
-    __syncthreads();
+  switch (r) {
+    case 1: ritz_rows<1>(D, T, S, row, V, W, Ys, X, R, red, part + (size_t)blockIdx.x * ps, r); break;
+    case 2: ritz_rows<2>(D, T, S, row, V, W, Ys, X, R, red, part + (size_t)blockIdx.x * ps, r); break;
+    case 3: ritz_rows<3>(D, T, S, row, V, W, Ys, X, R, red, part + (size_t)blockIdx.x * ps, r); break;
+    case 4: ritz_rows<4>(D, T, S, row, V, W, Ys, X, R, red, part + (size_t)blockIdx.x * ps, r); break;
+    case 5:
+    case 6: ritz_rows<6>(D, T, S, row, V, W, Ys, X, R, red, part + (size_t)blockIdx.x * ps, r); break;
+    case 7:
+    case 8: ritz_rows<8>(D, T, S, row, V, W, Ys, X, R, red, part + (size_t)blockIdx.x * ps, r); break;
+    default: ritz_rows<MAXR>(D, T, S, row, V, W, Ys, X, R, red, part + (size_t)blockIdx.x * ps, r); break;
   }
 }
 
@@ -894,6 +916,24 @@ __global__ void __launch_bounds__(256) k_b_colsum(const BDesc *__restrict__ desc
   }
 }
 
+// one row of V(:, m+q) -= V(:, 0:m) C(:, q), q < nb <= NB
+template <int NB>
+__device__ __forceinline__ void sub_row(double *Vi, int m, int n, const double *Cs, int nb) {
+  double acc[NB];
+#pragma unroll
+  for (int q = 0; q < NB; ++q) acc[q] = 0.0;
+#pragma unroll 4
+  for (int a = 0; a < m; ++a) {
+    const double v = Vi[(size_t)a * n];
+#pragma unroll
+    for (int q = 0; q < NB; ++q)
+      if (q < nb) acc[q] = fma(v, Cs[a * nb + q], acc[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < NB; ++q)
+    if (q < nb) Vi[(size_t)(m + q) * n] -= acc[q];
+}
+
 // new columns minus their projections: V(:, m+q) -= V(:, 0:m) C(:, q)
 __global__ void __launch_bounds__(RT) k_b_sub(const BTile *__restrict__ tiles, const BDesc *__restrict__ desc,
                                               const BState *__restrict__ st, double *__restrict__ V,
@@ -910,21 +950,18 @@ __global__ void __launch_bounds__(RT) k_b_sub(const BTile *__restrict__ tiles, c
   for (int idx = threadIdx.x; idx < m * nb; idx += RT) Cs[idx] = C[idx];
   __syncthreads();
   if (threadIdx.x >= T.nr) return;
-  const int i = T.r0 + threadIdx.x;
-  double *Vi = V + D.voff + i;
-  double acc[MAXR];
-#pragma unroll
-  for (int q = 0; q < MAXR; ++q) acc[q] = 0.0;
-#pragma unroll 4
-  for (int a = 0; a < m; ++a) {
-    const double v = Vi[(size_t)a * n];
-#pragma unroll
-    for (int q = 0; q < MAXR; ++q)
-      if (q < nb) acc[q] = fma(v, Cs[a * nb + q], acc[q]);
+  double *Vi = V + D.voff + T.r0 + threadIdx.x;
+  switch (nb) {
+    case 1: sub_row<1>(Vi, m, n, Cs, nb); break;
+    case 2: sub_row<2>(Vi, m, n, Cs, nb); break;
+    case 3: sub_row<3>(Vi, m, n, Cs, nb); break;
+    case 4: sub_row<4>(Vi, m, n, Cs, nb); break;
+    case 5:
+    case 6: sub_row<6>(Vi, m, n, Cs, nb); break;
+    case 7:
+    case 8: sub_row<8>(Vi, m, n, Cs, nb); break;
+    default: sub_row<MAXR>(Vi, m, n, Cs, nb); break;
   }
-#pragma unroll
-  for (int q = 0; q < MAXR; ++q)
-    if (q < nb) Vi[(size_t)(m + q) * n] -= acc[q];
 }
 
 // kept orthonormal new columns: V(:, m+c) = sum_q V_old(:, m+q) C[q][c]
@@ -1003,65 +1040,89 @@ __device__ __forceinline__ dfl df_add(dfl a, dfl b) {
 }
 
 // One row of W(:, m+q0 : m+q0+NQ) = H V(...): a warp over the row's entries,
-// x gathered from shared memory (staged) or from the row-major copy.
-template <bool SPLIT, int NQ>
-__device__ __forceinline__ void spmm_row(const BDesc &D, int i, int m, int q0, int lane, bool staged,
-                                         const X32 *__restrict__ smx, const char *__restrict__ gx, size_t gstride,
-                                         const double *__restrict__ V, double *__restrict__ W) {
-  const int64_t p0 = D.ptr[i], p1 = D.ptr[i + 1];
+// x gathered from shared memory (staged) or from the row-major copy. After
+// the cross-lane sums every lane holds every column's total, and lane q
+// finishes column q, so the FP64 epilogue is one warp instruction for all
+// columns (GB300 charges FP64 issue per warp instruction).
+template <int NQ>
+__device__ __forceinline__ void spmm_row_split(const BDesc &D, int i, int64_t p0, int64_t p1, int m, int q0, int lane,
+                                               bool staged, const X32 *__restrict__ smx,
+                                               const char *__restrict__ gx, size_t gstride,
+                                               const double *__restrict__ V, double *__restrict__ W) {
   const int n = D.n;
-  if (!SPLIT) {
-    double acc[NQ];
+  float sh[NQ], sl[NQ];
 #pragma unroll
-    for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
-#pragma unroll 4
-    for (int64_t p = p0 + lane; p < p1; p += 32) {
-      const double v = __ldg(D.val + p);
-      const int c = D.col16 ? (int)__ldg(D.col16 + p) : __ldg(D.col + p);
-      const double *xr = staged ? reinterpret_cast<const double *>(smx + c)
-                                : reinterpret_cast<const double *>(gx + c * gstride);
-#pragma unroll
-      for (int q = 0; q < NQ; ++q) acc[q] = fma(v, xr[q], acc[q]);
-    }
+  for (int q = 0; q < NQ; ++q) sh[q] = sl[q] = 0.f;
+  auto add = [&](float ah, float al, int c) {
+    const float2 *xr = staged ? reinterpret_cast<const float2 *>(smx + c)
+                              : reinterpret_cast<const float2 *>(gx + c * gstride);
 #pragma unroll
     for (int q = 0; q < NQ; ++q) {
-      const double t = warp_sum(acc[q]);
-      if (lane == 0) W[D.voff + (size_t)(m + q0 + q) * n + i] = t;
+      // Dot2 (Ogita, Rump & Oishi, SIAM J. Sci. Comput. 26 (2005) 1955): the
+      // running sum takes each product's high part through an error-free
+      // TwoSum; rounding errors and the products' low parts gather in sl
+      const float2 x = xr[q];
+      const float ph = __fmul_rn(ah, x.x);
+      const float t = fmaf(ah, x.y, fmaf(al, x.x, fmaf(ah, x.x, -ph)));
+      const float s = __fadd_rn(sh[q], ph);
+      const float bb = __fsub_rn(s, sh[q]);
+      const float err = __fadd_rn(__fsub_rn(sh[q], __fsub_rn(s, bb)), __fsub_rn(ph, bb));
+      sh[q] = s;
+      sl[q] = __fadd_rn(sl[q], __fadd_rn(err, t));
     }
-  } else {
-    dfl acc[NQ];
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) acc[q] = {0.f, 0.f};
+  };
 #pragma unroll 4
-    for (int64_t p = p0 + lane; p < p1; p += 32) {
-      const float ah = __ldg(D.hi + p), al = __ldg(D.lo + p);
-      const int c = D.col16 ? (int)__ldg(D.col16 + p) : __ldg(D.col + p);
-      const float2 *xr = staged ? reinterpret_cast<const float2 *>(smx + c)
-                                : reinterpret_cast<const float2 *>(gx + c * gstride);
+  for (int64_t p = p0 + lane; p < p1; p += 32)
+    add(__ldg(D.hi + p), __ldg(D.lo + p), D.col16 ? (int)__ldg(D.col16 + p) : __ldg(D.col + p));
+  float h = 0.f, l = 0.f;
 #pragma unroll
-      for (int q = 0; q < NQ; ++q) {
-        const float2 x = xr[q];
-        const float ph = __fmul_rn(ah, x.x);
-        const float pe = fmaf(ah, x.x, -ph);
-        const float cross = fmaf(ah, x.y, fmaf(al, x.x, pe));
-        acc[q] = df_add(acc[q], two_sum(ph, cross));
-      }
+  for (int q = 0; q < NQ; ++q) {
+    dfl acc = two_sum(sh[q], sl[q]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      dfl other;
+      other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
+      other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
+      acc = df_add(acc, other);
     }
-#pragma unroll
-    for (int q = 0; q < NQ; ++q) {
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        dfl other;
-        other.h = __shfl_xor_sync(0xffffffffu, acc[q].h, o);
-        other.l = __shfl_xor_sync(0xffffffffu, acc[q].l, o);
-        acc[q] = df_add(acc[q], other);
-      }
-      if (lane == 0) {
-        const size_t o = D.voff + (size_t)(m + q0 + q) * n + i;
-        W[o] = ((double)acc[q].h + (double)acc[q].l) + D.diag[i] * V[o];
-      }
+    if (lane == q) {
+      h = acc.h;
+      l = acc.l;
     }
   }
+  if (lane < NQ) {
+    const size_t o = D.voff + (size_t)(m + q0 + lane) * n + i;
+    W[o] = ((double)h + (double)l) + D.diag[i] * V[o];
+  }
+}
+
+// FP64 form: one DFMA per entry and column; each column's sum is reduced
+// across the warp and lane q writes column q.
+template <int NQ>
+__device__ __forceinline__ void spmm_row_fp64(const BDesc &D, int i, int64_t p0, int64_t p1, int m, int q0, int lane,
+                                              bool staged, const X32 *__restrict__ smx,
+                                              const char *__restrict__ gx, size_t gstride,
+                                              double *__restrict__ W) {
+  const int n = D.n;
+  double acc[NQ];
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) acc[q] = 0.0;
+#pragma unroll 4
+  for (int64_t p = p0 + lane; p < p1; p += 32) {
+    const double v = __ldg(D.val + p);
+    const int c = D.col16 ? (int)__ldg(D.col16 + p) : __ldg(D.col + p);
+    const double *xr = staged ? reinterpret_cast<const double *>(smx + c)
+                              : reinterpret_cast<const double *>(gx + c * gstride);
+#pragma unroll
+    for (int q = 0; q < NQ; ++q) acc[q] = fma(v, xr[q], acc[q]);
+  }
+  double t = 0.0;
+#pragma unroll
+  for (int q = 0; q < NQ; ++q) {
+    const double sq = warp_sum(acc[q]);
+    if (lane == q) t = sq;
+  }
+  if (lane < NQ) W[D.voff + (size_t)(m + q0 + lane) * n + i] = t;
 }
 
 // W(:, m:m+c) = H V(:, m:m+c) for every block. One CTA per row tile, one
@@ -1095,14 +1156,37 @@ __global__ void __launch_bounds__(256) k_b_spmm(const BTile *__restrict__ tiles,
       __syncthreads();
     }
     const int nq = min(4, nc - q0);
-    for (int rr = warp; rr < T.nr; rr += blockDim.x / 32) {
+    const int step = blockDim.x / 32;
+    int64_t p0 = 0, p1 = 0;
+    if (warp < T.nr) {
+      p0 = D.ptr[T.r0 + warp];
+      p1 = D.ptr[T.r0 + warp + 1];
+    }
+    for (int rr = warp; rr < T.nr; rr += step) {
       const int i = T.r0 + rr;
-      switch (nq) {
-        case 1: spmm_row<SPLIT, 1>(D, i, m, q0, lane, staged, smx, gx, gstride, V, W); break;
-        case 2: spmm_row<SPLIT, 2>(D, i, m, q0, lane, staged, smx, gx, gstride, V, W); break;
-        case 3: spmm_row<SPLIT, 3>(D, i, m, q0, lane, staged, smx, gx, gstride, V, W); break;
-        default: spmm_row<SPLIT, 4>(D, i, m, q0, lane, staged, smx, gx, gstride, V, W); break;
+      // the next row's bounds are fetched before this row's work
+      int64_t n0 = 0, n1 = 0;
+      if (rr + step < T.nr) {
+        n0 = D.ptr[i + step];
+        n1 = D.ptr[i + step + 1];
       }
+      if (SPLIT) {
+        switch (nq) {
+          case 1: spmm_row_split<1>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, V, W); break;
+          case 2: spmm_row_split<2>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, V, W); break;
+          case 3: spmm_row_split<3>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, V, W); break;
+          default: spmm_row_split<4>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, V, W); break;
+        }
+      } else {
+        switch (nq) {
+          case 1: spmm_row_fp64<1>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, W); break;
+          case 2: spmm_row_fp64<2>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, W); break;
+          case 3: spmm_row_fp64<3>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, W); break;
+          default: spmm_row_fp64<4>(D, i, p0, p1, m, q0, lane, staged, smx, gx, gstride, W); break;
+        }
+      }
+      p0 = n0;
+      p1 = n1;
     }
   }
 }
@@ -1157,49 +1241,95 @@ struct BatchRun {
     if (gexec) cudaGraphExecDestroy(gexec);
     if (graph) cudaGraphDestroy(graph);
     if (hNact) cudaFreeHost(hNact);
+    if (evFork) cudaEventDestroy(evFork);
+    if (evJoin) cudaEventDestroy(evJoin);
+    if (s2) cudaStreamDestroy(s2);
   }
+
+  // a contiguous range of blocks and their tiles
+  struct Group {
+    int b0 = 0, nb = 0, t0 = 0, nt = 0;
+  };
+  Group all, grp[2];
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t evFork = nullptr, evJoin = nullptr;
 
   // the kernels that add the new columns [m, m + ncur) to the basis: matvec
   // and S update
-  int enqueue_expand(cudaStream_t s, int *count) {
+  int enqueue_expand(cudaStream_t s, const Group &g, int *count) {
+    if (g.nb == 0) return GG_OK;
+    const BTile *tl = dTiles.p + g.t0;
+    const BDesc *de = dDesc.p + g.b0;
+    BState *sb = dSt.p + g.b0;
+    double *pt = part.p + (size_t)g.t0 * ps;
     const size_t sx = (size_t)sx_rows * sizeof(X32);
     if (precision == GG_SPLIT) {
-      k_b_gatherx<true><<<ntiles, RT, 0, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, XD.p, XS.p);
-      k_b_spmm<true><<<ntiles, 256, sx, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
+      k_b_gatherx<true><<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, XD.p, XS.p);
+      k_b_spmm<true><<<g.nt, 256, sx, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
     } else {
-      k_b_gatherx<false><<<ntiles, RT, 0, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, XD.p, XS.p);
-      k_b_spmm<false><<<ntiles, 256, sx, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
+      k_b_gatherx<false><<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, XD.p, XS.p);
+      k_b_spmm<false><<<g.nt, 256, sx, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
     }
-    k_b_dots<2><<<ntiles, BT, dots_smem, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, W.p, part.p, ps);
-    k_b_colsum<2><<<nb, 256, 0, s>>>(dDesc.p, dSt.p, part.p, ps, Sp.p, Cp.p, 0);
+    k_b_dots<2><<<g.nt, BT, dots_smem, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, pt, ps);
+    k_b_colsum<2><<<g.nb, 256, 0, s>>>(de, sb, part.p, ps, Sp.p, Cp.p, 0);
     *count += 4;
     GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
 
-  // one Davidson iteration for every active block
-  int enqueue_iteration(cudaStream_t s, int *count) {
-    k_b_eig<<<nb, EIG_T, eig.bytes(), s>>>(dDesc.p, dSt.p, Sp.p, Yp.p, eig);
-    k_b_ritz<<<ntiles, RT, 0, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, W.p, Yp.p, X.p, R.p, part.p, ps);
-    GG_CUDA(cudaMemsetAsync(dNact.p, 0, sizeof(int), s));
-    k_b_conv<<<(nb + 127) / 128, 128, 0, s>>>(dDesc.p, dSt.p, part.p, ps, nb, critr, dNact.p);
-    k_b_restart<<<ntiles, BT, restart_smem, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, W.p, Yp.p);
-    k_b_restart_fin<<<nb, 256, 0, s>>>(dDesc.p, dSt.p, Sp.p);
-    k_b_precond<<<ntiles, RT, 0, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, R.p);
+  // projected eigenproblem, Ritz pairs and residuals, convergence, restart,
+  // new vectors and their orthonormalisation
+  int enqueue_main(cudaStream_t s, const Group &g, int *count) {
+    if (g.nb == 0) return GG_OK;
+    const BTile *tl = dTiles.p + g.t0;
+    const BDesc *de = dDesc.p + g.b0;
+    BState *sb = dSt.p + g.b0;
+    double *pt = part.p + (size_t)g.t0 * ps;
+    k_b_eig<<<g.nb, EIG_T, eig.bytes(), s>>>(de, sb, Sp.p, Yp.p, eig);
+    k_b_ritz<<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, Yp.p, X.p, R.p, pt, ps);
+    k_b_conv<<<(g.nb + 127) / 128, 128, 0, s>>>(de, sb, part.p, ps, g.nb, critr, dNact.p);
+    k_b_restart<<<g.nt, BT, restart_smem, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, Yp.p);
+    k_b_restart_fin<<<g.nb, 256, 0, s>>>(de, sb, Sp.p);
+    k_b_precond<<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, R.p);
     *count += 6;
     for (int pass = 0; pass < 2; ++pass) {
-      k_b_dots<0><<<ntiles, BT, dots_smem, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, W.p, part.p, ps);
-      k_b_colsum<0><<<nb, 256, 0, s>>>(dDesc.p, dSt.p, part.p, ps, Sp.p, Cp.p, pass == 0);
-      k_b_sub<<<ntiles, RT, 0, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, Cp.p);
+      k_b_dots<0><<<g.nt, BT, dots_smem, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, pt, ps);
+      k_b_colsum<0><<<g.nb, 256, 0, s>>>(de, sb, part.p, ps, Sp.p, Cp.p, pass == 0);
+      k_b_sub<<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, Cp.p);
       *count += 3;
     }
     for (int pass = 0; pass < 2; ++pass) {
-      k_b_dots<1><<<ntiles, BT, dots_smem, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, W.p, part.p, ps);
-      k_b_colsum<1><<<nb, 256, 0, s>>>(dDesc.p, dSt.p, part.p, ps, Sp.p, Cp.p, pass == 0);
-      k_b_apply<<<ntiles, RT, 0, s>>>(dTiles.p, dDesc.p, dSt.p, V.p, Cp.p);
+      k_b_dots<1><<<g.nt, BT, dots_smem, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, pt, ps);
+      k_b_colsum<1><<<g.nb, 256, 0, s>>>(de, sb, part.p, ps, Sp.p, Cp.p, pass == 0);
+      k_b_apply<<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, Cp.p);
       *count += 3;
     }
-    GG_TRY(enqueue_expand(s, count));
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  }
+
+  // one Davidson iteration for every active block. The blocks are split in
+  // two groups whose iterations are staggered: group 0 runs the main part
+  // then the expansion, group 1 the expansion then the main part, on two
+  // streams, so one group's projected eigenproblems (FP64 pipe) run beside
+  // the other group's matvec (FP32 pipe and memory). Per block the sequence
+  // of steps is the same as without groups.
+  int enqueue_iteration(cudaStream_t s, bool fork, int *count) {
+    GG_CUDA(cudaMemsetAsync(dNact.p, 0, sizeof(int), s));
+    cudaStream_t sb = s;
+    if (fork && grp[1].nb > 0) {
+      GG_CUDA(cudaEventRecord(evFork, s));
+      GG_CUDA(cudaStreamWaitEvent(s2, evFork, 0));
+      sb = s2;
+    }
+    GG_TRY(enqueue_main(s, grp[0], count));
+    GG_TRY(enqueue_expand(s, grp[0], count));
+    GG_TRY(enqueue_expand(sb, grp[1], count));
+    GG_TRY(enqueue_main(sb, grp[1], count));
+    if (sb != s) {
+      GG_CUDA(cudaEventRecord(evJoin, sb));
+      GG_CUDA(cudaStreamWaitEvent(s, evJoin, 0));
+    }
     GG_CUDA(cudaMemcpyAsync(hNact, dNact.p, sizeof(int), cudaMemcpyDeviceToHost, s));
     GG_CUDA(cudaGetLastError());
     return GG_OK;
@@ -1300,6 +1430,22 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   }
   B.ntot = row0;
   B.ntiles = (int)B.ht.size();
+  // two groups of contiguous blocks with about half the rows each
+  B.all = BatchRun::Group{0, nblocks, 0, B.ntiles};
+  {
+    int split = nblocks;
+    if (nblocks >= 2) {
+      long long acc = 0;
+      split = 1;
+      for (int b = 0; b < nblocks - 1; ++b) {
+        acc += B.hd[b].n;
+        split = b + 1;
+        if (2 * acc >= row0) break;
+      }
+    }
+    B.grp[0] = BatchRun::Group{0, split, 0, split < nblocks ? B.hd[split].tile0 : B.ntiles};
+    B.grp[1] = BatchRun::Group{split, nblocks - split, B.grp[0].nt, B.ntiles - B.grp[0].nt};
+  }
   B.eig = EigShape{lmax, nvmax};
   B.ps = (lmax + 1) * MAXR;
   B.restart_smem = sizeof(double) * ((size_t)lmax * 64 + (size_t)RG * lmax);
@@ -1357,7 +1503,7 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   for (int c0 = 0; c0 < m0max; c0 += MAXR) {
     k_b_setnew<<<(nblocks + 127) / 128, 128, 0, s>>>(B.dDesc.p, B.dSt.p, nblocks);
     ++launches;
-    GG_TRY(B.enqueue_expand(s, &launches));
+    GG_TRY(B.enqueue_expand(s, B.all, &launches));
   }
   GG_CUDA(cudaGetLastError());
   // the iteration, captured once and replayed until no block is active
@@ -1365,8 +1511,11 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   if (const char *e = getenv("GRASP_GPU_DVD_GRAPH")) use_graph = (e[0] != '0');
   int per_iter = 0;
   if (use_graph) {
+    GG_CUDA(cudaStreamCreateWithFlags(&B.s2, cudaStreamNonBlocking));
+    GG_CUDA(cudaEventCreateWithFlags(&B.evFork, cudaEventDisableTiming));
+    GG_CUDA(cudaEventCreateWithFlags(&B.evJoin, cudaEventDisableTiming));
     GG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    const int rc = B.enqueue_iteration(s, &per_iter);
+    const int rc = B.enqueue_iteration(s, true, &per_iter);
     cudaGraph_t g = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(s, &g);
     if (rc != GG_OK) {
@@ -1383,7 +1532,7 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
       GG_CUDA(cudaGraphLaunch(B.gexec, s));
     } else {
       per_iter = 0;
-      GG_TRY(B.enqueue_iteration(s, &per_iter));
+      GG_TRY(B.enqueue_iteration(s, false, &per_iter));
     }
     launches += per_iter;
     ++iters;

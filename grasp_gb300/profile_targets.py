@@ -7,6 +7,7 @@ kernel family it is named for, a few times:
   python -m grasp_gb300.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
   python -m grasp_gb300.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
   python -m grasp_gb300.profile_targets batch    # two batched solves of the 310-block workload (split)
+  python -m grasp_gb300.profile_targets batch8   # the same for 8 ions (80 blocks), for detailed captures
 """
 from __future__ import annotations
 
@@ -57,9 +58,9 @@ def rk_split():
     rk(precision=1)
 
 
-def batch():
+def batch(zs=None):
     from . import SPLIT, Context, maneig_batched, workloads
-    w = workloads.batch()
+    w = workloads.batch() if zs is None else workloads.batch(zs=zs)
     ctx = Context(0)
     hs = workloads.assemble_batch(w, ctx)
     for _ in range(2):
@@ -68,4 +69,5 @@ def batch():
 
 
 if __name__ == "__main__":
-    {"spmv": spmv, "solve": solve, "rk": rk, "rk_split": rk_split, "batch": batch}[sys.argv[1]]()
+    {"spmv": spmv, "solve": solve, "rk": rk, "rk_split": rk_split, "batch": batch,
+     "batch8": lambda: batch(zs=tuple(range(10, 18)))}[sys.argv[1]]()
