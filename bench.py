@@ -10,6 +10,11 @@ fp64_ci_solve_s is the same solve with the FP64 matvec. e2e repeats the solve
 through the public API from pinned host buffers: orbitals, CSR structure and
 lists uploaded every step, eigenpairs read back every step.
 
+Two more workloads are measured in the same run and reported beside the
+headline: batched_310_blocks (31 ions x 10 J/parity blocks solved together
+by gg_maneig_batched) and rk_table_40_orbitals (the standalone R^k table on
+the tensor cores and in FP64).
+
 --impl reference runs the CPU restatement of the reference (oracle/, C++
 FP64, the reference's algorithm: SLATER per integral, SETHAM per label,
 dense INIEST2, DVDSON) with all host threads on a bounded sample of the same
@@ -43,6 +48,7 @@ def _args():
     ap.add_argument("--cpu-loops", type=int, default=12, help="Davidson loops timed in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-extra", action="store_true", help="skip the batched-block and R^k table legs")
     return ap.parse_args()
 
 
@@ -169,6 +175,83 @@ def cpu_sample(w, nthreads, loops, gpu_loops=None):
     del np
     return est, desc, dict(genintrk_s=t1 - t0, setham_s=t2 - t1, iniest2_s=t_ini, dvdson_loop_s=per_loop,
                            loops=n_loops)
+
+
+def batched_leg(local, steps, cpu=True):
+    """The 310-block workload (workloads.batch: 31 ions x 10 J/parity blocks,
+    3 roots each): all blocks assembled on the device, then MANEIG for all of
+    them in one batched solve (gg_maneig_batched), split and FP64 matvec. The
+    CPU sample runs the oracle's MANEIG (dense DSPEVX for these NCF <= 2000
+    blocks, as rci) on the ten blocks of one ion, 1 thread, x 31 ions."""
+    import numpy as np
+
+    from grasp_gb300 import FP64, SPLIT, Context, maneig_batched, workloads
+    w = workloads.batch()
+    ctx = Context(local)
+    t0 = time.perf_counter()
+    hs = workloads.assemble_batch(w, ctx)
+    ctx.synchronize()
+    t_asm = time.perf_counter() - t0
+    out = dict(w.describe())
+    res = {}
+    for prec, name in ((SPLIT, "split"), (FP64, "fp64")):
+        maneig_batched(ctx, hs, w.nroots, precision=prec)  # warm-up
+        ts, dev = [], []
+        for _ in range(max(3, steps)):
+            t = time.perf_counter()
+            r, info = maneig_batched(ctx, hs, w.nroots, precision=prec)
+            ts.append(time.perf_counter() - t)
+            dev.append(ctx.stage_stat(3))
+        res[name] = r
+        out[f"{name}_solve_s"] = statistics.median(ts)
+        out[f"{name}_solve_device_ms"] = statistics.median(dev)
+        out[f"{name}_iterations"] = int(ctx.stage_stat(21))
+        out[f"{name}_kernels_per_iteration"] = int(ctx.stage_stat(22))
+        out[f"{name}_block_loops_mean"] = float(np.mean(info["nloops"]))
+    out["max_abs_dE_split_vs_fp64_Eh"] = float(max(np.abs(a[0] - b[0]).max()
+                                                   for a, b in zip(res["split"], res["fp64"])))
+    out["assemble_s"] = t_asm
+    out["ci_solve_e2e_s"] = t_asm + out["split_solve_s"]
+    if cpu:
+        import oracle
+        oracle.build()
+        t = time.perf_counter()
+        for idx in range(len(w.blocks)):  # the first ion's blocks
+            b = w.blocks[idx][2]
+            oracle.maneig(0, b.ncf, w.nroots, b.iendc, b.irow, hs[idx].emt())
+        per_ion = time.perf_counter() - t
+        out["cpu_baseline"] = {"value": per_ion * len(w.zs), "unit": "s", "cores": 1, "kind": "port",
+                               "sample": f"oracle MANEIG (dense DSPEVX, rci's path for NCF <= 2000) on the "
+                                         f"{len(w.blocks)} blocks of one ion: {per_ion:.2f} s, x {len(w.zs)} ions"}
+    return out
+
+
+def rk_leg(local):
+    """The R^k table workload (workloads.rk40: 40 orbitals, k <= 8): GENINTRK
+    on the int8 tensor cores (Ozaki slices) and in FP64; max difference of
+    the two tables relative to max(|R^k|, 1e-2), i.e. the tests' 1e-12
+    relative bar with its 1e-14 absolute floor."""
+    import numpy as np
+
+    from grasp_gb300 import Context, workloads
+    w = workloads.rk40()
+    ctx = Context(local)
+    ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
+    ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    out = {"workload": w.name, "kmax": w.kmax}
+    vals = {}
+    for prec, name in ((1, "tensor_ozaki"), (0, "fp64")):
+        ctx.genintrk(kmax=w.kmax, precision=prec)
+        ts = []
+        for _ in range(5):
+            n, _ = ctx.genintrk(kmax=w.kmax, precision=prec)
+            ts.append(ctx.stage_stat(0))
+        out[f"{name}_ms"] = min(ts)
+        out["integrals"] = int(n)
+        vals[name] = ctx.rk_table()[1]
+    a, b = vals["tensor_ozaki"], vals["fp64"]
+    out["max_rel_diff"] = float((np.abs(a - b) / np.maximum(np.abs(b), 1e-2)).max())
+    return out
 
 
 def run_reference(a):
@@ -318,6 +401,8 @@ def run_ours(a):
                 t, ev_e = solve_e2e(w, SPLIT, local, arrays)
                 e2e_times.append(t)
     t_e2e = _max_over_ranks(pg, statistics.median(e2e_times)) if e2e_times else None
+    batched = batched_leg(local, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
+    rk = rk_leg(local) if not a.no_extra else None
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
         est, desc, parts = cpu_sample(w, 1, a.cpu_loops, gpu_loops=int(stage["loops_full"]) + 1)
@@ -345,6 +430,8 @@ def run_ours(a):
         "gpu_launches_per_step": int(l1 - l0) // max(1, a.steps),
         "clocks": clk,
         "cpu_baseline": cpu,
+        "batched_310_blocks": batched,
+        "rk_table_40_orbitals": rk,
     }
     print(json.dumps(out), flush=True)
     return 0
