@@ -29,6 +29,7 @@ class GGDvdParams(C.Structure):
     _fields_ = [
         ("flavour", C.c_int), ("precision", C.c_int), ("lim", C.c_int), ("maxiter", C.c_int),
         ("critr", C.c_double), ("critc", C.c_double), ("crite", C.c_double), ("robust", C.c_int),
+        ("mblock", C.c_int),
     ]
 
 

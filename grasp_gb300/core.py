@@ -199,8 +199,8 @@ class HMatrix:
         return c
 
     def maneig(self, nvec, flavour=0, precision=FP64, lim=0, maxiter=0, critr=0.0, critc=0.0, crite=0.0,
-               robust=False, raise_on_maxiter=True):
-        p = GGDvdParams(flavour, precision, lim, maxiter, critr, critc, crite, int(robust))
+               robust=False, raise_on_maxiter=True, mblock=0):
+        p = GGDvdParams(flavour, precision, lim, maxiter, critr, critc, crite, int(robust), int(mblock))
         ev = np.zeros(nvec); vec = np.zeros((nvec, self.ncf))
         nl, nm, ie = C.c_int(), C.c_int(), C.c_int()
         st = _lib.gpu().gg_maneig(self.ctx._h, self._h, nvec, C.byref(p), ptr(ev, _d), ptr(vec, _d), C.byref(nl),
@@ -234,7 +234,7 @@ def maneig_batched(ctx, hmats, nvec, precision=FP64, lim=0, maxiter=0, critr=0.0
     vec = np.zeros(int((ncf * nv).sum()))
     hs = (C.c_void_p * nb)(*[h._h.value for h in hmats])
     nl, nm, ie = (np.zeros(nb, np.int32) for _ in range(3))
-    p = GGDvdParams(0, precision, lim, maxiter, critr, 0.0, 0.0, 0)
+    p = GGDvdParams(0, precision, lim, maxiter, critr, 0.0, 0.0, 0, 0)
     st = _lib.gpu().gg_maneig_batched(ctx._h, nb, hs, ptr(nv, _int), C.byref(p), ptr(ev, _d), ptr(vec, _d),
                                       ptr(nl, _int), ptr(nm, _int), ptr(ie, _int))
     if st != 0 and (raise_on_maxiter or st != _lib_status("GG_ERR_CONVERGE")):

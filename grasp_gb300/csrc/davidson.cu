@@ -829,6 +829,7 @@ struct Dvd {
   cudaGraph_t graph = nullptr;    // single-vector pass (MBLOCK = 1)
   cudaGraphExec_t gexec = nullptr;
   cudaEvent_t gev0 = nullptr, gev1 = nullptr;
+  std::vector<cudaEvent_t> bev;    // matvec events of the block passes
   cudaEvent_t pev0 = nullptr, pev1 = nullptr;  // around each single-vector pass
   double pass_ms = 0;             // device ms of the single-vector passes
   int graph_kernels = 0;
@@ -966,6 +967,8 @@ struct Dvd {
     if (hpv) cudaFreeHost(hpv);
     if (graph) cudaGraphDestroy(graph);
     if (gev0) cudaEventDestroy(gev0);
+    for (auto e : bev)
+      if (e) cudaEventDestroy(e);
     if (gev1) cudaEventDestroy(gev1);
     if (pev0) cudaEventDestroy(pev0);
     if (pev1) cudaEventDestroy(pev1);
@@ -1067,13 +1070,24 @@ struct Dvd {
   // Gram-Schmidt, OP and ADDS of new columns P[v].c, v < m, in that order per
   // column (each column needs only the columns before it); the S columns go
   // to dS at their packed offsets
-  int enqueue_block(int m) {
+  int enqueue_block(int m, bool in_capture) {
     for (int v = 0; v < m; ++v) {
       const PSrc ps{dpv.p + v, IterParams{}};
       const int *dcol = reinterpret_cast<const int *>(reinterpret_cast<const char *>(dpv.p + v) +
                                                       offsetof(IterParams, c));
       cgs2(ps, false, nullptr, precision == GG_SPLIT ? h->dXs.p : nullptr);
+      // each matvec between two events (read after the pass)
+      if (in_capture) {
+        GG_CUDA(cudaEventRecordWithFlags(bev[2 * v], s, cudaEventRecordExternal));
+      } else {
+        GG_CUDA(cudaEventRecord(bev[2 * v], s));
+      }
       GG_TRY(spmv_col(h, precision, B.p, AB.p, ld, dcol, nullptr, s));
+      if (in_capture) {
+        GG_CUDA(cudaEventRecordWithFlags(bev[2 * v + 1], s, cudaEventRecordExternal));
+      } else {
+        GG_CUDA(cudaEventRecord(bev[2 * v + 1], s));
+      }
       launch_dots(false, ps, 1, AB.p, nullptr, -1, dS.p, 1);
     }
     return GG_OK;
@@ -1083,6 +1097,10 @@ struct Dvd {
   int block_pass(int kpass, int m, std::vector<double> &S) {
     if (m <= 0) return GG_OK;
     if (m > MT_MAX) return fail(GG_ERR_ARG, "block pass: more new vectors than supported");
+    if (bev.empty()) {
+      bev.resize(2 * MT_MAX, nullptr);
+      for (auto &e : bev) GG_CUDA(cudaEventCreate(&e));
+    }
     if (!dpv.p) {
       GG_TRY(dpv.alloc(MT_MAX));
       GG_CUDA(cudaMallocHost(&hpv, MT_MAX * sizeof(IterParams)));
@@ -1098,7 +1116,7 @@ struct Dvd {
       if (!bexec[m]) {
         GG_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         const long long before = gg_launch_count();
-        const int st = enqueue_block(m);
+        const int st = enqueue_block(m, true);
         const long long captured = gg_launch_count() - before;
         note_launches(-captured);
         cudaGraph_t g = nullptr;
@@ -1116,7 +1134,7 @@ struct Dvd {
       GG_CUDA(cudaGraphLaunch(bexec[m], s));
       note_launches(bkernels[m]);
     } else {
-      GG_TRY(enqueue_block(m));
+      GG_TRY(enqueue_block(m, false));
     }
     nmv += m;
     mv_count += m;
@@ -1126,6 +1144,11 @@ struct Dvd {
     GG_CUDA(cudaStreamSynchronize(s));
     t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     std::memcpy(S.data() + o0, hS + o0, (o1 - o0) * sizeof(double));
+    for (int v = 0; v < m; ++v) {
+      float ms = 0.f;
+      GG_CUDA(cudaEventElapsedTime(&ms, bev[2 * v], bev[2 * v + 1]));
+      mv_ms += ms;
+    }
     return GG_OK;
   }
 
@@ -1716,7 +1739,7 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   DvdParams P;
   P.nume = nvec;
   P.niv = nvec;
-  P.mblock = 1;
+  P.mblock = (p && p->mblock > 1) ? std::min(p->mblock, nvec) : 1;
   P.crite = (p && p->crite > 0) ? p->crite : 1.0e-17;
   P.critc = (p && p->critc > 0) ? p->critc : 1.0e-9;
   P.critr = (p && p->critr > 0) ? p->critr : 1.0e-9;

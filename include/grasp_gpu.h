@@ -184,6 +184,11 @@ typedef struct {
                      OLDVAL sentinel, dvdson.f90:703), which otherwise wastes
                      the first correction vector and can let the coefficient
                      test stop the solver early. */
+  int mblock;     /* DVDSON's MBLOCK for the full block: <= 0 or 1 keeps the
+                     reference's single-vector passes; up to nvec adds that
+                     many correction vectors per pass (one matvec pass over
+                     the matrix for all of them, one projected eigenproblem
+                     per pass) */
 } gg_dvd_params;
 
 int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double *eval, double *evec,

@@ -126,6 +126,13 @@ def test_maneig_davidson_path(gpu_ready, oracle_mod):
             assert info0["ierr"] == 0 and info["ierr"] == 0
             assert np.abs(ev - ev0).max() <= 1e-9, (robust, precision, ev, ev0)
             assert np.abs(vec - vec0).max() <= 1e-7, (robust, precision, np.abs(vec - vec0).max())
+    # block passes (DVDSON's MBLOCK = NVEC): fewer, wider passes converge to
+    # the same eigenpairs as the reference's single-vector run
+    for precision in (0, 1):
+        ev, vec, info = H.maneig(nvec, flavour=0, precision=precision, mblock=nvec)
+        assert info["ierr"] == 0
+        assert np.abs(ev - ev0).max() <= 1e-9, (precision, ev, ev0)
+        assert np.abs(vec - vec0).max() <= 1e-7, (precision, np.abs(vec - vec0).max())
 
 
 def test_maneig_graph_pass_matches_launch_path(gpu_ready, monkeypatch):
