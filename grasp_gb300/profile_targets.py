@@ -3,7 +3,7 @@ in profiles/. Each target builds the Fe XV workload once and runs only the
 kernel family it is named for, a few times:
 
   python -m grasp_gb300.profile_targets spmv     # 3 full-size y = H x launches per precision
-  python -m grasp_gb300.profile_targets solve    # one full CI solve (launch list)
+  python -m grasp_gb300.profile_targets solve    # one full MANEIG (split, MBLOCK = NVEC) (launch list)
   python -m grasp_gb300.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
   python -m grasp_gb300.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
   python -m grasp_gb300.profile_targets batch    # two batched solves of the 310-block workload (split)
@@ -39,7 +39,7 @@ def spmv():
 def solve():
     from . import SPLIT
     w, ctx, H = _fe15_context()
-    ev, vec, info = H.maneig(w.nroots, flavour=0, precision=SPLIT)
+    ev, vec, info = H.maneig(w.nroots, flavour=0, precision=SPLIT, mblock=w.nroots)
     print("loops", info["nloops"], "E0", ev[0])
 
 
