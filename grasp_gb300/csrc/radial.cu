@@ -12,8 +12,11 @@
 //   A buffer   [nP][KC]  w(i) * (P_a P_c + Q_a Q_c)(r_i) * RPOR(r_i) for
 //                        every pair a <= c, zero outside 2 <= i <= min(MF).
 //   VALTEIRK   [N_Rk]    written by the contraction epilogue in GENINTRK order.
+#include <cuda_fp16.h>
+
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -219,24 +222,20 @@ __global__ void k_apairs(const int2 *__restrict__ pairs, int npairs, const doubl
 // term at i = 2 and the end-panel correction at MTP (quad.f90), written at
 // its GENINTRK position; entries whose QUAD head index is not 2 go to the
 // general per-integral QUAD instead.
-__device__ __forceinline__ void rk_finish(const RkTile &T, int p, int idx_c, int f, double sum,
-                                          const int2 *__restrict__ pairs, const YDesc *__restrict__ yd,
-                                          const double *__restrict__ Y, int np, const double *__restrict__ PF,
-                                          const double *__restrict__ QF, int ld, const int *__restrict__ MF,
-                                          const double *__restrict__ R, const double *__restrict__ RP,
-                                          const double *__restrict__ RPOR, const QuadConst &q,
-                                          double *__restrict__ val, long long nval, QuadItem *__restrict__ fb,
-                                          int *__restrict__ nfb) {
-  const int a = T.a;
-  const int c = pairs[p].y;
+// QUAD's power-law head term and end-panel correction (quad.f90:52-103) for
+// integral (a, c; f) of order k whose GEMM part (grid points 3.., the
+// Newton-Cotes weights folded into A) is `sum`, stored at VALTEIRK position
+// pos; an integral whose head index is not 2 goes to the general QUAD list.
+__device__ __forceinline__ void rk_head_store(int k, int a, int c, int f, long long pos, double sum,
+                                              const YDesc *__restrict__ yd, const double *__restrict__ Y, int np,
+                                              const double *__restrict__ PF, const double *__restrict__ QF, int ld,
+                                              const int *__restrict__ MF, const double *__restrict__ R,
+                                              const double *__restrict__ RP, const double *__restrict__ RPOR,
+                                              const QuadConst &q, double *__restrict__ val,
+                                              QuadItem *__restrict__ fb, int *__restrict__ nfb) {
   const YDesc y = yd[f];
-  const long long pos = T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)idx_c * y.nd + (long long)(f - y.cs);
-  if (pos < 0 || pos >= nval) {  // position outside the table: report, never write
-    atomicExch(nfb + 1, 1);
-    return;
-  }
   int mtp;
-  if (T.k == 0 && y.b == y.d)
+  if (k == 0 && y.b == y.d)
     mtp = min(MF[a], MF[c]);
   else
     mtp = min(min(y.mtp, MF[a]), MF[c]);
@@ -265,6 +264,25 @@ __device__ __forceinline__ void rk_finish(const RkTile &T, int p, int idx_c, int
     const int slot = atomicAdd(nfb, 1);
     fb[slot] = QuadItem{a, c, f, mtp, pos};
   }
+}
+
+// the GEMM part `sum` of canonical entry (p = (a, c), f) of tile T: its
+// GENINTRK position, then the head term
+__device__ __forceinline__ void rk_finish(const RkTile &T, int p, int idx_c, int f, double sum,
+                                          const int2 *__restrict__ pairs, const YDesc *__restrict__ yd,
+                                          const double *__restrict__ Y, int np, const double *__restrict__ PF,
+                                          const double *__restrict__ QF, int ld, const int *__restrict__ MF,
+                                          const double *__restrict__ R, const double *__restrict__ RP,
+                                          const double *__restrict__ RPOR, const QuadConst &q,
+                                          double *__restrict__ val, long long nval, QuadItem *__restrict__ fb,
+                                          int *__restrict__ nfb) {
+  const YDesc y = yd[f];
+  const long long pos = T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)idx_c * y.nd + (long long)(f - y.cs);
+  if (pos < 0 || pos >= nval) {  // position outside the table: report, never write
+    atomicExch(nfb + 1, 1);
+    return;
+  }
+  rk_head_store(T.k, T.a, pairs[p].y, f, pos, sum, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val, fb, nfb);
 }
 
 // ---------------------------------------------------------------------------
@@ -344,14 +362,16 @@ __global__ void __launch_bounds__(256) k_rk_gemm(const RkTile *__restrict__ tile
 
 // ---------------------------------------------------------------------------
 // The same contraction on the tensor cores, split-precision (Ozaki): each row
-// of A and of Y is scaled by a power of two 2^e (|row| < 2^e) and cut into
-// OZ_S slices of 7 bits, x = 2^e sum_s q_s 2^(-7(s+1)) with q_s in [-127, 127]
-// (truncation toward zero; every step is exact in FP64). The products of
-// slice pairs (s, t) with s + t < OZ_S are exact int8 x int8 -> int32 tensor
-// products; pairs with the same q = s + t share one int32 accumulator
-// (at most OZ_S x KC x 127^2 < 2^31). The sum over q is then
-// sum_q acc_q 2^(eA + eY - 7(q + 2)) in FP64. With OZ_S = 10 the result
-// agrees with the FP64 contraction to a few 1e-13 relative on R^k data.
+// of A and of Y is scaled by a power of two 2^e (|row| < 2^(e-1)) and cut
+// into OZ_S slices of 7 bits, x = 2^e sum_s q_s 2^(-7(s+1)), each q_s the
+// nearest integer to the remainder, so |q_s| <= 64 (every step is exact in
+// FP64). Products of slice pairs (s, t) with s + t < OZ_S are exact integer
+// tensor products (|q_s q_t| <= 4096); pairs with the same q = s + t share one
+// accumulator: int32 on the mma.sync path, FP32 in TMEM on the tcgen05 path,
+// where at most 10 pairs x 256 grid points x 4096 < 2^24 keeps every partial
+// sum an exact integer between flushes. The sum over q is then
+// sum_q acc_q 2^(eA + eY - 7(q + 2)). With OZ_S = 10 the result agrees with
+// the FP64 contraction to a few 1e-13 relative on R^k data.
 // ---------------------------------------------------------------------------
 constexpr int OZ_S = 10;
 
@@ -370,17 +390,17 @@ __global__ void k_oz_split(const double *__restrict__ M, int nrows, int pitch, i
     __syncthreads();
   }
   mx = red[0];
-  const int e = (mx > 0.0) ? ilogb(mx) + 1 : 0;  // mx < 2^e
+  const int e = (mx > 0.0) ? ilogb(mx) + 2 : 0;  // mx < 2^(e-1)
   if (threadIdx.x == 0) exps[row] = e;
   const size_t plane = (size_t)(nrows + 1) * KP;
   for (int i = threadIdx.x; i < KP; i += blockDim.x) {
-    double x = (row < nrows && i < K) ? scalbn(M[(size_t)row * pitch + i], -e) : 0.0;
+    double x = (row < nrows && i < K) ? scalbn(M[(size_t)row * pitch + i], -e) : 0.0;  // |x| < 1/2
 #pragma unroll
     for (int q = 0; q < OZ_S; ++q) {
-      x *= 128.0;
-      const double t = trunc(x);
+      x *= 128.0;  // |x| <= 64
+      const double t = rint(x);
       slices[q * plane + (size_t)row * KP + i] = (signed char)(int)t;
-      x -= t;
+      x -= t;  // |x| <= 1/2
     }
   }
 }
@@ -473,6 +493,258 @@ __global__ void __launch_bounds__(256) k_rk_ozaki(const RkTile *__restrict__ til
 
 // General per-integral QUAD: TA(i) = ((P_a P_c + Q_a Q_c) RPOR) Y_f(i),
 // one warp per integral, sequential reference-order sum on lane 0.
+// ---------------------------------------------------------------------------
+// The Ozaki contraction on GB300's fifth-generation tensor cores (tcgen05).
+//
+// One CTA per tile of TC_M = 128 Y functions (the MMA's M) x TC_N = 32 rows
+// (a, c) pairs (N). Per stage of TC_KC = 32 grid points every thread converts
+// its share of the int8 slices (|q| <= 64) to fp16, which holds them exactly,
+// and stores them in the no-swizzle K-major core-matrix layout (8 rows x 16 B
+// per core matrix; neighbours in K 128 B apart, in M/N 256 B apart); then one
+// thread issues, per K = 16 step, the 55 slice-pair MMAs
+// tcgen05.mma.cta_group::1.kind::f16 into the accumulator of their group
+// q = s + t (OZ_S groups x TC_N FP32 columns of tensor memory). Two stages
+// alternate; tcgen05.commit to a per-stage mbarrier tells when a stage may
+// be refilled. Every TC_FLUSH stages (256 grid points, while every group sum
+// is still an exact integer below 2^24) the four warps read their 32 lanes
+// of each group (tcgen05.ld) and fold group q, scaled by 2^(-7q), into
+// double-float sums; the next MMA of each group then overwrites. The raw sum
+// 2^(eA+eY-14) (h + l) is stored at the entry's GENINTRK position; the head
+// term is added by k_rk_finish_all. Every wait is bounded: on a timeout the
+// CTA sets err, waits (bounded) for its issued MMAs, frees its tensor memory
+// and returns without writing.
+// ---------------------------------------------------------------------------
+constexpr int TC_M = 128, TC_N = 32, TC_KC = 32, TC_FLUSH = 8;
+constexpr int TC_YST = OZ_S * 2 * (TC_M / 8) * 2 * 64;  // fp16 elements per Y stage (80 KB)
+constexpr int TC_AST = OZ_S * 2 * (TC_N / 8) * 2 * 64;  // fp16 elements per A stage (20 KB)
+constexpr size_t TC_SMEM = (size_t)2 * (TC_YST + TC_AST) * sizeof(__half) + 64;
+constexpr uint32_t TC_TMEM_COLS = 512;  // >= OZ_S * TC_N, a power of two
+constexpr int TC_SPIN = 1 << 24;
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: start address, leading (K) byte offset
+// 128, stride (M/N) byte offset 256, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)(128 >> 4) << 16) | ((uint64_t)(256 >> 4) << 32) |
+         ((uint64_t)1 << 46);
+}
+
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+  uint32_t done = 0;
+  for (int it = 0; it < TC_SPIN && !done; ++it)
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+  return done != 0;
+}
+
+// 8 signed bytes -> 8 fp16 values (16 bytes)
+__device__ __forceinline__ int4 tc_cvt8(uint32_t lo, uint32_t hi) {
+  __half2 h[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const uint32_t w = (b < 2) ? lo : hi;
+    const int sh = (b & 1) * 16;
+    const int v0 = (int)(signed char)((w >> sh) & 0xffu), v1 = (int)(signed char)((w >> (sh + 8)) & 0xffu);
+    h[b] = __halves2half2(__int2half_rn(v0), __int2half_rn(v1));
+  }
+  int4 r;
+  memcpy(&r, h, sizeof(r));
+  return r;
+}
+
+// one row's 32 slice bytes at src into the stage: 4 groups of 8 grid points,
+// group g = (K step j = g / 2, core column k8 = g % 2)
+__device__ __forceinline__ void tc_row(const signed char *__restrict__ src, __half *dst, int rows8, int slice,
+                                       int row) {
+  const int4 v0 = __ldg(reinterpret_cast<const int4 *>(src));
+  const int4 v1 = __ldg(reinterpret_cast<const int4 *>(src + 16));
+  const uint32_t w[8] = {(uint32_t)v0.x, (uint32_t)v0.y, (uint32_t)v0.z, (uint32_t)v0.w,
+                         (uint32_t)v1.x, (uint32_t)v1.y, (uint32_t)v1.z, (uint32_t)v1.w};
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const int j = g >> 1, k8 = g & 1;
+    *reinterpret_cast<int4 *>(dst + (((slice * 2 + j) * rows8 + row / 8) * 2 + k8) * 64 + (row % 8) * 8) =
+        tc_cvt8(w[2 * g], w[2 * g + 1]);
+  }
+}
+
+__global__ void __launch_bounds__(128, 1) k_rk_tc(const RkTile *__restrict__ tiles, const int *__restrict__ rowpair,
+                                                  const signed char *__restrict__ As, const int *__restrict__ eA,
+                                                  int npairs, const signed char *__restrict__ Ys,
+                                                  const int *__restrict__ eY, int nf, int KP,
+                                                  const YDesc *__restrict__ yd, double *__restrict__ val,
+                                                  long long nval, int *__restrict__ flags) {
+  extern __shared__ __align__(1024) unsigned char tsm[];
+  __half *Ysm = reinterpret_cast<__half *>(tsm);
+  __half *Asm = Ysm + 2 * TC_YST;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(Asm + 2 * TC_AST);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
+  __shared__ int prow[TC_N];
+  const RkTile T = tiles[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int nrow = min(TC_N, T.ncA - T.r0), ncol = T.c1 - T.c0;
+  if (tid < TC_N) prow[tid] = (tid < nrow) ? rowpair[T.rowpair0 + T.r0 + tid] : npairs;
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
+                 "r"(TC_TMEM_COLS));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&mbar[0])), "r"(1));
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&mbar[1])), "r"(1));
+    asm volatile("fence.mbarrier_init.release.cluster;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;");
+  const uint32_t tmem = *tslot;
+  const uint32_t idesc = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+  const size_t aplane = (size_t)(npairs + 1) * KP, yplane = (size_t)(nf + 1) * KP;
+  const int myf = (tid < ncol) ? T.c0 + tid : nf;  // Y row of this thread (zero row pads)
+  float ah[TC_N], al[TC_N];
+#pragma unroll
+  for (int n = 0; n < TC_N; ++n) ah[n] = al[n] = 0.f;
+  const int nch = KP / TC_KC;
+  uint32_t fresh = (1u << OZ_S) - 1;  // groups whose next MMA overwrites (thread 0)
+  int last_commit = -1;
+  bool ok = true;
+  for (int j = 0; j < nch && ok; ++j) {
+    const int st = j & 1, k0 = j * TC_KC;
+    if (j >= 2) ok = tc_wait(smem_addr(&mbar[st]), ((j - 2) >> 1) & 1);
+    if (ok) {
+      __half *ydst = Ysm + st * TC_YST;
+      for (int t = 0; t < OZ_S; ++t) tc_row(Ys + t * yplane + (size_t)myf * KP + k0, ydst, TC_M / 8, t, tid);
+      __half *adst = Asm + st * TC_AST;
+      for (int it = tid; it < OZ_S * TC_N; it += blockDim.x) {
+        const int sl = it / TC_N, n = it % TC_N;
+        tc_row(As + sl * aplane + (size_t)prow[n] * KP + k0, adst, TC_N / 8, sl, n);
+      }
+    }
+    asm volatile("fence.proxy.async.shared::cta;");
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    ok = __syncthreads_and(ok);
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    if (!ok) break;
+    if (tid == 0) {
+      const uint32_t yb = smem_addr(Ysm + st * TC_YST), ab = smem_addr(Asm + st * TC_AST);
+#pragma unroll 1
+      for (int ks = 0; ks < 2; ++ks)
+#pragma unroll 1
+        for (int sa = 0; sa < OZ_S; ++sa) {
+          const uint64_t bdesc = tc_desc(ab + (uint32_t)(sa * 2 + ks) * ((TC_N / 8) * 2 * 64 * 2));
+#pragma unroll 1
+          for (int t = 0; t < OZ_S - sa; ++t) {
+            const int qg = sa + t;
+            const uint64_t adesc = tc_desc(yb + (uint32_t)(t * 2 + ks) * ((TC_M / 8) * 2 * 64 * 2));
+            const uint32_t accum = ((fresh >> qg) & 1u) ? 0u : 1u;
+            fresh &= ~(1u << qg);
+            asm volatile(
+                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem + (uint32_t)(qg * TC_N)),
+                "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+          }
+        }
+      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                       smem_addr(&mbar[st]))
+                   : "memory");
+    }
+    last_commit = j;
+    if ((j + 1) % TC_FLUSH == 0 || j == nch - 1) {
+      ok = tc_wait(smem_addr(&mbar[st]), (j >> 1) & 1);  // every MMA issued so far is done
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      if (__all_sync(0xffffffffu, ok)) {
+#pragma unroll 1
+        for (int qg = 0; qg < OZ_S; ++qg) {
+          uint32_t r[32];
+          const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(qg * TC_N);
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+                "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+                "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+              : "r"(taddr));
+          asm volatile("tcgen05.wait::ld.sync.aligned;");
+          const float scale = __int_as_float((127 - 7 * qg) << 23);  // 2^(-7 qg)
+#pragma unroll
+          for (int n = 0; n < TC_N; ++n) {
+            // (ah, al) += v exactly in the high part (TwoSum), errors into al
+            const float v = __uint_as_float(r[n]) * scale;
+            const float sv = ah[n] + v;
+            const float bb = sv - ah[n];
+            const float e = (ah[n] - (sv - bb)) + (v - bb);
+            ah[n] = sv;
+            al[n] = al[n] + e;
+          }
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;");
+      ok = __syncthreads_and(ok);
+      asm volatile("tcgen05.fence::after_thread_sync;");
+      if (tid == 0) fresh = (1u << OZ_S) - 1;
+    }
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicExch(flags + 1, 1);  // timed out
+      if (last_commit >= 0) tc_wait(smem_addr(&mbar[last_commit & 1]), (last_commit >> 1) & 1);
+    }
+  } else if (tid < ncol) {
+    const int f = T.c0 + tid;
+    const YDesc y = yd[f];
+    const int ey = eY[f];
+#pragma unroll
+    for (int n = 0; n < TC_N; ++n) {
+      if (n >= nrow) break;
+      const long long pos =
+          T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)(T.r0 + n) * y.nd + (long long)(f - y.cs);
+      if (pos < 0 || pos >= nval) {
+        atomicExch(flags, 1);  // position outside the table
+        continue;
+      }
+      const int ex = eA[prow[n]] + ey - 14;
+      val[pos] = scalbn((double)ah[n] + (double)al[n], ex);
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS));
+}
+
+// QUAD head term for every table entry, one thread per entry: (a, b, c, d)
+// from INDTEIRK, k from KSTART, the Y function from fidx[(k KEY + b) KEY + d];
+// val holds the entry's GEMM part on entry.
+__global__ void k_rk_finish_all(const int32_t *__restrict__ ind, long long n, const int32_t *__restrict__ kstart,
+                                int kloop, int KEY, const int *__restrict__ fidx, const YDesc *__restrict__ yd,
+                                const double *__restrict__ Y, int np, const double *__restrict__ PF,
+                                const double *__restrict__ QF, int ld, const int *__restrict__ MF,
+                                const double *__restrict__ R, const double *__restrict__ RP,
+                                const double *__restrict__ RPOR, QuadConst q, double *__restrict__ val,
+                                QuadItem *__restrict__ fb, int *__restrict__ nfb) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    int p = ind[i];
+    const int d = p % KEY;
+    p /= KEY;
+    const int c = p % KEY;
+    p /= KEY;
+    const int b = p % KEY, a = p / KEY;
+    int k = 0;
+    while (k < kloop && (long long)kstart[k + 1] - 1 <= i) ++k;
+    const int f = fidx[((size_t)k * KEY + b) * KEY + d];
+    if (f < 0) {
+      atomicExch(nfb + 1, 1);
+      continue;
+    }
+    rk_head_store(k, a, c, f, i, val[i], yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val, fb, nfb);
+  }
+}
+
 __global__ void k_quad_items(const QuadItem *__restrict__ items, const int *__restrict__ nitems_p, int nitems_max,
                              const double *__restrict__ Y, int np, const double *__restrict__ PF,
                              const double *__restrict__ QF, int ld, const double *__restrict__ R,
@@ -744,7 +1016,7 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   // contraction problems (k, a); each problem's entries are contiguous.
   rk.kstart.assign(kloop + 2, 0);
   rk.hInd.clear();
-  std::vector<RkTile> tiles;
+  std::vector<RkTile> tiles, tiles_tc;
   std::vector<int> rowpair;
   int64_t N = 0;
   rk.kstart[0] = 1;
@@ -779,6 +1051,21 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
           t.c1 = std::min(c1, cc + BN);
           t.base = base;
           tiles.push_back(t);
+        }
+      // tiles of the tcgen05 form: TC_N rows x TC_M Y functions
+      for (int r0 = 0; r0 < ncA; r0 += TC_N)
+        for (int cc = c0; cc < c1; cc += TC_M) {
+          RkTile t;
+          t.k = k;
+          t.a = a;
+          t.ncA = ncA;
+          t.r0 = r0;
+          t.rowpair0 = rp0;
+          t.cs_a = c0;
+          t.c0 = cc;
+          t.c1 = std::min(c1, cc + TC_M);
+          t.base = base;
+          tiles_tc.push_back(t);
         }
     }
     rk.kstart[k + 1] = (int32_t)(N + 1);
@@ -816,8 +1103,8 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
     GG_CUDA(cudaGetLastError());
   }
   GG_TRY(dFb.alloc(std::max<int64_t>(N, 1)));
-  GG_TRY(dNfb.alloc(2));  // [0] fallback count, [1] position error flag
-  GG_CUDA(cudaMemsetAsync(dNfb.p, 0, 2 * sizeof(int), ctx->stream));
+  GG_TRY(dNfb.alloc(3));  // [0] fallback count, [1] position error flag, [2] tensor-core wait timed out
+  GG_CUDA(cudaMemsetAsync(dNfb.p, 0, 3 * sizeof(int), ctx->stream));
   DBuf<signed char> dAs, dYs;
   DBuf<int> dEA, dEY;
   if (!tiles.empty() && precision == GG_SPLIT) {
@@ -829,9 +1116,43 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
     GG_TRY(dEY.alloc(nf + 1));
     k_oz_split<<<npairs + 1, 128, 0, ctx->stream>>>(dA.p, npairs, KC, KC, KP, dAs.p, dEA.p); ::gg::note_launch();
     k_oz_split<<<nf + 1, 128, 0, ctx->stream>>>(dY.p, nf, np, KC, KP, dYs.p, dEY.p); ::gg::note_launch();
-    k_rk_ozaki<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(
-        dTiles.p, dRowpair.p, dPairs.p, dAs.p, dEA.p, npairs, dYs.p, dEY.p, nf, KP, dY.p, dYd.p, np, o.dPF.p, o.dQF.p,
-        o.ld, o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p); ::gg::note_launch();
+    static const bool mma_sync = [] {
+      const char *e = getenv("GRASP_GPU_RK_TENSOR");
+      return e && std::strcmp(e, "mma_sync") == 0;
+    }();
+    if (mma_sync) {  // the legacy int8 mma.sync form, kept for comparison
+      k_rk_ozaki<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(
+          dTiles.p, dRowpair.p, dPairs.p, dAs.p, dEA.p, npairs, dYs.p, dEY.p, nf, KP, dY.p, dYd.p, np, o.dPF.p,
+          o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p);
+      ::gg::note_launch();
+    } else {
+      // tcgen05: raw GEMM parts at their positions, then the head terms
+      std::vector<int> fidx((size_t)(kloop + 1) * KEY * KEY, -1);
+      for (int f = 0; f < nf; ++f) fidx[((size_t)yd[f].k * KEY + yd[f].b) * KEY + yd[f].d] = f;
+      DBuf<RkTile> dTc;
+      DBuf<int> dFidx;
+      DBuf<int32_t> dKst;
+      GG_TRY(upload(dTc, tiles_tc, ctx->stream));
+      GG_TRY(upload(dFidx, fidx, ctx->stream));
+      GG_TRY(upload(dKst, rk.kstart, ctx->stream));
+      static bool attr = false;
+      if (!attr) {
+        GG_CUDA(cudaFuncSetAttribute(k_rk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
+        attr = true;
+      }
+      k_rk_tc<<<(unsigned)tiles_tc.size(), 128, TC_SMEM, ctx->stream>>>(dTc.p, dRowpair.p, dAs.p, dEA.p, npairs,
+                                                                          dYs.p, dEY.p, nf, KP, dYd.p, rk.dVal.p,
+                                                                          (long long)N, dNfb.p + 1);
+      ::gg::note_launch();
+      GG_CUDA(cudaGetLastError());
+      const unsigned fb_blocks = (unsigned)std::min<long long>((N + 255) / 256, 8LL * ctx->sms);
+      k_rk_finish_all<<<std::max(1u, fb_blocks), 256, 0, ctx->stream>>>(
+          rk.dInd.p, (long long)N, dKst.p, kloop, KEY, dFidx.p, dYd.p, dY.p, np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p,
+          g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, dFb.p, dNfb.p);
+      ::gg::note_launch();
+      GG_CUDA(cudaGetLastError());
+      GG_CUDA(cudaStreamSynchronize(ctx->stream));  // the tile and index uploads are freed on return
+    }
     GG_CUDA(cudaGetLastError());
   } else if (!tiles.empty()) {
     k_rk_gemm<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(dTiles.p, dRowpair.p, dPairs.p, dA.p, dY.p, dYd.p, KC,
@@ -839,10 +1160,11 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
                                                               g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
-  int hfb[2] = {0, 0};
-  GG_CUDA(cudaMemcpyAsync(hfb, dNfb.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  int hfb[3] = {0, 0, 0};
+  GG_CUDA(cudaMemcpyAsync(hfb, dNfb.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (hfb[1]) return fail(GG_ERR_STATE, "genintrk: contraction produced a table position out of range");
+  if (hfb[2]) return fail(GG_ERR_STATE, "genintrk: tensor-core contraction timed out waiting for its MMAs");
   const int nfb = hfb[0];
   ctx->stats[20] = nfb;
   if (nfb > 0) {

@@ -106,3 +106,28 @@ def test_batched_rejects_bad_arguments(gpu_ready):
         maneig_batched(ctx, hs, 17)             # more than 16 roots per block
     with pytest.raises(GGError):
         maneig_batched(ctx, hs, 3, lim=4)       # LIM below 2 NVEC
+
+
+def test_batched_tiny_blocks_and_two_contexts(gpu_ready, oracle_mod):
+    """Blocks of 1, 2 and 5 CSFs (NVEC up to NCF: the full unit basis),
+    together with ordinary blocks assembled on a second context (another
+    ion), in one batched call; each block against the oracle's MANEIG."""
+    import oracle
+    from grasp_gb300 import Context, maneig_batched, workloads as W
+    tiny = [W.batch(zs=(10,), two_js=(0,), parities=(0,), max_ncf=c) for c in (1, 2, 5)]
+    big = W.batch(zs=(23,), two_js=(4,), parities=(1,))
+    c1, c2 = Context(0), Context(0)
+    hs, blocks = [], []
+    for w in tiny:
+        hs += W.assemble_batch(w, c1)
+        blocks.append(w.blocks[0][2])
+    hs += W.assemble_batch(big, c2)
+    blocks.append(big.blocks[0][2])
+    assert [b.ncf for b in blocks[:3]] == [1, 2, 5]
+    nvec = [1, 2, 5, 3]
+    res, info = maneig_batched(c1, hs, nvec)
+    assert (info["ierr"] == 0).all()
+    for (ev, vec), H, b, r in zip(res, hs, blocks, nvec):
+        ev0, vec0, _ = oracle.maneig(0, b.ncf, r, b.iendc, b.irow, H.emt())
+        assert np.abs(ev - ev0).max() <= EV_TOL, (b.ncf, ev, ev0)
+        assert np.abs(vec - vec0).max() <= VEC_TOL, b.ncf
