@@ -299,7 +299,7 @@ def run_reference(a):
 # ---------------------------------------------------------------------------
 def solve_resident(ctx, H, nroots, precision, mblock=0):
     ctx.mark(0)
-    ctx.genintrk()
+    ctx.genintrk(precision=precision)  # split: the R^k contraction on the tensor cores
     ctx.iabint_table()
     H.setham_assemble()
     ev, vec, info = H.maneig(nroots, flavour=0, precision=precision, mblock=mblock)
@@ -317,7 +317,7 @@ def solve_e2e(w, precision, device, arrays, mblock=0):
     ctx = Context(device)
     ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
     ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
-    ctx.genintrk()
+    ctx.genintrk(precision=precision)
     ctx.iabint_table()
     H = HMatrix(ctx, b.ncf, b.iendc, b.irow)
     H.setham(b.iq, b.tlist, b.vlists)

@@ -82,6 +82,7 @@ int gg_ctx_destroy(gg_ctx *ctx) {
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  gg::rk_cache_free(ctx->rk.cache);
   delete ctx;
   return GG_OK;
 }

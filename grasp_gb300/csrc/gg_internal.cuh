@@ -88,7 +88,11 @@ struct Orbitals {
   DBuf<int> dMF, dNAK;                  // 1-based
 };
 
+struct RkCache;  // radial.cu: GENINTRK's orbital-set structure, reused between calls
+void rk_cache_free(RkCache *c);
+
 struct RkTable {
+  RkCache *cache = nullptr;
   int kloop = -1, j2max = 0;
   int64_t n = 0;
   std::vector<int32_t> kstart;          // KSTART(0:kloop+1)

@@ -496,30 +496,78 @@ __global__ void __launch_bounds__(256) k_rk_ozaki(const RkTile *__restrict__ til
 // ---------------------------------------------------------------------------
 // The Ozaki contraction on GB300's fifth-generation tensor cores (tcgen05).
 //
-// One CTA per tile of TC_M = 128 Y functions (the MMA's M) x TC_N = 32 rows
-// (a, c) pairs (N). Per stage of TC_KC = 32 grid points every thread converts
-// its share of the int8 slices (|q| <= 64) to fp16, which holds them exactly,
-// and stores them in the no-swizzle K-major core-matrix layout (8 rows x 16 B
-// per core matrix; neighbours in K 128 B apart, in M/N 256 B apart); then one
-// thread issues, per K = 16 step, the 55 slice-pair MMAs
-// tcgen05.mma.cta_group::1.kind::f16 into the accumulator of their group
-// q = s + t (OZ_S groups x TC_N FP32 columns of tensor memory). Two stages
-// alternate; tcgen05.commit to a per-stage mbarrier tells when a stage may
-// be refilled. Every TC_FLUSH stages (256 grid points, while every group sum
-// is still an exact integer below 2^24) the four warps read their 32 lanes
-// of each group (tcgen05.ld) and fold group q, scaled by 2^(-7q), into
-// double-float sums; the next MMA of each group then overwrites. The raw sum
-// 2^(eA+eY-14) (h + l) is stored at the entry's GENINTRK position; the head
-// term is added by k_rk_finish_all. Every wait is bounded: on a timeout the
-// CTA sets err, waits (bounded) for its issued MMAs, frees its tensor memory
-// and returns without writing.
+// For each k the rows of all (k, a) problems (the (a, c) pairs with a <= c
+// and TRIANGRK(l_a, k, l_c), in GENINTRK's order) and all Y functions of k
+// form one GEMM, cut into tiles of TC_M = 128 functions (the MMA's M) x
+// TC_N = 48 rows (N); tiles that hold no needed entry (b < a for all) are
+// skipped. k_oz_tile writes the int8-range slices (|q| <= 64) as fp16, which
+// holds them exactly, straight into per-tile blocks laid out as the MMA reads
+// them from shared memory (no-swizzle K-major core matrices: 8 rows x 16 B,
+// neighbours in K 128 B apart, in M/N 256 B apart), one block per 32 grid
+// points: 80 KB of Y slices, 30 KB of A slices.
+//
+// k_rk_tc, one CTA per tile, is warp-specialised. Warp 4 streams the blocks
+// into two shared-memory stages with cp.async.bulk (completion counted in
+// bytes on a per-stage "full" mbarrier) and issues, per K = 16 step, the 55
+// slice-pair MMAs tcgen05.mma.cta_group::1.kind::f16 into the FP32 tensor-
+// memory accumulator of their group q = s + t (OZ_S x TC_N columns); a
+// tcgen05.commit to the stage's "empty" mbarrier frees the stage. Every
+// TC_FLUSH stages (256 grid points, while every group sum is still an exact
+// integer below 2^24) warps 0-3 read their 32 lanes of each group
+// (tcgen05.ld) and fold group q, scaled by 2^(-7q), into double-float sums;
+// the next MMA of each group overwrites. The raw sum 2^(eA+eY-14) (h + l) is
+// stored at the entry's GENINTRK position; k_rk_finish_all adds the head
+// term. Every wait is bounded: on a timeout the CTA records it, waits
+// (bounded) for what it issued, frees its tensor memory and writes nothing.
 // ---------------------------------------------------------------------------
-constexpr int TC_M = 128, TC_N = 32, TC_KC = 32, TC_FLUSH = 8;
-constexpr int TC_YST = OZ_S * 2 * (TC_M / 8) * 2 * 64;  // fp16 elements per Y stage (80 KB)
-constexpr int TC_AST = OZ_S * 2 * (TC_N / 8) * 2 * 64;  // fp16 elements per A stage (20 KB)
-constexpr size_t TC_SMEM = (size_t)2 * (TC_YST + TC_AST) * sizeof(__half) + 64;
+constexpr int TC_M = 128, TC_N = 48, TC_KC = 32, TC_FLUSH = 8;
+constexpr int TC_YBLK = OZ_S * 2 * (TC_M / 8) * 2 * 64;  // fp16 elements per Y block (80 KB)
+constexpr int TC_ABLK = OZ_S * 2 * (TC_N / 8) * 2 * 64;  // fp16 elements per A block (30 KB)
+constexpr size_t TC_SMEM = (size_t)2 * (TC_YBLK + TC_ABLK) * sizeof(__half) + 128;
 constexpr uint32_t TC_TMEM_COLS = 512;  // >= OZ_S * TC_N, a power of two
 constexpr int TC_SPIN = 1 << 24;
+constexpr int TC_THREADS = 160;  // warps 0-3: accumulators; warp 4: copies and MMAs
+
+struct TcRow {  // one row of a k: its pair, problem and position data
+  int p, a, ic, ncA, cs_a;
+  long long base;
+};
+struct TcTile {
+  int k, fg, pg;  // k; global indices of the Y block column and the A block column
+  int f0, fn;     // first Y function and how many are valid
+  int r0, rn;     // first row (TcRow index) and how many are valid
+};
+
+}  // namespace
+
+// GENINTRK's orbital-set-dependent structure and its work buffers, kept on
+// the context between calls (gg_genintrk rebuilds it when the orbitals' l, j
+// or kmax change)
+struct RkCache {
+  std::vector<int> key;
+  int nf = 0, npairs = 0;
+  std::vector<YDesc> yd;
+  std::vector<int> kend, rowpair, yslot, aslot, fidx;
+  std::vector<int2> pairs;
+  std::vector<RkTile> tiles;
+  std::vector<TcRow> tcrows;
+  std::vector<TcTile> tct;
+  DBuf<YDesc> dYd;
+  DBuf<int2> dPairs;
+  DBuf<RkTile> dTiles;
+  DBuf<int> dRowpair, dYslot, dAslot, dFidx, dNfb, dEA, dEY;
+  DBuf<int32_t> dKst;
+  DBuf<TcTile> dTct;
+  DBuf<TcRow> dTcr;
+  DBuf<double> dY, dA, scratch;
+  DBuf<QuadItem> dFb;
+  DBuf<__half> dYt, dAt;
+  DBuf<signed char> dAs, dYs;
+};
+
+void rk_cache_free(RkCache *c) { delete c; }
+
+namespace {
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -541,175 +589,237 @@ __device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
   return done != 0;
 }
 
-// 8 signed bytes -> 8 fp16 values (16 bytes)
-__device__ __forceinline__ int4 tc_cvt8(uint32_t lo, uint32_t hi) {
-  __half2 h[4];
-#pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    const uint32_t w = (b < 2) ? lo : hi;
-    const int sh = (b & 1) * 16;
-    const int v0 = (int)(signed char)((w >> sh) & 0xffu), v1 = (int)(signed char)((w >> (sh + 8)) & 0xffu);
-    h[b] = __halves2half2(__int2half_rn(v0), __int2half_rn(v1));
+// Slices of rows into their tile blocks: one CTA per row slot (slot = tile
+// block column g, row m < R); src_row[slot] < 0 pads with zeros. The row's
+// exponent goes to exps[src_row] (the same row always gets the same value).
+template <int R>
+__global__ void k_oz_tile(const double *__restrict__ M, int pitch, int K, int nch, const int *__restrict__ src_row,
+                          int *__restrict__ exps, __half *__restrict__ dst) {
+  constexpr int BLK = OZ_S * 2 * (R / 8) * 2 * 64;
+  const int slot = blockIdx.x, g = slot / R, m = slot % R;
+  const int row = src_row[slot];
+  __shared__ double red[128];
+  double mx = 0.0;
+  if (row >= 0)
+    for (int i = threadIdx.x; i < K; i += blockDim.x) mx = fmax(mx, fabs(M[(size_t)row * pitch + i]));
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int st = 64; st > 0; st >>= 1) {
+    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
+    __syncthreads();
   }
-  int4 r;
-  memcpy(&r, h, sizeof(r));
-  return r;
+  mx = red[0];
+  const int e = (mx > 0.0) ? ilogb(mx) + 2 : 0;  // mx < 2^(e-1)
+  if (threadIdx.x == 0 && row >= 0) exps[row] = e;
+  __half *base = dst + (size_t)g * nch * BLK;
+  const int KP = nch * TC_KC;
+  for (int i = threadIdx.x; i < KP; i += blockDim.x) {
+    // x 2^35 = X1 + d exactly with X1 = rint(x 2^35), |d| <= 1/2 (|x| < 1/2);
+    // X2 = rint(d 2^35); x = (X1 + X2 2^-35) 2^-35 to 2^-71, |X1|, |X2| <= 2^34.
+    // Each of X1 and X2 gives five balanced base-128 digits (|digit| <= 64)
+    // in integer arithmetic: only the two roundings use the FP64 pipe, which
+    // GB300 issues slowly.
+    const double xs = (row >= 0 && i < K) ? scalbn(M[(size_t)row * pitch + i], 35 - e) : 0.0;
+    const double x1 = rint(xs);
+    long long X[2] = {(long long)x1, (long long)rint((xs - x1) * 34359738368.0)};  // 2^35
+    int dg[OZ_S];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      long long v = X[h];
+#pragma unroll
+      for (int u = 4; u >= 1; --u) {
+        const int r = (int)(((v + 64) & 127) - 64);  // balanced remainder in [-64, 63]
+        dg[h * 5 + u] = r;
+        v = (v - r) >> 7;
+      }
+      dg[h * 5] = (int)v;  // |v| <= 64
+    }
+    const int c = i / TC_KC, kk = i % TC_KC, j = kk / 16, k8 = (kk / 8) % 2, el = kk % 8;
+    __half *blk = base + (size_t)c * BLK + ((size_t)(m / 8) * 2 + k8) * 64 + (m % 8) * 8 + el;
+#pragma unroll
+    for (int q = 0; q < OZ_S; ++q) blk[(size_t)(q * 2 + j) * (R / 8) * 2 * 64] = __int2half_rn(dg[q]);
+  }
 }
 
-// one row's 32 slice bytes at src into the stage: 4 groups of 8 grid points,
-// group g = (K step j = g / 2, core column k8 = g % 2)
-__device__ __forceinline__ void tc_row(const signed char *__restrict__ src, __half *dst, int rows8, int slice,
-                                       int row) {
-  const int4 v0 = __ldg(reinterpret_cast<const int4 *>(src));
-  const int4 v1 = __ldg(reinterpret_cast<const int4 *>(src + 16));
-  const uint32_t w[8] = {(uint32_t)v0.x, (uint32_t)v0.y, (uint32_t)v0.z, (uint32_t)v0.w,
-                         (uint32_t)v1.x, (uint32_t)v1.y, (uint32_t)v1.z, (uint32_t)v1.w};
-#pragma unroll
-  for (int g = 0; g < 4; ++g) {
-    const int j = g >> 1, k8 = g & 1;
-    *reinterpret_cast<int4 *>(dst + (((slice * 2 + j) * rows8 + row / 8) * 2 + k8) * 64 + (row % 8) * 8) =
-        tc_cvt8(w[2 * g], w[2 * g + 1]);
-  }
-}
-
-__global__ void __launch_bounds__(128, 1) k_rk_tc(const RkTile *__restrict__ tiles, const int *__restrict__ rowpair,
-                                                  const signed char *__restrict__ As, const int *__restrict__ eA,
-                                                  int npairs, const signed char *__restrict__ Ys,
-                                                  const int *__restrict__ eY, int nf, int KP,
-                                                  const YDesc *__restrict__ yd, double *__restrict__ val,
-                                                  long long nval, int *__restrict__ flags) {
+__global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restrict__ tiles,
+                                                         const TcRow *__restrict__ rows,
+                                                         const __half *__restrict__ Yt,
+                                                         const __half *__restrict__ At, int nch,
+                                                         const int *__restrict__ eA, const int *__restrict__ eY,
+                                                         const YDesc *__restrict__ yd, double *__restrict__ val,
+                                                         long long nval, int *__restrict__ flags) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   __half *Ysm = reinterpret_cast<__half *>(tsm);
-  __half *Asm = Ysm + 2 * TC_YST;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(Asm + 2 * TC_AST);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(mbar + 2);
-  __shared__ int prow[TC_N];
-  const RkTile T = tiles[blockIdx.x];
-  const int tid = threadIdx.x, warp = tid >> 5;
-  const int nrow = min(TC_N, T.ncA - T.r0), ncol = T.c1 - T.c0;
-  if (tid < TC_N) prow[tid] = (tid < nrow) ? rowpair[T.rowpair0 + T.r0 + tid] : npairs;
+  __half *Asm = Ysm + 2 * TC_YBLK;
+  uint64_t *full = reinterpret_cast<uint64_t *>(Asm + 2 * TC_ABLK);
+  uint64_t *empty = full + 2;
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(empty + 2);
+  int *okflag = reinterpret_cast<int *>(tslot + 1);
+  __shared__ TcRow trow[TC_N];
+  const TcTile T = tiles[blockIdx.x];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid < TC_N) trow[tid] = (tid < T.rn) ? rows[T.r0 + tid] : TcRow{-1, 0, 0, 0, 0, 0};
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tslot)),
                  "r"(TC_TMEM_COLS));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&mbar[0])), "r"(1));
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&mbar[1])), "r"(1));
+    for (int st = 0; st < 2; ++st) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&full[st])), "r"(1));
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&empty[st])), "r"(1));
+    }
+    *okflag = 1;
     asm volatile("fence.mbarrier_init.release.cluster;");
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tslot;
-  const uint32_t idesc = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
-  const size_t aplane = (size_t)(npairs + 1) * KP, yplane = (size_t)(nf + 1) * KP;
-  const int myf = (tid < ncol) ? T.c0 + tid : nf;  // Y row of this thread (zero row pads)
-  float ah[TC_N], al[TC_N];
-#pragma unroll
-  for (int n = 0; n < TC_N; ++n) ah[n] = al[n] = 0.f;
-  const int nch = KP / TC_KC;
-  uint32_t fresh = (1u << OZ_S) - 1;  // groups whose next MMA overwrites (thread 0)
-  int last_commit = -1;
-  bool ok = true;
-  for (int j = 0; j < nch && ok; ++j) {
-    const int st = j & 1, k0 = j * TC_KC;
-    if (j >= 2) ok = tc_wait(smem_addr(&mbar[st]), ((j - 2) >> 1) & 1);
-    if (ok) {
-      __half *ydst = Ysm + st * TC_YST;
-      for (int t = 0; t < OZ_S; ++t) tc_row(Ys + t * yplane + (size_t)myf * KP + k0, ydst, TC_M / 8, t, tid);
-      __half *adst = Asm + st * TC_AST;
-      for (int it = tid; it < OZ_S * TC_N; it += blockDim.x) {
-        const int sl = it / TC_N, n = it % TC_N;
-        tc_row(As + sl * aplane + (size_t)prow[n] * KP + k0, adst, TC_N / 8, sl, n);
+  const int nflush = (nch + TC_FLUSH - 1) / TC_FLUSH;
+  if (warp == 4) {
+    // copies and MMAs (lane 0 issues; the warp stays converged)
+    const uint32_t idesc = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+    const char *ysrc = reinterpret_cast<const char *>(Yt + (size_t)T.fg * nch * TC_YBLK);
+    const char *asrc = reinterpret_cast<const char *>(At + (size_t)T.pg * nch * TC_ABLK);
+    constexpr uint32_t YB = TC_YBLK * sizeof(__half), AB = TC_ABLK * sizeof(__half);
+    auto copy = [&](int j) {
+      const int st = j & 1;
+      if (lane == 0) {
+        const uint32_t fb = smem_addr(&full[st]);
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fb), "r"(YB + AB) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_addr(Ysm + st * TC_YBLK)),
+            "l"(ysrc + (size_t)j * YB), "r"(YB), "r"(fb)
+            : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                smem_addr(Asm + st * TC_ABLK)),
+            "l"(asrc + (size_t)j * AB), "r"(AB), "r"(fb)
+            : "memory");
+      }
+      __syncwarp();
+    };
+    bool ok = true;
+    uint32_t fresh = (1u << OZ_S) - 1;
+    int issued = -1;  // last chunk whose MMAs were committed
+    copy(0);
+    int fl = 0;
+    for (int j = 0; j < nch; ++j) {
+      const int st = j & 1;
+      if (ok) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&full[st]), (j >> 1) & 1));
+      if (ok) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (lane == 0) {
+          const uint32_t yb = smem_addr(Ysm + st * TC_YBLK), ab = smem_addr(Asm + st * TC_ABLK);
+#pragma unroll 1
+          for (int ks = 0; ks < 2; ++ks)
+#pragma unroll 1
+            for (int sa = 0; sa < OZ_S; ++sa) {
+              const uint64_t bdesc = tc_desc(ab + (uint32_t)(sa * 2 + ks) * ((TC_N / 8) * 2 * 64 * 2));
+#pragma unroll 1
+              for (int t = 0; t < OZ_S - sa; ++t) {
+                const int qg = sa + t;
+                const uint64_t adesc = tc_desc(yb + (uint32_t)(t * 2 + ks) * ((TC_M / 8) * 2 * 64 * 2));
+                const uint32_t accum = ((fresh >> qg) & 1u) ? 0u : 1u;
+                fresh &= ~(1u << qg);
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(
+                        tmem + (uint32_t)(qg * TC_N)),
+                    "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
+              }
+            }
+          asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                           smem_addr(&empty[st]))
+                       : "memory");
+        }
+        __syncwarp();
+        issued = j;
+        // refill the other stage with chunk j + 1 once chunk j - 1's MMAs are done
+        if (j + 1 < nch) {
+          if (j >= 1) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&empty[(j - 1) & 1]), ((j - 1) >> 1) & 1));
+          if (ok) copy(j + 1);
+        }
+      }
+      if ((j + 1) % TC_FLUSH == 0 || j == nch - 1) {
+        if (ok) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&empty[st]), (j >> 1) & 1));  // MMAs done
+        if (!ok && lane == 0) *okflag = 0;
+        asm volatile("tcgen05.fence::before_thread_sync;");
+        __syncthreads();  // A: the accumulators are ready (or the flag says no)
+        __syncthreads();  // B: warps 0-3 have read them
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        fresh = (1u << OZ_S) - 1;
+        ++fl;
       }
     }
-    asm volatile("fence.proxy.async.shared::cta;");
-    asm volatile("tcgen05.fence::before_thread_sync;");
-    ok = __syncthreads_and(ok);
-    asm volatile("tcgen05.fence::after_thread_sync;");
-    if (!ok) break;
-    if (tid == 0) {
-      const uint32_t yb = smem_addr(Ysm + st * TC_YST), ab = smem_addr(Asm + st * TC_AST);
-#pragma unroll 1
-      for (int ks = 0; ks < 2; ++ks)
-#pragma unroll 1
-        for (int sa = 0; sa < OZ_S; ++sa) {
-          const uint64_t bdesc = tc_desc(ab + (uint32_t)(sa * 2 + ks) * ((TC_N / 8) * 2 * 64 * 2));
-#pragma unroll 1
-          for (int t = 0; t < OZ_S - sa; ++t) {
-            const int qg = sa + t;
-            const uint64_t adesc = tc_desc(yb + (uint32_t)(t * 2 + ks) * ((TC_M / 8) * 2 * 64 * 2));
-            const uint32_t accum = ((fresh >> qg) & 1u) ? 0u : 1u;
-            fresh &= ~(1u << qg);
-            asm volatile(
-                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}" ::"r"(tmem + (uint32_t)(qg * TC_N)),
-                "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accum));
-          }
-        }
-      asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                       smem_addr(&mbar[st]))
-                   : "memory");
+    for (; fl < nflush; ++fl) {  // a failed wait leaves the loop early: meet the remaining barriers
+      __syncthreads();
+      __syncthreads();
     }
-    last_commit = j;
-    if ((j + 1) % TC_FLUSH == 0 || j == nch - 1) {
-      ok = tc_wait(smem_addr(&mbar[st]), (j >> 1) & 1);  // every MMA issued so far is done
+    if (!ok && lane == 0) {
+      atomicExch(flags + 1, 1);  // timed out
+      if (issued >= 0) tc_wait(smem_addr(&empty[issued & 1]), (issued >> 1) & 1);
+    }
+  } else {
+    // warps 0-3: lane quadrant `warp` of each group accumulator
+    float ah[TC_N], al[TC_N];
+#pragma unroll
+    for (int n = 0; n < TC_N; ++n) ah[n] = al[n] = 0.f;
+    for (int fl = 0; fl < nflush; ++fl) {
+      __syncthreads();  // A
       asm volatile("tcgen05.fence::after_thread_sync;");
-      if (__all_sync(0xffffffffu, ok)) {
+      if (*okflag) {
 #pragma unroll 1
         for (int qg = 0; qg < OZ_S; ++qg) {
-          uint32_t r[32];
-          const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(qg * TC_N);
-          asm volatile(
-              "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-              "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-              : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
-                "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
-                "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-              : "r"(taddr));
-          asm volatile("tcgen05.wait::ld.sync.aligned;");
           const float scale = __int_as_float((127 - 7 * qg) << 23);  // 2^(-7 qg)
 #pragma unroll
-          for (int n = 0; n < TC_N; ++n) {
-            // (ah, al) += v exactly in the high part (TwoSum), errors into al
-            const float v = __uint_as_float(r[n]) * scale;
-            const float sv = ah[n] + v;
-            const float bb = sv - ah[n];
-            const float e = (ah[n] - (sv - bb)) + (v - bb);
-            ah[n] = sv;
-            al[n] = al[n] + e;
+          for (int h = 0; h < TC_N / 16; ++h) {
+            uint32_t r[16];
+            const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(qg * TC_N + h * 16);
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;");
+#pragma unroll
+            for (int u = 0; u < 16; ++u) {
+              // (ah, al) += v: TwoSum into the high part, the error into al
+              const int n = h * 16 + u;
+              const float v = __uint_as_float(r[u]) * scale;
+              const float sv = ah[n] + v;
+              const float bb = sv - ah[n];
+              const float e = (ah[n] - (sv - bb)) + (v - bb);
+              ah[n] = sv;
+              al[n] = al[n] + e;
+            }
           }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;");
-      ok = __syncthreads_and(ok);
-      asm volatile("tcgen05.fence::after_thread_sync;");
-      if (tid == 0) fresh = (1u << OZ_S) - 1;
+      __syncthreads();  // B
     }
-  }
-  if (!ok) {
-    if (tid == 0) {
-      atomicExch(flags + 1, 1);  // timed out
-      if (last_commit >= 0) tc_wait(smem_addr(&mbar[last_commit & 1]), (last_commit >> 1) & 1);
-    }
-  } else if (tid < ncol) {
-    const int f = T.c0 + tid;
-    const YDesc y = yd[f];
-    const int ey = eY[f];
+    const int m = warp * 32 + lane;
+    if (*okflag && m < T.fn) {
+      const int f = T.f0 + m;
+      const YDesc y = yd[f];
+      const int ey = eY[f];
 #pragma unroll
-    for (int n = 0; n < TC_N; ++n) {
-      if (n >= nrow) break;
-      const long long pos =
-          T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)(T.r0 + n) * y.nd + (long long)(f - y.cs);
-      if (pos < 0 || pos >= nval) {
-        atomicExch(flags, 1);  // position outside the table
-        continue;
+      for (int n = 0; n < TC_N; ++n) {
+        const TcRow rw = trow[n];
+        if (n >= T.rn || f < rw.cs_a) continue;  // padding, or b < a: not a GENINTRK entry
+        const long long pos =
+            rw.base + (long long)rw.ncA * (y.cs - rw.cs_a) + (long long)rw.ic * y.nd + (long long)(f - y.cs);
+        if (pos < 0 || pos >= nval) {
+          atomicExch(flags, 1);  // position outside the table
+          continue;
+        }
+        val[pos] = scalbn((double)ah[n] + (double)al[n], eA[rw.p] + ey - 14);
       }
-      const int ex = eA[prow[n]] + ey - 14;
-      val[pos] = scalbn((double)ah[n] + (double)al[n], ex);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;");
@@ -965,25 +1075,20 @@ using namespace gg;
 
 extern "C" {
 
-int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max_out) {
-  GG_TRY(ensure_orbitals(ctx));
-  if (precision != GG_FP64 && precision != GG_SPLIT) return fail(GG_ERR_ARG, "gg_genintrk: unknown precision");
-  GG_CUDA(cudaSetDevice(ctx->device));
+// The part of GENINTRK that depends only on the orbitals' l and j and on
+// kmax: Y functions, pairs, INDTEIRK and KSTART, the contraction tiles of
+// both forms, and their device copies. Built once per orbital set.
+static int rk_build_structure(gg_ctx *ctx, int kloop, RkCache &C) {
   Grid &g = ctx->grid;
   Orbitals &o = ctx->orb;
   RkTable &rk = ctx->rk;
   const int NW = o.nw, KEY = NW + 1;
-  int j2max = o.nkj[1];
-  for (int i = 2; i <= NW; ++i) j2max = std::max(j2max, o.nkj[i]);
-  if (j2max > KLIMIT) return fail(GG_ERR_ARG, "genintrk: KMAX too small");
-  const int kloop = kmax < 0 ? j2max : kmax;
-  if (kloop > KLIMIT) return fail(GG_ERR_ARG, "genintrk: k beyond KLIMIT = 20");
-  GG_TRY(timer_start(ctx));
-
   // Y functions, ordered (k, b, d): D(b,k) = {d >= b : TRIANGRK(l_b, k, l_d)}
-  std::vector<YDesc> yd;
+  std::vector<YDesc> &yd = C.yd;
+  yd.clear();
   std::vector<std::vector<int>> cs(kloop + 1, std::vector<int>(NW + 2, -1)), nd(kloop + 1, std::vector<int>(NW + 2, 0));
-  std::vector<int> kend(kloop + 1, 0);
+  std::vector<int> &kend = C.kend;
+  kend.assign(kloop + 1, 0);
   for (int k = 0; k <= kloop; ++k) {
     for (int b = 1; b <= NW; ++b) {
       cs[k][b] = (int)yd.size();
@@ -1005,7 +1110,8 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
     kend[k] = (int)yd.size();
   }
   // pair list for the A rows (a <= c), k-independent
-  std::vector<int2> pairs;
+  std::vector<int2> &pairs = C.pairs;
+  pairs.clear();
   std::vector<int> pidx((size_t)(NW + 1) * (NW + 1), -1);
   for (int a = 1; a <= NW; ++a)
     for (int c = a; c <= NW; ++c) {
@@ -1016,11 +1122,17 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   // contraction problems (k, a); each problem's entries are contiguous.
   rk.kstart.assign(kloop + 2, 0);
   rk.hInd.clear();
-  std::vector<RkTile> tiles, tiles_tc;
-  std::vector<int> rowpair;
+  std::vector<RkTile> &tiles = C.tiles;
+  std::vector<int> &rowpair = C.rowpair;
+  std::vector<TcRow> &tcrows = C.tcrows;
+  tiles.clear();
+  rowpair.clear();
+  tcrows.clear();
+  std::vector<int> tcr0(kloop + 2, 0);  // first tcrows entry of each k
   int64_t N = 0;
   rk.kstart[0] = 1;
   for (int k = 0; k <= kloop; ++k) {
+    tcr0[k] = (int)tcrows.size();
     for (int a = 1; a <= NW; ++a) {
       const int ncA = nd[k][a];
       if (ncA == 0) continue;
@@ -1052,116 +1164,198 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
           t.base = base;
           tiles.push_back(t);
         }
-      // tiles of the tcgen05 form: TC_N rows x TC_M Y functions
-      for (int r0 = 0; r0 < ncA; r0 += TC_N)
-        for (int cc = c0; cc < c1; cc += TC_M) {
-          RkTile t;
-          t.k = k;
-          t.a = a;
-          t.ncA = ncA;
-          t.r0 = r0;
-          t.rowpair0 = rp0;
-          t.cs_a = c0;
-          t.c0 = cc;
-          t.c1 = std::min(c1, cc + TC_M);
-          t.base = base;
-          tiles_tc.push_back(t);
-        }
+      // rows of the tcgen05 form (all problems of one k, in order)
+      for (int ic = 0; ic < ncA; ++ic) tcrows.push_back(TcRow{rowpair[rp0 + ic], a, ic, ncA, c0, base});
     }
     rk.kstart[k + 1] = (int32_t)(N + 1);
   }
+  tcr0[kloop + 1] = (int)tcrows.size();
   if (N > INT32_MAX) return fail(GG_ERR_RANGE, "genintrk: table too large");
   rk.n = N;
+  C.nf = (int)yd.size();
+  C.npairs = (int)pairs.size();
+  const int nf = C.nf;
+  {
+  std::vector<int> fg0(kloop + 1), pg0(kloop + 1), kbeg(kloop + 1);
+  std::vector<int> &yslot = C.yslot, &aslot = C.aslot;
+  std::vector<TcTile> &tct = C.tct;
+  yslot.clear();
+  aslot.clear();
+  tct.clear();
+  for (int k = 0; k <= kloop; ++k) {
+    kbeg[k] = (k == 0) ? 0 : kend[k - 1];
+    const int F = kend[k] - kbeg[k], Rk = tcr0[k + 1] - tcr0[k];
+    const int nft = (F + TC_M - 1) / TC_M, npt = (Rk + TC_N - 1) / TC_N;
+    fg0[k] = (int)(yslot.size() / TC_M);
+    pg0[k] = (int)(aslot.size() / TC_N);
+    for (int ft = 0; ft < nft; ++ft)
+      for (int m = 0; m < TC_M; ++m) {
+        const int f = kbeg[k] + ft * TC_M + m;
+        yslot.push_back(f < kend[k] ? f : -1);
+      }
+    for (int pt = 0; pt < npt; ++pt)
+      for (int n = 0; n < TC_N; ++n) {
+        const int r = tcr0[k] + pt * TC_N + n;
+        aslot.push_back(r < tcr0[k + 1] ? tcrows[r].p : -1);
+      }
+    for (int pt = 0; pt < npt; ++pt)
+      for (int ft = 0; ft < nft; ++ft) {
+        TcTile t;
+        t.k = k;
+        t.fg = fg0[k] + ft;
+        t.pg = pg0[k] + pt;
+        t.f0 = kbeg[k] + ft * TC_M;
+        t.fn = std::min(TC_M, F - ft * TC_M);
+        t.r0 = tcr0[k] + pt * TC_N;
+        t.rn = std::min(TC_N, Rk - pt * TC_N);
+        // rows are ordered by a, so the first row has the smallest cs_a:
+        // no needed entry when every function of the tile is below it
+        if (t.f0 + t.fn - 1 < tcrows[t.r0].cs_a) continue;
+        tct.push_back(t);
+      }
+  }
+    std::vector<int> &fidx = C.fidx;
+    fidx.assign((size_t)(kloop + 1) * KEY * KEY, -1);
+    for (int f = 0; f < nf; ++f) fidx[((size_t)yd[f].k * KEY + yd[f].b) * KEY + yd[f].d] = f;
+  }
+  GG_TRY(upload(C.dPairs, pairs, ctx->stream));
+  GG_TRY(upload(C.dTiles, tiles, ctx->stream));
+  GG_TRY(upload(C.dRowpair, rowpair, ctx->stream));
+  GG_TRY(upload(C.dTct, C.tct, ctx->stream));
+  GG_TRY(upload(C.dTcr, tcrows, ctx->stream));
+  GG_TRY(upload(C.dYslot, C.yslot, ctx->stream));
+  GG_TRY(upload(C.dAslot, C.aslot, ctx->stream));
+  GG_TRY(upload(C.dFidx, C.fidx, ctx->stream));
+  GG_TRY(upload(C.dKst, rk.kstart, ctx->stream));
+  GG_TRY(rk.dInd.alloc(std::max<int64_t>(N, 1)));
+  if (N > 0)
+    GG_CUDA(cudaMemcpyAsync(rk.dInd.p, rk.hInd.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GG_OK;
+}
+
+int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max_out) {
+  GG_TRY(ensure_orbitals(ctx));
+  if (precision != GG_FP64 && precision != GG_SPLIT) return fail(GG_ERR_ARG, "gg_genintrk: unknown precision");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  Grid &g = ctx->grid;
+  Orbitals &o = ctx->orb;
+  RkTable &rk = ctx->rk;
+  const int NW = o.nw, KEY = NW + 1;
+  int j2max = o.nkj[1];
+  for (int i = 2; i <= NW; ++i) j2max = std::max(j2max, o.nkj[i]);
+  if (j2max > KLIMIT) return fail(GG_ERR_ARG, "genintrk: KMAX too small");
+  const int kloop = kmax < 0 ? j2max : kmax;
+  if (kloop > KLIMIT) return fail(GG_ERR_ARG, "genintrk: k beyond KLIMIT = 20");
+  GG_TRY(timer_start(ctx));
+  // the index structure is rebuilt only when the orbital set's l, j or kmax change
+  std::vector<int> key{NW, kloop};
+  for (int i = 1; i <= NW; ++i) {
+    key.push_back(o.nkl[i]);
+    key.push_back(o.nkj[i]);
+  }
+  if (!rk.cache) rk.cache = new RkCache();
+  RkCache &C = *rk.cache;
+  if (C.key != key) {
+    C.key.clear();  // not valid until built
+    rk.valid = false;
+    GG_TRY(rk_build_structure(ctx, kloop, C));
+    C.key = key;
+  }
+  const int64_t N = rk.n;
   rk.kloop = kloop;
   rk.j2max = j2max;
-  // device work
-  const int nf = (int)yd.size();
+  // per call: each Y function's MTP from the current orbital extents
+  for (YDesc &y : C.yd) {
+    y.mtp = std::min(o.mf[y.b], o.mf[y.d]);
+    y.mtpb = (y.k == 0 && y.b == y.d) ? g.n : y.mtp;
+  }
+  GG_TRY(upload(C.dYd, C.yd, ctx->stream));
+  const int nf = C.nf, npairs = C.npairs;
   const int np = g.np;
   const int KC = ((g.n + 1 + KC_TILE - 1) / KC_TILE) * KC_TILE;
   if (KC > np) return fail(GG_ERR_ARG, "genintrk: grid padding too small");
-  DBuf<YDesc> dYd;
-  DBuf<int2> dPairs;
-  DBuf<RkTile> dTiles;
-  DBuf<int> dRowpair, dNfb;
-  DBuf<double> dY, dA, scratch;
-  DBuf<QuadItem> dFb;
-  GG_TRY(upload(dYd, yd, ctx->stream));
-  GG_TRY(upload(dPairs, pairs, ctx->stream));
-  GG_TRY(upload(dTiles, tiles, ctx->stream));
-  GG_TRY(upload(dRowpair, rowpair, ctx->stream));
-  GG_TRY(rk.dInd.alloc(std::max<int64_t>(N, 1)));
+  const std::vector<RkTile> &tiles = C.tiles;
   GG_TRY(rk.dVal.alloc(std::max<int64_t>(N, 1)));
-  if (N > 0)
-    GG_CUDA(cudaMemcpyAsync(rk.dInd.p, rk.hInd.data(), N * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-  GG_TRY(dY.alloc((size_t)std::max(nf, 1) * np));
-  if (nf > 0) GG_TRY(build_y(ctx, dYd.p, nf, dY.p, scratch));
-  const int npairs = (int)pairs.size();
-  GG_TRY(dA.alloc((size_t)npairs * KC));
-  {
+  GG_TRY(C.dY.alloc((size_t)std::max(nf, 1) * np));
+  if (nf > 0) GG_TRY(build_y(ctx, C.dYd.p, nf, C.dY.p, C.scratch));
+  GG_TRY(C.dA.alloc((size_t)std::max(npairs, 1) * KC));
+  if (npairs > 0) {
     dim3 gr((KC + 127) / 128, npairs);
-    k_apairs<<<gr, 128, 0, ctx->stream>>>(dPairs.p, npairs, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dRPOR.p, KC, g.q, dA.p); ::gg::note_launch();
+    k_apairs<<<gr, 128, 0, ctx->stream>>>(C.dPairs.p, npairs, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dRPOR.p, KC, g.q,
+                                          C.dA.p);
+    ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
-  GG_TRY(dFb.alloc(std::max<int64_t>(N, 1)));
-  GG_TRY(dNfb.alloc(3));  // [0] fallback count, [1] position error flag, [2] tensor-core wait timed out
-  GG_CUDA(cudaMemsetAsync(dNfb.p, 0, 3 * sizeof(int), ctx->stream));
-  DBuf<signed char> dAs, dYs;
-  DBuf<int> dEA, dEY;
+  GG_TRY(C.dFb.alloc(std::max<int64_t>(N, 1)));
+  GG_TRY(C.dNfb.alloc(3));  // [0] fallback count, [1] position error flag, [2] tensor-core wait timed out
+  GG_CUDA(cudaMemsetAsync(C.dNfb.p, 0, 3 * sizeof(int), ctx->stream));
   if (!tiles.empty() && precision == GG_SPLIT) {
-    // tensor-core contraction on int8 slices of A and Y (k_oz_split, k_rk_ozaki)
+    // tensor-core contraction on Ozaki slices of A and Y
     const int KP = (KC + 31) / 32 * 32;
-    GG_TRY(dAs.alloc((size_t)OZ_S * (npairs + 1) * KP));
-    GG_TRY(dYs.alloc((size_t)OZ_S * (nf + 1) * KP));
-    GG_TRY(dEA.alloc(npairs + 1));
-    GG_TRY(dEY.alloc(nf + 1));
-    k_oz_split<<<npairs + 1, 128, 0, ctx->stream>>>(dA.p, npairs, KC, KC, KP, dAs.p, dEA.p); ::gg::note_launch();
-    k_oz_split<<<nf + 1, 128, 0, ctx->stream>>>(dY.p, nf, np, KC, KP, dYs.p, dEY.p); ::gg::note_launch();
+    GG_TRY(C.dEA.alloc(npairs + 1));
+    GG_TRY(C.dEY.alloc(nf + 1));
     static const bool mma_sync = [] {
       const char *e = getenv("GRASP_GPU_RK_TENSOR");
       return e && std::strcmp(e, "mma_sync") == 0;
     }();
-    if (mma_sync) {  // the legacy int8 mma.sync form, kept for comparison
+    if (mma_sync) {  // the legacy int8 mma.sync form (k_oz_split, k_rk_ozaki), kept for comparison
+      GG_TRY(C.dAs.alloc((size_t)OZ_S * (npairs + 1) * KP));
+      GG_TRY(C.dYs.alloc((size_t)OZ_S * (nf + 1) * KP));
+      k_oz_split<<<npairs + 1, 128, 0, ctx->stream>>>(C.dA.p, npairs, KC, KC, KP, C.dAs.p, C.dEA.p);
+      ::gg::note_launch();
+      k_oz_split<<<nf + 1, 128, 0, ctx->stream>>>(C.dY.p, nf, np, KC, KP, C.dYs.p, C.dEY.p);
+      ::gg::note_launch();
       k_rk_ozaki<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(
-          dTiles.p, dRowpair.p, dPairs.p, dAs.p, dEA.p, npairs, dYs.p, dEY.p, nf, KP, dY.p, dYd.p, np, o.dPF.p,
-          o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p);
+          C.dTiles.p, C.dRowpair.p, C.dPairs.p, C.dAs.p, C.dEA.p, npairs, C.dYs.p, C.dEY.p, nf, KP, C.dY.p, C.dYd.p,
+          np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, (long long)N, C.dFb.p,
+          C.dNfb.p);
       ::gg::note_launch();
     } else {
-      // tcgen05: raw GEMM parts at their positions, then the head terms
-      std::vector<int> fidx((size_t)(kloop + 1) * KEY * KEY, -1);
-      for (int f = 0; f < nf; ++f) fidx[((size_t)yd[f].k * KEY + yd[f].b) * KEY + yd[f].d] = f;
-      DBuf<RkTile> dTc;
-      DBuf<int> dFidx;
-      DBuf<int32_t> dKst;
-      GG_TRY(upload(dTc, tiles_tc, ctx->stream));
-      GG_TRY(upload(dFidx, fidx, ctx->stream));
-      GG_TRY(upload(dKst, rk.kstart, ctx->stream));
+      // tcgen05: the slices written into the tile blocks, the raw GEMM parts
+      // at their positions, then the head terms
+      const int nch = KP / TC_KC;
+      GG_TRY(C.dYt.alloc(std::max<size_t>(1, C.yslot.size() / TC_M * nch * TC_YBLK)));
+      GG_TRY(C.dAt.alloc(std::max<size_t>(1, C.aslot.size() / TC_N * nch * TC_ABLK)));
+      if (!C.yslot.empty()) {
+        k_oz_tile<TC_M><<<(unsigned)C.yslot.size(), 128, 0, ctx->stream>>>(C.dY.p, np, KC, nch, C.dYslot.p, C.dEY.p,
+                                                                          C.dYt.p);
+        ::gg::note_launch();
+      }
+      if (!C.aslot.empty()) {
+        k_oz_tile<TC_N><<<(unsigned)C.aslot.size(), 128, 0, ctx->stream>>>(C.dA.p, KC, KC, nch, C.dAslot.p, C.dEA.p,
+                                                                          C.dAt.p);
+        ::gg::note_launch();
+      }
       static bool attr = false;
       if (!attr) {
         GG_CUDA(cudaFuncSetAttribute(k_rk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
         attr = true;
       }
-      k_rk_tc<<<(unsigned)tiles_tc.size(), 128, TC_SMEM, ctx->stream>>>(dTc.p, dRowpair.p, dAs.p, dEA.p, npairs,
-                                                                          dYs.p, dEY.p, nf, KP, dYd.p, rk.dVal.p,
-                                                                          (long long)N, dNfb.p + 1);
-      ::gg::note_launch();
+      if (!C.tct.empty()) {
+        k_rk_tc<<<(unsigned)C.tct.size(), TC_THREADS, TC_SMEM, ctx->stream>>>(
+            C.dTct.p, C.dTcr.p, C.dYt.p, C.dAt.p, nch, C.dEA.p, C.dEY.p, C.dYd.p, rk.dVal.p, (long long)N,
+            C.dNfb.p + 1);
+        ::gg::note_launch();
+      }
       GG_CUDA(cudaGetLastError());
       const unsigned fb_blocks = (unsigned)std::min<long long>((N + 255) / 256, 8LL * ctx->sms);
       k_rk_finish_all<<<std::max(1u, fb_blocks), 256, 0, ctx->stream>>>(
-          rk.dInd.p, (long long)N, dKst.p, kloop, KEY, dFidx.p, dYd.p, dY.p, np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p,
-          g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, dFb.p, dNfb.p);
+          rk.dInd.p, (long long)N, C.dKst.p, kloop, KEY, C.dFidx.p, C.dYd.p, C.dY.p, np, o.dPF.p, o.dQF.p, o.ld,
+          o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, C.dFb.p, C.dNfb.p);
       ::gg::note_launch();
-      GG_CUDA(cudaGetLastError());
-      GG_CUDA(cudaStreamSynchronize(ctx->stream));  // the tile and index uploads are freed on return
     }
     GG_CUDA(cudaGetLastError());
   } else if (!tiles.empty()) {
-    k_rk_gemm<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(dTiles.p, dRowpair.p, dPairs.p, dA.p, dY.p, dYd.p, KC,
-                                                              np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p,
-                                                              g.dRPOR.p, g.q, rk.dVal.p, (long long)N, dFb.p, dNfb.p); ::gg::note_launch();
+    k_rk_gemm<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(C.dTiles.p, C.dRowpair.p, C.dPairs.p, C.dA.p, C.dY.p,
+                                                              C.dYd.p, KC, np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p,
+                                                              g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p,
+                                                              (long long)N, C.dFb.p, C.dNfb.p);
+    ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   int hfb[3] = {0, 0, 0};
-  GG_CUDA(cudaMemcpyAsync(hfb, dNfb.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaMemcpyAsync(hfb, C.dNfb.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (hfb[1]) return fail(GG_ERR_STATE, "genintrk: contraction produced a table position out of range");
   if (hfb[2]) return fail(GG_ERR_STATE, "genintrk: tensor-core contraction timed out waiting for its MMAs");
@@ -1170,8 +1364,9 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   if (nfb > 0) {
     const int wpb = 8;
     const int blocks = std::min((nfb + wpb - 1) / wpb, 8 * ctx->sms);
-    k_quad_table<<<blocks, 32 * wpb, 0, ctx->stream>>>(dFb.p, dNfb.p, nfb, dY.p, np, o.dPF.p, o.dQF.p, o.ld, g.dR.p,
-                                                          g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p); ::gg::note_launch();
+    k_quad_table<<<blocks, 32 * wpb, 0, ctx->stream>>>(C.dFb.p, C.dNfb.p, nfb, C.dY.p, np, o.dPF.p, o.dQF.p, o.ld,
+                                                       g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p);
+    ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   double ms = 0;

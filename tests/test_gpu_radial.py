@@ -122,3 +122,27 @@ def test_slater_rkintc_rinti(gpu_ready, oracle_mod):
         ctx.rinti(1, 3)  # 1s / 2p-: different kappa (rinti.f90:48-51 STOPs)
     with pytest.raises(GGError):
         ctx.rkintc(1, 1, 1, 3, 0)  # not in the table (rkintc.f90 STOPs)
+
+
+def test_genintrk_structure_reused_and_rebuilt(gpu_ready, oracle_mod):
+    """gg_genintrk keeps its index structure between calls: the same orbital
+    set with other radial functions reuses it, another set rebuilds it. Every
+    table, FP64 and tensor-core, matches the oracle."""
+    from grasp_gb300 import Context
+    cases = [hydrogenic_case(nmax=4, lmax=3, z=10.0),
+             hydrogenic_case(nmax=4, lmax=3, z=26.0, sigma="random", seed=3),  # same set, other functions
+             hydrogenic_case(nmax=3, lmax=2, z=10.0),                          # another set
+             hydrogenic_case(nmax=4, lmax=3, z=10.0)]
+    ctx = Context(0)
+    for case in cases:
+        ob = case["orb"]
+        ctx.set_grid(case["n"], case["rnt"], case["h"], case["c"], case["zz"])
+        ctx.set_orbitals(ob.nak, ob.mf, ob.pf, ob.qf)
+        ind0, val0, ks0, _ = oracle_for(case).genintrk(nthreads=8)
+        for precision in (0, 1):
+            ctx.genintrk(precision=precision)
+            ind, val, ks = ctx.rk_table()
+            np.testing.assert_array_equal(ind, ind0)
+            np.testing.assert_array_equal(ks, ks0)
+            rel = np.abs(val - val0) / np.maximum(np.abs(val0), RK_ATOL / RK_RTOL)
+            assert rel.max() <= RK_RTOL, (precision, float(rel.max()))
