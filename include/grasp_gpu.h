@@ -80,10 +80,12 @@ int gg_set_orbitals(gg_ctx *ctx, int nw, int ld, const int *nak, const int *mf, 
  * a<=b, a<=c, b<=d and TRIANGRK(l_a,k,l_c) & TRIANGRK(l_b,k,l_d), for
  * k = 0..J2MAX (kmax < 0) or k = 0..kmax. The table stays on the device.
  * precision: GG_FP64: FP64 contraction on the CUDA cores; GG_SPLIT: the
- * contraction on the int8 tensor cores, A and Y each split into 10 signed
- * 7-bit slices under a per-row power-of-two scale (Ozaki scheme), the exact
- * int32 slice products summed in FP64 (relative error ~1e-13 of the row
- * scales' product); the QUAD head term and end correction stay FP64.     */
+ * contraction on the tensor cores (tcgen05.mma kind::f16), A and Y each
+ * split into 10 balanced 7-bit digits under a per-row power-of-two scale
+ * (Ozaki scheme), exact products and exact FP32 group sums in tensor memory,
+ * folded in double-float (relative error ~1e-13 of the row scales'
+ * product); the QUAD head term and end correction stay FP64. The index
+ * structure is kept between calls with the same orbital l, j and kmax.     */
 int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max_out);
 /* Copies INDTEIRK (int32, packed ((a*KEY+b)*KEY+c)*KEY+d, KEY = NW+1),
  * VALTEIRK (double) and KSTART(0:kloop+1) (1-based positions). Any pointer
