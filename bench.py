@@ -189,11 +189,18 @@ def batched_leg(local, steps, cpu=True):
 
     from grasp_gb300 import FP64, SPLIT, Context, maneig_batched, workloads
     w = workloads.batch()
+    workloads.assemble_batch(workloads.batch(zs=w.zs[:1]), Context(local), precision=SPLIT)  # warm (loads, builds)
     ctx = Context(local)
+    # end to end from host arrays: every ion's tables, the blocks (views for
+    # ions after the first), and the first batched solve, which also builds
+    # the shared symmetric matvec structures
     t0 = time.perf_counter()
-    hs = workloads.assemble_batch(w, ctx)
+    hs = workloads.assemble_batch(w, ctx, precision=SPLIT)
     ctx.synchronize()
     t_asm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    maneig_batched(ctx, hs, w.nroots, precision=SPLIT)
+    t_first = time.perf_counter() - t0
     out = dict(w.describe())
     res = {}
     for prec, name in ((SPLIT, "split"), (FP64, "fp64")):
@@ -213,7 +220,8 @@ def batched_leg(local, steps, cpu=True):
     out["max_abs_dE_split_vs_fp64_Eh"] = float(max(np.abs(a[0] - b[0]).max()
                                                    for a, b in zip(res["split"], res["fp64"])))
     out["assemble_s"] = t_asm
-    out["ci_solve_e2e_s"] = t_asm + out["split_solve_s"]
+    out["first_solve_s"] = t_first
+    out["ci_solve_e2e_s"] = t_asm + t_first
     if cpu:
         import oracle
         oracle.build()

@@ -60,6 +60,7 @@ GPU_SYMBOLS = {
     "gg_iabint_table": (C.c_int, [C.c_void_p, _d]),
     "gg_hmat_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, _i64, _i32, C.POINTER(C.c_void_p)]),
     "gg_hmat_destroy": (C.c_int, [C.c_void_p]),
+    "gg_hmat_create_view": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p)]),
     "gg_setham_upload": (C.c_int, [C.c_void_p, C.c_void_p, _u8, C.POINTER(GGList), C.c_int, C.POINTER(GGList)]),
     "gg_setham_assemble": (C.c_int, [C.c_void_p, C.c_void_p, _d]),
     "gg_setham": (C.c_int, [C.c_void_p, C.c_void_p, _u8, C.POINTER(GGList), C.c_int, C.POINTER(GGList), _d]),

@@ -150,6 +150,21 @@ class HMatrix:
         ctx._children.append(self._box)
         self.eav = None
 
+    @classmethod
+    def view(cls, src, ctx=None):
+        """A matrix sharing src's structure, lists and assembly plan, with its
+        own EMT (gg_hmat_create_view): the same block for another ion."""
+        ctx = src.ctx if ctx is None else ctx
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.ncf, self.nnz, self.iendc, self.irow = src.ncf, src.nnz, src.iendc, src.irow
+        self._box = [C.c_void_p()]
+        check(_lib.gpu().gg_hmat_create_view(ctx._h, src._h, C.byref(self._box[0])))
+        ctx._children.append(self._box)
+        self._source = src
+        self.eav = None
+        return self
+
     @property
     def _h(self):
         return self._box[0]

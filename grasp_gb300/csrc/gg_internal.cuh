@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -38,14 +39,23 @@ constexpr int GPAD = 16;     // padding slots after NNN1 in device grid arrays
 template <class T> struct DBuf {
   T *p = nullptr;
   size_t n = 0;
+  bool own = true;  // false: borrowed from another buffer, never freed here
   DBuf() = default;
   DBuf(const DBuf &) = delete;
   DBuf &operator=(const DBuf &) = delete;
   ~DBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p && own) cudaFree(p);
     p = nullptr;
     n = 0;
+    own = true;
+  }
+  // refer to o's memory without owning it (o must outlive this buffer)
+  void borrow(const DBuf &o) {
+    release();
+    p = o.p;
+    n = o.n;
+    own = false;
   }
   int alloc(size_t count) {
     if (count <= n && p) return GG_OK;
@@ -112,6 +122,17 @@ struct Lists {  // device copies of one block's T/V lists, concatenated in SETHA
   DBuf<double> dCoeff;                  // [ncontr]
   DBuf<uint8_t> dIq;                    // [ncf][nw]
   bool valid = false;
+  // assembly plan (setham.cu): the contributions sorted by LOC with their
+  // integral slots, and the diagonal terms; it depends only on these lists
+  // and on the R^k table's index structure, whose key it records
+  std::vector<int> plan_key;
+  int64_t plan_nrk = -1;
+  DBuf<int64_t> pOff;                   // [nnz + 1] contribution offsets per EMT position
+  DBuf<int32_t> pSlot;                  // [ncontr] integral slot, sorted order
+  DBuf<double> pCoeff;                  // [ncontr] coefficient, sorted order
+  DBuf<unsigned char> pTerms;           // diagonal terms (setham.cu's DiagTerm records)
+  int nterms = 0;
+  DBuf<double> integ;                   // [VALTEIRK | I(ab)] of the last assembly
 };
 
 constexpr int LT_TW = 1024;  // tile width of the tiled lower-triangle matvec
@@ -154,9 +175,13 @@ struct gg_hmat {
   gg::DBuf<int32_t> dIrow;              // [nnz]
   gg::DBuf<double> dEmt;                // [nnz]
   gg::DBuf<double> dDiag;               // [ncf]
+  gg::DBuf<double> dEav;                // EAV of the last assembly
   bool emt_valid = false;
   double eav = 0.0;
-  gg::Lists lists;
+  std::shared_ptr<gg::Lists> lists = std::make_shared<gg::Lists>();  // shared with views
+  gg_hmat *base = nullptr;              // a view's source (views borrow its structure)
+  int views = 0;                        // views of this matrix still alive
+  bool dead = false;                    // destroyed while views were alive
   // full symmetric CSR used by the matvec (both triangles, diagonal first)
   bool sym_valid = false;
   int64_t sym_nnz = 0;
@@ -175,6 +200,8 @@ struct gg_hmat {
 namespace gg {
 // radial.cu
 int ensure_grid(gg_ctx *ctx);
+// key of the R^k table's index structure (null before the first table)
+const std::vector<int> *rk_structure_key(const gg_ctx *ctx);
 int ensure_orbitals(gg_ctx *ctx);
 // timing helpers (ctx.cu)
 int timer_start(gg_ctx *ctx);

@@ -567,6 +567,10 @@ struct RkCache {
 
 void rk_cache_free(RkCache *c) { delete c; }
 
+const std::vector<int> *rk_structure_key(const gg_ctx *ctx) {
+  return (ctx->rk.cache && ctx->rk.valid) ? &ctx->rk.cache->key : nullptr;
+}
+
 namespace {
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }

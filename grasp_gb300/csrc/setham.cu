@@ -388,7 +388,53 @@ int gg_hmat_destroy(gg_hmat *h) {
   if (!h) return GG_OK;
   cudaSetDevice(h->ctx->device);
   cudaStreamSynchronize(h->ctx->stream);
+  if (gg_hmat *root = h->base) {  // a view: its borrowed buffers are not freed with it
+    delete h;
+    if (--root->views == 0 && root->dead) delete root;
+    return GG_OK;
+  }
+  if (h->views > 0) {  // freed with its last view
+    h->dead = true;
+    return GG_OK;
+  }
   delete h;
+  return GG_OK;
+}
+
+int gg_hmat_create_view(gg_ctx *ctx, gg_hmat *src, gg_hmat **out) {
+  if (!ctx || !src || !out) return fail(GG_ERR_ARG, "gg_hmat_create_view: bad arguments");
+  *out = nullptr;
+  gg_hmat *root = src->base ? src->base : src;
+  if (root->dead) return fail(GG_ERR_STATE, "gg_hmat_create_view: the source was destroyed");
+  if (ctx->device != root->ctx->device) return fail(GG_ERR_ARG, "gg_hmat_create_view: source on another device");
+  // the source's symmetric structure is built once and shared
+  GG_TRY(build_sym(root));
+  GG_CUDA(cudaStreamSynchronize(root->ctx->stream));
+  GG_CUDA(cudaSetDevice(ctx->device));
+  gg_hmat *h = new gg_hmat;
+  h->ctx = ctx;
+  h->ncf = root->ncf;
+  h->nnz = root->nnz;
+  h->hIendc = root->hIendc;
+  h->dIendc.borrow(root->dIendc);
+  h->dIrow.borrow(root->dIrow);
+  h->lists = root->lists;
+  h->sym_valid = root->sym_valid;
+  h->sym_nnz = root->sym_nnz;
+  h->sym_col16 = root->sym_col16;
+  h->dSymPtr.borrow(root->dSymPtr);
+  h->dSymCol.borrow(root->dSymCol);
+  h->dSymCol16.borrow(root->dSymCol16);
+  h->dSymSrc.borrow(root->dSymSrc);
+  int s = h->dEmt.alloc(h->nnz);
+  if (s == GG_OK) s = h->dDiag.alloc(h->ncf);
+  if (s != GG_OK) {
+    delete h;
+    return s;
+  }
+  h->base = root;
+  ++root->views;
+  *out = h;
   return GG_OK;
 }
 
@@ -399,7 +445,9 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
   GG_TRY(ensure_orbitals(ctx));
   GG_CUDA(cudaSetDevice(ctx->device));
   GG_TRY(timer_start(ctx));
-  Lists &L = h->lists;
+  if (h->base) return fail(GG_ERR_STATE, "gg_setham_upload: a view shares its source's lists (upload to the source)");
+  Lists &L = *h->lists;
+  L.plan_key.clear();  // new lists: the assembly plan is rebuilt
   const int nlists = kmaxf + 2;
   std::vector<const gg_list *> ls;
   ls.push_back(tlist);
@@ -458,27 +506,19 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
   return GG_OK;
 }
 
-int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
-  if (!ctx || !h || h->ctx != ctx) return fail(GG_ERR_ARG, "gg_setham_assemble: bad arguments");
-  Lists &L = h->lists;
-  if (!L.valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no lists (call gg_setham_upload)");
-  if (!ctx->rk.valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no R^k table (call gg_genintrk)");
-  if (!ctx->iab_valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no I(ab) table (call gg_iabint_table)");
-  if (L.kmaxf > ctx->rk.kloop) return fail(GG_ERR_STATE, "gg_setham_assemble: R^k table does not reach KMAXF");
-  GG_CUDA(cudaSetDevice(ctx->device));
+// The assembly plan of lists L for the current R^k table: integral slots of
+// every label (k_label_slots), a counting transpose of the contributions by
+// LOC (k_count_loc, scans, k_scatter_perm) and a per-segment sort back into
+// list order (k_sort_gather), plus the diagonal term list in the loop order
+// of setham.f90:83-219. Kept in L until the lists or the table's index
+// structure change.
+static int build_plan(gg_ctx *ctx, gg_hmat *h, Lists &L) {
   cudaStream_t s = ctx->stream;
   const Orbitals &o = ctx->orb;
   const RkTable &rk = ctx->rk;
-  const int nw = o.nw, ncf = h->ncf;
+  const int nw = o.nw;
   const int64_t nnz = h->nnz, ncontr = L.ncontr;
-  GG_TRY(timer_start(ctx));
-  // combined integral array [VALTEIRK | I(ab)]
-  DBuf<double> integ;
   const long long nrk = rk.n;
-  GG_TRY(integ.alloc((size_t)nrk + (size_t)nw * nw));
-  if (nrk) GG_CUDA(cudaMemcpyAsync(integ.p, rk.dVal.p, nrk * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  GG_CUDA(cudaMemcpyAsync(integ.p + nrk, ctx->dIab.p, (size_t)nw * nw * sizeof(double), cudaMemcpyDeviceToDevice, s));
-  // diagonal term list in the loop order of setham.f90:83-219
   std::vector<DiagTerm> terms;
   auto iab_slot = [&](int a) { return (long long)nrk + (long long)(a - 1) * nw + (a - 1); };
   auto add = [&](int type, int a, int b, int k, double fac) -> int {
@@ -533,19 +573,20 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
         }
     } while (K < km);
   }
-  DBuf<DiagTerm> dTerms;
-  GG_TRY(upload(dTerms, terms.data(), terms.size(), s));
-  DBuf<int32_t> cslot, perm, slot_s;
+  GG_TRY(L.pTerms.alloc(std::max<size_t>(1, terms.size() * sizeof(DiagTerm))));
+  if (!terms.empty())
+    GG_CUDA(cudaMemcpyAsync(L.pTerms.p, terms.data(), terms.size() * sizeof(DiagTerm), cudaMemcpyHostToDevice, s));
+  L.nterms = (int)terms.size();
+  DBuf<int32_t> cslot, perm;
   DBuf<int> cnt, fill, err;
-  DBuf<int64_t> off, part;
-  DBuf<double> coeff_s;
+  DBuf<int64_t> part;
   GG_TRY(cslot.alloc(ncontr));
   GG_TRY(perm.alloc(ncontr));
-  GG_TRY(slot_s.alloc(ncontr));
-  GG_TRY(coeff_s.alloc(ncontr));
+  GG_TRY(L.pSlot.alloc(ncontr));
+  GG_TRY(L.pCoeff.alloc(ncontr));
   GG_TRY(cnt.alloc(nnz));
   GG_TRY(fill.alloc(nnz));
-  GG_TRY(off.alloc(nnz + 1));
+  GG_TRY(L.pOff.alloc(nnz + 1));
   GG_TRY(err.alloc(1));
   GG_CUDA(cudaMemsetAsync(err.p, 0, sizeof(int), s));
   GG_CUDA(cudaMemsetAsync(cnt.p, 0, nnz * sizeof(int), s));
@@ -561,7 +602,7 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
                                          dKstart.p, rk.kloop, nrk, cslot.p, err.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
-  const int gblocks = 152 * 8;
+  const int gblocks = ctx->sms * 8;
   if (ncontr) {
     k_count_loc<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, nnz, cnt.p, err.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
@@ -577,27 +618,59 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
     GG_TRY(part.alloc(nparts + 1));
     k_scan_blocks<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk); ::gg::note_launch();
     k_scan_parts<<<1, 32, 0, s>>>(part.p, nparts); ::gg::note_launch();
-    k_scan_final<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk, off.p); ::gg::note_launch();
+    k_scan_final<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk, L.pOff.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
   if (ncontr) {
-    k_scatter_perm<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, off.p, fill.p, perm.p); ::gg::note_launch();
-    k_sort_gather<<<gblocks, 256, 0, s>>>(off.p, nnz, perm.p, L.dCoeff.p, cslot.p, coeff_s.p, slot_s.p); ::gg::note_launch();
+    k_scatter_perm<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, L.pOff.p, fill.p, perm.p); ::gg::note_launch();
+    k_sort_gather<<<gblocks, 256, 0, s>>>(L.pOff.p, nnz, perm.p, L.dCoeff.p, cslot.p, L.pCoeff.p, L.pSlot.p);
+    ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
+  GG_CUDA(cudaStreamSynchronize(s));  // the temporaries are freed on return
+  L.plan_key = *rk_structure_key(ctx);
+  L.plan_nrk = nrk;
+  return GG_OK;
+}
+
+int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
+  if (!ctx || !h || h->ctx != ctx) return fail(GG_ERR_ARG, "gg_setham_assemble: bad arguments");
+  Lists &L = *h->lists;
+  if (!L.valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no lists (call gg_setham_upload)");
+  if (!ctx->rk.valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no R^k table (call gg_genintrk)");
+  if (!ctx->iab_valid) return fail(GG_ERR_STATE, "gg_setham_assemble: no I(ab) table (call gg_iabint_table)");
+  if (L.kmaxf > ctx->rk.kloop) return fail(GG_ERR_STATE, "gg_setham_assemble: R^k table does not reach KMAXF");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t s = ctx->stream;
+  const Orbitals &o = ctx->orb;
+  const RkTable &rk = ctx->rk;
+  const int nw = o.nw, ncf = h->ncf;
+  const int64_t nnz = h->nnz;
+  GG_TRY(timer_start(ctx));
+  const std::vector<int> *key = rk_structure_key(ctx);
+  if (!key || L.plan_key != *key || L.plan_nrk != rk.n) {
+    L.plan_key.clear();
+    GG_TRY(build_plan(ctx, h, L));
+  }
+  // combined integral array [VALTEIRK | I(ab)]
+  const long long nrk = rk.n;
+  GG_TRY(L.integ.alloc((size_t)nrk + (size_t)nw * nw));
+  if (nrk) GG_CUDA(cudaMemcpyAsync(L.integ.p, rk.dVal.p, nrk * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  GG_CUDA(cudaMemcpyAsync(L.integ.p + nrk, ctx->dIab.p, (size_t)nw * nw * sizeof(double), cudaMemcpyDeviceToDevice,
+                          s));
   // EMT = 0 ; diagonal pieces ; list contributions ; EAV shift
+  const int gblocks = ctx->sms * 8;
   GG_CUDA(cudaMemsetAsync(h->dEmt.p, 0, nnz * sizeof(double), s));
-  k_diag_terms<<<(ncf + 127) / 128, 128, 0, s>>>(dTerms.p, (int)terms.size(), L.dIq.p, nw, ncf, h->dIendc.p, integ.p,
-                                                 h->dEmt.p); ::gg::note_launch();
+  k_diag_terms<<<(ncf + 127) / 128, 128, 0, s>>>(reinterpret_cast<const DiagTerm *>(L.pTerms.p), L.nterms, L.dIq.p,
+                                                 nw, ncf, h->dIendc.p, L.integ.p, h->dEmt.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
-  k_assemble<<<gblocks, 256, 0, s>>>(off.p, nnz, coeff_s.p, slot_s.p, integ.p, h->dEmt.p); ::gg::note_launch();
+  k_assemble<<<gblocks, 256, 0, s>>>(L.pOff.p, nnz, L.pCoeff.p, L.pSlot.p, L.integ.p, h->dEmt.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
-  DBuf<double> deav;
-  GG_TRY(deav.alloc(1));
-  k_eav<<<1, 1024, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dDiag.p, deav.p); ::gg::note_launch();
+  GG_TRY(h->dEav.alloc(1));
+  k_eav<<<1, 1024, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dDiag.p, h->dEav.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   double eav = 0;
-  GG_CUDA(cudaMemcpyAsync(&eav, deav.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync(&eav, h->dEav.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   double ms = 0;
   GG_TRY(timer_stop(ctx, &ms));
   ctx->stats[2] = ms;

@@ -137,20 +137,28 @@ def batch(zs=tuple(range(10, 41)), two_js=(0, 2, 4, 6, 8), parities=(0, 1), max_
     return BatchWorkload(f"ne_like_{len(zs)}ions_{len(zs) * len(blocks)}blocks", list(zs), orbs, blocks, nroots)
 
 
-def assemble_batch(w, ctx):
+def assemble_batch(w, ctx, precision=0):
     """All blocks of all ions on one context: per ion the grid, orbitals,
-    R^k and I(ab) tables, then SETHAM of each block. Returns the HMatrix
-    objects in (ion, block) order."""
+    R^k (GG_FP64 or the tensor cores) and I(ab) tables, then SETHAM of each
+    block. The first ion uploads each block's structure and T/V lists; the
+    other ions' blocks are views of them (gg_hmat_create_view), which share
+    the lists and the assembly plan. Returns the HMatrix objects in
+    (ion, block) order."""
     from . import HMatrix
-    hs = []
-    for z in w.zs:
+    hs, first = [], []
+    for iz, z in enumerate(w.zs):
         n, rnt, ob = w.ion(z)
         ctx.set_grid(n, rnt, 0.05, S.CVAC, np.full(n, float(z)))
         ctx.set_orbitals(ob.nak, ob.mf, ob.pf, ob.qf)
-        ctx.genintrk()
+        ctx.genintrk(precision=precision)
         ctx.iabint_table()
-        for _, _, b in w.blocks:
-            H = HMatrix(ctx, b.ncf, b.iendc, b.irow)
-            H.setham(b.iq, b.tlist, b.vlists)
+        for j, (_, _, b) in enumerate(w.blocks):
+            if iz == 0:
+                H = HMatrix(ctx, b.ncf, b.iendc, b.irow)
+                H.setham(b.iq, b.tlist, b.vlists)
+                first.append(H)
+            else:
+                H = HMatrix.view(first[j], ctx)
+                H.setham_assemble()
             hs.append(H)
     return hs

@@ -123,6 +123,14 @@ int gg_iabint_table(gg_ctx *ctx, double *iab);
 int gg_hmat_create(gg_ctx *ctx, int ncf, int64_t nnz, const int64_t *iendc, const int32_t *irow,
                    gg_hmat **out);
 int gg_hmat_destroy(gg_hmat *h);
+/* A matrix with src's structure (IENDC/IROW, the symmetric matvec structure)
+ * and src's T/V lists and assembly plan, shared, but its own EMT: for the
+ * same J/parity block of another ion (other orbitals, same CSFs). Assemble it
+ * with gg_setham_assemble on ctx (any context of src's device) after that
+ * context's gg_genintrk and gg_iabint_table; gg_setham_upload on a view is an
+ * error. src may be destroyed before its views (its memory is released with
+ * the last view).                                                           */
+int gg_hmat_create_view(gg_ctx *ctx, gg_hmat *src, gg_hmat **out);
 
 /* One rangular coefficient list (mcp.31 or mcp.32+k, one block), as
  * SORTMEM writes it (rangular90/sortmem.f90:232-284): nlab labels; label l

@@ -131,3 +131,26 @@ def test_batched_tiny_blocks_and_two_contexts(gpu_ready, oracle_mod):
         ev0, vec0, _ = oracle.maneig(0, b.ncf, r, b.iendc, b.irow, H.emt())
         assert np.abs(ev - ev0).max() <= EV_TOL, (b.ncf, ev, ev0)
         assert np.abs(vec - vec0).max() <= VEC_TOL, b.ncf
+
+
+def test_views_match_full_assembly_and_outlive_source(gpu_ready):
+    """A view (gg_hmat_create_view: another ion's copy of a block) assembles
+    the same EMT as a matrix built from its own upload; uploading into a view
+    is an error; the view keeps working after its source is destroyed."""
+    from grasp_gb300 import Context, GGError, HMatrix, workloads as W
+    w = W.batch(zs=(10, 17), two_js=(2,), parities=(1,))
+    b = w.blocks[0][2]
+    ctx = Context(0)
+    src, view = W.assemble_batch(w, ctx)  # ion 10 uploaded, ion 17 a view; ctx holds ion 17's tables
+    full = HMatrix(ctx, b.ncf, b.iendc, b.irow)
+    full.setham(b.iq, b.tlist, b.vlists)
+    np.testing.assert_array_equal(view.emt(), full.emt())
+    assert view.eav == full.eav
+    with pytest.raises(GGError):
+        view.setham(b.iq, b.tlist, b.vlists)
+    src.close()
+    view.setham_assemble()
+    np.testing.assert_array_equal(view.emt(), full.emt())
+    (ev, vec), = [r for r in __import__("grasp_gb300").maneig_batched(ctx, [view], 3)[0]]
+    ev0, _, _ = full.maneig(3)
+    assert np.abs(ev - ev0).max() <= EV_TOL
