@@ -390,6 +390,7 @@ def run_ours(a):
         times64.append(t)
         t, _, _, _ = solve_resident(ctx, H, w.nroots, SPLIT)
         times_ref.append(t)
+    loops_mblock1 = int(ctx.stage_stat(9))  # full-block DVDSON loops with rci's MBLOCK = 1
     t_fp64 = _max_over_ranks(pg, statistics.median(times64))
     t_ref_mblock = _max_over_ranks(pg, statistics.median(times_ref))
     dE = float(np.abs(ev - ev64).max())
@@ -422,7 +423,8 @@ def run_ours(a):
     rk = rk_leg(local) if not a.no_extra else None
     cpu = None
     if rank == 0 and not a.no_cpu_baseline:
-        est, desc, parts = cpu_sample(w, 1, a.cpu_loops, gpu_loops=int(stage["loops_full"]) + 1)
+        # the reference's DVDSON runs MBLOCK = 1: extrapolate to that loop count
+        est, desc, parts = cpu_sample(w, 1, a.cpu_loops, gpu_loops=loops_mblock1 + 1)
         cpu = {"value": est, "unit": "s", "cores": 1, "kind": "port", "sample": desc}
     if rank != 0:
         return 0
