@@ -366,6 +366,9 @@ constexpr int MT_SMEM = 4096;  // doubles of Ritz coefficients held in shared me
 // For targets t < nt: b_t = BASIS s_t -> T(:, 2t), r_t = AB s_t - lambda_t b_t
 // -> T(:, 2t + 1), rn2[t] = |r_t|^2 (block partials added in order by the
 // last block). s_t = S + t k.
+// Targets [g NT, g NT + NT) for g = blockIdx.y (nt in all); the last block
+// of the whole grid adds the partials of every target in block order.
+template <int NT>
 __global__ void __launch_bounds__(RT) k_ritz_multi(const double *__restrict__ B, const double *__restrict__ AB,
                                                    int64_t ld, int k, int nt, const double *__restrict__ S,
                                                    const double *__restrict__ lam, double *__restrict__ T, int n,
@@ -374,37 +377,40 @@ __global__ void __launch_bounds__(RT) k_ritz_multi(const double *__restrict__ B,
   __shared__ double sv[MT_SMEM];
   __shared__ double red[RT / 32];
   __shared__ bool last;
-  for (int q = threadIdx.x; q < nt * k; q += RT) sv[q] = S[q];
+  const int t0 = blockIdx.y * NT;
+  for (int q = threadIdx.x; q < NT * k; q += RT) sv[q] = S[(size_t)t0 * k + q];
   __syncthreads();
   const int i = blockIdx.x * RT + threadIdx.x;
-  double bacc[MT_MAX], aacc[MT_MAX];
+  double bacc[NT], aacc[NT];
 #pragma unroll
-  for (int t = 0; t < MT_MAX; ++t) bacc[t] = aacc[t] = 0.0;
+  for (int t = 0; t < NT; ++t) bacc[t] = aacc[t] = 0.0;
   if (i < n) {
     for (int j = 0; j < k; ++j) {
       const double bj = B[(size_t)j * ld + i], aj = AB[(size_t)j * ld + i];
 #pragma unroll
-      for (int t = 0; t < MT_MAX; ++t)
-        if (t < nt) {
-          bacc[t] = fma(bj, sv[t * k + j], bacc[t]);
-          aacc[t] = fma(aj, sv[t * k + j], aacc[t]);
-        }
+      for (int t = 0; t < NT; ++t) {
+        bacc[t] = fma(bj, sv[t * k + j], bacc[t]);
+        aacc[t] = fma(aj, sv[t * k + j], aacc[t]);
+      }
     }
   }
 #pragma unroll
-  for (int t = 0; t < MT_MAX; ++t) {
-    if (t >= nt) break;
+  for (int t = 0; t < NT; ++t) {
     double r = 0.0;
     if (i < n) {
-      r = fma(-lam[t], bacc[t], aacc[t]);
-      T[(size_t)(2 * t) * ld + i] = bacc[t];
-      T[(size_t)(2 * t + 1) * ld + i] = r;
+      r = fma(-lam[t0 + t], bacc[t], aacc[t]);
+      T[(size_t)(2 * (t0 + t)) * ld + i] = bacc[t];
+      T[(size_t)(2 * (t0 + t) + 1) * ld + i] = r;
     }
     const double sq = block_sum<RT>(r * r, red);
-    if (threadIdx.x == 0) part[(size_t)t * gridDim.x + blockIdx.x] = sq;
+    if (threadIdx.x == 0) part[(size_t)(t0 + t) * gridDim.x + blockIdx.x] = sq;
     __syncthreads();
   }
-  if (!arrive_last(counter, &last)) return;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1);
+  __syncthreads();
+  if (!last) return;
   for (int t = 0; t < nt; ++t) {
     double u = 0.0;
     for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + (size_t)t * gridDim.x + q);
@@ -799,6 +805,519 @@ __global__ void __launch_bounds__(PT, 2) k_pass(PassArgs A) {
   pass_colreduce(A.part2, G, k + 1, 1.0, false, A.out, red);
 }
 
+// ---------------------------------------------------------------------------
+// Block Gram-Schmidt for the block pass (MBLOCK > 1). The m new columns
+// kpass .. kpass+m-1 (kpass = pv[0].c on the device) are orthogonalised
+// against the basis by two passes of block classical Gram-Schmidt, then among
+// themselves by two rounds of Cholesky QR. A column whose Cholesky pivot is
+// not above 1e-14 of its own squared norm (or is zero) is dropped and the
+// kept columns are compacted: the pass adds nk <= m columns (bst[0]). The
+// span is the one of DVDSON's MGS_NRM (dvdson.f90:1417-1508), which
+// normalises such a column instead. Then OP per kept column and the new
+// columns of S (packed upper) from one block of dot products. The dot
+// products are per-CTA partials over row ranges, added in CTA order.
+//   MODE 0  X = B(:, 0:kpass),      W = B(:, kpass:kpass+m)
+//   MODE 1  X = W = B(:, kpass:kpass+c), c = bst[0]
+//   MODE 2  X = B(:, 0:kpass+c),    W = AB(:, kpass:kpass+c)
+// ---------------------------------------------------------------------------
+constexpr int BD_R = 64, BD_T = 256, BD_AC = 32, BD_RED = 1024;
+constexpr int BD_PAIRS = (BD_AC * MT_MAX + BD_T - 1) / BD_T;
+
+template <int MODE>
+__global__ void __launch_bounds__(BD_T) k_bd_dots(const double *__restrict__ B, const double *__restrict__ AB,
+                                                  int64_t ld, const IterParams *__restrict__ pv, int m,
+                                                  const int *__restrict__ bst, int n, int cpc,
+                                                  double *__restrict__ part, int ps) {
+  __shared__ double Bs[BD_R * MT_MAX];       // [i][q]
+  __shared__ double As[BD_R * (BD_AC + 1)];  // [i][a]
+  const int kpass = pv[0].c;
+  const int nb = (MODE == 0) ? m : bst[0];
+  if (nb <= 0) return;
+  const int na = (MODE == 0) ? kpass : (MODE == 1 ? nb : kpass + nb);
+  const int a0 = (MODE == 1) ? kpass : 0;
+  const double *Wb = ((MODE == 2) ? AB : B) + (size_t)kpass * ld;
+  const double *Xb = B + (size_t)a0 * ld;
+  double *out = part + (size_t)blockIdx.x * ps;
+  const int rbeg = blockIdx.x * cpc * BD_R, rend = min(n, rbeg + cpc * BD_R);
+  for (int ac = blockIdx.y * BD_AC; ac < na; ac += gridDim.y * BD_AC) {
+    const int nac = min(BD_AC, na - ac), np = nac * nb;
+    double acc[BD_PAIRS];
+#pragma unroll
+    for (int k = 0; k < BD_PAIRS; ++k) acc[k] = 0.0;
+    for (int r0 = rbeg; r0 < rend; r0 += BD_R) {
+      const int nr = min(BD_R, rend - r0);
+      for (int idx = threadIdx.x; idx < nr * nb; idx += BD_T) {
+        const int i = idx % nr, q = idx / nr;
+        Bs[i * MT_MAX + q] = Wb[(size_t)q * ld + r0 + i];
+      }
+      for (int idx = threadIdx.x; idx < nr * nac; idx += BD_T) {
+        const int i = idx % nr, a = idx / nr;
+        As[i * (BD_AC + 1) + a] = Xb[(size_t)(ac + a) * ld + r0 + i];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < BD_PAIRS; ++k) {
+        const int pr = threadIdx.x + k * BD_T;
+        if (pr < np) {
+          const int a = pr % nac, q = pr / nac;
+          double s0 = 0.0, s1 = 0.0;
+          int i = 0;
+          for (; i + 1 < nr; i += 2) {
+            s0 = fma(As[i * (BD_AC + 1) + a], Bs[i * MT_MAX + q], s0);
+            s1 = fma(As[(i + 1) * (BD_AC + 1) + a], Bs[(i + 1) * MT_MAX + q], s1);
+          }
+          if (i < nr) s0 = fma(As[i * (BD_AC + 1) + a], Bs[i * MT_MAX + q], s0);
+          acc[k] += s0 + s1;
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < BD_PAIRS; ++k) {
+      const int pr = threadIdx.x + k * BD_T;
+      if (pr < np) out[(ac + pr % nac) * nb + pr / nac] = acc[k];
+    }
+  }
+}
+
+// sum over the CTA partials of k_bd_dots for outputs o0 .. o0+32: lane = output,
+// warps take CTAs w, w + nw, ...; the warp sums are then added in warp order
+__device__ __forceinline__ double bd_reduce(const double *__restrict__ part, int ps, int ntiles, int o, bool ok,
+                                           double *red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double u = 0.0;
+  if (ok)
+    for (int t = w; t < ntiles; t += nw) u += part[(size_t)t * ps + o];
+  red[w * 32 + lane] = u;
+  __syncthreads();
+  double sum = 0.0;
+  if (w == 0)
+    for (int v = 0; v < nw; ++v) sum += red[v * 32 + lane];
+  return sum;
+}
+
+// MODE 0: Gram-Schmidt coefficients C = X^T W (kpass x m, row a at a m);
+// MODE 2: the new columns of S into dS (packed upper, S(i, j) at j (j+1)/2 + i).
+// 32 outputs per CTA.
+template <int MODE>
+__global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict__ pv, int m,
+                                                    const int *__restrict__ bst, const double *__restrict__ part,
+                                                    int ps, int ntiles, double *__restrict__ C,
+                                                    double *__restrict__ dS) {
+  __shared__ double red[BD_T];
+  const int kpass = pv[0].c;
+  const int nb = (MODE == 0) ? m : bst[0];
+  const int na = (MODE == 0) ? kpass : kpass + nb;
+  const int o = blockIdx.x * 32 + (threadIdx.x & 31);
+  if (nb <= 0 || (int)blockIdx.x * 32 >= na * nb) return;
+  const bool ok = o < na * nb;
+  const double sum = bd_reduce(part, ps, ntiles, o, ok, red);
+  if (threadIdx.x >= 32 || !ok) return;
+  if (MODE == 0) {
+    C[o] = sum;
+  } else {
+    const int a = o / nb, j = kpass + o % nb;
+    if (a <= j) dS[(size_t)j * (j + 1) / 2 + a] = sum;
+  }
+}
+
+// Cholesky QR step: G = W^T W (reduced from the partials), G = R^T R with
+// drops; C[q MT_MAX + c] = the map from current column q to kept column c
+// (R^-1 on the kept rows), bst[1] = columns before, bst[0] = kept. The last
+// round also writes the matvec skip flags of the m columns. Right-looking
+// Cholesky on the Schur complement in shared memory (one column per step,
+// one thread per element), then one thread per column of R^-1. When G is
+// within 1e-8 of the identity (the second round, after a first one), R^-1 =
+// I - F to first order (F the upper triangle of G - I, diagonal halved):
+// its error is O(|G - I|^2) and it needs no serial chain of square roots and
+// divisions, which are slow in FP64.
+__global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst, const double *__restrict__ part,
+                                                    int ps, int ntiles, double *__restrict__ C,
+                                                    double *__restrict__ skipf, int last) {
+  __shared__ double red[BD_RED];
+  __shared__ double G[MT_MAX * MT_MAX];   // Schur complement [q][q']
+  __shared__ double R[MT_MAX * MT_MAX];   // row c of R over the current columns
+  __shared__ double Ri[MT_MAX * MT_MAX];  // R^-1 of the kept columns [i][c]
+  __shared__ double g0[MT_MAX], invd[MT_MAX];
+  __shared__ int keep[MT_MAX], pos[MT_MAX];
+  const int nb = bst[0];
+  const int tid = threadIdx.x;
+  // 8 groups of 32 outputs, 4 warps per group
+  const int grp = tid >> 7, sub = (tid >> 5) & 3, lane = tid & 31;
+  const int o = grp * 32 + lane;
+  const bool ok = nb > 0 && o < nb * nb;
+  double u = 0.0;
+  if (ok)
+    for (int t = sub; t < ntiles; t += 4) u += part[(size_t)t * ps + o];
+  red[tid] = u;
+  __syncthreads();
+  if (sub == 0 && ok) G[o] = ((red[tid] + red[tid + 32]) + red[tid + 64]) + red[tid + 96];
+  __syncthreads();
+  const bool near = __syncthreads_and(tid >= nb * nb || fabs(G[tid] - ((tid / nb == tid % nb) ? 1.0 : 0.0)) <= 1e-8);
+  if (near) {
+    if (tid < MT_MAX * MT_MAX) {
+      const int q = tid / MT_MAX, c = tid % MT_MAX;
+      double v = 0.0;
+      if (q < nb && c < nb) v = (q == c) ? 1.0 - 0.5 * (G[q * nb + q] - 1.0) : (q < c ? -G[q * nb + c] : 0.0);
+      C[tid] = v;
+    }
+    if (tid == 0) bst[1] = nb;  // bst[0] stays nb
+    if (last && tid < m) skipf[tid] = (tid < nb) ? 0.0 : 1.0;
+    return;
+  }
+  if (tid < nb) {
+    g0[tid] = G[tid * nb + tid];
+    pos[tid] = -1;
+  }
+  __syncthreads();
+  int nk = 0;  // uniform
+  for (int q = 0; q < nb; ++q) {
+    const double dq = G[q * nb + q];
+    if (dq > 1e-14 * g0[q] && dq > 1e-300) {
+      const double inv = rsqrt(dq), rd = dq * inv;
+      if (tid < nb) R[nk * MT_MAX + tid] = (tid < q) ? 0.0 : (tid == q ? rd : G[q * nb + tid] * inv);
+      __syncthreads();
+      if (tid < nb * nb) {
+        const int a = tid / nb, b = tid % nb;
+        if (a > q && b > q) G[tid] -= R[nk * MT_MAX + a] * R[nk * MT_MAX + b];
+      }
+      if (tid == 0) {
+        keep[nk] = q;
+        pos[q] = nk;
+        invd[nk] = inv;
+      }
+      ++nk;
+    }
+    __syncthreads();
+  }
+  // column c of R_kk^-1, R_kk(i, j) = R[i][keep[j]]
+  if (tid < nk) {
+    const int c = tid;
+    Ri[c * MT_MAX + c] = invd[c];
+    for (int i = c - 1; i >= 0; --i) {
+      double sum = 0.0;
+      for (int l = i + 1; l <= c; ++l) sum += R[i * MT_MAX + keep[l]] * Ri[l * MT_MAX + c];
+      Ri[i * MT_MAX + c] = -sum * invd[i];
+    }
+  }
+  __syncthreads();
+  if (tid < MT_MAX * MT_MAX) {
+    const int q = tid / MT_MAX, c = tid % MT_MAX;
+    const int i = (q < nb) ? pos[q] : -1;
+    C[tid] = (i >= 0 && c < nk && i <= c) ? Ri[i * MT_MAX + c] : 0.0;
+  }
+  if (tid == 0) {
+    bst[1] = nb;
+    bst[0] = nk;
+  }
+  if (last && tid < m) skipf[tid] = (tid < nk) ? 0.0 : 1.0;
+}
+
+// first kernel of the pass: bst[0] = m
+__global__ void k_bd_start(int m, int *bst) {
+  if (threadIdx.x == 0) {
+    bst[0] = m;
+    bst[1] = m;
+  }
+}
+
+// new columns minus their projections: B(:, kpass+q) -= B(:, 0:kpass) C(:, q)
+constexpr int BD_CCH = 64;  // rows of C staged per step
+// (columns q0 = blockIdx.y M .. q0 + M of the m; C row a at a m)
+template <int M>
+__global__ void __launch_bounds__(RT) k_bd_sub(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
+                                               const double *__restrict__ C, int m, int n) {
+  __shared__ double Cs[BD_CCH * M];
+  const int ka = pv[0].c, q0 = blockIdx.y * M;
+  const int i = blockIdx.x * RT + threadIdx.x;
+  double acc[M];
+#pragma unroll
+  for (int q = 0; q < M; ++q) acc[q] = 0.0;
+  for (int a0 = 0; a0 < ka; a0 += BD_CCH) {
+    const int na = min(BD_CCH, ka - a0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < na * M; idx += RT) Cs[idx] = C[(size_t)(a0 + idx / M) * m + q0 + idx % M];
+    __syncthreads();
+    if (i < n) {
+#pragma unroll 4
+      for (int a = 0; a < na; ++a) {
+        const double v = B[(size_t)(a0 + a) * ld + i];
+#pragma unroll
+        for (int q = 0; q < M; ++q) acc[q] = fma(v, Cs[a * M + q], acc[q]);
+      }
+    }
+  }
+  if (i >= n) return;
+#pragma unroll
+  for (int q = 0; q < M; ++q) B[(size_t)(ka + q0 + q) * ld + i] -= acc[q];
+}
+
+// kept orthonormal columns: B(:, kpass+c) = sum_q B_old(:, kpass+q) C[q][c],
+// c < bst[0], q < bst[1]; the last round also writes each kept column's hi + lo
+// FP32 copy for the split matvec (xs: m columns of ld pairs) and into the
+// split copy of the basis (xstore, column kpass + c)
+template <int NP>
+__device__ __forceinline__ void bd_apply_rows(double *__restrict__ B, int64_t ld, int kpass, int nc,
+                                              const double *Cs, int i, float2 *xs, float2 *xstore) {
+  double x[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) x[q] = B[(size_t)(kpass + q) * ld + i];
+  for (int c = 0; c < nc; ++c) {
+    double sum = 0.0;
+#pragma unroll
+    for (int q = 0; q < NP; ++q) sum = fma(x[q], Cs[q * MT_MAX + c], sum);
+    B[(size_t)(kpass + c) * ld + i] = sum;
+    if (xs) {
+      const float h = __double2float_rn(sum);
+      const float2 v = make_float2(h, __double2float_rn(sum - (double)h));
+      xs[(size_t)c * ld + i] = v;
+      xstore[(size_t)(kpass + c) * ld + i] = v;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(RT) k_bd_apply(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
+                                                 const int *__restrict__ bst, const double *__restrict__ C, int n,
+                                                 float2 *__restrict__ xs, float2 *__restrict__ xstore) {
+  __shared__ double Cs[MT_MAX * MT_MAX];
+  const int kpass = pv[0].c, np = bst[1], nc = bst[0];
+  for (int idx = threadIdx.x; idx < MT_MAX * MT_MAX; idx += RT) Cs[idx] = C[idx];
+  __syncthreads();
+  const int i = blockIdx.x * RT + threadIdx.x;
+  if (i >= n || np <= 0) return;
+  switch (np) {
+#define BD_CASE(K) \
+  case K: bd_apply_rows<K>(B, ld, kpass, nc, Cs, i, xs, xstore); break;
+    BD_CASE(1) BD_CASE(2) BD_CASE(3) BD_CASE(4) BD_CASE(5) BD_CASE(6) BD_CASE(7) BD_CASE(8)
+    BD_CASE(9) BD_CASE(10) BD_CASE(11) BD_CASE(12) BD_CASE(13) BD_CASE(14) BD_CASE(15) BD_CASE(16)
+#undef BD_CASE
+    default: break;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Split-precision block pass (SPLIT): the dot products and linear
+// combinations of the block pass on hi + lo FP32 copies of the basis
+// (x = hi + lo to 2^-48 relative), each product and sum in Dot2 form (Ogita,
+// Rump & Oishi, SIAM J. Sci. Comput. 26 (2005) 1955): the running sum takes
+// each product's high part through an error-free TwoSum, the rounding errors
+// and the low parts gather in a second float. On GB300 an FP64 FMA costs 64
+// times the issue of an FP32 one; the eleven FP32 operations of a Dot2 step
+// make these kernels about five times faster than their FP64 forms at about
+// 2^-48 relative accuracy, the accuracy of the split matvec. The FP64
+// columns stay the master copies; Bx and ABx hold the split copies of the
+// basis columns and of their products with H.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void dot2_step(float &sh, float &sl, float ah, float al, float xh, float xl) {
+  const float ph = __fmul_rn(ah, xh);
+  const float t = fmaf(ah, xl, fmaf(al, xh, fmaf(ah, xh, -ph)));
+  const float sn = __fadd_rn(sh, ph);
+  const float bb = __fsub_rn(sn, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(sn, bb)), __fsub_rn(ph, bb));
+  sh = sn;
+  sl = __fadd_rn(sl, __fadd_rn(err, t));
+}
+__device__ __forceinline__ float2 split2(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
+
+// hi + lo copies of columns c0 .. c0+nc of X
+__global__ void k_split_cols(const double *__restrict__ X, int64_t ld, int c0, int nc, int n, float2 *__restrict__ Xx) {
+  const int64_t tot = (int64_t)nc * n;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int c = (int)(e / n), i = (int)(e % n);
+    const size_t o = (size_t)(c0 + c) * ld + i;
+    Xx[o] = split2(X[o]);
+  }
+}
+
+// k_bd_dots in split form (same MODEs, same partial layout); X from the
+// split store (MODE 0, 2) or the FP64 new columns (MODE 1), W split while it
+// is staged; MODE 2 also writes the split copies of the new AB columns.
+template <int MODE>
+__global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B, const double *__restrict__ AB,
+                                                   const float2 *__restrict__ Bx, float2 *__restrict__ ABx,
+                                                   int64_t ld, const IterParams *__restrict__ pv, int m,
+                                                   const int *__restrict__ bst, int n, int cpc,
+                                                   double *__restrict__ part, int ps) {
+  __shared__ float2 Bs[BD_R * MT_MAX];       // [i][q]
+  __shared__ float2 As[BD_R * (BD_AC + 1)];  // [i][a]
+  const int kpass = pv[0].c;
+  const int nb = (MODE == 0) ? m : bst[0];
+  if (nb <= 0) return;
+  const int na = (MODE == 0) ? kpass : (MODE == 1 ? nb : kpass + nb);
+  const double *Wb = ((MODE == 2) ? AB : B) + (size_t)kpass * ld;
+  double *out = part + (size_t)blockIdx.x * ps;
+  const int rbeg = blockIdx.x * cpc * BD_R, rend = min(n, rbeg + cpc * BD_R);
+  for (int ac = blockIdx.y * BD_AC; ac < na; ac += gridDim.y * BD_AC) {
+    const int nac = min(BD_AC, na - ac), np = nac * nb;
+    float sh[BD_PAIRS], sl[BD_PAIRS];
+#pragma unroll
+    for (int k = 0; k < BD_PAIRS; ++k) sh[k] = sl[k] = 0.f;
+    for (int r0 = rbeg; r0 < rend; r0 += BD_R) {
+      const int nr = min(BD_R, rend - r0);
+      for (int idx = threadIdx.x; idx < nr * nb; idx += BD_T) {
+        const int i = idx % nr, q = idx / nr;
+        const float2 v = split2(Wb[(size_t)q * ld + r0 + i]);
+        Bs[i * MT_MAX + q] = v;
+        if (MODE == 2 && blockIdx.y == 0 && ac == 0) ABx[(size_t)(kpass + q) * ld + r0 + i] = v;
+      }
+      for (int idx = threadIdx.x; idx < nr * nac; idx += BD_T) {
+        const int i = idx % nr, a = idx / nr;
+        As[i * (BD_AC + 1) + a] = (MODE == 1) ? split2(B[(size_t)(kpass + ac + a) * ld + r0 + i])
+                                              : Bx[(size_t)(ac + a) * ld + r0 + i];
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < BD_PAIRS; ++k) {
+        const int pr = threadIdx.x + k * BD_T;
+        if (pr < np) {
+          const int a = pr % nac, q = pr / nac;
+          float h = sh[k], l = sl[k];
+          for (int i = 0; i < nr; ++i) {
+            const float2 x = As[i * (BD_AC + 1) + a], w = Bs[i * MT_MAX + q];
+            dot2_step(h, l, x.x, x.y, w.x, w.y);
+          }
+          sh[k] = h;
+          sl[k] = l;
+        }
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int k = 0; k < BD_PAIRS; ++k) {
+      const int pr = threadIdx.x + k * BD_T;
+      if (pr < np) out[(ac + pr % nac) * nb + pr / nac] = (double)sh[k] + (double)sl[k];
+    }
+  }
+}
+
+// k_bd_sub in split form: B(:, kpass+q) -= Bx(:, 0:kpass) C(:, q)
+template <int M>
+__global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const float2 *__restrict__ Bx, int64_t ld,
+                                                const IterParams *__restrict__ pv, const double *__restrict__ C,
+                                                int m, int n) {
+  __shared__ float2 Cs[BD_CCH * M];
+  const int ka = pv[0].c, q0 = blockIdx.y * M;
+  const int i = blockIdx.x * RT + threadIdx.x;
+  float sh[M], sl[M];
+#pragma unroll
+  for (int q = 0; q < M; ++q) sh[q] = sl[q] = 0.f;
+  for (int a0 = 0; a0 < ka; a0 += BD_CCH) {
+    const int na = min(BD_CCH, ka - a0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < na * M; idx += RT)
+      Cs[idx] = split2(C[(size_t)(a0 + idx / M) * m + q0 + idx % M]);
+    __syncthreads();
+    if (i < n) {
+#pragma unroll 2
+      for (int a = 0; a < na; ++a) {
+        const float2 x = Bx[(size_t)(a0 + a) * ld + i];
+#pragma unroll
+        for (int q = 0; q < M; ++q) {
+          const float2 c = Cs[a * M + q];
+          dot2_step(sh[q], sl[q], c.x, c.y, x.x, x.y);
+        }
+      }
+    }
+  }
+  if (i >= n) return;
+#pragma unroll
+  for (int q = 0; q < M; ++q) B[(size_t)(ka + q0 + q) * ld + i] -= (double)sh[q] + (double)sl[q];
+}
+
+// k_ritz_multi in split form (Bx, ABx for the basis and its products)
+template <int NT>
+__global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ Bx, const float2 *__restrict__ ABx,
+                                                    int64_t ld, int k, int nt, const double *__restrict__ S,
+                                                    const double *__restrict__ lam, double *__restrict__ T, int n,
+                                                    double *__restrict__ part, unsigned *__restrict__ counter,
+                                                    double *__restrict__ rn2) {
+  __shared__ float2 sv[MT_SMEM];
+  __shared__ double red[RT / 32];
+  __shared__ bool last;
+  const int t0 = blockIdx.y * NT;
+  for (int q = threadIdx.x; q < NT * k; q += RT) sv[q] = split2(S[(size_t)t0 * k + q]);
+  __syncthreads();
+  const int i = blockIdx.x * RT + threadIdx.x;
+  float bh[NT], bl[NT], ah[NT], al[NT];
+#pragma unroll
+  for (int t = 0; t < NT; ++t) bh[t] = bl[t] = ah[t] = al[t] = 0.f;
+  if (i < n) {
+    for (int j = 0; j < k; ++j) {
+      const float2 bj = Bx[(size_t)j * ld + i], aj = ABx[(size_t)j * ld + i];
+#pragma unroll
+      for (int t = 0; t < NT; ++t) {
+        const float2 c = sv[t * k + j];
+        dot2_step(bh[t], bl[t], c.x, c.y, bj.x, bj.y);
+        dot2_step(ah[t], al[t], c.x, c.y, aj.x, aj.y);
+      }
+    }
+  }
+#pragma unroll
+  for (int t = 0; t < NT; ++t) {
+    double r = 0.0;
+    if (i < n) {
+      const double b = (double)bh[t] + (double)bl[t], a = (double)ah[t] + (double)al[t];
+      r = fma(-lam[t0 + t], b, a);
+      T[(size_t)(2 * (t0 + t)) * ld + i] = b;
+      T[(size_t)(2 * (t0 + t) + 1) * ld + i] = r;
+    }
+    const double sq = block_sum<RT>(r * r, red);
+    if (threadIdx.x == 0) part[(size_t)(t0 + t) * gridDim.x + blockIdx.x] = sq;
+    __syncthreads();
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1);
+  __syncthreads();
+  if (!last) return;
+  for (int t = 0; t < nt; ++t) {
+    double u = 0.0;
+    for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + (size_t)t * gridDim.x + q);
+    u = block_sum<RT>(u, red);
+    if (threadIdx.x == 0) rn2[t] = u;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *counter = 0u;
+}
+
+// k_multbc in split form: out(:, j) = Xx(:, 0:k) C(:, j) for j in grid row
+// blockIdx.y's group of MB_G columns (C column j at C + j k)
+constexpr int MB_G = 8, MB_CH = 128;
+__global__ void __launch_bounds__(RT) k_multbcx(const float2 *__restrict__ Xx, int64_t ld, int k,
+                                                const double *__restrict__ C, int m, double *__restrict__ out,
+                                                int n) {
+  __shared__ float2 Cs[MB_CH * MB_G];
+  const int j0 = blockIdx.y * MB_G;
+  const int i = blockIdx.x * RT + threadIdx.x;
+  float sh[MB_G], sl[MB_G];
+#pragma unroll
+  for (int u = 0; u < MB_G; ++u) sh[u] = sl[u] = 0.f;
+  for (int q0 = 0; q0 < k; q0 += MB_CH) {
+    const int nq = min(MB_CH, k - q0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < nq * MB_G; idx += RT) {
+      const int q = idx / MB_G, j = j0 + idx % MB_G;
+      Cs[idx] = (j < m) ? split2(C[(size_t)j * k + q0 + q]) : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    if (i < n) {
+#pragma unroll 2
+      for (int q = 0; q < nq; ++q) {
+        const float2 x = Xx[(size_t)(q0 + q) * ld + i];
+#pragma unroll
+        for (int u = 0; u < MB_G; ++u) dot2_step(sh[u], sl[u], Cs[q * MB_G + u].x, Cs[q * MB_G + u].y, x.x, x.y);
+      }
+    }
+  }
+  if (i >= n) return;
+#pragma unroll
+  for (int u = 0; u < MB_G; ++u)
+    if (j0 + u < m) out[(size_t)(j0 + u) * ld + i] = (double)sh[u] + (double)sl[u];
+}
+
 struct Dvd {
   gg_ctx *ctx;
   gg_hmat *h;
@@ -837,6 +1356,33 @@ struct Dvd {
   // Gram-Schmidt -> OP -> ADDS, as one graph per m; parameters in dpv[v]
   DBuf<IterParams> dpv;
   IterParams *hpv = nullptr;      // pinned
+  // block Gram-Schmidt: CTA partials (bd_G CTAs, pitch bd_ps), coefficients,
+  // matvec skip flags, [kept, before] counts, split copies of the new columns
+  DBuf<double> bpart, bC, bskip;
+  DBuf<int> bst;
+  DBuf<float2> bxs;
+  int bd_G = 0, bd_Y = 1, bd_cpc = 0, bd_ps = 0;
+  // SPLIT: hi + lo copies of the basis and its products (split-precision
+  // block kernels); columns [0, bx_cols) of both are current
+  DBuf<float2> Bx, ABx;
+  int bx_cols = 0;
+  bool use_x() const { return precision == GG_SPLIT; }
+  int sync_split(int k) {
+    if (!use_x() || bx_cols >= k) return GG_OK;
+    if (!Bx.p) {
+      GG_TRY(Bx.alloc((size_t)lim * ld));
+      GG_TRY(ABx.alloc((size_t)lim * ld));
+    }
+    const int nc = k - bx_cols;
+    const int grid = std::min<int64_t>(((int64_t)nc * n + TPB - 1) / TPB, 8 * ctx->sms);
+    k_split_cols<<<grid, TPB, 0, s>>>(B.p, ld, bx_cols, nc, n, Bx.p);
+    k_split_cols<<<grid, TPB, 0, s>>>(AB.p, ld, bx_cols, nc, n, ABx.p);
+    note_launches(2);
+    GG_CUDA(cudaGetLastError());
+    bx_cols = k;
+    return GG_OK;
+  }
+  int *hbst = nullptr;            // pinned copy of bst
   std::vector<cudaGraphExec_t> bexec;
   std::vector<int> bkernels;
   bool use_graph = true;          // GRASP_GPU_DVD_GRAPH=0 launches the same pass kernel by kernel
@@ -965,6 +1511,7 @@ struct Dvd {
     for (cudaGraphExec_t e : bexec)
       if (e) cudaGraphExecDestroy(e);
     if (hpv) cudaFreeHost(hpv);
+    if (hbst) cudaFreeHost(hbst);
     if (graph) cudaGraphDestroy(graph);
     if (gev0) cudaEventDestroy(gev0);
     for (auto e : bev)
@@ -1067,34 +1614,87 @@ struct Dvd {
     return GG_OK;
   }
 
-  // Gram-Schmidt, OP and ADDS of new columns P[v].c, v < m, in that order per
-  // column (each column needs only the columns before it); the S columns go
-  // to dS at their packed offsets
+  // Block Gram-Schmidt of the new columns kpass .. kpass+m-1 (two block CGS
+  // passes against the basis, two Cholesky QR rounds among themselves), OP of
+  // each kept column, the new columns of S into dS at their packed offsets.
+  // kpass comes from dpv[0].c, so one graph per m serves every pass.
   int enqueue_block(int m, bool in_capture) {
+    const bool split = (precision == GG_SPLIT);
+    const int nred = std::max(1, (lim * m + 31) / 32);
+    const bool sub_split = (int64_t)nrow * 2 < ctx->sms;  // small blocks: one column per grid row
+    k_bd_start<<<1, 32, 0, s>>>(m, bst.p);
+    note_launch();
+    const dim3 gd(bd_G, bd_Y);
+    for (int round = 0; round < 2; ++round) {
+      if (split)
+        k_bdx_dots<0><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
+      else
+        k_bd_dots<0><<<gd, BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
+      k_bd_reduce<0><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p);
+      if (sub_split) {
+        if (split)
+          k_bdx_sub<1><<<dim3(nrow, m), RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);
+        else
+          k_bd_sub<1><<<dim3(nrow, m), RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);
+      } else {
+        switch (m) {
+#define BD_SUB(K)                                                                  \
+  case K:                                                                          \
+    if (split)                                                                     \
+      k_bdx_sub<K><<<nrow, RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);          \
+    else                                                                           \
+      k_bd_sub<K><<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);                 \
+    break;
+        BD_SUB(1) BD_SUB(2) BD_SUB(3) BD_SUB(4) BD_SUB(5) BD_SUB(6) BD_SUB(7) BD_SUB(8)
+        BD_SUB(9) BD_SUB(10) BD_SUB(11) BD_SUB(12) BD_SUB(13) BD_SUB(14) BD_SUB(15) BD_SUB(16)
+#undef BD_SUB
+          default: return fail(GG_ERR_ARG, "block pass: more new vectors than supported");
+        }
+      }
+      note_launches(3);
+    }
+    for (int round = 0; round < 2; ++round) {
+      if (split)
+        k_bdx_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc,
+                                                      bpart.p, bd_ps);
+      else
+        k_bd_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
+      k_bd_chol<<<1, BD_RED, 0, s>>>(m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round);
+      k_bd_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, (round == 1 && split) ? bxs.p : nullptr,
+                                     Bx.p);
+      note_launches(3);
+    }
+    GG_CUDA(cudaGetLastError());
     for (int v = 0; v < m; ++v) {
-      const PSrc ps{dpv.p + v, IterParams{}};
       const int *dcol = reinterpret_cast<const int *>(reinterpret_cast<const char *>(dpv.p + v) +
                                                       offsetof(IterParams, c));
-      cgs2(ps, false, nullptr, precision == GG_SPLIT ? h->dXs.p : nullptr);
       // each matvec between two events (read after the pass)
       if (in_capture) {
         GG_CUDA(cudaEventRecordWithFlags(bev[2 * v], s, cudaEventRecordExternal));
       } else {
         GG_CUDA(cudaEventRecord(bev[2 * v], s));
       }
-      GG_TRY(spmv_col(h, precision, B.p, AB.p, ld, dcol, nullptr, s));
+      GG_TRY(spmv_col(h, precision, B.p, AB.p, ld, dcol, bskip.p + v, s, split ? bxs.p + (size_t)v * ld : nullptr));
       if (in_capture) {
         GG_CUDA(cudaEventRecordWithFlags(bev[2 * v + 1], s, cudaEventRecordExternal));
       } else {
         GG_CUDA(cudaEventRecord(bev[2 * v + 1], s));
       }
-      launch_dots(false, ps, 1, AB.p, nullptr, -1, dS.p, 1);
     }
+    if (split)
+      k_bdx_dots<2><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
+    else
+      k_bd_dots<2><<<gd, BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
+    k_bd_reduce<2><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p);
+    note_launches(2);
+    GG_CUDA(cudaMemcpyAsync(hbst, bst.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+    GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
   // the block pass for columns kpass .. kpass+m-1: one graph launch, one copy
   // of the new S columns back
-  int block_pass(int kpass, int m, std::vector<double> &S) {
+  int block_pass(int kpass, int m, std::vector<double> &S, int *nkept) {
+    *nkept = 0;
     if (m <= 0) return GG_OK;
     if (m > MT_MAX) return fail(GG_ERR_ARG, "block pass: more new vectors than supported");
     if (bev.empty()) {
@@ -1106,7 +1706,22 @@ struct Dvd {
       GG_CUDA(cudaMallocHost(&hpv, MT_MAX * sizeof(IterParams)));
       bexec.assign(MT_MAX + 1, nullptr);
       bkernels.assign(MT_MAX + 1, 0);
+      // row ranges of BD_R-row chunks, about two CTAs per SM
+      // (grid rows: column chunks of BD_AC, up to LIM / BD_AC of them)
+      const int nchunk = (n + BD_R - 1) / BD_R;
+      bd_Y = std::max(1, (lim + BD_AC - 1) / BD_AC);
+      const int want = std::max(1, (2 * ctx->sms + bd_Y - 1) / bd_Y);
+      bd_cpc = (nchunk + want - 1) / want;
+      bd_G = (nchunk + bd_cpc - 1) / bd_cpc;
+      bd_ps = lim * MT_MAX;
+      GG_TRY(bpart.alloc((size_t)bd_G * bd_ps));
+      GG_TRY(bC.alloc((size_t)std::max(lim * MT_MAX, MT_MAX * MT_MAX)));
+      GG_TRY(bskip.alloc(MT_MAX));
+      GG_TRY(bst.alloc(2));
+      GG_CUDA(cudaMallocHost(&hbst, 2 * sizeof(int)));
+      if (precision == GG_SPLIT) GG_TRY(bxs.alloc((size_t)MT_MAX * ld));
     }
+    GG_TRY(sync_split(kpass));
     for (int v = 0; v < m; ++v) {
       hpv[v] = IterParams{};
       hpv[v].c = kpass + v;
@@ -1136,19 +1751,23 @@ struct Dvd {
     } else {
       GG_TRY(enqueue_block(m, false));
     }
-    nmv += m;
-    mv_count += m;
     const size_t o0 = (size_t)kpass * (kpass + 1) / 2, o1 = (size_t)(kpass + m) * (kpass + m + 1) / 2;
     GG_CUDA(cudaMemcpyAsync(hS + o0, dS.p + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, s));
     const auto t0 = std::chrono::steady_clock::now();
     GG_CUDA(cudaStreamSynchronize(s));
     t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    const int nk = hbst[0];
+    if (nk < 0 || nk > m) return fail(GG_ERR_STATE, "block pass: kept column count out of range");
     std::memcpy(S.data() + o0, hS + o0, (o1 - o0) * sizeof(double));
     for (int v = 0; v < m; ++v) {
       float ms = 0.f;
       GG_CUDA(cudaEventElapsedTime(&ms, bev[2 * v], bev[2 * v + 1]));
       mv_ms += ms;
     }
+    nmv += nk;
+    mv_count += nk;
+    if (use_x()) bx_cols = kpass + nk;  // written by the pass (k_bd_apply, k_bdx_dots<2>)
+    *nkept = nk;
     return GG_OK;
   }
 
@@ -1295,8 +1914,37 @@ struct Dvd {
     GG_CUDA(cudaMemcpyAsync(dmt.p, hmt, (size_t)nt * k * sizeof(double), cudaMemcpyHostToDevice, s));
     GG_CUDA(cudaMemcpyAsync(dmt.p + (size_t)MT_MAX * lim, hl, nt * sizeof(double), cudaMemcpyHostToDevice, s));
     double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
-    k_ritz_multi<<<nrow, RT, 0, s>>>(B.p, AB.p, ld, k, nt, dmt.p, dmt.p + (size_t)MT_MAX * lim, T.p, n, part.p,
-                                     counters.p + 3, drn);
+    // one group of all targets, or (small blocks) one target per grid row
+    const bool per_target = (int64_t)nrow * 2 < ctx->sms;
+    const double *dl = dmt.p + (size_t)MT_MAX * lim;
+    if (use_x()) {
+      GG_TRY(sync_split(k));
+      if (per_target) {
+        k_ritzx_multi<1><<<dim3(nrow, nt), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
+                                                       counters.p + 3, drn);
+      } else {
+        switch (nt) {
+#define RM_CASE(K) \
+  case K: k_ritzx_multi<K><<<nrow, RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
+          RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
+          RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
+#undef RM_CASE
+          default: return fail(GG_ERR_ARG, "ritz_multi: more targets than supported");
+        }
+      }
+    } else if (per_target) {
+      k_ritz_multi<1><<<dim3(nrow, nt), RT, 0, s>>>(B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3,
+                                                    drn);
+    } else {
+      switch (nt) {
+#define RM_CASE(K) \
+  case K: k_ritz_multi<K><<<nrow, RT, 0, s>>>(B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
+        RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
+        RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
+#undef RM_CASE
+        default: return fail(GG_ERR_ARG, "ritz_multi: more targets than supported");
+      }
+    }
     note_launch();
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaMemcpyAsync(hl + MT_MAX, drn, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -1314,13 +1962,26 @@ struct Dvd {
   }
   // X[:, 0:m) = X[:, 0:k) C (k x m): computed into T, copied back (BASIS and
   // AB keep their addresses, which the iteration graph holds)
-  int multbc(DBuf<double> &X, int k, int m, const double *hC) {
+  // (SPLIT: from the split copies, which are made current first)
+  int multbc(DBuf<double> &X, DBuf<float2> &Xx, int k, int m, const double *hC) {
     if ((size_t)k * m > small.n) GG_TRY(small.alloc((size_t)k * m));
     GG_CUDA(cudaMemcpyAsync(small.p, hC, (size_t)k * m * sizeof(double), cudaMemcpyHostToDevice, s));
-    k_multbc<<<(n + RC - 1) / RC, TPB, 0, s>>>(X.p, ld, k, small.p, m, T.p, n);
+    if (use_x()) {
+      GG_TRY(sync_split(k));
+      k_multbcx<<<dim3(nrow, (m + MB_G - 1) / MB_G), RT, 0, s>>>(Xx.p, ld, k, small.p, m, T.p, n);
+    } else {
+      k_multbc<<<(n + RC - 1) / RC, TPB, 0, s>>>(X.p, ld, k, small.p, m, T.p, n);
+    }
     note_launch();
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaMemcpyAsync(X.p, T.p, (size_t)m * ld * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return GG_OK;
+  }
+  // BASIS and AB both times C (OVFLOW's restart, the final eigenvectors)
+  int multbc2(int k, int m, const double *hC) {
+    GG_TRY(multbc(B, Bx, k, m, hC));
+    GG_TRY(multbc(AB, ABx, k, m, hC));
+    bx_cols = 0;  // the split copies no longer match
     return GG_OK;
   }
   // Block pass (MBLOCK > 1): Ritz vector and residual of one target into
@@ -1492,8 +2153,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
     }
     if (DONE || KPASS >= n) break;
     if (KPASS == LIM) {  // OVFLOW (dvdson.f90:1179-1256)
-      GG_TRY(D.multbc(D.B, KPASS, REST, SVEC.data()));
-      GG_TRY(D.multbc(D.AB, KPASS, REST, SVEC.data()));
+      GG_TRY(D.multbc2(KPASS, REST, SVEC.data()));
       std::fill(S.begin(), S.end(), 0.0);
       std::fill(SVEC.begin(), SVEC.begin() + (size_t)REST * REST, 0.0);
       int64_t ind = 0, icur = 0;
@@ -1625,7 +2285,10 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
     }
     // Gram-Schmidt of the new vectors, OP, ADDS
     if (NNCV <= MT_MAX) {
-      GG_TRY(D.block_pass(KPASS, NNCV, S));
+      int nk = 0;
+      GG_TRY(D.block_pass(KPASS, NNCV, S, &nk));
+      if (nk == 0) break;  // no direction outside the basis is left
+      NNCV = nk;
     } else {
       for (int v = 0; v < NNCV; ++v) GG_TRY(D.orthonormalize(KPASS + v));
       GG_TRY(D.op(KPASS, NNCV));
@@ -1641,8 +2304,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   }
   // label 30 (dvdson.f90:821-836)
   for (int i = 0; i < NUME; ++i) OLDVAL[i] = std::fabs(OLDVAL[i] - EIGVAL[i]);
-  GG_TRY(D.multbc(D.B, KPASS, NUME, SVEC.data()));
-  GG_TRY(D.multbc(D.AB, KPASS, NUME, SVEC.data()));
+  GG_TRY(D.multbc2(KPASS, NUME, SVEC.data()));
   resid_out.assign(NUME, 0.0);
   for (int i = 0; i < NUME; ++i) {
     const int nb = std::min((n + TPB - 1) / TPB, 1024);

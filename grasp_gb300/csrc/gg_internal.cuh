@@ -210,8 +210,9 @@ int timer_stop(gg_ctx *ctx, double *ms);
 int build_sym(gg_hmat *h);
 int refresh_sym_values(gg_hmat *h);
 int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s);
+// xs: the split (hi + lo FP32) copy of x to read; null = the matrix's dXs
 int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
-             const double *skip, cudaStream_t s);
+             const double *skip, cudaStream_t s, const float2 *xs = nullptr);
 double spmv_bytes(const gg_hmat *h, int precision, int m);
 // ltile.cu
 int build_ltile(gg_hmat *h);

@@ -278,17 +278,20 @@ __global__ void k_col16(const int32_t *__restrict__ col, int64_t nnz, unsigned s
 // y = H x with x = Bbase + c ld, y = ABbase + c ld, c = *dcol on the device;
 // GG_SPLIT reads x from h->dXs (the caller's split copy of the same column)
 int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
-             const double *skip, cudaStream_t s) {
+             const double *skip, cudaStream_t s, const float2 *xs) {
   const int n = h->ncf;
   const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
   if (precision == GG_SPLIT) {
-    if (h->dXs.n < (size_t)n) return fail(GG_ERR_STATE, "spmv_col: split copy of x not allocated");
-    if (h->lt.usable) return spmv_ltile(h, h->dXs.p, Bbase, ABbase, ld, dcol, skip, s);
+    if (!xs) {
+      if (h->dXs.n < (size_t)n) return fail(GG_ERR_STATE, "spmv_col: split copy of x not allocated");
+      xs = h->dXs.p;
+    }
+    if (h->lt.usable) return spmv_ltile(h, xs, Bbase, ABbase, ld, dcol, skip, s);
     if (h->sym_col16)
-      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
+      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, xs,
                                               h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
     else
-      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
+      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xs,
                                               h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
     ::gg::note_launch();
   } else {
