@@ -1054,11 +1054,12 @@ __global__ void __launch_bounds__(RT) k_bd_sub(double *__restrict__ B, int64_t l
 
 // kept orthonormal columns: B(:, kpass+c) = sum_q B_old(:, kpass+q) C[q][c],
 // c < bst[0], q < bst[1]; the last round also writes each kept column's hi + lo
-// FP32 copy for the split matvec (xs: m columns of ld pairs) and into the
-// split copy of the basis (xstore, column kpass + c)
+// FP32 copy for the block matvec (xs: interleaved by row, mp per row, zeros
+// beyond the kept columns) and into the split copy of the basis (xstore,
+// column kpass + c)
 template <int NP>
 __device__ __forceinline__ void bd_apply_rows(double *__restrict__ B, int64_t ld, int kpass, int nc,
-                                              const double *Cs, int i, float2 *xs, float2 *xstore) {
+                                              const double *Cs, int i, float2 *xs, int mp, float2 *xstore) {
   double x[NP];
 #pragma unroll
   for (int q = 0; q < NP; ++q) x[q] = B[(size_t)(kpass + q) * ld + i];
@@ -1070,15 +1071,17 @@ __device__ __forceinline__ void bd_apply_rows(double *__restrict__ B, int64_t ld
     if (xs) {
       const float h = __double2float_rn(sum);
       const float2 v = make_float2(h, __double2float_rn(sum - (double)h));
-      xs[(size_t)c * ld + i] = v;
+      xs[(size_t)i * mp + c] = v;
       xstore[(size_t)(kpass + c) * ld + i] = v;
     }
   }
+  if (xs)
+    for (int c = nc; c < mp; ++c) xs[(size_t)i * mp + c] = make_float2(0.f, 0.f);
 }
 
 __global__ void __launch_bounds__(RT) k_bd_apply(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
                                                  const int *__restrict__ bst, const double *__restrict__ C, int n,
-                                                 float2 *__restrict__ xs, float2 *__restrict__ xstore) {
+                                                 float2 *__restrict__ xs, int mp, float2 *__restrict__ xstore) {
   __shared__ double Cs[MT_MAX * MT_MAX];
   const int kpass = pv[0].c, np = bst[1], nc = bst[0];
   for (int idx = threadIdx.x; idx < MT_MAX * MT_MAX; idx += RT) Cs[idx] = C[idx];
@@ -1087,7 +1090,7 @@ __global__ void __launch_bounds__(RT) k_bd_apply(double *__restrict__ B, int64_t
   if (i >= n || np <= 0) return;
   switch (np) {
 #define BD_CASE(K) \
-  case K: bd_apply_rows<K>(B, ld, kpass, nc, Cs, i, xs, xstore); break;
+  case K: bd_apply_rows<K>(B, ld, kpass, nc, Cs, i, xs, mp, xstore); break;
     BD_CASE(1) BD_CASE(2) BD_CASE(3) BD_CASE(4) BD_CASE(5) BD_CASE(6) BD_CASE(7) BD_CASE(8)
     BD_CASE(9) BD_CASE(10) BD_CASE(11) BD_CASE(12) BD_CASE(13) BD_CASE(14) BD_CASE(15) BD_CASE(16)
 #undef BD_CASE
@@ -1661,11 +1664,26 @@ struct Dvd {
         k_bd_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
       k_bd_chol<<<1, BD_RED, 0, s>>>(m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round);
       k_bd_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, (round == 1 && split) ? bxs.p : nullptr,
-                                     Bx.p);
+                                     (m + 1) & ~1, Bx.p);
       note_launches(3);
     }
     GG_CUDA(cudaGetLastError());
-    for (int v = 0; v < m; ++v) {
+    if (split) {
+      // all m columns in one sweep over the matrix (dropped columns are zero)
+      const int *dcol0 = reinterpret_cast<const int *>(reinterpret_cast<const char *>(dpv.p) + offsetof(IterParams, c));
+      if (in_capture) {
+        GG_CUDA(cudaEventRecordWithFlags(bev[0], s, cudaEventRecordExternal));
+      } else {
+        GG_CUDA(cudaEventRecord(bev[0], s));
+      }
+      GG_TRY(spmm_block(h, m, bxs.p, B.p, AB.p, ld, dcol0, s));
+      if (in_capture) {
+        GG_CUDA(cudaEventRecordWithFlags(bev[1], s, cudaEventRecordExternal));
+      } else {
+        GG_CUDA(cudaEventRecord(bev[1], s));
+      }
+    }
+    for (int v = 0; v < m && !split; ++v) {
       const int *dcol = reinterpret_cast<const int *>(reinterpret_cast<const char *>(dpv.p + v) +
                                                       offsetof(IterParams, c));
       // each matvec between two events (read after the pass)
@@ -1674,7 +1692,7 @@ struct Dvd {
       } else {
         GG_CUDA(cudaEventRecord(bev[2 * v], s));
       }
-      GG_TRY(spmv_col(h, precision, B.p, AB.p, ld, dcol, bskip.p + v, s, split ? bxs.p + (size_t)v * ld : nullptr));
+      GG_TRY(spmv_col(h, precision, B.p, AB.p, ld, dcol, bskip.p + v, s));
       if (in_capture) {
         GG_CUDA(cudaEventRecordWithFlags(bev[2 * v + 1], s, cudaEventRecordExternal));
       } else {
@@ -1759,7 +1777,7 @@ struct Dvd {
     const int nk = hbst[0];
     if (nk < 0 || nk > m) return fail(GG_ERR_STATE, "block pass: kept column count out of range");
     std::memcpy(S.data() + o0, hS + o0, (o1 - o0) * sizeof(double));
-    for (int v = 0; v < m; ++v) {
+    for (int v = 0; v < (use_x() ? 1 : m); ++v) {
       float ms = 0.f;
       GG_CUDA(cudaEventElapsedTime(&ms, bev[2 * v], bev[2 * v + 1]));
       mv_ms += ms;

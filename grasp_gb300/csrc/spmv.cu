@@ -266,6 +266,67 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
   if (lane == 0) ABbase[off + row] = ((double)acc.h + (double)acc.l) + diag[row] * Bbase[off + row];
 }
 
+// Y = H X for the m new columns of a Davidson block pass in one sweep over
+// the matrix (SPLIT): X interleaved by row, xb[j MP + v] = hi + lo of
+// x_v[j] (MP = m rounded up to even, so that a row is whole 16-byte loads);
+// y_v = ABbase + (kpass + v) ld with kpass = *pc on the device, the diagonal
+// term from the FP64 x_v = Bbase + (kpass + v) ld. One warp per row; each
+// lane's products go into per-vector Dot2 sums (Ogita, Rump & Oishi), which
+// are then added across the warp in double-float.
+template <int M, typename CI>
+__global__ void __launch_bounds__(256) k_spmm_split(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
+                                                    const float *__restrict__ hi, const float *__restrict__ lo,
+                                                    const float2 *__restrict__ xb, const double *__restrict__ diag,
+                                                    const double *__restrict__ Bbase, double *__restrict__ ABbase,
+                                                    int64_t ld, const int *__restrict__ pc, int n) {
+  constexpr int MP = (M + 1) & ~1;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const int64_t p0 = ptr[row], p1 = ptr[row + 1];
+  float sh[M], sl[M];
+#pragma unroll
+  for (int v = 0; v < M; ++v) sh[v] = sl[v] = 0.f;
+#pragma unroll 2
+  for (int64_t p = p0 + lane; p < p1; p += 32) {
+    const float ah = __ldg(hi + p), al = __ldg(lo + p);
+    const float4 *xr = reinterpret_cast<const float4 *>(xb + (size_t)__ldg(col + p) * MP);
+#pragma unroll
+    for (int u = 0; u < MP / 2; ++u) {
+      const float4 x = __ldg(xr + u);
+      const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int v = 2 * u + h;
+        if (v < M) {
+          const float xh = xv[2 * h], xl = xv[2 * h + 1];
+          const float ph = __fmul_rn(ah, xh);
+          const float t = fmaf(ah, xl, fmaf(al, xh, fmaf(ah, xh, -ph)));
+          const float sn = __fadd_rn(sh[v], ph);
+          const float bb = __fsub_rn(sn, sh[v]);
+          const float err = __fadd_rn(__fsub_rn(sh[v], __fsub_rn(sn, bb)), __fsub_rn(ph, bb));
+          sh[v] = sn;
+          sl[v] = __fadd_rn(sl[v], __fadd_rn(err, t));
+        }
+      }
+    }
+  }
+  const size_t off = (size_t)(*pc) * ld + row;
+  double mine = 0.0;
+#pragma unroll
+  for (int v = 0; v < M; ++v) {
+    df acc = two_sum(sh[v], sl[v]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      df other;
+      other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
+      other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
+      acc = df_add(acc, other);
+    }
+    if (lane == v) mine = (double)acc.h + (double)acc.l;
+  }
+  if (lane < M) ABbase[off + (size_t)lane * ld] = mine + diag[row] * Bbase[off + (size_t)lane * ld];
+}
+
 // 16-bit copy of the column indices (blocks of at most 65,536 CSFs): the
 // split matvec then reads 10 bytes per stored entry instead of 12
 __global__ void k_col16(const int32_t *__restrict__ col, int64_t nnz, unsigned short *__restrict__ c16) {
@@ -416,6 +477,31 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
 // Algorithmic bytes of one y = H x in the reference's storage (lower
 // triangle once): nnz_l (8 + 4) + (ncf + 1) 8 + 3 ncf 8 m for FP64 (hi+lo is
 // the same byte count).
+// the block form of spmv_col (SPLIT only): m new columns from kpass = *dcol
+int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,
+               const int *dcol, cudaStream_t s) {
+  const int n = h->ncf;
+  const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
+  switch (m) {
+#define SPMM_CASE(K)                                                                                              \
+  case K:                                                                                                         \
+    if (h->sym_col16)                                                                                             \
+      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, xb,          \
+                                             h->dDiag.p, Bbase, ABbase, ld, dcol, n);                             \
+    else                                                                                                          \
+      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xb,            \
+                                             h->dDiag.p, Bbase, ABbase, ld, dcol, n);                             \
+    break;
+    SPMM_CASE(1) SPMM_CASE(2) SPMM_CASE(3) SPMM_CASE(4) SPMM_CASE(5) SPMM_CASE(6) SPMM_CASE(7) SPMM_CASE(8)
+    SPMM_CASE(9) SPMM_CASE(10) SPMM_CASE(11) SPMM_CASE(12) SPMM_CASE(13) SPMM_CASE(14) SPMM_CASE(15) SPMM_CASE(16)
+#undef SPMM_CASE
+    default: return fail(GG_ERR_ARG, "spmm_block: 1 to 16 columns");
+  }
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
 double spmv_bytes(const gg_hmat *h, int precision, int m) {
   (void)precision;
   return (double)h->nnz * 12.0 + (double)(h->ncf + 1) * 8.0 + 3.0 * h->ncf * 8.0 * m;
