@@ -232,6 +232,12 @@ class HMatrix:
         check(_lib.gpu().gg_matvec_timing(self.ctx._h, self._h, precision, iters, C.byref(ms), C.byref(by)))
         return ms.value, by.value
 
+    def spmm_timing(self, m, iters=20):
+        """(ms per split Y = H X launch over m vectors, algorithmic bytes per launch)."""
+        ms = C.c_double(); by = C.c_double()
+        check(_lib.gpu().gg_spmm_timing(self.ctx._h, self._h, m, iters, C.byref(ms), C.byref(by)))
+        return ms.value, by.value
+
 
 def maneig_batched(ctx, hmats, nvec, precision=FP64, lim=0, maxiter=0, critr=0.0, raise_on_maxiter=True):
     """MANEIG for many blocks in one batched GPU Davidson (gg_maneig_batched).

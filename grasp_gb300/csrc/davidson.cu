@@ -887,6 +887,7 @@ __device__ __forceinline__ double bd_reduce(const double *__restrict__ part, int
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double u = 0.0;
   if (ok)
+#pragma unroll 8
     for (int t = w; t < ntiles; t += nw) u += part[(size_t)t * ps + o];
   red[w * 32 + lane] = u;
   __syncthreads();
@@ -948,6 +949,7 @@ __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst
   const bool ok = nb > 0 && o < nb * nb;
   double u = 0.0;
   if (ok)
+#pragma unroll 8
     for (int t = sub; t < ntiles; t += 4) u += part[(size_t)t * ps + o];
   red[tid] = u;
   __syncthreads();
@@ -1214,7 +1216,7 @@ __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const fl
       Cs[idx] = split2(C[(size_t)(a0 + idx / M) * m + q0 + idx % M]);
     __syncthreads();
     if (i < n) {
-#pragma unroll 2
+#pragma unroll 8
       for (int a = 0; a < na; ++a) {
         const float2 x = Bx[(size_t)(a0 + a) * ld + i];
 #pragma unroll
@@ -1248,6 +1250,7 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
 #pragma unroll
   for (int t = 0; t < NT; ++t) bh[t] = bl[t] = ah[t] = al[t] = 0.f;
   if (i < n) {
+#pragma unroll 4
     for (int j = 0; j < k; ++j) {
       const float2 bj = Bx[(size_t)j * ld + i], aj = ABx[(size_t)j * ld + i];
 #pragma unroll
@@ -1307,7 +1310,7 @@ __global__ void __launch_bounds__(RT) k_multbcx(const float2 *__restrict__ Xx, i
     }
     __syncthreads();
     if (i < n) {
-#pragma unroll 2
+#pragma unroll 8
       for (int q = 0; q < nq; ++q) {
         const float2 x = Xx[(size_t)(q0 + q) * ld + i];
 #pragma unroll
@@ -1726,8 +1729,9 @@ struct Dvd {
       bkernels.assign(MT_MAX + 1, 0);
       // row ranges of BD_R-row chunks, about two CTAs per SM
       // (grid rows: column chunks of BD_AC, up to LIM / BD_AC of them)
+      // (column chunks as grid rows only when the row ranges alone leave SMs idle)
       const int nchunk = (n + BD_R - 1) / BD_R;
-      bd_Y = std::max(1, (lim + BD_AC - 1) / BD_AC);
+      bd_Y = (nchunk >= 2 * ctx->sms) ? 1 : std::max(1, (lim + BD_AC - 1) / BD_AC);
       const int want = std::max(1, (2 * ctx->sms + bd_Y - 1) / bd_Y);
       bd_cpc = (nchunk + want - 1) / want;
       bd_G = (nchunk + bd_cpc - 1) / bd_cpc;
@@ -1850,6 +1854,27 @@ struct Dvd {
   // OP (gdvd.f90:137-142): AB[:, j0:j0+m) = H BASIS[:, j0:j0+m); each launch
   // is bracketed by events that are read after the solve (no extra sync)
   int op(int j0, int m) {
+    if (precision == GG_SPLIT && m >= 2) {  // blocks of up to 16 columns, one sweep each
+      for (int v0 = 0; v0 < m; v0 += 16) {
+        const int mb = std::min(16, m - v0);
+        if (ev_used + 2 > evs.size())
+          for (int q = 0; q < 64; ++q) {
+            cudaEvent_t e;
+            GG_CUDA(cudaEventCreate(&e));
+            evs.push_back(e);
+          }
+        GG_CUDA(cudaEventRecord(evs[ev_used], s));
+        if (mb >= 2)
+          GG_TRY(spmm_cols(h, col(B, j0 + v0), col(AB, j0 + v0), ld, mb, s));
+        else
+          GG_TRY(spmv(h, precision, col(B, j0 + v0), col(AB, j0 + v0), 1, s));
+        GG_CUDA(cudaEventRecord(evs[ev_used + 1], s));
+        ev_used += 2;
+        mv_count += mb;
+      }
+      nmv += m;
+      return GG_OK;
+    }
     for (int v = 0; v < m; ++v) {
       if (ev_used + 2 > evs.size()) {
         for (int q = 0; q < 64; ++q) {

@@ -193,6 +193,7 @@ struct gg_hmat {
   gg::DBuf<double> dSymVal;             // [sym_nnz] FP64 values
   gg::DBuf<float> dSymHi, dSymLo;       // [sym_nnz] split values
   gg::DBuf<float2> dXs;                 // [ncf] split copy of the input vector
+  gg::DBuf<float2> dXb;                 // [ncf][m even] split copies of m input vectors, by row
   bool sym_vals_valid = false;
   gg::LTile lt;                         // tiled lower-triangle layout (split matvec)
 };
@@ -213,10 +214,12 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
 // xs: the split (hi + lo FP32) copy of x to read; null = the matrix's dXs
 int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
              const double *skip, cudaStream_t s, const float2 *xs = nullptr);
-// block form (SPLIT): columns kpass .. kpass+m-1, kpass = *dcol; xb holds their
+// block form (SPLIT): columns kpass .. kpass+m-1, kpass = *dcol (0 when dcol is
+// null); xb holds their
 // hi + lo values interleaved by row (row j at xb + j (m rounded up to even))
 int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,
                const int *dcol, cudaStream_t s);
+int spmm_cols(gg_hmat *h, const double *X, double *Y, int64_t ld, int m, cudaStream_t s);
 double spmv_bytes(const gg_hmat *h, int precision, int m);
 // ltile.cu
 int build_ltile(gg_hmat *h);

@@ -268,63 +268,85 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
 
 // Y = H X for the m new columns of a Davidson block pass in one sweep over
 // the matrix (SPLIT): X interleaved by row, xb[j MP + v] = hi + lo of
-// x_v[j] (MP = m rounded up to even, so that a row is whole 16-byte loads);
-// y_v = ABbase + (kpass + v) ld with kpass = *pc on the device, the diagonal
-// term from the FP64 x_v = Bbase + (kpass + v) ld. One warp per row; each
-// lane's products go into per-vector Dot2 sums (Ogita, Rump & Oishi), which
-// are then added across the warp in double-float.
+// x_v[j] (MP = m rounded up to even: a row is MP / 2 16-byte pieces);
+// y_v = ABbase + (kpass + v) ld with kpass = *pc on the device (0 when pc is
+// null), the diagonal term from the FP64 x_v = Bbase + (kpass + v) ld.
+// One warp per row. A stored entry is taken by LPE = MP / 2 lanes, lane u
+// reading piece u of the gathered row (vectors 2u, 2u + 1), so that each
+// load instruction touches a few whole rows of xb instead of 32 scattered
+// ones; EPW = 32 / LPE entries per step. Products go into per-vector Dot2
+// sums (Ogita, Rump & Oishi), added over the EPW entry slots by a fixed
+// shuffle tree in double-float.
 template <int M, typename CI>
 __global__ void __launch_bounds__(256) k_spmm_split(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
                                                     const float *__restrict__ hi, const float *__restrict__ lo,
                                                     const float2 *__restrict__ xb, const double *__restrict__ diag,
                                                     const double *__restrict__ Bbase, double *__restrict__ ABbase,
                                                     int64_t ld, const int *__restrict__ pc, int n) {
-  constexpr int MP = (M + 1) & ~1;
+  constexpr int MP = (M + 1) & ~1, LPE = MP / 2, EPW = 32 / LPE;
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (row >= n) return;
+  const int e = lane / LPE, u = lane % LPE;
+  const bool act = e < EPW;
   const int64_t p0 = ptr[row], p1 = ptr[row + 1];
-  float sh[M], sl[M];
-#pragma unroll
-  for (int v = 0; v < M; ++v) sh[v] = sl[v] = 0.f;
-#pragma unroll 2
-  for (int64_t p = p0 + lane; p < p1; p += 32) {
-    const float ah = __ldg(hi + p), al = __ldg(lo + p);
-    const float4 *xr = reinterpret_cast<const float4 *>(xb + (size_t)__ldg(col + p) * MP);
-#pragma unroll
-    for (int u = 0; u < MP / 2; ++u) {
-      const float4 x = __ldg(xr + u);
-      const float xv[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int v = 2 * u + h;
-        if (v < M) {
-          const float xh = xv[2 * h], xl = xv[2 * h + 1];
-          const float ph = __fmul_rn(ah, xh);
-          const float t = fmaf(ah, xl, fmaf(al, xh, fmaf(ah, xh, -ph)));
-          const float sn = __fadd_rn(sh[v], ph);
-          const float bb = __fsub_rn(sn, sh[v]);
-          const float err = __fadd_rn(__fsub_rn(sh[v], __fsub_rn(sn, bb)), __fsub_rn(ph, bb));
-          sh[v] = sn;
-          sl[v] = __fadd_rn(sl[v], __fadd_rn(err, t));
-        }
-      }
+  const float4 *xr = reinterpret_cast<const float4 *>(xb) + u;
+  float h0 = 0.f, l0 = 0.f, h1 = 0.f, l1 = 0.f;
+  auto step = [&](float &sh, float &sl, float ah, float al, float xh, float xl) {
+    const float ph = __fmul_rn(ah, xh);
+    const float t = fmaf(ah, xl, fmaf(al, xh, fmaf(ah, xh, -ph)));
+    const float sn = __fadd_rn(sh, ph);
+    const float bb = __fsub_rn(sn, sh);
+    const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(sn, bb)), __fsub_rn(ph, bb));
+    sh = sn;
+    sl = __fadd_rn(sl, __fadd_rn(err, t));
+  };
+  if (act) {
+#pragma unroll 4
+    for (int64_t p = p0 + e; p < p1; p += EPW) {
+      const float ah = __ldg(hi + p), al = __ldg(lo + p);
+      const float4 x = __ldg(xr + (size_t)__ldg(col + p) * LPE);
+      step(h0, l0, ah, al, x.x, x.y);
+      if (2 * u + 1 < M) step(h1, l1, ah, al, x.z, x.w);
     }
   }
-  const size_t off = (size_t)(*pc) * ld + row;
-  double mine = 0.0;
+  df a0 = two_sum(h0, l0), a1 = two_sum(h1, l1);
+  // slot e takes slot e + s (s = 1, 2, 4, ...) for e a multiple of 2 s
 #pragma unroll
-  for (int v = 0; v < M; ++v) {
-    df acc = two_sum(sh[v], sl[v]);
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      df other;
-      other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
-      other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
-      acc = df_add(acc, other);
+  for (int s = 1; s < EPW; s <<= 1) {
+    df o0, o1;
+    o0.h = __shfl_down_sync(0xffffffffu, a0.h, s * LPE);
+    o0.l = __shfl_down_sync(0xffffffffu, a0.l, s * LPE);
+    o1.h = __shfl_down_sync(0xffffffffu, a1.h, s * LPE);
+    o1.l = __shfl_down_sync(0xffffffffu, a1.l, s * LPE);
+    if (e % (2 * s) == 0 && e + s < EPW) {
+      a0 = df_add(a0, o0);
+      a1 = df_add(a1, o1);
     }
-    if (lane == v) mine = (double)acc.h + (double)acc.l;
   }
-  if (lane < M) ABbase[off + (size_t)lane * ld] = mine + diag[row] * Bbase[off + (size_t)lane * ld];
+  if (e != 0) return;
+  const size_t off = (pc ? (size_t)(*pc) : 0) * ld + row;
+  const double dg = diag[row];
+  const size_t o0 = off + (size_t)(2 * u) * ld;
+  ABbase[o0] = ((double)a0.h + (double)a0.l) + dg * Bbase[o0];
+  if (2 * u + 1 < M) {
+    const size_t o1 = o0 + ld;
+    ABbase[o1] = ((double)a1.h + (double)a1.l) + dg * Bbase[o1];
+  }
+}
+
+// xb[i mp + v] = hi + lo of x[v ld + i] for v < m, zero for m <= v < mp
+__global__ void k_split_block(const double *__restrict__ x, int64_t ld, int m, int mp, int n, float2 *__restrict__ xb) {
+  const int64_t tot = (int64_t)n * mp;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(e / mp), v = (int)(e % mp);
+    float2 r = make_float2(0.f, 0.f);
+    if (v < m) {
+      const double d = x[(size_t)v * ld + i];
+      const float h = __double2float_rn(d);
+      r = make_float2(h, __double2float_rn(d - (double)h));
+    }
+    xb[e] = r;
+  }
 }
 
 // 16-bit copy of the column indices (blocks of at most 65,536 CSFs): the
@@ -445,10 +467,12 @@ int refresh_sym_values(gg_hmat *h) {
   return GG_OK;
 }
 
-// y[:, v] = H x[:, v] for v < m (column-major [ncf x m]); stream-ordered
+// y[:, v] = H x[:, v] for v < m (column-major [ncf x m]); stream-ordered.
+// SPLIT with 2 to 16 vectors: one sweep over the matrix for all of them.
 int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s) {
   const int n = h->ncf;
   const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
+  if (precision == GG_SPLIT && m >= 2 && m <= 16) return spmm_cols(h, dx, dy, n, m, s);
   for (int v = 0; v < m; ++v) {
     const double *x = dx + (size_t)v * n;
     double *y = dy + (size_t)v * n;
@@ -486,11 +510,11 @@ int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double 
 #define SPMM_CASE(K)                                                                                              \
   case K:                                                                                                         \
     if (h->sym_col16)                                                                                             \
-      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, xb,          \
-                                             h->dDiag.p, Bbase, ABbase, ld, dcol, n);                             \
+      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, xb,       \
+                                                h->dDiag.p, Bbase, ABbase, ld, dcol, n);                          \
     else                                                                                                          \
-      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xb,            \
-                                             h->dDiag.p, Bbase, ABbase, ld, dcol, n);                             \
+      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xb,         \
+                                                h->dDiag.p, Bbase, ABbase, ld, dcol, n);                          \
     break;
     SPMM_CASE(1) SPMM_CASE(2) SPMM_CASE(3) SPMM_CASE(4) SPMM_CASE(5) SPMM_CASE(6) SPMM_CASE(7) SPMM_CASE(8)
     SPMM_CASE(9) SPMM_CASE(10) SPMM_CASE(11) SPMM_CASE(12) SPMM_CASE(13) SPMM_CASE(14) SPMM_CASE(15) SPMM_CASE(16)
@@ -502,6 +526,17 @@ int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double 
   return GG_OK;
 }
 
+// Y = H X for m columns (2 to 16) of leading dimension ld, SPLIT: the split
+// copies go to h->dXb, then one block sweep
+int spmm_cols(gg_hmat *h, const double *X, double *Y, int64_t ld, int m, cudaStream_t s) {
+  const int n = h->ncf, mp = (m + 1) & ~1;
+  GG_TRY(h->dXb.alloc((size_t)n * mp));
+  k_split_block<<<(unsigned)std::min<int64_t>(((int64_t)n * mp + 255) / 256, 4096), 256, 0, s>>>(X, ld, m, mp, n,
+                                                                                                 h->dXb.p);
+  ::gg::note_launch();
+  return spmm_block(h, m, h->dXb.p, X, Y, ld, nullptr, s);
+}
+
 double spmv_bytes(const gg_hmat *h, int precision, int m) {
   (void)precision;
   return (double)h->nnz * 12.0 + (double)(h->ncf + 1) * 8.0 + 3.0 * h->ncf * 8.0 * m;
@@ -510,6 +545,35 @@ double spmv_bytes(const gg_hmat *h, int precision, int m) {
 }  // namespace gg
 
 using namespace gg;
+
+extern "C" int gg_spmm_timing(gg_ctx *ctx, gg_hmat *h, int m, int iters, double *ms_per_launch,
+                              double *alg_bytes) {
+  if (!ctx || !h || h->ctx != ctx || iters < 1 || m < 1 || m > 16 || !ms_per_launch)
+    return fail(GG_ERR_ARG, "gg_spmm_timing: bad args");
+  if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_spmm_timing: EMT not set");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  GG_TRY(refresh_sym_values(h));
+  const int n = h->ncf, mp = (m + 1) & ~1;
+  DBuf<double> x, y;
+  DBuf<float2> xb;
+  GG_TRY(x.alloc((size_t)n * m));
+  GG_TRY(y.alloc((size_t)n * m));
+  GG_TRY(xb.alloc((size_t)n * mp));
+  std::vector<double> hx((size_t)n * m);
+  for (size_t i = 0; i < hx.size(); ++i) hx[i] = 1.0 / (1.0 + (double)(i % 97));
+  GG_CUDA(cudaMemcpyAsync(x.p, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  k_split_block<<<(unsigned)std::min<int64_t>(((int64_t)n * mp + 255) / 256, 4096), 256, 0, ctx->stream>>>(
+      x.p, n, m, mp, n, xb.p);
+  ::gg::note_launch();
+  GG_TRY(spmm_block(h, m, xb.p, x.p, y.p, n, nullptr, ctx->stream));  // warm-up
+  GG_TRY(timer_start(ctx));
+  for (int it = 0; it < iters; ++it) GG_TRY(spmm_block(h, m, xb.p, x.p, y.p, n, nullptr, ctx->stream));
+  double ms = 0;
+  GG_TRY(timer_stop(ctx, &ms));
+  *ms_per_launch = ms / iters;
+  if (alg_bytes) *alg_bytes = spmv_bytes(h, GG_SPLIT, m);
+  return GG_OK;
+}
 
 extern "C" int gg_matvec_timing(gg_ctx *ctx, gg_hmat *h, int precision, int iters, double *ms_per_launch,
                                 double *alg_bytes) {

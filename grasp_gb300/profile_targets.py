@@ -3,6 +3,7 @@ in profiles/. Each target builds the Fe XV workload once and runs only the
 kernel family it is named for, a few times:
 
   python -m grasp_gb300.profile_targets spmv     # 3 full-size y = H x launches per precision
+  python -m grasp_gb300.profile_targets spmm     # split Y = H X launches for 1 to 16 vectors
   python -m grasp_gb300.profile_targets solve    # one full MANEIG (split, MBLOCK = NVEC) (launch list)
   python -m grasp_gb300.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
   python -m grasp_gb300.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
@@ -34,6 +35,14 @@ def spmv():
     for prec in (FP64, SPLIT):
         ms, by = H.matvec_timing(prec, 3)
         print(f"precision {prec}: {ms * 1e3:.1f} us per launch, {by / 1e6:.1f} MB algorithmic")
+
+
+def spmm():
+    w, ctx, H = _fe15_context()
+    for m in (1, 2, 5, 10, 16):
+        ms, by = H.spmm_timing(m, 5)
+        print(f"split Y = H X, {m} vectors: {ms * 1e3:.1f} us per launch, {by / 1e6:.1f} MB algorithmic, "
+              f"{by / (ms * 1e-3) / 1e9:.0f} GB/s")
 
 
 def solve():
@@ -69,5 +78,5 @@ def batch(zs=None):
 
 
 if __name__ == "__main__":
-    {"spmv": spmv, "solve": solve, "rk": rk, "rk_split": rk_split, "batch": batch,
+    {"spmv": spmv, "spmm": spmm, "solve": solve, "rk": rk, "rk_split": rk_split, "batch": batch,
      "batch8": lambda: batch(zs=tuple(range(10, 18)))}[sys.argv[1]]()

@@ -247,7 +247,10 @@ double gg_stage_stat(gg_ctx *ctx, int which);
  * gg_event_record / gg_event_elapsed: CUDA events (8 slots) on the context
  * stream; elapsed synchronises on slot b.
  * gg_matvec_timing: average device time of one y = H x launch (after a
- * warm-up) over iters launches, and its algorithmic bytes.                  */
+ * warm-up) over iters launches, and its algorithmic bytes.
+ * gg_spmm_timing: the same for one split-precision Y = H X launch over m
+ * vectors (1 <= m <= 16; the Davidson block pass's matvec), algorithmic
+ * bytes = the matrix in the reference's storage once + 3 m NCF doubles.     */
 long long gg_launch_count(void);
 /* Page-locks (pins) caller memory so that uploads from it run at full link
  * rate; unregister before freeing it. */
@@ -256,6 +259,7 @@ int gg_host_unregister(void *p);
 int gg_event_record(gg_ctx *ctx, int slot);
 int gg_event_elapsed(gg_ctx *ctx, int a, int b, double *ms);
 int gg_matvec_timing(gg_ctx *ctx, gg_hmat *h, int precision, int iters, double *ms_per_launch, double *alg_bytes);
+int gg_spmm_timing(gg_ctx *ctx, gg_hmat *h, int m, int iters, double *ms_per_launch, double *alg_bytes);
 
 #ifdef __cplusplus
 }
