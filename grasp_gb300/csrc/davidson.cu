@@ -1056,8 +1056,8 @@ __global__ void __launch_bounds__(RT) k_bd_sub(double *__restrict__ B, int64_t l
 
 // kept orthonormal columns: B(:, kpass+c) = sum_q B_old(:, kpass+q) C[q][c],
 // c < bst[0], q < bst[1]; the last round also writes each kept column's hi + lo
-// FP32 copy for the block matvec (xs: interleaved by row, mp per row, zeros
-// beyond the kept columns) and into the split copy of the basis (xstore,
+// FP32 copy for the block matvec (xs: interleaved by row, mp = spmm_pitch(m)
+// per row, zeros beyond the kept columns) and into the split copy of the basis (xstore,
 // column kpass + c)
 template <int NP>
 __device__ __forceinline__ void bd_apply_rows(double *__restrict__ B, int64_t ld, int kpass, int nc,
@@ -1667,7 +1667,7 @@ struct Dvd {
         k_bd_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
       k_bd_chol<<<1, BD_RED, 0, s>>>(m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round);
       k_bd_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, (round == 1 && split) ? bxs.p : nullptr,
-                                     (m + 1) & ~1, Bx.p);
+                                     spmm_pitch(m), Bx.p);
       note_launches(3);
     }
     GG_CUDA(cudaGetLastError());

@@ -214,9 +214,13 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
 // xs: the split (hi + lo FP32) copy of x to read; null = the matrix's dXs
 int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
              const double *skip, cudaStream_t s, const float2 *xs = nullptr);
+// Row pitch (in float2) of the interleaved split copies of m vectors that the
+// block matvec reads: m rounded up to a power of two (at least 2), so that a
+// row is whole 16-byte pieces and never straddles a 128-byte line.
+__host__ __device__ constexpr int spmm_pitch(int m) { return m <= 2 ? 2 : m <= 4 ? 4 : m <= 8 ? 8 : 16; }
 // block form (SPLIT): columns kpass .. kpass+m-1, kpass = *dcol (0 when dcol is
 // null); xb holds their
-// hi + lo values interleaved by row (row j at xb + j (m rounded up to even))
+// hi + lo values interleaved by row (row j at xb + j spmm_pitch(m))
 int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,
                const int *dcol, cudaStream_t s);
 int spmm_cols(gg_hmat *h, const double *X, double *Y, int64_t ld, int m, cudaStream_t s);

@@ -267,15 +267,14 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
 }
 
 // Y = H X for the m new columns of a Davidson block pass in one sweep over
-// the matrix (SPLIT): X interleaved by row, xb[j MP + v] = hi + lo of
-// x_v[j] (MP = m rounded up to even: a row is MP / 2 16-byte pieces);
-// y_v = ABbase + (kpass + v) ld with kpass = *pc on the device (0 when pc is
-// null), the diagonal term from the FP64 x_v = Bbase + (kpass + v) ld.
-// One warp per row. A stored entry is taken by LPE = MP / 2 lanes, lane u
-// reading piece u of the gathered row (vectors 2u, 2u + 1), so that each
-// load instruction touches a few whole rows of xb instead of 32 scattered
-// ones; EPW = 32 / LPE entries per step. Products go into per-vector Dot2
-// sums (Ogita, Rump & Oishi), added over the EPW entry slots by a fixed
+// the matrix (SPLIT): X interleaved by row, xb[j MP + v] = hi + lo of x_v[j]
+// (MP = spmm_pitch(m)); y_v = ABbase + (kpass + v) ld with kpass = *pc on the
+// device (0 when pc is null), the diagonal term from the FP64
+// x_v = Bbase + (kpass + v) ld. One warp per row. A stored entry is taken by
+// LPE = ceil(m / 2) lanes, lane u reading piece u of the gathered row
+// (vectors 2u, 2u + 1), so that a load instruction touches EPW = 32 / LPE
+// whole rows of xb instead of 32 scattered ones. Products go into per-vector
+// Dot2 sums (Ogita, Rump & Oishi), added over the EPW entry slots by a fixed
 // shuffle tree in double-float.
 template <int M, typename CI>
 __global__ void __launch_bounds__(256) k_spmm_split(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
@@ -283,7 +282,7 @@ __global__ void __launch_bounds__(256) k_spmm_split(const int64_t *__restrict__ 
                                                     const float2 *__restrict__ xb, const double *__restrict__ diag,
                                                     const double *__restrict__ Bbase, double *__restrict__ ABbase,
                                                     int64_t ld, const int *__restrict__ pc, int n) {
-  constexpr int MP = (M + 1) & ~1, LPE = MP / 2, EPW = 32 / LPE;
+  constexpr int MP = spmm_pitch(M), LPE = (M + 1) / 2, EPW = 32 / LPE;
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (row >= n) return;
   const int e = lane / LPE, u = lane % LPE;
@@ -304,7 +303,7 @@ __global__ void __launch_bounds__(256) k_spmm_split(const int64_t *__restrict__ 
 #pragma unroll 4
     for (int64_t p = p0 + e; p < p1; p += EPW) {
       const float ah = __ldg(hi + p), al = __ldg(lo + p);
-      const float4 x = __ldg(xr + (size_t)__ldg(col + p) * LPE);
+      const float4 x = __ldg(xr + (size_t)__ldg(col + p) * (MP / 2));
       step(h0, l0, ah, al, x.x, x.y);
       if (2 * u + 1 < M) step(h1, l1, ah, al, x.z, x.w);
     }
@@ -529,7 +528,7 @@ int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double 
 // Y = H X for m columns (2 to 16) of leading dimension ld, SPLIT: the split
 // copies go to h->dXb, then one block sweep
 int spmm_cols(gg_hmat *h, const double *X, double *Y, int64_t ld, int m, cudaStream_t s) {
-  const int n = h->ncf, mp = (m + 1) & ~1;
+  const int n = h->ncf, mp = spmm_pitch(m);
   GG_TRY(h->dXb.alloc((size_t)n * mp));
   k_split_block<<<(unsigned)std::min<int64_t>(((int64_t)n * mp + 255) / 256, 4096), 256, 0, s>>>(X, ld, m, mp, n,
                                                                                                  h->dXb.p);
@@ -553,7 +552,7 @@ extern "C" int gg_spmm_timing(gg_ctx *ctx, gg_hmat *h, int m, int iters, double 
   if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_spmm_timing: EMT not set");
   GG_CUDA(cudaSetDevice(ctx->device));
   GG_TRY(refresh_sym_values(h));
-  const int n = h->ncf, mp = (m + 1) & ~1;
+  const int n = h->ncf, mp = spmm_pitch(m);
   DBuf<double> x, y;
   DBuf<float2> xb;
   GG_TRY(x.alloc((size_t)n * m));
