@@ -78,6 +78,7 @@ GPU_SYMBOLS = {
     "gg_event_elapsed": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _d]),
     "gg_matvec_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _d, _d]),
     "gg_spmm_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _d, _d]),
+    "gg_projected_eig": (C.c_int, [C.c_int, _d, C.c_int, C.c_int, _d, _d]),
 }
 
 SYNTH_SYMBOLS = {

@@ -269,6 +269,20 @@ def maneig_batched(ctx, hmats, nvec, precision=FP64, lim=0, maxiter=0, critr=0.0
     return out, dict(nloops=nl, nmv=nm, ierr=ie, status=st)
 
 
+def projected_eig(s, m, mvec=None):
+    """DVDSON's projected eigenproblem (DSPEVX on S, libdvd90/dvdson.f90:724)
+    on the host: the lowest ``m`` eigenvalues of the symmetric matrix ``s``
+    (its upper triangle is read) and the eigenvectors of the lowest ``mvec``."""
+    s = np.asarray(s, np.float64)
+    n = s.shape[0]
+    mvec = m if mvec is None else mvec
+    ap = np.concatenate([s[: j + 1, j] for j in range(n)]).astype(np.float64)
+    w = np.zeros(m)
+    z = np.zeros((max(mvec, 1), n))
+    check(_lib.gpu().gg_projected_eig(n, ptr(ap, _d), m, mvec, ptr(w, _d), ptr(z, _d)))
+    return w, z[:mvec].T.copy()
+
+
 def _lib_status(name):
     return {"GG_ERR_CONVERGE": -7}[name]
 

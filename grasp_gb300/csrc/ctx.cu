@@ -277,6 +277,15 @@ double gg_stage_stat(gg_ctx *ctx, int which) {
 
 long long gg_launch_count(void) { return g_launches.load(); }
 
+int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double *z) {
+  if (n < 1 || !ap || m < 1 || m > n || mvec < 0 || mvec > m || !w || (mvec > 0 && !z))
+    return fail(GG_ERR_ARG, "gg_projected_eig: bad arguments");
+  const int st = gg::sym_eig_lowest(n, ap, m, mvec, w, z);
+  if (st == -1) return fail(GG_ERR_ARG, "gg_projected_eig: bad arguments");
+  if (st != 0) return fail(GG_ERR_CONVERGE, "gg_projected_eig: eigenvalue search did not finish");
+  return GG_OK;
+}
+
 int gg_host_register(void *p, size_t bytes) {
   if (!p || bytes == 0) return fail(GG_ERR_ARG, "gg_host_register: bad arguments");
   GG_CUDA(cudaHostRegister(p, bytes, cudaHostRegisterDefault));

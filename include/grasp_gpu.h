@@ -242,6 +242,17 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * solve's total ms).                                                       */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
+/* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors
+ * also', 'In a range', 'Upper triangular', KPASS, S, ...) at
+ * libdvd90/dvdson.f90:724, on the host (no GPU): the lowest m eigenvalues
+ * (ascending) of the symmetric n x n matrix in packed upper storage
+ * ap[i + j(j+1)/2] = A(i, j), 0 <= i <= j < n, into w[m], and the eigenvectors
+ * of the lowest mvec <= m of them into z (n x mvec, column-major, unit norm,
+ * sign unspecified). The Davidson iteration calls the same routine once per
+ * pass. Returns GG_ERR_ARG for bad sizes, GG_ERR_CONVERGE if the
+ * eigenvalue search does not finish.                                       */
+int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double *z);
+
 /* ---- measurement helpers (no counterpart in the reference) ------------------
  * gg_launch_count: kernels this library has launched in this process.
  * gg_event_record / gg_event_elapsed: CUDA events (8 slots) on the context
