@@ -323,6 +323,24 @@ __global__ void k_eav(const int64_t *__restrict__ iendc, int ncf, double *__rest
   if (threadIdx.x == 0) *eav_out = eav;
 }
 
+// IROW checks of gg_hmat_create, one warp per row: each row ends with its
+// diagonal (IROW = row, 1-based) and its other entries lie in 1 .. row - 1.
+// bad = min over offending rows of (row << 2 | kind), kind 1 for a missing
+// diagonal, 2 for an entry outside the lower triangle.
+__global__ void k_check_irow(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow, int ncf,
+                             unsigned long long *__restrict__ bad) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (warp >= ncf) return;
+  const int i = warp + 1;
+  const int64_t p0 = iendc[warp], p1 = iendc[warp + 1];
+  int kind = 0;
+  if (lane == 0 && irow[p1 - 1] != i) kind = 1;
+  for (int64_t p = p0 + lane; p < p1 - 1; p += 32)
+    if (irow[p] < 1 || irow[p] >= i) kind = 2;
+  kind = __reduce_max_sync(0xffffffffu, kind);
+  if (lane == 0 && kind) atomicMin(bad, ((unsigned long long)i << 2) | (unsigned long long)kind);
+}
+
 template <class T> int upload(DBuf<T> &b, const T *h, size_t n, cudaStream_t s) {
   GG_TRY(b.alloc(n));
   if (n) GG_CUDA(cudaMemcpyAsync(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice, s));
@@ -358,13 +376,8 @@ int gg_hmat_create(gg_ctx *ctx, int ncf, int64_t nnz, const int64_t *iendc, cons
   if (!ctx || !out || !iendc || !irow || ncf < 1 || nnz < ncf) return fail(GG_ERR_ARG, "gg_hmat_create: bad arguments");
   *out = nullptr;
   if (iendc[0] != 0 || iendc[ncf] != nnz) return fail(GG_ERR_ARG, "gg_hmat_create: IENDC(0) must be 0, IENDC(NCF) = NNZ");
-  for (int i = 1; i <= ncf; ++i) {
+  for (int i = 1; i <= ncf; ++i)
     if (iendc[i] <= iendc[i - 1]) return fail(GG_ERR_ARG, "gg_hmat_create: empty row (the diagonal is required)");
-    // diagonal last in each row (lower-triangle-by-rows mode, spicmv2.f90)
-    if (irow[iendc[i] - 1] != i) return fail(GG_ERR_ARG, "gg_hmat_create: row does not end with its diagonal");
-    for (int64_t p = iendc[i - 1]; p < iendc[i] - 1; ++p)
-      if (irow[p] < 1 || irow[p] >= i) return fail(GG_ERR_ARG, "gg_hmat_create: IROW outside the lower triangle");
-  }
   GG_CUDA(cudaSetDevice(ctx->device));
   gg_hmat *h = new gg_hmat;
   h->ctx = ctx;
@@ -375,7 +388,22 @@ int gg_hmat_create(gg_ctx *ctx, int ncf, int64_t nnz, const int64_t *iendc, cons
   if (s == GG_OK) s = upload(h->dIrow, irow, (size_t)nnz, ctx->stream);
   if (s == GG_OK) s = h->dEmt.alloc(nnz);
   if (s == GG_OK) s = h->dDiag.alloc(ncf);
-  if (s == GG_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess) s = fail(GG_ERR_CUDA, "gg_hmat_create: copy failed");
+  // IROW checked on the device (diagonal last in each row: the
+  // lower-triangle-by-rows mode of spicmv2.f90), the verdict read back here
+  DBuf<unsigned long long> dbad;
+  unsigned long long hbad[1] = {~0ull};
+  if (s == GG_OK) s = upload(dbad, hbad, 1, ctx->stream);
+  if (s == GG_OK) {
+    k_check_irow<<<(unsigned)(((int64_t)ncf * 32 + 255) / 256), 256, 0, ctx->stream>>>(h->dIendc.p, h->dIrow.p, ncf,
+                                                                                       dbad.p);
+    ::gg::note_launch();
+    if (cudaMemcpyAsync(hbad, dbad.p, sizeof(hbad), cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+      s = fail(GG_ERR_CUDA, "gg_hmat_create: copy failed");
+  }
+  if (s == GG_OK && hbad[0] != ~0ull)
+    s = fail(GG_ERR_ARG, (hbad[0] & 3) == 1 ? "gg_hmat_create: row does not end with its diagonal"
+                                            : "gg_hmat_create: IROW outside the lower triangle");
   if (s != GG_OK) {
     delete h;
     return s;

@@ -27,25 +27,28 @@
 namespace gg {
 namespace {
 
-constexpr int NCHUNK = 128;
+constexpr int NCHUNK = 1024;  // most row chunks of the symmetric structure build
 
 // counts of transposed entries per (chunk, column)
+// per chunk of rows, how many of its stored entries fall in each column c
+// (entries above the diagonal of the symmetric matrix); warps take rows
 __global__ void k_tcount(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow,
                          const int *__restrict__ chunk_r0, int ncf, int *__restrict__ cnt) {
   const int ch = blockIdx.x;
   const int r0 = chunk_r0[ch], r1 = chunk_r0[ch + 1];
   int *c = cnt + (size_t)ch * ncf;
-  for (int r = r0; r < r1; ++r) {
+  const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int r = r0 + (threadIdx.x >> 5); r < r1; r += nw) {
     const int64_t lo = iendc[r], hi = iendc[r + 1] - 1;  // last entry is the diagonal
-    for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) atomicAdd(&c[irow[p] - 1], 1);
+    for (int64_t p = lo + lane; p < hi; p += 32) atomicAdd(&c[irow[p] - 1], 1);
   }
 }
 
 // cursor(chunk, col) = start of col's transposed part + entries of earlier chunks
-__global__ void k_cursor(const int *__restrict__ cnt, int ncf, int nch, const int64_t *__restrict__ symptr,
-                         const int64_t *__restrict__ iendc, int64_t *__restrict__ cursor) {
+__global__ void k_cursor(const int *__restrict__ cnt, int ncf, int nch, const int64_t *__restrict__ iendc,
+                         int *__restrict__ cursor) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncf; c += gridDim.x * blockDim.x) {
-    int64_t pos = symptr[c] + (iendc[c + 1] - iendc[c]);
+    int pos = (int)(iendc[c + 1] - iendc[c]);  // the row's own entries come first
     for (int ch = 0; ch < nch; ++ch) {
       cursor[(size_t)ch * ncf + c] = pos;
       pos += cnt[(size_t)ch * ncf + c];
@@ -64,18 +67,22 @@ __global__ void k_tcol_total(const int *__restrict__ cnt, int ncf, int nch, cons
 
 // transposed placement: rows of a chunk in order; within one row the columns
 // are distinct, so the cursors need no atomics
+// rows of a chunk in order, the entries of a row in parallel (distinct
+// columns): entry (r, c) goes to row c at symptr[c] + cur[c], so each row's
+// entries from other rows ascend in r; cursor holds offsets within the row
 __global__ void k_tplace(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow,
-                         const int *__restrict__ chunk_r0, int ncf, int64_t *__restrict__ cursor,
-                         int32_t *__restrict__ scol, int64_t *__restrict__ ssrc) {
+                         const int *__restrict__ chunk_r0, int ncf, const int64_t *__restrict__ symptr,
+                         int *__restrict__ cursor, int32_t *__restrict__ scol, int64_t *__restrict__ ssrc) {
   const int ch = blockIdx.x;
   const int r0 = chunk_r0[ch], r1 = chunk_r0[ch + 1];
-  int64_t *cur = cursor + (size_t)ch * ncf;
+  int *cur = cursor + (size_t)ch * ncf;
   for (int r = r0; r < r1; ++r) {
     const int64_t lo = iendc[r], hi = iendc[r + 1] - 1;
     for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
       const int c = irow[p] - 1;
-      const int64_t pos = cur[c];
-      cur[c] = pos + 1;
+      const int q = cur[c];
+      cur[c] = q + 1;
+      const int64_t pos = symptr[c] + q;
       scol[pos] = r;
       ssrc[pos] = p;
     }
@@ -389,21 +396,25 @@ int build_sym(gg_hmat *h) {
   gg_ctx *ctx = h->ctx;
   cudaStream_t s = ctx->stream;
   const int ncf = h->ncf;
-  // row chunks balanced by stored entries
-  const int nch = std::min(NCHUNK, ncf);
+  // row chunks balanced by work: about one per 32 rows, at most NCHUNK and
+  // as many as the per-chunk count and cursor arrays (8 bytes per chunk and
+  // row) allow within 512 MB; k_tplace walks each chunk's rows in order
+  const int nch = (int)std::max<int64_t>(
+      1, std::min<int64_t>({(int64_t)ncf / 32, (int64_t)NCHUNK, std::max<int64_t>(128, (512ll << 20) / (8ll * ncf))}));
   std::vector<int> r0(nch + 1, ncf);
   r0[0] = 0;
   {
-    const double per = (double)h->nnz / nch;
+    // a row costs its entries plus a block-wide step (256 entries' worth)
+    const double per = ((double)h->nnz + 256.0 * ncf) / nch;
     int c = 1;
     for (int r = 0; r < ncf && c < nch; ++r)
-      if ((double)h->hIendc[r + 1] >= per * c) r0[c++] = r + 1;
+      if ((double)h->hIendc[r + 1] + 256.0 * (r + 1) >= per * c) r0[c++] = r + 1;
     for (; c < nch; ++c) r0[c] = ncf;
     r0[nch] = ncf;
     for (int i = 1; i <= nch; ++i) r0[i] = std::max(r0[i], r0[i - 1]);
   }
-  DBuf<int> dr0, cnt;
-  DBuf<int64_t> rowlen, cursor;
+  DBuf<int> dr0, cnt, cursor;
+  DBuf<int64_t> rowlen;
   GG_TRY(dr0.alloc(nch + 1));
   GG_CUDA(cudaMemcpyAsync(dr0.p, r0.data(), (nch + 1) * sizeof(int), cudaMemcpyHostToDevice, s));
   GG_TRY(cnt.alloc((size_t)nch * ncf));
@@ -423,9 +434,10 @@ int build_sym(gg_hmat *h) {
   GG_TRY(h->dSymCol.alloc(total));
   GG_TRY(h->dSymSrc.alloc(total));
   GG_TRY(cursor.alloc((size_t)nch * ncf));
-  k_cursor<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dSymPtr.p, h->dIendc.p, cursor.p); ::gg::note_launch();
+  k_cursor<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dIendc.p, cursor.p); ::gg::note_launch();
   k_own<<<(ncf * 32 + 255) / 256, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, ncf, h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p); ::gg::note_launch();
-  k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, cursor.p, h->dSymCol.p, h->dSymSrc.p); ::gg::note_launch();
+  k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, h->dSymPtr.p, cursor.p, h->dSymCol.p,
+                               h->dSymSrc.p); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   if (ncf <= 65536) {
     GG_TRY(h->dSymCol16.alloc(h->sym_nnz));

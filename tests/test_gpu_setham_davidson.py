@@ -59,6 +59,29 @@ def test_setham_bad_label_is_an_error(gpu_ready):
         H.setham(blk.iq, t, blk.vlists)
 
 
+def test_hmat_bad_structure_is_an_error(gpu_ready):
+    """IENDC / IROW outside the lower-triangle-by-rows mode of spicmv2.f90
+    (checked on the device for IROW): the matrix is refused."""
+    from grasp_gb300 import Context, GGError, HMatrix
+    orbs, blk = ne7_block()
+    ctx = Context(0)
+    HMatrix(ctx, blk.ncf, blk.iendc, blk.irow).close()  # the real structure is accepted
+    r = blk.iendc[5] - 1                                 # diagonal of row 5 (1-based)
+    irow = blk.irow.copy()
+    irow[r] = 3
+    with pytest.raises(GGError, match="diagonal"):
+        HMatrix(ctx, blk.ncf, blk.iendc, irow)
+    irow = blk.irow.copy()
+    row = int(np.argmax(np.diff(blk.iendc) > 1)) + 1     # a row with an off-diagonal entry
+    irow[blk.iendc[row - 1]] = row + 1                   # above the diagonal
+    with pytest.raises(GGError, match="lower triangle"):
+        HMatrix(ctx, blk.ncf, blk.iendc, irow)
+    iendc = blk.iendc.copy()
+    iendc[3] = iendc[2]                                  # an empty row
+    with pytest.raises(GGError):
+        HMatrix(ctx, blk.ncf, iendc, blk.irow)
+
+
 def test_spicmv2_parity(gpu_ready, oracle_mod):
     o, ctx, H, blk, oracle = _setup()
     H.setham(blk.iq, blk.tlist, blk.vlists)
