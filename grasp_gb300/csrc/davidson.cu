@@ -1368,6 +1368,9 @@ struct Dvd {
   DBuf<int> bst;
   DBuf<float2> bxs;
   int bd_G = 0, bd_Y = 1, bd_cpc = 0, bd_ps = 0;
+  int full_m = 0;                 // MBLOCK: block matvecs over this many columns are timed apart
+  double spmm_full_ms = 0;
+  int spmm_full_n = 0;
   // SPLIT: hi + lo copies of the basis and its products (split-precision
   // block kernels); columns [0, bx_cols) of both are current
   DBuf<float2> Bx, ABx;
@@ -1785,6 +1788,10 @@ struct Dvd {
       float ms = 0.f;
       GG_CUDA(cudaEventElapsedTime(&ms, bev[2 * v], bev[2 * v + 1]));
       mv_ms += ms;
+      if (use_x() && m == full_m) {
+        spmm_full_ms += ms;
+        ++spmm_full_n;
+      }
     }
     nmv += nk;
     mv_count += nk;
@@ -2115,6 +2122,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
     EIGVAL[i] = 1.0e30;
     ICV[i + 1] = 0;
   }
+  D.full_m = MBLOCK;
   int KPASS = NIV, NNCV = KPASS;
   int REST = std::max(LIM / 2, 2 * NUME);
   REST = std::min(REST, LIM - 3);
@@ -2557,6 +2565,8 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   ctx->stats[17] = 1e3 * D1.t_total;
   ctx->stats[18] = 1e3 * D2.t_total;
   ctx->stats[19] = 1e3 * D2.t_eig;
+  ctx->stats[23] = D2.spmm_full_ms;
+  ctx->stats[24] = D2.spmm_full_n;
   *nloops = nl_total;
   *nmv = nmv_total;
   if (*ierr & 2048) return fail(GG_ERR_CONVERGE, "DVDSON: maximum number of iterations reached (IERR 2048)");

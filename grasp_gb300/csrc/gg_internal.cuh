@@ -161,7 +161,7 @@ struct gg_ctx {
   gg::RkTable rk;
   gg::DBuf<double> dIab;                // [nw * nw]
   bool iab_valid = false;
-  double stats[24] = {};
+  double stats[26] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t marks[8] = {};  // gg_event_record slots
 };

@@ -239,7 +239,8 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * table entries the last genintrk evaluated with the general QUAD (head
  * index above 2), 21 iterations of the last gg_maneig_batched (all blocks
  * together), 22 kernels per batched iteration (stage 3 is the batched
- * solve's total ms).                                                       */
+ * solve's total ms), 23 / 24 device ms / number of the full-block block
+ * matvecs (split SpMM) over MBLOCK columns of the last gg_maneig.         */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors
