@@ -446,6 +446,75 @@ __global__ void k_precond_multi(double *__restrict__ B, const double *__restrict
   diag[i] = dg;
 }
 
+// NEWVEC's choices for a block pass (dvdson.f90:1002-1172) on the device, so
+// that the Ritz sweep, the preconditioners and the block pass follow each
+// other without a host round trip. Inputs per candidate target t (in
+// TSTSEL's order): its eigenvalue, GAP and DL (from EIGVAL and OLDVAL on the
+// host); rn2[t] = |r_t|^2 from the Ritz sweep. Same decisions in the same
+// order as the reference: a target with |r| < CRITR converges (DONE when all
+// have), the others are kept with RHSEPS = sqrt(DL |r|) when GAP > |r| and
+// min(DL, sqrt(DL)) otherwise, up to LIMADD - KPASS of them.
+struct NvIn {
+  int nt, kpass, limadd;
+  double critr;
+  double lam[MT_MAX], gap[MT_MAX], dl[MT_MAX];
+};
+struct NvOut {
+  int nadded, done;
+  double res[MT_MAX];
+};
+__global__ void k_newvec(const NvIn *__restrict__ in, const double *__restrict__ rn2, PrecList *__restrict__ L,
+                         NvOut *__restrict__ out) {
+  if (threadIdx.x != 0) return;
+  PrecList l;
+  l.m = 0;
+  int icvc = 0, nadded = 0, done = 0;
+  const int nt = in->nt;
+  for (int i = 0; i < nt; ++i) {
+    const double res = sqrt(rn2[i]);
+    out->res[i] = res;
+    if (res < in->critr) {
+      ++icvc;
+      if (icvc < nt) continue;
+      done = 1;
+      break;
+    }
+    ++nadded;
+    const double gap = in->gap[i], dl = in->dl[i];
+    l.col[l.m] = in->kpass + nadded - 1;
+    l.t[l.m] = i;
+    l.lam[l.m] = in->lam[i];
+    l.rhs[l.m] = (gap > res) ? sqrt(dl * res) : fmin(dl, sqrt(dl));
+    ++l.m;
+    if (nadded + in->kpass == in->limadd) break;
+  }
+  *L = l;
+  out->nadded = nadded;
+  out->done = done;
+}
+
+// k_precond_multi with the kept targets read from device memory; columns
+// kpass + L.m .. kpass + mg - 1 of the pass are zeroed (the block pass then
+// drops them)
+__global__ void k_precond_dev(double *__restrict__ B, const double *__restrict__ T, int64_t ld,
+                              const PrecList *__restrict__ Lp, double *__restrict__ diag, int n, int mg, int kpass) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int m = Lp->m;
+  double dg = diag[i];
+  for (int q = 0; q < m; ++q) {
+    const int t = Lp->t[q];
+    const double b = T[(size_t)(2 * t) * ld + i], r = T[(size_t)(2 * t + 1) * ld + i];
+    const double rr = fma(-Lp->rhs[q], b, r);
+    const double lam = Lp->lam[q];
+    const double d = dg - lam;
+    B[(size_t)Lp->col[q] * ld + i] = (fabs(d) > 1.0e-06) ? rr / d : rr * 1.0e06;
+    dg = d + lam;
+  }
+  diag[i] = dg;
+  for (int q = m; q < mg; ++q) B[(size_t)(kpass + q) * ld + i] = 0.0;
+}
+
 // column c <- scal[fslot] * column c; with xs, also its hi+lo split for the matvec
 __global__ void k_cscale(double *X, int64_t ld, PSrc ps, const double *skip, const double *__restrict__ scal,
                          int fslot, int n, float2 *__restrict__ xs) {
@@ -1395,6 +1464,9 @@ struct Dvd {
   std::vector<cudaGraphExec_t> bexec;
   std::vector<int> bkernels;
   bool use_graph = true;          // GRASP_GPU_DVD_GRAPH=0 launches the same pass kernel by kernel
+  // block passes with NEWVEC's choices on the device (GRASP_GPU_DVD_FUSED=0:
+  // on the host, with a wait for the residual norms)
+  bool use_fused = true;
   // single-vector pass as one cooperative kernel with grid barriers
   // (GRASP_GPU_DVD_PASS=persistent). Off by default: on GB300 the separate
   // kernels run at full occupancy and finish the pass sooner.
@@ -1449,6 +1521,8 @@ struct Dvd {
     if (precision == GG_SPLIT) GG_TRY(h->dXs.alloc(n));
     const char *e = std::getenv("GRASP_GPU_DVD_GRAPH");
     use_graph = !(e && e[0] == '0');
+    const char *ef = std::getenv("GRASP_GPU_DVD_FUSED");
+    use_fused = !(ef && ef[0] == '0');
     const char *e2 = std::getenv("GRASP_GPU_DVD_PASS");
     use_pass = (e2 && std::strcmp(e2, "persistent") == 0);
     if (use_pass) {
@@ -1521,6 +1595,8 @@ struct Dvd {
       if (e) cudaGraphExecDestroy(e);
     if (hpv) cudaFreeHost(hpv);
     if (hbst) cudaFreeHost(hbst);
+    if (hnv_in) cudaFreeHost(hnv_in);
+    if (hnv_out) cudaFreeHost(hnv_out);
     if (graph) cudaGraphDestroy(graph);
     if (gev0) cudaEventDestroy(gev0);
     for (auto e : bev)
@@ -1958,6 +2034,18 @@ struct Dvd {
   // vectors svec[t], length k; eigenvalues lam[t]) in one sweep; rn2[t] = |r_t|^2
   bool ritz_multi_fits(int k, int nt) const { return nt <= MT_MAX && nt * k <= MT_SMEM && 2 * nt <= lim; }
   int ritz_multi(int k, int nt, const double *const *svec, const double *lam, double *rn2) {
+    GG_TRY(launch_ritz_multi(k, nt, svec, lam));
+    double *hl = hmt + (size_t)MT_MAX * lim;
+    double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
+    GG_CUDA(cudaMemcpyAsync(hl + MT_MAX, drn, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
+    const auto t0 = std::chrono::steady_clock::now();
+    GG_CUDA(cudaStreamSynchronize(s));
+    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    for (int t = 0; t < nt; ++t) rn2[t] = hl[MT_MAX + t];
+    return GG_OK;
+  }
+  // the Ritz sweep (residual norms |r_t|^2 left on the device)
+  int launch_ritz_multi(int k, int nt, const double *const *svec, const double *lam) {
     for (int t = 0; t < nt; ++t) std::memcpy(hmt + (size_t)t * k, svec[t], k * sizeof(double));
     double *hl = hmt + (size_t)MT_MAX * lim;
     for (int t = 0; t < nt; ++t) hl[t] = lam[t];
@@ -1997,11 +2085,39 @@ struct Dvd {
     }
     note_launch();
     GG_CUDA(cudaGetLastError());
-    GG_CUDA(cudaMemcpyAsync(hl + MT_MAX, drn, nt * sizeof(double), cudaMemcpyDeviceToHost, s));
-    const auto t0 = std::chrono::steady_clock::now();
-    GG_CUDA(cudaStreamSynchronize(s));
-    t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    for (int t = 0; t < nt; ++t) rn2[t] = hl[MT_MAX + t];
+    return GG_OK;
+  }
+  // One block pass with NEWVEC's choices made on the device: Ritz sweep of
+  // the nt candidates, k_newvec, preconditioners of the kept ones (the rest
+  // of the mg columns zeroed), the block pass graph over mg columns. One
+  // host wait, at the end. *nk = columns added, *done = all candidates
+  // converged (nothing added).
+  DBuf<NvIn> dnv_in;
+  DBuf<NvOut> dnv_out;
+  DBuf<PrecList> dL;
+  NvIn *hnv_in = nullptr;
+  NvOut *hnv_out = nullptr;
+  int pass_fused(int k, int nt, const double *const *svec, const NvIn &in, int mg, std::vector<double> &S, int *nk,
+                 bool *done) {
+    if (!hnv_in) {
+      GG_TRY(dnv_in.alloc(1));
+      GG_TRY(dnv_out.alloc(1));
+      GG_TRY(dL.alloc(1));
+      GG_CUDA(cudaMallocHost(&hnv_in, sizeof(NvIn)));
+      GG_CUDA(cudaMallocHost(&hnv_out, sizeof(NvOut)));
+    }
+    *hnv_in = in;
+    GG_CUDA(cudaMemcpyAsync(dnv_in.p, hnv_in, sizeof(NvIn), cudaMemcpyHostToDevice, s));
+    GG_TRY(launch_ritz_multi(k, nt, svec, in.lam));
+    const double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
+    k_newvec<<<1, 32, 0, s>>>(dnv_in.p, drn, dL.p, dnv_out.p);
+    k_precond_dev<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(B.p, T.p, ld, dL.p, diag.p, n, mg, k);
+    note_launches(2);
+    GG_CUDA(cudaGetLastError());
+    GG_CUDA(cudaMemcpyAsync(hnv_out, dnv_out.p, sizeof(NvOut), cudaMemcpyDeviceToHost, s));
+    GG_TRY(block_pass(k, mg, S, nk));  // waits for the stream
+    *done = hnv_out->done != 0;
+    if (*nk > hnv_out->nadded) return fail(GG_ERR_STATE, "block pass: more columns kept than added");
     return GG_OK;
   }
   int precond_multi(const PrecList &L) {
@@ -2260,6 +2376,40 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
       }
       if (DONE) break;
       NNCV = nadded;
+      KPASS += NNCV;
+      ++NLOOPS;
+      if (NLOOPS <= MAXITER) continue;
+      IERR += 2048;
+      --NLOOPS;
+      KPASS -= NNCV;
+      break;
+    }
+    if (D.use_fused && NNCV <= MT_MAX && D.ritz_multi_fits(KPASS, NNCV)) {
+      // NEWVEC on the device: Ritz sweep, choices, preconditioners and the
+      // block pass back to back, one host wait
+      const int limadd = std::min(LIM, MBLOCK + KPASS);
+      const int mg = std::min(NNCV, limadd - KPASS);
+      NvIn in{};
+      in.nt = NNCV;
+      in.kpass = KPASS;
+      in.limadd = limadd;
+      in.critr = P.critr;
+      std::vector<const double *> sv(NNCV);
+      for (int t = 0; t < NNCV; ++t) {
+        const int indx = INCV[t + 1];
+        sv[t] = SVEC.data() + (size_t)(indx - 1) * KPASS;
+        in.lam[t] = EIGVAL[indx - 1];
+        gap_dl(indx, &in.gap[t], &in.dl[t]);
+      }
+      int nk = 0;
+      bool done = false;
+      GG_TRY(D.pass_fused(KPASS, NNCV, sv.data(), in, mg, S, &nk, &done));
+      if (done) {
+        DONE = true;
+        break;
+      }
+      if (nk == 0) break;  // no direction outside the basis is left
+      NNCV = nk;
       KPASS += NNCV;
       ++NLOOPS;
       if (NLOOPS <= MAXITER) continue;

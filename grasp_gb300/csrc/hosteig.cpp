@@ -258,16 +258,40 @@ bool tri_lowest(int n, const std::vector<double> &d, const std::vector<double> &
   return true;
 }
 
-void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector<double>> &orth, unsigned seed,
-              double tnorm) {
+// Inverse iteration for one eigenvalue lam of T (Golub & Van Loan 8.2.2,
+// with LAPACK DSTEIN's stopping rule): LU of T - lam I with partial pivoting,
+// then solves from a fixed pseudo-random start, each followed by
+// orthogonalisation against the earlier vectors of the same cluster (the
+// n-long rows of orth, north of them) and normalisation. It stops two
+// solves after the growth |y| of a solve first reached 1 / (10 n eps
+// tnorm) (the normalised vector then has a residual at rounding level), and
+// after four solves at most.
+struct InvWork {
+  std::vector<double> u0, u1, u2, l, r0;
+  std::vector<char> piv;
+  void size(int n) {
+    if ((int)u0.size() >= n) return;
+    u0.resize(n);
+    u1.resize(n);
+    u2.resize(n);
+    l.resize(n);
+    r0.resize(n);
+    piv.resize(n);
+  }
+};
+
+void inv_iter(const Tri &T, double lam, double *x, const double *orth, int north, unsigned seed, double tnorm,
+              InvWork &W) {
   const int n = T.n;
   if (n == 1) {
     x[0] = 1.0;
     return;
   }
-  const double tiny = 2.220446049250313e-16 * std::max(tnorm, 1e-300);
-  std::vector<double> u0(n), u1(n), u2(n), l(n);
-  std::vector<char> piv(n);
+  const double eps = 2.220446049250313e-16;
+  const double tiny = eps * std::max(tnorm, 1e-300);
+  W.size(n);
+  double *u0 = W.u0.data(), *u1 = W.u1.data(), *u2 = W.u2.data(), *l = W.l.data(), *r0 = W.r0.data();
+  char *piv = W.piv.data();
   double a0 = T.d[0] - lam, a1 = T.e[0];
   for (int i = 0; i < n; ++i) {
     double sub = 0, b0 = 0, b1 = 0;
@@ -298,6 +322,11 @@ void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector
       a1 = b1;
     }
   }
+  for (int i = 0; i < n; ++i) {
+    double d = u0[i];
+    if (std::fabs(d) < tiny) d = d < 0 ? -tiny : tiny;
+    r0[i] = 1.0 / d;
+  }
   unsigned s = 2463534242u ^ (seed * 2654435761u);
   for (int i = 0; i < n; ++i) {
     s ^= s << 13;
@@ -305,6 +334,14 @@ void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector
     s ^= s << 5;
     x[i] = (double)(s & 0xffff) / 65536.0 - 0.5 + 1e-3;
   }
+  {  // start with unit norm, so that the growth of the first solve is |y|
+    double nrm = 0.0;
+    for (int i = 0; i < n; ++i) nrm += x[i] * x[i];
+    const double inv = 1.0 / std::sqrt(nrm);
+    for (int i = 0; i < n; ++i) x[i] *= inv;
+  }
+  const double grown = 1.0 / (10.0 * n * eps * std::max(tnorm, 1e-300));
+  int extra = -1;
   for (int it = 0; it < 4; ++it) {
     for (int i = 0; i + 1 < n; ++i) {
       if (piv[i]) std::swap(x[i], x[i + 1]);
@@ -314,21 +351,25 @@ void inv_iter(const Tri &T, double lam, double *x, const std::vector<std::vector
       double v = x[i];
       if (i + 1 < n) v -= u1[i] * x[i + 1];
       if (i + 2 < n) v -= u2[i] * x[i + 2];
-      double d = u0[i];
-      if (std::fabs(d) < tiny) d = d < 0 ? -tiny : tiny;
-      x[i] = v / d;
-    }
-    for (const auto &q : orth) {
-      double dot = 0.0;
-      for (int i = 0; i < n; ++i) dot += q[i] * x[i];
-      for (int i = 0; i < n; ++i) x[i] -= dot * q[i];
+      x[i] = v * r0[i];
     }
     double nrm = 0.0;
+    for (int i = 0; i < n; ++i) nrm += x[i] * x[i];
+    const double growth = std::sqrt(nrm);
+    for (int q = 0; q < north; ++q) {
+      const double *oq = orth + (size_t)q * n;
+      double dot = 0.0;
+      for (int i = 0; i < n; ++i) dot += oq[i] * x[i];
+      for (int i = 0; i < n; ++i) x[i] -= dot * oq[i];
+    }
+    nrm = 0.0;
     for (int i = 0; i < n; ++i) nrm += x[i] * x[i];
     nrm = std::sqrt(nrm);
     if (nrm == 0.0) nrm = 1.0;
     const double inv = 1.0 / nrm;
     for (int i = 0; i < n; ++i) x[i] *= inv;
+    if (extra < 0 && growth >= grown) extra = 1;  // one more solve after the first large growth
+    else if (extra > 0 && --extra == 0) break;
   }
 }
 
@@ -363,7 +404,10 @@ int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *
     tnorm = std::max(tnorm, std::fabs(T.d[i]) + (i > 0 ? std::fabs(T.e[i - 1]) : 0.0) +
                                 (i + 1 < n ? std::fabs(T.e[i]) : 0.0));
   const double ortol = 1e-3 * tnorm, eps = 2.220446049250313e-16;
-  std::vector<std::vector<double>> cluster;
+  // vectors of the current cluster, n-long rows
+  std::vector<double> cluster((size_t)n * std::max(mvec, 1));
+  int ncl = 0;
+  InvWork work;
   std::vector<double> x(n);
   // eigenvectors of T, row-major [n][mvec] so that the back-transformation
   // below runs all vectors together
@@ -372,10 +416,11 @@ int sym_eig_lowest(int n, const double *ap, int m, int mvec, double *w, double *
   for (int j = 0; j < m; ++j) w[j] = ev[j];
   for (int j = 0; j < mvec; ++j) {
     double lam = ev[j];
-    if (j > 0 && lam - prev > ortol) cluster.clear();
+    if (j > 0 && lam - prev > ortol) ncl = 0;
     if (j > 0 && lam - prev < 10.0 * eps * std::fabs(lam)) lam = prev + 10.0 * eps * std::fabs(lam);
-    inv_iter(T, lam, x.data(), cluster, (unsigned)j + 1u, tnorm);
-    cluster.push_back(x);
+    inv_iter(T, lam, x.data(), cluster.data(), ncl, (unsigned)j + 1u, tnorm, work);
+    std::copy(x.begin(), x.end(), cluster.begin() + (size_t)ncl * n);
+    ++ncl;
     prev = lam;
     for (int i = 0; i < n; ++i) Y[(size_t)i * mvec + j] = x[i];
   }

@@ -187,6 +187,39 @@ def test_maneig_graph_pass_matches_launch_path(gpu_ready, monkeypatch):
             assert np.array_equal(vec, vec0)
 
 
+def test_block_pass_device_newvec_matches_host(gpu_ready, monkeypatch):
+    """Block passes with NEWVEC's choices made on the device (one host wait
+    per pass) and on the host (a wait for the residual norms) give the same
+    eigenpairs; the graph and launch-by-launch forms of the fused pass are
+    bit-identical."""
+    from grasp_gb300 import Context, HMatrix
+    from grasp_gb300 import synth as S
+    orbs = S.orbital_set(6, 3)
+    case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
+    occ = lambda d: S.occupation(orbs, d)  # noqa: E731
+    refs = [occ({(1, -1): 2, (2, -1): 2}), occ({(1, -1): 2, (2, 1): 2}), occ({(1, -1): 2, (2, -2): 2})]
+    blk = S.ci_block(orbs, refs, [0] * len(orbs), two_j=2, parity=0, density=0.05, seed=9)
+    ctx = Context(0)
+    ctx.set_grid(case["n"], case["rnt"], case["h"], case["c"], case["zz"])
+    ob = case["orb"]
+    ctx.set_orbitals(ob.nak, ob.mf, ob.pf, ob.qf)
+    ctx.genintrk()
+    ctx.iabint_table()
+    H = HMatrix(ctx, blk.ncf, blk.iendc, blk.irow)
+    H.setham(blk.iq, blk.tlist, blk.vlists)
+    for precision in (0, 1):
+        monkeypatch.setenv("GRASP_GPU_DVD_FUSED", "0")
+        ev0, vec0, _ = H.maneig(4, flavour=0, precision=precision, mblock=4, robust=True)
+        monkeypatch.setenv("GRASP_GPU_DVD_FUSED", "1")
+        ev1, vec1, _ = H.maneig(4, flavour=0, precision=precision, mblock=4, robust=True)
+        monkeypatch.setenv("GRASP_GPU_DVD_GRAPH", "0")
+        ev2, vec2, _ = H.maneig(4, flavour=0, precision=precision, mblock=4, robust=True)
+        monkeypatch.delenv("GRASP_GPU_DVD_GRAPH")
+        assert np.abs(ev1 - ev0).max() <= 1e-11, (precision, ev0, ev1)
+        assert np.abs(vec1 - vec0).max() <= 1e-8
+        assert np.array_equal(ev1, ev2) and np.array_equal(vec1, vec2)
+
+
 @pytest.mark.parametrize("env", [("GRASP_GPU_DVD_PASS", "persistent"), ("GRASP_GPU_MATVEC", "ltile")])
 def test_maneig_alternative_kernels(gpu_ready, oracle_mod, monkeypatch, env):
     """The opt-in kernels (the single-vector pass as one cooperative kernel;
