@@ -465,14 +465,22 @@ struct NvOut {
 };
 __global__ void k_newvec(const NvIn *__restrict__ in, const double *__restrict__ rn2, PrecList *__restrict__ L,
                          NvOut *__restrict__ out) {
-  if (threadIdx.x != 0) return;
+  // the square roots in parallel (lane t), the choices by lane 0 in order
+  __shared__ double sres[MT_MAX], srhs[MT_MAX];
+  const int nt = in->nt, t = threadIdx.x;
+  if (t < nt) {
+    const double res = sqrt(rn2[t]), gap = in->gap[t], dl = in->dl[t];
+    sres[t] = res;
+    out->res[t] = res;
+    srhs[t] = (gap > res) ? sqrt(dl * res) : fmin(dl, sqrt(dl));
+  }
+  __syncthreads();
+  if (t != 0) return;
   PrecList l;
   l.m = 0;
   int icvc = 0, nadded = 0, done = 0;
-  const int nt = in->nt;
   for (int i = 0; i < nt; ++i) {
-    const double res = sqrt(rn2[i]);
-    out->res[i] = res;
+    const double res = sres[i];
     if (res < in->critr) {
       ++icvc;
       if (icvc < nt) continue;
@@ -480,11 +488,10 @@ __global__ void k_newvec(const NvIn *__restrict__ in, const double *__restrict__
       break;
     }
     ++nadded;
-    const double gap = in->gap[i], dl = in->dl[i];
     l.col[l.m] = in->kpass + nadded - 1;
     l.t[l.m] = i;
     l.lam[l.m] = in->lam[i];
-    l.rhs[l.m] = (gap > res) ? sqrt(dl * res) : fmin(dl, sqrt(dl));
+    l.rhs[l.m] = srhs[i];
     ++l.m;
     if (nadded + in->kpass == in->limadd) break;
   }
@@ -995,8 +1002,8 @@ __global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict
 // drops; C[q MT_MAX + c] = the map from current column q to kept column c
 // (R^-1 on the kept rows), bst[1] = columns before, bst[0] = kept. The last
 // round also writes the matvec skip flags of the m columns. Right-looking
-// Cholesky on the Schur complement in shared memory (one column per step,
-// one thread per element), then one thread per column of R^-1. When G is
+// Cholesky on the Schur complement in shared memory by one warp (one column
+// per step), then one lane per column of R^-1. When G is
 // within 1e-8 of the identity (the second round, after a first one), R^-1 =
 // I - F to first order (F the upper triangle of G - I, diagonal halved):
 // its error is O(|G - I|^2) and it needs no serial chain of square roots and
@@ -1036,34 +1043,36 @@ __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst
     if (last && tid < m) skipf[tid] = (tid < nb) ? 0.0 : 1.0;
     return;
   }
-  if (tid < nb) {
-    g0[tid] = G[tid * nb + tid];
-    pos[tid] = -1;
+  // the factorisation by warp 0 alone: its steps then need warp syncs only
+  if (tid >= 32) return;
+  if (lane < nb) {
+    g0[lane] = G[lane * nb + lane];
+    pos[lane] = -1;
   }
-  __syncthreads();
+  __syncwarp();
   int nk = 0;  // uniform
   for (int q = 0; q < nb; ++q) {
     const double dq = G[q * nb + q];
     if (dq > 1e-14 * g0[q] && dq > 1e-300) {
       const double inv = rsqrt(dq), rd = dq * inv;
-      if (tid < nb) R[nk * MT_MAX + tid] = (tid < q) ? 0.0 : (tid == q ? rd : G[q * nb + tid] * inv);
-      __syncthreads();
-      if (tid < nb * nb) {
-        const int a = tid / nb, b = tid % nb;
-        if (a > q && b > q) G[tid] -= R[nk * MT_MAX + a] * R[nk * MT_MAX + b];
+      if (lane < nb) R[nk * MT_MAX + lane] = (lane < q) ? 0.0 : (lane == q ? rd : G[q * nb + lane] * inv);
+      __syncwarp();
+      for (int e = lane; e < nb * nb; e += 32) {
+        const int a = e / nb, b = e % nb;
+        if (a > q && b > q) G[e] -= R[nk * MT_MAX + a] * R[nk * MT_MAX + b];
       }
-      if (tid == 0) {
+      if (lane == 0) {
         keep[nk] = q;
         pos[q] = nk;
         invd[nk] = inv;
       }
       ++nk;
     }
-    __syncthreads();
+    __syncwarp();
   }
   // column c of R_kk^-1, R_kk(i, j) = R[i][keep[j]]
-  if (tid < nk) {
-    const int c = tid;
+  if (lane < nk) {
+    const int c = lane;
     Ri[c * MT_MAX + c] = invd[c];
     for (int i = c - 1; i >= 0; --i) {
       double sum = 0.0;
@@ -1071,17 +1080,17 @@ __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst
       Ri[i * MT_MAX + c] = -sum * invd[i];
     }
   }
-  __syncthreads();
-  if (tid < MT_MAX * MT_MAX) {
-    const int q = tid / MT_MAX, c = tid % MT_MAX;
+  __syncwarp();
+  for (int e = lane; e < MT_MAX * MT_MAX; e += 32) {
+    const int q = e / MT_MAX, c = e % MT_MAX;
     const int i = (q < nb) ? pos[q] : -1;
-    C[tid] = (i >= 0 && c < nk && i <= c) ? Ri[i * MT_MAX + c] : 0.0;
+    C[e] = (i >= 0 && c < nk && i <= c) ? Ri[i * MT_MAX + c] : 0.0;
   }
-  if (tid == 0) {
+  if (lane == 0) {
     bst[1] = nb;
     bst[0] = nk;
   }
-  if (last && tid < m) skipf[tid] = (tid < nk) ? 0.0 : 1.0;
+  if (last && lane < m) skipf[lane] = (lane < nk) ? 0.0 : 1.0;
 }
 
 // first kernel of the pass: bst[0] = m
@@ -1267,14 +1276,32 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
   }
 }
 
-// k_bd_sub in split form: B(:, kpass+q) -= Bx(:, 0:kpass) C(:, q)
-template <int M>
+// k_bd_sub in split form: B(:, kpass+q) -= Bx(:, 0:kpass) C(:, q). L lanes
+// share a row (L = SP for small blocks, whose one-thread-per-row grids leave
+// most SMs idle; 1 otherwise), lane p taking basis columns a = p mod L; their
+// Dot2 sums are added by a fixed double-float butterfly and column q is
+// written by lane q mod L
+constexpr int SP = 4;  // lanes per row of the small-block forms
+template <int L>
+__device__ __forceinline__ df df_lanes(float sh, float sl) {
+  df acc = two_sum(sh, sl);
+#pragma unroll
+  for (int o = 1; o < L; o <<= 1) {
+    df other;
+    other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
+    other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
+    acc = df_add(acc, other);
+  }
+  return acc;
+}
+template <int M, int L>
 __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const float2 *__restrict__ Bx, int64_t ld,
                                                 const IterParams *__restrict__ pv, const double *__restrict__ C,
                                                 int m, int n) {
   __shared__ float2 Cs[BD_CCH * M];
   const int ka = pv[0].c, q0 = blockIdx.y * M;
-  const int i = blockIdx.x * RT + threadIdx.x;
+  const int part = threadIdx.x % L;
+  const int i = blockIdx.x * (RT / L) + threadIdx.x / L;
   float sh[M], sl[M];
 #pragma unroll
   for (int q = 0; q < M; ++q) sh[q] = sl[q] = 0.f;
@@ -1285,8 +1312,8 @@ __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const fl
       Cs[idx] = split2(C[(size_t)(a0 + idx / M) * m + q0 + idx % M]);
     __syncthreads();
     if (i < n) {
-#pragma unroll 8
-      for (int a = 0; a < na; ++a) {
+#pragma unroll 4
+      for (int a = part; a < na; a += L) {
         const float2 x = Bx[(size_t)(a0 + a) * ld + i];
 #pragma unroll
         for (int q = 0; q < M; ++q) {
@@ -1296,13 +1323,16 @@ __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const fl
       }
     }
   }
-  if (i >= n) return;
 #pragma unroll
-  for (int q = 0; q < M; ++q) B[(size_t)(ka + q0 + q) * ld + i] -= (double)sh[q] + (double)sl[q];
+  for (int q = 0; q < M; ++q) {
+    const df acc = df_lanes<L>(sh[q], sl[q]);
+    if (i < n && q % L == part) B[(size_t)(ka + q0 + q) * ld + i] -= (double)acc.h + (double)acc.l;
+  }
 }
 
-// k_ritz_multi in split form (Bx, ABx for the basis and its products)
-template <int NT>
+// k_ritz_multi in split form (Bx, ABx for the basis and its products); L
+// lanes per row as in k_bdx_sub, target t finished by lane t mod L
+template <int NT, int L>
 __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ Bx, const float2 *__restrict__ ABx,
                                                     int64_t ld, int k, int nt, const double *__restrict__ S,
                                                     const double *__restrict__ lam, double *__restrict__ T, int n,
@@ -1314,13 +1344,14 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
   const int t0 = blockIdx.y * NT;
   for (int q = threadIdx.x; q < NT * k; q += RT) sv[q] = split2(S[(size_t)t0 * k + q]);
   __syncthreads();
-  const int i = blockIdx.x * RT + threadIdx.x;
+  const int lp = threadIdx.x % L;
+  const int i = blockIdx.x * (RT / L) + threadIdx.x / L;
   float bh[NT], bl[NT], ah[NT], al[NT];
 #pragma unroll
   for (int t = 0; t < NT; ++t) bh[t] = bl[t] = ah[t] = al[t] = 0.f;
   if (i < n) {
 #pragma unroll 4
-    for (int j = 0; j < k; ++j) {
+    for (int j = lp; j < k; j += L) {
       const float2 bj = Bx[(size_t)j * ld + i], aj = ABx[(size_t)j * ld + i];
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
@@ -1332,9 +1363,10 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
   }
 #pragma unroll
   for (int t = 0; t < NT; ++t) {
+    const df b2 = df_lanes<L>(bh[t], bl[t]), a2 = df_lanes<L>(ah[t], al[t]);
     double r = 0.0;
-    if (i < n) {
-      const double b = (double)bh[t] + (double)bl[t], a = (double)ah[t] + (double)al[t];
+    if (i < n && t % L == lp) {
+      const double b = (double)b2.h + (double)b2.l, a = (double)a2.h + (double)a2.l;
       r = fma(-lam[t0 + t], b, a);
       T[(size_t)(2 * (t0 + t)) * ld + i] = b;
       T[(size_t)(2 * (t0 + t) + 1) * ld + i] = r;
@@ -1359,14 +1391,17 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
 }
 
 // k_multbc in split form: out(:, j) = Xx(:, 0:k) C(:, j) for j in grid row
-// blockIdx.y's group of MB_G columns (C column j at C + j k)
+// blockIdx.y's group of MB_G columns (C column j at C + j k); L lanes per row
+// as in k_bdx_sub, column j finished by lane j mod L
 constexpr int MB_G = 8, MB_CH = 128;
+template <int L>
 __global__ void __launch_bounds__(RT) k_multbcx(const float2 *__restrict__ Xx, int64_t ld, int k,
                                                 const double *__restrict__ C, int m, double *__restrict__ out,
                                                 int n) {
   __shared__ float2 Cs[MB_CH * MB_G];
   const int j0 = blockIdx.y * MB_G;
-  const int i = blockIdx.x * RT + threadIdx.x;
+  const int lp = threadIdx.x % L;
+  const int i = blockIdx.x * (RT / L) + threadIdx.x / L;
   float sh[MB_G], sl[MB_G];
 #pragma unroll
   for (int u = 0; u < MB_G; ++u) sh[u] = sl[u] = 0.f;
@@ -1379,18 +1414,19 @@ __global__ void __launch_bounds__(RT) k_multbcx(const float2 *__restrict__ Xx, i
     }
     __syncthreads();
     if (i < n) {
-#pragma unroll 8
-      for (int q = 0; q < nq; ++q) {
+#pragma unroll 4
+      for (int q = lp; q < nq; q += L) {
         const float2 x = Xx[(size_t)(q0 + q) * ld + i];
 #pragma unroll
         for (int u = 0; u < MB_G; ++u) dot2_step(sh[u], sl[u], Cs[q * MB_G + u].x, Cs[q * MB_G + u].y, x.x, x.y);
       }
     }
   }
-  if (i >= n) return;
 #pragma unroll
-  for (int u = 0; u < MB_G; ++u)
-    if (j0 + u < m) out[(size_t)(j0 + u) * ld + i] = (double)sh[u] + (double)sl[u];
+  for (int u = 0; u < MB_G; ++u) {
+    const df acc = df_lanes<L>(sh[u], sl[u]);
+    if (i < n && j0 + u < m && u % L == lp) out[(size_t)(j0 + u) * ld + i] = (double)acc.h + (double)acc.l;
+  }
 }
 
 struct Dvd {
@@ -1405,6 +1441,7 @@ struct Dvd {
   DBuf<double> dup;               // [0, 8) IterParams, [8, 8 + lim) Ritz coefficients
   DBuf<unsigned> counters;        // last-block counters, one per kernel kind
   int nrow = 0;                   // blocks of the block-pass Ritz kernel (RT rows each)
+  int nrow4 = 0;                  // blocks of the split row kernels (RT / SP rows each)
   int nrr = 0;                    // blocks of the row kernels (RR rows each)
   int cd_rows = 0, cd_blocks = 0, kp = 0;  // column-dot layout: rows per block, blocks, partial pitch
   int nmv = 0;
@@ -1491,6 +1528,7 @@ struct Dvd {
     s = c->stream;
     ld = ((int64_t)n + 31) / 32 * 32;
     nrow = (n + RT - 1) / RT;
+    nrow4 = (n + RT / SP - 1) / (RT / SP);
     nrr = (n + RR - 1) / RR;
     // about two column-dot blocks per SM, rows a multiple of 32
     int sms = 152;
@@ -1502,7 +1540,7 @@ struct Dvd {
     GG_TRY(AB.alloc((size_t)ld * lim));
     GG_TRY(T.alloc((size_t)ld * lim));
     GG_TRY(diag.alloc(n));
-    GG_TRY(part.alloc((size_t)std::max(std::max(cd_blocks * kp, nrow * MT_MAX), nrr) + 1024));
+    GG_TRY(part.alloc((size_t)std::max(std::max(cd_blocks * kp, nrow4 * MT_MAX), nrr) + 1024));
     GG_TRY(dS.alloc((size_t)lim * (lim + 1) / 2));
     GG_TRY(dmt.alloc((size_t)MT_MAX * lim + 2 * MT_MAX));
     GG_CUDA(cudaMallocHost(&hS, (size_t)lim * (lim + 1) / 2 * sizeof(double)));
@@ -1540,6 +1578,44 @@ struct Dvd {
         GG_CUDA(cudaMemsetAsync(ptmv.p, 0, sizeof(unsigned long long), s));
         if (part.n < (size_t)(lim + 2) * pass_grid + 1024) GG_TRY(part.alloc((size_t)(lim + 2) * pass_grid + 1024));
       }
+    }
+    return GG_OK;
+  }
+  // the environment switches read at init
+  static bool env_off(const char *name) {
+    const char *e = std::getenv(name);
+    return e && e[0] == '0';
+  }
+  static bool env_pass() {
+    const char *e = std::getenv("GRASP_GPU_DVD_PASS");
+    return e && std::strcmp(e, "persistent") == 0;
+  }
+  bool reusable(gg_hmat *hm, int prec, int nn, int lm) const {
+    return h == hm && precision == prec && n == nn && lim == lm && use_pass == env_pass();
+  }
+  // a reused workspace (same matrix, sizes and precision; allocations and
+  // graphs kept) starts a new solve
+  int reset() {
+    nmv = 0;
+    mv_ms = 0;
+    mv_count = 0;
+    t_eig = t_wait = t_total = 0;
+    ev_used = 0;
+    pass_ms = 0;
+    spmm_full_ms = 0;
+    spmm_full_n = 0;
+    bx_cols = 0;
+    full_m = 0;
+    use_graph = !env_off("GRASP_GPU_DVD_GRAPH");
+    use_fused = !env_off("GRASP_GPU_DVD_FUSED");
+    GG_CUDA(cudaMemsetAsync(counters.p, 0, 16 * sizeof(unsigned), s));
+    GG_CUDA(cudaMemsetAsync(dots.p, 0, (lim + 8 + SC_N) * sizeof(double), s));
+    std::memset(hup, 0, (size_t)(8 + lim) * sizeof(double));
+    GG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)ld * lim * 8, s));
+    GG_CUDA(cudaMemsetAsync(AB.p, 0, (size_t)ld * lim * 8, s));
+    if (use_pass) {
+      GG_CUDA(cudaMemsetAsync(pbar.p, 0, 2 * sizeof(unsigned), s));
+      GG_CUDA(cudaMemsetAsync(ptmv.p, 0, sizeof(unsigned long long), s));
     }
     return GG_OK;
   }
@@ -1718,7 +1794,7 @@ struct Dvd {
       k_bd_reduce<0><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p);
       if (sub_split) {
         if (split)
-          k_bdx_sub<1><<<dim3(nrow, m), RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);
+          k_bdx_sub<1, SP><<<dim3(nrow4, m), RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);
         else
           k_bd_sub<1><<<dim3(nrow, m), RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);
       } else {
@@ -1726,7 +1802,7 @@ struct Dvd {
 #define BD_SUB(K)                                                                  \
   case K:                                                                          \
     if (split)                                                                     \
-      k_bdx_sub<K><<<nrow, RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);          \
+      k_bdx_sub<K, 1><<<nrow, RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);        \
     else                                                                           \
       k_bd_sub<K><<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);                 \
     break;
@@ -1814,6 +1890,7 @@ struct Dvd {
       const int want = std::max(1, (2 * ctx->sms + bd_Y - 1) / bd_Y);
       bd_cpc = (nchunk + want - 1) / want;
       bd_G = (nchunk + bd_cpc - 1) / bd_cpc;
+
       bd_ps = lim * MT_MAX;
       GG_TRY(bpart.alloc((size_t)bd_G * bd_ps));
       GG_TRY(bC.alloc((size_t)std::max(lim * MT_MAX, MT_MAX * MT_MAX)));
@@ -2058,12 +2135,12 @@ struct Dvd {
     if (use_x()) {
       GG_TRY(sync_split(k));
       if (per_target) {
-        k_ritzx_multi<1><<<dim3(nrow, nt), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
+        k_ritzx_multi<1, SP><<<dim3(nrow4, nt), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
                                                        counters.p + 3, drn);
       } else {
         switch (nt) {
 #define RM_CASE(K) \
-  case K: k_ritzx_multi<K><<<nrow, RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
+  case K: k_ritzx_multi<K, 1><<<nrow, RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
           RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
           RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
 #undef RM_CASE
@@ -2134,7 +2211,10 @@ struct Dvd {
     GG_CUDA(cudaMemcpyAsync(small.p, hC, (size_t)k * m * sizeof(double), cudaMemcpyHostToDevice, s));
     if (use_x()) {
       GG_TRY(sync_split(k));
-      k_multbcx<<<dim3(nrow, (m + MB_G - 1) / MB_G), RT, 0, s>>>(Xx.p, ld, k, small.p, m, T.p, n);
+      if ((int64_t)nrow * 2 < ctx->sms)
+        k_multbcx<SP><<<dim3(nrow4, (m + MB_G - 1) / MB_G), RT, 0, s>>>(Xx.p, ld, k, small.p, m, T.p, n);
+      else
+        k_multbcx<1><<<dim3(nrow, (m + MB_G - 1) / MB_G), RT, 0, s>>>(Xx.p, ld, k, small.p, m, T.p, n);
     } else {
       k_multbc<<<(n + RC - 1) / RC, TPB, 0, s>>>(X.p, ld, k, small.p, m, T.p, n);
     }
@@ -2629,14 +2709,42 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   // leading ns x ns block, here by the same Davidson solver from unit vectors.
   const int ns = std::min(nmax, ncf);
   gg_hmat *blk = h;
-  if (ns < ncf) GG_TRY(leading_block(h, ns, &blk));
-  struct Guard {
-    gg_hmat *b, *h;
-    ~Guard() {
-      if (b != h) gg_hmat_destroy(b);
+  if (ns < ncf) {
+    // the leading block is kept with the matrix; its values follow EMT
+    if (h->lead && h->lead->ncf != ns) {
+      delete h->lead;
+      h->lead = nullptr;
     }
-  } guard{blk, h};
-  Dvd D1;
+    if (!h->lead) {
+      GG_TRY(leading_block(h, ns, &h->lead));
+    } else {
+      gg_hmat *b = h->lead;
+      GG_CUDA(cudaMemcpyAsync(b->dEmt.p, h->dEmt.p, b->nnz * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+      GG_CUDA(cudaMemcpyAsync(b->dDiag.p, h->dDiag.p, ns * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+      b->sym_vals_valid = false;
+    }
+    blk = h->lead;
+  }
+  // Davidson workspaces kept with the matrix, by stage and precision
+  auto workspace = [&](int stage, gg_hmat *hm, int nn, int lm, Dvd **out) -> int {
+    std::shared_ptr<void> &c = h->dvd_cache[2 * stage + (precision == GG_SPLIT ? 1 : 0)];
+    Dvd *d = static_cast<Dvd *>(c.get());
+    if (d && d->reusable(hm, precision, nn, lm)) {
+      GG_TRY(d->reset());
+    } else {
+      c.reset();
+      d = new Dvd;
+      c = std::shared_ptr<void>(d, [](void *q) { delete static_cast<Dvd *>(q); });
+      const int st = d->init(ctx, hm, precision, nn, lm);
+      if (st != GG_OK) {
+        c.reset();
+        return st;
+      }
+    }
+    *out = d;
+    return GG_OK;
+  };
+  Dvd *D1p = nullptr, *D2p = nullptr;
   {
     GG_TRY(refresh_sym_values(blk));
     DvdParams P1 = P;
@@ -2649,7 +2757,8 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     P1.mblock = nvec;
     P1.lim = std::min(ns, P.lim);
     if (ns < ncf && P1.lim < P.nume + 1) P1.lim = ns;
-    GG_TRY(D1.init(ctx, blk, precision, ns, P1.lim));
+    GG_TRY(workspace(0, blk, ns, P1.lim, &D1p));
+    Dvd &D1 = *D1p;
     GG_CUDA(cudaMemcpyAsync(D1.diag.p, blk->dDiag.p, ns * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     GG_TRY(unit_start(D1, blk, nvec));
     int nl = 0, ie = 0;
@@ -2663,11 +2772,15 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     ctx->stats[9] = 0;   // stage-2 loops
     ctx->stats[10] = D1.mv_ms;
   }
+  Dvd &D1 = *D1p;
   Dvd *Dout = &D1;
-  Dvd D2;
+  Dvd D2none;  // statistics of an absent stage 2
   if (ns < ncf) {
     // Stage 2: GDVD on the whole block from the zero-padded estimates
-    GG_TRY(D2.init(ctx, h, precision, ncf, P.lim));
+    GG_TRY(workspace(1, h, ncf, P.lim, &D2p));
+  }
+  Dvd &D2 = D2p ? *D2p : D2none;
+  if (ns < ncf) {
     GG_CUDA(cudaMemcpyAsync(D2.diag.p, h->dDiag.p, ncf * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
     GG_CUDA(cudaMemcpy2DAsync(D2.B.p, D2.ld * 8, D1.B.p, D1.ld * 8, (size_t)ns * 8, nvec, cudaMemcpyDeviceToDevice,
                               ctx->stream));

@@ -196,6 +196,16 @@ struct gg_hmat {
   gg::DBuf<float2> dXb;                 // [ncf][m even] split copies of m input vectors, by row
   bool sym_vals_valid = false;
   gg::LTile lt;                         // tiled lower-triangle layout (split matvec)
+  // kept between gg_maneig calls (davidson.cu): the leading block of the
+  // INIEST2 stage (its structure and symmetric matvec structure; values
+  // recopied per call) and the Davidson workspaces with their CUDA graphs,
+  // by stage and precision
+  gg_hmat *lead = nullptr;
+  std::shared_ptr<void> dvd_cache[4];
+  ~gg_hmat() {
+    for (auto &c : dvd_cache) c.reset();
+    delete lead;
+  }
 };
 
 namespace gg {
