@@ -51,6 +51,8 @@ def _args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-extra", action="store_true", help="skip the batched-block and R^k table legs")
+    ap.add_argument("--large", action="store_true",
+                    help="run only the large-scale leg (~3e5 CSFs, ~1e9 elements; minutes) and print its JSON line")
     return ap.parse_args()
 
 
@@ -261,6 +263,50 @@ def rk_leg(local):
         vals[name] = ctx.rk_table()[1]
     a, b = vals["tensor_ozaki"], vals["fp64"]
     out["max_rel_diff"] = float((np.abs(a - b) / np.maximum(np.abs(b), 1e-2)).max())
+    return out
+
+
+def large_leg(local, steps=2):
+    """The large-scale CI workload (workloads.large: ~3e5 CSFs, ~1e9 stored
+    elements of a seeded synthetic H, the Z = 40 47-orbital R^k table to
+    k = 10, 5 roots): table, block, split and FP64 solves. Opt-in
+    (--large): generating and uploading the block takes minutes."""
+    import numpy as np
+
+    from grasp_gb300 import FP64, SPLIT, Context, HMatrix, workloads
+    t0 = time.perf_counter()
+    w = workloads.large()
+    t_gen = time.perf_counter() - t0
+    ctx = Context(local)
+    ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
+    ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    out = dict(w.describe(), generate_s=t_gen)
+    for prec, name in ((1, "tensor_ozaki"), (0, "fp64")):
+        ctx.genintrk(kmax=w.kmax, precision=prec)
+        n, _ = ctx.genintrk(kmax=w.kmax, precision=prec)
+        out[f"rk_{name}_ms"] = ctx.stage_stat(0)
+        out["rk_integrals"] = int(n)
+    t0 = time.perf_counter()
+    H = HMatrix(ctx, w.ncf, w.iendc, w.irow)
+    H.set_emt(w.emt)
+    out["upload_s"] = time.perf_counter() - t0
+    res = {}
+    for prec, name in ((SPLIT, "split"), (FP64, "fp64")):
+        ts = []
+        for _ in range(steps):
+            ctx.mark(0)
+            ev, vec, info = H.maneig(w.nroots, flavour=0, precision=prec, mblock=w.nroots)
+            ctx.mark(1)
+            ts.append(ctx.elapsed(0, 1) * 1e-3)
+        res[name] = ev
+        out[f"{name}_solve_s"] = min(ts)
+        out[f"{name}_loops"] = info["nloops"]
+    out["max_abs_dE_split_vs_fp64_Eh"] = float(np.abs(res["split"] - res["fp64"]).max())
+    ms, by = H.spmm_timing(w.nroots, 5)
+    out["spmm_us_per_launch"] = ms * 1e3
+    out["spmm_alg_gbs"] = by / (ms * 1e-3) / 1e9
+    H.close()
+    ctx.close()
     return out
 
 
@@ -479,6 +525,12 @@ def run_ours(a):
 
 def main():
     a = _args()
+    if a.large:
+        ws, rank, local, pg = _dist()
+        out = large_leg(local)
+        if rank == 0:
+            print(json.dumps({"leg": "large", **out}), flush=True)
+        return 0
     if a.impl == "reference":
         return run_reference(a)
     return run_ours(a)

@@ -89,6 +89,7 @@ SYNTH_SYMBOLS = {
     "gs_block_sizes": (C.c_int, [C.c_void_p, _int, _i64, _int, _int, _i64, _i64]),
     "gs_block_structure": (C.c_int, [C.c_void_p, _i64, _i32, _u8]),
     "gs_block_list": (C.c_int, [C.c_void_p, C.c_int, _i32, _i64, _i32, _i32, _d]),
+    "gs_synthetic_h": (C.c_int, [C.c_int, C.c_double, C.c_uint64, _i64, _i32, _d]),
 }
 
 
@@ -134,6 +135,12 @@ class GGError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"[{status}] {msg}")
         self.status = status
+
+
+def check_synth(status):
+    if status != 0:
+        raise ValueError(f"synthetic-input generator rejected its arguments (status {status})")
+    return status
 
 
 def check(status):

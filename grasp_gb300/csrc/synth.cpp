@@ -510,3 +510,73 @@ extern "C" int gs_block_list(const gs_block *b, int list, int32_t *lab, int64_t 
   if (coeff) std::memcpy(coeff, o.coeff.data(), o.coeff.size() * sizeof(double));
   return 0;
 }
+
+namespace {
+inline uint64_t sh_mix(uint64_t x) {  // splitmix64 finaliser
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+struct ShRng {
+  uint64_t s;
+  double u() {  // uniform in (0, 1)
+    s = sh_mix(s);
+    return ((double)(s >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  }
+  double normal() {  // Box-Muller, one value per call
+    const double a = u(), b = u();
+    return std::sqrt(-2.0 * std::log(a)) * std::cos(6.283185307179586 * b);
+  }
+};
+// the columns of row r, ascending: Bernoulli(p) per column by geometric skips
+template <class F> void sh_row(int r, double lq, uint64_t seed, F &&emit) {
+  if (lq >= 0.0) return;  // p = 0
+  ShRng g{sh_mix(seed ^ (0xD1B54A32D192ED03ull * (uint64_t)(r + 1)))};
+  int64_t c = -1;
+  for (;;) {
+    c += 1 + (int64_t)std::floor(std::log(g.u()) / lq);
+    if (c >= r) break;
+    emit((int)c);
+  }
+}
+}  // namespace
+
+extern "C" int gs_synthetic_h(int ncf, double p, uint64_t seed, int64_t *iendc, int32_t *irow, double *emt) {
+  if (ncf < 1 || !(p >= 0.0) || p >= 1.0 || !iendc || ((irow == nullptr) != (emt == nullptr))) return -1;
+  const double lq = (p > 0.0) ? std::log1p(-p) : 0.0;
+  const int nt = std::max(1, std::min(64, (int)std::thread::hardware_concurrency()));
+  auto rows = [&](int t, bool fill) {
+    const int r0 = (int)((int64_t)ncf * t / nt), r1 = (int)((int64_t)ncf * (t + 1) / nt);
+    for (int r = r0; r < r1; ++r) {
+      if (!fill) {
+        int64_t k = 1;  // the diagonal
+        sh_row(r, lq, seed, [&](int) { ++k; });
+        iendc[r + 1] = k;
+        continue;
+      }
+      int64_t q = iendc[r];
+      ShRng g{sh_mix(~seed ^ (0x9E3779B97F4A7C15ull * (uint64_t)(r + 1)))};  // values
+      sh_row(r, lq, seed, [&](int c) {
+        irow[q] = c + 1;
+        emt[q] = 2e-3 * g.normal();
+        ++q;
+      });
+      irow[q] = r + 1;
+      emt[q] = -1000.0 + 30.0 * std::sqrt((double)r / ncf) + 1e-3 * g.normal();
+    }
+  };
+  auto run = [&](bool fill) {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t) th.emplace_back(rows, t, fill);
+    for (auto &x : th) x.join();
+  };
+  if (!irow) {
+    iendc[0] = 0;
+    run(false);
+    for (int r = 0; r < ncf; ++r) iendc[r + 1] += iendc[r];
+    return 0;
+  }
+  run(true);
+  return 0;
+}

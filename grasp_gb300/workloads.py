@@ -18,6 +18,13 @@ Sizes versus the workload descriptions they stand in for:
         (2 % by default).
   rk40  The R^k table workload: n <= 7, |kappa| <= 4 (40 orbitals), Z = 26,
         screening drawn U[0, Z-1] from the seed, k = 0..8.
+  large The large-scale CI workload: Ni-like Z = 40 orbital set (n <= 7,
+        l <= 5: 47 orbitals, R^k to k = 10) and a seeded synthetic symmetric
+        H of ~3e5 CSFs with ~1e9 stored lower-triangle elements (sorted
+        configuration-like diagonal, small random couplings, uniform random
+        structure), 5 roots. The Hamiltonian is generated directly (no T/V
+        lists: at this size they would be ~2.4e9 contributions), so it
+        exercises the tables and the eigensolver, not SETHAM.
   batch The ne7 expansion for every ion Z = 10..40 (31 ions) and every
         2J = 0, 2, 4, 6, 8 of both parities: 310 blocks of 321-1007 CSFs
         (7,027 CSFs and 1.04 M stored elements per ion), 3 roots each. The
@@ -101,6 +108,62 @@ def rk40(seed=2024):
     sig = np.random.default_rng(seed).uniform(0.0, z - 1.0, size=len(orbs))
     n, rnt, ob = _orbitals(orbs, z, sig)
     return Workload("rk_table_40orb_k8", z, orbs, n, rnt, 0.05, S.CVAC, np.full(n, z), ob, None, 0, kmax=8)
+
+
+@dataclass
+class LargeWorkload:
+    """Orbitals for the R^k table and a lower-triangle-by-rows H (IENDC,
+    1-based IROW with the diagonal last in each row, EMT)."""
+    name: str
+    z: float
+    orbs: list
+    n: int
+    rnt: float
+    h: float
+    c: float
+    zz: np.ndarray
+    orb: S.Orbitals
+    ncf: int
+    iendc: np.ndarray
+    irow: np.ndarray
+    emt: np.ndarray
+    nroots: int
+    kmax: int
+
+    @property
+    def nnz(self):
+        return int(self.iendc[-1])
+
+    def describe(self):
+        return dict(workload=self.name, z=self.z, norb=len(self.orbs), kmax=self.kmax, grid_points=self.n,
+                    ncf=self.ncf, nnz=self.nnz, density=round(2.0 * self.nnz / (self.ncf * (self.ncf + 1.0)), 5),
+                    nroots=self.nroots, hamiltonian="synthetic (seeded), no T/V lists")
+
+
+def synthetic_h(ncf, nnz, seed=7):
+    """Seeded symmetric H in GRASP's lower-triangle-by-rows storage with about
+    ``nnz`` stored elements (gs_synthetic_h, include/grasp_synth.h): each
+    column below the diagonal of row r is present with the same probability;
+    diagonal -1000 + 30 sqrt(r / ncf) Eh (sorted, like configuration
+    energies) plus N(0, 1e-3), off-diagonal elements N(0, 2e-3) Eh."""
+    from ._lib import _d, _i32, _i64, check_synth, ptr
+    p = 2.0 * max(nnz - ncf, 0) / (ncf * (ncf - 1.0))
+    iendc = np.zeros(ncf + 1, np.int64)
+    lib = S._lib.synth()
+    check_synth(lib.gs_synthetic_h(ncf, p, seed, ptr(iendc, _i64), None, None))
+    irow = np.empty(int(iendc[-1]), np.int32)
+    emt = np.empty(int(iendc[-1]), np.float64)
+    check_synth(lib.gs_synthetic_h(ncf, p, seed, ptr(iendc, _i64), ptr(irow, _i32), ptr(emt, _d)))
+    return iendc, irow, emt
+
+
+def large(ncf=300000, nnz=1.0e9, seed=7, nroots=5):
+    orbs = S.orbital_set(7, 5)
+    z = 40.0
+    n, rnt, ob = _orbitals(orbs, z, S.screenpar([k for _, k in orbs], 4))  # n <= 2 core: 1s, 2s, 2p-, 2p
+    iendc, irow, emt = synthetic_h(ncf, int(nnz), seed=seed)
+    return LargeWorkload(f"ni_like_z40_j1o_{ncf}csf_synthetic", z, orbs, n, rnt, 0.05, S.CVAC, np.full(n, z), ob,
+                         ncf, iendc, irow, emt, nroots, 10)
 
 
 @dataclass

@@ -68,6 +68,16 @@ int gs_block_structure(const gs_block *b, int64_t *iendc, int32_t *irow, uint8_t
 int gs_block_list(const gs_block *b, int list, int32_t *lab, int64_t *start, int32_t *iclmn, int32_t *loc,
                   double *coeff);
 
+/* A seeded synthetic symmetric H in GRASP's lower-triangle-by-rows storage
+ * (mcp.30's IENDC / IROW, diagonal last in each row, 1-based IROW) with
+ * off-diagonal density p: row r holds each column c < r with probability p
+ * (independent draws, taken in ascending order by geometric skips), then its
+ * diagonal. EMT: diagonal -1000 + 30 sqrt(r / ncf) + N(0, 1e-3) Eh,
+ * off-diagonal N(0, 2e-3) Eh. Every row draws from its own counter-based
+ * stream, so the result does not depend on the thread count. Call with
+ * irow = emt = NULL to get IENDC(0:ncf) (sizes), then again with all three. */
+int gs_synthetic_h(int ncf, double p, uint64_t seed, int64_t *iendc, int32_t *irow, double *emt);
+
 #ifdef __cplusplus
 }
 #endif
