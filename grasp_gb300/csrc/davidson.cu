@@ -1818,13 +1818,15 @@ struct Dvd {
         else
           k_bd_sub<1><<<dim3(nrow, m), RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);
       } else {
-        switch (m) {
-#define BD_SUB(K)                                                                  \
-  case K:                                                                          \
-    if (split)                                                                     \
-      k_bdx_sub<K, 1><<<nrow, RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);        \
-    else                                                                           \
-      k_bd_sub<K><<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);                 \
+        // an even m as two grid rows of m / 2 columns (twice the warps)
+        const int half = (m % 2 == 0) ? 2 : 1;
+        switch (m / half) {
+#define BD_SUB(K)                                                                           \
+  case K:                                                                                   \
+    if (split)                                                                              \
+      k_bdx_sub<K, 1><<<dim3(nrow, half), RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);     \
+    else                                                                                    \
+      k_bd_sub<K><<<dim3(nrow, half), RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);              \
     break;
         BD_SUB(1) BD_SUB(2) BD_SUB(3) BD_SUB(4) BD_SUB(5) BD_SUB(6) BD_SUB(7) BD_SUB(8)
         BD_SUB(9) BD_SUB(10) BD_SUB(11) BD_SUB(12) BD_SUB(13) BD_SUB(14) BD_SUB(15) BD_SUB(16)
@@ -1905,10 +1907,11 @@ struct Dvd {
       buses.assign(MT_MAX + 1, 0);
       // row ranges of BD_R-row chunks, about two CTAs per SM
       // (grid rows: column chunks of BD_AC, up to LIM / BD_AC of them)
-      // (column chunks as grid rows only when the row ranges alone leave SMs idle)
+      // (grid rows: the column chunks; about two row ranges per SM, or one
+      // CTA per row chunk for small blocks)
       const int nchunk = (n + BD_R - 1) / BD_R;
-      bd_Y = (nchunk >= 2 * ctx->sms) ? 1 : std::max(1, (lim + BD_AC - 1) / BD_AC);
-      const int want = std::max(1, (2 * ctx->sms + bd_Y - 1) / bd_Y);
+      bd_Y = std::max(1, (lim + BD_AC - 1) / BD_AC);
+      const int want = std::max(1, (nchunk >= 2 * ctx->sms) ? 2 * ctx->sms : (2 * ctx->sms + bd_Y - 1) / bd_Y);
       bd_cpc = (nchunk + want - 1) / want;
       bd_G = (nchunk + bd_cpc - 1) / bd_cpc;
 
@@ -2163,9 +2166,11 @@ struct Dvd {
         k_ritzx_multi<1, SP><<<dim3(nrow4, nt), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
                                                        counters.p + 3, drn);
       } else {
-        switch (nt) {
+        // an even nt as two grid rows of nt / 2 targets (twice the warps)
+        const int half = (nt % 2 == 0) ? 2 : 1;
+        switch (nt / half) {
 #define RM_CASE(K) \
-  case K: k_ritzx_multi<K, 1><<<nrow, RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
+  case K: k_ritzx_multi<K, 1><<<dim3(nrow, half), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
           RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
           RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
 #undef RM_CASE
