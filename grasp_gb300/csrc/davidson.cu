@@ -1818,8 +1818,9 @@ struct Dvd {
         else
           k_bd_sub<1><<<dim3(nrow, m), RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);
       } else {
-        // an even m as two grid rows of m / 2 columns (twice the warps)
-        const int half = (m % 2 == 0) ? 2 : 1;
+        // an even m as m / 2 grid rows of two columns (more warps in flight;
+        // each grid row reads the basis, from L2)
+        const int half = (m % 2 == 0) ? m / 2 : 1;
         switch (m / half) {
 #define BD_SUB(K)                                                                           \
   case K:                                                                                   \
@@ -2166,7 +2167,8 @@ struct Dvd {
         k_ritzx_multi<1, SP><<<dim3(nrow4, nt), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
                                                        counters.p + 3, drn);
       } else {
-        // an even nt as two grid rows of nt / 2 targets (twice the warps)
+        // an even nt as two grid rows of nt / 2 targets (twice the warps;
+        // finer splits re-read the basis more than they gain)
         const int half = (nt % 2 == 0) ? 2 : 1;
         switch (nt / half) {
 #define RM_CASE(K) \
