@@ -120,7 +120,10 @@ struct Lists {  // device copies of one block's T/V lists, concatenated in SETHA
   DBuf<int64_t> dStart;                 // [nlab + 1], global contribution offsets
   DBuf<int32_t> dLoc;                   // [ncontr]
   DBuf<double> dCoeff;                  // [ncontr]
-  DBuf<uint8_t> dIq;                    // [ncf][nw]
+  DBuf<uint8_t> dIq;                    // [nconf][nw] occupations of each run of equal IQ rows
+  DBuf<int32_t> dConf;                  // [ncf] the run of each CSF
+  DBuf<double> dConfDiag;               // [nconf] diagonal pieces per run, last assembly
+  int nconf = 0;
   bool valid = false;
   // assembly plan (setham.cu): the contributions sorted by LOC with their
   // integral slots, and the diagonal terms; it depends only on these lists

@@ -248,14 +248,17 @@ __global__ void k_sort_gather(const int64_t *__restrict__ off, int64_t nnz, int3
 
 // Diagonal pieces without MCP coefficients (setham.f90:83-219), one thread
 // per CSF, terms in the reference's loop order, zero coefficients skipped.
+// The diagonal pieces of EMT per run of equal occupations (a configuration),
+// one warp per run: lane l takes the terms t = l, l + 32, ...; the lane sums
+// are added by a fixed shuffle tree (the order of the reference's sum
+// differs only by rounding); k_diag_scatter copies them to the CSFs
 __global__ void k_diag_terms(const DiagTerm *__restrict__ terms, int nterms, const uint8_t *__restrict__ iq, int nw,
-                             int ncf, const int64_t *__restrict__ iendc, const double *__restrict__ integ,
-                             double *__restrict__ emt) {
-  const int ir = blockIdx.x * blockDim.x + threadIdx.x;
-  if (ir >= ncf) return;
+                             int nconf, const double *__restrict__ integ, double *__restrict__ cdiag) {
+  const int ir = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (ir >= nconf) return;
   const uint8_t *q = iq + (size_t)ir * nw;
   double acc = 0.0;
-  for (int t = 0; t < nterms; ++t) {
+  for (int t = lane; t < nterms; t += 32) {
     const DiagTerm T = terms[t];
     const int qa = q[T.a];
     double coef = 0.0;
@@ -283,22 +286,39 @@ __global__ void k_diag_terms(const DiagTerm *__restrict__ terms, int nterms, con
       }
     }
     if (coef == 0.0) continue;
-    acc = acc + coef * integ[T.slot];
+    acc = fma(coef, integ[T.slot], acc);
   }
-  emt[iendc[ir + 1] - 1] = acc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) cdiag[ir] = acc;
+}
+__global__ void k_diag_scatter(const int32_t *__restrict__ conf, const double *__restrict__ cdiag, int ncf,
+                               const int64_t *__restrict__ iendc, double *__restrict__ emt) {
+  const int ir = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ir < ncf) emt[iendc[ir + 1] - 1] = cdiag[conf[ir]];
 }
 
 // EMT(LOC) = EMT(LOC) + I * COEFF over the element's contributions, in order
+// one EMT element per thread, its contributions added in list order; the
+// loads of two contributions are issued before their products are added
 __global__ void k_assemble(const int64_t *__restrict__ off, int64_t nnz, const double *__restrict__ coeff_s,
                            const int32_t *__restrict__ slot_s, const double *__restrict__ integ,
                            double *__restrict__ emt) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t lo = off[e], hi = off[e + 1];
-    if (lo == hi) continue;
-    double acc = emt[e];
-    for (int64_t i = lo; i < hi; ++i) acc = acc + integ[slot_s[i]] * coeff_s[i];
-    emt[e] = acc;
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= nnz) return;
+  const int64_t lo = off[e], hi = off[e + 1];
+  if (lo == hi) return;
+  double acc = emt[e];
+  int64_t i = lo;
+  for (; i + 1 < hi; i += 2) {
+    const int32_t s0 = slot_s[i], s1 = slot_s[i + 1];
+    const double c0 = coeff_s[i], c1 = coeff_s[i + 1];
+    const double v0 = integ[s0], v1 = integ[s1];
+    acc = acc + v0 * c0;
+    acc = acc + v1 * c1;
   }
+  if (i < hi) acc = acc + integ[slot_s[i]] * coeff_s[i];
+  emt[e] = acc;
 }
 
 // EAV = sum of diagonals / NCF (deterministic tree), then H - EAV I
@@ -306,6 +326,7 @@ __global__ void k_eav(const int64_t *__restrict__ iendc, int ncf, double *__rest
                       double *__restrict__ eav_out) {
   __shared__ double s[1024];
   double acc = 0.0;
+#pragma unroll 8
   for (int i = threadIdx.x; i < ncf; i += blockDim.x) acc = acc + emt[iendc[i + 1] - 1];
   s[threadIdx.x] = acc;
   __syncthreads();
@@ -314,6 +335,7 @@ __global__ void k_eav(const int64_t *__restrict__ iendc, int ncf, double *__rest
     __syncthreads();
   }
   const double eav = s[0] / (double)ncf;
+#pragma unroll 8
   for (int i = threadIdx.x; i < ncf; i += blockDim.x) {
     const int64_t p = iendc[i + 1] - 1;
     const double v = emt[p] - eav;
@@ -499,8 +521,31 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
   L.nlab = nlab;
   L.ncontr = ncontr;
   const int nw = ctx->orb.nw;
-  GG_TRY(L.dIq.alloc((size_t)h->ncf * nw));
-  GG_CUDA(cudaMemcpyAsync(L.dIq.p, iq, (size_t)h->ncf * nw, cudaMemcpyHostToDevice, ctx->stream));
+  {
+    // runs of equal IQ rows (GRASP lists a configuration's CSFs together):
+    // the diagonal pieces depend on the occupations only, so they are
+    // evaluated once per run
+    std::vector<int32_t> conf(h->ncf);
+    std::vector<uint8_t> rows;
+    rows.reserve((size_t)h->ncf * nw);
+    int nc = 0;
+    for (int ir = 0; ir < h->ncf; ++ir) {
+      const uint8_t *q = iq + (size_t)ir * nw;
+      if (ir == 0 || std::memcmp(q, q - nw, nw) != 0) {
+        rows.insert(rows.end(), q, q + nw);
+        ++nc;
+      }
+      conf[ir] = nc - 1;
+    }
+    L.nconf = nc;
+    GG_TRY(L.dIq.alloc((size_t)nc * nw));
+    GG_TRY(L.dConf.alloc(h->ncf));
+    GG_TRY(L.dConfDiag.alloc(nc));
+    GG_CUDA(cudaMemcpyAsync(L.dIq.p, rows.data(), rows.size(), cudaMemcpyHostToDevice, ctx->stream));
+    GG_CUDA(cudaMemcpyAsync(L.dConf.p, conf.data(), conf.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    GG_CUDA(cudaStreamSynchronize(ctx->stream));  // rows and conf are host temporaries
+  }
   GG_TRY(L.dLab.alloc(nlab));
   GG_TRY(L.dStart.alloc(nlab + 1));
   GG_TRY(L.dLoc.alloc(ncontr));
@@ -687,12 +732,15 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
   GG_CUDA(cudaMemcpyAsync(L.integ.p + nrk, ctx->dIab.p, (size_t)nw * nw * sizeof(double), cudaMemcpyDeviceToDevice,
                           s));
   // EMT = 0 ; diagonal pieces ; list contributions ; EAV shift
-  const int gblocks = ctx->sms * 8;
   GG_CUDA(cudaMemsetAsync(h->dEmt.p, 0, nnz * sizeof(double), s));
-  k_diag_terms<<<(ncf + 127) / 128, 128, 0, s>>>(reinterpret_cast<const DiagTerm *>(L.pTerms.p), L.nterms, L.dIq.p,
-                                                 nw, ncf, h->dIendc.p, L.integ.p, h->dEmt.p); ::gg::note_launch();
+  k_diag_terms<<<(unsigned)(((int64_t)L.nconf * 32 + 255) / 256), 256, 0, s>>>(
+      reinterpret_cast<const DiagTerm *>(L.pTerms.p), L.nterms, L.dIq.p, nw, L.nconf, L.integ.p, L.dConfDiag.p);
+  k_diag_scatter<<<(ncf + 255) / 256, 256, 0, s>>>(L.dConf.p, L.dConfDiag.p, ncf, h->dIendc.p, h->dEmt.p);
+  ::gg::note_launches(2);
   GG_CUDA(cudaGetLastError());
-  k_assemble<<<gblocks, 256, 0, s>>>(L.pOff.p, nnz, L.pCoeff.p, L.pSlot.p, L.integ.p, h->dEmt.p); ::gg::note_launch();
+  k_assemble<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(L.pOff.p, nnz, L.pCoeff.p, L.pSlot.p, L.integ.p,
+                                                         h->dEmt.p);
+  ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   GG_TRY(h->dEav.alloc(1));
   k_eav<<<1, 1024, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dDiag.p, h->dEav.p); ::gg::note_launch();
