@@ -299,50 +299,75 @@ __global__ void k_diag_scatter(const int32_t *__restrict__ conf, const double *_
 }
 
 // EMT(LOC) = EMT(LOC) + I * COEFF over the element's contributions, in order
-// one EMT element per thread, its contributions added in list order; the
-// loads of two contributions are issued before their products are added
-__global__ void k_assemble(const int64_t *__restrict__ off, int64_t nnz, const double *__restrict__ coeff_s,
-                           const int32_t *__restrict__ slot_s, const double *__restrict__ integ,
-                           double *__restrict__ emt) {
-  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= nnz) return;
-  const int64_t lo = off[e], hi = off[e + 1];
-  if (lo == hi) return;
-  double acc = emt[e];
-  int64_t i = lo;
-  for (; i + 1 < hi; i += 2) {
-    const int32_t s0 = slot_s[i], s1 = slot_s[i + 1];
-    const double c0 = coeff_s[i], c1 = coeff_s[i + 1];
-    const double v0 = integ[s0], v1 = integ[s1];
-    acc = acc + v0 * c0;
-    acc = acc + v1 * c1;
+// One EMT element per lane, its contributions added in list order. The 32
+// elements of a warp own one contiguous range of contributions: the warp
+// forms the products integ[slot] coeff of that range with coalesced loads
+// into shared memory, then each lane adds its own segment in order (the
+// same sums as a lane walking its segment alone, which is what a range
+// longer than the staging buffer does).
+constexpr int AS_WARPS = 8, AS_MAX = 256;
+__global__ void __launch_bounds__(AS_WARPS * 32) k_assemble(const int64_t *__restrict__ off, int64_t nnz,
+                                                            const double *__restrict__ coeff_s,
+                                                            const int32_t *__restrict__ slot_s,
+                                                            const double *__restrict__ integ,
+                                                            double *__restrict__ emt) {
+  __shared__ double sv[AS_WARPS][AS_MAX];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e0 = ((int64_t)blockIdx.x * AS_WARPS + warp) * 32;
+  if (e0 >= nnz) return;
+  const int ne = (int)min((int64_t)32, nnz - e0);
+  const int64_t e = e0 + lane;
+  const int64_t c0 = off[e0], c1 = off[e0 + ne];
+  const int64_t lo = (lane < ne) ? off[e] : 0, hi = (lane < ne) ? off[e + 1] : 0;
+  if (c1 - c0 <= AS_MAX) {
+    for (int64_t i = c0 + lane; i < c1; i += 32) sv[warp][i - c0] = integ[slot_s[i]] * coeff_s[i];
+    __syncwarp();
+    if (lo < hi) {
+      double acc = emt[e];
+      for (int64_t i = lo; i < hi; ++i) acc = acc + sv[warp][i - c0];
+      emt[e] = acc;
+    }
+  } else if (lo < hi) {
+    double acc = emt[e];
+    for (int64_t i = lo; i < hi; ++i) acc = acc + integ[slot_s[i]] * coeff_s[i];
+    emt[e] = acc;
   }
-  if (i < hi) acc = acc + integ[slot_s[i]] * coeff_s[i];
-  emt[e] = acc;
 }
 
 // EAV = sum of diagonals / NCF (deterministic tree), then H - EAV I
-__global__ void k_eav(const int64_t *__restrict__ iendc, int ncf, double *__restrict__ emt, double *__restrict__ diag,
-                      double *__restrict__ eav_out) {
-  __shared__ double s[1024];
+// EAV = mean of the diagonal, subtracted from it (matrix.f90:123-203): CTA
+// partial sums over contiguous row ranges (EAV_CTAS of them, each in a fixed
+// order), their sum by one CTA in CTA order, then the shift in parallel
+constexpr int EAV_CTAS = 64;
+__global__ void __launch_bounds__(256) k_eav_part(const int64_t *__restrict__ iendc, int ncf,
+                                                  const double *__restrict__ emt, double *__restrict__ part) {
+  __shared__ double s[256];
+  const int per = (ncf + EAV_CTAS - 1) / EAV_CTAS;
+  const int r0 = blockIdx.x * per, r1 = min(ncf, r0 + per);
   double acc = 0.0;
-#pragma unroll 8
-  for (int i = threadIdx.x; i < ncf; i += blockDim.x) acc = acc + emt[iendc[i + 1] - 1];
+  for (int i = r0 + threadIdx.x; i < r1; i += blockDim.x) acc = acc + emt[iendc[i + 1] - 1];
   s[threadIdx.x] = acc;
   __syncthreads();
   for (int w = blockDim.x / 2; w > 0; w >>= 1) {
     if ((int)threadIdx.x < w) s[threadIdx.x] = s[threadIdx.x] + s[threadIdx.x + w];
     __syncthreads();
   }
-  const double eav = s[0] / (double)ncf;
-#pragma unroll 8
-  for (int i = threadIdx.x; i < ncf; i += blockDim.x) {
-    const int64_t p = iendc[i + 1] - 1;
-    const double v = emt[p] - eav;
-    emt[p] = v;
-    diag[i] = v;
-  }
-  if (threadIdx.x == 0) *eav_out = eav;
+  if (threadIdx.x == 0) part[blockIdx.x] = s[0];
+}
+__global__ void k_eav_fin(const double *__restrict__ part, int ncf, double *__restrict__ eav_out) {
+  if (threadIdx.x != 0) return;
+  double sum = 0.0;
+  for (int b = 0; b < EAV_CTAS; ++b) sum = sum + part[b];
+  *eav_out = sum / (double)ncf;
+}
+__global__ void k_eav_sub(const int64_t *__restrict__ iendc, int ncf, const double *__restrict__ eav,
+                          double *__restrict__ emt, double *__restrict__ diag) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ncf) return;
+  const int64_t p = iendc[i + 1] - 1;
+  const double v = emt[p] - *eav;
+  emt[p] = v;
+  diag[i] = v;
 }
 
 // IROW checks of gg_hmat_create, one warp per row: each row ends with its
@@ -738,12 +763,15 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
   k_diag_scatter<<<(ncf + 255) / 256, 256, 0, s>>>(L.dConf.p, L.dConfDiag.p, ncf, h->dIendc.p, h->dEmt.p);
   ::gg::note_launches(2);
   GG_CUDA(cudaGetLastError());
-  k_assemble<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(L.pOff.p, nnz, L.pCoeff.p, L.pSlot.p, L.integ.p,
-                                                         h->dEmt.p);
+  k_assemble<<<(unsigned)((nnz + AS_WARPS * 32 - 1) / (AS_WARPS * 32)), AS_WARPS * 32, 0, s>>>(
+      L.pOff.p, nnz, L.pCoeff.p, L.pSlot.p, L.integ.p, h->dEmt.p);
   ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
-  GG_TRY(h->dEav.alloc(1));
-  k_eav<<<1, 1024, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dDiag.p, h->dEav.p); ::gg::note_launch();
+  GG_TRY(h->dEav.alloc(1 + EAV_CTAS));
+  k_eav_part<<<EAV_CTAS, 256, 0, s>>>(h->dIendc.p, ncf, h->dEmt.p, h->dEav.p + 1);
+  k_eav_fin<<<1, 32, 0, s>>>(h->dEav.p + 1, ncf, h->dEav.p);
+  k_eav_sub<<<(ncf + 255) / 256, 256, 0, s>>>(h->dIendc.p, ncf, h->dEav.p, h->dEmt.p, h->dDiag.p);
+  ::gg::note_launches(3);
   GG_CUDA(cudaGetLastError());
   double eav = 0;
   GG_CUDA(cudaMemcpyAsync(&eav, h->dEav.p, sizeof(double), cudaMemcpyDeviceToHost, s));
