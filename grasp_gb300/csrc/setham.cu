@@ -224,11 +224,20 @@ __global__ void k_scatter_perm(const int32_t *__restrict__ loc, int64_t n, const
 
 // sort each element's segment back into list order, then gather the
 // coefficient and integral slot of each contribution
-__global__ void k_sort_gather(const int64_t *__restrict__ off, int64_t nnz, int32_t *__restrict__ perm,
-                              const double *__restrict__ coeff, const int32_t *__restrict__ cslot,
-                              double *__restrict__ coeff_s, int32_t *__restrict__ slot_s) {
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nnz; e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t lo = off[e], hi = off[e + 1];
+// Each element's contributions back into list order (insertion sort of its
+// short segment of perm, one lane per element), then the coefficients and
+// integral slots gathered in that order: the 32 elements of a warp own one
+// contiguous range, which the warp writes with coalesced stores.
+__global__ void __launch_bounds__(256) k_sort_gather(const int64_t *__restrict__ off, int64_t nnz,
+                                                     int32_t *__restrict__ perm, const double *__restrict__ coeff,
+                                                     const int32_t *__restrict__ cslot, double *__restrict__ coeff_s,
+                                                     int32_t *__restrict__ slot_s) {
+  const int lane = threadIdx.x & 31;
+  const int64_t e0 = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 32;
+  if (e0 >= nnz) return;
+  const int ne = (int)min((int64_t)32, nnz - e0);
+  if (lane < ne) {
+    const int64_t lo = off[e0 + lane], hi = off[e0 + lane + 1];
     for (int64_t i = lo + 1; i < hi; ++i) {
       const int32_t v = perm[i];
       int64_t j = i - 1;
@@ -238,11 +247,13 @@ __global__ void k_sort_gather(const int64_t *__restrict__ off, int64_t nnz, int3
       }
       perm[j + 1] = v;
     }
-    for (int64_t i = lo; i < hi; ++i) {
-      const int32_t p = perm[i];
-      coeff_s[i] = coeff[p];
-      slot_s[i] = cslot[p];
-    }
+  }
+  __syncwarp();
+  const int64_t c0 = off[e0], c1 = off[e0 + ne];
+  for (int64_t i = c0 + lane; i < c1; i += 32) {
+    const int32_t p = perm[i];
+    coeff_s[i] = coeff[p];
+    slot_s[i] = cslot[p];
   }
 }
 
@@ -721,7 +732,8 @@ static int build_plan(gg_ctx *ctx, gg_hmat *h, Lists &L) {
   }
   if (ncontr) {
     k_scatter_perm<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, L.pOff.p, fill.p, perm.p); ::gg::note_launch();
-    k_sort_gather<<<gblocks, 256, 0, s>>>(L.pOff.p, nnz, perm.p, L.dCoeff.p, cslot.p, L.pCoeff.p, L.pSlot.p);
+    k_sort_gather<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(L.pOff.p, nnz, perm.p, L.dCoeff.p, cslot.p,
+                                                                L.pCoeff.p, L.pSlot.p);
     ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
