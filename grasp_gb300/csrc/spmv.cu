@@ -49,6 +49,7 @@ __global__ void k_cursor(const int *__restrict__ cnt, int ncf, int nch, const in
                          int *__restrict__ cursor) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncf; c += gridDim.x * blockDim.x) {
     int pos = (int)(iendc[c + 1] - iendc[c]);  // the row's own entries come first
+#pragma unroll 8
     for (int ch = 0; ch < nch; ++ch) {
       cursor[(size_t)ch * ncf + c] = pos;
       pos += cnt[(size_t)ch * ncf + c];
@@ -60,6 +61,7 @@ __global__ void k_tcol_total(const int *__restrict__ cnt, int ncf, int nch, cons
                              int64_t *__restrict__ rowlen) {
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncf; c += gridDim.x * blockDim.x) {
     int64_t t = iendc[c + 1] - iendc[c];
+#pragma unroll 8
     for (int ch = 0; ch < nch; ++ch) t += cnt[(size_t)ch * ncf + c];
     rowlen[c] = t;
   }
@@ -102,27 +104,41 @@ __global__ void k_own(const int64_t *__restrict__ iendc, const int32_t *__restri
   }
 }
 
-__global__ void k_rowlen_scan(const int64_t *__restrict__ rowlen, int n, int64_t *__restrict__ ptr) {
-  // single block scan (n up to a few million rows is fine for a one-time build)
-  __shared__ long long s[1024];
-  long long base = 0;
-  for (int i0 = 0; i0 < n; i0 += blockDim.x) {
-    const int i = i0 + threadIdx.x;
-    const long long v = (i < n) ? rowlen[i] : 0;
-    s[threadIdx.x] = v;
-    __syncthreads();
-    for (int w = 1; w < (int)blockDim.x; w <<= 1) {
-      const long long t = ((int)threadIdx.x >= w) ? s[threadIdx.x - w] : 0;
-      __syncthreads();
-      s[threadIdx.x] += t;
-      __syncthreads();
-    }
-    if (i < n) ptr[i] = base + s[threadIdx.x] - v;
-    const long long tot = s[blockDim.x - 1];
-    __syncthreads();
-    base += tot;
+// exclusive scan of the row lengths into ptr[0..n] by one CTA of 1024
+// threads: thread t sums its contiguous slice, the slice sums are scanned
+// with warp shuffles, then each thread writes its slice's prefix
+__global__ void __launch_bounds__(1024) k_rowlen_scan(const int64_t *__restrict__ rowlen, int n,
+                                                      int64_t *__restrict__ ptr) {
+  __shared__ long long wsum[32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const int per = (n + 1023) / 1024;
+  const int i0 = min(n, t * per), i1 = min(n, i0 + per);
+  long long my = 0;
+  for (int i = i0; i < i1; ++i) my += rowlen[i];
+  long long x = my;  // inclusive scan within the warp
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
   }
-  if (threadIdx.x == 0) ptr[n] = base;
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    long long v = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += y;
+    }
+    wsum[lane] = v;  // inclusive over warps
+  }
+  __syncthreads();
+  long long base = x - my + (w > 0 ? wsum[w - 1] : 0);
+  for (int i = i0; i < i1; ++i) {
+    ptr[i] = base;
+    base += rowlen[i];
+  }
+  if (t == 1023) ptr[n] = x + (w > 0 ? wsum[w - 1] : 0);
 }
 
 // values: FP64 copy and the hi/lo split (diagonal excluded from the split)
