@@ -91,6 +91,33 @@ __global__ void k_tplace(const int64_t *__restrict__ iendc, const int32_t *__res
     __syncthreads();
   }
 }
+// k_tplace with the chunk's cursor row in shared memory (NCF ints): the
+// per-entry read-modify-write of the cursor stays on chip
+constexpr int TPLACE_SMEM_MAX = 200 * 1024;
+__global__ void k_tplace_smem(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow,
+                              const int *__restrict__ chunk_r0, int ncf, const int64_t *__restrict__ symptr,
+                              const int *__restrict__ cursor, int32_t *__restrict__ scol,
+                              int64_t *__restrict__ ssrc) {
+  extern __shared__ int cur[];
+  const int ch = blockIdx.x;
+  const int r0 = chunk_r0[ch], r1 = chunk_r0[ch + 1];
+  if (r0 == r1) return;
+  const int *c0 = cursor + (size_t)ch * ncf;
+  for (int c = threadIdx.x; c < ncf; c += blockDim.x) cur[c] = c0[c];
+  __syncthreads();
+  for (int r = r0; r < r1; ++r) {
+    const int64_t lo = iendc[r], hi = iendc[r + 1] - 1;
+    for (int64_t p = lo + threadIdx.x; p < hi; p += blockDim.x) {
+      const int c = irow[p] - 1;
+      const int q = cur[c];
+      cur[c] = q + 1;
+      const int64_t pos = symptr[c] + q;
+      scol[pos] = r;
+      ssrc[pos] = p;
+    }
+    __syncthreads();
+  }
+}
 
 __global__ void k_own(const int64_t *__restrict__ iendc, const int32_t *__restrict__ irow, int ncf,
                       const int64_t *__restrict__ symptr, int32_t *__restrict__ scol, int64_t *__restrict__ ssrc) {
@@ -452,8 +479,16 @@ int build_sym(gg_hmat *h) {
   GG_TRY(cursor.alloc((size_t)nch * ncf));
   k_cursor<<<(ncf + 255) / 256, 256, 0, s>>>(cnt.p, ncf, nch, h->dIendc.p, cursor.p); ::gg::note_launch();
   k_own<<<(ncf * 32 + 255) / 256, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, ncf, h->dSymPtr.p, h->dSymCol.p, h->dSymSrc.p); ::gg::note_launch();
-  k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, h->dSymPtr.p, cursor.p, h->dSymCol.p,
-                               h->dSymSrc.p); ::gg::note_launch();
+  if ((size_t)ncf * sizeof(int) <= (size_t)TPLACE_SMEM_MAX) {
+    const int smem = ncf * (int)sizeof(int);
+    GG_CUDA(cudaFuncSetAttribute(k_tplace_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    k_tplace_smem<<<nch, 1024, smem, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, h->dSymPtr.p, cursor.p,
+                                           h->dSymCol.p, h->dSymSrc.p);
+  } else {
+    k_tplace<<<nch, 256, 0, s>>>(h->dIendc.p, h->dIrow.p, dr0.p, ncf, h->dSymPtr.p, cursor.p, h->dSymCol.p,
+                                 h->dSymSrc.p);
+  }
+  ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   if (ncf <= 65536) {
     GG_TRY(h->dSymCol16.alloc(h->sym_nnz));
