@@ -447,7 +447,7 @@ int gg_hmat_create(gg_ctx *ctx, int ncf, int64_t nnz, const int64_t *iendc, cons
   if (s == GG_OK) s = h->dEmt.alloc(nnz);
   if (s == GG_OK) s = h->dDiag.alloc(ncf);
   // IROW checked on the device (diagonal last in each row: the
-  // lower-triangle-by-rows mode of spicmv2.f90), the verdict read back here
+  // lower-triangle-by-rows mode of spicmv2.f90), the result read back here
   DBuf<unsigned long long> dbad;
   unsigned long long hbad[1] = {~0ull};
   if (s == GG_OK) s = upload(dbad, hbad, 1, ctx->stream);

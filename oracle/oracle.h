@@ -6,7 +6,7 @@
  * legs of bench.py may load it. It is never part of the product path.
  *
  * Every routine restates one reference subroutine, loop by loop, in FP64.
- * The reference (GRASP2018, Fortran 90) cannot be compiled in this build
+ * The reference (GRASP2018, Fortran 90) cannot be compiled in this
  * environment (no Fortran compiler), so parity is pinned by the reference's
  * own QUAD known-answer test (test/lib9290_quad.f90:22-33) and by analytic
  * hydrogenic known answers; see tests/test_oracle_kat.py.

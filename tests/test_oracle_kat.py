@@ -99,7 +99,7 @@ def test_slater_symmetries(oracle_mod):
             # numbers: it integrates rho_bd Y_ac instead of rho_ac Y_bd with the
             # MTP cut of slater.f90:56-60, and for k = 0 with b != d YZK forces
             # the asymptote of Z to 0 (yzk.f90:154-158) even when b and d differ
-            # only in j. GENINTRK fixes the order (a <= b) and so does this build.
+            # only in j. GENINTRK fixes the order (a <= b) and so does this library.
             assert o.slater(c, b, a, d, k) == v and o.slater(a, d, c, b, k) == v
             checked += 1
 
