@@ -12,6 +12,9 @@ int32, REAL*8 is float64, LOGICAL is 4 bytes).
                 rmcdhf90/setham.f90:223-341)
   rwfn          radial wavefunctions (lib9290/lodrwf.f90:100-108)
   .cm / .mix    mixing coefficients (rci90/matrix.f90:209-212, lodmix.f90:75)
+  rci.res       rci's run parameters and stored Hamiltonian rows, with rci's
+                element filter (rci90/setres.f90:105, getcid.f90:284-314,
+                genmat.f90:117, setham_gg.f90:364-378; lodres.f90:58-101)
 
 The coefficient lists convert to and from the label-grouped arrays that
 :meth:`grasp_gb300.HMatrix.setham` takes (dicts of lab/start/loc/coeff).
@@ -332,6 +335,217 @@ def write_mix(path, m: MixFile):
             ff.write_record(np.asarray(b.ivec, _I4))
             ff.write_record(np.concatenate([[b.eav], np.asarray(b.eval, _F8)]).astype(_F8))
             ff.write_record(np.asarray(b.evec, _F8).T.copy())
+
+
+# ---------------------------------------------------------------------------
+# rci.res (rci's run parameters and Hamiltonian rows)
+# ---------------------------------------------------------------------------
+
+# rci stores an off-diagonal element only if |H| > CUTOFF (rci90/setham_gg.f90:364)
+RCI_CUTOFF = 1.0e-12
+
+
+@dataclass
+class ResOrbital:
+    e: float
+    gama: float
+    pz: float
+    p: np.ndarray                       # PF(1:MF)
+    q: np.ndarray                       # QF(1:MF)
+
+
+@dataclass
+class ResHeader:
+    """Records 1-7 + 2 NW of rci.res (rci90/setres.f90:105, getcid.f90:284-314;
+    read back by rci90/lodres.f90:58-101)."""
+    nelec: int
+    ncf: int                            # all blocks
+    nw: int
+    z: float
+    emn: float
+    parm: np.ndarray                    # PARM(1:NPARM)
+    zz: np.ndarray                      # ZZ(1:N)
+    nnuc: int
+    c: float
+    lfordr: bool
+    iccut: list                         # ICCUTblk, one per block
+    ltrans: bool
+    wfact: float
+    lvp: bool
+    lnms: bool
+    lsms: bool
+    rnt: float
+    h: float
+    hp: float
+    r: np.ndarray                       # R, RP, RPOR: N + 10 points each
+    rp: np.ndarray
+    rpor: np.ndarray
+    orbitals: list                      # ResOrbital, NW of them
+
+
+@dataclass
+class ResBlock:
+    """One block's rows as rci writes them (rci90/genmat.f90:117,
+    setham_gg.f90:378): the rows held by rank myid of nprocs (rows myid+1,
+    myid+1+nprocs, ...), each lower-triangle row with its diagonal last.
+    iendc/irow/emt are those rows in the CSR-lower layout of hmat_C; an
+    interrupted run leaves fewer rows than res_rows(ncf, myid, nprocs)."""
+    ncf: int
+    iccut: int
+    iendc: np.ndarray                   # int64 [rows + 1]
+    irow: np.ndarray                    # int32, 1-based
+    emt: np.ndarray                     # float64, without ELSTO
+    elsto: float = 0.0
+    myid: int = 0
+    nprocs: int = 1
+
+
+def res_rows(ncf, myid=0, nprocs=1):
+    """Rows of a block that rank myid owns (rci90/genmat.f90:97-98)."""
+    if ncf < nprocs:
+        return ncf // (myid + 1)
+    return (ncf - myid - 1 + nprocs) // nprocs
+
+
+def rci_filter(iendc, irow, emt, cutoff=RCI_CUTOFF):
+    """The rows rci stores for an assembled block: every diagonal element and
+    the off-diagonal ones with |H| > cutoff (rci90/setham_gg.f90:364-368).
+    Takes and returns the CSR-lower layout (IENDC with IENDC(0) = 0, 1-based
+    IROW, diagonal last in each row); order within a row is kept."""
+    iendc = np.asarray(iendc, np.int64)
+    irow = np.asarray(irow, np.int32)
+    emt = np.asarray(emt, np.float64)
+    ncf = iendc.size - 1
+    row_of = np.repeat(np.arange(1, ncf + 1, dtype=np.int64), np.diff(iendc))
+    keep = (irow == row_of) | (np.abs(emt) > cutoff)
+    kept_before = np.concatenate([[0], np.cumsum(keep, dtype=np.int64)])
+    return kept_before[iendc], irow[keep].copy(), emt[keep].copy()
+
+
+def res_eav(block: ResBlock):
+    """EAV of a block whose rows are all present: the diagonal mean plus
+    ELSTO (rci90/setham_gg.f90:382, genmat2.f90:36)."""
+    diag = block.emt[block.iendc[1:] - 1]
+    return float(diag.sum()) / block.ncf + block.elsto
+
+
+def res_to_hmat(block: ResBlock, eav):
+    """(iendc, irow, emt) with the diagonal shifted by -EAV, as rci's MANEIG
+    loads rci.res into core (rci90/maneig.f90:318-330): the arrays
+    HMatrix(ctx, ncf, iendc, irow) and HMatrix.set_emt take. The eigenvalues
+    of that matrix plus EAV are rci's; plus ELSTO once more where rci adds it
+    (rci90/matrix.f90:197-201)."""
+    if block.nprocs != 1 or block.iendc.size - 1 != block.ncf:
+        raise ValueError("a block's rows are all needed (one rank, no interrupted rows)")
+    emt = block.emt.copy()
+    emt[block.iendc[1:] - 1] -= eav
+    return block.iendc.copy(), block.irow.copy(), emt
+
+
+def _write_res_header(ff, hd: ResHeader):
+    n = hd.zz.size
+    ff.write_record(b"R92RES")
+    ff.write_record(_i4(hd.nelec, hd.ncf, hd.nw, len(hd.iccut)))
+    ff.write_record(np.array([hd.z, hd.emn], _F8))
+    ff.write_record(_i4(len(hd.parm)), np.asarray(hd.parm, _F8))
+    ff.write_record(_i4(n), np.asarray(hd.zz, _F8), _i4(hd.nnuc))
+    ff.write_record(np.array([hd.c], _F8), _i4(int(hd.lfordr)), np.asarray(hd.iccut, _I4), _i4(int(hd.ltrans)),
+                    np.array([hd.wfact], _F8), _i4(int(hd.lvp), int(hd.lnms), int(hd.lsms)))
+    for a in (hd.r, hd.rp, hd.rpor):
+        if np.asarray(a).size != n + 10:
+            raise ValueError("R, RP and RPOR hold N + 10 points")
+    ff.write_record(np.array([hd.rnt, hd.h, hd.hp], _F8), np.asarray(hd.r, _F8), np.asarray(hd.rp, _F8),
+                    np.asarray(hd.rpor, _F8))
+    if len(hd.orbitals) != hd.nw:
+        raise ValueError("NW orbitals expected")
+    for o in hd.orbitals:
+        ff.write_record(np.array([o.e, o.gama, o.pz], _F8), _i4(np.asarray(o.p).size))
+        ff.write_record(np.asarray(o.p, _F8), np.asarray(o.q, _F8))
+
+
+def _read_res_header(ff) -> ResHeader:
+    if ff.read_record()[:6] != b"R92RES":
+        raise ValueError("not an RCI92 .res file")
+    nelec, ncf, nw, nblock = (int(x) for x in np.frombuffer(ff.read_record(), _I4))
+    z, emn = np.frombuffer(ff.read_record(), _F8)
+    r = ff.read_record()
+    (nparm,) = np.frombuffer(r[:4], _I4)
+    parm = np.frombuffer(r[4:4 + 8 * nparm], _F8).copy()
+    r = ff.read_record()
+    (n,) = np.frombuffer(r[:4], _I4)
+    zz = np.frombuffer(r[4:4 + 8 * n], _F8).copy()
+    (nnuc,) = np.frombuffer(r[4 + 8 * n:8 + 8 * n], _I4)
+    r = ff.read_record()
+    (c,) = np.frombuffer(r[:8], _F8)
+    (lfordr,) = np.frombuffer(r[8:12], _I4)
+    iccut = [int(x) for x in np.frombuffer(r[12:12 + 4 * nblock], _I4)]
+    o = 12 + 4 * nblock
+    (ltrans,) = np.frombuffer(r[o:o + 4], _I4)
+    (wfact,) = np.frombuffer(r[o + 4:o + 12], _F8)
+    lvp, lnms, lsms = np.frombuffer(r[o + 12:o + 24], _I4)
+    d = np.frombuffer(ff.read_record(), _F8)
+    np10 = n + 10
+    rnt, h, hp = d[:3]
+    grid = [d[3 + i * np10:3 + (i + 1) * np10].copy() for i in range(3)]
+    orbs = []
+    for _ in range(nw):
+        r = ff.read_record()
+        e, gama, pz = np.frombuffer(r[:24], _F8)
+        (mf,) = np.frombuffer(r[24:28], _I4)
+        pq = np.frombuffer(ff.read_record(), _F8)
+        orbs.append(ResOrbital(float(e), float(gama), float(pz), pq[:mf].copy(), pq[mf:2 * mf].copy()))
+    return ResHeader(nelec, ncf, nw, float(z), float(emn), parm, zz, int(nnuc), float(c), bool(lfordr), iccut,
+                     bool(ltrans), float(wfact), bool(lvp), bool(lnms), bool(lsms), float(rnt), float(h), float(hp),
+                     grid[0], grid[1], grid[2], orbs)
+
+
+def write_res(path, header: ResHeader, blocks):
+    """rci.res: the header records, then per block its (NCF, ICCUT, MYID,
+    NPROCS) record and one record (NELC, ELSTO, EMT(1:NELC), IROW(1:NELC))
+    per row held (rci90/genmat.f90:117, setham_gg.f90:378)."""
+    if len(blocks) != len(header.iccut):
+        raise ValueError("one ICCUT per block")
+    with FortranFile(path, "wb") as ff:
+        _write_res_header(ff, header)
+        for b in blocks:
+            ff.write_record(_i4(b.ncf, b.iccut, b.myid, b.nprocs))
+            iendc = np.asarray(b.iendc, np.int64)
+            if iendc.size - 1 > res_rows(b.ncf, b.myid, b.nprocs):
+                raise ValueError("more rows than the rank owns")
+            for i in range(iendc.size - 1):
+                s, e = int(iendc[i]), int(iendc[i + 1])
+                ff.write_record(_i4(e - s), np.array([b.elsto], _F8), np.asarray(b.emt[s:e], _F8),
+                                np.asarray(b.irow[s:e], _I4))
+
+
+def read_res(path):
+    """(ResHeader, [ResBlock]) from rci.res. A block's rows end where its
+    rank's rows end or where the file ends (an interrupted run, which rci
+    resumes from, rci90/genmat.f90:69-87)."""
+    with FortranFile(path) as ff:
+        hd = _read_res_header(ff)
+        blocks = []
+        for _ in range(len(hd.iccut)):
+            try:
+                r = ff.read_record()
+            except EOFError:
+                break
+            ncf, iccut, myid, nprocs = (int(x) for x in np.frombuffer(r, _I4))
+            lens, irows, emts, elsto = [0], [], [], 0.0
+            for _ in range(res_rows(ncf, myid, nprocs)):
+                try:
+                    r = ff.read_record()
+                except EOFError:
+                    break
+                (nelc,) = np.frombuffer(r[:4], _I4)
+                (elsto,) = np.frombuffer(r[4:12], _F8)
+                emts.append(np.frombuffer(r[12:12 + 8 * nelc], _F8))
+                irows.append(np.frombuffer(r[12 + 8 * nelc:12 + 12 * nelc], _I4))
+                lens.append(int(nelc))
+            blocks.append(ResBlock(ncf, iccut, np.cumsum(lens).astype(np.int64),
+                                   np.concatenate(irows).astype(np.int32) if irows else np.zeros(0, np.int32),
+                                   np.concatenate(emts) if emts else np.zeros(0), float(elsto), myid, nprocs))
+    return hd, blocks
 
 
 def exists(path):

@@ -161,3 +161,158 @@ def test_reference_files_round_trip_bytes(tmp_path):
         else:
             F.write_mix(out, F.read_mix(path))
         assert out.read_bytes() == open(path, "rb").read(), path
+
+
+# ---------------------------------------------------------------------------
+# rci.res
+# ---------------------------------------------------------------------------
+
+def _res_header(case, nblock, nw):
+    n = case["n"]
+    ob = case["orb"]
+    pad = np.linspace(1.0, 2.0, 10)
+    r = np.concatenate([np.exp(np.arange(n) * case["h"]) - 1.0, pad])
+    orbs = [F.ResOrbital(-float(ob.e[j]), 1.0, 2.5 + j, ob.pf[j, :ob.mf[j]].copy(), ob.qf[j, :ob.mf[j]].copy())
+            for j in range(nw)]
+    return F.ResHeader(nelec=4, ncf=0, nw=nw, z=10.0, emn=20.18, parm=np.array([2.9, 0.52]), zz=case["zz"][:n].copy(),
+                       nnuc=1, c=case["c"], lfordr=False, iccut=[0] * nblock, ltrans=False, wfact=1e-6, lvp=False,
+                       lnms=False, lsms=False, rnt=case["rnt"], h=case["h"], hp=0.0, r=r, rp=r + 1.0, rpor=r * 0.5,
+                       orbitals=orbs)
+
+
+def _row_loop_filter(iendc, irow, emt, cutoff):
+    """rci90/setham_gg.f90:364-368, row by row: an element is stored if it is
+    on the diagonal or |ELEMNT| > CUTOFF."""
+    out_iendc, out_irow, out_emt = [0], [], []
+    for ic in range(1, iendc.size):
+        for p in range(iendc[ic - 1], iendc[ic]):
+            if irow[p] == ic or abs(emt[p]) > cutoff:
+                out_irow.append(irow[p])
+                out_emt.append(emt[p])
+        out_iendc.append(len(out_irow))
+    return np.array(out_iendc, np.int64), np.array(out_irow, np.int32), np.array(out_emt)
+
+
+def test_rci_filter_matches_row_loop(oracle_mod):
+    """The element filter on an assembled Ne VII block with planted small
+    elements: exactly CUTOFF (dropped), just above it (kept), tiny negative
+    values, zeros, and a zero diagonal (always kept). Bit-exact."""
+    case = hydrogenic_case(nmax=4, lmax=3, z=10.0)
+    _, blk = ne7_block()
+    o = oracle_for(case)
+    o.genintrk()
+    emt = o.setham(blk.ncf, blk.nnz, blk.iendc, blk.iq, blk.tlist, blk.vlists)
+    rng = np.random.default_rng(5)
+    off = np.setdiff1d(np.arange(blk.nnz), blk.iendc[1:] - 1)
+    pick = rng.choice(off, size=min(40, off.size), replace=False)
+    emt[pick[:8]] = F.RCI_CUTOFF
+    emt[pick[8:16]] = -F.RCI_CUTOFF
+    emt[pick[16:24]] = np.nextafter(F.RCI_CUTOFF, 1.0)
+    emt[pick[24:32]] = -3e-13
+    emt[pick[32:]] = 0.0
+    emt[blk.iendc[3] - 1] = 0.0
+    got = F.rci_filter(blk.iendc, blk.irow, emt)
+    want = _row_loop_filter(np.asarray(blk.iendc), np.asarray(blk.irow), emt, F.RCI_CUTOFF)
+    for g, w in zip(got, want):
+        np.testing.assert_array_equal(g, w)
+    assert got[0][-1] == blk.nnz - np.count_nonzero(np.abs(emt[off]) <= F.RCI_CUTOFF)
+    assert np.count_nonzero(np.abs(emt[off]) <= F.RCI_CUTOFF) >= 8 + 8 + 8 + len(pick[32:])
+    # every row keeps its diagonal, last
+    assert np.all(got[1][got[0][1:] - 1] == np.arange(1, blk.ncf + 1))
+    assert np.count_nonzero(np.abs(got[2][np.setdiff1d(np.arange(got[0][-1]), got[0][1:] - 1)]) <= F.RCI_CUTOFF) == 0
+
+
+def test_res_round_trip_and_record_layout(tmp_path, oracle_mod):
+    case = hydrogenic_case(nmax=4, lmax=3, z=10.0)
+    _, blk = ne7_block()
+    o = oracle_for(case)
+    o.genintrk()
+    emt = o.setham(blk.ncf, blk.nnz, blk.iendc, blk.iq, blk.tlist, blk.vlists)
+    iendc, irow, emtf = F.rci_filter(blk.iendc, blk.irow, emt)
+    hd = _res_header(case, 2, case["orb"].nw)
+    hd.ncf = blk.ncf + 3
+    small = F.ResBlock(3, 0, np.array([0, 1, 3, 6], np.int64), np.array([1, 1, 2, 1, 2, 3], np.int32),
+                       np.array([-1.0, 0.5, -2.0, 0.25, 0.125, -3.0]), elsto=-7.5)
+    blocks = [F.ResBlock(blk.ncf, 0, iendc, irow, emtf, elsto=-7.5), small]
+    p = tmp_path / "rci.res"
+    F.write_res(p, hd, blocks)
+    hd2, back = F.read_res(p)
+    for key in ("nelec", "ncf", "nw", "z", "emn", "nnuc", "c", "lfordr", "iccut", "ltrans", "wfact", "lvp", "lnms",
+                "lsms", "rnt", "h", "hp"):
+        assert getattr(hd2, key) == getattr(hd, key), key
+    for key in ("parm", "zz", "r", "rp", "rpor"):
+        np.testing.assert_array_equal(getattr(hd2, key), getattr(hd, key))
+    for a, b in zip(hd2.orbitals, hd.orbitals):
+        assert (a.e, a.gama, a.pz) == (b.e, b.gama, b.pz)
+        np.testing.assert_array_equal(a.p, b.p)
+        np.testing.assert_array_equal(a.q, b.q)
+    for a, b in zip(back, blocks):
+        assert (a.ncf, a.iccut, a.myid, a.nprocs, a.elsto) == (b.ncf, b.iccut, b.myid, b.nprocs, b.elsto)
+        np.testing.assert_array_equal(a.iendc, b.iendc)
+        np.testing.assert_array_equal(a.irow, b.irow)
+        np.testing.assert_array_equal(a.emt, b.emt)
+    # the bytes of the file again, and the small block's records at its end:
+    # (NCF, ICCUT, MYID, NPROCS), then (NELC, ELSTO, EMT(1:NELC), IROW(1:NELC)) per row
+    F.write_res(tmp_path / "again", hd2, back)
+    raw = p.read_bytes()
+    assert (tmp_path / "again").read_bytes() == raw
+    row3 = (np.array([3], "<i4").tobytes() + np.array([-7.5, 0.25, 0.125, -3.0], "<f8").tobytes()
+            + np.array([1, 2, 3], "<i4").tobytes())
+    framed = len(row3).to_bytes(4, "little") + row3 + len(row3).to_bytes(4, "little")
+    assert raw.endswith(framed)
+    head = np.array([3, 0, 0, 1], "<i4").tobytes()
+    assert (len(head).to_bytes(4, "little") + head + len(head).to_bytes(4, "little")) in raw
+
+
+def test_res_eav_and_shifted_matrix(oracle_mod):
+    """EAV = diagonal mean + ELSTO (rci90/genmat2.f90:36) and the in-core
+    matrix with its diagonal shifted by EAV (rci90/maneig.f90:318-330): its
+    eigenvalues + EAV are those of the unfiltered H + ELSTO to rounding (the
+    dropped elements are at most 1e-12 each)."""
+    case = hydrogenic_case(nmax=4, lmax=3, z=10.0)
+    _, blk = ne7_block()
+    o = oracle_for(case)
+    o.genintrk()
+    emt = o.setham(blk.ncf, blk.nnz, blk.iendc, blk.iq, blk.tlist, blk.vlists)
+    iendc, irow, emtf = F.rci_filter(blk.iendc, blk.irow, emt)
+    b = F.ResBlock(blk.ncf, 0, iendc, irow, emtf, elsto=-2.0)
+    eav = F.res_eav(b)
+    diag = emt[np.asarray(blk.iendc)[1:] - 1]
+    assert eav == pytest.approx(diag.mean() - 2.0, abs=1e-12)
+    i2, r2, e2 = F.res_to_hmat(b, eav)
+
+    def dense(iendc_, irow_, v):
+        a = np.zeros((blk.ncf, blk.ncf))
+        for ic in range(blk.ncf):
+            for p in range(iendc_[ic], iendc_[ic + 1]):
+                a[ic, irow_[p] - 1] = a[irow_[p] - 1, ic] = v[p]
+        return a
+
+    w_shift = np.linalg.eigvalsh(dense(i2, r2, e2))[:5] + eav + b.elsto  # rci90/matrix.f90:197-201
+    w_full = np.linalg.eigvalsh(dense(np.asarray(blk.iendc), np.asarray(blk.irow), emt))[:5] - 2.0
+    assert np.abs(w_shift - w_full).max() <= 1e-10
+    with pytest.raises(ValueError):
+        F.res_to_hmat(F.ResBlock(3, 0, np.array([0, 1], np.int64), np.array([1], np.int32), np.array([1.0])), 0.0)
+
+
+def test_res_rank_rows_and_interrupted_file(tmp_path):
+    """Rows per rank (rci90/genmat.f90:97-98) and a file that ends inside a
+    block's rows, as an interrupted rci run leaves it: the rows present are
+    read and the block is short."""
+    assert [F.res_rows(10, r, 3) for r in range(3)] == [4, 3, 3]
+    assert F.res_rows(2, 0, 4) == 2 and F.res_rows(2, 1, 4) == 1
+    case = hydrogenic_case(nmax=2, lmax=1, z=10.0)
+    hd = _res_header(case, 1, case["orb"].nw)
+    iendc = np.array([0, 1, 3, 5, 8], np.int64)
+    irow = np.array([1, 1, 2, 2, 3, 1, 3, 4], np.int32)
+    emt = np.arange(1.0, 9.0)
+    p = tmp_path / "rci.res"
+    F.write_res(p, hd, [F.ResBlock(4, 0, iendc, irow, emt)])
+    raw = p.read_bytes()
+    last = 4 + 4 + 8 + 3 * 12 + 4
+    (tmp_path / "cut.res").write_bytes(raw[:-last])
+    _, blocks = F.read_res(tmp_path / "cut.res")
+    np.testing.assert_array_equal(blocks[0].iendc, iendc[:4])
+    np.testing.assert_array_equal(blocks[0].emt, emt[:5])
+    with pytest.raises(ValueError):
+        F.write_res(tmp_path / "x", hd, [F.ResBlock(4, 0, iendc, irow, emt, myid=1, nprocs=2)])
