@@ -254,3 +254,24 @@ def test_maneig_alternative_kernels(gpu_ready, oracle_mod, monkeypatch, env):
         ev, vec, info = H.maneig(3, flavour=0, precision=precision, robust=True)
         assert np.abs(ev - ev0).max() <= 1e-9
         assert np.abs(vec - vec0).max() <= 1e-7
+
+
+@pytest.mark.parametrize("flavour", [0, 1])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_maneig_tiny_blocks(gpu_ready, oracle_mod, flavour, precision):
+    """Blocks of 1, 2 and 5 CSFs with NVEC = NCF: the trivial NCF = 1 case
+    (rci90/maneig.f90:122-137) and Davidson in the full unit basis, for both
+    MANEIG flavours and both matvec precisions, against the oracle's MANEIG."""
+    import oracle
+    from grasp_gb300 import Context, workloads as W
+    ctx = Context(0)
+    for c in (1, 2, 5):
+        w = W.batch(zs=(10,), two_js=(0,), parities=(0,), max_ncf=c)
+        (H,) = W.assemble_batch(w, ctx)
+        b = w.blocks[0][2]
+        assert b.ncf == c
+        ev, vec, info = H.maneig(c, flavour=flavour, precision=precision)
+        ev0, vec0, _ = oracle.maneig(flavour, b.ncf, c, b.iendc, b.irow, H.emt())
+        assert info["ierr"] == 0
+        assert np.abs(ev - ev0).max() <= 1e-9, (c, ev, ev0)
+        assert np.abs(vec - vec0).max() <= 1e-7, c
