@@ -2325,7 +2325,7 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   std::vector<double> ROWLAST(LIM + 2, 0.0);
   // INITDVD (dvdson.f90:848-948) with NUME + 1
   {
-    const int NUME1 = NUME + 1;
+    const int NUME1 = std::min(NUME + 1, LIM);  // no more vectors than the basis holds
     int IST = 1, IEND = NIV, NEW = NIV;
     for (;;) {
       GG_TRY(D.op(IST - 1, NEW));
@@ -2356,7 +2356,8 @@ int dvdson(Dvd &D, const DvdParams &P, std::vector<double> &eigval_out, std::vec
   std::vector<double> w, hlo, hhi;
   int kprev = -1, mprev = 0;  // size of S and number of eigenvalues at the previous solve
   for (;;) {
-    const int IFIND = std::min(KPASS, REST);
+    // with the whole space in the basis every Ritz pair is exact: take all
+    const int IFIND = (KPASS == n) ? KPASS : std::min(KPASS, REST);
     for (int i = 0; i < IFIND; ++i) OLDVAL[i] = EIGVAL[i];
     // DSPEVX returns IFIND eigenpairs. Read afterwards are EIGVAL(1:NUME+1)
     // (TSTSEL, NEWVEC's GAP) and the first NUME eigenvectors (TSTSEL,
@@ -2729,7 +2730,10 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   }
   if (p && p->lim > 0) P.lim = std::min(ncf, p->lim);
   if (p && p->maxiter > 0) P.maxiter = p->maxiter;
-  if (P.lim < nvec + 1 && P.lim != ncf) return fail(GG_ERR_ARG, "gg_maneig: LIM too small");
+  // DVDSON keeps REST = min(max(LIM/2, 2 NUME), LIM - 3) Ritz vectors and
+  // reads NUME + 1 of them: LIM >= NUME + 4 unless the basis holds the
+  // whole space (LIM = NCF, solved in the full unit basis below)
+  if (P.lim < nvec + 4 && P.lim != ncf) return fail(GG_ERR_ARG, "gg_maneig: LIM too small (below NVEC + 4)");
   if (P.lim > 1024) return fail(GG_ERR_ARG, "gg_maneig: LIM above 1024 is not supported");
   GG_TRY(refresh_sym_values(h));
   std::vector<double> ev, res;
@@ -2796,7 +2800,12 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     GG_TRY(workspace(0, blk, ns, P1.lim, &D1p));
     Dvd &D1 = *D1p;
     GG_CUDA(cudaMemcpyAsync(D1.diag.p, blk->dDiag.p, ns * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-    GG_TRY(unit_start(D1, blk, nvec));
+    // A block too small for DVDSON's restart size (NCF < NVEC + 4; the
+    // reference solves such blocks densely, rci90/maneig.f90:157-241,
+    // rmcdhf90/maneig.f90:104-120) starts from all NCF unit vectors: S is
+    // then the whole matrix and its eigenpairs are exact after one pass.
+    if (P1.lim == ns && ns < nvec + 4) P1.niv = ns;
+    GG_TRY(unit_start(D1, blk, P1.niv));
     int nl = 0, ie = 0;
     GG_TRY(dvdson(D1, P1, ev, res, &nl, &ie));
     mv_ms += D1.mv_ms;
