@@ -177,14 +177,18 @@ int gg_spicmv2(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c, int p
  * dvdson.f90:1) with the reference's constants: CRITE 1e-17, CRITC = CRITR
  * = 1e-9, MBLOCK 1, LIM/MAXITR per flavour. Where the reference uses dense
  * DSPEVX (rci, ncf <= 2000), this library runs the same Davidson to the
- * same tolerances. Initial estimates follow INIEST2
+ * same tolerances; a block with NCF < NVEC + 4 is solved in its full unit
+ * basis (one projected eigenproblem of the whole matrix). Initial estimates
+ * follow INIEST2
  * (lib9290/iniest2.f90:3): the lowest eigenvectors of the leading
  * min(nmax, ncf) block.
  * eval[nvec] (relative to EAV), evec[ncf x nvec] column-major.             */
 typedef struct {
   int flavour;    /* 0 = rci, 1 = rmcdhf */
   int precision;  /* gg_precision of the matvec */
-  int lim;        /* <= 0: reference default */
+  int lim;        /* <= 0: reference default; else NCF or at least NVEC + 4
+                     (DVDSON's restart keeps min(max(LIM/2, 2 NVEC), LIM - 3)
+                     vectors and needs NVEC + 1 of them) */
   int maxiter;    /* <= 0: reference default */
   double critr;   /* <= 0: 1e-9 */
   double critc;   /* <= 0: 1e-9 */
