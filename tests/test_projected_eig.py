@@ -67,3 +67,28 @@ def test_projected_eig_rejects_bad_sizes():
         projected_eig(np.eye(3), 4)
     with pytest.raises(GGError):
         projected_eig(np.eye(3), 2, 3)
+
+
+@pytest.mark.parametrize("n,seed", [(12, 8), (41, 9)])
+def test_projected_eig_trivial_reflectors(n, seed):
+    """Columns that are already reduced (zero below the subdiagonal), so some
+    Householder steps have nothing to do: a block-diagonal matrix with
+    diagonal and tridiagonal blocks."""
+    _lib_or_skip()
+    from grasp_gb300.core import projected_eig
+    rng = np.random.default_rng(seed)
+    s = np.zeros((n, n))
+    h = n // 3
+    a = rng.normal(size=(h, h))
+    s[:h, :h] = a + a.T
+    s[h:2 * h, h:2 * h] = np.diag(rng.normal(size=h))
+    t = 2 * h
+    d = rng.normal(size=n - t)
+    e = rng.normal(size=n - t - 1)
+    s[t:, t:] = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    w, z = projected_eig(s, n // 2, n // 2 - 1)
+    w0 = np.linalg.eigvalsh(s)
+    norm = np.abs(w0).max()
+    assert np.abs(w - w0[:n // 2]).max() <= 1e-12 * norm
+    assert np.abs(s @ z - z * w[:n // 2 - 1]).max() <= 1e-11 * norm
+    assert np.abs(z.T @ z - np.eye(n // 2 - 1)).max() <= 1e-12
