@@ -316,3 +316,43 @@ def test_res_rank_rows_and_interrupted_file(tmp_path):
     np.testing.assert_array_equal(blocks[0].emt, emt[:5])
     with pytest.raises(ValueError):
         F.write_res(tmp_path / "x", hd, [F.ResBlock(4, 0, iendc, irow, emt, myid=1, nprocs=2)])
+
+
+def test_mcp_two_blocks_with_empty_lists(tmp_path):
+    """Two blocks, the second with no T contributions and an empty V^1 list
+    (only the (0, 0) terminator record): everything reads back, and a file
+    whose blocks are out of order is rejected as MATRX rejects it."""
+    def lst(labs, sizes, seed):
+        rng = np.random.default_rng(seed)
+        start = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        return dict(lab=np.array(labs, np.int32), start=start,
+                    loc=rng.integers(1, 6, size=start[-1]).astype(np.int32), coeff=rng.normal(size=start[-1]),
+                    iclmn=rng.integers(1, 4, size=start[-1]).astype(np.int32))
+    empty = lst([], [], 0)
+    b1 = F.McpBlock(3, np.array([0, 1, 3, 6], np.int64), np.array([1, 1, 2, 1, 2, 3], np.int32),
+                    lst([216, 217], [2, 3], 1), [lst([46226 * 215 + 216], [4], 2), lst([216 * 46225 + 217], [1], 3)])
+    b2 = F.McpBlock(2, np.array([0, 1, 3], np.int64), np.array([1, 1, 2], np.int32), empty,
+                    [lst([46226 * 215 + 216], [2], 4), empty])
+    s = F.McpSet(ncore=1, nelec=2, ncf=5, nw=2, kmaxf=1, idblk=["  1/2-  ", "  3/2-  "], blocks=[b1, b2])
+    head = str(tmp_path / "m")
+    F.write_mcp(head, s)
+    r = F.read_mcp(head)
+    assert [b.ncf for b in r.blocks] == [3, 2] and r.idblk == s.idblk and r.ncore == 1
+    for got, want in zip(r.blocks, s.blocks):
+        np.testing.assert_array_equal(got.iendc, want.iendc)
+        np.testing.assert_array_equal(got.irow, want.irow)
+        for g, w in zip([got.tlist] + got.vlists, [want.tlist] + want.vlists):
+            for key in ("lab", "start", "loc", "coeff", "iclmn"):
+                np.testing.assert_array_equal(g[key], w[key])
+    assert r.blocks[1].tlist["lab"].size == 0 and r.blocks[1].vlists[1]["start"].tolist() == [0]
+    s.blocks = [b2, b1]
+    s.idblk = s.idblk[::-1]
+    F.write_mcp(head, s)
+    raw = bytearray(open(f"{head}.30", "rb").read())
+    # renumber the first structure block as block 2: MATRX's consistency check
+    i = raw.find(b"MCP" + np.array([1, 2], "<i4").tobytes())
+    assert i > 0
+    raw[i + 3:i + 7] = np.array([2], "<i4").tobytes()
+    open(f"{head}.30", "wb").write(bytes(raw))
+    with pytest.raises(ValueError):
+        F.read_mcp(head)
