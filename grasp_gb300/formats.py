@@ -442,6 +442,34 @@ def res_to_hmat(block: ResBlock, eav):
     return block.iendc.copy(), block.irow.copy(), emt
 
 
+def merge_res_ranks(parts):
+    """One block's rows from the rci.res files of all ranks of an MPI run
+    (rank myid holds rows myid+1, myid+1+nprocs, ...; rci90/genmat.f90:77,
+    setham_gg.f90:162) merged into a single-rank block, rows in order."""
+    parts = sorted(parts, key=lambda b: b.myid)
+    if not parts:
+        raise ValueError("no rank files")
+    ncf, nprocs = parts[0].ncf, parts[0].nprocs
+    if [b.myid for b in parts] != list(range(nprocs)) or any(b.ncf != ncf or b.nprocs != nprocs for b in parts):
+        raise ValueError("one block from every rank of the same run expected")
+    for b in parts:
+        if b.iendc.size - 1 != res_rows(ncf, b.myid, nprocs):
+            raise ValueError(f"rank {b.myid} holds {b.iendc.size - 1} rows, not all of its own")
+    lens = np.zeros(ncf, np.int64)
+    for b in parts:
+        lens[b.myid::nprocs] = np.diff(b.iendc)
+    iendc = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    irow = np.zeros(iendc[-1], np.int32)
+    emt = np.zeros(iendc[-1])
+    for b in parts:
+        for r in range(b.iendc.size - 1):
+            i = b.myid + r * nprocs
+            s, e = int(b.iendc[r]), int(b.iendc[r + 1])
+            irow[iendc[i]:iendc[i + 1]] = b.irow[s:e]
+            emt[iendc[i]:iendc[i + 1]] = b.emt[s:e]
+    return ResBlock(ncf, parts[0].iccut, iendc, irow, emt, parts[0].elsto)
+
+
 def _write_res_header(ff, hd: ResHeader):
     n = hd.zz.size
     ff.write_record(b"R92RES")
@@ -521,7 +549,7 @@ def write_res(path, header: ResHeader, blocks):
 def read_res(path):
     """(ResHeader, [ResBlock]) from rci.res. A block's rows end where its
     rank's rows end or where the file ends (an interrupted run, which rci
-    resumes from, rci90/genmat.f90:69-87)."""
+    resumes from, rci90/genmat.f90:65-90)."""
     with FortranFile(path) as ff:
         hd = _read_res_header(ff)
         blocks = []

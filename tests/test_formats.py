@@ -356,3 +356,38 @@ def test_mcp_two_blocks_with_empty_lists(tmp_path):
     open(f"{head}.30", "wb").write(bytes(raw))
     with pytest.raises(ValueError):
         F.read_mcp(head)
+
+
+def test_res_merge_ranks(tmp_path):
+    """rci.res files of a 3-rank run (rows dealt round-robin, as rci_mpi
+    writes them) merge into the single-rank block; a missing rank or a
+    short rank file is an error."""
+    rng = np.random.default_rng(11)
+    ncf, nprocs = 10, 3
+    lens = rng.integers(1, 5, size=ncf)
+    lens = np.minimum(lens, np.arange(1, ncf + 1))
+    iendc = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    irow = np.concatenate([np.concatenate([np.sort(rng.choice(np.arange(1, i + 1), n - 1, replace=False)), [i + 1]])
+                           if n > 1 else [i + 1] for i, n in enumerate(lens)]).astype(np.int32)
+    emt = rng.normal(size=iendc[-1])
+    full = F.ResBlock(ncf, 0, iendc, irow, emt, elsto=-0.5)
+    case = hydrogenic_case(nmax=2, lmax=1, z=10.0)
+    parts = []
+    for r in range(nprocs):
+        rows = range(r, ncf, nprocs)
+        sub_i = np.concatenate([[0], np.cumsum([lens[i] for i in rows])]).astype(np.int64)
+        sub_r = np.concatenate([irow[iendc[i]:iendc[i + 1]] for i in rows])
+        sub_e = np.concatenate([emt[iendc[i]:iendc[i + 1]] for i in rows])
+        p = tmp_path / f"rci{r}.res"
+        F.write_res(p, _res_header(case, 1, case["orb"].nw), [F.ResBlock(ncf, 0, sub_i, sub_r, sub_e, -0.5, r, nprocs)])
+        parts.append(F.read_res(p)[1][0])
+    m = F.merge_res_ranks(parts[::-1])
+    np.testing.assert_array_equal(m.iendc, full.iendc)
+    np.testing.assert_array_equal(m.irow, full.irow)
+    np.testing.assert_array_equal(m.emt, full.emt)
+    assert (m.myid, m.nprocs, m.elsto) == (0, 1, -0.5)
+    with pytest.raises(ValueError):
+        F.merge_res_ranks(parts[:2])
+    short = F.ResBlock(ncf, 0, parts[1].iendc[:-1], parts[1].irow, parts[1].emt, -0.5, 1, nprocs)
+    with pytest.raises(ValueError):
+        F.merge_res_ranks([parts[0], short, parts[2]])
