@@ -1,7 +1,7 @@
 #!/usr/bin/env python
 """CI-solve benchmark for the GB300 path (and the CPU reference arm).
 
-One step = one CI solve of the Fe XV workload (grasp_gb300.workloads.fe15):
+One step = one CI solve of the Fe XV workload (inputs.workloads.fe15):
 R^k table (GENINTRK, 123,092 integrals) + I(ab) table + SETHAM from the T/V
 lists (45M contributions) + MANEIG (10 lowest roots, rci settings: INIEST2
 block 2000, DVDSON with CRITR = CRITC = 1e-9), on inputs resident in HBM.
@@ -189,7 +189,8 @@ def batched_leg(local, steps, cpu=True):
     blocks, as rci) on the ten blocks of one ion, 1 thread, x 31 ions."""
     import numpy as np
 
-    from grasp_gb300 import FP64, SPLIT, Context, maneig_batched, workloads
+    from grasp_gb300 import FP64, SPLIT, Context, maneig_batched
+    from inputs import workloads
     w = workloads.batch()
     workloads.assemble_batch(workloads.batch(zs=w.zs[:1]), Context(local), precision=SPLIT)  # warm (loads, builds)
     ctx = Context(local)
@@ -245,7 +246,8 @@ def rk_leg(local):
     relative bar with its 1e-14 absolute floor."""
     import numpy as np
 
-    from grasp_gb300 import Context, workloads
+    from grasp_gb300 import Context
+    from inputs import workloads
     w = workloads.rk40()
     ctx = Context(local)
     ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
@@ -273,7 +275,8 @@ def large_leg(local, steps=2):
     (--large): generating and uploading the block takes minutes."""
     import numpy as np
 
-    from grasp_gb300 import FP64, SPLIT, Context, HMatrix, workloads
+    from grasp_gb300 import FP64, SPLIT, Context, HMatrix
+    from inputs import workloads
     t0 = time.perf_counter()
     w = workloads.large()
     t_gen = time.perf_counter() - t0
@@ -314,7 +317,7 @@ def run_reference(a):
     ws, rank, local, pg = _dist()
     if rank != 0:
         return 0
-    from grasp_gb300 import workloads
+    from inputs import workloads
     w = workloads.fe15(density=a.density)
     nth = os.cpu_count() or 1
     # the reference's own Davidson loop count on this matrix, from one full run
@@ -387,7 +390,8 @@ def run_ours(a):
     ws, rank, local, pg = _dist()
     import numpy as np
 
-    from grasp_gb300 import FP64, SPLIT, Context, HMatrix, build, workloads
+    from grasp_gb300 import FP64, SPLIT, Context, HMatrix, build
+    from inputs import workloads
     from grasp_gb300.core import launch_count, pinned
     build.build()
     w = workloads.fe15(density=a.density)

@@ -2,10 +2,8 @@
 Davidson) as hand-written sm_103a CUDA behind a C ABI (include/grasp_gpu.h).
 
 Layout:
-  csrc/       CUDA kernels and the C ABI (libgraspgpu.so), input producers
-              (libgraspsynth.so)
+  csrc/       CUDA kernels and the C ABI (libgraspgpu.so)
   core.py     Context / HMatrix: the reference-named host interface
-  synth.py    seeded synthetic orbitals, CSF spaces and T/V lists
   formats.py  GRASP file formats (Fortran unformatted records)
   build.py    nvcc build recipe (sm_103a)
 """

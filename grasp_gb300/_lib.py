@@ -1,8 +1,7 @@
-"""ctypes bindings of libgraspgpu (the C ABI in include/grasp_gpu.h) and
-libgraspsynth (include/grasp_synth.h).
+"""ctypes bindings of libgraspgpu (the C ABI in include/grasp_gpu.h).
 
-The libraries are built in-tree (grasp_gb300/_build). Loading fails loudly
-when they are missing: there is no CPU fallback for the GPU path.
+The library is built in-tree (grasp_gb300/_build). Loading fails loudly
+when it is missing: there is no CPU fallback for the GPU path.
 """
 from __future__ import annotations
 
@@ -18,7 +17,6 @@ _int = C.POINTER(C.c_int)
 _u8 = C.POINTER(C.c_uint8)
 
 _gpu = None
-_synth = None
 
 
 class GGList(C.Structure):
@@ -30,14 +28,6 @@ class GGDvdParams(C.Structure):
         ("flavour", C.c_int), ("precision", C.c_int), ("lim", C.c_int), ("maxiter", C.c_int),
         ("critr", C.c_double), ("critc", C.c_double), ("crite", C.c_double), ("robust", C.c_int),
         ("mblock", C.c_int),
-    ]
-
-
-class GSBlockSpec(C.Structure):
-    _fields_ = [
-        ("nw", C.c_int), ("np", _int), ("nak", _int), ("frozen", _u8), ("nref", C.c_int), ("refs", _u8),
-        ("max_rank", C.c_int), ("two_j", C.c_int), ("parity", C.c_int), ("kmaxf", C.c_int),
-        ("max_ncf", C.c_int64), ("density", C.c_double), ("coeff_scale", C.c_double), ("seed", C.c_uint64),
     ]
 
 
@@ -72,6 +62,7 @@ GPU_SYMBOLS = {
                                     _d, _int, _int, _int]),
     "gg_stage_stat": (C.c_double, [C.c_void_p, C.c_int]),
     "gg_launch_count": (C.c_longlong, []),
+    "gg_alloc_count": (C.c_longlong, []),
     "gg_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),
     "gg_host_unregister": (C.c_int, [C.c_void_p]),
     "gg_event_record": (C.c_int, [C.c_void_p, C.c_int]),
@@ -79,17 +70,6 @@ GPU_SYMBOLS = {
     "gg_matvec_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _d, _d]),
     "gg_spmm_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _d, _d]),
     "gg_projected_eig": (C.c_int, [C.c_int, _d, C.c_int, C.c_int, _d, _d]),
-}
-
-SYNTH_SYMBOLS = {
-    "gs_dcbsrw": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, _d, C.c_int, C.c_double, _d, _d, _d, _d, _int]),
-    "gs_screenpar": (C.c_int, [C.c_int, _int, C.c_int, _d]),
-    "gs_block_generate": (C.c_int, [C.POINTER(GSBlockSpec), C.POINTER(C.c_void_p)]),
-    "gs_block_free": (None, [C.c_void_p]),
-    "gs_block_sizes": (C.c_int, [C.c_void_p, _int, _i64, _int, _int, _i64, _i64]),
-    "gs_block_structure": (C.c_int, [C.c_void_p, _i64, _i32, _u8]),
-    "gs_block_list": (C.c_int, [C.c_void_p, C.c_int, _i32, _i64, _i32, _i32, _d]),
-    "gs_synthetic_h": (C.c_int, [C.c_int, C.c_double, C.c_uint64, _i64, _i32, _d]),
 }
 
 
@@ -101,12 +81,12 @@ def _bind(lib, table):
     return lib
 
 
-def lib_paths():
-    return _build.LIB_GPU, _build.LIB_SYNTH
+def lib_path():
+    return _build.LIB_GPU
 
 
 def ensure_built():
-    if not (os.path.exists(_build.LIB_GPU) and os.path.exists(_build.LIB_SYNTH)):
+    if not os.path.exists(_build.LIB_GPU):
         _build.build()
 
 
@@ -122,25 +102,10 @@ def gpu():
     return _gpu
 
 
-def synth():
-    global _synth
-    if _synth is None:
-        if not os.path.exists(_build.LIB_SYNTH):
-            _build.build()
-        _synth = _bind(C.CDLL(_build.LIB_SYNTH), SYNTH_SYMBOLS)
-    return _synth
-
-
 class GGError(RuntimeError):
     def __init__(self, status, msg):
         super().__init__(f"[{status}] {msg}")
         self.status = status
-
-
-def check_synth(status):
-    if status != 0:
-        raise ValueError(f"synthetic-input generator rejected its arguments (status {status})")
-    return status
 
 
 def check(status):

@@ -1,4 +1,4 @@
-"""Builds libgraspgpu.so (CUDA, sm_103a) and libgraspsynth.so (host C++) in-tree.
+"""Builds libgraspgpu.so (CUDA, sm_103a) in-tree.
 
 Run ``python -m grasp_gb300.build`` or call :func:`build`. Objects go to
 ``grasp_gb300/_build/``; translation units compile in parallel.
@@ -23,10 +23,8 @@ NVCC_FLAGS = GENCODE + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
 NO_FMAD = {"radial.cu", "setham.cu", "spmv.cu", "ltile.cu", "davidson.cu"}  # exact FP64 sums; error-free double-float steps
 CU_SOURCES = ["ctx.cu", "radial.cu", "setham.cu", "spmv.cu", "ltile.cu", "davidson.cu", "bdvd.cu"]
 CPP_SOURCES = ["hosteig.cpp"]
-SYNTH_SOURCES = ["synth.cpp"]
 
 LIB_GPU = os.path.join(OUT, "libgraspgpu.so")
-LIB_SYNTH = os.path.join(OUT, "libgraspsynth.so")
 
 
 def _nvcc() -> str:
@@ -56,7 +54,7 @@ def _headers():
     return hs
 
 
-def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = False) -> tuple[str, str]:
+def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = False) -> str:
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     hdrs = _headers()
@@ -85,17 +83,13 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
             logs.append(out)
     if force or jobs or not os.path.exists(LIB_GPU):
         _run([nvcc] + GENCODE + ["-shared", "-o", LIB_GPU] + objs)
-    synth_srcs = [os.path.join(CSRC, f) for f in SYNTH_SOURCES]
-    if force or _stale(LIB_SYNTH, synth_srcs + hdrs):
-        _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + INC, "-o", LIB_SYNTH] + synth_srcs + ["-lpthread"])
     if verbose:
         for l in logs:
             if l.strip():
                 print(l)
-    return LIB_GPU, LIB_SYNTH
+    return LIB_GPU
 
 
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose=True, ptxas_verbose="--ptxas" in sys.argv)
     print(LIB_GPU)
-    print(LIB_SYNTH)

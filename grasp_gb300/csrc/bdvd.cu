@@ -1488,6 +1488,7 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   else
     GG_TRY(B.XD.alloc((size_t)B.ntot * MAXR));
   if (cudaMallocHost(&B.hNact, sizeof(int)) != cudaSuccess) return fail(GG_ERR_NOMEM, "cudaMallocHost");
+  note_alloc();
   GG_CUDA(cudaMemcpyAsync(B.dDesc.p, B.hd.data(), nblocks * sizeof(BDesc), cudaMemcpyHostToDevice, s));
   GG_CUDA(cudaMemcpyAsync(B.dSt.p, hst.data(), nblocks * sizeof(BState), cudaMemcpyHostToDevice, s));
   GG_CUDA(cudaMemcpyAsync(B.dTiles.p, B.ht.data(), B.ntiles * sizeof(BTile), cudaMemcpyHostToDevice, s));

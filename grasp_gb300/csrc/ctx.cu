@@ -9,9 +9,11 @@ namespace gg {
 
 static thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};
+static std::atomic<long long> g_allocs{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 void note_launches(long long m) { g_launches.fetch_add(m, std::memory_order_relaxed); }
+void note_alloc() { g_allocs.fetch_add(1, std::memory_order_relaxed); }
 void set_error(const std::string &msg) { g_last_error = msg; }
 int fail(int status, const std::string &msg) {
   g_last_error = msg;
@@ -276,6 +278,7 @@ double gg_stage_stat(gg_ctx *ctx, int which) {
 }
 
 long long gg_launch_count(void) { return g_launches.load(); }
+long long gg_alloc_count(void) { return g_allocs.load(); }
 
 int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double *z) {
   if (n < 1 || !ap || m < 1 || m > n || mvec < 0 || mvec > m || !w || (mvec > 0 && !z))

@@ -1555,6 +1555,7 @@ struct Dvd {
       const size_t bin = al(sizeof(NvIn)), bout = al(sizeof(NvOut));
       char *a = nullptr;
       GG_CUDA(cudaMallocHost(&a, bS + bmt + bup + bdown + bpv + bbst + bin + bout));
+      note_alloc();
       pinned = a;
       hS = reinterpret_cast<double *>(a);
       a += bS;

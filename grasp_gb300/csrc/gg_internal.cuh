@@ -17,6 +17,8 @@ int fail(int status, const std::string &msg);
 void note_launch();
 // adds m (possibly negative: launches recorded while a graph was captured)
 void note_launches(long long m);
+// counts this library's device and pinned-host allocations (gg_alloc_count)
+void note_alloc();
 
 #define GG_CUDA(call)                                                                   \
   do {                                                                                  \
@@ -62,6 +64,7 @@ template <class T> struct DBuf {
     release();
     if (count == 0) count = 1;
     cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    note_alloc();
     if (e != cudaSuccess) {
       p = nullptr;
       return fail(GG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));

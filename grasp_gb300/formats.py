@@ -401,10 +401,12 @@ class ResBlock:
 
 
 def res_rows(ncf, myid=0, nprocs=1):
-    """Rows of a block that rank myid owns (rci90/genmat.f90:97-98)."""
-    if ncf < nprocs:
-        return ncf // (myid + 1)
-    return (ncf - myid - 1 + nprocs) // nprocs
+    """Rows of a block that rank myid writes to rci.res: rows myid+1,
+    myid+1+nprocs, ... up to NCF (the row loop of rci90/setham_gg.f90:160).
+    genmat.f90:97-99 counts NCF/(MYID+1) rows where NCF < NPROCS, which is
+    more than the rank wrote (ncf = 2, nprocs = 3: rank 0 wrote one row);
+    the rows actually written are what a reader must take."""
+    return max(0, (ncf - myid + nprocs - 1) // nprocs)
 
 
 def rci_filter(iendc, irow, emt, cutoff=RCI_CUTOFF):

@@ -260,6 +260,8 @@ int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double
 
 /* ---- measurement helpers (no counterpart in the reference) ------------------
  * gg_launch_count: kernels this library has launched in this process.
+ * gg_alloc_count: device (cudaMalloc) and pinned host (cudaMallocHost)
+ * allocations this library has made in this process.
  * gg_event_record / gg_event_elapsed: CUDA events (8 slots) on the context
  * stream; elapsed synchronises on slot b.
  * gg_matvec_timing: average device time of one y = H x launch (after a
@@ -268,6 +270,7 @@ int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double
  * vectors (1 <= m <= 16; the Davidson block pass's matvec), algorithmic
  * bytes = the matrix in the reference's storage once + 3 m NCF doubles.     */
 long long gg_launch_count(void);
+long long gg_alloc_count(void);
 /* Page-locks (pins) caller memory so that uploads from it run at full link
  * rate; unregister before freeing it. */
 int gg_host_register(void *p, size_t bytes);

@@ -1,6 +1,6 @@
 // synth.cpp - seeded input producers for the CI hot path (libgraspsynth).
-// See include/grasp_synth.h for what is and is not physical here.
-#include "../../include/grasp_synth.h"
+// See inputs/grasp_synth.h for what is and is not physical here.
+#include "../grasp_synth.h"
 
 #include <algorithm>
 #include <cmath>

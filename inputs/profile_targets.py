@@ -2,13 +2,13 @@
 in profiles/. Each target builds the Fe XV workload once and runs only the
 kernel family it is named for, a few times:
 
-  python -m grasp_gb300.profile_targets spmv     # 3 full-size y = H x launches per precision
-  python -m grasp_gb300.profile_targets spmm     # split Y = H X launches for 1 to 16 vectors
-  python -m grasp_gb300.profile_targets solve    # one full MANEIG (split, MBLOCK = NVEC) (launch list)
-  python -m grasp_gb300.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
-  python -m grasp_gb300.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
-  python -m grasp_gb300.profile_targets batch    # two batched solves of the 310-block workload (split)
-  python -m grasp_gb300.profile_targets batch8   # the same for 8 ions (80 blocks), for detailed captures
+  python -m inputs.profile_targets spmv     # 3 full-size y = H x launches per precision
+  python -m inputs.profile_targets spmm     # split Y = H X launches for 1 to 16 vectors
+  python -m inputs.profile_targets solve    # one full MANEIG (split, MBLOCK = NVEC) (launch list)
+  python -m inputs.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
+  python -m inputs.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
+  python -m inputs.profile_targets batch    # two batched solves of the 310-block workload (split)
+  python -m inputs.profile_targets batch8   # the same for 8 ions (80 blocks), for detailed captures
 """
 from __future__ import annotations
 
@@ -16,7 +16,8 @@ import sys
 
 
 def _fe15_context():
-    from . import Context, HMatrix, workloads
+    from grasp_gb300 import Context, HMatrix
+    from . import workloads
     w = workloads.fe15()
     b = w.block
     ctx = Context(0)
@@ -30,7 +31,7 @@ def _fe15_context():
 
 
 def spmv():
-    from . import FP64, SPLIT
+    from grasp_gb300 import FP64, SPLIT
     w, ctx, H = _fe15_context()
     for prec in (FP64, SPLIT):
         ms, by = H.matvec_timing(prec, 3)
@@ -46,14 +47,15 @@ def spmm():
 
 
 def solve():
-    from . import SPLIT
+    from grasp_gb300 import SPLIT
     w, ctx, H = _fe15_context()
     ev, vec, info = H.maneig(w.nroots, flavour=0, precision=SPLIT, mblock=w.nroots)
     print("loops", info["nloops"], "E0", ev[0])
 
 
 def rk(precision=0):
-    from . import Context, workloads
+    from grasp_gb300 import Context
+    from . import workloads
     w = workloads.rk40()
     ctx = Context(0)
     ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
@@ -68,7 +70,8 @@ def rk_split():
 
 
 def batch(zs=None):
-    from . import SPLIT, Context, maneig_batched, workloads
+    from grasp_gb300 import SPLIT, Context, maneig_batched
+    from . import workloads
     w = workloads.batch() if zs is None else workloads.batch(zs=zs)
     ctx = Context(0)
     hs = workloads.assemble_batch(w, ctx)

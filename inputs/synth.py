@@ -1,4 +1,4 @@
-"""Seeded synthetic inputs with the reference's formats (see include/grasp_synth.h).
+"""Seeded synthetic inputs with the reference's formats (see inputs/grasp_synth.h).
 
 Orbital sets, screened-hydrogenic Dirac spinors (DCBSRW at Z - sigma), and
 CI blocks (CSF occupations, mcp.30 structure, T/V lists).
@@ -10,8 +10,59 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _lib
-from ._lib import _d, _i32, _i64, _int, _u8, ptr
+from . import build as _build
+
+_d = C.POINTER(C.c_double)
+_i32 = C.POINTER(C.c_int32)
+_i64 = C.POINTER(C.c_int64)
+_int = C.POINTER(C.c_int)
+_u8 = C.POINTER(C.c_uint8)
+
+
+def ptr(a, t):
+    return a.ctypes.data_as(t)
+
+
+class GSBlockSpec(C.Structure):
+    _fields_ = [
+        ("nw", C.c_int), ("np", _int), ("nak", _int), ("frozen", _u8), ("nref", C.c_int), ("refs", _u8),
+        ("max_rank", C.c_int), ("two_j", C.c_int), ("parity", C.c_int), ("kmaxf", C.c_int),
+        ("max_ncf", C.c_int64), ("density", C.c_double), ("coeff_scale", C.c_double), ("seed", C.c_uint64),
+    ]
+
+
+# symbol name -> (restype, argtypes); every symbol grasp_synth.h declares
+SYNTH_SYMBOLS = {
+    "gs_dcbsrw": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, _d, C.c_int, C.c_double, _d, _d, _d, _d, _int]),
+    "gs_screenpar": (C.c_int, [C.c_int, _int, C.c_int, _d]),
+    "gs_block_generate": (C.c_int, [C.POINTER(GSBlockSpec), C.POINTER(C.c_void_p)]),
+    "gs_block_free": (None, [C.c_void_p]),
+    "gs_block_sizes": (C.c_int, [C.c_void_p, _int, _i64, _int, _int, _i64, _i64]),
+    "gs_block_structure": (C.c_int, [C.c_void_p, _i64, _i32, _u8]),
+    "gs_block_list": (C.c_int, [C.c_void_p, C.c_int, _i32, _i64, _i32, _i32, _d]),
+    "gs_synthetic_h": (C.c_int, [C.c_int, C.c_double, C.c_uint64, _i64, _i32, _d]),
+}
+
+_synth = None
+
+
+def lib():
+    """libgraspsynth, built on first use."""
+    global _synth
+    if _synth is None:
+        _build.build()
+        _synth = C.CDLL(_build.LIB_SYNTH)
+        for name, (res, args) in SYNTH_SYMBOLS.items():
+            f = getattr(_synth, name)
+            f.restype = res
+            f.argtypes = args
+    return _synth
+
+
+def check(status):
+    if status != 0:
+        raise ValueError(f"synthetic-input generator rejected its arguments (status {status})")
+    return status
 
 CVAC = 137.035999139  # lib9290/setcon.f90:25 (ALFAI)
 NNNP = 590            # parameter_def_M.f90:23
@@ -61,7 +112,7 @@ def dcbsrw(n, kappa, z, r, ntp, c=CVAC, accy=None, h=0.05):
     r = np.ascontiguousarray(r, np.float64)
     p = np.zeros(ntp); q = np.zeros(ntp)
     e = C.c_double(); pz = C.c_double(); mtp = C.c_int()
-    rc = _lib.synth().gs_dcbsrw(n, kappa, float(z), c, ptr(r, _d), ntp, accy, C.byref(e), C.byref(pz), ptr(p, _d),
+    rc = lib().gs_dcbsrw(n, kappa, float(z), c, ptr(r, _d), ntp, accy, C.byref(e), C.byref(pz), ptr(p, _d),
                                 ptr(q, _d), C.byref(mtp))
     if rc != 0:
         raise ValueError(f"DCBSRW: invalid (n={n}, kappa={kappa}, z={z})")
@@ -100,7 +151,7 @@ def hydrogenic_orbitals(orbs, z, sigma, r, n=NNNP, c=CVAC, h=0.05, ld=None):
 def screenpar(nak, ncore):
     nak = np.ascontiguousarray(nak, np.int32)
     s = np.zeros(len(nak))
-    _lib.synth().gs_screenpar(len(nak), ptr(nak, _int), ncore, ptr(s, _d))
+    lib().gs_screenpar(len(nak), ptr(nak, _int), ncore, ptr(s, _d))
     return s
 
 
@@ -128,7 +179,7 @@ class CIBlock:
 
 def ci_block(orbs, refs, frozen, two_j=0, parity=0, kmaxf=None, max_rank=2, max_ncf=0, density=0.0,
              coeff_scale=1.0, seed=1):
-    """Generate a synthetic CI block (see include/grasp_synth.h)."""
+    """Generate a synthetic CI block (see inputs/grasp_synth.h)."""
     nw = len(orbs)
     npq = np.array([o[0] for o in orbs], np.int32)
     nak = np.array([o[1] for o in orbs], np.int32)
@@ -136,10 +187,10 @@ def ci_block(orbs, refs, frozen, two_j=0, parity=0, kmaxf=None, max_rank=2, max_
         kmaxf = max(nkj(k) for k in nak)
     refs = np.ascontiguousarray(np.asarray(refs, np.uint8).reshape(-1, nw))
     frozen = np.ascontiguousarray(np.asarray(frozen, np.uint8))
-    spec = _lib.GSBlockSpec(nw, ptr(npq, _int), ptr(nak, _int), ptr(frozen, _u8), refs.shape[0], ptr(refs, _u8),
+    spec = GSBlockSpec(nw, ptr(npq, _int), ptr(nak, _int), ptr(frozen, _u8), refs.shape[0], ptr(refs, _u8),
                             max_rank, two_j, parity, kmaxf, max_ncf, density, coeff_scale, seed)
     h = C.c_void_p()
-    L = _lib.synth()
+    L = lib()
     rc = L.gs_block_generate(C.byref(spec), C.byref(h))
     if rc != 0:
         raise ValueError(f"gs_block_generate failed ({rc})")

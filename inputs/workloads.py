@@ -2,7 +2,7 @@
 
 Every workload is: a 590-point log grid (RNT = 2e-6/Z, H = 0.05), screened
 hydrogenic Dirac orbitals (DCBSRW at Z - sigma, SCREENPAR screening), and a
-CI block from :func:`grasp_gb300.synth.ci_block` (CSF occupations, mcp.30
+CI block from :func:`inputs.synth.ci_block` (CSF occupations, mcp.30
 structure, T/V lists with seeded coefficients).
 
 Sizes versus the workload descriptions they stand in for:
@@ -142,14 +142,15 @@ class LargeWorkload:
 
 def synthetic_h(ncf, nnz, seed=7):
     """Seeded symmetric H in GRASP's lower-triangle-by-rows storage with about
-    ``nnz`` stored elements (gs_synthetic_h, include/grasp_synth.h): each
+    ``nnz`` stored elements (gs_synthetic_h, inputs/grasp_synth.h): each
     column below the diagonal of row r is present with the same probability;
     diagonal -1000 + 30 sqrt(r / ncf) Eh (sorted, like configuration
     energies) plus N(0, 1e-3), off-diagonal elements N(0, 2e-3) Eh."""
-    from ._lib import _d, _i32, _i64, check_synth, ptr
+    from .synth import _d, _i32, _i64, ptr
+    from .synth import check as check_synth
     p = 2.0 * max(nnz - ncf, 0) / (ncf * (ncf - 1.0))
     iendc = np.zeros(ncf + 1, np.int64)
-    lib = S._lib.synth()
+    lib = S.lib()
     check_synth(lib.gs_synthetic_h(ncf, p, seed, ptr(iendc, _i64), None, None))
     irow = np.empty(int(iendc[-1]), np.int32)
     emt = np.empty(int(iendc[-1]), np.float64)
@@ -207,7 +208,7 @@ def assemble_batch(w, ctx, precision=0):
     other ions' blocks are views of them (gg_hmat_create_view), which share
     the lists and the assembly plan. Returns the HMatrix objects in
     (ion, block) order."""
-    from . import HMatrix
+    from grasp_gb300 import HMatrix
     hs, first = [], []
     for iz, z in enumerate(w.zs):
         n, rnt, ob = w.ion(z)

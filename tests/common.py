@@ -1,7 +1,7 @@
 """Shared fixtures-in-code: seeded orbital sets and CI blocks for the tests."""
 import numpy as np
 
-from grasp_gb300 import synth as S
+from inputs import synth as S
 
 CVAC = S.CVAC
 

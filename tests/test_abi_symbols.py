@@ -1,6 +1,6 @@
-"""The C-ABI libraries load on a machine without a GPU and export every
-function their headers (include/grasp_gpu.h, include/grasp_synth.h) declare.
-No compute calls here."""
+"""The C-ABI library loads on a machine without a GPU and exports every
+function include/grasp_gpu.h declares; the synthetic-input library
+(inputs/) exports what inputs/grasp_synth.h declares. No compute calls here."""
 import ctypes
 import os
 import re
@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def declared(header):
-    src = open(os.path.join(ROOT, "include", header)).read()
+    src = open(os.path.join(ROOT, header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:gg|gs)_\w+)\s*\(", src, flags=re.M)
     return sorted(set(names))
@@ -26,11 +26,12 @@ def exported(path):
 @pytest.fixture(scope="module")
 def libs():
     from grasp_gb300 import build
-    return build.build()
+    from inputs import build as ibuild
+    return build.build(), ibuild.build()
 
 
 def test_gpu_header_symbols_exported(libs):
-    names = declared("grasp_gpu.h")
+    names = declared("include/grasp_gpu.h")
     assert len(names) >= 30
     syms = exported(libs[0])
     missing = [n for n in names if n not in syms]
@@ -38,7 +39,7 @@ def test_gpu_header_symbols_exported(libs):
 
 
 def test_synth_header_symbols_exported(libs):
-    names = declared("grasp_synth.h")
+    names = declared("inputs/grasp_synth.h")
     syms = exported(libs[1])
     assert not [n for n in names if n not in syms]
 
@@ -56,5 +57,6 @@ def test_gpu_library_loads_and_reports_errors(libs):
 
 def test_python_bindings_cover_header(libs):
     from grasp_gb300 import _lib
-    assert set(declared("grasp_gpu.h")) <= set(_lib.GPU_SYMBOLS)
-    assert set(declared("grasp_synth.h")) <= set(_lib.SYNTH_SYMBOLS)
+    assert set(declared("include/grasp_gpu.h")) <= set(_lib.GPU_SYMBOLS)
+    from inputs import synth
+    assert set(declared("inputs/grasp_synth.h")) <= set(synth.SYNTH_SYMBOLS)

@@ -1,7 +1,8 @@
 """GRASP file formats (grasp_gb300/formats.py): round trips of mcp.30/31/32+k,
 rwfn and .cm, and checks against the reference's own example data
 (src/appl/rhfszeeman95/examples: rwfn and mixing files written by GRASP runs,
-and their text summaries), when the reference tree is present.
+and their text summaries), copied into tests/golden/grasp_examples by
+tests/golden/copy_grasp_examples.py.
 
 The reference-data checks also pin the oracle's grid and quadrature on
 orbitals GRASP produced: RADGRD reproduces the stored grid, QUAD finds the
@@ -17,8 +18,8 @@ import pytest
 from grasp_gb300 import formats as F
 from tests.common import hydrogenic_case, ne7_block, oracle_for
 
-REF = "/root/reference/src/appl/rhfszeeman95/examples"
-ref_data = pytest.mark.skipif(not os.path.isdir(REF), reason="reference example data not present")
+REF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "grasp_examples")
+ref_data = pytest.mark.skipif(not os.path.isdir(REF), reason="GRASP example data not present")
 
 
 def test_mcp_round_trip_and_setham(tmp_path, oracle_mod):
@@ -300,7 +301,8 @@ def test_res_rank_rows_and_interrupted_file(tmp_path):
     block's rows, as an interrupted rci run leaves it: the rows present are
     read and the block is short."""
     assert [F.res_rows(10, r, 3) for r in range(3)] == [4, 3, 3]
-    assert F.res_rows(2, 0, 4) == 2 and F.res_rows(2, 1, 4) == 1
+    # fewer CSFs than ranks: each rank wrote the rows of its own stride only
+    assert [F.res_rows(2, r, 4) for r in range(4)] == [1, 1, 0, 0]
     case = hydrogenic_case(nmax=2, lmax=1, z=10.0)
     hd = _res_header(case, 1, case["orb"].nw)
     iendc = np.array([0, 1, 3, 5, 8], np.int64)
@@ -391,3 +393,45 @@ def test_res_merge_ranks(tmp_path):
     short = F.ResBlock(ncf, 0, parts[1].iendc[:-1], parts[1].irow, parts[1].emt, -0.5, 1, nprocs)
     with pytest.raises(ValueError):
         F.merge_res_ranks([parts[0], short, parts[2]])
+
+
+def _random_lower_rows(rng, ncf):
+    lens = np.minimum(rng.integers(1, 5, size=ncf), np.arange(1, ncf + 1))
+    iendc = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+    irow = np.concatenate([np.concatenate([np.sort(rng.choice(np.arange(1, i + 1), n - 1, replace=False)), [i + 1]])
+                           if n > 1 else [i + 1] for i, n in enumerate(lens)]).astype(np.int32)
+    return iendc, irow, rng.normal(size=iendc[-1])
+
+
+def _rank_rows(iendc, irow, emt, r, nprocs):
+    rows = list(range(r, iendc.size - 1, nprocs))
+    sub_i = np.concatenate([[0], np.cumsum([iendc[i + 1] - iendc[i] for i in rows])]).astype(np.int64)
+    sub_r = np.concatenate([irow[iendc[i]:iendc[i + 1]] for i in rows] + [np.zeros(0, np.int32)]).astype(np.int32)
+    sub_e = np.concatenate([emt[iendc[i]:iendc[i + 1]] for i in rows] + [np.zeros(0)])
+    return sub_i, sub_r, sub_e
+
+
+def test_res_block_with_fewer_csfs_than_ranks(tmp_path):
+    """A 2-CSF block between two larger ones, written by 3 ranks: rank 2
+    owns no row of it (setham_gg.f90:160 deals rows MYID+1, MYID+1+NPROCS,
+    ...). Every rank's file reads back block by block (the small block does
+    not swallow the next block's header record) and the blocks merge."""
+    rng = np.random.default_rng(5)
+    sizes, nprocs = [10, 2, 7], 3
+    blocks = [_random_lower_rows(rng, n) for n in sizes]
+    case = hydrogenic_case(nmax=2, lmax=1, z=10.0)
+    hd = _res_header(case, len(sizes), case["orb"].nw)
+    read = []
+    for r in range(nprocs):
+        p = tmp_path / f"rci{r}.res"
+        F.write_res(p, hd, [F.ResBlock(n, 0, *_rank_rows(*blk, r, nprocs), 0.25, r, nprocs)
+                            for n, blk in zip(sizes, blocks)])
+        _, got = F.read_res(p)
+        assert [b.ncf for b in got] == sizes
+        assert [b.iendc.size - 1 for b in got] == [len(range(r, n, nprocs)) for n in sizes]
+        read.append(got)
+    for j, (iendc, irow, emt) in enumerate(blocks):
+        m = F.merge_res_ranks([read[r][j] for r in range(nprocs)])
+        np.testing.assert_array_equal(m.iendc, iendc)
+        np.testing.assert_array_equal(m.irow, irow)
+        np.testing.assert_array_equal(m.emt, emt)

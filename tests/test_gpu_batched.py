@@ -17,7 +17,7 @@ EV_TOL, VEC_TOL = 1e-9, 1e-7
 
 
 def _small_batch():
-    from grasp_gb300 import workloads as W
+    from inputs import workloads as W
     # two ions; blocks of 321-548 CSFs, plus one capped at 40 CSFs, which is
     # below LIM and is solved in the full unit basis
     w = W.batch(zs=(10, 17), two_js=(0, 8), parities=(0, 1))
@@ -27,7 +27,8 @@ def _small_batch():
 
 
 def _setup():
-    from grasp_gb300 import Context, workloads as W
+    from grasp_gb300 import Context
+    from inputs import workloads as W
     w = _small_batch()
     ctx = Context(0)
     hs = W.assemble_batch(w, ctx)
@@ -113,7 +114,8 @@ def test_batched_tiny_blocks_and_two_contexts(gpu_ready, oracle_mod):
     together with ordinary blocks assembled on a second context (another
     ion), in one batched call; each block against the oracle's MANEIG."""
     import oracle
-    from grasp_gb300 import Context, maneig_batched, workloads as W
+    from grasp_gb300 import Context, maneig_batched
+    from inputs import workloads as W
     tiny = [W.batch(zs=(10,), two_js=(0,), parities=(0,), max_ncf=c) for c in (1, 2, 5)]
     big = W.batch(zs=(23,), two_js=(4,), parities=(1,))
     c1, c2 = Context(0), Context(0)
@@ -137,7 +139,8 @@ def test_views_match_full_assembly_and_outlive_source(gpu_ready):
     """A view (gg_hmat_create_view: another ion's copy of a block) assembles
     the same EMT as a matrix built from its own upload; uploading into a view
     is an error; the view keeps working after its source is destroyed."""
-    from grasp_gb300 import Context, GGError, HMatrix, workloads as W
+    from grasp_gb300 import Context, GGError, HMatrix
+    from inputs import workloads as W
     w = W.batch(zs=(10, 17), two_js=(2,), parities=(1,))
     b = w.blocks[0][2]
     ctx = Context(0)

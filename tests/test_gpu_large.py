@@ -12,7 +12,7 @@ pytestmark = pytest.mark.gpu
 def test_large_block_matches_oracle(gpu_ready, oracle_mod):
     import oracle
     from grasp_gb300 import FP64, SPLIT, Context, HMatrix
-    from grasp_gb300 import workloads as W
+    from inputs import workloads as W
     ncf, nvec = 70000, 5
     iendc, irow, emt = W.synthetic_h(ncf, 3.0e6, seed=5)
     ctx = Context(0)

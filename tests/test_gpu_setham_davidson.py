@@ -125,7 +125,7 @@ def test_maneig_davidson_path(gpu_ready, oracle_mod):
     """ncf > 2000: INIEST2 on the leading 2000 block, then DVDSON (rci)."""
     import oracle
     from grasp_gb300 import Context, HMatrix
-    from grasp_gb300 import synth as S
+    from inputs import synth as S
     orbs = S.orbital_set(6, 3)
     case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
     occ = lambda d: S.occupation(orbs, d)  # noqa: E731
@@ -162,7 +162,7 @@ def test_maneig_graph_pass_matches_launch_path(gpu_ready, monkeypatch):
     """The single-vector pass replayed as a CUDA graph and the same pass
     launched kernel by kernel do the same arithmetic in the same order."""
     from grasp_gb300 import Context, HMatrix
-    from grasp_gb300 import synth as S
+    from inputs import synth as S
     orbs = S.orbital_set(6, 3)
     case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
     occ = lambda d: S.occupation(orbs, d)  # noqa: E731
@@ -193,7 +193,7 @@ def test_block_pass_device_newvec_matches_host(gpu_ready, monkeypatch):
     eigenpairs; the graph and launch-by-launch forms of the fused pass are
     bit-identical."""
     from grasp_gb300 import Context, HMatrix
-    from grasp_gb300 import synth as S
+    from inputs import synth as S
     orbs = S.orbital_set(6, 3)
     case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
     occ = lambda d: S.occupation(orbs, d)  # noqa: E731
@@ -226,7 +226,7 @@ def test_maneig_alternative_kernels(gpu_ready, oracle_mod, monkeypatch, env):
     the tiled lower-triangle split matvec) give the same eigenpairs."""
     import oracle
     from grasp_gb300 import Context, HMatrix
-    from grasp_gb300 import synth as S
+    from inputs import synth as S
     orbs = S.orbital_set(6, 3)
     case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
     occ = lambda d: S.occupation(orbs, d)  # noqa: E731
@@ -263,7 +263,8 @@ def test_maneig_tiny_blocks(gpu_ready, oracle_mod, flavour, precision):
     (rci90/maneig.f90:122-137) and Davidson in the full unit basis, for both
     MANEIG flavours and both matvec precisions, against the oracle's MANEIG."""
     import oracle
-    from grasp_gb300 import Context, workloads as W
+    from grasp_gb300 import Context
+    from inputs import workloads as W
     ctx = Context(0)
     for c in (1, 2, 5):
         w = W.batch(zs=(10,), two_js=(0,), parities=(0,), max_ncf=c)

@@ -72,7 +72,7 @@ def test_setham_and_maneig_vs_lapack(oracle_mod):
 def test_gdvd_davidson_vs_lapack(oracle_mod):
     """The DVDSON restatement (rmcdhf flavour forces Davidson above 4000 only,
     so call with rci's flavour on a block above 2000 CSFs)."""
-    from grasp_gb300 import synth as S
+    from inputs import synth as S
     orbs = S.orbital_set(6, 3)
     occ = lambda d: S.occupation(orbs, d)  # noqa: E731
     refs = [occ({(1, -1): 2, (2, -1): 2}), occ({(1, -1): 2, (2, 1): 2}), occ({(1, -1): 2, (2, -2): 2})]

@@ -84,7 +84,7 @@ def test_slater_symmetries(oracle_mod):
     case = hydrogenic_case(nmax=3, lmax=2, z=10.0)
     o = oracle_for(case)
     rng = np.random.default_rng(0)
-    from grasp_gb300.synth import lval
+    from inputs.synth import lval
     L = [lval(k) for _, k in case["orbs"]]
     nw = len(L)
     checked = 0

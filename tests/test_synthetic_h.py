@@ -8,7 +8,7 @@ import numpy as np
 
 
 def test_synthetic_h_structure_and_values():
-    from grasp_gb300 import workloads as W
+    from inputs import workloads as W
     ncf, nnz = 5000, 400_000
     iendc, irow, emt = W.synthetic_h(ncf, nnz, seed=3)
     assert iendc[0] == 0 and iendc.size == ncf + 1 and np.all(np.diff(iendc) >= 1)
@@ -29,7 +29,7 @@ def test_synthetic_h_structure_and_values():
 
 
 def test_synthetic_h_deterministic():
-    from grasp_gb300 import workloads as W
+    from inputs import workloads as W
     a = W.synthetic_h(3000, 100_000, seed=11)
     b = W.synthetic_h(3000, 100_000, seed=11)
     c = W.synthetic_h(3000, 100_000, seed=12)

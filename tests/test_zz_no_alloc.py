@@ -27,12 +27,16 @@ def test_slater_noalloc_matches_slater_twice(gpu_ready):
     idx = {o: j + 1 for j, o in enumerate(case["orbs"])}
     calls = [(idx[(2, -1)], idx[(3, -2)], idx[(2, -1)], idx[(3, -2)], 0),
              (idx[(1, -1)], idx[(3, 2)], idx[(3, 2)], idx[(1, -1)], 2)]
-    for a, b, c, d, k in calls:
+    refs = [ctx.slater(a, b, c, d, k) for a, b, c, d, k in calls]
+    # the property the entry point exists for: the library makes no device
+    # (or pinned host) allocation during these calls, the first included
+    allocs = lib.gg_alloc_count()
+    for (a, b, c, d, k), ref in zip(calls, refs):
         v = C.c_double(np.nan)
         st = lib.gg_slater_noalloc(ctx._h, a, b, c, d, k, C.byref(v))
         assert st == 0, lib.gg_last_error()
-        ref = ctx.slater(a, b, c, d, k)
         assert abs(v.value - ref) <= 1e-14 * abs(ref) + 1e-16, (a, b, c, d, k, v.value, ref)
+    assert lib.gg_alloc_count() == allocs
     # a grid beyond the fixed scratch is rejected with a clear error
     big = Context(0)
     n = 2100
