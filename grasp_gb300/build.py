@@ -1,4 +1,5 @@
-"""Builds libgraspgpu.so (CUDA, sm_103a) in-tree.
+"""Builds libgraspgpu.so (CUDA, sm_103a) and libgraspangular.so (host C++,
+the T/V list producer) in-tree.
 
 Run ``python -m grasp_gb300.build`` or call :func:`build`. Objects go to
 ``grasp_gb300/_build/``; translation units compile in parallel.
@@ -23,8 +24,10 @@ NVCC_FLAGS = GENCODE + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
 NO_FMAD = {"radial.cu", "setham.cu", "spmv.cu", "ltile.cu", "davidson.cu"}  # exact FP64 sums; error-free double-float steps
 CU_SOURCES = ["ctx.cu", "radial.cu", "setham.cu", "spmv.cu", "ltile.cu", "davidson.cu", "bdvd.cu"]
 CPP_SOURCES = ["hosteig.cpp"]
+ANGULAR_SOURCES = ["angular.cpp"]
 
 LIB_GPU = os.path.join(OUT, "libgraspgpu.so")
+LIB_ANGULAR = os.path.join(OUT, "libgraspangular.so")
 
 
 def _nvcc() -> str:
@@ -77,11 +80,16 @@ def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = Fals
         objs.append(obj)
         if force or _stale(obj, [src] + hdrs):
             jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-I" + INC, "-c", src, "-o", obj])
+    relink = bool(jobs)
+    ang_srcs = [os.path.join(CSRC, f) for f in ANGULAR_SOURCES]
+    if force or _stale(LIB_ANGULAR, ang_srcs + hdrs):
+        jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I" + INC, "-o", LIB_ANGULAR] + ang_srcs +
+                    ["-lpthread"])
     logs = []
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         for out in ex.map(_run, jobs):
             logs.append(out)
-    if force or jobs or not os.path.exists(LIB_GPU):
+    if force or relink or not os.path.exists(LIB_GPU):
         _run([nvcc] + GENCODE + ["-shared", "-o", LIB_GPU] + objs)
     if verbose:
         for l in logs:

@@ -580,3 +580,134 @@ def read_res(path):
 
 def exists(path):
     return os.path.exists(path)
+
+
+# ---------------------------------------------------------------------------
+# CSF lists (.c)
+# ---------------------------------------------------------------------------
+
+@dataclass
+class CslBlock:
+    """One J/parity block of a CSF list, as LODCSH2 reads it
+    (lib9290/lodcsh2.f90:150-330): per CSF the occupation of every subshell,
+    the 2J and seniority of the open ones and the intermediate couplings."""
+    two_j: int
+    parity: int           # +1 even, -1 odd
+    iq: np.ndarray        # uint8 [ncsf, nw]: electrons per subshell (IQ)
+    jqs: np.ndarray       # int32 [ncsf, nw]: 2J of each open subshell, 0 for empty and closed ones
+    nu: np.ndarray        # int32 [ncsf, nw]: seniority where the list gives it, else 0
+    xj: np.ndarray        # int32 [ncsf, nw]: 2X after each open subshell (JCUP), -1 elsewhere
+
+    @property
+    def ncsf(self):
+        return self.iq.shape[0]
+
+
+@dataclass
+class CslFile:
+    subshells: list       # (n, kappa) in list order: core subshells, then peel subshells
+    labels: list
+    ncore: int
+    blocks: list
+
+
+_SHELL_L = "spdfghiklmn"
+
+
+def subshell_kappa(label):
+    """'4p-' -> (4, 1), '4p' -> (4, -2): j = l - 1/2 for a trailing '-'."""
+    label = label.strip()
+    neg = label.endswith("-")
+    body = label[:-1] if neg else label
+    n, l = int(body[:-1]), _SHELL_L.index(body[-1])
+    return n, (l if neg else -(l + 1))
+
+
+def _two_j(tok):
+    tok = tok.strip().rstrip("+-")
+    return int(tok[:-2]) if tok.endswith("/2") else 2 * int(tok)
+
+
+def read_csl(path) -> CslFile:
+    """A GRASP CSF list (rcsfgenerate's .c file, read by LODCSH/LODCSH2):
+    the core and peel subshell records, then three lines per CSF — the
+    occupied peel subshells with their occupations, the 2J (and, where
+    ambiguous, seniority 'nu;J') of each open subshell, the intermediate
+    couplings of the open subshells after the first whose J is not zero,
+    and the final J with the parity sign — blocks separated by ' *'."""
+    lines = open(path).read().splitlines()
+    core = lines[lines.index("Core subshells:") + 1].split()
+    peel = lines[lines.index("Peel subshells:") + 1].split()
+    labels = core + peel
+    shells = [subshell_kappa(s) for s in labels]
+    index = {s: i for i, s in enumerate(labels)}
+    nw = len(shells)
+    cap = [2 * abs(k) for _, k in shells]
+    body = lines[lines.index("CSF(s):") + 1:]
+    blocks, cur = [], []
+
+    def flush():
+        if not cur:
+            return
+        iq = np.array([c[0] for c in cur], np.uint8)
+        jqs = np.array([c[1] for c in cur], np.int32)
+        nu = np.array([c[2] for c in cur], np.int32)
+        xj = np.array([c[3] for c in cur], np.int32)
+        tj = {c[4] for c in cur}
+        par = {c[5] for c in cur}
+        if len(tj) != 1 or len(par) != 1:
+            raise ValueError("a block holds CSFs of one J and parity")
+        blocks.append(CslBlock(tj.pop(), par.pop(), iq, jqs, nu, xj))
+        cur.clear()
+
+    i = 0
+    import re
+    pat = re.compile(r"(\d+[a-z]-?)\s*\(\s*(\d+)\)")
+    while i < len(body):
+        if body[i].strip() == "*":
+            flush()
+            i += 1
+            continue
+        if not body[i].strip():
+            i += 1
+            continue
+        occ_line, j_line, x_line = body[i], body[i + 1], body[i + 2]
+        i += 3
+        iq = [cap[a] if a < len(core) else 0 for a in range(nw)]
+        for lab, q in pat.findall(occ_line):
+            iq[index[lab]] = int(q)
+        jtoks = j_line.split()
+        xtoks = x_line.split()
+        parity = 1 if xtoks[-1].endswith("+") else -1
+        jqs = [0] * nw
+        nu = [0] * nw
+        xj = [-1] * nw
+        jl = xl = 0
+        jlast = None
+        for a in range(len(core), nw):
+            if iq[a] == 0 or iq[a] == cap[a]:
+                continue
+            tok = jtoks[jl]
+            jl += 1
+            if ";" in tok:
+                s, t = tok.split(";")
+                nu[a] = int(s)
+                jqs[a] = _two_j(t)
+            else:
+                jqs[a] = _two_j(tok)
+            if jlast is None:
+                jlast = jqs[a]
+            elif jqs[a] == 0:
+                pass
+            else:
+                jlast = _two_j(xtoks[xl])
+                xl += 1
+            xj[a] = jlast
+        final = _two_j(xtoks[-1])
+        if jlast is None:
+            jlast = 0
+        if final != jlast:
+            raise ValueError(f"{path}: final J does not match the couplings of CSF {len(cur) + 1}")
+        cur.append((iq, jqs, nu, xj, final, parity))
+    flush()
+    return CslFile(shells, labels, len(core), blocks)

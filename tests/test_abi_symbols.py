@@ -1,5 +1,6 @@
 """The C-ABI library loads on a machine without a GPU and exports every
-function include/grasp_gpu.h declares; the synthetic-input library
+function include/grasp_gpu.h declares, the angular-coefficient library
+every function include/grasp_angular.h declares; the synthetic-input library
 (inputs/) exports what inputs/grasp_synth.h declares. No compute calls here."""
 import ctypes
 import os
@@ -14,7 +15,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared(header):
     src = open(os.path.join(ROOT, header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:gg|gs)_\w+)\s*\(", src, flags=re.M)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b((?:gg|gs|ga)_\w+)\s*\(", src, flags=re.M)
     return sorted(set(names))
 
 
@@ -42,6 +43,15 @@ def test_synth_header_symbols_exported(libs):
     names = declared("inputs/grasp_synth.h")
     syms = exported(libs[1])
     assert not [n for n in names if n not in syms]
+
+
+def test_angular_header_symbols_exported(libs):
+    from grasp_gb300 import angular, build
+    names = declared("include/grasp_angular.h")
+    assert len(names) >= 6
+    syms = exported(build.LIB_ANGULAR)
+    assert not [n for n in names if n not in syms]
+    assert set(names) <= set(angular.SYMBOLS)
 
 
 def test_gpu_library_loads_and_reports_errors(libs):
