@@ -181,6 +181,29 @@ def cpu_sample(w, nthreads, loops, gpu_loops=None):
                            loops=n_loops)
 
 
+def oracle_parity(w, ev, vec, emt_gpu, nthreads):
+    """The GPU's solve of the timed workload against the oracle's on the same
+    inputs: SETHAM (EMT, EAV) and MANEIG (rci's INIEST2 + DVDSON, MBLOCK = 1,
+    rci90/maneig.f90:389-555) with all host threads."""
+    import numpy as np
+
+    import oracle
+    oracle.build()
+    b = w.block
+    t0 = time.perf_counter()
+    o = oracle.Oracle(n=w.n, rnt=w.rnt, h=w.h, c=w.c, zz=w.zz)
+    o.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    o.genintrk(nthreads=nthreads)
+    emt = o.setham(b.ncf, b.nnz, b.iendc, b.iq, b.tlist, b.vlists)
+    oracle.shift_eav(b.ncf, b.iendc, emt)
+    ev0, vec0, info = oracle.maneig(0, b.ncf, w.nroots, b.iendc, b.irow, emt, nthreads=nthreads)
+    return {"max_abs_dE_vs_oracle_Eh": float(np.abs(ev - ev0).max()),
+            "max_vec_diff_vs_oracle": float(np.abs(vec - vec0).max()),
+            "max_emt_diff_rel": float(np.abs(emt_gpu - emt).max() / np.abs(emt).max()),
+            "oracle_loops": info["nloops"], "oracle_s": time.perf_counter() - t0, "oracle_threads": nthreads,
+            "oracle": "oracle GENINTRK + SETHAM + MANEIG (INIEST2 + DVDSON, MBLOCK = 1) on the same inputs"}
+
+
 def batched_leg(local, steps, cpu=True):
     """The 310-block workload (workloads.batch: 31 ions x 10 J/parity blocks,
     3 roots each): all blocks assembled on the device, then MANEIG for all of
@@ -226,6 +249,8 @@ def batched_leg(local, steps, cpu=True):
     out["first_solve_s"] = t_first
     out["ci_solve_e2e_s"] = t_asm + t_first
     if cpu:
+        import concurrent.futures as cf
+
         import oracle
         oracle.build()
         t = time.perf_counter()
@@ -236,6 +261,19 @@ def batched_leg(local, steps, cpu=True):
         out["cpu_baseline"] = {"value": per_ion * len(w.zs), "unit": "s", "cores": 1, "kind": "port",
                                "sample": f"oracle MANEIG (dense DSPEVX, rci's path for NCF <= 2000) on the "
                                          f"{len(w.blocks)} blocks of one ion: {per_ion:.2f} s, x {len(w.zs)} ions"}
+        # every block of the split solve against the oracle's MANEIG of that block
+        nb = len(w.blocks)
+        jobs = [(w.blocks[i % nb][2], hs[i].emt()) for i in range(len(hs))]
+
+        def ref(job):
+            b, emt = job
+            return oracle.maneig(0, b.ncf, w.nroots, b.iendc, b.irow, emt)[:2]
+
+        with cf.ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+            refs = list(ex.map(ref, jobs))
+        out["max_abs_dE_vs_oracle_Eh"] = float(max(np.abs(a[0] - r[0]).max() for a, r in zip(res["split"], refs)))
+        out["max_vec_diff_vs_oracle"] = float(max(np.abs(a[1] - r[1]).max() for a, r in zip(res["split"], refs)))
+        out["blocks_checked_vs_oracle"] = len(refs)
     return out
 
 
@@ -460,6 +498,8 @@ def run_ours(a):
     ms_split, _ = H.matvec_timing(SPLIT, 50)
     ms_64, _ = H.matvec_timing(FP64, 50)
     ms_spmm_alone, spmm_bytes = H.spmm_timing(w.nroots, 50)
+    # the SpMV autotuner's choices for this matrix and the timings behind them
+    tuning = {f"block_matvec_m{w.nroots}": H.tune(0, w.nroots), "single_vector_matvec": H.tune(1)}
     ms_spmm = sp_ms / sp_n if sp_n > 0 else ms_spmm_alone
     peak, peak_kind = _peaks()
     achieved = spmm_bytes / (ms_spmm * 1e-3) / 1e9
@@ -485,10 +525,12 @@ def run_ours(a):
     batched = batched_leg(local, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
     rk = rk_leg(local) if not a.no_extra else None
     cpu = None
+    parity = None
     if rank == 0 and not a.no_cpu_baseline:
         # the reference's DVDSON runs MBLOCK = 1: extrapolate to that loop count
         est, desc, parts = cpu_sample(w, 1, a.cpu_loops, gpu_loops=loops_mblock1 + 1)
         cpu = {"value": est, "unit": "s", "cores": 1, "kind": "port", "sample": desc}
+        parity = oracle_parity(w, ev, vec, H.emt(), os.cpu_count() or 1)
     if rank != 0:
         return 0
     out = {
@@ -501,6 +543,7 @@ def run_ours(a):
         "fp64_ci_solve_s": t_fp64,
         "split_ci_solve_mblock1_s": t_ref_mblock,
         "max_abs_dE_split_vs_fp64_Eh": dE,  # against FP64 with rci's MBLOCK = 1
+        "parity_vs_oracle": parity,
         "matvec": {"in_solve_split_us": ms_insolve * 1e3, "in_solve_launches": int(mv_n),
                    "standalone_split_us": ms_split * 1e3, "standalone_fp64_us": ms_64 * 1e3,
                    "alg_bytes": alg_bytes, "standalone_split_gbs": alg_bytes / (ms_split * 1e-3) / 1e9,
@@ -514,6 +557,7 @@ def run_ours(a):
                      "peak_kind": peak_kind,
                      "note": "reads the matrix once for all vectors; limited by FP32 Dot2 issue and L1 gathers, "
                              "not by HBM"},
+        "autotune": tuning,
         "stages": stage,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(l1 - l0),

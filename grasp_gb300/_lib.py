@@ -70,6 +70,9 @@ GPU_SYMBOLS = {
     "gg_matvec_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _d, _d]),
     "gg_spmm_timing": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, _d, _d]),
     "gg_projected_eig": (C.c_int, [C.c_int, _d, C.c_int, C.c_int, _d, _d]),
+    "gg_hmat_tune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _int, _int, _d]),
+    "gg_hmat_tune_force": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "gg_tune_variant_name": (C.c_char_p, [C.c_int, C.c_int]),
 }
 
 

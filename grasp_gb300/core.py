@@ -226,6 +226,18 @@ class HMatrix:
         return ev, vec.T.copy(), info
 
 
+    def tune(self, kernel, m=1):
+        """The SpMV autotuner's result for this matrix (include/grasp_gpu.h,
+        gg_hmat_tune): dict(chosen=name, ms={name: ms per launch})."""
+        ch = C.c_int(); nv = C.c_int()
+        ms = np.zeros(16)
+        check(_lib.gpu().gg_hmat_tune(self._h, kernel, m, C.byref(ch), C.byref(nv), ptr(ms, _d)))
+        name = lambda v: _lib.gpu().gg_tune_variant_name(kernel, v).decode()  # noqa: E731
+        return dict(chosen=name(ch.value), ms={name(v): float(ms[v]) for v in range(nv.value)})
+
+    def tune_force(self, kernel, m, variant):
+        check(_lib.gpu().gg_hmat_tune_force(self._h, kernel, m, variant))
+
     def matvec_timing(self, precision=FP64, iters=20):
         """(ms per y = H x launch, algorithmic bytes per launch)."""
         ms = C.c_double(); by = C.c_double()

@@ -1508,10 +1508,8 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   }
   GG_CUDA(cudaGetLastError());
   // the iteration, captured once and replayed until no block is active
-  bool use_graph = true;
-  if (const char *e = getenv("GRASP_GPU_DVD_GRAPH")) use_graph = (e[0] != '0');
   int per_iter = 0;
-  if (use_graph) {
+  {
     GG_CUDA(cudaStreamCreateWithFlags(&B.s2, cudaStreamNonBlocking));
     GG_CUDA(cudaEventCreateWithFlags(&B.evFork, cudaEventDisableTiming));
     GG_CUDA(cudaEventCreateWithFlags(&B.evJoin, cudaEventDisableTiming));
@@ -1529,12 +1527,7 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   }
   int iters = 0;
   for (;;) {
-    if (use_graph) {
-      GG_CUDA(cudaGraphLaunch(B.gexec, s));
-    } else {
-      per_iter = 0;
-      GG_TRY(B.enqueue_iteration(s, false, &per_iter));
-    }
+    GG_CUDA(cudaGraphLaunch(B.gexec, s));
     launches += per_iter;
     ++iters;
     GG_CUDA(cudaStreamSynchronize(s));

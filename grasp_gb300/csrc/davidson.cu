@@ -586,302 +586,6 @@ __global__ void k_final_res_part(const double *__restrict__ B, const double *__r
 }
 
 // ---------------------------------------------------------------------------
-// The single-vector pass as one cooperative kernel. Blocks own contiguous row
-// ranges for the N-length work; phases that need a global result (a norm, the
-// Gram-Schmidt coefficients, the complete x for the matvec) are separated by
-// grid barriers. Column sums over the blocks' partials are spread over the
-// blocks (block b adds column b, b + G, ...). Every spin on a barrier is
-// bounded: past the limit the kernel sets an error flag and returns.
-// ---------------------------------------------------------------------------
-constexpr int PT = 512;          // threads per block
-constexpr int PR = 64;           // rows per row-product tile
-constexpr int PCH = PT / PR;     // column chunks per row in a tile
-constexpr int PMAXR = 1024;      // rows per block, at most
-constexpr unsigned long long SPIN_LIMIT = 1ull << 24;  // barrier polls (~seconds) before giving up
-
-struct PassArgs {
-  double *B, *AB;
-  int64_t ld;
-  int n, rows;                  // rows per block
-  const IterParams *P;
-  const double *svec;
-  double *diag;                 // preconditioner diagonal (updated in place)
-  int precision;
-  const int64_t *sptr;          // full symmetric CSR of the block
-  const int32_t *scol;
-  const double *sval;
-  const float *shi, *slo;
-  const double *mdiag;          // H's diagonal (FP64 term of the split matvec)
-  float2 *xs;
-  double *part1;                // [G]
-  double *part2;                // [(lim + 1) G]
-  double *coef;                 // [lim + 1]
-  double *out;                  // S column [lim + 1]
-  double *scal;                 // SC_* slots
-  unsigned *bar;                // [0] arrivals, [1] generation
-  int *err;
-  unsigned long long *tmv;      // [0] accumulated matvec-phase ns
-};
-
-// grid barrier (all blocks co-resident: cooperative launch)
-__device__ __forceinline__ bool gsync(const PassArgs &A, int *s_ok) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned *gen = A.bar + 1;
-    const unsigned g = *gen;
-    int ok = 1;
-    __threadfence();
-    if (atomicAdd(A.bar, 1u) == gridDim.x - 1) {
-      atomicExch(A.bar, 0u);
-      __threadfence();
-      atomicAdd(A.bar + 1, 1u);
-    } else {
-      unsigned long long it = 0;
-      while (*gen == g) {
-        if (++it > SPIN_LIMIT) {
-          atomicExch(A.err, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    __threadfence();
-    *s_ok = ok && (*(volatile int *)A.err == 0);
-  }
-  __syncthreads();
-  return *s_ok != 0;
-}
-
-// part2[j G + b] = sum over this block's rows of X[i, j] ws[i - r0], j < kk
-__device__ __forceinline__ void pass_coldots(const double *X, int64_t ld, int kk, const double *ws, int r0, int nr,
-                                             double *part2, int G) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const bool hi16 = (lane & 16) != 0, hi8 = (lane & 8) != 0;
-  const int ngrp = (kk + 3) / 4;
-  for (int g = wid; g < ngrp; g += PT / 32) {
-    const int j0 = g * 4;
-    const int m = min(4, kk - j0);
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-    const double *x0 = X + (size_t)j0 * ld + r0;
-    for (int t = lane; t < nr; t += 32) {
-      const double wv = ws[t];
-      a0 = fma(__ldcg(x0 + t), wv, a0);
-      if (m > 1) a1 = fma(__ldcg(x0 + t + ld), wv, a1);
-      if (m > 2) a2 = fma(__ldcg(x0 + t + 2 * ld), wv, a2);
-      if (m > 3) a3 = fma(__ldcg(x0 + t + 3 * ld), wv, a3);
-    }
-    const double s0 = hi16 ? a0 : a2, s1 = hi16 ? a1 : a3;
-    const double k0 = (hi16 ? a2 : a0) + __shfl_xor_sync(0xffffffffu, s0, 16);
-    const double k1 = (hi16 ? a3 : a1) + __shfl_xor_sync(0xffffffffu, s1, 16);
-    double v = (hi8 ? k1 : k0) + __shfl_xor_sync(0xffffffffu, hi8 ? k0 : k1, 8);
-    v += __shfl_xor_sync(0xffffffffu, v, 4);
-    v += __shfl_xor_sync(0xffffffffu, v, 2);
-    v += __shfl_xor_sync(0xffffffffu, v, 1);
-    const int q = (lane >> 3) & 3;
-    if ((lane & 7) == 0 && q < m) part2[(size_t)(j0 + q) * G + blockIdx.x] = v;
-  }
-}
-
-// out[j] = f sum_q part2[j G + q] for the columns j = b, b + G, ... < kk
-__device__ __forceinline__ void pass_colreduce(const double *part2, int G, int kk, double f, bool scaled, double *out,
-                                               double *red) {
-  for (int j = blockIdx.x; j < kk; j += G) {
-    double u = 0.0;
-    for (int q = threadIdx.x; q < G; q += PT) u += __ldcg(part2 + (size_t)j * G + q);
-    u = block_sum<PT>(u, red);
-    if (threadIdx.x == 0) out[j] = scaled ? f * u : u;
-    __syncthreads();
-  }
-}
-
-// sum_q part1[q] in block order (the same value in every block)
-__device__ __forceinline__ double pass_total(const double *part1, int G, double *red, double *s_val) {
-  double u = 0.0;
-  for (int q = threadIdx.x; q < G; q += PT) u += __ldcg(part1 + q);
-  u = block_sum<PT>(u, red);
-  if (threadIdx.x == 0) *s_val = u;
-  __syncthreads();
-  return *s_val;
-}
-
-// w <- f w - X[:, 0:kk) v for this block's rows (w in ws and in column c of
-// X); returns this thread's sum of the new w^2 (chunk-0 threads only)
-__device__ __forceinline__ double pass_rowupdate(double *X, int64_t ld, int kk, const double *v, double *wc,
-                                                 double *ws, int r0, int r1, double f, bool scaled,
-                                                 double (*pt)[PR]) {
-  const int rl = threadIdx.x % PR, ch = threadIdx.x / PR;
-  const int per = (kk + PCH - 1) / PCH, jb = min(kk, ch * per), je = min(kk, jb + per);
-  double sq = 0.0;
-  for (int base = r0; base < r1; base += PR) {
-    const int i = base + rl;
-    pt[ch][rl] = (i < r1) ? chunk_dot(X + i, ld, v, jb, je) : 0.0;
-    __syncthreads();
-    if (ch == 0 && i < r1) {
-      double t = pt[0][rl];
-#pragma unroll
-      for (int q = 1; q < PCH; ++q) t += pt[q][rl];
-      const double w0 = scaled ? f * ws[i - r0] : ws[i - r0];
-      const double wn = w0 - t;
-      ws[i - r0] = wn;
-      wc[i] = wn;
-      sq = fma(wn, wn, sq);
-    }
-    __syncthreads();
-  }
-  return sq;
-}
-
-__global__ void __launch_bounds__(PT, 2) k_pass(PassArgs A) {
-  __shared__ double sv[SV_MAX];
-  __shared__ double ta[PCH][PR], tb[PCH][PR];
-  __shared__ double ws[PMAXR];
-  __shared__ double red[PT / 32];
-  __shared__ double s_val[4];
-  __shared__ int s_ok;
-  const IterParams P = *A.P;
-  const int G = gridDim.x, tid = threadIdx.x;
-  const int n = A.n, c = P.c, k = P.k;
-  const int r0 = min(n, blockIdx.x * A.rows), r1 = min(n, r0 + A.rows), nr = r1 - r0;
-  double *Bc = A.B + (size_t)c * A.ld, *ABc = A.AB + (size_t)c * A.ld;
-
-  // ---- Ritz vector b = BASIS s, residual r = AB s - lambda b (NEWVEC)
-  for (int j = tid; j < k; j += PT) sv[j] = A.svec[j];
-  __syncthreads();
-  double sq = 0.0;
-  {
-    const int rl = tid % PR, ch = tid / PR;
-    const int per = (k + PCH - 1) / PCH, jb = min(k, ch * per), je = min(k, jb + per);
-    for (int base = r0; base < r1; base += PR) {
-      const int i = base + rl;
-      double bs = 0.0, as = 0.0;
-      if (i < r1) {
-        bs = chunk_dot(A.B + i, A.ld, sv, jb, je);
-        as = chunk_dot(A.AB + i, A.ld, sv, jb, je);
-      }
-      tb[ch][rl] = bs;
-      ta[ch][rl] = as;
-      __syncthreads();
-      if (ch == 0 && i < r1) {
-        double bb = tb[0][rl], aa = ta[0][rl];
-#pragma unroll
-        for (int q = 1; q < PCH; ++q) {
-          bb += tb[q][rl];
-          aa += ta[q][rl];
-        }
-        const double r = fma(-P.lam, bb, aa);
-        Bc[i] = bb;
-        ABc[i] = r;
-        sq = fma(r, r, sq);
-      }
-      __syncthreads();
-    }
-  }
-  sq = block_sum<PT>(sq, red);
-  if (tid == 0) A.part1[blockIdx.x] = sq;
-  if (!gsync(A, &s_ok)) return;
-  const double rn2 = pass_total(A.part1, G, red, s_val);
-  const double res = sqrt(rn2);
-  const double rhseps = (P.gap > res) ? sqrt(P.dl * res) : fmin(P.dl, sqrt(P.dl));
-  const bool conv = res < P.critr;
-  if (blockIdx.x == 0 && tid == 0) {
-    A.scal[SC_RN2] = rn2;
-    A.scal[SC_RHS] = rhseps;
-    A.scal[SC_CONV] = conv ? 1.0 : 0.0;
-  }
-  if (conv) return;  // the same decision in every block
-
-  // ---- robust shift + preconditioner, then C1 = BASIS^T w
-  for (int t = tid; t < nr; t += PT) ws[t] = precond_row(Bc, ABc, A.diag, r0 + t, rhseps, P.lam);
-  __syncthreads();
-  pass_coldots(A.B, A.ld, k, ws, r0, nr, A.part2, G);
-  if (!gsync(A, &s_ok)) return;
-  pass_colreduce(A.part2, G, k, 1.0, false, A.coef, red);
-  if (!gsync(A, &s_ok)) return;
-
-  // ---- w1 = w - BASIS C1, |w1|^2, D2 = BASIS^T w1
-  for (int j = tid; j < k; j += PT) sv[j] = __ldcg(A.coef + j);
-  __syncthreads();
-  sq = pass_rowupdate(A.B, A.ld, k, sv, Bc, ws, r0, r1, 1.0, false, ta);
-  sq = block_sum<PT>(sq, red);
-  if (tid == 0) A.part1[blockIdx.x] = sq;
-  pass_coldots(A.B, A.ld, k, ws, r0, nr, A.part2, G);
-  if (!gsync(A, &s_ok)) return;
-  const double f1 = 1.0 / sqrt(pass_total(A.part1, G, red, s_val));
-  pass_colreduce(A.part2, G, k, f1, true, A.coef, red);  // C2 = f1 D2
-  if (!gsync(A, &s_ok)) return;
-
-  // ---- w2 = f1 w1 - BASIS C2, f2 = 1/|w2|, x = f2 w2
-  for (int j = tid; j < k; j += PT) sv[j] = __ldcg(A.coef + j);
-  __syncthreads();
-  sq = pass_rowupdate(A.B, A.ld, k, sv, Bc, ws, r0, r1, f1, true, ta);
-  sq = block_sum<PT>(sq, red);
-  if (tid == 0) A.part1[blockIdx.x] = sq;
-  if (!gsync(A, &s_ok)) return;
-  const double f2 = 1.0 / sqrt(pass_total(A.part1, G, red, s_val));
-  for (int t = tid; t < nr; t += PT) {
-    const double x = f2 * ws[t];
-    ws[t] = x;
-    Bc[r0 + t] = x;
-    if (A.precision == GG_SPLIT) {
-      const float hv = __double2float_rn(x);
-      A.xs[r0 + t] = make_float2(hv, __double2float_rn(x - (double)hv));
-    }
-  }
-  if (!gsync(A, &s_ok)) return;
-
-  // ---- y = H x (OP): one warp per row, rows strided over all warps
-  unsigned long long t0 = 0;
-  if (blockIdx.x == 0 && tid == 0) asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
-  {
-    const int lane = tid & 31;
-    const int gw = blockIdx.x * (PT / 32) + (tid >> 5), nw = G * (PT / 32);
-    for (int row = gw; row < n; row += nw) {
-      const int64_t p0 = A.sptr[row], p1 = A.sptr[row + 1];
-      double y;
-      if (A.precision == GG_SPLIT) {
-        df acc = {0.f, 0.f};
-#pragma unroll 4
-        for (int64_t p = p0 + lane; p < p1; p += 32) {
-          const float ah = __ldg(A.shi + p), al = __ldg(A.slo + p);
-          const float2 xv = __ldcg(A.xs + __ldg(A.scol + p));
-          const float ph = ah * xv.x;
-          const float pe = fmaf(ah, xv.x, -ph);
-          const float cross = fmaf(ah, xv.y, fmaf(al, xv.x, pe));
-          acc = df_add(acc, two_sum(ph, cross));
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          df other;
-          other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
-          other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
-          acc = df_add(acc, other);
-        }
-        y = ((double)acc.h + (double)acc.l) + A.mdiag[row] * __ldcg(Bc + row);
-      } else {
-        double acc = 0.0;
-        for (int64_t p = p0 + lane; p < p1; p += 32) acc = fma(__ldg(A.sval + p), __ldcg(Bc + __ldg(A.scol + p)), acc);
-        y = warp_sum(acc);
-      }
-      if (lane == 0) ABc[row] = y;
-    }
-  }
-  if (!gsync(A, &s_ok)) return;
-  if (blockIdx.x == 0 && tid == 0) {
-    unsigned long long t1;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t1));
-    A.tmv[0] += t1 - t0;
-  }
-
-  // ---- S(0:c, c) = BASIS(:, 0:c]^T y (ADDS)
-  for (int t = tid; t < nr; t += PT) ws[t] = __ldcg(ABc + r0 + t);
-  __syncthreads();
-  pass_coldots(A.B, A.ld, k + 1, ws, r0, nr, A.part2, G);
-  if (!gsync(A, &s_ok)) return;
-  pass_colreduce(A.part2, G, k + 1, 1.0, false, A.out, red);
-}
-
-// ---------------------------------------------------------------------------
 // Block Gram-Schmidt for the block pass (MBLOCK > 1). The m new columns
 // kpass .. kpass+m-1 (kpass = pv[0].c on the device) are orthogonalised
 // against the basis by two passes of block classical Gram-Schmidt, then among
@@ -1502,18 +1206,10 @@ struct Dvd {
   std::vector<cudaGraphExec_t> bexec;
   std::vector<int> bkernels;
   std::vector<int> buses;         // block passes run per width
-  bool use_graph = true;          // GRASP_GPU_DVD_GRAPH=0 launches the same pass kernel by kernel
-  // block passes with NEWVEC's choices on the device (GRASP_GPU_DVD_FUSED=0:
-  // on the host, with a wait for the residual norms)
+  bool use_graph = true;          // passes replayed as CUDA graphs
+  // block passes with NEWVEC's choices on the device (one host wait per
+  // pass); more than MT_MAX targets take the host path
   bool use_fused = true;
-  // single-vector pass as one cooperative kernel with grid barriers
-  // (GRASP_GPU_DVD_PASS=persistent). Off by default: on GB300 the separate
-  // kernels run at full occupancy and finish the pass sooner.
-  bool use_pass = false;
-  int pass_grid = 0, pass_rows = 0;
-  DBuf<unsigned> pbar;
-  DBuf<double> pcoef;
-  DBuf<unsigned long long> ptmv;
 
   double *scal() { return dots.p + lim + 8; }
   IterParams *dpar() { return reinterpret_cast<IterParams *>(dup.p); }
@@ -1584,41 +1280,10 @@ struct Dvd {
     GG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)ld * lim * 8, s));
     GG_CUDA(cudaMemsetAsync(AB.p, 0, (size_t)ld * lim * 8, s));
     if (precision == GG_SPLIT) GG_TRY(h->dXs.alloc(n));
-    const char *e = std::getenv("GRASP_GPU_DVD_GRAPH");
-    use_graph = !(e && e[0] == '0');
-    const char *ef = std::getenv("GRASP_GPU_DVD_FUSED");
-    use_fused = !(ef && ef[0] == '0');
-    const char *e2 = std::getenv("GRASP_GPU_DVD_PASS");
-    use_pass = (e2 && std::strcmp(e2, "persistent") == 0);
-    if (use_pass) {
-      int bps = 0;
-      GG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_pass, PT, 0));
-      pass_grid = std::min(bps, 2) * ctx->sms;
-      if (pass_grid < 1 || (int64_t)pass_grid * PMAXR < n) {
-        use_pass = false;  // rows per block would exceed the shared staging
-      } else {
-        pass_rows = (n + pass_grid - 1) / pass_grid;
-        GG_TRY(pbar.alloc(2));
-        GG_TRY(pcoef.alloc(lim + 2));
-        GG_TRY(ptmv.alloc(1));
-        GG_CUDA(cudaMemsetAsync(pbar.p, 0, 2 * sizeof(unsigned), s));
-        GG_CUDA(cudaMemsetAsync(ptmv.p, 0, sizeof(unsigned long long), s));
-        if (part.n < (size_t)(lim + 2) * pass_grid + 1024) GG_TRY(part.alloc((size_t)(lim + 2) * pass_grid + 1024));
-      }
-    }
     return GG_OK;
   }
-  // the environment switches read at init
-  static bool env_off(const char *name) {
-    const char *e = std::getenv(name);
-    return e && e[0] == '0';
-  }
-  static bool env_pass() {
-    const char *e = std::getenv("GRASP_GPU_DVD_PASS");
-    return e && std::strcmp(e, "persistent") == 0;
-  }
   bool reusable(gg_hmat *hm, int prec, int nn, int lm) const {
-    return h == hm && precision == prec && n == nn && lim == lm && use_pass == env_pass();
+    return h == hm && precision == prec && n == nn && lim == lm;
   }
   // a reused workspace (same matrix, sizes and precision; allocations and
   // graphs kept) starts a new solve
@@ -1633,58 +1298,11 @@ struct Dvd {
     spmm_full_n = 0;
     bx_cols = 0;
     full_m = 0;
-    use_graph = !env_off("GRASP_GPU_DVD_GRAPH");
-    use_fused = !env_off("GRASP_GPU_DVD_FUSED");
     GG_CUDA(cudaMemsetAsync(counters.p, 0, 16 * sizeof(unsigned), s));
     GG_CUDA(cudaMemsetAsync(dots.p, 0, (lim + 8 + SC_N) * sizeof(double), s));
     std::memset(hup, 0, (size_t)(8 + lim) * sizeof(double));
     GG_CUDA(cudaMemsetAsync(B.p, 0, (size_t)ld * lim * 8, s));
     GG_CUDA(cudaMemsetAsync(AB.p, 0, (size_t)ld * lim * 8, s));
-    if (use_pass) {
-      GG_CUDA(cudaMemsetAsync(pbar.p, 0, 2 * sizeof(unsigned), s));
-      GG_CUDA(cudaMemsetAsync(ptmv.p, 0, sizeof(unsigned long long), s));
-    }
-    return GG_OK;
-  }
-  int *pass_err() { return reinterpret_cast<int *>(scal() + 15); }
-  int launch_pass() {
-    PassArgs A{};
-    A.B = B.p;
-    A.AB = AB.p;
-    A.ld = ld;
-    A.n = n;
-    A.rows = pass_rows;
-    A.P = dpar();
-    A.svec = dup.p + 8;
-    A.diag = diag.p;
-    A.precision = precision;
-    A.sptr = h->dSymPtr.p;
-    A.scol = h->dSymCol.p;
-    A.sval = h->dSymVal.p;
-    A.shi = h->dSymHi.p;
-    A.slo = h->dSymLo.p;
-    A.mdiag = h->dDiag.p;
-    A.xs = h->dXs.p;
-    A.part2 = part.p;
-    A.part1 = part.p + (size_t)(lim + 2) * pass_grid;
-    A.coef = pcoef.p;
-    A.out = dots.p;
-    A.scal = scal();
-    A.bar = pbar.p;
-    A.err = pass_err();
-    A.tmv = ptmv.p;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(pass_grid);
-    cfg.blockDim = dim3(PT);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = s;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    GG_CUDA(cudaLaunchKernelEx(&cfg, k_pass, A));
-    note_launch();
     return GG_OK;
   }
   ~Dvd() {
@@ -1750,11 +1368,6 @@ struct Dvd {
   int enqueue_single(const PSrc &ps, const int *dcol, bool in_capture) {
     const double *skip = scal() + SC_CONV;
     GG_CUDA(cudaMemcpyAsync(dup.p, hup, (size_t)(8 + lim) * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (use_pass) {
-      GG_TRY(launch_pass());
-      GG_CUDA(cudaMemcpyAsync(hdown, dots.p, (size_t)(lim + 8 + SC_N) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      return GG_OK;
-    }
     launch_ritz(ps);
     cgs2(ps, true, skip, precision == GG_SPLIT ? h->dXs.p : nullptr);
     if (in_capture) {
@@ -2024,13 +1637,11 @@ struct Dvd {
       pass_ms += pms;
     }
     const double *sc = hdown + lim + 8;
-    if (use_pass && *reinterpret_cast<const int *>(sc + 15) != 0)
-      return fail(GG_ERR_CUDA, "Davidson pass kernel: grid barrier timed out");
     *res = std::sqrt(sc[SC_RN2]);
     if (sc[SC_CONV] == 0.0) {
       const size_t off = (size_t)kpass * (kpass + 1) / 2;
       std::memcpy(S.data() + off, hdown, (size_t)(kpass + 1) * sizeof(double));
-      if (!use_pass) {
+      {
         float ms = 0.f;
         GG_CUDA(cudaEventElapsedTime(&ms, gev0, gev1));
         mv_ms += ms;
@@ -2084,12 +1695,6 @@ struct Dvd {
   }
   int collect_matvec_time() {
     GG_CUDA(cudaStreamSynchronize(s));
-    if (use_pass && ptmv.p) {
-      unsigned long long ns = 0;
-      GG_CUDA(cudaMemcpy(&ns, ptmv.p, sizeof(ns), cudaMemcpyDeviceToHost));
-      mv_ms += 1e-6 * (double)ns;
-      GG_CUDA(cudaMemsetAsync(ptmv.p, 0, sizeof(unsigned long long), s));
-    }
     for (size_t q = 0; q + 1 < ev_used; q += 2) {
       float ms = 0.f;
       GG_CUDA(cudaEventElapsedTime(&ms, evs[q], evs[q + 1]));
@@ -2798,6 +2403,7 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     P1.mblock = nvec;
     P1.lim = std::min(ns, P.lim);
     if (ns < ncf && P1.lim < P.nume + 1) P1.lim = ns;
+    GG_TRY(tune_prepare(blk, precision, P1.mblock));
     GG_TRY(workspace(0, blk, ns, P1.lim, &D1p));
     Dvd &D1 = *D1p;
     GG_CUDA(cudaMemcpyAsync(D1.diag.p, blk->dDiag.p, ns * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -2823,6 +2429,7 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   Dvd D2none;  // statistics of an absent stage 2
   if (ns < ncf) {
     // Stage 2: GDVD on the whole block from the zero-padded estimates
+    GG_TRY(tune_prepare(h, precision, P.mblock));
     GG_TRY(workspace(1, h, ncf, P.lim, &D2p));
   }
   Dvd &D2 = D2p ? *D2p : D2none;

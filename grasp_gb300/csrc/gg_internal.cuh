@@ -141,21 +141,6 @@ struct Lists {  // device copies of one block's T/V lists, concatenated in SETHA
   DBuf<double> integ;                   // [VALTEIRK | I(ab)] of the last assembly
 };
 
-constexpr int LT_TW = 1024;  // tile width of the tiled lower-triangle matvec
-
-// Tiled lower-triangle layout of the split matvec (ltile.cu)
-struct LTile {
-  bool built = false, usable = false, vals_valid = false;
-  int nj = 0, nchunks = 0, nitems = 0;
-  int64_t nslots = 0;
-  size_t smem = 0;
-  DBuf<unsigned char> blob, chunks, items;
-  DBuf<long long> slot0;
-  DBuf<int64_t> src;                    // EMT index of every slot
-  DBuf<int> jptr, jlist;                // items per column tile
-  DBuf<double> pg, ps;                  // row partials [nj][ncf], column partials [items][LT_TW]
-};
-
 }  // namespace gg
 
 struct gg_ctx {
@@ -201,7 +186,13 @@ struct gg_hmat {
   gg::DBuf<float2> dXs;                 // [ncf] split copy of the input vector
   gg::DBuf<float2> dXb;                 // [ncf][m even] split copies of m input vectors, by row
   bool sym_vals_valid = false;
-  gg::LTile lt;                         // tiled lower-triangle layout (split matvec)
+  // autotuner overrides (spmv.cu): variant per kernel (0 block, 1 single) and
+  // m, -1 = the tuned choice
+  int tune_force[2][17];
+  gg_hmat() {
+    for (auto &r : tune_force)
+      for (int &v : r) v = -1;
+  }
   // kept between gg_maneig calls (davidson.cu): the leading block of the
   // INIEST2 stage (its structure and symmetric matvec structure; values
   // recopied per call) and the Davidson workspaces with their CUDA graphs,
@@ -241,12 +232,8 @@ int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double 
                const int *dcol, cudaStream_t s);
 int spmm_cols(gg_hmat *h, const double *X, double *Y, int64_t ld, int m, cudaStream_t s);
 double spmv_bytes(const gg_hmat *h, int precision, int m);
-// ltile.cu
-int build_ltile(gg_hmat *h);
-int refresh_ltile_values(gg_hmat *h);
-int spmv_ltile(gg_hmat *h, const float2 *xs, const double *Xbase, double *Ybase, int64_t ld, const int *dcol,
-               const double *skip, cudaStream_t s);
-double ltile_bytes(const gg_hmat *h);
+// tunes the split matvec a solve with this MBLOCK launches (outside capture)
+int tune_prepare(gg_hmat *h, int precision, int mblock);
 // hosteig.cpp: lowest m eigenvalues of a packed-upper symmetric matrix and
 // the eigenvectors of the lowest mvec <= m of them; blo/bhi (may be null)
 // bound eigenvalue j from below/above

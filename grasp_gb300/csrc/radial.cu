@@ -367,129 +367,12 @@ __global__ void __launch_bounds__(256) k_rk_gemm(const RkTile *__restrict__ tile
 // nearest integer to the remainder, so |q_s| <= 64 (every step is exact in
 // FP64). Products of slice pairs (s, t) with s + t < OZ_S are exact integer
 // tensor products (|q_s q_t| <= 4096); pairs with the same q = s + t share one
-// accumulator: int32 on the mma.sync path, FP32 in TMEM on the tcgen05 path,
-// where at most 10 pairs x 256 grid points x 4096 < 2^24 keeps every partial
-// sum an exact integer between flushes. The sum over q is then
+// FP32 accumulator in tensor memory, where at most 10 pairs x 256 grid points
+// x 4096 < 2^24 keeps every partial sum an exact integer between flushes. The sum over q is then
 // sum_q acc_q 2^(eA + eY - 7(q + 2)). With OZ_S = 10 the result agrees with
 // the FP64 contraction to a few 1e-13 relative on R^k data.
 // ---------------------------------------------------------------------------
 constexpr int OZ_S = 10;
-
-// slices[s][row][i] for rows < nrows (row nrows: zeros), exps[row]
-__global__ void k_oz_split(const double *__restrict__ M, int nrows, int pitch, int K, int KP,
-                           signed char *__restrict__ slices, int *__restrict__ exps) {
-  const int row = blockIdx.x;
-  __shared__ double red[128];
-  double mx = 0.0;
-  if (row < nrows)
-    for (int i = threadIdx.x; i < K; i += blockDim.x) mx = fmax(mx, fabs(M[(size_t)row * pitch + i]));
-  red[threadIdx.x] = mx;
-  __syncthreads();
-  for (int st = 64; st > 0; st >>= 1) {
-    if ((int)threadIdx.x < st) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + st]);
-    __syncthreads();
-  }
-  mx = red[0];
-  const int e = (mx > 0.0) ? ilogb(mx) + 2 : 0;  // mx < 2^(e-1)
-  if (threadIdx.x == 0) exps[row] = e;
-  const size_t plane = (size_t)(nrows + 1) * KP;
-  for (int i = threadIdx.x; i < KP; i += blockDim.x) {
-    double x = (row < nrows && i < K) ? scalbn(M[(size_t)row * pitch + i], -e) : 0.0;  // |x| < 1/2
-#pragma unroll
-    for (int q = 0; q < OZ_S; ++q) {
-      x *= 128.0;  // |x| <= 64
-      const double t = rint(x);
-      slices[q * plane + (size_t)row * KP + i] = (signed char)(int)t;
-      x -= t;  // |x| <= 1/2
-    }
-  }
-}
-
-__device__ __forceinline__ void mma_s8(int (&c)[4], int a0, int a1, int a2, int a3, int b0, int b1) {
-  asm volatile(
-      "mma.sync.aligned.m16n8k32.row.col.s32.s8.s8.s32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
-      : "+r"(c[0]), "+r"(c[1]), "+r"(c[2]), "+r"(c[3])
-      : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// Tiles as k_rk_gemm (BM x BN); warp w computes rows (w & 1) 16 .. +16 and
-// columns (w >> 1) 16 .. +16 (two m16n8k32 tiles).
-__global__ void __launch_bounds__(256) k_rk_ozaki(const RkTile *__restrict__ tiles, const int *__restrict__ rowpair,
-                                                  const int2 *__restrict__ pairs, const signed char *__restrict__ As,
-                                                  const int *__restrict__ eA, int npairs,
-                                                  const signed char *__restrict__ Ys, const int *__restrict__ eY,
-                                                  int nf, int KP, const double *__restrict__ Y,
-                                                  const YDesc *__restrict__ yd, int np, const double *__restrict__ PF,
-                                                  const double *__restrict__ QF, int ld, const int *__restrict__ MF,
-                                                  const double *__restrict__ R, const double *__restrict__ RP,
-                                                  const double *__restrict__ RPOR, QuadConst q,
-                                                  double *__restrict__ val, long long nval,
-                                                  QuadItem *__restrict__ fb, int *__restrict__ nfb) {
-  const RkTile T = tiles[blockIdx.x];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int gid = lane >> 2, tig = lane & 3;
-  const int nrow = min(BM, T.ncA - T.r0), ncol = T.c1 - T.c0;
-  const int rb = (w & 1) * 16, cb = (w >> 1) * 16;
-  // rows of this warp's fragments (pair index, or the zero row)
-  const int r_lo = rb + gid, r_hi = rb + gid + 8;
-  const int p_lo = (r_lo < nrow) ? rowpair[T.rowpair0 + T.r0 + r_lo] : npairs;
-  const int p_hi = (r_hi < nrow) ? rowpair[T.rowpair0 + T.r0 + r_hi] : npairs;
-  int fcol[2];
-#pragma unroll
-  for (int nt = 0; nt < 2; ++nt) {
-    const int j = cb + nt * 8 + gid;
-    fcol[nt] = (j < ncol) ? T.c0 + j : nf;
-  }
-  const size_t aplane = (size_t)(npairs + 1) * KP, yplane = (size_t)(nf + 1) * KP;
-  int acc[OZ_S][2][4];
-#pragma unroll
-  for (int qq = 0; qq < OZ_S; ++qq)
-#pragma unroll
-    for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-      for (int e = 0; e < 4; ++e) acc[qq][nt][e] = 0;
-  for (int k0 = 0; k0 < KP; k0 += 32) {
-    int bf[OZ_S][2][2];
-#pragma unroll
-    for (int t = 0; t < OZ_S; ++t)
-#pragma unroll
-      for (int nt = 0; nt < 2; ++nt) {
-        const signed char *yb = Ys + t * yplane + (size_t)fcol[nt] * KP + k0 + tig * 4;
-        bf[t][nt][0] = __ldg(reinterpret_cast<const int *>(yb));
-        bf[t][nt][1] = __ldg(reinterpret_cast<const int *>(yb + 16));
-      }
-#pragma unroll
-    for (int sa = 0; sa < OZ_S; ++sa) {
-      const signed char *alo = As + sa * aplane + (size_t)p_lo * KP + k0 + tig * 4;
-      const signed char *ahi = As + sa * aplane + (size_t)p_hi * KP + k0 + tig * 4;
-      const int a0 = __ldg(reinterpret_cast<const int *>(alo));
-      const int a1 = __ldg(reinterpret_cast<const int *>(ahi));
-      const int a2 = __ldg(reinterpret_cast<const int *>(alo + 16));
-      const int a3 = __ldg(reinterpret_cast<const int *>(ahi + 16));
-#pragma unroll
-      for (int t = 0; t < OZ_S - sa; ++t)
-#pragma unroll
-        for (int nt = 0; nt < 2; ++nt) mma_s8(acc[sa + t][nt], a0, a1, a2, a3, bf[t][nt][0], bf[t][nt][1]);
-    }
-  }
-  // fold the q sums in FP64, then QUAD's head/end terms and the table position
-  const int ea_lo = eA[p_lo], ea_hi = eA[p_hi];
-#pragma unroll
-  for (int nt = 0; nt < 2; ++nt)
-#pragma unroll
-    for (int e = 0; e < 4; ++e) {
-      const int r = (e < 2) ? r_lo : r_hi;
-      const int j = cb + nt * 8 + tig * 2 + (e & 1);
-      if (r >= nrow || j >= ncol) continue;
-      const int f = T.c0 + j;
-      const int ex = ((e < 2) ? ea_lo : ea_hi) + eY[f];
-      double sum = 0.0;
-#pragma unroll
-      for (int qq = OZ_S - 1; qq >= 0; --qq) sum += scalbn((double)acc[qq][nt][e], ex - 7 * (qq + 2));
-      rk_finish(T, (e < 2) ? p_lo : p_hi, T.r0 + r, f, sum, pairs, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val,
-                nval, fb, nfb);
-    }
-}
 
 // General per-integral QUAD: TA(i) = ((P_a P_c + Q_a Q_c) RPOR) Y_f(i),
 // one warp per integral, sequential reference-order sum on lane 0.
@@ -562,7 +445,6 @@ struct RkCache {
   DBuf<double> dY, dA, scratch;
   DBuf<QuadItem> dFb;
   DBuf<__half> dYt, dAt;
-  DBuf<signed char> dAs, dYs;
 };
 
 void rk_cache_free(RkCache *c) { delete c; }
@@ -1299,23 +1181,7 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
     const int KP = (KC + 31) / 32 * 32;
     GG_TRY(C.dEA.alloc(npairs + 1));
     GG_TRY(C.dEY.alloc(nf + 1));
-    static const bool mma_sync = [] {
-      const char *e = getenv("GRASP_GPU_RK_TENSOR");
-      return e && std::strcmp(e, "mma_sync") == 0;
-    }();
-    if (mma_sync) {  // the legacy int8 mma.sync form (k_oz_split, k_rk_ozaki), kept for comparison
-      GG_TRY(C.dAs.alloc((size_t)OZ_S * (npairs + 1) * KP));
-      GG_TRY(C.dYs.alloc((size_t)OZ_S * (nf + 1) * KP));
-      k_oz_split<<<npairs + 1, 128, 0, ctx->stream>>>(C.dA.p, npairs, KC, KC, KP, C.dAs.p, C.dEA.p);
-      ::gg::note_launch();
-      k_oz_split<<<nf + 1, 128, 0, ctx->stream>>>(C.dY.p, nf, np, KC, KP, C.dYs.p, C.dEY.p);
-      ::gg::note_launch();
-      k_rk_ozaki<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(
-          C.dTiles.p, C.dRowpair.p, C.dPairs.p, C.dAs.p, C.dEA.p, npairs, C.dYs.p, C.dEY.p, nf, KP, C.dY.p, C.dYd.p,
-          np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, (long long)N, C.dFb.p,
-          C.dNfb.p);
-      ::gg::note_launch();
-    } else {
+    {
       // tcgen05: the slices written into the tile blocks, the raw GEMM parts
       // at their positions, then the head terms
       const int nch = KP / TC_KC;

@@ -611,7 +611,6 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
   L.valid = true;
   h->emt_valid = false;
   h->sym_vals_valid = false;
-  h->lt.vals_valid = false;
   return GG_OK;
 }
 
@@ -793,7 +792,6 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
   h->eav = eav;
   h->emt_valid = true;
   h->sym_vals_valid = false;
-  h->lt.vals_valid = false;
   if (eav_out) *eav_out = eav;
   return GG_OK;
 }
@@ -823,7 +821,6 @@ int gg_hmat_set_emt(gg_hmat *h, const double *emt) {
   GG_CUDA(cudaStreamSynchronize(h->ctx->stream));
   h->emt_valid = true;
   h->sym_vals_valid = false;
-  h->lt.vals_valid = false;
   h->eav = 0.0;
   return GG_OK;
 }

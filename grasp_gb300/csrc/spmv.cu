@@ -20,6 +20,9 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "gg_internal.cuh"
@@ -233,20 +236,37 @@ __global__ void k_split_x(const double *__restrict__ x, float2 *__restrict__ xs,
 }
 
 // y = H x with H_offdiag = hi + lo (FP32 pair), x = xh + xl; double-float
-// accumulation; FP64 diagonal
-template <typename CI>
+// accumulation; FP64 diagonal. LPR lanes per row (32: a warp; 16: two rows
+// per warp), U loads in flight per lane (the autotuner picks both).
+template <int LPR>
+__device__ __forceinline__ unsigned row_mask() {
+  return LPR == 32 ? 0xffffffffu : (0xffffu << (threadIdx.x & 16));
+}
+template <int LPR>
+__device__ __forceinline__ df row_reduce(df acc) {
+  const unsigned mk = row_mask<LPR>();
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) {
+    df other;
+    other.h = __shfl_xor_sync(mk, acc.h, o);
+    other.l = __shfl_xor_sync(mk, acc.l, o);
+    acc = df_add(acc, other);
+  }
+  return acc;
+}
+template <typename CI, int LPR, int U>
 __global__ void __launch_bounds__(256) k_spmv_split(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
                                                     const float *__restrict__ hi, const float *__restrict__ lo,
                                                     const float2 *__restrict__ xs, const double *__restrict__ diag,
                                                     const double *__restrict__ x, double *__restrict__ y, int n) {
-  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (row >= n) return;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) / LPR, lane = threadIdx.x % LPR;
+  if (row >= n) return;  // whole LPR-lane groups leave together
   const int64_t p0 = ptr[row], p1 = ptr[row + 1];
   df acc = {0.f, 0.f};
   // unrolled so that several iterations' loads (and the dependent x gathers)
   // are in flight together; the additions keep their order
-#pragma unroll 4
-  for (int64_t p = p0 + lane; p < p1; p += 32) {
+#pragma unroll U
+  for (int64_t p = p0 + lane; p < p1; p += LPR) {
     const float ah = __ldg(hi + p), al = __ldg(lo + p);
     const float2 xv = __ldg(xs + __ldg(col + p));
     const float ph = ah * xv.x;
@@ -254,13 +274,7 @@ __global__ void __launch_bounds__(256) k_spmv_split(const int64_t *__restrict__ 
     const float cross = fmaf(ah, xv.y, fmaf(al, xv.x, pe));
     acc = df_add(acc, two_sum(ph, cross));
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    df other;
-    other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
-    other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
-    acc = df_add(acc, other);
-  }
+  acc = row_reduce<LPR>(acc);
   if (lane == 0) y[row] = ((double)acc.h + (double)acc.l) + diag[row] * x[row];
 }
 
@@ -284,7 +298,7 @@ __global__ void __launch_bounds__(256) k_spmv64_col(const int64_t *__restrict__ 
   if (lane == 0) ABbase[off + row] = acc;
 }
 
-template <typename CI>
+template <typename CI, int LPR, int U>
 __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
                                                         const float *__restrict__ hi, const float *__restrict__ lo,
                                                         const float2 *__restrict__ xs, const double *__restrict__ diag,
@@ -292,13 +306,13 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
                                                         int64_t ld, const int *__restrict__ pc, const double *skip,
                                                         int n) {
   if (skip && *skip != 0.0) return;
-  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) / LPR, lane = threadIdx.x % LPR;
   if (row >= n) return;
   const size_t off = (size_t)(*pc) * ld;
   const int64_t p0 = ptr[row], p1 = ptr[row + 1];
   df acc = {0.f, 0.f};
-#pragma unroll 4
-  for (int64_t p = p0 + lane; p < p1; p += 32) {
+#pragma unroll U
+  for (int64_t p = p0 + lane; p < p1; p += LPR) {
     const float ah = __ldg(hi + p), al = __ldg(lo + p);
     const float2 xv = xs[__ldg(col + p)];
     const float ph = ah * xv.x;
@@ -306,13 +320,7 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
     const float cross = fmaf(ah, xv.y, fmaf(al, xv.x, pe));
     acc = df_add(acc, two_sum(ph, cross));
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    df other;
-    other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
-    other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
-    acc = df_add(acc, other);
-  }
+  acc = row_reduce<LPR>(acc);
   if (lane == 0) ABbase[off + row] = ((double)acc.h + (double)acc.l) + diag[row] * Bbase[off + row];
 }
 
@@ -325,9 +333,10 @@ __global__ void __launch_bounds__(256) k_spmv_split_col(const int64_t *__restric
 // (vectors 2u, 2u + 1), so that a load instruction touches EPW = 32 / LPE
 // whole rows of xb instead of 32 scattered ones. Products go into per-vector
 // Dot2 sums (Ogita, Rump & Oishi), added over the EPW entry slots by a fixed
-// shuffle tree in double-float.
-template <int M, typename CI>
-__global__ void __launch_bounds__(256) k_spmm_split(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
+// shuffle tree in double-float. U loads in flight per lane; any block size
+// that is a multiple of 32 up to 512 (the autotuner picks both).
+template <int M, typename CI, int U>
+__global__ void __launch_bounds__(512) k_spmm_split(const int64_t *__restrict__ ptr, const CI *__restrict__ col,
                                                     const float *__restrict__ hi, const float *__restrict__ lo,
                                                     const float2 *__restrict__ xb, const double *__restrict__ diag,
                                                     const double *__restrict__ Bbase, double *__restrict__ ABbase,
@@ -350,7 +359,7 @@ __global__ void __launch_bounds__(256) k_spmm_split(const int64_t *__restrict__ 
     sl = __fadd_rn(sl, __fadd_rn(err, t));
   };
   if (act) {
-#pragma unroll 4
+#pragma unroll U
     for (int64_t p = p0 + e; p < p1; p += EPW) {
       const float ah = __ldg(hi + p), al = __ldg(lo + p);
       const float4 x = __ldg(xr + (size_t)__ldg(col + p) * (MP / 2));
@@ -407,6 +416,199 @@ __global__ void k_col16(const int32_t *__restrict__ col, int64_t nnz, unsigned s
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// SpMV autotuner. Kernel 0 is the split block matvec over m vectors
+// (k_spmm_split<m>): 9 variants, U = 2, 4, 8 loads in flight per lane x
+// 128, 256, 512 threads per block. Kernel 1 is the single-vector split
+// matvec (k_spmv_split and its column-indexed form for the single-vector
+// pass): 6 variants, 32 or 16 lanes per row x U = 2, 4, 8. The first launch
+// of a kernel for a matrix shape (device, NCF, stored elements, column width)
+// and m that is not inside a stream capture times every variant on a
+// scratch input with CUDA events (one warm-up, three timed launches each)
+// and keeps the fastest for that shape in this process; inside a capture,
+// before any tuning, the default variant runs. gg_hmat_tune_force pins a
+// variant for one matrix.
+// ---------------------------------------------------------------------------
+constexpr int TUNE_NVAR[2] = {9, 6};
+constexpr int TUNE_DEFAULT[2] = {4, 1};   // U = 4, 256 threads; 32 lanes per row, U = 4
+constexpr int TUNE_REPS = 3;
+
+struct TuneKey {
+  int dev, kernel, m, ncf;
+  int64_t nnz;
+  bool col16;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(dev, kernel, m, ncf, nnz, col16) < std::tie(o.dev, o.kernel, o.m, o.ncf, o.nnz, o.col16);
+  }
+};
+struct TuneEntry {
+  int variant = -1;
+  double ms[16] = {};
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneEntry> g_tune;
+
+TuneKey tune_key(const gg_hmat *h, int kernel, int m) {
+  return TuneKey{h->ctx->device, kernel, kernel == 0 ? m : 1, h->ncf, h->sym_nnz, h->sym_col16};
+}
+
+template <int M, int U>
+void launch_spmm_mu(const gg_hmat *h, int tpb, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,
+                    const int *dcol, cudaStream_t s) {
+  const int n = h->ncf;
+  const unsigned blocks = (unsigned)(((int64_t)n * 32 + tpb - 1) / tpb);
+  if (h->sym_col16)
+    k_spmm_split<M, unsigned short, U><<<blocks, tpb, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p,
+                                                              xb, h->dDiag.p, Bbase, ABbase, ld, dcol, n);
+  else
+    k_spmm_split<M, int32_t, U><<<blocks, tpb, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xb,
+                                                       h->dDiag.p, Bbase, ABbase, ld, dcol, n);
+}
+template <int M>
+void launch_spmm_m(const gg_hmat *h, int variant, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,
+                   const int *dcol, cudaStream_t s) {
+  const int tpb = 128 << (variant % 3);
+  switch (variant / 3) {
+    case 0: launch_spmm_mu<M, 2>(h, tpb, xb, Bbase, ABbase, ld, dcol, s); break;
+    case 1: launch_spmm_mu<M, 4>(h, tpb, xb, Bbase, ABbase, ld, dcol, s); break;
+    default: launch_spmm_mu<M, 8>(h, tpb, xb, Bbase, ABbase, ld, dcol, s); break;
+  }
+}
+int launch_spmm(const gg_hmat *h, int m, int variant, const float2 *xb, const double *Bbase, double *ABbase,
+                int64_t ld, const int *dcol, cudaStream_t s) {
+  switch (m) {
+#define SPMM_CASE(K) \
+  case K: launch_spmm_m<K>(h, variant, xb, Bbase, ABbase, ld, dcol, s); break;
+    SPMM_CASE(1) SPMM_CASE(2) SPMM_CASE(3) SPMM_CASE(4) SPMM_CASE(5) SPMM_CASE(6) SPMM_CASE(7) SPMM_CASE(8)
+    SPMM_CASE(9) SPMM_CASE(10) SPMM_CASE(11) SPMM_CASE(12) SPMM_CASE(13) SPMM_CASE(14) SPMM_CASE(15) SPMM_CASE(16)
+#undef SPMM_CASE
+    default: return fail(GG_ERR_ARG, "spmm_block: 1 to 16 columns");
+  }
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+template <int LPR, int U>
+void launch_spmv_lu(const gg_hmat *h, const float2 *xs, const double *x, double *y, const double *Bbase,
+                    double *ABbase, int64_t ld, const int *dcol, const double *skip, bool colform, cudaStream_t s) {
+  const int n = h->ncf;
+  const unsigned blocks = (unsigned)(((int64_t)n * LPR + 255) / 256);
+  if (colform) {
+    if (h->sym_col16)
+      k_spmv_split_col<unsigned short, LPR, U><<<blocks, 256, 0, s>>>(
+          h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, xs, h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
+    else
+      k_spmv_split_col<int32_t, LPR, U><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p,
+                                                               xs, h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
+  } else {
+    if (h->sym_col16)
+      k_spmv_split<unsigned short, LPR, U><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p,
+                                                                  h->dSymLo.p, xs, h->dDiag.p, x, y, n);
+    else
+      k_spmv_split<int32_t, LPR, U><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xs,
+                                                           h->dDiag.p, x, y, n);
+  }
+}
+// the single-vector split matvec, variant v: y = H x (colform false) or the
+// column-indexed form
+int launch_spmv(const gg_hmat *h, int v, const float2 *xs, const double *x, double *y, const double *Bbase,
+                double *ABbase, int64_t ld, const int *dcol, const double *skip, bool colform, cudaStream_t s) {
+  switch (v) {
+    case 0: launch_spmv_lu<32, 2>(h, xs, x, y, Bbase, ABbase, ld, dcol, skip, colform, s); break;
+    case 1: launch_spmv_lu<32, 4>(h, xs, x, y, Bbase, ABbase, ld, dcol, skip, colform, s); break;
+    case 2: launch_spmv_lu<32, 8>(h, xs, x, y, Bbase, ABbase, ld, dcol, skip, colform, s); break;
+    case 3: launch_spmv_lu<16, 2>(h, xs, x, y, Bbase, ABbase, ld, dcol, skip, colform, s); break;
+    case 4: launch_spmv_lu<16, 4>(h, xs, x, y, Bbase, ABbase, ld, dcol, skip, colform, s); break;
+    default: launch_spmv_lu<16, 8>(h, xs, x, y, Bbase, ABbase, ld, dcol, skip, colform, s); break;
+  }
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  return GG_OK;
+}
+
+// times every variant of `kernel` for this matrix and m; records the choice
+int tune_now(gg_hmat *h, int kernel, int m, TuneEntry *out) {
+  cudaStream_t s = h->ctx->stream;
+  const int n = h->ncf, mm = kernel == 0 ? m : 1, mp = spmm_pitch(mm);
+  DBuf<double> x, y;
+  DBuf<float2> xb;
+  GG_TRY(x.alloc((size_t)n * mm));
+  GG_TRY(y.alloc((size_t)n * mm));
+  GG_TRY(xb.alloc((size_t)n * mp));
+  std::vector<double> hx((size_t)n * mm);
+  for (size_t i = 0; i < hx.size(); ++i) hx[i] = 1.0 / (1.0 + (double)(i % 97));
+  GG_CUDA(cudaMemcpyAsync(x.p, hx.data(), hx.size() * 8, cudaMemcpyHostToDevice, s));
+  k_split_block<<<(unsigned)std::min<int64_t>(((int64_t)n * mp + 255) / 256, 4096), 256, 0, s>>>(x.p, n, mm, mp, n,
+                                                                                                 xb.p);
+  ::gg::note_launch();
+  cudaEvent_t e0, e1;
+  GG_CUDA(cudaEventCreate(&e0));
+  GG_CUDA(cudaEventCreate(&e1));
+  TuneEntry t;
+  double best = 1e300;
+  int rc = GG_OK;
+  for (int v = 0; v < TUNE_NVAR[kernel] && rc == GG_OK; ++v) {
+    auto one = [&]() {
+      return kernel == 0 ? launch_spmm(h, mm, v, xb.p, x.p, y.p, n, nullptr, s)
+                         : launch_spmv(h, v, xb.p, x.p, y.p, nullptr, nullptr, 0, nullptr, nullptr, false, s);
+    };
+    rc = one();  // warm-up
+    if (rc != GG_OK) break;
+    if (cudaEventRecord(e0, s) != cudaSuccess) rc = fail(GG_ERR_CUDA, "tuner: event record");
+    for (int r = 0; r < TUNE_REPS && rc == GG_OK; ++r) rc = one();
+    if (rc != GG_OK) break;
+    if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = fail(GG_ERR_CUDA, "tuner: event wait");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    t.ms[v] = ms / TUNE_REPS;
+    if (t.ms[v] < best) {
+      best = t.ms[v];
+      t.variant = v;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc != GG_OK) return rc;
+  *out = t;
+  return GG_OK;
+}
+
+// the variant to launch: forced for this matrix, else the tuned choice for
+// its shape (tuning now when the stream is not being captured), else the
+// default
+int tune_variant(gg_hmat *h, int kernel, int m, cudaStream_t s, int *variant) {
+  const int fm = kernel == 0 ? m : 1;
+  if (h->tune_force[kernel][fm] >= 0) {
+    *variant = h->tune_force[kernel][fm];
+    return GG_OK;
+  }
+  const TuneKey key = tune_key(h, kernel, m);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      *variant = it->second.variant;
+      return GG_OK;
+    }
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GG_CUDA(cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone) {
+    *variant = TUNE_DEFAULT[kernel];
+    return GG_OK;
+  }
+  TuneEntry t;
+  GG_TRY(tune_now(h, kernel, m, &t));
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = t;
+  *variant = t.variant;
+  return GG_OK;
+}
+
 // y = H x with x = Bbase + c ld, y = ABbase + c ld, c = *dcol on the device;
 // GG_SPLIT reads x from h->dXs (the caller's split copy of the same column)
 int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
@@ -418,14 +620,9 @@ int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int
       if (h->dXs.n < (size_t)n) return fail(GG_ERR_STATE, "spmv_col: split copy of x not allocated");
       xs = h->dXs.p;
     }
-    if (h->lt.usable) return spmv_ltile(h, xs, Bbase, ABbase, ld, dcol, skip, s);
-    if (h->sym_col16)
-      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, xs,
-                                              h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
-    else
-      k_spmv_split_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xs,
-                                              h->dDiag.p, Bbase, ABbase, ld, dcol, skip, n);
-    ::gg::note_launch();
+    int v = 0;
+    GG_TRY(tune_variant(h, 1, 1, s, &v));
+    return launch_spmv(h, v, xs, nullptr, nullptr, Bbase, ABbase, ld, dcol, skip, true, s);
   } else {
     k_spmv64_col<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, Bbase, ABbase, ld, dcol, skip, n);
     ::gg::note_launch();
@@ -503,20 +700,8 @@ int build_sym(gg_hmat *h) {
   return GG_OK;
 }
 
-// The tiled lower-triangle split matvec (ltile.cu) reads each stored value
-// once but is slower than the full symmetric kernel at present; it is used
-// when GRASP_GPU_MATVEC=ltile.
-static bool want_ltile() {
-  const char *e = std::getenv("GRASP_GPU_MATVEC");
-  return e && std::strcmp(e, "ltile") == 0;
-}
-
 int refresh_sym_values(gg_hmat *h) {
   GG_TRY(build_sym(h));
-  if (want_ltile()) {
-    GG_TRY(build_ltile(h));
-    GG_TRY(refresh_ltile_values(h));
-  }
   if (h->sym_vals_valid) return GG_OK;
   cudaStream_t s = h->ctx->stream;
   GG_TRY(h->dSymVal.alloc(h->sym_nnz));
@@ -541,17 +726,9 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
     if (precision == GG_SPLIT) {
       GG_TRY(h->dXs.alloc(n));
       k_split_x<<<(n + 255) / 256, 256, 0, s>>>(x, h->dXs.p, n); ::gg::note_launch();
-      if (h->lt.usable) {
-        GG_TRY(spmv_ltile(h, h->dXs.p, x, y, 0, nullptr, nullptr, s));
-      } else {
-        if (h->sym_col16)
-          k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
-                                              h->dDiag.p, x, y, n);
-        else
-          k_spmv_split<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, h->dXs.p,
-                                              h->dDiag.p, x, y, n);
-        ::gg::note_launch();
-      }
+      int v = 0;
+      GG_TRY(tune_variant(h, 1, 1, s, &v));
+      GG_TRY(launch_spmv(h, v, h->dXs.p, x, y, nullptr, nullptr, 0, nullptr, nullptr, false, s));
     } else {
       k_spmv64<<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymVal.p, x, y, n); ::gg::note_launch();
     }
@@ -566,26 +743,10 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
 // the block form of spmv_col (SPLIT only): m new columns from kpass = *dcol
 int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,
                const int *dcol, cudaStream_t s) {
-  const int n = h->ncf;
-  const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
-  switch (m) {
-#define SPMM_CASE(K)                                                                                              \
-  case K:                                                                                                         \
-    if (h->sym_col16)                                                                                             \
-      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p, xb,       \
-                                                h->dDiag.p, Bbase, ABbase, ld, dcol, n);                          \
-    else                                                                                                          \
-      k_spmm_split<K><<<blocks, 256, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xb,         \
-                                                h->dDiag.p, Bbase, ABbase, ld, dcol, n);                          \
-    break;
-    SPMM_CASE(1) SPMM_CASE(2) SPMM_CASE(3) SPMM_CASE(4) SPMM_CASE(5) SPMM_CASE(6) SPMM_CASE(7) SPMM_CASE(8)
-    SPMM_CASE(9) SPMM_CASE(10) SPMM_CASE(11) SPMM_CASE(12) SPMM_CASE(13) SPMM_CASE(14) SPMM_CASE(15) SPMM_CASE(16)
-#undef SPMM_CASE
-    default: return fail(GG_ERR_ARG, "spmm_block: 1 to 16 columns");
-  }
-  ::gg::note_launch();
-  GG_CUDA(cudaGetLastError());
-  return GG_OK;
+  if (m < 1 || m > 16) return fail(GG_ERR_ARG, "spmm_block: 1 to 16 columns");
+  int v = 0;
+  GG_TRY(tune_variant(h, 0, m, s, &v));
+  return launch_spmm(h, m, v, xb, Bbase, ABbase, ld, dcol, s);
 }
 
 // Y = H X for m columns (2 to 16) of leading dimension ld, SPLIT: the split
@@ -597,6 +758,14 @@ int spmm_cols(gg_hmat *h, const double *X, double *Y, int64_t ld, int m, cudaStr
                                                                                                  h->dXb.p);
   ::gg::note_launch();
   return spmm_block(h, m, h->dXb.p, X, Y, ld, nullptr, s);
+}
+
+// tunes, before any capture, the kernels a solve over this matrix launches
+int tune_prepare(gg_hmat *h, int precision, int mblock) {
+  if (precision != GG_SPLIT) return GG_OK;
+  int v = 0;
+  if (mblock > 1) return tune_variant(h, 0, std::min(mblock, 16), h->ctx->stream, &v);
+  return tune_variant(h, 1, 1, h->ctx->stream, &v);
 }
 
 double spmv_bytes(const gg_hmat *h, int precision, int m) {
@@ -658,6 +827,46 @@ extern "C" int gg_matvec_timing(gg_ctx *ctx, gg_hmat *h, int precision, int iter
   *ms_per_launch = ms / iters;
   if (alg_bytes) *alg_bytes = spmv_bytes(h, precision, 1);
   return GG_OK;
+}
+
+extern "C" int gg_hmat_tune(gg_hmat *h, int kernel, int m, int *chosen, int *nvariants, double *ms) {
+  if (!h || kernel < 0 || kernel > 1 || (kernel == 0 && (m < 1 || m > 16)))
+    return fail(GG_ERR_ARG, "gg_hmat_tune: kernel 0 (m = 1..16) or 1");
+  if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_hmat_tune: EMT not set");
+  GG_CUDA(cudaSetDevice(h->ctx->device));
+  GG_TRY(refresh_sym_values(h));
+  int v = 0;
+  const int fm = kernel == 0 ? m : 1;
+  const int forced = h->tune_force[kernel][fm];
+  h->tune_force[kernel][fm] = -1;
+  const int st = tune_variant(h, kernel, m, h->ctx->stream, &v);
+  h->tune_force[kernel][fm] = forced;
+  GG_TRY(st);
+  if (chosen) *chosen = forced >= 0 ? forced : v;
+  if (nvariants) *nvariants = TUNE_NVAR[kernel];
+  if (ms) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    const TuneEntry &t = g_tune[tune_key(h, kernel, m)];
+    for (int i = 0; i < TUNE_NVAR[kernel]; ++i) ms[i] = t.ms[i];
+  }
+  return GG_OK;
+}
+
+extern "C" int gg_hmat_tune_force(gg_hmat *h, int kernel, int m, int variant) {
+  if (!h || kernel < 0 || kernel > 1 || (kernel == 0 && (m < 1 || m > 16)) || variant < -1 ||
+      variant >= TUNE_NVAR[kernel])
+    return fail(GG_ERR_ARG, "gg_hmat_tune_force: bad kernel, m or variant");
+  h->tune_force[kernel][kernel == 0 ? m : 1] = variant;
+  return GG_OK;
+}
+
+extern "C" const char *gg_tune_variant_name(int kernel, int variant) {
+  static const char *k0[9] = {"U2 T128", "U2 T256", "U2 T512", "U4 T128", "U4 T256",
+                              "U4 T512", "U8 T128", "U8 T256", "U8 T512"};
+  static const char *k1[6] = {"L32 U2", "L32 U4", "L32 U8", "L16 U2", "L16 U4", "L16 U8"};
+  if (kernel == 0 && variant >= 0 && variant < 9) return k0[variant];
+  if (kernel == 1 && variant >= 0 && variant < 6) return k1[variant];
+  return "";
 }
 
 extern "C" int gg_spicmv2(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c, int precision) {

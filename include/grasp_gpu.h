@@ -258,6 +258,28 @@ double gg_stage_stat(gg_ctx *ctx, int which);
  * eigenvalue search does not finish.                                       */
 int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double *z);
 
+/* ---- SpMV autotuner (no counterpart in the reference) ---------------------
+ * The split-precision matvec kernels come in variants: kernel 0, the block
+ * matvec over m = 1..16 vectors (Davidson block passes; gg_spicmv2 with
+ * m >= 2), 9 variants = 2, 4 or 8 loads in flight per lane x 128, 256 or
+ * 512 threads per block; kernel 1, the single-vector matvec (MBLOCK = 1
+ * passes), 6 variants = 32 or 16 lanes per row x 2, 4 or 8 loads in flight.
+ * The first launch for a matrix shape (device, NCF, stored elements) and m
+ * outside a stream capture times every variant (CUDA events; one warm-up
+ * and three timed launches each) and keeps the fastest for that shape for
+ * the rest of the process; gg_maneig tunes the widths it will use before
+ * it captures its graphs. Every variant computes the same products and
+ * sums in double-float; their results differ only by the order of the
+ * partial sums.
+ * gg_hmat_tune: tunes if needed, then reports the variant the solver
+ * launches (*chosen), the number of variants and their mean times per
+ * launch (ms[nvariants]).
+ * gg_hmat_tune_force: launch `variant` for this matrix (-1: the tuned one).
+ * gg_tune_variant_name: a short name of a variant ("U4 T256", "L16 U8").   */
+int gg_hmat_tune(gg_hmat *h, int kernel, int m, int *chosen, int *nvariants, double *ms);
+int gg_hmat_tune_force(gg_hmat *h, int kernel, int m, int variant);
+const char *gg_tune_variant_name(int kernel, int variant);
+
 /* ---- measurement helpers (no counterpart in the reference) ------------------
  * gg_launch_count: kernels this library has launched in this process.
  * gg_alloc_count: device (cudaMalloc) and pinned host (cudaMallocHost)

@@ -158,9 +158,11 @@ def test_maneig_davidson_path(gpu_ready, oracle_mod):
         assert np.abs(vec - vec0).max() <= 1e-7, (precision, np.abs(vec - vec0).max())
 
 
-def test_maneig_graph_pass_matches_launch_path(gpu_ready, monkeypatch):
-    """The single-vector pass replayed as a CUDA graph and the same pass
-    launched kernel by kernel do the same arithmetic in the same order."""
+def test_maneig_repeated_solves_bit_identical(gpu_ready):
+    """Repeated solves of one matrix (the second one replays the CUDA graphs
+    and workspaces kept with the matrix) give bit-identical eigenpairs and
+    loop counts, for single-vector and block passes in both precisions: all
+    reductions have a fixed order."""
     from grasp_gb300 import Context, HMatrix
     from inputs import synth as S
     orbs = S.orbital_set(6, 3)
@@ -177,83 +179,12 @@ def test_maneig_graph_pass_matches_launch_path(gpu_ready, monkeypatch):
     H = HMatrix(ctx, blk.ncf, blk.iendc, blk.irow)
     H.setham(blk.iq, blk.tlist, blk.vlists)
     for precision in (0, 1):
-        for robust in (False, True):
-            monkeypatch.setenv("GRASP_GPU_DVD_GRAPH", "0")
-            ev0, vec0, info0 = H.maneig(3, flavour=0, precision=precision, robust=robust)
-            monkeypatch.setenv("GRASP_GPU_DVD_GRAPH", "1")
-            ev, vec, info = H.maneig(3, flavour=0, precision=precision, robust=robust)
+        for mblock in (1, 4):
+            ev0, vec0, info0 = H.maneig(4, flavour=0, precision=precision, mblock=mblock, robust=True)
+            ev, vec, info = H.maneig(4, flavour=0, precision=precision, mblock=mblock, robust=True)
             assert info["nloops"] == info0["nloops"]
             assert np.array_equal(ev, ev0), (ev, ev0)
             assert np.array_equal(vec, vec0)
-
-
-def test_block_pass_device_newvec_matches_host(gpu_ready, monkeypatch):
-    """Block passes with NEWVEC's choices made on the device (one host wait
-    per pass) and on the host (a wait for the residual norms) give the same
-    eigenpairs; the graph and launch-by-launch forms of the fused pass are
-    bit-identical."""
-    from grasp_gb300 import Context, HMatrix
-    from inputs import synth as S
-    orbs = S.orbital_set(6, 3)
-    case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
-    occ = lambda d: S.occupation(orbs, d)  # noqa: E731
-    refs = [occ({(1, -1): 2, (2, -1): 2}), occ({(1, -1): 2, (2, 1): 2}), occ({(1, -1): 2, (2, -2): 2})]
-    blk = S.ci_block(orbs, refs, [0] * len(orbs), two_j=2, parity=0, density=0.05, seed=9)
-    ctx = Context(0)
-    ctx.set_grid(case["n"], case["rnt"], case["h"], case["c"], case["zz"])
-    ob = case["orb"]
-    ctx.set_orbitals(ob.nak, ob.mf, ob.pf, ob.qf)
-    ctx.genintrk()
-    ctx.iabint_table()
-    H = HMatrix(ctx, blk.ncf, blk.iendc, blk.irow)
-    H.setham(blk.iq, blk.tlist, blk.vlists)
-    for precision in (0, 1):
-        monkeypatch.setenv("GRASP_GPU_DVD_FUSED", "0")
-        ev0, vec0, _ = H.maneig(4, flavour=0, precision=precision, mblock=4, robust=True)
-        monkeypatch.setenv("GRASP_GPU_DVD_FUSED", "1")
-        ev1, vec1, _ = H.maneig(4, flavour=0, precision=precision, mblock=4, robust=True)
-        monkeypatch.setenv("GRASP_GPU_DVD_GRAPH", "0")
-        ev2, vec2, _ = H.maneig(4, flavour=0, precision=precision, mblock=4, robust=True)
-        monkeypatch.delenv("GRASP_GPU_DVD_GRAPH")
-        assert np.abs(ev1 - ev0).max() <= 1e-11, (precision, ev0, ev1)
-        assert np.abs(vec1 - vec0).max() <= 1e-8
-        assert np.array_equal(ev1, ev2) and np.array_equal(vec1, vec2)
-
-
-@pytest.mark.parametrize("env", [("GRASP_GPU_DVD_PASS", "persistent"), ("GRASP_GPU_MATVEC", "ltile")])
-def test_maneig_alternative_kernels(gpu_ready, oracle_mod, monkeypatch, env):
-    """The opt-in kernels (the single-vector pass as one cooperative kernel;
-    the tiled lower-triangle split matvec) give the same eigenpairs."""
-    import oracle
-    from grasp_gb300 import Context, HMatrix
-    from inputs import synth as S
-    orbs = S.orbital_set(6, 3)
-    case = hydrogenic_case(nmax=6, lmax=3, z=10.0)
-    occ = lambda d: S.occupation(orbs, d)  # noqa: E731
-    refs = [occ({(1, -1): 2, (2, -1): 2}), occ({(1, -1): 2, (2, 1): 2}), occ({(1, -1): 2, (2, -2): 2})]
-    blk = S.ci_block(orbs, refs, [0] * len(orbs), two_j=2, parity=0, density=0.05, seed=9)
-    monkeypatch.setenv(*env)
-    ctx = Context(0)
-    ctx.set_grid(case["n"], case["rnt"], case["h"], case["c"], case["zz"])
-    ob = case["orb"]
-    ctx.set_orbitals(ob.nak, ob.mf, ob.pf, ob.qf)
-    ctx.genintrk()
-    ctx.iabint_table()
-    H = HMatrix(ctx, blk.ncf, blk.iendc, blk.irow)
-    H.setham(blk.iq, blk.tlist, blk.vlists)
-    emt = H.emt()
-    b = np.random.default_rng(4).normal(size=(blk.ncf, 2))
-    c0 = oracle.spicmv2(blk.ncf, blk.iendc, blk.irow, emt, b)
-    c1 = H.spicmv2(b, precision=1)
-    assert np.abs(c1 - c0).max() <= 1e-11 * np.abs(c0).max()
-    # converged solves (robust first shift): the reference's own settings can
-    # stop on the coefficient test with residuals far above CRITR, where the
-    # answer depends on the rounding order of the sums
-    ev0, vec0, _ = oracle.maneig(0, blk.ncf, 3, blk.iendc, blk.irow, emt, nthreads=8, robust=True)
-    for precision in (0, 1):
-        ev, vec, info = H.maneig(3, flavour=0, precision=precision, robust=True)
-        assert np.abs(ev - ev0).max() <= 1e-9
-        assert np.abs(vec - vec0).max() <= 1e-7
 
 
 @pytest.mark.parametrize("flavour", [0, 1])
