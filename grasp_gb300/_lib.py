@@ -27,7 +27,7 @@ class GGDvdParams(C.Structure):
     _fields_ = [
         ("flavour", C.c_int), ("precision", C.c_int), ("lim", C.c_int), ("maxiter", C.c_int),
         ("critr", C.c_double), ("critc", C.c_double), ("crite", C.c_double), ("robust", C.c_int),
-        ("mblock", C.c_int),
+        ("mblock", C.c_int), ("nstart", C.c_int), ("start", _d),
     ]
 
 
@@ -63,6 +63,7 @@ GPU_SYMBOLS = {
     "gg_stage_stat": (C.c_double, [C.c_void_p, C.c_int]),
     "gg_launch_count": (C.c_longlong, []),
     "gg_alloc_count": (C.c_longlong, []),
+    "gg_test_stall_rk_tile": (C.c_int, [C.c_void_p, C.c_int]),
     "gg_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),
     "gg_host_unregister": (C.c_int, [C.c_void_p]),
     "gg_event_record": (C.c_int, [C.c_void_p, C.c_int]),

@@ -214,8 +214,14 @@ class HMatrix:
         return c
 
     def maneig(self, nvec, flavour=0, precision=FP64, lim=0, maxiter=0, critr=0.0, critc=0.0, crite=0.0,
-               robust=False, raise_on_maxiter=True, mblock=0):
-        p = GGDvdParams(flavour, precision, lim, maxiter, critr, critc, crite, int(robust), int(mblock))
+               robust=False, raise_on_maxiter=True, mblock=0, start=None):
+        """MANEIG; start: [ncf x k] orthonormal start vectors (rmcdhf's warm
+        start from the previous eigenvectors) instead of INIEST2."""
+        st0 = None
+        if start is not None:
+            st0 = np.asfortranarray(np.asarray(start, np.float64).reshape(self.ncf, -1))
+        p = GGDvdParams(flavour, precision, lim, maxiter, critr, critc, crite, int(robust), int(mblock),
+                        0 if st0 is None else st0.shape[1], None if st0 is None else ptr(st0, _d))
         ev = np.zeros(nvec); vec = np.zeros((nvec, self.ncf))
         nl, nm, ie = C.c_int(), C.c_int(), C.c_int()
         st = _lib.gpu().gg_maneig(self.ctx._h, self._h, nvec, C.byref(p), ptr(ev, _d), ptr(vec, _d), C.byref(nl),

@@ -280,6 +280,12 @@ double gg_stage_stat(gg_ctx *ctx, int which) {
 long long gg_launch_count(void) { return g_launches.load(); }
 long long gg_alloc_count(void) { return g_allocs.load(); }
 
+int gg_test_stall_rk_tile(gg_ctx *ctx, int tile) {
+  if (!ctx) return fail(GG_ERR_ARG, "gg_test_stall_rk_tile: no context");
+  ctx->test_stall_tile = tile < 0 ? -1 : tile;
+  return GG_OK;
+}
+
 int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double *z) {
   if (n < 1 || !ap || m < 1 || m > n || mvec < 0 || mvec > m || !w || (mvec > 0 && !z))
     return fail(GG_ERR_ARG, "gg_projected_eig: bad arguments");

@@ -2384,8 +2384,19 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     *out = d;
     return GG_OK;
   };
+  // warm start (rmcdhf90/maneig.f90:116-128): the caller's vectors replace
+  // INIEST2's; with a leading block the stage-1 run is skipped
+  const int nstart = (p && p->start && p->nstart > 0) ? p->nstart : 0;
+  if (nstart > P.lim) return fail(GG_ERR_ARG, "gg_maneig: more start vectors than LIM");
+  auto load_start = [&](Dvd &D) -> int {
+    GG_CUDA(cudaMemcpy2DAsync(D.B.p, D.ld * 8, p->start, (size_t)ncf * 8, (size_t)ncf * 8, nstart,
+                              cudaMemcpyHostToDevice, ctx->stream));
+    return GG_OK;
+  };
   Dvd *D1p = nullptr, *D2p = nullptr;
-  {
+  Dvd D1none;  // statistics of a skipped stage 1
+  ctx->stats[8] = ctx->stats[9] = ctx->stats[10] = 0;
+  if (!(nstart > 0 && ns < ncf)) {
     GG_TRY(refresh_sym_values(blk));
     DvdParams P1 = P;
     // stands in for INIEST2's dense DSPEVX: converge on the residual (no
@@ -2412,7 +2423,12 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     // rmcdhf90/maneig.f90:104-120) starts from all NCF unit vectors: S is
     // then the whole matrix and its eigenpairs are exact after one pass.
     if (P1.lim == ns && ns < nvec + 4) P1.niv = ns;
-    GG_TRY(unit_start(D1, blk, P1.niv));
+    if (nstart > 0) {
+      P1.niv = nstart;
+      GG_TRY(load_start(D1));
+    } else {
+      GG_TRY(unit_start(D1, blk, P1.niv));
+    }
     int nl = 0, ie = 0;
     GG_TRY(dvdson(D1, P1, ev, res, &nl, &ie));
     mv_ms += D1.mv_ms;
@@ -2424,7 +2440,7 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     ctx->stats[9] = 0;   // stage-2 loops
     ctx->stats[10] = D1.mv_ms;
   }
-  Dvd &D1 = *D1p;
+  Dvd &D1 = D1p ? *D1p : D1none;
   Dvd *Dout = &D1;
   Dvd D2none;  // statistics of an absent stage 2
   if (ns < ncf) {
@@ -2435,10 +2451,16 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   Dvd &D2 = D2p ? *D2p : D2none;
   if (ns < ncf) {
     GG_CUDA(cudaMemcpyAsync(D2.diag.p, h->dDiag.p, ncf * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-    GG_CUDA(cudaMemcpy2DAsync(D2.B.p, D2.ld * 8, D1.B.p, D1.ld * 8, (size_t)ns * 8, nvec, cudaMemcpyDeviceToDevice,
-                              ctx->stream));
+    DvdParams P2 = P;
+    if (nstart > 0) {
+      P2.niv = nstart;
+      GG_TRY(load_start(D2));
+    } else {
+      GG_CUDA(cudaMemcpy2DAsync(D2.B.p, D2.ld * 8, D1.B.p, D1.ld * 8, (size_t)ns * 8, nvec, cudaMemcpyDeviceToDevice,
+                                ctx->stream));
+    }
     int nl = 0, ie = 0;
-    GG_TRY(dvdson(D2, P, ev, res, &nl, &ie));
+    GG_TRY(dvdson(D2, P2, ev, res, &nl, &ie));
     mv_ms += D2.mv_ms;
     mv_count += D2.mv_count;
     nmv_total += D2.nmv;

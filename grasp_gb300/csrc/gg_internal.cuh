@@ -155,6 +155,7 @@ struct gg_ctx {
   double stats[26] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t marks[8] = {};  // gg_event_record slots
+  int test_stall_tile = -1;     // gg_test_stall_rk_tile: one tensor-core tile withholds a copy, once
 };
 
 struct gg_hmat {

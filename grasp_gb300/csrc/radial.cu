@@ -419,6 +419,7 @@ struct TcTile {
   int k, fg, pg;  // k; global indices of the Y block column and the A block column
   int f0, fn;     // first Y function and how many are valid
   int r0, rn;     // first row (TcRow index) and how many are valid
+  int c0, c1, s;  // grid chunks [c0, c1) of this split of the tile, split index
 };
 
 }  // namespace
@@ -441,6 +442,12 @@ struct RkCache {
   DBuf<int> dRowpair, dYslot, dAslot, dFidx, dNfb, dEA, dEY;
   DBuf<int32_t> dKst;
   DBuf<TcTile> dTct;
+  // split-K form of tct (each tile's grid chunks over nsplit CTAs) for the
+  // chunk count it was made for, and the partial sums it writes
+  std::vector<TcTile> tcs;
+  int tcs_nch = -1, tcs_split = 0;
+  DBuf<TcTile> dTcs;
+  DBuf<double> dParts;
   DBuf<TcRow> dTcr;
   DBuf<double> dY, dA, scratch;
   DBuf<QuadItem> dFb;
@@ -464,9 +471,9 @@ __device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
          ((uint64_t)1 << 46);
 }
 
-__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity) {
+__device__ __forceinline__ bool tc_wait(uint32_t mbar, uint32_t parity, int spin = TC_SPIN) {
   uint32_t done = 0;
-  for (int it = 0; it < TC_SPIN && !done; ++it)
+  for (int it = 0; it < spin && !done; ++it)
     asm volatile(
         "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
         : "=r"(done)
@@ -533,7 +540,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
                                                          const __half *__restrict__ At, int nch,
                                                          const int *__restrict__ eA, const int *__restrict__ eY,
                                                          const YDesc *__restrict__ yd, double *__restrict__ val,
-                                                         long long nval, int *__restrict__ flags) {
+                                                         long long nval, int *__restrict__ flags, int stall_tile) {
   extern __shared__ __align__(1024) unsigned char tsm[];
   __half *Ysm = reinterpret_cast<__half *>(tsm);
   __half *Asm = Ysm + 2 * TC_YBLK;
@@ -562,13 +569,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;");
   const uint32_t tmem = *tslot;
-  const int nflush = (nch + TC_FLUSH - 1) / TC_FLUSH;
+  const int nloc = T.c1 - T.c0;  // chunks of this split
+  const int nflush = (nloc + TC_FLUSH - 1) / TC_FLUSH;
   if (warp == 4) {
-    // copies and MMAs (lane 0 issues; the warp stays converged)
+    // copies and MMAs (lane 0 issues; the warp stays converged). A tile
+    // named by stall_tile (a test of the bounded waits) withholds its first
+    // copy and polls briefly: its first wait runs out with nothing in flight.
+    const bool stall = (int)blockIdx.x == stall_tile;
+    const int spin = stall ? (1 << 12) : TC_SPIN;
     const uint32_t idesc = (1u << 4) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
     const char *ysrc = reinterpret_cast<const char *>(Yt + (size_t)T.fg * nch * TC_YBLK);
     const char *asrc = reinterpret_cast<const char *>(At + (size_t)T.pg * nch * TC_ABLK);
     constexpr uint32_t YB = TC_YBLK * sizeof(__half), AB = TC_ABLK * sizeof(__half);
+    // local chunk j of the split is grid chunk T.c0 + j
     auto copy = [&](int j) {
       const int st = j & 1;
       if (lane == 0) {
@@ -577,12 +590,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                 smem_addr(Ysm + st * TC_YBLK)),
-            "l"(ysrc + (size_t)j * YB), "r"(YB), "r"(fb)
+            "l"(ysrc + (size_t)(T.c0 + j) * YB), "r"(YB), "r"(fb)
             : "memory");
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                 smem_addr(Asm + st * TC_ABLK)),
-            "l"(asrc + (size_t)j * AB), "r"(AB), "r"(fb)
+            "l"(asrc + (size_t)(T.c0 + j) * AB), "r"(AB), "r"(fb)
             : "memory");
       }
       __syncwarp();
@@ -590,11 +603,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
     bool ok = true;
     uint32_t fresh = (1u << OZ_S) - 1;
     int issued = -1;  // last chunk whose MMAs were committed
-    copy(0);
+    int copied = -1;  // last chunk whose copy was issued
+    if (!stall) {
+      copy(0);
+      copied = 0;
+    }
     int fl = 0;
-    for (int j = 0; j < nch; ++j) {
+    for (int j = 0; j < nloc; ++j) {
       const int st = j & 1;
-      if (ok) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&full[st]), (j >> 1) & 1));
+      if (ok) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&full[st]), (j >> 1) & 1, spin));
       if (ok) {
         asm volatile("tcgen05.fence::after_thread_sync;");
         if (lane == 0) {
@@ -624,13 +641,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
         __syncwarp();
         issued = j;
         // refill the other stage with chunk j + 1 once chunk j - 1's MMAs are done
-        if (j + 1 < nch) {
-          if (j >= 1) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&empty[(j - 1) & 1]), ((j - 1) >> 1) & 1));
-          if (ok) copy(j + 1);
+        if (j + 1 < nloc) {
+          if (j >= 1)
+            ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&empty[(j - 1) & 1]), ((j - 1) >> 1) & 1, spin));
+          if (ok) {
+            copy(j + 1);
+            copied = j + 1;
+          }
         }
       }
-      if ((j + 1) % TC_FLUSH == 0 || j == nch - 1) {
-        if (ok) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&empty[st]), (j >> 1) & 1));  // MMAs done
+      if ((j + 1) % TC_FLUSH == 0 || j == nloc - 1) {
+        if (ok) ok = __all_sync(0xffffffffu, tc_wait(smem_addr(&empty[st]), (j >> 1) & 1, spin));  // MMAs done
         if (!ok && lane == 0) *okflag = 0;
         asm volatile("tcgen05.fence::before_thread_sync;");
         __syncthreads();  // A: the accumulators are ready (or the flag says no)
@@ -645,8 +666,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
       __syncthreads();
     }
     if (!ok && lane == 0) {
-      atomicExch(flags + 1, 1);  // timed out
-      if (issued >= 0) tc_wait(smem_addr(&empty[issued & 1]), (issued >> 1) & 1);
+      // timed out: before the tensor memory is freed and the CTA leaves,
+      // wait (bounded) for the last copy issued to land in shared memory and
+      // for the last committed MMAs to finish; 2 records a failed drain
+      bool drained = true;
+      if (copied >= 0) drained = tc_wait(smem_addr(&full[copied & 1]), (copied >> 1) & 1);
+      if (issued >= 0) drained = tc_wait(smem_addr(&empty[issued & 1]), (issued >> 1) & 1) && drained;
+      atomicMax(flags + 1, drained ? 1 : 2);
     }
   } else {
     // warps 0-3: lane quadrant `warp` of each group accumulator
@@ -704,7 +730,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
           atomicExch(flags, 1);  // position outside the table
           continue;
         }
-        val[pos] = scalbn((double)ah[n] + (double)al[n], eA[rw.p] + ey - 14);
+        // split s of the contraction: its partial sum (val + s nval)
+        val[(long long)T.s * nval + pos] = scalbn((double)ah[n] + (double)al[n], eA[rw.p] + ey - 14);
       }
     }
   }
@@ -715,14 +742,16 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_rk_tc(const TcTile *__restric
 
 // QUAD head term for every table entry, one thread per entry: (a, b, c, d)
 // from INDTEIRK, k from KSTART, the Y function from fidx[(k KEY + b) KEY + d];
-// val holds the entry's GEMM part on entry.
+// the entry's GEMM part is the sum, in split order, of parts[s n + i] for
+// s < nsplit (parts == val when the contraction was not split).
 __global__ void k_rk_finish_all(const int32_t *__restrict__ ind, long long n, const int32_t *__restrict__ kstart,
                                 int kloop, int KEY, const int *__restrict__ fidx, const YDesc *__restrict__ yd,
                                 const double *__restrict__ Y, int np, const double *__restrict__ PF,
                                 const double *__restrict__ QF, int ld, const int *__restrict__ MF,
                                 const double *__restrict__ R, const double *__restrict__ RP,
                                 const double *__restrict__ RPOR, QuadConst q, double *__restrict__ val,
-                                QuadItem *__restrict__ fb, int *__restrict__ nfb) {
+                                QuadItem *__restrict__ fb, int *__restrict__ nfb, const double *__restrict__ parts,
+                                int nsplit) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     int p = ind[i];
     const int d = p % KEY;
@@ -737,7 +766,9 @@ __global__ void k_rk_finish_all(const int32_t *__restrict__ ind, long long n, co
       atomicExch(nfb + 1, 1);
       continue;
     }
-    rk_head_store(k, a, c, f, i, val[i], yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val, fb, nfb);
+    double gemm = parts[i];
+    for (int t = 1; t < nsplit; ++t) gemm += parts[(long long)t * n + i];
+    rk_head_store(k, a, c, f, i, gemm, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val, fb, nfb);
   }
 }
 
@@ -1068,6 +1099,7 @@ static int rk_build_structure(gg_ctx *ctx, int kloop, RkCache &C) {
   yslot.clear();
   aslot.clear();
   tct.clear();
+  C.tcs_nch = -1;  // the split-K list follows tct
   for (int k = 0; k <= kloop; ++k) {
     kbeg[k] = (k == 0) ? 0 : kend[k - 1];
     const int F = kend[k] - kbeg[k], Rk = tcr0[k + 1] - tcr0[k];
@@ -1149,6 +1181,7 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
     C.key = key;
   }
   const int64_t N = rk.n;
+  rk.valid = false;  // until this call's table is complete
   rk.kloop = kloop;
   rk.j2max = j2max;
   // per call: each Y function's MTP from the current orbital extents
@@ -1202,17 +1235,47 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
         GG_CUDA(cudaFuncSetAttribute(k_rk_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM));
         attr = true;
       }
+      // split-K: one CTA per SM holds a tile (shared memory), so with
+      // fewer tiles than SMs each tile's grid chunks are cut into nsplit
+      // ranges of at least TC_FLUSH chunks, whose partial sums
+      // k_rk_finish_all adds in order
+      int nsplit = 1;
       if (!C.tct.empty()) {
-        k_rk_tc<<<(unsigned)C.tct.size(), TC_THREADS, TC_SMEM, ctx->stream>>>(
-            C.dTct.p, C.dTcr.p, C.dYt.p, C.dAt.p, nch, C.dEA.p, C.dEY.p, C.dYd.p, rk.dVal.p, (long long)N,
-            C.dNfb.p + 1);
+        const int want = (ctx->sms + (int)C.tct.size() - 1) / (int)C.tct.size();
+        nsplit = std::max(1, std::min(want, nch / TC_FLUSH));
+      }
+      if (C.tcs_nch != nch || C.tcs_split != nsplit) {
+        C.tcs.clear();
+        for (const TcTile &t : C.tct)
+          for (int sp = 0; sp < nsplit; ++sp) {
+            TcTile u = t;
+            u.c0 = (int)((long long)nch * sp / nsplit);
+            u.c1 = (int)((long long)nch * (sp + 1) / nsplit);
+            u.s = sp;
+            C.tcs.push_back(u);
+          }
+        GG_TRY(upload(C.dTcs, C.tcs, ctx->stream));
+        C.tcs_nch = nch;
+        C.tcs_split = nsplit;
+      }
+      double *parts = rk.dVal.p;
+      if (nsplit > 1) {
+        GG_TRY(C.dParts.alloc((size_t)nsplit * std::max<int64_t>(N, 1)));
+        parts = C.dParts.p;
+      }
+      if (!C.tcs.empty()) {
+        k_rk_tc<<<(unsigned)C.tcs.size(), TC_THREADS, TC_SMEM, ctx->stream>>>(
+            C.dTcs.p, C.dTcr.p, C.dYt.p, C.dAt.p, nch, C.dEA.p, C.dEY.p, C.dYd.p, parts, (long long)N,
+            C.dNfb.p + 1, ctx->test_stall_tile);
+        ctx->test_stall_tile = -1;  // one call only
         ::gg::note_launch();
       }
+      ctx->stats[25] = nsplit;
       GG_CUDA(cudaGetLastError());
       const unsigned fb_blocks = (unsigned)std::min<long long>((N + 255) / 256, 8LL * ctx->sms);
       k_rk_finish_all<<<std::max(1u, fb_blocks), 256, 0, ctx->stream>>>(
           rk.dInd.p, (long long)N, C.dKst.p, kloop, KEY, C.dFidx.p, C.dYd.p, C.dY.p, np, o.dPF.p, o.dQF.p, o.ld,
-          o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, C.dFb.p, C.dNfb.p);
+          o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, C.dFb.p, C.dNfb.p, parts, nsplit);
       ::gg::note_launch();
     }
     GG_CUDA(cudaGetLastError());
@@ -1228,7 +1291,11 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   GG_CUDA(cudaMemcpyAsync(hfb, C.dNfb.p, 3 * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (hfb[1]) return fail(GG_ERR_STATE, "genintrk: contraction produced a table position out of range");
-  if (hfb[2]) return fail(GG_ERR_STATE, "genintrk: tensor-core contraction timed out waiting for its MMAs");
+  if (hfb[2] == 1)
+    return fail(GG_ERR_TIMEOUT, "genintrk: a tensor-core tile timed out waiting for its copies or MMAs (drained; "
+                                "the table is not valid)");
+  if (hfb[2] > 1)
+    return fail(GG_ERR_TIMEOUT, "genintrk: a tensor-core tile timed out and its copies or MMAs did not drain");
   const int nfb = hfb[0];
   ctx->stats[20] = nfb;
   if (nfb > 0) {

@@ -40,7 +40,9 @@ enum gg_status {
   GG_ERR_RANGE = -5,     /* SETHAM: LOC beyond NELMNT, label out of range */
   GG_ERR_KAPPA = -6,     /* RINTI: orbitals with different kappa */
   GG_ERR_CONVERGE = -7,  /* DVDSON: MAXITER reached (ierr has bit 2048) */
-  GG_ERR_NOMEM = -8
+  GG_ERR_NOMEM = -8,
+  GG_ERR_TIMEOUT = -9    /* a bounded device wait ran out; the call's result
+                            is not valid, the context stays usable */
 };
 
 /* Precision of the R^k contraction and of the Davidson matvec. */
@@ -203,6 +205,15 @@ typedef struct {
                      many correction vectors per pass (one matvec pass over
                      the matrix for all of them, one projected eigenproblem
                      per pass) */
+  int nstart;     /* > 0: DVDSON starts from the nstart (<= LIM) vectors in
+                     start instead of INIEST2's estimates: rmcdhf's repeated
+                     solves, which start from the previous SCF iteration's
+                     eigenvectors (rmcdhf90/maneig.f90:116-128; the
+                     reference does so for NCF > 4000, this library for any
+                     NCF). Like DVDSON's initial vectors they must be
+                     orthonormal (libdvd90/dvdson.f90:228); the previous
+                     call's evec is. 0: INIEST2. */
+  const double *start; /* [ncf x nstart] column-major, host memory */
 } gg_dvd_params;
 
 int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params *p, double *eval, double *evec,
@@ -244,7 +255,9 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * index above 2), 21 iterations of the last gg_maneig_batched (all blocks
  * together), 22 kernels per batched iteration (stage 3 is the batched
  * solve's total ms), 23 / 24 device ms / number of the full-block block
- * matvecs (split SpMM) over MBLOCK columns of the last gg_maneig.         */
+ * matvecs (split SpMM) over MBLOCK columns of the last gg_maneig, 25 the
+ * number of grid-point ranges (split-K) of the last tensor-core
+ * gg_genintrk's contraction tiles.                                        */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors
@@ -292,6 +305,12 @@ const char *gg_tune_variant_name(int kernel, int variant);
  * vectors (1 <= m <= 16; the Davidson block pass's matvec), algorithmic
  * bytes = the matrix in the reference's storage once + 3 m NCF doubles.     */
 long long gg_launch_count(void);
+/* Test hook of the bounded device waits: in the next tensor-core
+ * gg_genintrk (GG_SPLIT) on ctx, tile `tile` of the contraction withholds
+ * its first copy and polls its barrier only briefly, so that wait runs out
+ * with nothing in flight. The call then returns GG_ERR_TIMEOUT and leaves
+ * no valid table; the context stays usable. tile < 0 cancels.             */
+int gg_test_stall_rk_tile(gg_ctx *ctx, int tile);
 long long gg_alloc_count(void);
 /* Page-locks (pins) caller memory so that uploads from it run at full link
  * rate; unregister before freeing it. */

@@ -207,3 +207,39 @@ def test_maneig_tiny_blocks(gpu_ready, oracle_mod, flavour, precision):
         assert info["ierr"] == 0
         assert np.abs(ev - ev0).max() <= 1e-9, (c, ev, ev0)
         assert np.abs(vec - vec0).max() <= 1e-7, c
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_rmcdhf_warm_start(gpu_ready, oracle_mod, precision):
+    """rmcdhf's repeated MANEIG (rmcdhf90/maneig.f90:116-128): after the
+    first solve of an SCF step, the next one starts from the previous
+    eigenvectors instead of INIEST2. On a block above N1000 = 4000 CSFs,
+    flavour 1, cold and warm: both against the oracle's eigenpairs (its
+    MANEIG with rci's settings, which converges to the same pairs with a
+    2000-row dense start instead of a 4000-row one), and the warm solve of a
+    slightly changed matrix (a perturbed diagonal, as after an orbital
+    update) needs fewer loops than its cold solve."""
+    from grasp_gb300 import Context, HMatrix
+    from inputs import workloads as W
+    ncf = 6000
+    iendc, irow, emt = W.synthetic_h(ncf, 150_000, seed=13)
+    ctx = Context(0)
+    H = HMatrix(ctx, ncf, iendc, irow)
+    H.set_emt(emt)
+    nvec = 3
+    ev0, vec0, info0 = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt, nthreads=8)
+    ev, vec, info = H.maneig(nvec, flavour=1, precision=precision)
+    assert np.abs(ev - ev0).max() <= 1e-9 and np.abs(vec - vec0).max() <= 1e-7
+    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec)
+    assert np.abs(evw - ev0).max() <= 1e-9 and np.abs(vecw - vec0).max() <= 1e-7
+    # the next SCF step: the diagonal moves by up to 1e-4 Eh
+    emt2 = emt.copy()
+    diag = iendc[1:] - 1
+    emt2[diag] += 1e-4 * np.sin(np.arange(ncf))
+    H.set_emt(emt2)
+    ev1, vec1, _ = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt2, nthreads=8)
+    evc, vecc, infoc = H.maneig(nvec, flavour=1, precision=precision)
+    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec)
+    for e, v in ((evc, vecc), (evw, vecw)):
+        assert np.abs(e - ev1).max() <= 1e-9 and np.abs(v - vec1).max() <= 1e-7
+    assert infow["nloops"] < infoc["nloops"], (infow, infoc)
