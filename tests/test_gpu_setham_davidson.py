@@ -218,7 +218,9 @@ def test_rmcdhf_warm_start(gpu_ready, oracle_mod, precision):
     MANEIG with rci's settings, which converges to the same pairs with a
     2000-row dense start instead of a 4000-row one), and the warm solve of a
     slightly changed matrix (a perturbed diagonal, as after an orbital
-    update) needs fewer loops than its cold solve."""
+    update) needs fewer loops than its cold solve. All solves use the robust
+    first shift: with DVDSON's 1e30 sentinel the coefficient test can stop a
+    solve of this matrix early, far from CRITR (see test_oracle_eigen)."""
     from grasp_gb300 import Context, HMatrix
     from inputs import workloads as W
     ncf = 6000
@@ -227,19 +229,19 @@ def test_rmcdhf_warm_start(gpu_ready, oracle_mod, precision):
     H = HMatrix(ctx, ncf, iendc, irow)
     H.set_emt(emt)
     nvec = 3
-    ev0, vec0, info0 = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt, nthreads=8)
-    ev, vec, info = H.maneig(nvec, flavour=1, precision=precision)
+    ev0, vec0, info0 = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt, nthreads=8, robust=True)
+    ev, vec, info = H.maneig(nvec, flavour=1, precision=precision, robust=True)
     assert np.abs(ev - ev0).max() <= 1e-9 and np.abs(vec - vec0).max() <= 1e-7
-    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec)
+    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec, robust=True)
     assert np.abs(evw - ev0).max() <= 1e-9 and np.abs(vecw - vec0).max() <= 1e-7
     # the next SCF step: the diagonal moves by up to 1e-4 Eh
     emt2 = emt.copy()
     diag = iendc[1:] - 1
     emt2[diag] += 1e-4 * np.sin(np.arange(ncf))
     H.set_emt(emt2)
-    ev1, vec1, _ = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt2, nthreads=8)
-    evc, vecc, infoc = H.maneig(nvec, flavour=1, precision=precision)
-    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec)
+    ev1, vec1, _ = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt2, nthreads=8, robust=True)
+    evc, vecc, infoc = H.maneig(nvec, flavour=1, precision=precision, robust=True)
+    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec, robust=True)
     for e, v in ((evc, vecc), (evw, vecw)):
         assert np.abs(e - ev1).max() <= 1e-9 and np.abs(v - vec1).max() <= 1e-7
     assert infow["nloops"] < infoc["nloops"], (infow, infoc)
