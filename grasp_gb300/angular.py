@@ -29,7 +29,8 @@ _u8 = C.POINTER(C.c_uint8)
 
 class GABlockSpec(C.Structure):
     _fields_ = [("nw", C.c_int), ("nak", _int), ("ncsf", C.c_int), ("iq", _u8), ("jqs", _int), ("nu", _int),
-                ("xj", _int), ("two_j", C.c_int), ("cutoff", C.c_double), ("nthreads", C.c_int)]
+                ("xj", _int), ("two_j", C.c_int), ("cutoff", C.c_double), ("nthreads", C.c_int),
+                ("average_split", C.c_int)]
 
 
 SYMBOLS = {
@@ -72,7 +73,7 @@ class AngularBlock:
     parity: int
     iendc: np.ndarray
     irow: np.ndarray
-    iq: np.ndarray          # zeros [ncf, nw]: the lists hold the whole H
+    iq: np.ndarray          # occupations for SETHAM: the CSFs' (average_split) or zeros (whole H in the lists)
     occupations: np.ndarray  # the CSFs' subshell occupations [ncf, nw]
     tlist: dict
     vlists: list = field(default_factory=list)
@@ -82,8 +83,11 @@ class AngularBlock:
         return int(self.tlist["loc"].size + sum(v["loc"].size for v in self.vlists))
 
 
-def block_lists(csl, block, cutoff=-1.0, nthreads=0) -> AngularBlock:
-    """Structure and T/V lists of block `block` (0-based) of a CslFile."""
+def block_lists(csl, block, cutoff=-1.0, nthreads=0, average_split=False) -> AngularBlock:
+    """Structure and T/V lists of block `block` (0-based) of a CslFile.
+    average_split: rangular's convention for rmcdhf (the occupation-driven
+    diagonal pieces left to SETHAM; .iq then holds the occupations), else
+    the whole H in the lists and .iq zero."""
     b = csl.blocks[block]
     nw = len(csl.subshells)
     nak = np.ascontiguousarray([k for _, k in csl.subshells], np.int32)
@@ -92,7 +96,7 @@ def block_lists(csl, block, cutoff=-1.0, nthreads=0) -> AngularBlock:
     nu = np.ascontiguousarray(b.nu, np.int32)
     xj = np.ascontiguousarray(b.xj, np.int32)
     spec = GABlockSpec(nw, _p(nak, _int), b.ncsf, _p(iq, _u8), _p(jqs, _int), _p(nu, _int), _p(xj, _int), b.two_j,
-                       cutoff, nthreads)
+                       cutoff, nthreads, int(bool(average_split)))
     h = C.c_void_p()
     L = lib()
     if L.ga_block_generate(C.byref(spec), C.byref(h)) != 0:
@@ -114,5 +118,28 @@ def block_lists(csl, block, cutoff=-1.0, nthreads=0) -> AngularBlock:
             lists.append(d)
     finally:
         L.ga_block_free(h)
-    return AngularBlock(ncf.value, nnz.value, km.value, b.two_j, b.parity, iendc, irow,
-                        np.zeros((ncf.value, nw), np.uint8), iq.copy(), lists[0], lists[1:])
+    iq_setham = iq.copy() if average_split else np.zeros((ncf.value, nw), np.uint8)
+    return AngularBlock(ncf.value, nnz.value, km.value, b.two_j, b.parity, iendc, irow, iq_setham, iq.copy(),
+                        lists[0], lists[1:])
+
+
+def mcp_set(csl, nelec, average_split=True, **kw):
+    """All blocks of a CSF list as an McpSet (grasp_gb300.formats): what
+    rangular writes to mcp.30/31/32+k for rmcdhf, with write_mcp then giving
+    the files. average_split=True keeps SETHAM's occupation-driven diagonal
+    pieces out of the lists (rangular's convention for rmcdhf)."""
+    from . import formats as F
+    blocks, idblk, kmaxf = [], [], 0
+    for bi, b in enumerate(csl.blocks):
+        ab = block_lists(csl, bi, average_split=average_split, **kw)
+        kmaxf = max(kmaxf, ab.kmaxf)
+        blocks.append(F.McpBlock(ab.ncf, ab.iendc, ab.irow, ab.tlist, list(ab.vlists)))
+        j = f"{b.two_j}/2" if b.two_j % 2 else f"{b.two_j // 2}"
+        idblk.append(f"{j:>4}{'+' if b.parity > 0 else '-'}   "[:8])
+    empty = dict(lab=np.zeros(0, np.int32), start=np.zeros(1, np.int64), loc=np.zeros(0, np.int32),
+                 coeff=np.zeros(0), iclmn=np.zeros(0, np.int32))
+    for blk in blocks:
+        while len(blk.vlists) < kmaxf + 1:
+            blk.vlists.append(dict(empty))
+    return F.McpSet(ncore=csl.ncore, nelec=nelec, ncf=sum(b.ncf for b in blocks), nw=len(csl.subshells),
+                    kmaxf=kmaxf, idblk=idblk, blocks=blocks)

@@ -788,6 +788,36 @@ int ga_block_generate(const ga_block_spec *spec, ga_block **outp) {
         for (int a = 0; a < nw; ++a)
           if (!E.core[a] && conf_iq[A][a])
             for (auto &kv : coreone[(size_t)a * nw + a]) dg[kv.first] += conf_iq[A][a] * kv.second;
+        if (spec->average_split) {
+          // the pieces rmcdhf's SETHAM adds from IQ (setham.f90:75-209):
+          // taken out here so that the lists hold the rest
+          const std::vector<uint8_t> &q = conf_iq[A];
+          auto clrx2 = [&](int a, int k, int b) {
+            const double w = threej(E.orbs[a].tj, 2 * k, E.orbs[b].tj, 1, 0, -1);
+            return w * w;
+          };
+          for (int a = 0; a < nw; ++a) {
+            const int qa = q[a];
+            if (!qa) continue;
+            const bool fa = qa == E.orbs[a].tj + 1;
+            dg[tkey(a + 1, a + 1)] -= qa;
+            dg[vkey(0, a + 1, a + 1, a + 1, a + 1)] -= (double)(qa * (qa - 1) / 2);
+            if (fa)
+              for (int k = 2; k <= E.orbs[a].tj - 1; k += 2)
+                dg[vkey(k, a + 1, a + 1, a + 1, a + 1)] -= -0.5 * clrx2(a, k, a) * qa * qa;
+            for (int b = a + 1; b < nw; ++b) {
+              const int qb = q[b];
+              if (!qb) continue;
+              dg[vkey(0, a + 1, b + 1, a + 1, b + 1)] -= (double)(qa * qb);
+              if (!(fa || qb == E.orbs[b].tj + 1)) continue;
+              const int kmin0 = std::abs(E.orbs[a].tj - E.orbs[b].tj) / 2;
+              const int kmin = (E.orbs[a].kappa * E.orbs[b].kappa > 0) ? kmin0 : kmin0 + 1;
+              const int kmax = (E.orbs[a].tj + E.orbs[b].tj) / 2;
+              for (int k = kmin; k <= kmax; k += 2)
+                dg[vkey(k, a + 1, b + 1, b + 1, a + 1)] -= -(double)(qa * qb) * clrx2(a, k, b);
+            }
+          }
+        }
         for (auto &kv : dg) {
           auto &v = acc[kv.first];
           if (v.empty()) v.assign((size_t)nA * nB, 0.0);

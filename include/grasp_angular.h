@@ -15,17 +15,26 @@
  *   <a m_a|C^k_q|c m_c> = (-1)^(j_a-m_a) (j_a k j_c; -m_a q m_c) <k_a||C^k||k_c>,
  * and the CSF coefficients follow by transforming each integral's
  * determinant coefficients with the CSF vectors. The coefficient of every
- * radial integral is exact up to rounding; CSF phases follow this
- * construction, so individual off-diagonal coefficients may differ from
- * rangular's in sign (the eigenvalues and |mixing coefficients| do not).
+ * radial integral is exact up to rounding. The CSFs carry the reference's
+ * phases (Clebsch-Gordan coupling of the subshell states in list order, the
+ * subshell states' own signs fixed by their parents): for a GRASP-written
+ * list with up to three electrons in an open subshell the mixing
+ * coefficients agree with rmcdhf's in sign, so the off-diagonal
+ * coefficients have rangular's signs too.
  *
  * Output per block: the CSR-lower structure (IENDC/IROW, rows in CSF order,
  * diagonal last; mcp.30) and the lists in SETHAM's layout: the T list
  * (labels min(a,b)*215 + max(a,b)), then V^0..V^kmaxf (labels
  * ((a*215+c)*215+b)*215+d with a <= c, b <= d, (a,c) <= (b,d)), each grouped
  * by label with (column, 1-based position in EMT, coefficient) per element.
- * The lists hold the whole Hamiltonian: pass zero occupations (IQ) to
- * gg_setham so that it adds no average-energy diagonal pieces.
+ * With average_split = 0 the lists hold the whole Hamiltonian: pass zero
+ * occupations (IQ) to gg_setham so that it adds no diagonal pieces. With
+ * average_split = 1 they follow rangular's convention for rmcdhf: the
+ * diagonal pieces that SETHAM adds from the occupations
+ * (rmcdhf90/setham.f90:75-209 with FCO/GCO, fco.f90, gco.f90: I(aa) times
+ * IQ(a), F^0 of every pair, F^k of closed subshells, G^k with a closed
+ * subshell) are left out of the lists; pass the CSFs' occupations to
+ * gg_setham.
  */
 #ifndef GRASP_ANGULAR_H
 #define GRASP_ANGULAR_H
@@ -55,6 +64,7 @@ typedef struct {
   int two_j;
   double cutoff;
   int nthreads;       /* <= 0: all hardware threads */
+  int average_split;  /* 1: leave SETHAM's occupation-driven diagonal pieces out */
 } ga_block_spec;
 
 int ga_block_generate(const ga_block_spec *spec, ga_block **out);

@@ -141,3 +141,38 @@ def test_diagonal_one_body_coefficients_count_electrons():
                 tot[r] += t["coeff"][p]
     np.testing.assert_allclose(tot, 2.0, atol=1e-13)
     assert nw == 36
+
+
+def test_average_split_lists_give_the_same_matrix(oracle_mod):
+    """rangular's convention for rmcdhf: the lists without the diagonal
+    pieces SETHAM adds from the occupations (FCO/GCO), assembled with the
+    CSFs' IQ, give the same Hamiltonian as the whole-H lists with zero IQ;
+    closed-subshell terms are then absent from the lists, which are
+    shorter."""
+    for run in ("He", "Ge"):
+        d, csl, o = _chain(oracle_mod, run)
+        ab = A.block_lists(csl, 0)
+        sp = A.block_lists(csl, 0, average_split=True)
+        np.testing.assert_array_equal(sp.iendc, ab.iendc)
+        np.testing.assert_array_equal(sp.irow, ab.irow)
+        assert sp.iq.any() and not ab.iq.any()
+        e_full = o.setham(ab.ncf, ab.nnz, ab.iendc, ab.iq, ab.tlist, ab.vlists)
+        e_split = o.setham(sp.ncf, sp.nnz, sp.iendc, sp.iq, sp.tlist, sp.vlists)
+        assert np.abs(e_split - e_full).max() <= 1e-12 * np.abs(e_full).max(), run
+        assert sp.ncontr < ab.ncontr
+
+
+def test_mcp_files_from_the_engine(tmp_path, oracle_mod):
+    """The engine's lists written as mcp.30/31/32+k (rangular's files for
+    rmcdhf) and read back give the same SETHAM."""
+    d, csl, o = _chain(oracle_mod, "He")
+    s = A.mcp_set(csl, nelec=2)
+    head = str(tmp_path / "mcp")
+    F.write_mcp(head, s)
+    r = F.read_mcp(head)
+    assert [b.ncf for b in r.blocks] == [70, 180, 222] and r.kmaxf == s.kmaxf
+    for bi, b in enumerate(r.blocks):
+        ab = A.block_lists(csl, bi, average_split=True)
+        e0 = o.setham(ab.ncf, ab.nnz, ab.iendc, ab.iq, ab.tlist, ab.vlists)
+        e1 = o.setham(b.ncf, int(b.iendc[-1]), b.iendc, ab.iq, b.tlist, b.vlists)
+        np.testing.assert_array_equal(e0, e1)
