@@ -52,7 +52,8 @@ def _args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-extra", action="store_true", help="skip the batched-block and R^k table legs")
     ap.add_argument("--large", action="store_true",
-                    help="run only the large-scale leg (~3e5 CSFs, ~1e9 elements; minutes) and print its JSON line")
+                    help="run only the large-scale leg (~3e5 CSFs, ~1e9 elements) and print its JSON line")
+    ap.add_argument("--no-large", action="store_true", help="skip the large-scale leg of the default run")
     return ap.parse_args()
 
 
@@ -308,11 +309,13 @@ def rk_leg(local):
     return out
 
 
-def large_leg(local, steps=2):
-    """The large-scale CI workload (workloads.large: ~3e5 CSFs, ~1e9 stored
+def large_leg(local, steps=2, cpu=True):
+    """The large-scale CI workload (workloads.large: 3e5 CSFs, 1e9 stored
     elements of a seeded synthetic H, the Z = 40 47-orbital R^k table to
-    k = 10, 5 roots): table, block, split and FP64 solves. Opt-in
-    (--large): generating and uploading the block takes minutes."""
+    k = 10, 5 roots): table, block, split and FP64 solves (MBLOCK = NVEC),
+    the block matvec's roofline, and parity against the oracle: SPICMV2 on
+    the whole matrix, and the eigenpairs of a 1e5-CSF block of the same
+    generator (the oracle's DVDSON on the full block takes too long here)."""
     import numpy as np
 
     from grasp_gb300 import FP64, SPLIT, Context, HMatrix
@@ -335,6 +338,7 @@ def large_leg(local, steps=2):
     out["upload_s"] = time.perf_counter() - t0
     res = {}
     for prec, name in ((SPLIT, "split"), (FP64, "fp64")):
+        H.maneig(w.nroots, flavour=0, precision=prec, mblock=w.nroots)  # warm-up (tuning, workspaces)
         ts = []
         for _ in range(steps):
             ctx.mark(0)
@@ -346,9 +350,43 @@ def large_leg(local, steps=2):
         out[f"{name}_loops"] = info["nloops"]
     out["max_abs_dE_split_vs_fp64_Eh"] = float(np.abs(res["split"] - res["fp64"]).max())
     ms, by = H.spmm_timing(w.nroots, 5)
+    peak, peak_kind = _peaks()
     out["spmm_us_per_launch"] = ms * 1e3
     out["spmm_alg_gbs"] = by / (ms * 1e-3) / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": by / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                       "frac": by / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+                       "kernel": "k_spmm_split<%d> (block matvec, 32-bit columns)" % w.nroots}
+    out["autotune"] = H.tune(0, w.nroots)
+    if cpu:
+        import oracle
+        oracle.build()
+        b = np.random.default_rng(3).normal(size=(w.ncf, 2))
+        t0 = time.perf_counter()
+        c0 = oracle.spicmv2(w.ncf, w.iendc, w.irow, w.emt, b)
+        t_o = time.perf_counter() - t0
+        c1 = H.spicmv2(b, precision=SPLIT)
+        c2 = H.spicmv2(b, precision=FP64)
+        out["parity_vs_oracle"] = {
+            "spicmv2_split_max_rel": float(np.abs(c1 - c0).max() / np.abs(c0).max()),
+            "spicmv2_fp64_max_rel": float(np.abs(c2 - c0).max() / np.abs(c0).max()),
+            "oracle_spicmv2_s": t_o}
     H.close()
+    if cpu:
+        # eigenpairs of a 1e5-CSF block of the same generator against the oracle
+        nsub = 100000
+        iendc, irow, emt = workloads.synthetic_h(nsub, int(w.nnz * (nsub / w.ncf) ** 2), seed=8)
+        Hs = HMatrix(ctx, nsub, iendc, irow)
+        Hs.set_emt(emt)
+        ev, vec, _ = Hs.maneig(w.nroots, flavour=0, precision=SPLIT, mblock=w.nroots, robust=True)
+        t0 = time.perf_counter()
+        ev0, vec0, info0 = oracle.maneig(0, nsub, w.nroots, iendc, irow, emt, nthreads=os.cpu_count() or 1,
+                                         robust=True)
+        out["parity_vs_oracle"].update({
+            "block_ncf": nsub, "block_nnz": int(iendc[-1]),
+            "max_abs_dE_vs_oracle_Eh": float(np.abs(ev - ev0).max()),
+            "max_vec_diff_vs_oracle": float(np.abs(vec - vec0).max()),
+            "oracle_maneig_s": time.perf_counter() - t0, "oracle_loops": info0["nloops"]})
+        Hs.close()
     ctx.close()
     return out
 
@@ -529,6 +567,7 @@ def run_ours(a):
     t_e2e = _max_over_ranks(pg, statistics.median(e2e_times)) if e2e_times else None
     batched = batched_leg(local, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
     rk = rk_leg(local) if not a.no_extra else None
+    large = large_leg(local, cpu=(rank == 0 and not a.no_cpu_baseline)) if not (a.no_extra or a.no_large) else None
     cpu = None
     parity = None
     if rank == 0 and not a.no_cpu_baseline:
@@ -571,6 +610,7 @@ def run_ours(a):
         "cpu_baseline": cpu,
         "batched_310_blocks": batched,
         "rk_table_40_orbitals": rk,
+        "large_300k_csf": large,
     }
     print(json.dumps(out), flush=True)
     return 0
@@ -580,7 +620,7 @@ def main():
     a = _args()
     if a.large:
         ws, rank, local, pg = _dist()
-        out = large_leg(local)
+        out = large_leg(local, cpu=not a.no_cpu_baseline)
         if rank == 0:
             print(json.dumps({"leg": "large", **out}), flush=True)
         return 0

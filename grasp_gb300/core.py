@@ -324,3 +324,25 @@ class pinned:
     def __exit__(self, *exc):
         for a in self.arrays:
             _lib.gpu().gg_host_unregister(C.c_void_p(a.ctypes.data))
+
+
+def rci_select_ivec(eval_, evec, ivec):
+    """rci's choice of states (rci90/maneig.f90:496-516): MANEIG solves for
+    the lowest NVECMX = max(IVEC) eigenpairs, then brings eigenpair IVEC(i)
+    to position i by the same sequence of swaps and keeps the first NVEC.
+    eval_[nvecmx], evec[ncf, nvecmx]; ivec 1-based. Returns (eval, evec)
+    with NVEC = len(ivec) columns."""
+    ev = np.array(eval_, dtype=np.float64, copy=True)
+    vec = np.array(evec, dtype=np.float64, copy=True)
+    nvecmx = ev.size
+    iwork = list(range(1, nvecmx + 1))
+    for i in range(1, len(ivec) + 1):
+        iofset = int(ivec[i - 1])
+        loc = iwork[i - 1]
+        if iofset == loc:
+            continue
+        ev[[iofset - 1, i - 1]] = ev[[i - 1, iofset - 1]]
+        iwork[i - 1] = iwork[iofset - 1]
+        iwork[iofset - 1] = loc
+        vec[:, [iofset - 1, i - 1]] = vec[:, [i - 1, iofset - 1]]
+    return ev[:len(ivec)].copy(), vec[:, :len(ivec)].copy()
