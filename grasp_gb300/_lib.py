@@ -38,6 +38,7 @@ GPU_SYMBOLS = {
     "gg_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
     "gg_ctx_destroy": (C.c_int, [C.c_void_p]),
     "gg_ctx_synchronize": (C.c_int, [C.c_void_p]),
+    "gg_release_memory": (C.c_int, [C.c_int]),
     "gg_set_grid": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, _d, _d, _d, _d]),
     "gg_get_grid": (C.c_int, [C.c_void_p, _d, _d, _d]),
     "gg_set_orbitals": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _int, _int, _d, _d]),

@@ -61,10 +61,19 @@ int gg_ctx_create(int device, gg_ctx **out) {
   GG_CUDA(cudaGetDeviceCount(&ndev));
   if (device < 0 || device >= ndev) return fail(GG_ERR_ARG, "gg_ctx_create: no such device");
   GG_CUDA(cudaSetDevice(device));
+  {
+    // device buffers come from the default pool, which keeps what is freed
+    cudaMemPool_t pool = nullptr;
+    GG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t keep = UINT64_MAX;
+    GG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
   gg_ctx *c = new gg_ctx;
   c->device = device;
   cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, device);
-  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  // a blocking stream: the legacy stream on which device buffers are
+  // allocated and freed (gg_internal.cuh, DBuf) is ordered with it
+  cudaError_t e = cudaStreamCreate(&c->stream);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
   if (e != cudaSuccess) {
@@ -86,6 +95,18 @@ int gg_ctx_destroy(gg_ctx *ctx) {
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   gg::rk_cache_free(ctx->rk.cache);
   delete ctx;
+  return GG_OK;
+}
+
+int gg_release_memory(int device) {
+  int ndev = 0;
+  GG_CUDA(cudaGetDeviceCount(&ndev));
+  if (device < 0 || device >= ndev) return fail(GG_ERR_ARG, "gg_release_memory: no such device");
+  GG_CUDA(cudaSetDevice(device));
+  GG_CUDA(cudaDeviceSynchronize());
+  cudaMemPool_t pool = nullptr;
+  GG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  GG_CUDA(cudaMemPoolTrimTo(pool, 0));
   return GG_OK;
 }
 

@@ -37,7 +37,13 @@ constexpr int KLIMIT = 20;   // yzk.f90:54 (KLIMIT), kkstart_C KMAX
 constexpr int KEYORB = 215;  // parameter_def_M.f90:22
 constexpr int GPAD = 16;     // padding slots after NNN1 in device grid arrays
 
-// Device buffer with RAII.
+// Device buffer with RAII. Memory comes from the device's default memory
+// pool in the order of the legacy stream (cudaMallocAsync/cudaFreeAsync on
+// stream 0): the contexts' streams are blocking streams, so a free is
+// ordered after all work issued before it and an allocation before all
+// work issued after it. The pool keeps freed memory (gg_ctx_create sets no
+// release threshold), so a new matrix or workspace of a size seen before
+// maps nothing; gg_release_memory hands it back to the driver.
 template <class T> struct DBuf {
   T *p = nullptr;
   size_t n = 0;
@@ -47,7 +53,7 @@ template <class T> struct DBuf {
   DBuf &operator=(const DBuf &) = delete;
   ~DBuf() { release(); }
   void release() {
-    if (p && own) cudaFree(p);
+    if (p && own) cudaFreeAsync(p, 0);
     p = nullptr;
     n = 0;
     own = true;
@@ -63,11 +69,12 @@ template <class T> struct DBuf {
     if (count <= n && p) return GG_OK;
     release();
     if (count == 0) count = 1;
-    cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    cudaError_t e = cudaMallocAsync(reinterpret_cast<void **>(&p), count * sizeof(T), 0);
     note_alloc();
     if (e != cudaSuccess) {
       p = nullptr;
-      return fail(GG_ERR_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+      cudaGetLastError();
+      return fail(GG_ERR_NOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
     }
     n = count;
     return GG_OK;

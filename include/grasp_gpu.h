@@ -19,7 +19,10 @@
  *    process (the reference STOPs; the caller decides what to do).
  *
  * Device memory is owned by the context and its handles. All work is issued
- * on the context's CUDA stream; calls are synchronous unless documented.
+ * on the context's CUDA stream (a blocking stream); calls are synchronous
+ * unless documented. Device buffers come from the device's default memory
+ * pool, which keeps memory the library frees for its later allocations;
+ * gg_release_memory returns it to the driver.
  */
 #ifndef GRASP_GPU_H
 #define GRASP_GPU_H
@@ -60,6 +63,9 @@ int gg_ctx_create(int device, gg_ctx **out);
 int gg_ctx_destroy(gg_ctx *ctx);
 /* Blocks until all work on the context's stream has finished. */
 int gg_ctx_synchronize(gg_ctx *ctx);
+/* Waits for the device, then returns the memory the library's freed
+ * buffers left in the device's default memory pool to the driver. */
+int gg_release_memory(int device);
 
 /* ---- grid (grid_C, npot_C, def_C) ---------------------------------------
  * Replaces RADGRD (lib9290/radgrd.f90:3) + SETQIC (lib9290/setqic.f90:3) as
