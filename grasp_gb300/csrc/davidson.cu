@@ -2403,12 +2403,13 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     // coefficient test) from a sane first shift
     P1.robust = 1;
     P1.critc = 0.0;
-    // When a full-block run follows, to a residual of 1e-4 (or CRITR if
-    // that is looser): these are only its start vectors. On the 43,493-CSF
-    // Fe XV block the full-block run takes 25 passes from start vectors at
-    // 1e-3, 1e-4 and 1e-6 alike, with eigenpairs equal to 1e-12 Eh, while
-    // the leading-block run takes 13 passes instead of 17.
-    if (ns < ncf) P1.critr = std::max(P.critr, 1e-4);
+    // When a full-block run follows, to a residual of 1e-6 (or CRITR if
+    // that is looser): these are only its start vectors. Looser start
+    // vectors save passes here (on Fe XV 13 instead of 17 at 1e-4, the
+    // full-block run keeping its 25) but let DVDSON's coefficient test
+    // (CRITC, with the reference's first-pass shift) stop the full-block
+    // run early on other matrices, 1e-6 Eh from the eigenvalues.
+    if (ns < ncf) P1.critr = std::max(P.critr, 1e-6);
     // block Davidson: up to NUME correction vectors per pass, so far fewer
     // projected eigenproblems than one vector per pass
     P1.mblock = nvec;

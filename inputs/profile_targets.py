@@ -5,6 +5,8 @@ kernel family it is named for, a few times:
   python -m inputs.profile_targets spmv     # 3 full-size y = H x launches per precision
   python -m inputs.profile_targets spmm     # split Y = H X launches for 1 to 16 vectors
   python -m inputs.profile_targets solve    # one full MANEIG (split, MBLOCK = NVEC) (launch list)
+  python -m inputs.profile_targets solve2   # a warm-up MANEIG, then the measured one; prints the launch
+                                            # counts that separate them in a launch list
   python -m inputs.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
   python -m inputs.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
   python -m inputs.profile_targets batch    # two batched solves of the 310-block workload (split)
@@ -53,6 +55,18 @@ def solve():
     print("loops", info["nloops"], "E0", ev[0])
 
 
+def solve2():
+    from grasp_gb300 import SPLIT
+    from grasp_gb300.core import launch_count
+    w, ctx, H = _fe15_context()
+    H.maneig(w.nroots, flavour=0, precision=SPLIT, mblock=w.nroots)  # tunes, builds workspaces and graphs
+    ctx.synchronize()
+    l0 = launch_count()
+    ev, vec, info = H.maneig(w.nroots, flavour=0, precision=SPLIT, mblock=w.nroots)
+    ctx.synchronize()
+    print("launches before the measured solve", l0, "in it", launch_count() - l0, "loops", info["nloops"])
+
+
 def rk(precision=0):
     from grasp_gb300 import Context
     from . import workloads
@@ -81,5 +95,5 @@ def batch(zs=None):
 
 
 if __name__ == "__main__":
-    {"spmv": spmv, "spmm": spmm, "solve": solve, "rk": rk, "rk_split": rk_split, "batch": batch,
+    {"spmv": spmv, "spmm": spmm, "solve": solve, "solve2": solve2, "rk": rk, "rk_split": rk_split, "batch": batch,
      "batch8": lambda: batch(zs=tuple(range(10, 18)))}[sys.argv[1]]()
