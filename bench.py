@@ -229,6 +229,8 @@ def batched_leg(local, steps, cpu=True):
     maneig_batched(ctx, hs, w.nroots, precision=SPLIT)
     t_first = time.perf_counter() - t0
     out = dict(w.describe())
+    # the batched matvec variant the autotuner picked on this batch shape
+    out["autotune_batched_matvec"] = ctx.batched_tune()
     res = {}
     for prec, name in ((SPLIT, "split"), (FP64, "fp64")):
         maneig_batched(ctx, hs, w.nroots, precision=prec)  # warm-up

@@ -74,6 +74,7 @@ GPU_SYMBOLS = {
     "gg_projected_eig": (C.c_int, [C.c_int, _d, C.c_int, C.c_int, _d, _d]),
     "gg_hmat_tune": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _int, _int, _d]),
     "gg_hmat_tune_force": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
+    "gg_batched_tune_info": (C.c_int, [C.c_void_p, _int, _int, _d]),
     "gg_tune_variant_name": (C.c_char_p, [C.c_int, C.c_int]),
 }
 

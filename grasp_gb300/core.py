@@ -111,6 +111,15 @@ class Context:
         check(_lib.gpu().gg_iabint_table(self._h, ptr(t, _d)))
         return t.reshape(self.nw, self.nw)
 
+    def batched_tune(self):
+        """The batched matvec variant of the last gg_maneig_batched on this
+        context and the tuner's times: dict(chosen=name, ms={name: ms})."""
+        ch = C.c_int(); nv = C.c_int()
+        ms = np.zeros(6)
+        check(_lib.gpu().gg_batched_tune_info(self._h, C.byref(ch), C.byref(nv), ptr(ms, _d)))
+        name = lambda v: _lib.gpu().gg_tune_variant_name(2, v).decode()  # noqa: E731
+        return dict(chosen=name(ch.value), ms={name(v): float(ms[v]) for v in range(nv.value)})
+
     def stage_stat(self, which):
         return _lib.gpu().gg_stage_stat(self._h, which)
 

@@ -41,8 +41,11 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "gg_internal.cuh"
@@ -51,6 +54,10 @@ namespace gg {
 namespace {
 
 constexpr int TR = 128;     // rows per tile
+// batched matvec variants for the autotuner: rows per CTA x threads per CTA
+constexpr int SPMM_TR[3] = {64, 128, 256};
+constexpr int SPMM_T[2] = {128, 256};
+constexpr int SPMM_NVAR = 6;
 constexpr int BT = 256;     // threads of the tile kernels
 constexpr int RT = 128;     // threads of the row-per-thread tile kernels (= TR)
 constexpr int EIG_T = 256;  // threads of the projected eigensolver
@@ -1216,6 +1223,22 @@ __global__ void k_b_setnew(const BDesc *__restrict__ desc, BState *__restrict__ 
 // ---------------------------------------------------------------------------
 namespace {
 
+// the batched matvec's tuned variant per batch shape, for this process
+struct BatchTuneKey {
+  int dev, nb, ntot;
+  long long nnz;
+  int prec;
+  bool operator<(const BatchTuneKey &o) const {
+    return std::tie(dev, nb, ntot, nnz, prec) < std::tie(o.dev, o.nb, o.ntot, o.nnz, o.prec);
+  }
+};
+struct BatchTuneEntry {
+  int variant = 3;
+  double ms[SPMM_NVAR] = {};
+};
+std::mutex g_btune_mu;
+std::map<BatchTuneKey, BatchTuneEntry> g_btune;
+
 struct BatchRun {
   gg_ctx *ctx;
   int nb = 0, ntiles = 0, ntot = 0;
@@ -1230,6 +1253,12 @@ struct BatchRun {
   DBuf<BDesc> dDesc;
   DBuf<BState> dSt;
   DBuf<BTile> dTiles;
+  // the batched matvec's own tiles, per autotuner variant: SPMM_TR[v / 2]
+  // rows per CTA, SPMM_T[v % 2] threads; and each group's tile range in them
+  std::vector<BTile> hsp_tiles[3];
+  DBuf<BTile> dSpTiles[3];
+  int sp_t0[3][3] = {}, sp_nt[3][3] = {};  // [tile size][all, group 0, group 1]
+  int sp_var = 3;                          // 128 rows, 256 threads
   DBuf<int> dPidx, dNact;
   DBuf<double> V, W, X, R, Sp, Yp, Cp, part, XD;
   DBuf<float2> XS;
@@ -1256,19 +1285,53 @@ struct BatchRun {
 
   // the kernels that add the new columns [m, m + ncur) to the basis: matvec
   // and S update
-  int enqueue_expand(cudaStream_t s, const Group &g, int *count) {
+  int gidx(const Group &g) const { return &g == &all ? 0 : (&g == &grp[0] ? 1 : 2); }
+  // W = H V for the new columns of the group's blocks with matvec variant v
+  void launch_spmm(cudaStream_t s, const Group &g, int v) {
+    const int ts = v / 2, gi = gidx(g), nt = sp_nt[ts][gi];
+    if (nt == 0) return;
+    const BTile *tl = dSpTiles[ts].p + sp_t0[ts][gi];
+    const int thr = SPMM_T[v % 2];
+    const size_t sx = (size_t)sx_rows * sizeof(X32);
+    if (precision == GG_SPLIT)
+      k_b_spmm<true><<<nt, thr, sx, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
+    else
+      k_b_spmm<false><<<nt, thr, sx, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
+  }
+  int enqueue_expand(cudaStream_t s, const Group &g, int *count, const cudaEvent_t *tune_ev = nullptr,
+                     double *tune_ms = nullptr) {
     if (g.nb == 0) return GG_OK;
     const BTile *tl = dTiles.p + g.t0;
     const BDesc *de = dDesc.p + g.b0;
     BState *sb = dSt.p + g.b0;
     double *pt = part.p + (size_t)g.t0 * ps;
-    const size_t sx = (size_t)sx_rows * sizeof(X32);
-    if (precision == GG_SPLIT) {
+    if (precision == GG_SPLIT)
       k_b_gatherx<true><<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, XD.p, XS.p);
-      k_b_spmm<true><<<g.nt, 256, sx, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
-    } else {
+    else
       k_b_gatherx<false><<<g.nt, RT, 0, s>>>(tl, dDesc.p, dSt.p, V.p, XD.p, XS.p);
-      k_b_spmm<false><<<g.nt, 256, sx, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, XD.p, XS.p, sx_rows);
+    if (tune_ev) {
+      // the autotuner: every variant computes the same W (each row is one
+      // warp's whatever the tiles, and W is overwritten), so all run here,
+      // each between events
+      for (int v = 0; v < SPMM_NVAR; ++v) {
+        GG_CUDA(cudaEventRecord(tune_ev[2 * v], s));
+        launch_spmm(s, g, v);
+        GG_CUDA(cudaEventRecord(tune_ev[2 * v + 1], s));
+      }
+      GG_CUDA(cudaEventSynchronize(tune_ev[2 * SPMM_NVAR - 1]));
+      double best = 1e300;
+      for (int v = 0; v < SPMM_NVAR; ++v) {
+        float ms = 0.f;
+        GG_CUDA(cudaEventElapsedTime(&ms, tune_ev[2 * v], tune_ev[2 * v + 1]));
+        tune_ms[v] = ms;
+        if (ms < best) {
+          best = ms;
+          sp_var = v;
+        }
+      }
+      *count += SPMM_NVAR - 1;
+    } else {
+      launch_spmm(s, g, sp_var);
     }
     k_b_dots<2><<<g.nt, BT, dots_smem, s>>>(tl, dDesc.p, dSt.p, V.p, W.p, pt, ps);
     k_b_colsum<2><<<g.nb, 256, 0, s>>>(de, sb, part.p, ps, Sp.p, Cp.p, 0);
@@ -1445,6 +1508,25 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
     }
     B.grp[0] = BatchRun::Group{0, split, 0, split < nblocks ? B.hd[split].tile0 : B.ntiles};
     B.grp[1] = BatchRun::Group{split, nblocks - split, B.grp[0].nt, B.ntiles - B.grp[0].nt};
+    // the batched matvec's tiles for each tile size of the autotuner
+    for (int ts = 0; ts < 3; ++ts) {
+      std::vector<BTile> &v = B.hsp_tiles[ts];
+      v.clear();
+      int first_of_split = 0;
+      for (int b = 0; b < nblocks; ++b) {
+        if (b == split) first_of_split = (int)v.size();
+        const int n = B.hd[b].n, tr = SPMM_TR[ts];
+        for (int r0 = 0; r0 < n; r0 += tr) v.push_back(BTile{b, r0, std::min(tr, n - r0)});
+      }
+      if (split >= nblocks) first_of_split = (int)v.size();
+      const int tot = (int)v.size();
+      B.sp_t0[ts][0] = 0;
+      B.sp_nt[ts][0] = tot;
+      B.sp_t0[ts][1] = 0;
+      B.sp_nt[ts][1] = first_of_split;
+      B.sp_t0[ts][2] = first_of_split;
+      B.sp_nt[ts][2] = tot - first_of_split;
+    }
   }
   B.eig = EigShape{lmax, nvmax};
   B.ps = (lmax + 1) * MAXR;
@@ -1493,6 +1575,12 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   GG_CUDA(cudaMemcpyAsync(B.dSt.p, hst.data(), nblocks * sizeof(BState), cudaMemcpyHostToDevice, s));
   GG_CUDA(cudaMemcpyAsync(B.dTiles.p, B.ht.data(), B.ntiles * sizeof(BTile), cudaMemcpyHostToDevice, s));
   GG_CUDA(cudaMemcpyAsync(B.dPidx.p, hpidx.data(), pofs * sizeof(int), cudaMemcpyHostToDevice, s));
+  for (int ts = 0; ts < 3; ++ts) {
+    const size_t tot = B.hsp_tiles[ts].size();
+    GG_TRY(B.dSpTiles[ts].alloc(std::max<size_t>(tot, 1)));
+    GG_CUDA(cudaMemcpyAsync(B.dSpTiles[ts].p, B.hsp_tiles[ts].data(), tot * sizeof(BTile), cudaMemcpyHostToDevice,
+                            s));
+  }
   GG_CUDA(cudaMemsetAsync(B.Sp.p, 0, soff * sizeof(double), s));
   GG_CUDA(cudaMemsetAsync(B.part.p, 0, (size_t)B.ntiles * B.ps * sizeof(double), s));
   // start: V = unit vectors, W = H V and S = V^T W, MAXR columns at a time
@@ -1501,11 +1589,47 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
   ++launches;
   int m0max = 0;
   for (auto &d : B.hd) m0max = std::max(m0max, d.m0);
+  // the batched matvec variant: tuned on this batch shape's first start-up
+  // expansion, then kept for the shape in this process
+  long long nnz_all = 0;
+  for (int b = 0; b < nblocks; ++b) nnz_all += hs[b]->sym_nnz;
+  const BatchTuneKey tkey{ctx->device, nblocks, B.ntot, nnz_all, precision};
+  bool tune = false;
+  double tms[SPMM_NVAR] = {};
+  {
+    std::lock_guard<std::mutex> lk(g_btune_mu);
+    auto it = g_btune.find(tkey);
+    if (it != g_btune.end()) {
+      B.sp_var = it->second.variant;
+      std::copy(it->second.ms, it->second.ms + SPMM_NVAR, tms);
+    } else {
+      tune = true;
+    }
+  }
+  std::vector<cudaEvent_t> tev;
+  if (tune) {
+    tev.resize(2 * SPMM_NVAR);
+    for (auto &e : tev) GG_CUDA(cudaEventCreate(&e));
+  }
   for (int c0 = 0; c0 < m0max; c0 += MAXR) {
     k_b_setnew<<<(nblocks + 127) / 128, 128, 0, s>>>(B.dDesc.p, B.dSt.p, nblocks);
     ++launches;
-    GG_TRY(B.enqueue_expand(s, B.all, &launches));
+    const bool t = tune && c0 == 0;
+    const int rc = B.enqueue_expand(s, B.all, &launches, t ? tev.data() : nullptr, t ? tms : nullptr);
+    if (t) {
+      for (auto &e : tev) cudaEventDestroy(e);
+      tev.clear();
+    }
+    GG_TRY(rc);
+    if (t) {
+      std::lock_guard<std::mutex> lk(g_btune_mu);
+      BatchTuneEntry &en = g_btune[tkey];
+      en.variant = B.sp_var;
+      std::copy(tms, tms + SPMM_NVAR, en.ms);
+    }
   }
+  ctx->btune_var = B.sp_var;
+  std::copy(tms, tms + SPMM_NVAR, ctx->btune_ms);
   GG_CUDA(cudaGetLastError());
   // the iteration, captured once and replayed until no block is active
   int per_iter = 0;

@@ -92,6 +92,11 @@ int gg_ctx_destroy(gg_ctx *ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->aux) {
+    cudaStreamSynchronize(ctx->aux);
+    cudaStreamDestroy(ctx->aux);
+  }
+  if (ctx->aux_done) cudaEventDestroy(ctx->aux_done);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   gg::rk_cache_free(ctx->rk.cache);
   delete ctx;
@@ -300,6 +305,16 @@ double gg_stage_stat(gg_ctx *ctx, int which) {
 
 long long gg_launch_count(void) { return g_launches.load(); }
 long long gg_alloc_count(void) { return g_allocs.load(); }
+
+int gg_batched_tune_info(gg_ctx *ctx, int *chosen, int *nvariants, double *ms) {
+  if (!ctx) return fail(GG_ERR_ARG, "gg_batched_tune_info: no context");
+  if (ctx->btune_var < 0) return fail(GG_ERR_STATE, "gg_batched_tune_info: no batched solve on this context yet");
+  if (chosen) *chosen = ctx->btune_var;
+  if (nvariants) *nvariants = 6;
+  if (ms)
+    for (int i = 0; i < 6; ++i) ms[i] = ctx->btune_ms[i];
+  return GG_OK;
+}
 
 int gg_test_stall_rk_tile(gg_ctx *ctx, int tile) {
   if (!ctx) return fail(GG_ERR_ARG, "gg_test_stall_rk_tile: no context");

@@ -163,6 +163,10 @@ struct gg_ctx {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t marks[8] = {};  // gg_event_record slots
   int test_stall_tile = -1;     // gg_test_stall_rk_tile: one tensor-core tile withholds a copy, once
+  int btune_var = -1;           // the last gg_maneig_batched's matvec variant and the
+  double btune_ms[6] = {};      // tuner's times of its variants (ms)
+  cudaStream_t aux = nullptr;   // second blocking stream: uploads that overlap work on `stream`
+  cudaEvent_t aux_done = nullptr;
 };
 
 struct gg_hmat {

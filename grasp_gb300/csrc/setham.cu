@@ -524,6 +524,8 @@ int gg_hmat_create_view(gg_ctx *ctx, gg_hmat *src, gg_hmat **out) {
   return GG_OK;
 }
 
+static int build_plan(gg_ctx *ctx, gg_hmat *h, Lists &L, cudaEvent_t coeff_ready);
+
 int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *tlist, int kmaxf,
                      const gg_list *vlists) {
   if (!ctx || !h || h->ctx != ctx || !iq || !tlist || kmaxf < -1 || (kmaxf >= 0 && !vlists))
@@ -586,6 +588,11 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
   GG_TRY(L.dStart.alloc(nlab + 1));
   GG_TRY(L.dLoc.alloc(ncontr));
   GG_TRY(L.dCoeff.alloc(ncontr));
+  // the coefficients (two thirds of the bytes) travel on the second stream
+  // while the assembly plan, which reads them only in its last step, is
+  // built from the labels and LOC on the context stream
+  if (!ctx->aux) GG_CUDA(cudaStreamCreate(&ctx->aux));
+  if (!ctx->aux_done) GG_CUDA(cudaEventCreateWithFlags(&ctx->aux_done, cudaEventDisableTiming));
   // concatenate lists; label starts are shifted to global contribution offsets
   std::vector<int64_t> st;
   st.reserve(nlab + 1);
@@ -598,19 +605,33 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
     GG_CUDA(cudaMemcpyAsync(L.dLab.p + l0, x->lab, x->nlab * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
     if (nc) {
       GG_CUDA(cudaMemcpyAsync(L.dLoc.p + c0, x->loc, nc * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
-      GG_CUDA(cudaMemcpyAsync(L.dCoeff.p + c0, x->coeff, nc * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+      GG_CUDA(cudaMemcpyAsync(L.dCoeff.p + c0, x->coeff, nc * sizeof(double), cudaMemcpyHostToDevice, ctx->aux));
     }
     c0 += nc;
     l0 += x->nlab;
   }
+  GG_CUDA(cudaEventRecord(ctx->aux_done, ctx->aux));
   st.push_back(c0);
   GG_CUDA(cudaMemcpyAsync(L.dStart.p, st.data(), st.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-  double ms = 0;
-  GG_TRY(timer_stop(ctx, &ms));  // synchronises: the host vector st may go
-  ctx->stats[7] = ms;
   L.valid = true;
   h->emt_valid = false;
   h->sym_vals_valid = false;
+  int st_plan = GG_OK;
+  const std::vector<int> *key = rk_structure_key(ctx);
+  if (key && ctx->rk.valid && L.kmaxf <= ctx->rk.kloop) {
+    st_plan = build_plan(ctx, h, L, ctx->aux_done);
+    if (st_plan != GG_OK) L.plan_key.clear();
+  }
+  // the coefficients and the host arrays' copies are done before returning
+  GG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->aux_done, 0));
+  GG_CUDA(cudaStreamSynchronize(ctx->aux));
+  if (st_plan != GG_OK) {
+    L.valid = false;
+    return st_plan;
+  }
+  double ms = 0;
+  GG_TRY(timer_stop(ctx, &ms));  // synchronises: the host vector st may go
+  ctx->stats[7] = ms;
   return GG_OK;
 }
 
@@ -620,7 +641,9 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
 // list order (k_sort_gather), plus the diagonal term list in the loop order
 // of setham.f90:83-219. Kept in L until the lists or the table's index
 // structure change.
-static int build_plan(gg_ctx *ctx, gg_hmat *h, Lists &L) {
+// coeff_ready (may be null): an event after the upload of L.dCoeff, which
+// only the last step (k_sort_gather) reads.
+static int build_plan(gg_ctx *ctx, gg_hmat *h, Lists &L, cudaEvent_t coeff_ready) {
   cudaStream_t s = ctx->stream;
   const Orbitals &o = ctx->orb;
   const RkTable &rk = ctx->rk;
@@ -729,6 +752,7 @@ static int build_plan(gg_ctx *ctx, gg_hmat *h, Lists &L) {
     k_scan_final<<<(unsigned)nparts, 1024, 0, s>>>(cnt.p, nnz, part.p, chunk, L.pOff.p); ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
+  if (coeff_ready) GG_CUDA(cudaStreamWaitEvent(s, coeff_ready, 0));
   if (ncontr) {
     k_scatter_perm<<<gblocks, 256, 0, s>>>(L.dLoc.p, ncontr, L.pOff.p, fill.p, perm.p); ::gg::note_launch();
     k_sort_gather<<<(unsigned)((nnz + 255) / 256), 256, 0, s>>>(L.pOff.p, nnz, perm.p, L.dCoeff.p, cslot.p,
@@ -759,7 +783,7 @@ int gg_setham_assemble(gg_ctx *ctx, gg_hmat *h, double *eav_out) {
   const std::vector<int> *key = rk_structure_key(ctx);
   if (!key || L.plan_key != *key || L.plan_nrk != rk.n) {
     L.plan_key.clear();
-    GG_TRY(build_plan(ctx, h, L));
+    GG_TRY(build_plan(ctx, h, L, nullptr));
   }
   // combined integral array [VALTEIRK | I(ab)]
   const long long nrk = rk.n;

@@ -864,8 +864,10 @@ extern "C" const char *gg_tune_variant_name(int kernel, int variant) {
   static const char *k0[9] = {"U2 T128", "U2 T256", "U2 T512", "U4 T128", "U4 T256",
                               "U4 T512", "U8 T128", "U8 T256", "U8 T512"};
   static const char *k1[6] = {"L32 U2", "L32 U4", "L32 U8", "L16 U2", "L16 U4", "L16 U8"};
+  static const char *k2[6] = {"R64 T128", "R64 T256", "R128 T128", "R128 T256", "R256 T128", "R256 T256"};
   if (kernel == 0 && variant >= 0 && variant < 9) return k0[variant];
   if (kernel == 1 && variant >= 0 && variant < 6) return k1[variant];
+  if (kernel == 2 && variant >= 0 && variant < 6) return k2[variant];
   return "";
 }
 

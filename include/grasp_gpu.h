@@ -294,9 +294,18 @@ int gg_projected_eig(int n, const double *ap, int m, int mvec, double *w, double
  * launches (*chosen), the number of variants and their mean times per
  * launch (ms[nvariants]).
  * gg_hmat_tune_force: launch `variant` for this matrix (-1: the tuned one).
- * gg_tune_variant_name: a short name of a variant ("U4 T256", "L16 U8").   */
+ * Kernel 2 is the batched matvec of gg_maneig_batched (k_b_spmm), 6
+ * variants = 64, 128 or 256 rows per CTA x 128 or 256 threads: all of them
+ * run on the first start-up expansion of a batch shape (device, blocks,
+ * rows, stored elements, precision), each computing the same columns, and
+ * the fastest is kept for the shape in this process; gg_batched_tune_info
+ * reports the last batched solve's choice on the context and the variants'
+ * times from the run that tuned the shape.
+ * gg_tune_variant_name: a short name of a variant ("U4 T256", "L16 U8",
+ * "R128 T256").                                                           */
 int gg_hmat_tune(gg_hmat *h, int kernel, int m, int *chosen, int *nvariants, double *ms);
 int gg_hmat_tune_force(gg_hmat *h, int kernel, int m, int variant);
+int gg_batched_tune_info(gg_ctx *ctx, int *chosen, int *nvariants, double *ms);
 const char *gg_tune_variant_name(int kernel, int variant);
 
 /* ---- measurement helpers (no counterpart in the reference) ------------------

@@ -74,6 +74,24 @@ def test_batched_deterministic(gpu_ready):
     np.testing.assert_array_equal(i1["nloops"], i2["nloops"])
 
 
+def test_batched_matvec_tuner(gpu_ready):
+    """The batched matvec's autotuner times its six variants on a new batch
+    shape and keeps the fastest; a second solve of the same shape reuses the
+    choice and gives bit-identical results."""
+    from grasp_gb300 import SPLIT, maneig_batched
+    w, ctx, hs = _setup()
+    hs2 = hs[:-1]   # a batch shape no other test solved in this process
+    r1, _ = maneig_batched(ctx, hs2, 3, precision=SPLIT)
+    t = ctx.batched_tune()
+    assert len(t["ms"]) == 6 and all(x > 0 for x in t["ms"].values())
+    assert t["chosen"] == min(t["ms"], key=t["ms"].get)
+    r2, _ = maneig_batched(ctx, hs2, 3, precision=SPLIT)
+    assert ctx.batched_tune()["chosen"] == t["chosen"]
+    for a, b in zip(r1, r2):
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+
+
 def test_batched_split_vs_fp64_energies(gpu_ready):
     from grasp_gb300 import FP64, SPLIT, maneig_batched
     w, ctx, hs = _setup()
