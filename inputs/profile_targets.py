@@ -8,7 +8,7 @@ kernel family it is named for, a few times:
   python -m inputs.profile_targets solve2   # a warm-up MANEIG, then the measured one; prints the launch
                                             # counts that separate them in a launch list
   python -m inputs.profile_targets rk       # the R^k table of the 40-orbital k <= 8 workload
-  python -m inputs.profile_targets rk_split # the same on the tensor cores (int8 Ozaki slices)
+  python -m inputs.profile_targets rk_split # the same on the tensor cores (fp16 Ozaki digits, tcgen05)
   python -m inputs.profile_targets batch    # two batched solves of the 310-block workload (split)
   python -m inputs.profile_targets batch8   # the same for 8 ions (80 blocks), for detailed captures
 """

@@ -209,39 +209,45 @@ def test_maneig_tiny_blocks(gpu_ready, oracle_mod, flavour, precision):
         assert np.abs(vec - vec0).max() <= 1e-7, c
 
 
-@pytest.mark.parametrize("precision", [0, 1])
-def test_rmcdhf_warm_start(gpu_ready, oracle_mod, precision):
+def test_rmcdhf_warm_start(gpu_ready, oracle_mod):
     """rmcdhf's repeated MANEIG (rmcdhf90/maneig.f90:116-128): after the
     first solve of an SCF step, the next one starts from the previous
-    eigenvectors instead of INIEST2. On a block above N1000 = 4000 CSFs,
-    flavour 1, cold and warm: both against the oracle's eigenpairs (its
-    MANEIG with rci's settings, which converges to the same pairs with a
-    2000-row dense start instead of a 4000-row one), and the warm solve of a
-    slightly changed matrix (a perturbed diagonal, as after an orbital
-    update) needs fewer loops than its cold solve. All solves use the robust
-    first shift: with DVDSON's 1e30 sentinel the coefficient test can stop a
-    solve of this matrix early, far from CRITR (see test_oracle_eigen)."""
+    eigenvectors instead of INIEST2. On the 43,493-CSF Fe XV block (above
+    N1000 = 4000), flavour 1, both matvec precisions, cold and warm: all
+    against the oracle's eigenpairs (its MANEIG with rci's settings, which
+    converges to the same pairs with a 2000-row dense start instead of a
+    4000-row one), and the warm solve of a slightly changed matrix (a
+    perturbed diagonal, as after an orbital update) needs fewer loops than
+    its cold solve. All solves use the robust first shift."""
+    import os
+
     from grasp_gb300 import Context, HMatrix
     from inputs import workloads as W
-    ncf = 6000
-    iendc, irow, emt = W.synthetic_h(ncf, 150_000, seed=13)
+    w = W.fe15()
+    b = w.block
     ctx = Context(0)
-    H = HMatrix(ctx, ncf, iendc, irow)
-    H.set_emt(emt)
-    nvec = 3
-    ev0, vec0, info0 = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt, nthreads=8, robust=True)
-    ev, vec, info = H.maneig(nvec, flavour=1, precision=precision, robust=True)
-    assert np.abs(ev - ev0).max() <= 1e-9 and np.abs(vec - vec0).max() <= 1e-7
-    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec, robust=True)
-    assert np.abs(evw - ev0).max() <= 1e-9 and np.abs(vecw - vec0).max() <= 1e-7
+    ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
+    ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    ctx.genintrk()
+    ctx.iabint_table()
+    H = HMatrix(ctx, b.ncf, b.iendc, b.irow)
+    H.setham(b.iq, b.tlist, b.vlists)
+    emt = H.emt()
+    ncf, nvec, nth = b.ncf, 3, os.cpu_count() or 1
+    ev0, vec0, _ = oracle_mod.maneig(0, ncf, nvec, b.iendc, b.irow, emt, nthreads=nth, robust=True)
     # the next SCF step: the diagonal moves by up to 1e-4 Eh
     emt2 = emt.copy()
-    diag = iendc[1:] - 1
-    emt2[diag] += 1e-4 * np.sin(np.arange(ncf))
-    H.set_emt(emt2)
-    ev1, vec1, _ = oracle_mod.maneig(0, ncf, nvec, iendc, irow, emt2, nthreads=8, robust=True)
-    evc, vecc, infoc = H.maneig(nvec, flavour=1, precision=precision, robust=True)
-    evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec, robust=True)
-    for e, v in ((evc, vecc), (evw, vecw)):
-        assert np.abs(e - ev1).max() <= 1e-9 and np.abs(v - vec1).max() <= 1e-7
-    assert infow["nloops"] < infoc["nloops"], (infow, infoc)
+    emt2[b.iendc[1:] - 1] += 1e-4 * np.sin(np.arange(ncf))
+    ev1, vec1, _ = oracle_mod.maneig(0, ncf, nvec, b.iendc, b.irow, emt2, nthreads=nth, robust=True)
+    for precision in (0, 1):
+        H.set_emt(emt)
+        ev, vec, info = H.maneig(nvec, flavour=1, precision=precision, robust=True)
+        assert np.abs(ev - ev0).max() <= 1e-9 and np.abs(vec - vec0).max() <= 1e-7
+        evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec, robust=True)
+        assert np.abs(evw - ev0).max() <= 1e-9 and np.abs(vecw - vec0).max() <= 1e-7
+        H.set_emt(emt2)
+        evc, vecc, infoc = H.maneig(nvec, flavour=1, precision=precision, robust=True)
+        evw, vecw, infow = H.maneig(nvec, flavour=1, precision=precision, start=vec, robust=True)
+        for e, v in ((evc, vecc), (evw, vecw)):
+            assert np.abs(e - ev1).max() <= 1e-9 and np.abs(v - vec1).max() <= 1e-7, precision
+        assert infow["nloops"] < infoc["nloops"], (precision, infow, infoc)
