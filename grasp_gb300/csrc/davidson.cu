@@ -32,6 +32,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gg_internal.cuh"
@@ -500,6 +501,16 @@ __global__ void k_newvec(const NvIn *__restrict__ in, const double *__restrict__
   out->done = done;
 }
 
+// a / b to about 2^-46 relative: an FP32 reciprocal of b refined by one
+// Newton step on the quotient (three FP64 operations instead of the FP64
+// division's longer sequence; |b| > 1e-6 here, far inside FP32's range
+// after the cast for the matrices' diagonal scales)
+__device__ __forceinline__ double quot(double a, double b) {
+  const double y = (double)__frcp_rn(__double2float_rn(b));
+  const double q0 = a * y;
+  return fma(fma(-b, q0, a), y, q0);
+}
+
 // k_precond_multi with the kept targets read from device memory; columns
 // kpass + L.m .. kpass + mg - 1 of the pass are zeroed (the block pass then
 // drops them)
@@ -515,7 +526,7 @@ __global__ void k_precond_dev(double *__restrict__ B, const double *__restrict__
     const double rr = fma(-Lp->rhs[q], b, r);
     const double lam = Lp->lam[q];
     const double d = dg - lam;
-    B[(size_t)Lp->col[q] * ld + i] = (fabs(d) > 1.0e-06) ? rr / d : rr * 1.0e06;
+    B[(size_t)Lp->col[q] * ld + i] = (fabs(d) > 1.0e-06) ? quot(rr, d) : rr * 1.0e06;
     dg = d + lam;
   }
   diag[i] = dg;
@@ -677,16 +688,46 @@ __device__ __forceinline__ double bd_reduce(const double *__restrict__ part, int
   return sum;
 }
 
+// the same over double-float partials (the split kernels' CTA sums), added
+// in double-float on the FP32 pipes: GB300 issues FP64 adds at about 1/70
+// of its FP32 rate, and these reductions run on few SMs
+__device__ __forceinline__ double bd_reduce(const float2 *__restrict__ part, int ps, int ntiles, int o, bool ok,
+                                           float2 *red) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  df u{0.f, 0.f};
+  if (ok)
+#pragma unroll 8
+    for (int t = w; t < ntiles; t += nw) {
+      const float2 p = part[(size_t)t * ps + o];
+      u = df_add(u, df{p.x, p.y});
+    }
+  red[w * 32 + lane] = make_float2(u.h, u.l);
+  __syncthreads();
+  df sum{0.f, 0.f};
+  if (w == 0)
+    for (int v = 0; v < nw; ++v) {
+      const float2 p = red[v * 32 + lane];
+      sum = df_add(sum, df{p.x, p.y});
+    }
+  return (double)sum.h + (double)sum.l;
+}
+
 // MODE 0: Gram-Schmidt coefficients C = X^T W (kpass x m, row a at a m);
 // MODE 2: the new columns of S into dS (packed upper, S(i, j) at j (j+1)/2 + i).
-// 32 outputs per CTA.
-template <int MODE>
+// 32 outputs per CTA. P: the partials' type (double, or float2 double-float
+// sums of the split kernels). set_bst: block 0 also starts the pass's
+// column counts (bst = {m, m}), read first by the Gram dots after it.
+template <int MODE, typename P>
 __global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict__ pv, int m,
-                                                    const int *__restrict__ bst, const double *__restrict__ part,
+                                                    int *__restrict__ bst, const P *__restrict__ part,
                                                     int ps, int ntiles, double *__restrict__ C,
-                                                    double *__restrict__ dS) {
-  __shared__ double red[BD_T];
+                                                    double *__restrict__ dS, int set_bst) {
+  __shared__ P red[BD_T];
   const int kpass = pv[0].c;
+  if (MODE == 0 && set_bst && blockIdx.x == 0 && threadIdx.x == 0) {
+    bst[0] = m;
+    bst[1] = m;
+  }
   const int nb = (MODE == 0) ? m : bst[0];
   const int na = (MODE == 0) ? kpass : kpass + nb;
   const int o = blockIdx.x * 32 + (threadIdx.x & 31);
@@ -712,10 +753,11 @@ __global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict
 // I - F to first order (F the upper triangle of G - I, diagonal halved):
 // its error is O(|G - I|^2) and it needs no serial chain of square roots and
 // divisions, which are slow in FP64.
-__global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst, const double *__restrict__ part,
+template <typename P>
+__global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst, const P *__restrict__ part,
                                                     int ps, int ntiles, double *__restrict__ C,
                                                     double *__restrict__ skipf, int last) {
-  __shared__ double red[BD_RED];
+  __shared__ P red[BD_RED];
   __shared__ double G[MT_MAX * MT_MAX];   // Schur complement [q][q']
   __shared__ double R[MT_MAX * MT_MAX];   // row c of R over the current columns
   __shared__ double Ri[MT_MAX * MT_MAX];  // R^-1 of the kept columns [i][c]
@@ -727,13 +769,32 @@ __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst
   const int grp = tid >> 7, sub = (tid >> 5) & 3, lane = tid & 31;
   const int o = grp * 32 + lane;
   const bool ok = nb > 0 && o < nb * nb;
-  double u = 0.0;
-  if (ok)
+  if constexpr (std::is_same<P, double>::value) {
+    double u = 0.0;
+    if (ok)
 #pragma unroll 8
-    for (int t = sub; t < ntiles; t += 4) u += part[(size_t)t * ps + o];
-  red[tid] = u;
-  __syncthreads();
-  if (sub == 0 && ok) G[o] = ((red[tid] + red[tid + 32]) + red[tid + 64]) + red[tid + 96];
+      for (int t = sub; t < ntiles; t += 4) u += part[(size_t)t * ps + o];
+    red[tid] = u;
+    __syncthreads();
+    if (sub == 0 && ok) G[o] = ((red[tid] + red[tid + 32]) + red[tid + 64]) + red[tid + 96];
+  } else {
+    // double-float sums (FP32 pipes)
+    df u{0.f, 0.f};
+    if (ok)
+#pragma unroll 8
+      for (int t = sub; t < ntiles; t += 4) {
+        const float2 p = part[(size_t)t * ps + o];
+        u = df_add(u, df{p.x, p.y});
+      }
+    red[tid] = make_float2(u.h, u.l);
+    __syncthreads();
+    if (sub == 0 && ok) {
+      df g{0.f, 0.f};
+#pragma unroll
+      for (int v = 0; v < 4; ++v) g = df_add(g, df{red[tid + 32 * v].x, red[tid + 32 * v].y});
+      G[o] = (double)g.h + (double)g.l;
+    }
+  }
   __syncthreads();
   const bool near = __syncthreads_and(tid >= nb * nb || fabs(G[tid] - ((tid / nb == tid % nb) ? 1.0 : 0.0)) <= 1e-8);
   if (near) {
@@ -797,13 +858,6 @@ __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst
   if (last && lane < m) skipf[lane] = (lane < nk) ? 0.0 : 1.0;
 }
 
-// first kernel of the pass: bst[0] = m
-__global__ void k_bd_start(int m, int *bst) {
-  if (threadIdx.x == 0) {
-    bst[0] = m;
-    bst[1] = m;
-  }
-}
 
 // new columns minus their projections: B(:, kpass+q) -= B(:, 0:kpass) C(:, q)
 constexpr int BD_CCH = 64;  // rows of C staged per step
@@ -909,6 +963,54 @@ __device__ __forceinline__ float2 split2(double v) {
   return make_float2(h, __double2float_rn(v - (double)h));
 }
 
+// k_bd_apply in split form: each row's np column values are split into hi +
+// lo floats and combined with the split C by Dot2 sums (FP32 pipes); the
+// FP64 result is the sum's hi + lo, whose split is the same pair, so the
+// matvec copy (xs) and the basis store (xstore) hold exactly the FP64 value
+template <int NP>
+__device__ __forceinline__ void bdx_apply_rows(double *__restrict__ B, int64_t ld, int kpass, int nc,
+                                               const float2 *Cs, int i, float2 *xs, int mp, float2 *xstore) {
+  float2 x[NP];
+#pragma unroll
+  for (int q = 0; q < NP; ++q) x[q] = split2(B[(size_t)(kpass + q) * ld + i]);
+  for (int c = 0; c < nc; ++c) {
+    float h = 0.f, l = 0.f;
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+      const float2 cq = Cs[q * MT_MAX + c];
+      dot2_step(h, l, cq.x, cq.y, x[q].x, x[q].y);
+    }
+    const df v = two_sum(h, l);
+    B[(size_t)(kpass + c) * ld + i] = (double)v.h + (double)v.l;
+    if (xs) {
+      const float2 v2 = make_float2(v.h, v.l);
+      xs[(size_t)i * mp + c] = v2;
+      xstore[(size_t)(kpass + c) * ld + i] = v2;
+    }
+  }
+  if (xs)
+    for (int c = nc; c < mp; ++c) xs[(size_t)i * mp + c] = make_float2(0.f, 0.f);
+}
+
+__global__ void __launch_bounds__(RT) k_bdx_apply(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
+                                                  const int *__restrict__ bst, const double *__restrict__ C, int n,
+                                                  float2 *__restrict__ xs, int mp, float2 *__restrict__ xstore) {
+  __shared__ float2 Cs[MT_MAX * MT_MAX];
+  const int kpass = pv[0].c, np = bst[1], nc = bst[0];
+  for (int idx = threadIdx.x; idx < MT_MAX * MT_MAX; idx += RT) Cs[idx] = split2(C[idx]);
+  __syncthreads();
+  const int i = blockIdx.x * RT + threadIdx.x;
+  if (i >= n || np <= 0) return;
+  switch (np) {
+#define BD_CASE(K) \
+  case K: bdx_apply_rows<K>(B, ld, kpass, nc, Cs, i, xs, mp, xstore); break;
+    BD_CASE(1) BD_CASE(2) BD_CASE(3) BD_CASE(4) BD_CASE(5) BD_CASE(6) BD_CASE(7) BD_CASE(8)
+    BD_CASE(9) BD_CASE(10) BD_CASE(11) BD_CASE(12) BD_CASE(13) BD_CASE(14) BD_CASE(15) BD_CASE(16)
+#undef BD_CASE
+    default: break;
+  }
+}
+
 // hi + lo copies of columns c0 .. c0+nc of X
 __global__ void k_split_cols(const double *__restrict__ X, int64_t ld, int c0, int nc, int n, float2 *__restrict__ Xx) {
   const int64_t tot = (int64_t)nc * n;
@@ -927,7 +1029,7 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
                                                    const float2 *__restrict__ Bx, float2 *__restrict__ ABx,
                                                    int64_t ld, const IterParams *__restrict__ pv, int m,
                                                    const int *__restrict__ bst, int n, int cpc,
-                                                   double *__restrict__ part, int ps) {
+                                                   float2 *__restrict__ part, int ps) {
   __shared__ float2 Bs[BD_R * MT_MAX];       // [i][q]
   __shared__ float2 As[BD_R * (BD_AC + 1)];  // [i][a]
   const int kpass = pv[0].c;
@@ -935,7 +1037,7 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
   if (nb <= 0) return;
   const int na = (MODE == 0) ? kpass : (MODE == 1 ? nb : kpass + nb);
   const double *Wb = ((MODE == 2) ? AB : B) + (size_t)kpass * ld;
-  double *out = part + (size_t)blockIdx.x * ps;
+  float2 *out = part + (size_t)blockIdx.x * ps;
   const int rbeg = blockIdx.x * cpc * BD_R, rend = min(n, rbeg + cpc * BD_R);
   for (int ac = blockIdx.y * BD_AC; ac < na; ac += gridDim.y * BD_AC) {
     const int nac = min(BD_AC, na - ac), np = nac * nb;
@@ -975,7 +1077,10 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
 #pragma unroll
     for (int k = 0; k < BD_PAIRS; ++k) {
       const int pr = threadIdx.x + k * BD_T;
-      if (pr < np) out[(ac + pr % nac) * nb + pr / nac] = (double)sh[k] + (double)sl[k];
+      if (pr < np) {
+        const df v = two_sum(sh[k], sl[k]);
+        out[(ac + pr % nac) * nb + pr / nac] = make_float2(v.h, v.l);
+      }
     }
   }
 }
@@ -1043,10 +1148,13 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
                                                     double *__restrict__ part, unsigned *__restrict__ counter,
                                                     double *__restrict__ rn2) {
   __shared__ float2 sv[MT_SMEM];
+  __shared__ float2 slam[NT];
   __shared__ double red[RT / 32];
+  __shared__ float fred[RT / 32];
   __shared__ bool last;
   const int t0 = blockIdx.y * NT;
   for (int q = threadIdx.x; q < NT * k; q += RT) sv[q] = split2(S[(size_t)t0 * k + q]);
+  if (threadIdx.x < NT) slam[threadIdx.x] = split2(lam[t0 + threadIdx.x]);
   __syncthreads();
   const int lp = threadIdx.x % L;
   const int i = blockIdx.x * (RT / L) + threadIdx.x / L;
@@ -1065,18 +1173,32 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
       }
     }
   }
+  // r = a - lambda b in double-float (FP32 pipes); only the two stores
+  // convert to FP64. |r|^2 is summed in FP32 (a norm for NEWVEC's tests, to
+  // about 1e-7 relative)
 #pragma unroll
   for (int t = 0; t < NT; ++t) {
     const df b2 = df_lanes<L>(bh[t], bl[t]), a2 = df_lanes<L>(ah[t], al[t]);
-    double r = 0.0;
+    float rsq = 0.f;
     if (i < n && t % L == lp) {
-      const double b = (double)b2.h + (double)b2.l, a = (double)a2.h + (double)a2.l;
-      r = fma(-lam[t0 + t], b, a);
-      T[(size_t)(2 * (t0 + t)) * ld + i] = b;
-      T[(size_t)(2 * (t0 + t) + 1) * ld + i] = r;
+      const float2 lm = slam[t];
+      const float ph = lm.x * b2.h;
+      const float pl = fmaf(lm.x, b2.l, fmaf(lm.y, b2.h, fmaf(lm.x, b2.h, -ph)));
+      const df r = df_add(a2, df{-ph, -pl});
+      T[(size_t)(2 * (t0 + t)) * ld + i] = (double)b2.h + (double)b2.l;
+      T[(size_t)(2 * (t0 + t) + 1) * ld + i] = (double)r.h + (double)r.l;
+      rsq = r.h * r.h;
     }
-    const double sq = block_sum<RT>(r * r, red);
-    if (threadIdx.x == 0) part[(size_t)(t0 + t) * gridDim.x + blockIdx.x] = sq;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) rsq += __shfl_xor_sync(0xffffffffu, rsq, o);
+    if ((threadIdx.x & 31) == 0) fred[threadIdx.x >> 5] = rsq;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float sq = 0.f;
+#pragma unroll
+      for (int q = 0; q < RT / 32; ++q) sq += fred[q];
+      part[(size_t)(t0 + t) * gridDim.x + blockIdx.x] = (double)sq;
+    }
     __syncthreads();
   }
   __threadfence();
@@ -1417,15 +1539,17 @@ struct Dvd {
     const bool split = (precision == GG_SPLIT);
     const int nred = std::max(1, (lim * m + 31) / 32);
     const bool sub_split = (int64_t)nrow * 2 < ctx->sms;  // small blocks: one column per grid row
-    k_bd_start<<<1, 32, 0, s>>>(m, bst.p);
-    note_launch();
+    // the split kernels' CTA partials are double-float pairs in the same buffer
+    float2 *bpx = reinterpret_cast<float2 *>(bpart.p);
     const dim3 gd(bd_G, bd_Y);
     for (int round = 0; round < 2; ++round) {
-      if (split)
-        k_bdx_dots<0><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-      else
+      if (split) {
+        k_bdx_dots<0><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx, bd_ps);
+        k_bd_reduce<0, float2><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p, round == 0);
+      } else {
         k_bd_dots<0><<<gd, BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-      k_bd_reduce<0><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p);
+        k_bd_reduce<0, double><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, round == 0);
+      }
       if (sub_split) {
         if (split)
           k_bdx_sub<1, SP><<<dim3(nrow4, m), RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);
@@ -1452,14 +1576,17 @@ struct Dvd {
       note_launches(3);
     }
     for (int round = 0; round < 2; ++round) {
-      if (split)
-        k_bdx_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc,
-                                                      bpart.p, bd_ps);
-      else
+      if (split) {
+        k_bdx_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
+                                                      bd_ps);
+        k_bd_chol<float2><<<1, BD_RED, 0, s>>>(m, bst.p, bpx, bd_ps, bd_G, bC.p, bskip.p, round);
+        k_bdx_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, round == 1 ? bxs.p : nullptr,
+                                        spmm_pitch(m), Bx.p);
+      } else {
         k_bd_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-      k_bd_chol<<<1, BD_RED, 0, s>>>(m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round);
-      k_bd_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, (round == 1 && split) ? bxs.p : nullptr,
-                                     spmm_pitch(m), Bx.p);
+        k_bd_chol<double><<<1, BD_RED, 0, s>>>(m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round);
+        k_bd_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, nullptr, spmm_pitch(m), Bx.p);
+      }
       note_launches(3);
     }
     GG_CUDA(cudaGetLastError());
@@ -1494,11 +1621,13 @@ struct Dvd {
         GG_CUDA(cudaEventRecord(bev[2 * v + 1], s));
       }
     }
-    if (split)
-      k_bdx_dots<2><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-    else
+    if (split) {
+      k_bdx_dots<2><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx, bd_ps);
+      k_bd_reduce<2, float2><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p, 0);
+    } else {
       k_bd_dots<2><<<gd, BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-    k_bd_reduce<2><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p);
+      k_bd_reduce<2, double><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, 0);
+    }
     note_launches(2);
     GG_CUDA(cudaMemcpyAsync(hbst, bst.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     GG_CUDA(cudaGetLastError());
