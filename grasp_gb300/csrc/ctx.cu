@@ -92,6 +92,7 @@ int gg_ctx_destroy(gg_ctx *ctx) {
     if (e) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev_mid) cudaEventDestroy(ctx->ev_mid);
   if (ctx->aux) {
     cudaStreamSynchronize(ctx->aux);
     cudaStreamDestroy(ctx->aux);
@@ -299,7 +300,7 @@ int gg_set_orbitals(gg_ctx *ctx, int nw, int ld, const int *nak, const int *mf, 
 }
 
 double gg_stage_stat(gg_ctx *ctx, int which) {
-  if (!ctx || which < 0 || which >= 26) return -1.0;
+  if (!ctx || which < 0 || which >= 30) return -1.0;
   return ctx->stats[which];
 }
 

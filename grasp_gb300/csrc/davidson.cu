@@ -375,6 +375,7 @@ __global__ void __launch_bounds__(RT) k_ritz_multi(const double *__restrict__ B,
                                                    const double *__restrict__ lam, double *__restrict__ T, int n,
                                                    double *__restrict__ part, unsigned *__restrict__ counter,
                                                    double *__restrict__ rn2) {
+  pdl_wait();
   __shared__ double sv[MT_SMEM];
   __shared__ double red[RT / 32];
   __shared__ bool last;
@@ -466,6 +467,7 @@ struct NvOut {
 };
 __global__ void k_newvec(const NvIn *__restrict__ in, const double *__restrict__ rn2, PrecList *__restrict__ L,
                          NvOut *__restrict__ out) {
+  pdl_wait();
   // the square roots in parallel (lane t), the choices by lane 0 in order
   __shared__ double sres[MT_MAX], srhs[MT_MAX];
   const int nt = in->nt, t = threadIdx.x;
@@ -516,6 +518,7 @@ __device__ __forceinline__ double quot(double a, double b) {
 // drops them)
 __global__ void k_precond_dev(double *__restrict__ B, const double *__restrict__ T, int64_t ld,
                               const PrecList *__restrict__ Lp, double *__restrict__ diag, int n, int mg, int kpass) {
+  pdl_wait();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int m = Lp->m;
@@ -619,6 +622,7 @@ __global__ void __launch_bounds__(BD_T) k_bd_dots(const double *__restrict__ B, 
                                                   int64_t ld, const IterParams *__restrict__ pv, int m,
                                                   const int *__restrict__ bst, int n, int cpc,
                                                   double *__restrict__ part, int ps) {
+  pdl_wait();
   __shared__ double Bs[BD_R * MT_MAX];       // [i][q]
   __shared__ double As[BD_R * (BD_AC + 1)];  // [i][a]
   const int kpass = pv[0].c;
@@ -722,6 +726,7 @@ __global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict
                                                     int *__restrict__ bst, const P *__restrict__ part,
                                                     int ps, int ntiles, double *__restrict__ C,
                                                     double *__restrict__ dS, int set_bst) {
+  pdl_wait();
   __shared__ P red[BD_T];
   const int kpass = pv[0].c;
   if (MODE == 0 && set_bst && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -757,6 +762,7 @@ template <typename P>
 __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst, const P *__restrict__ part,
                                                     int ps, int ntiles, double *__restrict__ C,
                                                     double *__restrict__ skipf, int last) {
+  pdl_wait();
   __shared__ P red[BD_RED];
   __shared__ double G[MT_MAX * MT_MAX];   // Schur complement [q][q']
   __shared__ double R[MT_MAX * MT_MAX];   // row c of R over the current columns
@@ -865,6 +871,7 @@ constexpr int BD_CCH = 64;  // rows of C staged per step
 template <int M>
 __global__ void __launch_bounds__(RT) k_bd_sub(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
                                                const double *__restrict__ C, int m, int n) {
+  pdl_wait();
   __shared__ double Cs[BD_CCH * M];
   const int ka = pv[0].c, q0 = blockIdx.y * M;
   const int i = blockIdx.x * RT + threadIdx.x;
@@ -920,6 +927,7 @@ __device__ __forceinline__ void bd_apply_rows(double *__restrict__ B, int64_t ld
 __global__ void __launch_bounds__(RT) k_bd_apply(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
                                                  const int *__restrict__ bst, const double *__restrict__ C, int n,
                                                  float2 *__restrict__ xs, int mp, float2 *__restrict__ xstore) {
+  pdl_wait();
   __shared__ double Cs[MT_MAX * MT_MAX];
   const int kpass = pv[0].c, np = bst[1], nc = bst[0];
   for (int idx = threadIdx.x; idx < MT_MAX * MT_MAX; idx += RT) Cs[idx] = C[idx];
@@ -995,6 +1003,7 @@ __device__ __forceinline__ void bdx_apply_rows(double *__restrict__ B, int64_t l
 __global__ void __launch_bounds__(RT) k_bdx_apply(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
                                                   const int *__restrict__ bst, const double *__restrict__ C, int n,
                                                   float2 *__restrict__ xs, int mp, float2 *__restrict__ xstore) {
+  pdl_wait();
   __shared__ float2 Cs[MT_MAX * MT_MAX];
   const int kpass = pv[0].c, np = bst[1], nc = bst[0];
   for (int idx = threadIdx.x; idx < MT_MAX * MT_MAX; idx += RT) Cs[idx] = split2(C[idx]);
@@ -1013,6 +1022,7 @@ __global__ void __launch_bounds__(RT) k_bdx_apply(double *__restrict__ B, int64_
 
 // hi + lo copies of columns c0 .. c0+nc of X
 __global__ void k_split_cols(const double *__restrict__ X, int64_t ld, int c0, int nc, int n, float2 *__restrict__ Xx) {
+  pdl_wait();
   const int64_t tot = (int64_t)nc * n;
   for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
     const int c = (int)(e / n), i = (int)(e % n);
@@ -1030,6 +1040,7 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
                                                    int64_t ld, const IterParams *__restrict__ pv, int m,
                                                    const int *__restrict__ bst, int n, int cpc,
                                                    float2 *__restrict__ part, int ps) {
+  pdl_wait();
   __shared__ float2 Bs[BD_R * MT_MAX];       // [i][q]
   __shared__ float2 As[BD_R * (BD_AC + 1)];  // [i][a]
   const int kpass = pv[0].c;
@@ -1107,6 +1118,7 @@ template <int M, int L>
 __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const float2 *__restrict__ Bx, int64_t ld,
                                                 const IterParams *__restrict__ pv, const double *__restrict__ C,
                                                 int m, int n) {
+  pdl_wait();
   __shared__ float2 Cs[BD_CCH * M];
   const int ka = pv[0].c, q0 = blockIdx.y * M;
   const int part = threadIdx.x % L;
@@ -1147,6 +1159,7 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
                                                     const double *__restrict__ lam, double *__restrict__ T, int n,
                                                     double *__restrict__ part, unsigned *__restrict__ counter,
                                                     double *__restrict__ rn2) {
+  pdl_wait();
   __shared__ float2 sv[MT_SMEM];
   __shared__ float2 slam[NT];
   __shared__ double red[RT / 32];
@@ -1317,8 +1330,8 @@ struct Dvd {
     }
     const int nc = k - bx_cols;
     const int grid = std::min<int64_t>(((int64_t)nc * n + TPB - 1) / TPB, 8 * ctx->sms);
-    k_split_cols<<<grid, TPB, 0, s>>>(B.p, ld, bx_cols, nc, n, Bx.p);
-    k_split_cols<<<grid, TPB, 0, s>>>(AB.p, ld, bx_cols, nc, n, ABx.p);
+    GG_CUDA(launch_pdl(k_split_cols, grid, TPB, 0, s, B.p, ld, bx_cols, nc, n, Bx.p));
+    GG_CUDA(launch_pdl(k_split_cols, grid, TPB, 0, s, AB.p, ld, bx_cols, nc, n, ABx.p));
     note_launches(2);
     GG_CUDA(cudaGetLastError());
     bx_cols = k;
@@ -1544,28 +1557,31 @@ struct Dvd {
     const dim3 gd(bd_G, bd_Y);
     for (int round = 0; round < 2; ++round) {
       if (split) {
-        k_bdx_dots<0><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx, bd_ps);
-        k_bd_reduce<0, float2><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p, round == 0);
+        GG_CUDA(launch_pdl(k_bdx_dots<0>, gd, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
+                           bd_ps));
+        GG_CUDA(launch_pdl(k_bd_reduce<0, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p,
+                           round == 0));
       } else {
-        k_bd_dots<0><<<gd, BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-        k_bd_reduce<0, double><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, round == 0);
+        GG_CUDA(launch_pdl(k_bd_dots<0>, gd, BD_T, 0, s, B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps));
+        GG_CUDA(launch_pdl(k_bd_reduce<0, double>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, round == 0));
       }
       if (sub_split) {
         if (split)
-          k_bdx_sub<1, SP><<<dim3(nrow4, m), RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);
+          GG_CUDA(launch_pdl(k_bdx_sub<1, SP>, dim3(nrow4, m), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n));
         else
-          k_bd_sub<1><<<dim3(nrow, m), RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);
+          GG_CUDA(launch_pdl(k_bd_sub<1>, dim3(nrow, m), RT, 0, s, B.p, ld, dpv.p, bC.p, m, n));
       } else {
         // an even m as m / 2 grid rows of two columns (more warps in flight;
-        // each grid row reads the basis, from L2)
+        // each grid row reads the basis, from L2; all m columns with two
+        // lanes per row measured slower)
         const int half = (m % 2 == 0) ? m / 2 : 1;
         switch (m / half) {
 #define BD_SUB(K)                                                                           \
   case K:                                                                                   \
     if (split)                                                                              \
-      k_bdx_sub<K, 1><<<dim3(nrow, half), RT, 0, s>>>(B.p, Bx.p, ld, dpv.p, bC.p, m, n);     \
+      GG_CUDA(launch_pdl(k_bdx_sub<K, 1>, dim3(nrow, half), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n));     \
     else                                                                                    \
-      k_bd_sub<K><<<dim3(nrow, half), RT, 0, s>>>(B.p, ld, dpv.p, bC.p, m, n);              \
+      GG_CUDA(launch_pdl(k_bd_sub<K>, dim3(nrow, half), RT, 0, s, B.p, ld, dpv.p, bC.p, m, n));              \
     break;
         BD_SUB(1) BD_SUB(2) BD_SUB(3) BD_SUB(4) BD_SUB(5) BD_SUB(6) BD_SUB(7) BD_SUB(8)
         BD_SUB(9) BD_SUB(10) BD_SUB(11) BD_SUB(12) BD_SUB(13) BD_SUB(14) BD_SUB(15) BD_SUB(16)
@@ -1577,15 +1593,15 @@ struct Dvd {
     }
     for (int round = 0; round < 2; ++round) {
       if (split) {
-        k_bdx_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
-                                                      bd_ps);
-        k_bd_chol<float2><<<1, BD_RED, 0, s>>>(m, bst.p, bpx, bd_ps, bd_G, bC.p, bskip.p, round);
-        k_bdx_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, round == 1 ? bxs.p : nullptr,
-                                        spmm_pitch(m), Bx.p);
+        GG_CUDA(launch_pdl(k_bdx_dots<1>, dim3(bd_G, 1), BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n,
+                           bd_cpc, bpx, bd_ps));
+        GG_CUDA(launch_pdl(k_bd_chol<float2>, 1, BD_RED, 0, s, m, bst.p, bpx, bd_ps, bd_G, bC.p, bskip.p, round));
+        GG_CUDA(launch_pdl(k_bdx_apply, nrow, RT, 0, s, B.p, ld, dpv.p, bst.p, bC.p, n, round == 1 ? bxs.p : nullptr,
+                                        spmm_pitch(m), Bx.p));
       } else {
-        k_bd_dots<1><<<dim3(bd_G, 1), BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-        k_bd_chol<double><<<1, BD_RED, 0, s>>>(m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round);
-        k_bd_apply<<<nrow, RT, 0, s>>>(B.p, ld, dpv.p, bst.p, bC.p, n, nullptr, spmm_pitch(m), Bx.p);
+        GG_CUDA(launch_pdl(k_bd_dots<1>, dim3(bd_G, 1), BD_T, 0, s, B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps));
+        GG_CUDA(launch_pdl(k_bd_chol<double>, 1, BD_RED, 0, s, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round));
+        GG_CUDA(launch_pdl(k_bd_apply, nrow, RT, 0, s, B.p, ld, dpv.p, bst.p, bC.p, n, nullptr, spmm_pitch(m), Bx.p));
       }
       note_launches(3);
     }
@@ -1622,11 +1638,12 @@ struct Dvd {
       }
     }
     if (split) {
-      k_bdx_dots<2><<<gd, BD_T, 0, s>>>(B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx, bd_ps);
-      k_bd_reduce<2, float2><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p, 0);
+      GG_CUDA(launch_pdl(k_bdx_dots<2>, gd, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
+                         bd_ps));
+      GG_CUDA(launch_pdl(k_bd_reduce<2, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p, 0));
     } else {
-      k_bd_dots<2><<<gd, BD_T, 0, s>>>(B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps);
-      k_bd_reduce<2, double><<<nred, BD_T, 0, s>>>(dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, 0);
+      GG_CUDA(launch_pdl(k_bd_dots<2>, gd, BD_T, 0, s, B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps));
+      GG_CUDA(launch_pdl(k_bd_reduce<2, double>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, 0));
     }
     note_launches(2);
     GG_CUDA(cudaMemcpyAsync(hbst, bst.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -1899,15 +1916,16 @@ struct Dvd {
     if (use_x()) {
       GG_TRY(sync_split(k));
       if (per_target) {
-        k_ritzx_multi<1, SP><<<dim3(nrow4, nt), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
-                                                       counters.p + 3, drn);
+        GG_CUDA(launch_pdl(k_ritzx_multi<1, SP>, dim3(nrow4, nt), RT, 0, s, Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
+                                                       counters.p + 3, drn));
       } else {
         // an even nt as two grid rows of nt / 2 targets (twice the warps;
-        // finer splits re-read the basis more than they gain)
+        // one sweep of all targets with one or two lanes per row, and finer
+        // splits, measured slower)
         const int half = (nt % 2 == 0) ? 2 : 1;
         switch (nt / half) {
 #define RM_CASE(K) \
-  case K: k_ritzx_multi<K, 1><<<dim3(nrow, half), RT, 0, s>>>(Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
+  case K: GG_CUDA(launch_pdl(k_ritzx_multi<K, 1>, dim3(nrow, half), RT, 0, s, Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn)); break;
           RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
           RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
 #undef RM_CASE
@@ -1915,12 +1933,12 @@ struct Dvd {
         }
       }
     } else if (per_target) {
-      k_ritz_multi<1><<<dim3(nrow, nt), RT, 0, s>>>(B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3,
-                                                    drn);
+      GG_CUDA(launch_pdl(k_ritz_multi<1>, dim3(nrow, nt), RT, 0, s, B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3,
+                                                    drn));
     } else {
       switch (nt) {
 #define RM_CASE(K) \
-  case K: k_ritz_multi<K><<<nrow, RT, 0, s>>>(B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn); break;
+  case K: GG_CUDA(launch_pdl(k_ritz_multi<K>, nrow, RT, 0, s, B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn)); break;
         RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
         RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
 #undef RM_CASE
@@ -1952,8 +1970,8 @@ struct Dvd {
     GG_CUDA(cudaMemcpyAsync(dnv_in.p, hnv_in, sizeof(NvIn), cudaMemcpyHostToDevice, s));
     GG_TRY(launch_ritz_multi(k, nt, svec, in.lam));
     const double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
-    k_newvec<<<1, 32, 0, s>>>(dnv_in.p, drn, dL.p, dnv_out.p);
-    k_precond_dev<<<(n + TPB - 1) / TPB, TPB, 0, s>>>(B.p, T.p, ld, dL.p, diag.p, n, mg, k);
+    GG_CUDA(launch_pdl(k_newvec, 1, 32, 0, s, dnv_in.p, drn, dL.p, dnv_out.p));
+    GG_CUDA(launch_pdl(k_precond_dev, (n + TPB - 1) / TPB, TPB, 0, s, B.p, T.p, ld, dL.p, diag.p, n, mg, k));
     note_launches(2);
     GG_CUDA(cudaGetLastError());
     GG_CUDA(cudaMemcpyAsync(hnv_out, dnv_out.p, sizeof(NvOut), cudaMemcpyDeviceToHost, s));
@@ -2470,6 +2488,8 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   // whole space (LIM = NCF, solved in the full unit basis below)
   if (P.lim < nvec + 4 && P.lim != ncf) return fail(GG_ERR_ARG, "gg_maneig: LIM too small (below NVEC + 4)");
   if (P.lim > 1024) return fail(GG_ERR_ARG, "gg_maneig: LIM above 1024 is not supported");
+  using hclock = std::chrono::steady_clock;
+  const auto th0 = hclock::now();
   GG_TRY(refresh_sym_values(h));
   std::vector<double> ev, res;
   double mv_ms = 0;
@@ -2494,8 +2514,20 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
     }
     blk = h->lead;
   }
+  // device time to here (symmetric structures of the block and of its
+  // leading block) is read at the end; host time of the workspaces apart
+  if (!ctx->ev_mid) GG_CUDA(cudaEventCreate(&ctx->ev_mid));
+  GG_CUDA(cudaEventRecord(ctx->ev_mid, ctx->stream));
+  ctx->stats[26] = 1e3 * std::chrono::duration<double>(hclock::now() - th0).count();
+  ctx->stats[27] = 0;
   // Davidson workspaces kept with the matrix, by stage and precision
   auto workspace = [&](int stage, gg_hmat *hm, int nn, int lm, Dvd **out) -> int {
+    const auto tw0 = hclock::now();
+    struct Acc {
+      double *dst;
+      hclock::time_point t0;
+      ~Acc() { *dst += 1e3 * std::chrono::duration<double>(hclock::now() - t0).count(); }
+    } acc{&ctx->stats[27], tw0};
     std::shared_ptr<void> &c = h->dvd_cache[2 * stage + (precision == GG_SPLIT ? 1 : 0)];
     Dvd *d = static_cast<Dvd *>(c.get());
     if (d && d->reusable(hm, precision, nn, lm)) {
@@ -2623,6 +2655,11 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   }
   double ms = 0;
   GG_TRY(timer_stop(ctx, &ms));
+  {
+    float f = 0.f;
+    GG_CUDA(cudaEventElapsedTime(&f, ctx->ev0, ctx->ev_mid));
+    ctx->stats[28] = f;
+  }
   ctx->stats[3] = ms;
   ctx->stats[4] = mv_ms;
   ctx->stats[5] = mv_count;

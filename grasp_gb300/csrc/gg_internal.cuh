@@ -5,6 +5,7 @@
 
 #include <memory>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/grasp_gpu.h"
@@ -32,6 +33,32 @@ void note_alloc();
     int s_ = (call);             \
     if (s_ != GG_OK) return s_;  \
   } while (0)
+
+// Programmatic dependent launch. A kernel launched by launch_pdl may be
+// scheduled while the kernel before it on the stream is still running, so
+// that its launch overlaps that kernel's last wave; it must call pdl_wait()
+// before it touches memory (griddepcontrol.wait returns once every
+// prerequisite grid has completed and its writes are visible). pdl_trigger()
+// lets the next such kernel be scheduled (it only starts waiting: the
+// ordering is kept by its own pdl_wait). In a stream capture the launches
+// become programmatic graph edges.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args &&...args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Args>(args)...);
+}
 
 constexpr int KLIMIT = 20;   // yzk.f90:54 (KLIMIT), kkstart_C KMAX
 constexpr int KEYORB = 215;  // parameter_def_M.f90:22
@@ -159,8 +186,9 @@ struct gg_ctx {
   gg::RkTable rk;
   gg::DBuf<double> dIab;                // [nw * nw]
   bool iab_valid = false;
-  double stats[26] = {};
+  double stats[32] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev_mid = nullptr;  // a point inside a timed call (gg_maneig: after its structures)
   cudaEvent_t marks[8] = {};  // gg_event_record slots
   int test_stall_tile = -1;     // gg_test_stall_rk_tile: one tensor-core tile withholds a copy, once
   int btune_var = -1;           // the last gg_maneig_batched's matvec variant and the

@@ -618,7 +618,10 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
   h->sym_vals_valid = false;
   int st_plan = GG_OK;
   const std::vector<int> *key = rk_structure_key(ctx);
+  ctx->stats[29] = 0;
   if (key && ctx->rk.valid && L.kmaxf <= ctx->rk.kloop) {
+    if (!ctx->ev_mid) GG_CUDA(cudaEventCreate(&ctx->ev_mid));
+    GG_CUDA(cudaEventRecord(ctx->ev_mid, ctx->stream));
     st_plan = build_plan(ctx, h, L, ctx->aux_done);
     if (st_plan != GG_OK) L.plan_key.clear();
   }
@@ -632,6 +635,11 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
   double ms = 0;
   GG_TRY(timer_stop(ctx, &ms));  // synchronises: the host vector st may go
   ctx->stats[7] = ms;
+  if (!L.plan_key.empty()) {
+    float f = 0.f;  // the plan, from its first kernel to the end of the call
+    GG_CUDA(cudaEventElapsedTime(&f, ctx->ev_mid, ctx->ev1));
+    ctx->stats[29] = f;
+  }
   return GG_OK;
 }
 

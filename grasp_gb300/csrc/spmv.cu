@@ -341,6 +341,7 @@ __global__ void __launch_bounds__(512) k_spmm_split(const int64_t *__restrict__ 
                                                     const float2 *__restrict__ xb, const double *__restrict__ diag,
                                                     const double *__restrict__ Bbase, double *__restrict__ ABbase,
                                                     int64_t ld, const int *__restrict__ pc, int n) {
+  pdl_wait();
   constexpr int MP = spmm_pitch(M), LPE = (M + 1) / 2, EPW = 32 / LPE;
   const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (row >= n) return;
@@ -457,12 +458,14 @@ void launch_spmm_mu(const gg_hmat *h, int tpb, const float2 *xb, const double *B
                     const int *dcol, cudaStream_t s) {
   const int n = h->ncf;
   const unsigned blocks = (unsigned)(((int64_t)n * 32 + tpb - 1) / tpb);
+  // a programmatic launch: inside the Davidson block pass it may be
+  // scheduled while the pass's previous kernel finishes
   if (h->sym_col16)
-    k_spmm_split<M, unsigned short, U><<<blocks, tpb, 0, s>>>(h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p, h->dSymLo.p,
-                                                              xb, h->dDiag.p, Bbase, ABbase, ld, dcol, n);
+    launch_pdl(k_spmm_split<M, unsigned short, U>, blocks, tpb, 0, s, h->dSymPtr.p, h->dSymCol16.p, h->dSymHi.p,
+               h->dSymLo.p, xb, h->dDiag.p, Bbase, ABbase, ld, dcol, n);
   else
-    k_spmm_split<M, int32_t, U><<<blocks, tpb, 0, s>>>(h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p, xb,
-                                                       h->dDiag.p, Bbase, ABbase, ld, dcol, n);
+    launch_pdl(k_spmm_split<M, int32_t, U>, blocks, tpb, 0, s, h->dSymPtr.p, h->dSymCol.p, h->dSymHi.p, h->dSymLo.p,
+               xb, h->dDiag.p, Bbase, ABbase, ld, dcol, n);
 }
 template <int M>
 void launch_spmm_m(const gg_hmat *h, int variant, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,

@@ -263,7 +263,11 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * solve's total ms), 23 / 24 device ms / number of the full-block block
  * matvecs (split SpMM) over MBLOCK columns of the last gg_maneig, 25 the
  * number of grid-point ranges (split-K) of the last tensor-core
- * gg_genintrk's contraction tiles.                                        */
+ * gg_genintrk's contraction tiles, 26 / 27 host ms of the last gg_maneig's
+ * structure set-up (symmetric matvec structures of the block and of its
+ * leading block) / Davidson workspaces, 28 device ms from the start of that
+ * gg_maneig to the end of its structure set-up, 29 device ms of the
+ * assembly plan built by the last gg_setham_upload (0 when it built none).
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors
