@@ -717,7 +717,8 @@ __device__ __forceinline__ double bd_reduce(const float2 *__restrict__ part, int
 }
 
 // MODE 0: Gram-Schmidt coefficients C = X^T W (kpass x m, row a at a m);
-// MODE 2: the new columns of S into dS (packed upper, S(i, j) at j (j+1)/2 + i).
+// MODE 2: the new columns of S into dS (packed upper, S(i, j) at
+// j (j+1)/2 + i - kpass (kpass+1)/2: the columns from kpass on).
 // 32 outputs per CTA. P: the partials' type (double, or float2 double-float
 // sums of the split kernels). set_bst: block 0 also starts the pass's
 // column counts (bst = {m, m}), read first by the Gram dots after it.
@@ -744,7 +745,7 @@ __global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict
     C[o] = sum;
   } else {
     const int a = o / nb, j = kpass + o % nb;
-    if (a <= j) dS[(size_t)j * (j + 1) / 2 + a] = sum;
+    if (a <= j) dS[(size_t)j * (j + 1) / 2 + a - (size_t)kpass * (kpass + 1) / 2] = sum;
   }
 }
 
@@ -1307,7 +1308,6 @@ struct Dvd {
   // block pass (MBLOCK > 1): new columns c_v = KPASS + v, v < m, each
   // Gram-Schmidt -> OP -> ADDS, as one graph per m; parameters in dpv[v]
   DBuf<IterParams> dpv;
-  IterParams *hpv = nullptr;      // pinned
   // block Gram-Schmidt: CTA partials (bd_G CTAs, pitch bd_ps), coefficients,
   // matvec skip flags, [kept, before] counts, split copies of the new columns
   DBuf<double> bpart, bC, bskip;
@@ -1337,7 +1337,30 @@ struct Dvd {
     bx_cols = k;
     return GG_OK;
   }
-  int *hbst = nullptr;            // pinned copy of bst
+  // One block pass moves its inputs in one host-to-device copy and its
+  // results in one device-to-host copy:
+  //   in:  NvIn | IterParams[MT_MAX] | Ritz coefficients [MT_MAX][lim]
+  //   out: NvOut | kept/before counts | the new S columns, packed upper
+  //        from offset kpass (kpass + 1) / 2
+  DBuf<char> dio_in, dio_out;
+  char *hio_in = nullptr, *hio_out = nullptr;  // pinned mirrors
+  size_t io_in_bytes = 0, io_out_bytes = 0, io_pv = 0, io_coef = 0, io_bst = 0, io_scol = 0;
+  void io_layout() {
+    auto a16 = [](size_t b) { return (b + 15) / 16 * 16; };
+    io_pv = a16(sizeof(NvIn));
+    io_coef = io_pv + a16(MT_MAX * sizeof(IterParams));
+    io_in_bytes = io_coef + (size_t)MT_MAX * lim * sizeof(double);
+    io_bst = a16(sizeof(NvOut));
+    io_scol = io_bst + 16;
+    io_out_bytes = io_scol + (size_t)MT_MAX * (lim + MT_MAX) * sizeof(double);
+  }
+  NvIn *din_nv() { return reinterpret_cast<NvIn *>(dio_in.p); }
+  double *din_coef() { return reinterpret_cast<double *>(dio_in.p + io_coef); }
+  NvOut *dout_nv() { return reinterpret_cast<NvOut *>(dio_out.p); }
+  double *dout_scol() { return reinterpret_cast<double *>(dio_out.p + io_scol); }
+  NvOut *hout_nv() { return reinterpret_cast<NvOut *>(hio_out); }
+  const int *hout_bst() { return reinterpret_cast<const int *>(hio_out + io_bst); }
+  const double *hout_scol() { return reinterpret_cast<const double *>(hio_out + io_scol); }
   std::vector<cudaGraphExec_t> bexec;
   std::vector<int> bkernels;
   std::vector<int> buses;         // block passes run per width
@@ -1382,10 +1405,10 @@ struct Dvd {
       const size_t bS = al((size_t)lim * (lim + 1) / 2 * sizeof(double));
       const size_t bmt = al(((size_t)MT_MAX * lim + 2 * MT_MAX) * sizeof(double));
       const size_t bup = al((size_t)(8 + lim) * sizeof(double)), bdown = al((size_t)(lim + 8 + SC_N) * sizeof(double));
-      const size_t bpv = al(MT_MAX * sizeof(IterParams)), bbst = al(2 * sizeof(int));
-      const size_t bin = al(sizeof(NvIn)), bout = al(sizeof(NvOut));
+      io_layout();
+      const size_t bio = al(io_in_bytes) + al(io_out_bytes);
       char *a = nullptr;
-      GG_CUDA(cudaMallocHost(&a, bS + bmt + bup + bdown + bpv + bbst + bin + bout));
+      GG_CUDA(cudaMallocHost(&a, bS + bmt + bup + bdown + bio));
       note_alloc();
       pinned = a;
       hS = reinterpret_cast<double *>(a);
@@ -1396,14 +1419,12 @@ struct Dvd {
       a += bup;
       hdown = reinterpret_cast<double *>(a);
       a += bdown;
-      hpv = reinterpret_cast<IterParams *>(a);
-      a += bpv;
-      hbst = reinterpret_cast<int *>(a);
-      a += bbst;
-      hnv_in = reinterpret_cast<NvIn *>(a);
-      a += bin;
-      hnv_out = reinterpret_cast<NvOut *>(a);
+      hio_in = a;
+      a += al(io_in_bytes);
+      hio_out = a;
     }
+    GG_TRY(dio_in.alloc(io_in_bytes));
+    GG_TRY(dio_out.alloc(io_out_bytes));
     GG_TRY(small.alloc(4096));
     GG_TRY(dots.alloc(lim + 8 + SC_N));
     GG_TRY(dup.alloc(8 + lim));
@@ -1640,19 +1661,21 @@ struct Dvd {
     if (split) {
       GG_CUDA(launch_pdl(k_bdx_dots<2>, gd, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
                          bd_ps));
-      GG_CUDA(launch_pdl(k_bd_reduce<2, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p, 0));
+      GG_CUDA(launch_pdl(k_bd_reduce<2, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p,
+                         dout_scol(), 0));
     } else {
       GG_CUDA(launch_pdl(k_bd_dots<2>, gd, BD_T, 0, s, B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps));
-      GG_CUDA(launch_pdl(k_bd_reduce<2, double>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, 0));
+      GG_CUDA(launch_pdl(k_bd_reduce<2, double>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p,
+                         dout_scol(), 0));
     }
     note_launches(2);
-    GG_CUDA(cudaMemcpyAsync(hbst, bst.p, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
     GG_CUDA(cudaGetLastError());
     return GG_OK;
   }
   // the block pass for columns kpass .. kpass+m-1: one graph launch, one copy
   // of the new S columns back
-  int block_pass(int kpass, int m, std::vector<double> &S, int *nkept) {
+  // staged: the caller copied the pass's IterParams with its inputs
+  int block_pass(int kpass, int m, std::vector<double> &S, int *nkept, bool staged = false) {
     *nkept = 0;
     if (m <= 0) return GG_OK;
     if (m > MT_MAX) return fail(GG_ERR_ARG, "block pass: more new vectors than supported");
@@ -1661,7 +1684,9 @@ struct Dvd {
       for (auto &e : bev) GG_CUDA(cudaEventCreate(&e));
     }
     if (!dpv.p) {
-      GG_TRY(dpv.alloc(MT_MAX));
+      dpv.p = reinterpret_cast<IterParams *>(dio_in.p + io_pv);
+      dpv.n = MT_MAX;
+      dpv.own = false;
 
       bexec.assign(MT_MAX + 1, nullptr);
       bkernels.assign(MT_MAX + 1, 0);
@@ -1680,16 +1705,21 @@ struct Dvd {
       GG_TRY(bpart.alloc((size_t)bd_G * bd_ps));
       GG_TRY(bC.alloc((size_t)std::max(lim * MT_MAX, MT_MAX * MT_MAX)));
       GG_TRY(bskip.alloc(MT_MAX));
-      GG_TRY(bst.alloc(2));
+      bst.p = reinterpret_cast<int *>(dio_out.p + io_bst);
+      bst.n = 2;
+      bst.own = false;
 
       if (precision == GG_SPLIT) GG_TRY(bxs.alloc((size_t)MT_MAX * ld));
     }
     GG_TRY(sync_split(kpass));
-    for (int v = 0; v < m; ++v) {
-      hpv[v] = IterParams{};
-      hpv[v].c = kpass + v;
+    if (!staged) {
+      IterParams *hp = reinterpret_cast<IterParams *>(hio_in + io_pv);
+      for (int v = 0; v < m; ++v) {
+        hp[v] = IterParams{};
+        hp[v].c = kpass + v;
+      }
+      GG_CUDA(cudaMemcpyAsync(dpv.p, hp, m * sizeof(IterParams), cudaMemcpyHostToDevice, s));
     }
-    GG_CUDA(cudaMemcpyAsync(dpv.p, hpv, m * sizeof(IterParams), cudaMemcpyHostToDevice, s));
     // a graph per batch size m, captured at the first pass of the full width
     // or the second pass of another width (a width used once is launched
     // kernel by kernel: cheaper than capturing it)
@@ -1718,14 +1748,15 @@ struct Dvd {
     } else {
       GG_TRY(enqueue_block(m, false));
     }
+    // NEWVEC's results, the column counts and the new S columns in one copy
     const size_t o0 = (size_t)kpass * (kpass + 1) / 2, o1 = (size_t)(kpass + m) * (kpass + m + 1) / 2;
-    GG_CUDA(cudaMemcpyAsync(hS + o0, dS.p + o0, (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    GG_CUDA(cudaMemcpyAsync(hio_out, dio_out.p, io_scol + (o1 - o0) * sizeof(double), cudaMemcpyDeviceToHost, s));
     const auto t0 = std::chrono::steady_clock::now();
     GG_CUDA(cudaStreamSynchronize(s));
     t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    const int nk = hbst[0];
+    const int nk = hout_bst()[0];
     if (nk < 0 || nk > m) return fail(GG_ERR_STATE, "block pass: kept column count out of range");
-    std::memcpy(S.data() + o0, hS + o0, (o1 - o0) * sizeof(double));
+    std::memcpy(S.data() + o0, hout_scol(), (o1 - o0) * sizeof(double));
     for (int v = 0; v < (use_x() ? 1 : m); ++v) {
       float ms = 0.f;
       GG_CUDA(cudaEventElapsedTime(&ms, bev[2 * v], bev[2 * v + 1]));
@@ -1903,20 +1934,27 @@ struct Dvd {
     return GG_OK;
   }
   // the Ritz sweep (residual norms |r_t|^2 left on the device)
-  int launch_ritz_multi(int k, int nt, const double *const *svec, const double *lam) {
-    for (int t = 0; t < nt; ++t) std::memcpy(hmt + (size_t)t * k, svec[t], k * sizeof(double));
-    double *hl = hmt + (size_t)MT_MAX * lim;
-    for (int t = 0; t < nt; ++t) hl[t] = lam[t];
-    GG_CUDA(cudaMemcpyAsync(dmt.p, hmt, (size_t)nt * k * sizeof(double), cudaMemcpyHostToDevice, s));
-    GG_CUDA(cudaMemcpyAsync(dmt.p + (size_t)MT_MAX * lim, hl, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+  // staged: the coefficients and eigenvalues are already in the pass's
+  // input region (din_coef, din_nv()->lam)
+  int launch_ritz_multi(int k, int nt, const double *const *svec, const double *lam, bool staged = false) {
+    const double *dcoef = dmt.p, *dl = dmt.p + (size_t)MT_MAX * lim;
+    if (staged) {
+      dcoef = din_coef();
+      dl = din_nv()->lam;
+    } else {
+      for (int t = 0; t < nt; ++t) std::memcpy(hmt + (size_t)t * k, svec[t], k * sizeof(double));
+      double *hl = hmt + (size_t)MT_MAX * lim;
+      for (int t = 0; t < nt; ++t) hl[t] = lam[t];
+      GG_CUDA(cudaMemcpyAsync(dmt.p, hmt, (size_t)nt * k * sizeof(double), cudaMemcpyHostToDevice, s));
+      GG_CUDA(cudaMemcpyAsync(dmt.p + (size_t)MT_MAX * lim, hl, nt * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
     double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
     // one group of all targets, or (small blocks) one target per grid row
     const bool per_target = (int64_t)nrow * 2 < ctx->sms;
-    const double *dl = dmt.p + (size_t)MT_MAX * lim;
     if (use_x()) {
       GG_TRY(sync_split(k));
       if (per_target) {
-        GG_CUDA(launch_pdl(k_ritzx_multi<1, SP>, dim3(nrow4, nt), RT, 0, s, Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p,
+        GG_CUDA(launch_pdl(k_ritzx_multi<1, SP>, dim3(nrow4, nt), RT, 0, s, Bx.p, ABx.p, ld, k, nt, dcoef, dl, T.p, n, part.p,
                                                        counters.p + 3, drn));
       } else {
         // an even nt as two grid rows of nt / 2 targets (twice the warps;
@@ -1925,7 +1963,7 @@ struct Dvd {
         const int half = (nt % 2 == 0) ? 2 : 1;
         switch (nt / half) {
 #define RM_CASE(K) \
-  case K: GG_CUDA(launch_pdl(k_ritzx_multi<K, 1>, dim3(nrow, half), RT, 0, s, Bx.p, ABx.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn)); break;
+  case K: GG_CUDA(launch_pdl(k_ritzx_multi<K, 1>, dim3(nrow, half), RT, 0, s, Bx.p, ABx.p, ld, k, nt, dcoef, dl, T.p, n, part.p, counters.p + 3, drn)); break;
           RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
           RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
 #undef RM_CASE
@@ -1933,12 +1971,12 @@ struct Dvd {
         }
       }
     } else if (per_target) {
-      GG_CUDA(launch_pdl(k_ritz_multi<1>, dim3(nrow, nt), RT, 0, s, B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3,
+      GG_CUDA(launch_pdl(k_ritz_multi<1>, dim3(nrow, nt), RT, 0, s, B.p, AB.p, ld, k, nt, dcoef, dl, T.p, n, part.p, counters.p + 3,
                                                     drn));
     } else {
       switch (nt) {
 #define RM_CASE(K) \
-  case K: GG_CUDA(launch_pdl(k_ritz_multi<K>, nrow, RT, 0, s, B.p, AB.p, ld, k, nt, dmt.p, dl, T.p, n, part.p, counters.p + 3, drn)); break;
+  case K: GG_CUDA(launch_pdl(k_ritz_multi<K>, nrow, RT, 0, s, B.p, AB.p, ld, k, nt, dcoef, dl, T.p, n, part.p, counters.p + 3, drn)); break;
         RM_CASE(1) RM_CASE(2) RM_CASE(3) RM_CASE(4) RM_CASE(5) RM_CASE(6) RM_CASE(7) RM_CASE(8)
         RM_CASE(9) RM_CASE(10) RM_CASE(11) RM_CASE(12) RM_CASE(13) RM_CASE(14) RM_CASE(15) RM_CASE(16)
 #undef RM_CASE
@@ -1954,30 +1992,31 @@ struct Dvd {
   // of the mg columns zeroed), the block pass graph over mg columns. One
   // host wait, at the end. *nk = columns added, *done = all candidates
   // converged (nothing added).
-  DBuf<NvIn> dnv_in;
-  DBuf<NvOut> dnv_out;
   DBuf<PrecList> dL;
-  NvIn *hnv_in = nullptr;
-  NvOut *hnv_out = nullptr;
   int pass_fused(int k, int nt, const double *const *svec, const NvIn &in, int mg, std::vector<double> &S, int *nk,
                  bool *done) {
-    if (!dnv_in.p) {
-      GG_TRY(dnv_in.alloc(1));
-      GG_TRY(dnv_out.alloc(1));
-      GG_TRY(dL.alloc(1));
+    if (!dL.p) GG_TRY(dL.alloc(1));
+    if (mg > MT_MAX || nt > MT_MAX) return fail(GG_ERR_ARG, "block pass: more targets than supported");
+    // the pass's inputs in one copy: NEWVEC's, the block pass's columns, the
+    // Ritz coefficients
+    *reinterpret_cast<NvIn *>(hio_in) = in;
+    IterParams *hp = reinterpret_cast<IterParams *>(hio_in + io_pv);
+    for (int v = 0; v < mg; ++v) {
+      hp[v] = IterParams{};
+      hp[v].c = k + v;
     }
-    *hnv_in = in;
-    GG_CUDA(cudaMemcpyAsync(dnv_in.p, hnv_in, sizeof(NvIn), cudaMemcpyHostToDevice, s));
-    GG_TRY(launch_ritz_multi(k, nt, svec, in.lam));
+    double *hc = reinterpret_cast<double *>(hio_in + io_coef);
+    for (int t = 0; t < nt; ++t) std::memcpy(hc + (size_t)t * k, svec[t], k * sizeof(double));
+    GG_CUDA(cudaMemcpyAsync(dio_in.p, hio_in, io_coef + (size_t)nt * k * sizeof(double), cudaMemcpyHostToDevice, s));
+    GG_TRY(launch_ritz_multi(k, nt, svec, in.lam, true));
     const double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
-    GG_CUDA(launch_pdl(k_newvec, 1, 32, 0, s, dnv_in.p, drn, dL.p, dnv_out.p));
+    GG_CUDA(launch_pdl(k_newvec, 1, 32, 0, s, din_nv(), drn, dL.p, dout_nv()));
     GG_CUDA(launch_pdl(k_precond_dev, (n + TPB - 1) / TPB, TPB, 0, s, B.p, T.p, ld, dL.p, diag.p, n, mg, k));
     note_launches(2);
     GG_CUDA(cudaGetLastError());
-    GG_CUDA(cudaMemcpyAsync(hnv_out, dnv_out.p, sizeof(NvOut), cudaMemcpyDeviceToHost, s));
-    GG_TRY(block_pass(k, mg, S, nk));  // waits for the stream
-    *done = hnv_out->done != 0;
-    if (*nk > hnv_out->nadded) return fail(GG_ERR_STATE, "block pass: more columns kept than added");
+    GG_TRY(block_pass(k, mg, S, nk, true));  // copies NEWVEC's results with its own, waits for the stream
+    *done = hout_nv()->done != 0;
+    if (*nk > hout_nv()->nadded) return fail(GG_ERR_STATE, "block pass: more columns kept than added");
     return GG_OK;
   }
   int precond_multi(const PrecList &L) {
