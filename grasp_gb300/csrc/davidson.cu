@@ -815,23 +815,53 @@ __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst
     if (last && tid < m) skipf[tid] = (tid < nb) ? 0.0 : 1.0;
     return;
   }
-  // the factorisation by warp 0 alone: its steps then need warp syncs only
+  // The factorisation by warp 0 alone: its steps then need warp syncs only.
+  // GB300 issues an FP64 warp instruction in about as many cycles as FP32
+  // issues 70, so the serial chain is kept short: G16 holds G with a fixed
+  // row pitch of 16 (no division by nb), only the lower triangle of the
+  // Schur complement is updated, its entries listed with their column
+  // descending so that step q updates a prefix of the list (ceil(T_q / 32)
+  // instructions, T_q = (nb - q - 1)(nb - q) / 2), and 1/sqrt(pivot) is an
+  // FP32 estimate refined by two Newton steps.
   if (tid >= 32) return;
-  if (lane < nb) {
-    g0[lane] = G[lane * nb + lane];
-    pos[lane] = -1;
+  double *G16 = Ri;  // R^-1 is formed after the factorisation; until then its storage holds G
+  __shared__ unsigned char pa[MT_MAX * (MT_MAX + 1) / 2], pb[MT_MAX * (MT_MAX + 1) / 2];
+  for (int e = lane; e < MT_MAX * MT_MAX; e += 32) {
+    const int r = e >> 4, c = e & 15;
+    G16[e] = (r < nb && c < nb) ? G[r * nb + c] : 0.0;
   }
+  if (lane == 0) {
+    int e = 0;
+    for (int c = nb - 1; c >= 0; --c)
+      for (int r = c; r < nb; ++r) {
+        pa[e] = (unsigned char)r;
+        pb[e] = (unsigned char)c;
+        ++e;
+      }
+  }
+  if (lane < nb) pos[lane] = -1;
+  __syncwarp();
+  if (lane < nb) g0[lane] = G16[lane * 17];
   __syncwarp();
   int nk = 0;  // uniform
   for (int q = 0; q < nb; ++q) {
-    const double dq = G[q * nb + q];
+    const double dq = G16[q * 17];
     if (dq > 1e-14 * g0[q] && dq > 1e-300) {
-      const double inv = rsqrt(dq), rd = dq * inv;
-      if (lane < nb) R[nk * MT_MAX + lane] = (lane < q) ? 0.0 : (lane == q ? rd : G[q * nb + lane] * inv);
+      double inv;
+      if (dq > 1e-36 && dq < 1e36) {
+        double y = (double)rsqrtf((float)dq);
+        y = y * fma(-0.5 * dq * y, y, 1.5);
+        inv = y * fma(-0.5 * dq * y, y, 1.5);
+      } else {
+        inv = rsqrt(dq);
+      }
+      const double rd = dq * inv;
+      if (lane < nb) R[nk * MT_MAX + lane] = (lane < q) ? 0.0 : (lane == q ? rd : G16[lane * 16 + q] * inv);
       __syncwarp();
-      for (int e = lane; e < nb * nb; e += 32) {
-        const int a = e / nb, b = e % nb;
-        if (a > q && b > q) G[e] -= R[nk * MT_MAX + a] * R[nk * MT_MAX + b];
+      const int tq = (nb - q - 1) * (nb - q) / 2;
+      for (int e = lane; e < tq; e += 32) {
+        const int r = pa[e], c = pb[e];
+        G16[r * 16 + c] -= R[nk * MT_MAX + r] * R[nk * MT_MAX + c];
       }
       if (lane == 0) {
         keep[nk] = q;
@@ -842,6 +872,7 @@ __global__ void __launch_bounds__(BD_RED) k_bd_chol(int m, int *__restrict__ bst
     }
     __syncwarp();
   }
+  __syncwarp();
   // column c of R_kk^-1, R_kk(i, j) = R[i][keep[j]]
   if (lane < nk) {
     const int c = lane;
