@@ -458,12 +458,15 @@ def solve_e2e(w, precision, device, arrays, mblock=0):
     ctx.iabint_table()
     H = HMatrix(ctx, b.ncf, b.iendc, b.irow)
     H.setham(b.iq, b.tlist, b.vlists)
+    parts = {"genintrk_ms": ctx.stage_stat(0), "iabint_ms": ctx.stage_stat(1),
+             "setham_upload_and_assemble_ms": ctx.stage_stat(7), "setham_plan_ms": ctx.stage_stat(29)}
     ev, vec, info = H.maneig(w.nroots, flavour=0, precision=precision, mblock=mblock)
     t1 = time.perf_counter()
+    parts.update(maneig_ms=ctx.stage_stat(3), maneig_structure_setup_ms=ctx.stage_stat(28))
     H.close()
     ctx.close()
     del np
-    return t1 - t0, ev
+    return t1 - t0, ev, parts
 
 
 def run_ours(a):
@@ -518,9 +521,11 @@ def run_ours(a):
     clk = clocks.stop()
     _barrier(pg)
     t_split = _max_over_ranks(pg, statistics.median(times))
+    # (the resident matrix's list upload was a first, unpinned call: the
+    # pinned upload is in e2e_parts)
     stage = {k: ctx.stage_stat(i) for i, k in enumerate(
         ["genintrk_ms", "iabint_ms", "setham_assemble_ms", "maneig_ms", "matvec_ms", "matvec_launches",
-         "matvec_alg_bytes", "setham_upload_ms", "loops_block2000", "loops_full"])}
+         "matvec_alg_bytes", None, "loops_block2000", "loops_full"]) if k}
     times64, times_ref = [], []
     for _ in range(max(1, a.steps // 2)):
         t, _, _, _ = solve_resident(ctx, H, w.nroots, FP64, mb)
@@ -559,13 +564,14 @@ def run_ours(a):
         arrays += [v["lab"], v["start"], v["loc"], v["coeff"]]
     h2d = int(sum(x.nbytes for x in arrays) + w.zz.nbytes + w.orb.nak.nbytes + w.orb.mf.nbytes)
     d2h = int(w.nroots * (b.ncf + 1) * 8)
-    e2e_times = []
+    e2e_times, e2e_parts = [], []
     if a.e2e_steps > 0:
         with pinned(*arrays):
             solve_e2e(w, SPLIT, local, arrays, mb)  # warm
             for _ in range(a.e2e_steps):
-                t, ev_e = solve_e2e(w, SPLIT, local, arrays, mb)
+                t, ev_e, parts = solve_e2e(w, SPLIT, local, arrays, mb)
                 e2e_times.append(t)
+                e2e_parts.append(parts)
     t_e2e = _max_over_ranks(pg, statistics.median(e2e_times)) if e2e_times else None
     batched = batched_leg(local, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
     rk = rk_leg(local) if not a.no_extra else None
@@ -606,6 +612,9 @@ def run_ours(a):
         "autotune": tuning,
         "stages": stage,
         "e2e": {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        # device ms of the e2e step's stages (medians; the SETHAM upload
+        # includes its plan, the first solve on a new matrix its structures)
+        "e2e_parts": ({k: statistics.median(p[k] for p in e2e_parts) for k in e2e_parts[0]} if e2e_parts else None),
         "gpu_launches": int(l1 - l0),
         "gpu_launches_per_step": int(l1 - l0) // max(1, a.steps),
         "clocks": clk,

@@ -236,6 +236,16 @@ int gg_set_grid(gg_ctx *ctx, int n, double rnt, double h, double c, const double
     }
   GG_TRY(g.dPow.alloc(pw.size()));
   GG_CUDA(cudaMemcpy(g.dPow.p, pw.data(), pw.size() * 8, cudaMemcpyHostToDevice));
+  {
+    std::vector<double> hd((size_t)3 * g.np, 0.0);
+    for (int i = 2; i + 1 < g.np && i + 1 <= n + 9; ++i) {
+      hd[i] = 1.0 / std::log(g.R[i + 1] / g.R[i]);
+      hd[(size_t)g.np + i] = g.RP[i] / g.RP[i + 1];
+      hd[(size_t)2 * g.np + i] = g.R[i] / g.RP[i];
+    }
+    GG_TRY(g.dHead.alloc(hd.size()));
+    GG_CUDA(cudaMemcpy(g.dHead.p, hd.data(), hd.size() * 8, cudaMemcpyHostToDevice));
+  }
   // a new grid invalidates everything computed on the old one
   ctx->rk.valid = false;
   ctx->iab_valid = false;

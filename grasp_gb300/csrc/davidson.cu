@@ -465,44 +465,6 @@ struct NvOut {
   int nadded, done;
   double res[MT_MAX];
 };
-__global__ void k_newvec(const NvIn *__restrict__ in, const double *__restrict__ rn2, PrecList *__restrict__ L,
-                         NvOut *__restrict__ out) {
-  pdl_wait();
-  // the square roots in parallel (lane t), the choices by lane 0 in order
-  __shared__ double sres[MT_MAX], srhs[MT_MAX];
-  const int nt = in->nt, t = threadIdx.x;
-  if (t < nt) {
-    const double res = sqrt(rn2[t]), gap = in->gap[t], dl = in->dl[t];
-    sres[t] = res;
-    out->res[t] = res;
-    srhs[t] = (gap > res) ? sqrt(dl * res) : fmin(dl, sqrt(dl));
-  }
-  __syncthreads();
-  if (t != 0) return;
-  PrecList l;
-  l.m = 0;
-  int icvc = 0, nadded = 0, done = 0;
-  for (int i = 0; i < nt; ++i) {
-    const double res = sres[i];
-    if (res < in->critr) {
-      ++icvc;
-      if (icvc < nt) continue;
-      done = 1;
-      break;
-    }
-    ++nadded;
-    l.col[l.m] = in->kpass + nadded - 1;
-    l.t[l.m] = i;
-    l.lam[l.m] = in->lam[i];
-    l.rhs[l.m] = srhs[i];
-    ++l.m;
-    if (nadded + in->kpass == in->limadd) break;
-  }
-  *L = l;
-  out->nadded = nadded;
-  out->done = done;
-}
-
 // a / b to about 2^-46 relative: an FP32 reciprocal of b refined by one
 // Newton step on the quotient (three FP64 operations instead of the FP64
 // division's longer sequence; |b| > 1e-6 here, far inside FP32's range
@@ -513,23 +475,65 @@ __device__ __forceinline__ double quot(double a, double b) {
   return fma(fma(-b, q0, a), y, q0);
 }
 
-// k_precond_multi with the kept targets read from device memory; columns
-// kpass + L.m .. kpass + mg - 1 of the pass are zeroed (the block pass then
-// drops them)
-__global__ void k_precond_dev(double *__restrict__ B, const double *__restrict__ T, int64_t ld,
-                              const PrecList *__restrict__ Lp, double *__restrict__ diag, int n, int mg, int kpass) {
+// NEWVEC's choices and the preconditioners of the kept targets in one
+// kernel: every CTA makes the choices (the square roots in parallel, lane t;
+// the choices by thread 0 in TSTSEL's order), block 0 also writes them for
+// the host; then each thread preconditions its row for the kept targets in
+// NEWVEC's order (GDVD, gdvd.f90:114-129, DIAG updated after each as in the
+// reference) and zeroes columns kpass + L.m .. kpass + mg - 1 of the pass
+// (the block pass then drops them)
+__global__ void k_newvec_precond(const NvIn *__restrict__ in, const double *__restrict__ rn2,
+                                 NvOut *__restrict__ out, double *__restrict__ B, const double *__restrict__ T,
+                                 int64_t ld, double *__restrict__ diag, int n, int mg, int kpass) {
   pdl_wait();
+  __shared__ double sres[MT_MAX], srhs[MT_MAX];
+  __shared__ PrecList L;
+  const int nt = in->nt, t = threadIdx.x;
+  if (t < nt) {
+    const double res = sqrt(rn2[t]), gap = in->gap[t], dl = in->dl[t];
+    sres[t] = res;
+    if (blockIdx.x == 0) out->res[t] = res;
+    srhs[t] = (gap > res) ? sqrt(dl * res) : fmin(dl, sqrt(dl));
+  }
+  __syncthreads();
+  if (t == 0) {
+    PrecList l;
+    l.m = 0;
+    int icvc = 0, nadded = 0, done = 0;
+    for (int i = 0; i < nt; ++i) {
+      const double res = sres[i];
+      if (res < in->critr) {
+        ++icvc;
+        if (icvc < nt) continue;
+        done = 1;
+        break;
+      }
+      ++nadded;
+      l.col[l.m] = in->kpass + nadded - 1;
+      l.t[l.m] = i;
+      l.lam[l.m] = in->lam[i];
+      l.rhs[l.m] = srhs[i];
+      ++l.m;
+      if (nadded + in->kpass == in->limadd) break;
+    }
+    L = l;
+    if (blockIdx.x == 0) {
+      out->nadded = nadded;
+      out->done = done;
+    }
+  }
+  __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int m = Lp->m;
+  const int m = L.m;
   double dg = diag[i];
   for (int q = 0; q < m; ++q) {
-    const int t = Lp->t[q];
-    const double b = T[(size_t)(2 * t) * ld + i], r = T[(size_t)(2 * t + 1) * ld + i];
-    const double rr = fma(-Lp->rhs[q], b, r);
-    const double lam = Lp->lam[q];
+    const int tq = L.t[q];
+    const double b = T[(size_t)(2 * tq) * ld + i], r = T[(size_t)(2 * tq + 1) * ld + i];
+    const double rr = fma(-L.rhs[q], b, r);
+    const double lam = L.lam[q];
     const double d = dg - lam;
-    B[(size_t)Lp->col[q] * ld + i] = (fabs(d) > 1.0e-06) ? quot(rr, d) : rr * 1.0e06;
+    B[(size_t)L.col[q] * ld + i] = (fabs(d) > 1.0e-06) ? quot(rr, d) : rr * 1.0e06;
     dg = d + lam;
   }
   diag[i] = dg;
@@ -1082,8 +1086,10 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
   const double *Wb = ((MODE == 2) ? AB : B) + (size_t)kpass * ld;
   float2 *out = part + (size_t)blockIdx.x * ps;
   const int rbeg = blockIdx.x * cpc * BD_R, rend = min(n, rbeg + cpc * BD_R);
-  for (int ac = blockIdx.y * BD_AC; ac < na; ac += gridDim.y * BD_AC) {
-    const int nac = min(BD_AC, na - ac), np = nac * nb;
+  // columns per chunk: at most one output pair per thread
+  const int acl = min(BD_AC, max(1, BD_T / nb));
+  for (int ac = blockIdx.y * acl; ac < na; ac += gridDim.y * acl) {
+    const int nac = min(acl, na - ac), np = nac * nb;
     float sh[BD_PAIRS], sl[BD_PAIRS];
 #pragma unroll
     for (int k = 0; k < BD_PAIRS; ++k) sh[k] = sl[k] = 0.f;
@@ -1165,13 +1171,24 @@ __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const fl
       Cs[idx] = split2(C[(size_t)(a0 + idx / M) * m + q0 + idx % M]);
     __syncthreads();
     if (i < n) {
-#pragma unroll 4
-      for (int a = part; a < na; a += L) {
-        const float2 x = Bx[(size_t)(a0 + a) * ld + i];
+      // eight basis loads in flight, then their steps
+      for (int ab = part; ab < na; ab += 8 * L) {
+        float2 xv[8];
 #pragma unroll
-        for (int q = 0; q < M; ++q) {
-          const float2 c = Cs[a * M + q];
-          dot2_step(sh[q], sl[q], c.x, c.y, x.x, x.y);
+        for (int u = 0; u < 8; ++u) {
+          const int a = ab + u * L;
+          xv[u] = (a < na) ? Bx[(size_t)(a0 + a) * ld + i] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int a = ab + u * L;
+          if (a < na) {
+#pragma unroll
+            for (int q = 0; q < M; ++q) {
+              const float2 c = Cs[a * M + q];
+              dot2_step(sh[q], sl[q], c.x, c.y, xv[u].x, xv[u].y);
+            }
+          }
         }
       }
     }
@@ -1186,7 +1203,7 @@ __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const fl
 // k_ritz_multi in split form (Bx, ABx for the basis and its products); L
 // lanes per row as in k_bdx_sub, target t finished by lane t mod L
 template <int NT, int L>
-__global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ Bx, const float2 *__restrict__ ABx,
+__global__ void __launch_bounds__(RT, 8) k_ritzx_multi(const float2 *__restrict__ Bx, const float2 *__restrict__ ABx,
                                                     int64_t ld, int k, int nt, const double *__restrict__ S,
                                                     const double *__restrict__ lam, double *__restrict__ T, int n,
                                                     double *__restrict__ part, unsigned *__restrict__ counter,
@@ -1194,7 +1211,6 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
   pdl_wait();
   __shared__ float2 sv[MT_SMEM];
   __shared__ float2 slam[NT];
-  __shared__ double red[RT / 32];
   __shared__ float fred[RT / 32];
   __shared__ bool last;
   const int t0 = blockIdx.y * NT;
@@ -1251,12 +1267,13 @@ __global__ void __launch_bounds__(RT) k_ritzx_multi(const float2 *__restrict__ B
   if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x * gridDim.y - 1);
   __syncthreads();
   if (!last) return;
-  for (int t = 0; t < nt; ++t) {
-    double u = 0.0;
-    for (int q = threadIdx.x; q < (int)gridDim.x; q += RT) u += __ldcg(part + (size_t)t * gridDim.x + q);
-    u = block_sum<RT>(u, red);
-    if (threadIdx.x == 0) rn2[t] = u;
-    __syncthreads();
+  // the norms' block partials, one warp per target, summed in FP32
+  for (int t = threadIdx.x >> 5; t < nt; t += RT / 32) {
+    float u = 0.f;
+    for (int q = threadIdx.x & 31; q < (int)gridDim.x; q += 32) u += (float)__ldcg(part + (size_t)t * gridDim.x + q);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) u += __shfl_xor_sync(0xffffffffu, u, o);
+    if ((threadIdx.x & 31) == 0) rn2[t] = (double)u;
   }
   if (threadIdx.x == 0) *counter = 0u;
 }
@@ -1607,9 +1624,11 @@ struct Dvd {
     // the split kernels' CTA partials are double-float pairs in the same buffer
     float2 *bpx = reinterpret_cast<float2 *>(bpart.p);
     const dim3 gd(bd_G, bd_Y);
+    // split dots: chunks of max(1, BD_T / m) columns (one pair per thread)
+    const dim3 gdx(bd_G, (lim + std::min(BD_AC, std::max(1, BD_T / m)) - 1) / std::min(BD_AC, std::max(1, BD_T / m)));
     for (int round = 0; round < 2; ++round) {
       if (split) {
-        GG_CUDA(launch_pdl(k_bdx_dots<0>, gd, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
+        GG_CUDA(launch_pdl(k_bdx_dots<0>, gdx, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
                            bd_ps));
         GG_CUDA(launch_pdl(k_bd_reduce<0, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p,
                            round == 0));
@@ -1690,7 +1709,7 @@ struct Dvd {
       }
     }
     if (split) {
-      GG_CUDA(launch_pdl(k_bdx_dots<2>, gd, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
+      GG_CUDA(launch_pdl(k_bdx_dots<2>, gdx, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
                          bd_ps));
       GG_CUDA(launch_pdl(k_bd_reduce<2, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p,
                          dout_scol(), 0));
@@ -2019,14 +2038,12 @@ struct Dvd {
     return GG_OK;
   }
   // One block pass with NEWVEC's choices made on the device: Ritz sweep of
-  // the nt candidates, k_newvec, preconditioners of the kept ones (the rest
+  // the nt candidates, NEWVEC's choices with the preconditioners of the kept ones (the rest
   // of the mg columns zeroed), the block pass graph over mg columns. One
   // host wait, at the end. *nk = columns added, *done = all candidates
   // converged (nothing added).
-  DBuf<PrecList> dL;
   int pass_fused(int k, int nt, const double *const *svec, const NvIn &in, int mg, std::vector<double> &S, int *nk,
                  bool *done) {
-    if (!dL.p) GG_TRY(dL.alloc(1));
     if (mg > MT_MAX || nt > MT_MAX) return fail(GG_ERR_ARG, "block pass: more targets than supported");
     // the pass's inputs in one copy: NEWVEC's, the block pass's columns, the
     // Ritz coefficients
@@ -2041,9 +2058,12 @@ struct Dvd {
     GG_CUDA(cudaMemcpyAsync(dio_in.p, hio_in, io_coef + (size_t)nt * k * sizeof(double), cudaMemcpyHostToDevice, s));
     GG_TRY(launch_ritz_multi(k, nt, svec, in.lam, true));
     const double *drn = dmt.p + (size_t)MT_MAX * lim + MT_MAX;
-    GG_CUDA(launch_pdl(k_newvec, 1, 32, 0, s, din_nv(), drn, dL.p, dout_nv()));
-    GG_CUDA(launch_pdl(k_precond_dev, (n + TPB - 1) / TPB, TPB, 0, s, B.p, T.p, ld, dL.p, diag.p, n, mg, k));
-    note_launches(2);
+    // small CTAs for small blocks: the preconditioner is FP64 work, spread
+    // over more SMs
+    const int tp = (n < 128 * ctx->sms) ? 64 : TPB;
+    GG_CUDA(launch_pdl(k_newvec_precond, (n + tp - 1) / tp, tp, 0, s, din_nv(), drn, dout_nv(), B.p, T.p, ld, diag.p,
+                       n, mg, k));
+    note_launch();
     GG_CUDA(cudaGetLastError());
     GG_TRY(block_pass(k, mg, S, nk, true));  // copies NEWVEC's results with its own, waits for the stream
     *done = hout_nv()->done != 0;

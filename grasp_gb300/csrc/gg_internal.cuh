@@ -125,6 +125,10 @@ struct Grid {
   QuadConst q{};
   DBuf<double> dR, dRP, dRPOR, dZZ;     // device, 1-based like the host copies
   DBuf<double> dPow;                    // [4][KLIMIT+1][np]: RTTK, RTTKM, RTTK1, RTTKM1 ; k = 0 row holds RM
+  // QUAD's power-law head term at point i (quad.f90:61-75) needs
+  // log(R(i+1)/R(i)), RP(i)/RP(i+1) and R(i)/RP(i): [3][np] per point
+  // (1 / the logarithm, the two ratios), 0 below i = 2
+  DBuf<double> dHead;
   int np = 0;                           // row pitch of dPow (>= n + GPAD)
 };
 

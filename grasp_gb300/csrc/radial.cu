@@ -4,7 +4,8 @@
 // Compiled with -fmad=false: every multiply and add below is rounded on its
 // own, as in the reference's FP64 loops, so that the Y^k functions and the
 // per-integral quadratures reproduce the reference's arithmetic step by
-// step. The R^k contraction uses explicit fma() and is not bit-exact.
+// step. The R^k contraction uses explicit fma() and QUAD's head term takes
+// the grid's factors per point from a table, so neither is bit-exact.
 //
 // Layout in HBM (all FP64):
 //   Y buffer   [nY][np]  Y^k_bd(r_i) at [f*np + i] (1-based i), zero beyond
@@ -231,8 +232,9 @@ __device__ __forceinline__ void rk_head_store(int k, int a, int c, int f, long l
                                               const double *__restrict__ PF, const double *__restrict__ QF, int ld,
                                               const int *__restrict__ MF, const double *__restrict__ R,
                                               const double *__restrict__ RP, const double *__restrict__ RPOR,
-                                              const QuadConst &q, double *__restrict__ val,
-                                              QuadItem *__restrict__ fb, int *__restrict__ nfb) {
+                                              const double *__restrict__ HD, const QuadConst &q,
+                                              double *__restrict__ val, QuadItem *__restrict__ fb,
+                                              int *__restrict__ nfb) {
   const YDesc y = yd[f];
   int mtp;
   if (k == 0 && y.b == y.d)
@@ -247,13 +249,14 @@ __device__ __forceinline__ void rk_head_store(int k, int a, int c, int f, long l
   double res = 0.0;
   if (ok) {
     const double tai = ta(2), taip1 = ta(3);
-    ok = !(fabs(tai) <= 0.0) && (taip1 / tai > 0.0);
+    const double t = taip1 / tai;
+    ok = !(fabs(tai) <= 0.0) && (t > 0.0);
     if (ok) {
-      const double frip1 = taip1 / RP[3];
-      double fri = tai / RP[2];
-      const double ratio = frip1 / fri;
-      const double sigma = log(ratio) / log(R[3] / R[2]);
-      fri = R[2] * fri;
+      // QUAD's head term with the grid's factors per point (HD): the ratio
+      // (TA(3)/RP(3)) / (TA(2)/RP(2)), sigma = log(ratio) / log(R(3)/R(2)),
+      // R(2) TA(2)/RP(2) / (sigma + 1); equal to quad.f90's to rounding
+      const double sigma = log(t * HD[np + 2]) * HD[2];
+      const double fri = tai * HD[2 * np + 2];
       res = fri / (sigma + 1.0) + sum;
       if ((mtp - 2) % 4 == 0) res = res - q.C1 * ta(mtp);
     }
@@ -273,16 +276,16 @@ __device__ __forceinline__ void rk_finish(const RkTile &T, int p, int idx_c, int
                                           const double *__restrict__ Y, int np, const double *__restrict__ PF,
                                           const double *__restrict__ QF, int ld, const int *__restrict__ MF,
                                           const double *__restrict__ R, const double *__restrict__ RP,
-                                          const double *__restrict__ RPOR, const QuadConst &q,
-                                          double *__restrict__ val, long long nval, QuadItem *__restrict__ fb,
-                                          int *__restrict__ nfb) {
+                                          const double *__restrict__ RPOR, const double *__restrict__ HD,
+                                          const QuadConst &q, double *__restrict__ val, long long nval,
+                                          QuadItem *__restrict__ fb, int *__restrict__ nfb) {
   const YDesc y = yd[f];
   const long long pos = T.base + (long long)T.ncA * (y.cs - T.cs_a) + (long long)idx_c * y.nd + (long long)(f - y.cs);
   if (pos < 0 || pos >= nval) {  // position outside the table: report, never write
     atomicExch(nfb + 1, 1);
     return;
   }
-  rk_head_store(T.k, T.a, pairs[p].y, f, pos, sum, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val, fb, nfb);
+  rk_head_store(T.k, T.a, pairs[p].y, f, pos, sum, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, HD, q, val, fb, nfb);
 }
 
 // ---------------------------------------------------------------------------
@@ -297,7 +300,8 @@ __global__ void __launch_bounds__(256) k_rk_gemm(const RkTile *__restrict__ tile
                                                  int np, const double *__restrict__ PF, const double *__restrict__ QF,
                                                  int ld, const int *__restrict__ MF, const double *__restrict__ R,
                                                  const double *__restrict__ RP, const double *__restrict__ RPOR,
-                                                 QuadConst q, double *__restrict__ val, long long nval,
+                                                 const double *__restrict__ HD, QuadConst q,
+                                                 double *__restrict__ val, long long nval,
                                                  QuadItem *__restrict__ fb, int *__restrict__ nfb) {
   __shared__ double As[2][KC_TILE][BM];
   __shared__ double Bs[2][KC_TILE][BN + 1];
@@ -354,8 +358,8 @@ __global__ void __launch_bounds__(256) k_rk_gemm(const RkTile *__restrict__ tile
     for (int v = 0; v < 4; ++v) {
       const int j = tx * 4 + v;
       if (j >= ncol) continue;
-      rk_finish(T, rowp[r], T.r0 + r, T.c0 + j, acc[u][v], pairs, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val,
-                nval, fb, nfb);
+      rk_finish(T, rowp[r], T.r0 + r, T.c0 + j, acc[u][v], pairs, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, HD, q,
+                val, nval, fb, nfb);
     }
   }
 }
@@ -749,9 +753,9 @@ __global__ void k_rk_finish_all(const int32_t *__restrict__ ind, long long n, co
                                 const double *__restrict__ Y, int np, const double *__restrict__ PF,
                                 const double *__restrict__ QF, int ld, const int *__restrict__ MF,
                                 const double *__restrict__ R, const double *__restrict__ RP,
-                                const double *__restrict__ RPOR, QuadConst q, double *__restrict__ val,
-                                QuadItem *__restrict__ fb, int *__restrict__ nfb, const double *__restrict__ parts,
-                                int nsplit) {
+                                const double *__restrict__ RPOR, const double *__restrict__ HD, QuadConst q,
+                                double *__restrict__ val, QuadItem *__restrict__ fb, int *__restrict__ nfb,
+                                const double *__restrict__ parts, int nsplit) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     int p = ind[i];
     const int d = p % KEY;
@@ -768,7 +772,7 @@ __global__ void k_rk_finish_all(const int32_t *__restrict__ ind, long long n, co
     }
     double gemm = parts[i];
     for (int t = 1; t < nsplit; ++t) gemm += parts[(long long)t * n + i];
-    rk_head_store(k, a, c, f, i, gemm, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, q, val, fb, nfb);
+    rk_head_store(k, a, c, f, i, gemm, yd, Y, np, PF, QF, ld, MF, R, RP, RPOR, HD, q, val, fb, nfb);
   }
 }
 
@@ -807,55 +811,67 @@ __global__ void k_quad_items(const QuadItem *__restrict__ items, const int *__re
 __global__ void k_quad_table(const QuadItem *__restrict__ items, const int *__restrict__ nitems_p, int nitems_max,
                              const double *__restrict__ Y, int np, const double *__restrict__ PF,
                              const double *__restrict__ QF, int ld, const double *__restrict__ R,
-                             const double *__restrict__ RP, const double *__restrict__ RPOR, QuadConst q,
-                             double *__restrict__ out) {
+                             const double *__restrict__ RP, const double *__restrict__ RPOR,
+                             const double *__restrict__ HD, QuadConst q, double *__restrict__ out) {
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   const int nitems = min(*nitems_p, nitems_max);
-  for (int it = blockIdx.x * wpb + (threadIdx.x >> 5); it < nitems; it += gridDim.x * wpb) {
-    const QuadItem w = items[it];
-    const int mtp = w.mtp;
-    const double *Yf = Y + (size_t)w.f * np;
+  // TA(i) of quad.f90 for item w, zero outside [2, MTP] (the pads TA(MTP+1..MTP+3))
+  auto ta = [&](const QuadItem &w, int i) -> double {
+    if (i < 2 || i > w.mtp) return 0.0;
     const double *Pa = PF + (size_t)(w.a - 1) * ld, *Pc = PF + (size_t)(w.c - 1) * ld;
     const double *Qa = QF + (size_t)(w.a - 1) * ld, *Qc = QF + (size_t)(w.c - 1) * ld;
-    // TA(i) of quad.f90, zero outside [2, MTP] (the pads TA(MTP+1..MTP+3))
-    auto ta = [&](int i) -> double {
-      if (i < 2 || i > mtp) return 0.0;
-      return ((Pa[i - 1] * Pc[i - 1] + Qa[i - 1] * Qc[i - 1]) * RPOR[i]) * Yf[i];
-    };
-    int head = -1;
-    for (int i0 = 2; i0 <= mtp - 1 && head < 0; i0 += 32) {
-      const int i = i0 + lane;
-      bool hit = false;
-      if (i <= mtp - 1) {
-        const double tai = ta(i);
-        hit = !(fabs(tai) <= 0.0) && (ta(i + 1) / tai > 0.0);
+    return ((Pa[i - 1] * Pc[i - 1] + Qa[i - 1] * Qc[i - 1]) * RPOR[i]) * Y[(size_t)w.f * np + i];
+  };
+  // One item per warp for the head index and the panel sum; the block's
+  // items then get their head terms (a logarithm and divisions: serial FP64
+  // work that would otherwise occupy a warp per item) from the lanes of
+  // warp 0, one item each
+  __shared__ int sh_head[32];
+  __shared__ double sh_s[32];
+  for (int base = blockIdx.x * wpb; base < nitems; base += gridDim.x * wpb) {
+    const int it = base + (threadIdx.x >> 5);
+    if (it < nitems) {
+      const QuadItem w = items[it];
+      int head = -1;
+      for (int i0 = 2; i0 <= w.mtp - 1 && head < 0; i0 += 32) {
+        const int i = i0 + lane;
+        bool hit = false;
+        if (i <= w.mtp - 1) {
+          const double tai = ta(w, i);
+          hit = !(fabs(tai) <= 0.0) && (ta(w, i + 1) / tai > 0.0);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, hit);
+        if (bal) head = i0 + __ffs(bal) - 1;
       }
-      const unsigned b = __ballot_sync(0xffffffffu, hit);
-      if (b) head = i0 + __ffs(b) - 1;
-    }
-    double s = 0.0;
-    if (head >= 0)
-      for (int j = head + 1 + 4 * lane; j <= mtp; j += 128)
-        s += q.C2 * (ta(j) + ta(j + 2)) + q.C3 * ta(j + 1) + q.C4 * ta(j + 3);
+      double sp = 0.0;
+      if (head >= 0)
+        for (int j = head + 1 + 4 * lane; j <= w.mtp; j += 128)
+          sp += q.C2 * (ta(w, j) + ta(w, j + 2)) + q.C3 * ta(w, j + 1) + q.C4 * ta(w, j + 3);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) {
+      for (int o = 16; o > 0; o >>= 1) sp += __shfl_xor_sync(0xffffffffu, sp, o);
+      if (lane == 0) {
+        sh_head[threadIdx.x >> 5] = head;
+        sh_s[threadIdx.x >> 5] = sp;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x < wpb && base + (int)threadIdx.x < nitems) {
+      const QuadItem w = items[base + threadIdx.x];
+      const int i = sh_head[threadIdx.x];
       double result = 0.0;
-      if (head >= 0) {
-        const int i = head, ip1 = i + 1;
-        const double tai = ta(i), taip1 = ta(ip1);
-        const double frip1 = taip1 / RP[ip1];
-        double fri = tai / RP[i];
-        const double sigma = log(frip1 / fri) / log(R[ip1] / R[i]);
-        fri = R[i] * fri;
-        result = fri / (sigma + 1.0);
+      if (i >= 0) {
+        // quad.f90:61-103 with the grid's factors per point (HD)
+        const double tai = ta(w, i), taip1 = ta(w, i + 1);
+        const double sigma = log((taip1 / tai) * HD[np + i]) * HD[i];
+        result = (tai * HD[2 * np + i]) / (sigma + 1.0);
         result = result + q.C1 * tai;
-        result = result + s;
-        if ((mtp - i) % 4 == 0) result = result - q.C1 * ta(mtp);
+        result = result + sh_s[threadIdx.x];
+        if ((w.mtp - i) % 4 == 0) result = result - q.C1 * ta(w, w.mtp);
       }
       out[w.pos] = result;
     }
+    __syncthreads();
   }
 }
 
@@ -1275,14 +1291,14 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
       const unsigned fb_blocks = (unsigned)std::min<long long>((N + 255) / 256, 8LL * ctx->sms);
       k_rk_finish_all<<<std::max(1u, fb_blocks), 256, 0, ctx->stream>>>(
           rk.dInd.p, (long long)N, C.dKst.p, kloop, KEY, C.dFidx.p, C.dYd.p, C.dY.p, np, o.dPF.p, o.dQF.p, o.ld,
-          o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p, C.dFb.p, C.dNfb.p, parts, nsplit);
+          o.dMF.p, g.dR.p, g.dRP.p, g.dRPOR.p, g.dHead.p, g.q, rk.dVal.p, C.dFb.p, C.dNfb.p, parts, nsplit);
       ::gg::note_launch();
     }
     GG_CUDA(cudaGetLastError());
   } else if (!tiles.empty()) {
     k_rk_gemm<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(C.dTiles.p, C.dRowpair.p, C.dPairs.p, C.dA.p, C.dY.p,
                                                               C.dYd.p, KC, np, o.dPF.p, o.dQF.p, o.ld, o.dMF.p,
-                                                              g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p,
+                                                              g.dR.p, g.dRP.p, g.dRPOR.p, g.dHead.p, g.q, rk.dVal.p,
                                                               (long long)N, C.dFb.p, C.dNfb.p);
     ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
@@ -1299,10 +1315,10 @@ int gg_genintrk(gg_ctx *ctx, int kmax, int precision, int64_t *n_out, int *j2max
   const int nfb = hfb[0];
   ctx->stats[20] = nfb;
   if (nfb > 0) {
-    const int wpb = 8;
-    const int blocks = std::min((nfb + wpb - 1) / wpb, 8 * ctx->sms);
+    const int wpb = 16;  // warps per block: an item each, their head terms by warp 0
+    const int blocks = std::min((nfb + wpb - 1) / wpb, 4 * ctx->sms);
     k_quad_table<<<blocks, 32 * wpb, 0, ctx->stream>>>(C.dFb.p, C.dNfb.p, nfb, C.dY.p, np, o.dPF.p, o.dQF.p, o.ld,
-                                                       g.dR.p, g.dRP.p, g.dRPOR.p, g.q, rk.dVal.p);
+                                                       g.dR.p, g.dRP.p, g.dRPOR.p, g.dHead.p, g.q, rk.dVal.p);
     ::gg::note_launch();
     GG_CUDA(cudaGetLastError());
   }
