@@ -230,7 +230,25 @@ def batched_leg(local, steps, cpu=True):
     t_first = time.perf_counter() - t0
     out = dict(w.describe())
     # the batched matvec variant the autotuner picked on this batch shape
-    out["autotune_batched_matvec"] = ctx.batched_tune()
+    tune = ctx.batched_tune()
+    out["autotune_batched_matvec"] = tune
+    # its roofline: the tuner timed every variant on the first start-up
+    # expansion, 16 new columns per block (MAXR; every block here has more
+    # than LIM = 66 CSFs or is solved in its full unit basis from 16 columns
+    # on). Algorithmic bytes as for one block: the stored lower triangles
+    # (12 B per element) and row pointers, x, y and the diagonal term per
+    # column; FP32 work 12 operations per Dot2 step of both triangles.
+    ncols = 16
+    ms = tune["ms"][tune["chosen"]]
+    nnz_l, ncf_t = out["nnz_total"], out["ncf_total"]
+    by = nnz_l * 12 + (ncf_t + len(w.blocks) * len(w.zs)) * 8 + 3 * ncf_t * 8 * ncols
+    peak, peak_kind = _peaks()
+    ach = by / (ms * 1e-3) / 1e9
+    out["roofline_batched_matvec"] = {
+        "kernel": "k_b_spmm (first start-up expansion, 16 columns per block, all blocks)", "bound": "hbm",
+        "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind,
+        "us_per_launch": ms * 1e3, "alg_bytes": by,
+        "fp32_tera_ops_per_s": (2 * nnz_l - ncf_t) * ncols * 12 / (ms * 1e-3) / 1e12}
     res = {}
     for prec, name in ((SPLIT, "split"), (FP64, "fp64")):
         maneig_batched(ctx, hs, w.nroots, precision=prec)  # warm-up
