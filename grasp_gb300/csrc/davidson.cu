@@ -730,9 +730,13 @@ template <int MODE, typename P>
 __global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict__ pv, int m,
                                                     int *__restrict__ bst, const P *__restrict__ part,
                                                     int ps, int ntiles, double *__restrict__ C,
-                                                    double *__restrict__ dS, int set_bst) {
+                                                    double *__restrict__ dS, int set_bst, int cgs) {
   pdl_wait();
   __shared__ P red[BD_T];
+  // cgs (MODE 0, split form): 0 = first pass (its partials also hold the
+  // new columns' squared norms, at na nb + q), 1 = second pass (skipped
+  // when bst[2] says the first one was enough); -1 neither
+  if (MODE == 0 && cgs == 1 && bst[2]) return;
   const int kpass = pv[0].c;
   if (MODE == 0 && set_bst && blockIdx.x == 0 && threadIdx.x == 0) {
     bst[0] = m;
@@ -740,9 +744,10 @@ __global__ void __launch_bounds__(BD_T) k_bd_reduce(const IterParams *__restrict
   }
   const int nb = (MODE == 0) ? m : bst[0];
   const int na = (MODE == 0) ? kpass : kpass + nb;
+  const int nout = na * nb + ((MODE == 0 && cgs == 0) ? nb : 0);
   const int o = blockIdx.x * 32 + (threadIdx.x & 31);
-  if (nb <= 0 || (int)blockIdx.x * 32 >= na * nb) return;
-  const bool ok = o < na * nb;
+  if (nb <= 0 || (int)blockIdx.x * 32 >= nout) return;
+  const bool ok = o < nout;
   const double sum = bd_reduce(part, ps, ntiles, o, ok, red);
   if (threadIdx.x >= 32 || !ok) return;
   if (MODE == 0) {
@@ -1056,6 +1061,20 @@ __global__ void __launch_bounds__(RT) k_bdx_apply(double *__restrict__ B, int64_
   }
 }
 
+constexpr int SP = 4;  // lanes per row of the small-block forms
+template <int L>
+__device__ __forceinline__ df df_lanes(float sh, float sl) {
+  df acc = two_sum(sh, sl);
+#pragma unroll
+  for (int o = 1; o < L; o <<= 1) {
+    df other;
+    other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
+    other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
+    acc = df_add(acc, other);
+  }
+  return acc;
+}
+
 // hi + lo copies of columns c0 .. c0+nc of X
 __global__ void k_split_cols(const double *__restrict__ X, int64_t ld, int c0, int nc, int n, float2 *__restrict__ Xx) {
   pdl_wait();
@@ -1075,10 +1094,13 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
                                                    const float2 *__restrict__ Bx, float2 *__restrict__ ABx,
                                                    int64_t ld, const IterParams *__restrict__ pv, int m,
                                                    const int *__restrict__ bst, int n, int cpc,
-                                                   float2 *__restrict__ part, int ps) {
+                                                   float2 *__restrict__ part, int ps, int cgs) {
   pdl_wait();
   __shared__ float2 Bs[BD_R * MT_MAX];       // [i][q]
   __shared__ float2 As[BD_R * (BD_AC + 1)];  // [i][a]
+  // the second Gram-Schmidt pass, when the first one kept enough of every
+  // column (bst[2], set by the first pass's update)
+  if (MODE == 0 && cgs == 1 && bst[2]) return;
   const int kpass = pv[0].c;
   const int nb = (MODE == 0) ? m : bst[0];
   if (nb <= 0) return;
@@ -1086,9 +1108,25 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
   const double *Wb = ((MODE == 2) ? AB : B) + (size_t)kpass * ld;
   float2 *out = part + (size_t)blockIdx.x * ps;
   const int rbeg = blockIdx.x * cpc * BD_R, rend = min(n, rbeg + cpc * BD_R);
+  if (MODE == 0 && cgs == 0 && blockIdx.y == gridDim.y - 1) {
+    // first pass: the last grid row sums the new columns' squared norms over
+    // its rows (warp w: columns w, w + 8, ...), at outputs na nb + q
+    const int lane = threadIdx.x & 31;
+    for (int q = threadIdx.x >> 5; q < nb; q += BD_T / 32) {
+      float h = 0.f, l = 0.f;
+      for (int i = rbeg + lane; i < rend; i += 32) {
+        const float2 v = split2(Wb[(size_t)q * ld + i]);
+        dot2_step(h, l, v.x, v.y, v.x, v.y);
+      }
+      const df t = df_lanes<32>(h, l);
+      if (lane == 0) out[na * nb + q] = make_float2(t.h, t.l);
+    }
+    return;
+  }
   // columns per chunk: at most one output pair per thread
   const int acl = min(BD_AC, max(1, BD_T / nb));
-  for (int ac = blockIdx.y * acl; ac < na; ac += gridDim.y * acl) {
+  const int gy = (MODE == 0 && cgs == 0) ? gridDim.y - 1 : gridDim.y;
+  for (int ac = blockIdx.y * acl; ac < na; ac += gy * acl) {
     const int nac = min(acl, na - ac), np = nac * nb;
     float sh[BD_PAIRS], sl[BD_PAIRS];
 #pragma unroll
@@ -1139,26 +1177,31 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
 // most SMs idle; 1 otherwise), lane p taking basis columns a = p mod L; their
 // Dot2 sums are added by a fixed double-float butterfly and column q is
 // written by lane q mod L
-constexpr int SP = 4;  // lanes per row of the small-block forms
-template <int L>
-__device__ __forceinline__ df df_lanes(float sh, float sl) {
-  df acc = two_sum(sh, sl);
-#pragma unroll
-  for (int o = 1; o < L; o <<= 1) {
-    df other;
-    other.h = __shfl_xor_sync(0xffffffffu, acc.h, o);
-    other.l = __shfl_xor_sync(0xffffffffu, acc.l, o);
-    acc = df_add(acc, other);
-  }
-  return acc;
-}
 template <int M, int L>
 __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const float2 *__restrict__ Bx, int64_t ld,
                                                 const IterParams *__restrict__ pv, const double *__restrict__ C,
-                                                int m, int n) {
+                                                int m, int n, int *__restrict__ bst, int cgs) {
   pdl_wait();
   __shared__ float2 Cs[BD_CCH * M];
+  if (cgs == 1 && bst[2]) return;
   const int ka = pv[0].c, q0 = blockIdx.y * M;
+  if (cgs == 0 && blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x < 32) {
+    // "twice is enough" (Kahan, Parlett): the second pass is needed only if
+    // the first removed more than half of a column's squared norm; |w - X c|^2
+    // = |w|^2 - |c|^2 for the orthonormal basis X. FP32 is enough for the test.
+    bool keep = true;
+    for (int q = threadIdx.x; q < m; q += 32) {
+      float cc = 0.f;
+      for (int a = 0; a < ka; ++a) {
+        const float c = (float)C[(size_t)a * m + q];
+        cc = fmaf(c, c, cc);
+      }
+      const float w2 = (float)C[(size_t)ka * m + q];
+      keep = keep && (w2 - cc >= 0.5f * w2);
+    }
+    keep = __all_sync(0xffffffffu, keep);
+    if (threadIdx.x == 0) bst[2] = keep ? 1 : 0;
+  }
   const int part = threadIdx.x % L;
   const int i = blockIdx.x * (RT / L) + threadIdx.x / L;
   float sh[M], sl[M];
@@ -1365,6 +1408,7 @@ struct Dvd {
   int full_m = 0;                 // MBLOCK: block matvecs over this many columns are timed apart
   double spmm_full_ms = 0;
   int spmm_full_n = 0;
+  int cgs_once = 0;               // split block passes whose second Gram-Schmidt pass was skipped
   // SPLIT: hi + lo copies of the basis and its products (split-precision
   // block kernels); columns [0, bx_cols) of both are current
   DBuf<float2> Bx, ABx;
@@ -1500,6 +1544,7 @@ struct Dvd {
     pass_ms = 0;
     spmm_full_ms = 0;
     spmm_full_n = 0;
+    cgs_once = 0;
     bx_cols = 0;
     full_m = 0;
     GG_CUDA(cudaMemsetAsync(counters.p, 0, 16 * sizeof(unsigned), s));
@@ -1628,17 +1673,20 @@ struct Dvd {
     const dim3 gdx(bd_G, (lim + std::min(BD_AC, std::max(1, BD_T / m)) - 1) / std::min(BD_AC, std::max(1, BD_T / m)));
     for (int round = 0; round < 2; ++round) {
       if (split) {
-        GG_CUDA(launch_pdl(k_bdx_dots<0>, gdx, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
-                           bd_ps));
+        // the first pass's last grid row sums the new columns' squared norms
+        const dim3 g0(gdx.x, gdx.y + (round == 0 ? 1 : 0));
+        GG_CUDA(launch_pdl(k_bdx_dots<0>, g0, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
+                           bd_ps, round));
         GG_CUDA(launch_pdl(k_bd_reduce<0, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p,
-                           round == 0));
+                           round == 0, round));
       } else {
         GG_CUDA(launch_pdl(k_bd_dots<0>, gd, BD_T, 0, s, B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps));
-        GG_CUDA(launch_pdl(k_bd_reduce<0, double>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p, round == 0));
+        GG_CUDA(launch_pdl(k_bd_reduce<0, double>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, dS.p,
+                           round == 0, -1));
       }
       if (sub_split) {
         if (split)
-          GG_CUDA(launch_pdl(k_bdx_sub<1, SP>, dim3(nrow4, m), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n));
+          GG_CUDA(launch_pdl(k_bdx_sub<1, SP>, dim3(nrow4, m), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n, bst.p, round));
         else
           GG_CUDA(launch_pdl(k_bd_sub<1>, dim3(nrow, m), RT, 0, s, B.p, ld, dpv.p, bC.p, m, n));
       } else {
@@ -1650,7 +1698,8 @@ struct Dvd {
 #define BD_SUB(K)                                                                           \
   case K:                                                                                   \
     if (split)                                                                              \
-      GG_CUDA(launch_pdl(k_bdx_sub<K, 1>, dim3(nrow, half), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n));     \
+      GG_CUDA(launch_pdl(k_bdx_sub<K, 1>, dim3(nrow, half), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n, bst.p,   \
+                         round));                                                           \
     else                                                                                    \
       GG_CUDA(launch_pdl(k_bd_sub<K>, dim3(nrow, half), RT, 0, s, B.p, ld, dpv.p, bC.p, m, n));              \
     break;
@@ -1665,7 +1714,7 @@ struct Dvd {
     for (int round = 0; round < 2; ++round) {
       if (split) {
         GG_CUDA(launch_pdl(k_bdx_dots<1>, dim3(bd_G, 1), BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n,
-                           bd_cpc, bpx, bd_ps));
+                           bd_cpc, bpx, bd_ps, -1));
         GG_CUDA(launch_pdl(k_bd_chol<float2>, 1, BD_RED, 0, s, m, bst.p, bpx, bd_ps, bd_G, bC.p, bskip.p, round));
         GG_CUDA(launch_pdl(k_bdx_apply, nrow, RT, 0, s, B.p, ld, dpv.p, bst.p, bC.p, n, round == 1 ? bxs.p : nullptr,
                                         spmm_pitch(m), Bx.p));
@@ -1710,13 +1759,13 @@ struct Dvd {
     }
     if (split) {
       GG_CUDA(launch_pdl(k_bdx_dots<2>, gdx, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
-                         bd_ps));
+                         bd_ps, -1));
       GG_CUDA(launch_pdl(k_bd_reduce<2, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p,
-                         dout_scol(), 0));
+                         dout_scol(), 0, -1));
     } else {
       GG_CUDA(launch_pdl(k_bd_dots<2>, gd, BD_T, 0, s, B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps));
       GG_CUDA(launch_pdl(k_bd_reduce<2, double>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpart.p, bd_ps, bd_G, bC.p,
-                         dout_scol(), 0));
+                         dout_scol(), 0, -1));
     }
     note_launches(2);
     GG_CUDA(cudaGetLastError());
@@ -1806,6 +1855,7 @@ struct Dvd {
     t_wait += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     const int nk = hout_bst()[0];
     if (nk < 0 || nk > m) return fail(GG_ERR_STATE, "block pass: kept column count out of range");
+    if (use_x()) cgs_once += hout_bst()[2];
     std::memcpy(S.data() + o0, hout_scol(), (o1 - o0) * sizeof(double));
     for (int v = 0; v < (use_x() ? 1 : m); ++v) {
       float ms = 0.f;
@@ -2760,6 +2810,7 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   ctx->stats[17] = 1e3 * D1.t_total;
   ctx->stats[18] = 1e3 * D2.t_total;
   ctx->stats[19] = 1e3 * D2.t_eig;
+  ctx->stats[30] = D1.cgs_once + D2.cgs_once;
   ctx->stats[23] = D2.spmm_full_ms;
   ctx->stats[24] = D2.spmm_full_n;
   *nloops = nl_total;

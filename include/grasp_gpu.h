@@ -267,7 +267,10 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * structure set-up (symmetric matvec structures of the block and of its
  * leading block) / Davidson workspaces, 28 device ms from the start of that
  * gg_maneig to the end of its structure set-up, 29 device ms of the
- * assembly plan built by the last gg_setham_upload (0 when it built none).
+ * assembly plan built by the last gg_setham_upload (0 when it built none),
+ * 30 block passes of the last split gg_maneig whose second Gram-Schmidt
+ * pass was skipped (the first kept at least half of every new column's
+ * squared norm).
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors
