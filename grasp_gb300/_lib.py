@@ -46,6 +46,8 @@ GPU_SYMBOLS = {
     "gg_get_rk_table": (C.c_int, [C.c_void_p, _i32, _d, _i32]),
     "gg_rkintc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
     "gg_slater": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
+    "gg_ypot": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _d]),
+    "gg_xpot": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _d, _d]),
     "gg_slater_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
     "gg_rinti": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _d]),
     "gg_iabint_table": (C.c_int, [C.c_void_p, _d]),

@@ -101,6 +101,22 @@ class Context:
         check(_lib.gpu().gg_slater(self._h, a, b, c, d, k, C.byref(out)))
         return out.value
 
+    def ypot(self, nya, ya):
+        """YPOT (rmcdhf90/ypot.f90): the direct potential YP(1:N) of a SETCOF
+        list (NYA labels (IOY2*215 + IOY1)*215 + K, YA coefficients)."""
+        nya = np.ascontiguousarray(nya, np.int32); ya = np.ascontiguousarray(ya, np.float64)
+        yp = np.zeros(self.n)
+        check(_lib.gpu().gg_ypot(self._h, nya.size, ptr(nya, _i32), ptr(ya, _d), ptr(yp, _d)))
+        return yp
+
+    def xpot(self, nxa, xa):
+        """XPOT (rmcdhf90/xpot.f90): the exchange potential XP(1:N), XQ(1:N) of
+        a SETCOF list (NXA labels ((IORB*215 + IOY2)*215 + IOY1)*215 + K)."""
+        nxa = np.ascontiguousarray(nxa, np.int32); xa = np.ascontiguousarray(xa, np.float64)
+        xp = np.zeros(self.n); xq = np.zeros(self.n)
+        check(_lib.gpu().gg_xpot(self._h, nxa.size, ptr(nxa, _i32), ptr(xa, _d), ptr(xp, _d), ptr(xq, _d)))
+        return xp, xq
+
     def rinti(self, j, k, mode=0):
         out = C.c_double()
         check(_lib.gpu().gg_rinti(self._h, j, k, mode, C.byref(out)))

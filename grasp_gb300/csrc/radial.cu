@@ -16,6 +16,8 @@
 #include <cuda_fp16.h>
 
 #include <algorithm>
+#include <map>
+#include <tuple>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -875,6 +877,33 @@ __global__ void k_quad_table(const QuadItem *__restrict__ items, const int *__re
   }
 }
 
+// YPOT / XPOT (rmcdhf90/ypot.f90:35-49, xpot.f90:31-54): one thread per grid
+// point combines the list's Y functions in the list's order (the reference's
+// per-point operations: YP = YP - COEFF*TB; CTB = COEFF*TB, XP += CTB*QF,
+// XQ -= CTB*PF, with COEFF = XA/C formed on the host).
+__global__ void k_potential(int mode, int ncof, const int *__restrict__ fidx, const double *__restrict__ coef,
+                            const int *__restrict__ iorb, const double *__restrict__ Y, int np,
+                            const double *__restrict__ ZZ, const double *__restrict__ PF,
+                            const double *__restrict__ QF, int ld, int n, double *__restrict__ out0,
+                            double *__restrict__ out1) {
+  for (int i = 1 + blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+    if (mode == 0) {
+      double yp = ZZ[i];
+      for (int t = 0; t < ncof; ++t) yp = yp - coef[t] * Y[(size_t)fidx[t] * np + i];
+      out0[i - 1] = yp;
+    } else {
+      double xp = 0.0, xq = 0.0;
+      for (int t = 0; t < ncof; ++t) {
+        const double ctb = coef[t] * Y[(size_t)fidx[t] * np + i];
+        xp = xp + ctb * pf(QF, ld, i, iorb[t]);
+        xq = xq - ctb * pf(PF, ld, i, iorb[t]);
+      }
+      out0[i - 1] = xp;
+      out1[i - 1] = xq;
+    }
+  }
+}
+
 // DPBDT (lib9290/dpbdt.f90:39-99): 13-point derivative of orbital J (per
 // grid index) into dP, dQ (1-based).
 __device__ void dpbdt_warp(const double *PF, const double *QF, int ld, int J, const QuadConst &q, double *dP,
@@ -1421,6 +1450,86 @@ int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out) {
   GG_CUDA(cudaMemcpyAsync(out, dout.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   GG_CUDA(cudaStreamSynchronize(ctx->stream));
   return GG_OK;
+}
+
+}  // extern "C"
+
+
+// YPOT / XPOT on the device: the list's distinct Y^k_ab (every grid point,
+// YZK's TB), then k_potential.
+static int potential(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const double *co, double *out0,
+                     double *out1) {
+  GG_TRY(ensure_orbitals(ctx));
+  Orbitals &o = ctx->orb;
+  Grid &g = ctx->grid;
+  const int nw = o.nw;
+  if (ncof < 0 || (ncof > 0 && (!lab || !co)) || !out0 || (mode == 1 && !out1))
+    return fail(GG_ERR_ARG, "gg_ypot/gg_xpot: bad arguments");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  std::vector<YDesc> hy;
+  std::vector<int> fidx(std::max(ncof, 1)), iorb(std::max(ncof, 1), 1);
+  std::vector<double> coef(std::max(ncof, 1));
+  std::map<std::tuple<int, int, int>, int> seen;
+  for (int t = 0; t < ncof; ++t) {
+    int64_t l = lab[t];
+    const int k = (int)(l % KEYORB);
+    l /= KEYORB;
+    const int a = (int)(l % KEYORB);
+    l /= KEYORB;
+    const int b = (int)(mode == 0 ? l : l % KEYORB);
+    const int io = (mode == 0) ? 1 : (int)(l / KEYORB);
+    if (lab[t] < 0 || k > KLIMIT || a < 1 || a > nw || b < 1 || b > nw || io < 1 || io > nw)
+      return fail(GG_ERR_ARG, "gg_ypot/gg_xpot: label outside the orbital set or K above 20");
+    auto it = seen.find({k, a, b});
+    if (it == seen.end()) {
+      YDesc y;
+      y.k = k;
+      y.b = a;
+      y.d = b;
+      y.mtp = std::min(o.mf[a], o.mf[b]);
+      y.mtpb = g.n;  // the whole function: the potentials use TB(1:N)
+      y.cs = 0;
+      y.nd = 1;
+      it = seen.emplace(std::make_tuple(k, a, b), (int)hy.size()).first;
+      hy.push_back(y);
+    }
+    fidx[t] = it->second;
+    iorb[t] = io;
+    coef[t] = (mode == 0) ? co[t] : co[t] / g.c;  // XPOT: COEFF = COEFF/C
+  }
+  const int nf = std::max(1, (int)hy.size());
+  if (hy.empty()) hy.push_back(YDesc{0, 1, 1, 2, 2, 0, 1});  // no terms: the loop below adds none
+  DBuf<YDesc> dy;
+  DBuf<int> dfi, dio;
+  DBuf<double> dco, dY, scratch, d0, d1;
+  GG_TRY(upload(dy, hy, ctx->stream));
+  GG_TRY(upload(dfi, fidx, ctx->stream));
+  GG_TRY(upload(dio, iorb, ctx->stream));
+  GG_TRY(upload(dco, coef, ctx->stream));
+  GG_TRY(dY.alloc((size_t)nf * g.np));
+  GG_TRY(d0.alloc(g.n));
+  if (mode == 1) GG_TRY(d1.alloc(g.n));
+  GG_TRY(build_y(ctx, dy.p, nf, dY.p, scratch));
+  k_potential<<<(g.n + 127) / 128, 128, 0, ctx->stream>>>(mode, ncof, dfi.p, dco.p, dio.p, dY.p, g.np, g.dZZ.p,
+                                                           o.dPF.p, o.dQF.p, o.ld, g.n, d0.p, d1.p);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(out0, d0.p, g.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (mode == 1) GG_CUDA(cudaMemcpyAsync(out1, d1.p, g.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return GG_OK;
+}
+
+extern "C" {
+
+int gg_ypot(gg_ctx *ctx, int ncof, const int32_t *nya, const double *ya, double *yp) {
+  if (!ctx) return fail(GG_ERR_ARG, "gg_ypot: no context");
+  return potential(ctx, 0, ncof, nya, ya, yp, nullptr);
+}
+
+int gg_xpot(gg_ctx *ctx, int ncof, const int32_t *nxa, const double *xa, double *xp, double *xq) {
+  if (!ctx) return fail(GG_ERR_ARG, "gg_xpot: no context");
+  return potential(ctx, 1, ncof, nxa, xa, xp, xq);
 }
 
 }  // extern "C"

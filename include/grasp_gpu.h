@@ -104,6 +104,22 @@ int gg_get_rk_table(gg_ctx *ctx, int32_t *indteirk, double *valteirk, int32_t *k
 int gg_rkintc(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *tegral);
 /* SLATER (lib9290/slater.f90:3): one R^k(ab;cd) evaluated on the device. */
 int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out);
+/* ---- SCF potentials from the Y^k functions (rmcdhf) ------------------------
+ * The Y^k_ab functions of YZK (lib9290/yzk.f90:3: TB(1:N), every grid point),
+ * built on the device for a coefficient list of SETCOF and combined in the
+ * list's order, each grid point's operations those of the reference loop.
+ * gg_ypot: YPOT(J) (rmcdhf90/ypot.f90:35-49), the direct potential
+ *   yp[i-1] = ZZ(i) - sum_t ya[t] Y^K_{IOY1 IOY2}(r_i), i = 1..N;
+ *   nya[t] = (IOY2 * 215 + IOY1) * 215 + K (rmcdhf's NYA, KEY = KEYORB).
+ * gg_xpot: XPOT(J) (rmcdhf90/xpot.f90:31-54), the exchange potential
+ *   xp[i-1] = sum_t (xa[t] / C) Y^K_{IOY1 IOY2}(r_i) QF(i, IORB),
+ *   xq[i-1] = -sum_t (xa[t] / C) Y^K_{IOY1 IOY2}(r_i) PF(i, IORB);
+ *   nxa[t] = ((IORB * 215 + IOY2) * 215 + IOY1) * 215 + K (NXA).
+ * Orbital indices are 1-based in the context's orbital order; yp, xp and xq
+ * hold N doubles. GG_ERR_ARG for a label outside the orbital set or
+ * K > 20 (YZK's KLIMIT).                                                    */
+int gg_ypot(gg_ctx *ctx, int ncof, const int32_t *nya, const double *ya, double *yp);
+int gg_xpot(gg_ctx *ctx, int ncof, const int32_t *nxa, const double *xa, double *xp, double *xq);
 /* gg_slater without any device allocation. No counterpart in the reference:
  * for callers that cannot allocate device memory at the point where they
  * need an integral (device memory fully handed to a pool or to a large

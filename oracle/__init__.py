@@ -70,6 +70,8 @@ def lib():
         L.or_quad.restype = C.c_double
         L.or_quad.argtypes = [C.c_void_p, C.c_int, _d]
         L.or_yzk.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _d]
+        L.or_ypot.argtypes = [C.c_void_p, C.c_int, _i32, _d, _d]
+        L.or_xpot.argtypes = [C.c_void_p, C.c_int, _i32, _d, _d, _d]
         L.or_slater.restype = C.c_double
         L.or_slater.argtypes = [C.c_void_p] + [C.c_int] * 5
         L.or_rinti.restype = C.c_double
@@ -152,6 +154,23 @@ class Oracle:
         yk = np.zeros(self.n)
         mtp = lib().or_yzk(self._h, k, i, j, _p(yk, _d))
         return yk, mtp
+
+    def ypot(self, nya, ya):
+        """YPOT (rmcdhf90/ypot.f90): the direct potential YP(1:N) of the
+        coefficient list (NYA labels, YA coefficients)."""
+        nya = np.ascontiguousarray(nya, np.int32); ya = np.ascontiguousarray(ya, np.float64)
+        yp = np.zeros(self.n)
+        if lib().or_ypot(self._h, nya.size, _p(nya, _i32), _p(ya, _d), _p(yp, _d)) != 0:
+            raise ValueError("ypot: label outside the orbital set")
+        return yp
+
+    def xpot(self, nxa, xa):
+        """XPOT (rmcdhf90/xpot.f90): the exchange potential XP(1:N), XQ(1:N)."""
+        nxa = np.ascontiguousarray(nxa, np.int32); xa = np.ascontiguousarray(xa, np.float64)
+        xp = np.zeros(self.n); xq = np.zeros(self.n)
+        if lib().or_xpot(self._h, nxa.size, _p(nxa, _i32), _p(xa, _d), _p(xp, _d), _p(xq, _d)) != 0:
+            raise ValueError("xpot: label outside the orbital set")
+        return xp, xq
 
     def slater(self, a, b, c, d, k):
         return lib().or_slater(self._h, a, b, c, d, k)

@@ -886,6 +886,56 @@ double or_slater(or_ctx *g, int ia, int ib, int ic, int id, int k) {
   return slater(g, ia, ib, ic, id, k, TA.data(), TB.data());
 }
 
+// YPOT (rmcdhf90/ypot.f90:35-49): YP(:N) = ZZ(:N), then for each index of
+// the list YP(:N) = YP(:N) - COEFF*TB(:N) with TB from YZK(K, IOY1, IOY2);
+// NYA = (IOY2*KEY + IOY1)*KEY + K, KEY = 215. yp[0..N-1] = YP(1..N).
+int or_ypot(or_ctx *g, int ncof, const int32_t *nya, const double *ya, double *yp) {
+  const int N = g->n, KEY = 215;
+  std::vector<double> YP(g->nn1(), 0.0), TA(g->nn1(), 0.0), TB(g->nn1(), 0.0);
+  for (int i = 1; i <= N; ++i) YP[i] = g->ZZ[i];
+  for (int idx = 0; idx < ncof; ++idx) {
+    int label = nya[idx];
+    const int K = label % KEY;
+    label /= KEY;
+    const int IOY1 = label % KEY, IOY2 = label / KEY;
+    if (IOY1 < 1 || IOY1 > g->nw || IOY2 < 1 || IOY2 > g->nw || K > KLIMIT) return -1;
+    const double COEFF = ya[idx];
+    yzk(g, K, IOY1, IOY2, TA.data(), TB.data());
+    for (int i = 1; i <= N; ++i) YP[i] = YP[i] - COEFF * TB[i];
+  }
+  for (int i = 1; i <= N; ++i) yp[i - 1] = YP[i];
+  return 0;
+}
+
+// XPOT (rmcdhf90/xpot.f90:31-54): XP = XQ = 0; for each index, TB from
+// YZK(K, IOY1, IOY2), COEFF = XA/C, CTB = COEFF*TB(I), XP(I) += CTB*QF(I,IORB),
+// XQ(I) -= CTB*PF(I,IORB); NXA = ((IORB*KEY + IOY2)*KEY + IOY1)*KEY + K.
+int or_xpot(or_ctx *g, int ncof, const int32_t *nxa, const double *xa, double *xp, double *xq) {
+  const int N = g->n, KEY = 215;
+  std::vector<double> XP(g->nn1(), 0.0), XQ(g->nn1(), 0.0), TA(g->nn1(), 0.0), TB(g->nn1(), 0.0);
+  for (int idx = 0; idx < ncof; ++idx) {
+    int label = nxa[idx];
+    const int K = label % KEY;
+    label /= KEY;
+    const int IOY1 = label % KEY;
+    label /= KEY;
+    const int IOY2 = label % KEY, IORB = label / KEY;
+    if (IOY1 < 1 || IOY1 > g->nw || IOY2 < 1 || IOY2 > g->nw || IORB < 1 || IORB > g->nw || K > KLIMIT) return -1;
+    yzk(g, K, IOY1, IOY2, TA.data(), TB.data());
+    const double COEFF = xa[idx] / g->c;
+    for (int i = 1; i <= N; ++i) {
+      const double CTB = COEFF * TB[i];
+      XP[i] = XP[i] + CTB * g->qf(i, IORB);
+      XQ[i] = XQ[i] - CTB * g->pf(i, IORB);
+    }
+  }
+  for (int i = 1; i <= N; ++i) {
+    xp[i - 1] = XP[i];
+    xq[i - 1] = XQ[i];
+  }
+  return 0;
+}
+
 double or_rinti(or_ctx *g, int j, int k, int mode, int *err) {
   std::vector<double> TA(g->nn1(), 0.0), TB(g->nn1(), 0.0);
   return rinti(g, j, k, mode, TA.data(), TB.data(), err);
