@@ -465,6 +465,12 @@ struct NvOut {
   int nadded, done;
   double res[MT_MAX];
 };
+// hi + lo FP32 pair of an FP64 value (its nearest float and the rest)
+__device__ __forceinline__ float2 split2(double v) {
+  const float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
+
 // a / b to about 2^-46 relative: an FP32 reciprocal of b refined by one
 // Newton step on the quotient (three FP64 operations instead of the FP64
 // division's longer sequence; |b| > 1e-6 here, far inside FP32's range
@@ -484,7 +490,8 @@ __device__ __forceinline__ double quot(double a, double b) {
 // (the block pass then drops them)
 __global__ void k_newvec_precond(const NvIn *__restrict__ in, const double *__restrict__ rn2,
                                  NvOut *__restrict__ out, double *__restrict__ B, const double *__restrict__ T,
-                                 int64_t ld, double *__restrict__ diag, int n, int mg, int kpass) {
+                                 int64_t ld, double *__restrict__ diag, int n, int mg, int kpass,
+                                 float2 *__restrict__ wx) {
   pdl_wait();
   __shared__ double sres[MT_MAX], srhs[MT_MAX];
   __shared__ PrecList L;
@@ -533,11 +540,16 @@ __global__ void k_newvec_precond(const NvIn *__restrict__ in, const double *__re
     const double rr = fma(-L.rhs[q], b, r);
     const double lam = L.lam[q];
     const double d = dg - lam;
-    B[(size_t)L.col[q] * ld + i] = (fabs(d) > 1.0e-06) ? quot(rr, d) : rr * 1.0e06;
+    const double v = (fabs(d) > 1.0e-06) ? quot(rr, d) : rr * 1.0e06;
+    B[(size_t)L.col[q] * ld + i] = v;
+    if (wx) wx[(size_t)(L.col[q] - kpass) * ld + i] = split2(v);
     dg = d + lam;
   }
   diag[i] = dg;
-  for (int q = m; q < mg; ++q) B[(size_t)(kpass + q) * ld + i] = 0.0;
+  for (int q = m; q < mg; ++q) {
+    B[(size_t)(kpass + q) * ld + i] = 0.0;
+    if (wx) wx[(size_t)q * ld + i] = make_float2(0.f, 0.f);
+  }
 }
 
 // column c <- scal[fslot] * column c; with xs, also its hi+lo split for the matvec
@@ -1007,10 +1019,6 @@ __device__ __forceinline__ void dot2_step(float &sh, float &sl, float ah, float 
   sh = sn;
   sl = __fadd_rn(sl, __fadd_rn(err, t));
 }
-__device__ __forceinline__ float2 split2(double v) {
-  const float h = __double2float_rn(v);
-  return make_float2(h, __double2float_rn(v - (double)h));
-}
 
 // k_bd_apply in split form: each row's np column values are split into hi +
 // lo floats and combined with the split C by Dot2 sums (FP32 pipes); the
@@ -1018,10 +1026,11 @@ __device__ __forceinline__ float2 split2(double v) {
 // matvec copy (xs) and the basis store (xstore) hold exactly the FP64 value
 template <int NP>
 __device__ __forceinline__ void bdx_apply_rows(double *__restrict__ B, int64_t ld, int kpass, int nc,
-                                               const float2 *Cs, int i, float2 *xs, int mp, float2 *xstore) {
+                                               const float2 *Cs, int i, float2 *xs, int mp, float2 *xstore,
+                                               float2 *wx) {
   float2 x[NP];
 #pragma unroll
-  for (int q = 0; q < NP; ++q) x[q] = split2(B[(size_t)(kpass + q) * ld + i]);
+  for (int q = 0; q < NP; ++q) x[q] = wx[(size_t)q * ld + i];
   for (int c = 0; c < nc; ++c) {
     float h = 0.f, l = 0.f;
 #pragma unroll
@@ -1031,6 +1040,7 @@ __device__ __forceinline__ void bdx_apply_rows(double *__restrict__ B, int64_t l
     }
     const df v = two_sum(h, l);
     B[(size_t)(kpass + c) * ld + i] = (double)v.h + (double)v.l;
+    wx[(size_t)c * ld + i] = make_float2(v.h, v.l);
     if (xs) {
       const float2 v2 = make_float2(v.h, v.l);
       xs[(size_t)i * mp + c] = v2;
@@ -1043,7 +1053,8 @@ __device__ __forceinline__ void bdx_apply_rows(double *__restrict__ B, int64_t l
 
 __global__ void __launch_bounds__(RT) k_bdx_apply(double *__restrict__ B, int64_t ld, const IterParams *__restrict__ pv,
                                                   const int *__restrict__ bst, const double *__restrict__ C, int n,
-                                                  float2 *__restrict__ xs, int mp, float2 *__restrict__ xstore) {
+                                                  float2 *__restrict__ xs, int mp, float2 *__restrict__ xstore,
+                                                  float2 *__restrict__ wx) {
   pdl_wait();
   __shared__ float2 Cs[MT_MAX * MT_MAX];
   const int kpass = pv[0].c, np = bst[1], nc = bst[0];
@@ -1053,7 +1064,7 @@ __global__ void __launch_bounds__(RT) k_bdx_apply(double *__restrict__ B, int64_
   if (i >= n || np <= 0) return;
   switch (np) {
 #define BD_CASE(K) \
-  case K: bdx_apply_rows<K>(B, ld, kpass, nc, Cs, i, xs, mp, xstore); break;
+  case K: bdx_apply_rows<K>(B, ld, kpass, nc, Cs, i, xs, mp, xstore, wx); break;
     BD_CASE(1) BD_CASE(2) BD_CASE(3) BD_CASE(4) BD_CASE(5) BD_CASE(6) BD_CASE(7) BD_CASE(8)
     BD_CASE(9) BD_CASE(10) BD_CASE(11) BD_CASE(12) BD_CASE(13) BD_CASE(14) BD_CASE(15) BD_CASE(16)
 #undef BD_CASE
@@ -1094,7 +1105,8 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
                                                    const float2 *__restrict__ Bx, float2 *__restrict__ ABx,
                                                    int64_t ld, const IterParams *__restrict__ pv, int m,
                                                    const int *__restrict__ bst, int n, int cpc,
-                                                   float2 *__restrict__ part, int ps, int cgs) {
+                                                   float2 *__restrict__ part, int ps, int cgs,
+                                                   const float2 *__restrict__ wx) {
   pdl_wait();
   __shared__ float2 Bs[BD_R * MT_MAX];       // [i][q]
   __shared__ float2 As[BD_R * (BD_AC + 1)];  // [i][a]
@@ -1115,7 +1127,7 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
     for (int q = threadIdx.x >> 5; q < nb; q += BD_T / 32) {
       float h = 0.f, l = 0.f;
       for (int i = rbeg + lane; i < rend; i += 32) {
-        const float2 v = split2(Wb[(size_t)q * ld + i]);
+        const float2 v = wx[(size_t)q * ld + i];
         dot2_step(h, l, v.x, v.y, v.x, v.y);
       }
       const df t = df_lanes<32>(h, l);
@@ -1135,13 +1147,14 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
       const int nr = min(BD_R, rend - r0);
       for (int idx = threadIdx.x; idx < nr * nb; idx += BD_T) {
         const int i = idx % nr, q = idx / nr;
-        const float2 v = split2(Wb[(size_t)q * ld + r0 + i]);
+        // MODE 0, 1: the new columns' split copy (written by their producer)
+        const float2 v = (MODE == 2) ? split2(Wb[(size_t)q * ld + r0 + i]) : wx[(size_t)q * ld + r0 + i];
         Bs[i * MT_MAX + q] = v;
         if (MODE == 2 && blockIdx.y == 0 && ac == 0) ABx[(size_t)(kpass + q) * ld + r0 + i] = v;
       }
       for (int idx = threadIdx.x; idx < nr * nac; idx += BD_T) {
         const int i = idx % nr, a = idx / nr;
-        As[i * (BD_AC + 1) + a] = (MODE == 1) ? split2(B[(size_t)(kpass + ac + a) * ld + r0 + i])
+        As[i * (BD_AC + 1) + a] = (MODE == 1) ? wx[(size_t)(ac + a) * ld + r0 + i]
                                               : Bx[(size_t)(ac + a) * ld + r0 + i];
       }
       __syncthreads();
@@ -1180,7 +1193,8 @@ __global__ void __launch_bounds__(BD_T) k_bdx_dots(const double *__restrict__ B,
 template <int M, int L>
 __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const float2 *__restrict__ Bx, int64_t ld,
                                                 const IterParams *__restrict__ pv, const double *__restrict__ C,
-                                                int m, int n, int *__restrict__ bst, int cgs) {
+                                                int m, int n, int *__restrict__ bst, int cgs,
+                                                float2 *__restrict__ wx) {
   pdl_wait();
   __shared__ float2 Cs[BD_CCH * M];
   if (cgs == 1 && bst[2]) return;
@@ -1239,7 +1253,12 @@ __global__ void __launch_bounds__(RT) k_bdx_sub(double *__restrict__ B, const fl
 #pragma unroll
   for (int q = 0; q < M; ++q) {
     const df acc = df_lanes<L>(sh[q], sl[q]);
-    if (i < n && q % L == part) B[(size_t)(ka + q0 + q) * ld + i] -= (double)acc.h + (double)acc.l;
+    if (i < n && q % L == part) {
+      const size_t o = (size_t)(ka + q0 + q) * ld + i;
+      const double v = B[o] - ((double)acc.h + (double)acc.l);
+      B[o] = v;
+      wx[(size_t)(q0 + q) * ld + i] = split2(v);
+    }
   }
 }
 
@@ -1404,6 +1423,11 @@ struct Dvd {
   DBuf<double> bpart, bC, bskip;
   DBuf<int> bst;
   DBuf<float2> bxs;
+  DBuf<float2> wx;                // SPLIT: hi + lo copy of the pass's new columns, kept by their producers
+  int ensure_wx() {
+    if (use_x() && !wx.p) GG_TRY(wx.alloc((size_t)MT_MAX * ld));
+    return GG_OK;
+  }
   int bd_G = 0, bd_Y = 1, bd_cpc = 0, bd_ps = 0;
   int full_m = 0;                 // MBLOCK: block matvecs over this many columns are timed apart
   double spmm_full_ms = 0;
@@ -1676,7 +1700,7 @@ struct Dvd {
         // the first pass's last grid row sums the new columns' squared norms
         const dim3 g0(gdx.x, gdx.y + (round == 0 ? 1 : 0));
         GG_CUDA(launch_pdl(k_bdx_dots<0>, g0, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
-                           bd_ps, round));
+                           bd_ps, round, wx.p));
         GG_CUDA(launch_pdl(k_bd_reduce<0, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p, dS.p,
                            round == 0, round));
       } else {
@@ -1686,7 +1710,8 @@ struct Dvd {
       }
       if (sub_split) {
         if (split)
-          GG_CUDA(launch_pdl(k_bdx_sub<1, SP>, dim3(nrow4, m), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n, bst.p, round));
+          GG_CUDA(launch_pdl(k_bdx_sub<1, SP>, dim3(nrow4, m), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n, bst.p, round,
+                             wx.p));
         else
           GG_CUDA(launch_pdl(k_bd_sub<1>, dim3(nrow, m), RT, 0, s, B.p, ld, dpv.p, bC.p, m, n));
       } else {
@@ -1699,7 +1724,7 @@ struct Dvd {
   case K:                                                                                   \
     if (split)                                                                              \
       GG_CUDA(launch_pdl(k_bdx_sub<K, 1>, dim3(nrow, half), RT, 0, s, B.p, Bx.p, ld, dpv.p, bC.p, m, n, bst.p,   \
-                         round));                                                           \
+                         round, wx.p));                                                     \
     else                                                                                    \
       GG_CUDA(launch_pdl(k_bd_sub<K>, dim3(nrow, half), RT, 0, s, B.p, ld, dpv.p, bC.p, m, n));              \
     break;
@@ -1714,10 +1739,10 @@ struct Dvd {
     for (int round = 0; round < 2; ++round) {
       if (split) {
         GG_CUDA(launch_pdl(k_bdx_dots<1>, dim3(bd_G, 1), BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n,
-                           bd_cpc, bpx, bd_ps, -1));
+                           bd_cpc, bpx, bd_ps, -1, wx.p));
         GG_CUDA(launch_pdl(k_bd_chol<float2>, 1, BD_RED, 0, s, m, bst.p, bpx, bd_ps, bd_G, bC.p, bskip.p, round));
         GG_CUDA(launch_pdl(k_bdx_apply, nrow, RT, 0, s, B.p, ld, dpv.p, bst.p, bC.p, n, round == 1 ? bxs.p : nullptr,
-                                        spmm_pitch(m), Bx.p));
+                                        spmm_pitch(m), Bx.p, wx.p));
       } else {
         GG_CUDA(launch_pdl(k_bd_dots<1>, dim3(bd_G, 1), BD_T, 0, s, B.p, AB.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpart.p, bd_ps));
         GG_CUDA(launch_pdl(k_bd_chol<double>, 1, BD_RED, 0, s, m, bst.p, bpart.p, bd_ps, bd_G, bC.p, bskip.p, round));
@@ -1759,7 +1784,7 @@ struct Dvd {
     }
     if (split) {
       GG_CUDA(launch_pdl(k_bdx_dots<2>, gdx, BD_T, 0, s, B.p, AB.p, Bx.p, ABx.p, ld, dpv.p, m, bst.p, n, bd_cpc, bpx,
-                         bd_ps, -1));
+                         bd_ps, -1, wx.p));
       GG_CUDA(launch_pdl(k_bd_reduce<2, float2>, nred, BD_T, 0, s, dpv.p, m, bst.p, bpx, bd_ps, bd_G, bC.p,
                          dout_scol(), 0, -1));
     } else {
@@ -1810,8 +1835,18 @@ struct Dvd {
 
       if (precision == GG_SPLIT) GG_TRY(bxs.alloc((size_t)MT_MAX * ld));
     }
+    GG_TRY(ensure_wx());
     GG_TRY(sync_split(kpass));
     if (!staged) {
+      // the caller's new columns: their split copy (a staged pass's NEWVEC
+      // writes it with the columns)
+      if (use_x()) {
+        const int64_t tot = (int64_t)m * n;
+        const int nb = (int)std::min<int64_t>((tot + TPB - 1) / TPB, 4 * ctx->sms);
+        k_split_cols<<<nb, TPB, 0, s>>>(B.p + (size_t)kpass * ld, ld, 0, m, n, wx.p);
+        note_launch();
+        GG_CUDA(cudaGetLastError());
+      }
       IterParams *hp = reinterpret_cast<IterParams *>(hio_in + io_pv);
       for (int v = 0; v < m; ++v) {
         hp[v] = IterParams{};
@@ -2111,8 +2146,9 @@ struct Dvd {
     // small CTAs for small blocks: the preconditioner is FP64 work, spread
     // over more SMs
     const int tp = (n < 128 * ctx->sms) ? 64 : TPB;
+    GG_TRY(ensure_wx());
     GG_CUDA(launch_pdl(k_newvec_precond, (n + tp - 1) / tp, tp, 0, s, din_nv(), drn, dout_nv(), B.p, T.p, ld, diag.p,
-                       n, mg, k));
+                       n, mg, k, use_x() ? wx.p : nullptr));
     note_launch();
     GG_CUDA(cudaGetLastError());
     GG_TRY(block_pass(k, mg, S, nk, true));  // copies NEWVEC's results with its own, waits for the stream
