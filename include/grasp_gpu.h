@@ -26,6 +26,7 @@
  */
 #ifndef GRASP_GPU_H
 #define GRASP_GPU_H
+#include <stddef.h>
 #include <stdint.h>
 #ifdef __cplusplus
 extern "C" {
@@ -286,7 +287,7 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * assembly plan built by the last gg_setham_upload (0 when it built none),
  * 30 block passes of the last split gg_maneig whose second Gram-Schmidt
  * pass was skipped (the first kept at least half of every new column's
- * squared norm).
+ * squared norm).                                                            */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors

@@ -70,3 +70,18 @@ def test_python_bindings_cover_header(libs):
     assert set(declared("include/grasp_gpu.h")) <= set(_lib.GPU_SYMBOLS)
     from inputs import synth
     assert set(declared("inputs/grasp_synth.h")) <= set(synth.SYNTH_SYMBOLS)
+
+
+@pytest.mark.parametrize("header", ["include/grasp_gpu.h", "include/grasp_angular.h", "inputs/grasp_synth.h"])
+@pytest.mark.parametrize("lang", [["gcc", "-x", "c", "-std=c99"], ["g++", "-x", "c++", "-std=c++17"]])
+def test_header_compiles_alone(header, lang, tmp_path):
+    """Each public header compiles on its own, as C and as C++, and its
+    declarations are not hidden in a comment (the symbol list above is taken
+    with comments removed, so an unclosed comment would hide names from it)."""
+    src = tmp_path / "h.c"
+    src.write_text('#include "%s"\nint main(void) { return 0; }\n' % os.path.join(ROOT, header))
+    r = subprocess.run(lang + ["-Wall", "-Wextra", "-Werror", "-fsyntax-only", str(src)], capture_output=True,
+                       text=True)
+    assert r.returncode == 0, r.stderr
+    text = open(os.path.join(ROOT, header)).read()
+    assert text.count("/*") == text.count("*/"), "unbalanced comment markers"
