@@ -60,6 +60,11 @@ GPU_SYMBOLS = {
     "gg_hmat_get_emt": (C.c_int, [C.c_void_p, _d]),
     "gg_hmat_set_emt": (C.c_int, [C.c_void_p, _d]),
     "gg_spicmv2": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, _d, _d, C.c_int]),
+    "gg_hmat_create_host": (C.c_int, [C.c_void_p, C.c_int, C.c_int64, _i64, _i32, _d, C.c_double, C.c_int,
+                                      C.POINTER(C.c_void_p)]),
+    "gg_hmat_host_precision": (C.c_int, [C.c_void_p]),
+    "gg_spodmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, _d, _d]),
+    "gg_hmat_create_packed": (C.c_int, [C.c_void_p, C.c_int, _d, C.POINTER(C.c_void_p)]),
     "gg_maneig": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(GGDvdParams), _d, _d, _int, _int, _int]),
     "gg_maneig_batched": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), _int, C.POINTER(GGDvdParams), _d,
                                     _d, _int, _int, _int]),

@@ -176,6 +176,61 @@ class HMatrix:
         self.eav = None
 
     @classmethod
+    def host(cls, ctx: Context, ncf, iendc, irow, emt, eav=0.0, precision=FP64):
+        """A block kept in pinned host memory and read over the host link by
+        every product (gg_hmat_create_host, SPODMV's role): emt as rci writes
+        it to rci.res, the diagonal shifted by eav. Products and solves use
+        the given precision only."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.ncf = int(ncf)
+        self.iendc = np.ascontiguousarray(iendc, np.int64)
+        self.irow = np.ascontiguousarray(irow, np.int32)
+        self.nnz = int(self.iendc[-1])
+        emt = np.ascontiguousarray(emt, np.float64)
+        if emt.size != self.nnz:
+            raise ValueError("emt must hold IENDC(NCF) values")
+        self._box = [C.c_void_p()]
+        check(_lib.gpu().gg_hmat_create_host(ctx._h, self.ncf, self.nnz, ptr(self.iendc, _i64), ptr(self.irow, _i32),
+                                             ptr(emt, _d), float(eav), int(precision), C.byref(self._box[0])))
+        ctx._children.append(self._box)
+        self.eav = float(eav)
+        return self
+
+    @classmethod
+    def packed(cls, ctx: Context, ncf, ap):
+        """A dense block from its lower triangle packed by rows (DNICMV's EMT,
+        gg_hmat_create_packed)."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.ncf = int(ncf)
+        ap = np.ascontiguousarray(ap, np.float64)
+        if ap.size != self.ncf * (self.ncf + 1) // 2:
+            raise ValueError("ap must hold NCF (NCF + 1) / 2 values")
+        r = np.arange(self.ncf, dtype=np.int64)
+        self.iendc = np.concatenate([[0], np.cumsum(r + 1)]).astype(np.int64)
+        self.irow = np.concatenate([np.arange(1, i + 2, dtype=np.int32) for i in range(self.ncf)])
+        self.nnz = int(self.iendc[-1])
+        self._box = [C.c_void_p()]
+        check(_lib.gpu().gg_hmat_create_packed(ctx._h, self.ncf, ptr(ap, _d), C.byref(self._box[0])))
+        ctx._children.append(self._box)
+        self.eav = None
+        return self
+
+    @property
+    def host_precision(self):
+        """The precision a host-resident matrix was built for; None on the device."""
+        p = _lib.gpu().gg_hmat_host_precision(self._h)
+        return None if p < 0 else p
+
+    def spodmv(self, b):
+        """SPODMV: C = (H - EAV) B for a host-resident matrix, in its precision."""
+        b = np.asfortranarray(np.asarray(b, np.float64).reshape(self.ncf, -1))
+        c = np.zeros_like(b, order="F")
+        check(_lib.gpu().gg_spodmv(self.ctx._h, self._h, b.shape[1], ptr(b, _d), ptr(c, _d)))
+        return c
+
+    @classmethod
     def view(cls, src, ctx=None):
         """A matrix sharing src's structure, lists and assembly plan, with its
         own EMT (gg_hmat_create_view): the same block for another ion."""

@@ -1421,6 +1421,7 @@ extern "C" int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *hs, c
     if (!h || nvec[b] < 1 || nvec[b] > MAXR || nvec[b] > h->ncf)
       return fail(GG_ERR_ARG, "gg_maneig_batched: bad block or NVEC (1 <= NVEC <= min(NCF, 16))");
     if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_maneig_batched: EMT not assembled");
+    if (h->host_prec >= 0) return fail(GG_ERR_ARG, "gg_maneig_batched: host-resident blocks are solved by gg_maneig");
     if (h->ctx->device != ctx->device) return fail(GG_ERR_ARG, "gg_maneig_batched: blocks on another device");
     if (h->ncf >= (1 << 30)) return fail(GG_ERR_ARG, "gg_maneig_batched: block too large");
   }

@@ -2619,6 +2619,8 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
   GG_CUDA(cudaSetDevice(ctx->device));
   const int flavour = p ? p->flavour : 0;
   const int precision = p ? p->precision : GG_FP64;
+  if (h->host_prec >= 0 && precision != h->host_prec)
+    return fail(GG_ERR_ARG, "gg_maneig: p->precision must be the host-resident matrix's precision");
   const int ncf = h->ncf;
   int dummy_nl = 0, dummy_nmv = 0, dummy_ierr = 0;
   if (!nloops) nloops = &dummy_nl;
@@ -2681,8 +2683,8 @@ extern "C" int gg_maneig(gg_ctx *ctx, gg_hmat *h, int nvec, const gg_dvd_params 
       h->lead = nullptr;
     }
     if (!h->lead) {
-      GG_TRY(leading_block(h, ns, &h->lead));
-    } else {
+      GG_TRY(h->host_prec >= 0 ? leading_block_host(h, ns, &h->lead) : leading_block(h, ns, &h->lead));
+    } else if (h->host_prec < 0) {
       gg_hmat *b = h->lead;
       GG_CUDA(cudaMemcpyAsync(b->dEmt.p, h->dEmt.p, b->nnz * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
       GG_CUDA(cudaMemcpyAsync(b->dDiag.p, h->dDiag.p, ns * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));

@@ -243,9 +243,18 @@ struct gg_hmat {
   // by stage and precision
   gg_hmat *lead = nullptr;
   std::shared_ptr<void> dvd_cache[4];
+  // a matrix kept in host memory (gg_hmat_create_host): the precision its
+  // symmetric form was built for (-1: the matrix is on the device), the
+  // pinned host arrays the dSym* buffers borrow, and the leading rows
+  // (lower triangle by rows, diagonal shifted) for MANEIG's leading block
+  int host_prec = -1;
+  std::vector<void *> host_bufs;
+  std::vector<int32_t> hLeadIrow;
+  std::vector<double> hLeadEmt;
   ~gg_hmat() {
     for (auto &c : dvd_cache) c.reset();
     delete lead;
+    for (void *p : host_bufs) cudaFreeHost(p);
   }
 };
 
@@ -260,6 +269,9 @@ int timer_start(gg_ctx *ctx);
 int timer_stop(gg_ctx *ctx, double *ms);
 // spmv.cu
 int build_sym(gg_hmat *h);
+// hostmat.cu: the leading ns x ns block of a host-resident matrix as a
+// device matrix
+int leading_block_host(gg_hmat *h, int ns, gg_hmat **out);
 int refresh_sym_values(gg_hmat *h);
 int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s);
 // xs: the split (hi + lo FP32) copy of x to read; null = the matrix's dXs

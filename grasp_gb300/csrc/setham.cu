@@ -492,6 +492,7 @@ int gg_hmat_create_view(gg_ctx *ctx, gg_hmat *src, gg_hmat **out) {
   *out = nullptr;
   gg_hmat *root = src->base ? src->base : src;
   if (root->dead) return fail(GG_ERR_STATE, "gg_hmat_create_view: the source was destroyed");
+  if (root->host_prec >= 0) return fail(GG_ERR_ARG, "gg_hmat_create_view: the source is a host-resident matrix");
   if (ctx->device != root->ctx->device) return fail(GG_ERR_ARG, "gg_hmat_create_view: source on another device");
   // the source's symmetric structure is built once and shared
   GG_TRY(build_sym(root));
@@ -530,6 +531,7 @@ int gg_setham_upload(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *
                      const gg_list *vlists) {
   if (!ctx || !h || h->ctx != ctx || !iq || !tlist || kmaxf < -1 || (kmaxf >= 0 && !vlists))
     return fail(GG_ERR_ARG, "gg_setham_upload: bad arguments");
+  if (h->host_prec >= 0) return fail(GG_ERR_ARG, "gg_setham_upload: a host-resident matrix is not assembled here");
   GG_TRY(ensure_orbitals(ctx));
   GG_CUDA(cudaSetDevice(ctx->device));
   GG_TRY(timer_start(ctx));
@@ -837,6 +839,7 @@ int gg_setham(gg_ctx *ctx, gg_hmat *h, const uint8_t *iq, const gg_list *tlist, 
 int gg_hmat_get_emt(gg_hmat *h, double *emt) {
   if (!h || !emt) return fail(GG_ERR_ARG, "gg_hmat_get_emt: bad arguments");
   if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_hmat_get_emt: EMT not assembled");
+  if (h->host_prec >= 0) return fail(GG_ERR_ARG, "gg_hmat_get_emt: a host-resident matrix keeps no EMT");
   GG_CUDA(cudaSetDevice(h->ctx->device));
   GG_CUDA(cudaMemcpyAsync(emt, h->dEmt.p, h->nnz * sizeof(double), cudaMemcpyDeviceToHost, h->ctx->stream));
   GG_CUDA(cudaStreamSynchronize(h->ctx->stream));
@@ -845,6 +848,7 @@ int gg_hmat_get_emt(gg_hmat *h, double *emt) {
 
 int gg_hmat_set_emt(gg_hmat *h, const double *emt) {
   if (!h || !emt) return fail(GG_ERR_ARG, "gg_hmat_set_emt: bad arguments");
+  if (h->host_prec >= 0) return fail(GG_ERR_ARG, "gg_hmat_set_emt: a host-resident matrix keeps no EMT");
   GG_CUDA(cudaSetDevice(h->ctx->device));
   GG_CUDA(cudaMemcpyAsync(h->dEmt.p, emt, h->nnz * sizeof(double), cudaMemcpyHostToDevice, h->ctx->stream));
   std::vector<double> d(h->ncf);

@@ -438,8 +438,10 @@ struct TuneKey {
   int dev, kernel, m, ncf;
   int64_t nnz;
   bool col16;
+  bool host;  // the matrix in host memory (read over the host link)
   bool operator<(const TuneKey &o) const {
-    return std::tie(dev, kernel, m, ncf, nnz, col16) < std::tie(o.dev, o.kernel, o.m, o.ncf, o.nnz, o.col16);
+    return std::tie(dev, kernel, m, ncf, nnz, col16, host) <
+           std::tie(o.dev, o.kernel, o.m, o.ncf, o.nnz, o.col16, o.host);
   }
 };
 struct TuneEntry {
@@ -450,7 +452,7 @@ std::mutex g_tune_mu;
 std::map<TuneKey, TuneEntry> g_tune;
 
 TuneKey tune_key(const gg_hmat *h, int kernel, int m) {
-  return TuneKey{h->ctx->device, kernel, kernel == 0 ? m : 1, h->ncf, h->sym_nnz, h->sym_col16};
+  return TuneKey{h->ctx->device, kernel, kernel == 0 ? m : 1, h->ncf, h->sym_nnz, h->sym_col16, h->host_prec >= 0};
 }
 
 template <int M, int U>
@@ -612,10 +614,18 @@ int tune_variant(gg_hmat *h, int kernel, int m, cudaStream_t s, int *variant) {
   return GG_OK;
 }
 
+// a host-resident matrix holds the values of one precision only
+int check_precision(const gg_hmat *h, int precision) {
+  if (h->host_prec >= 0 && precision != h->host_prec)
+    return fail(GG_ERR_ARG, "matvec: the host-resident matrix was built for the other precision");
+  return GG_OK;
+}
+
 // y = H x with x = Bbase + c ld, y = ABbase + c ld, c = *dcol on the device;
 // GG_SPLIT reads x from h->dXs (the caller's split copy of the same column)
 int spmv_col(gg_hmat *h, int precision, const double *Bbase, double *ABbase, int64_t ld, const int *dcol,
              const double *skip, cudaStream_t s, const float2 *xs) {
+  GG_TRY(check_precision(h, precision));
   const int n = h->ncf;
   const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
   if (precision == GG_SPLIT) {
@@ -720,6 +730,7 @@ int refresh_sym_values(gg_hmat *h) {
 // y[:, v] = H x[:, v] for v < m (column-major [ncf x m]); stream-ordered.
 // SPLIT with 2 to 16 vectors: one sweep over the matrix for all of them.
 int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStream_t s) {
+  GG_TRY(check_precision(h, precision));
   const int n = h->ncf;
   const unsigned blocks = (unsigned)(((int64_t)n * 32 + 255) / 256);
   if (precision == GG_SPLIT && m >= 2 && m <= 16) return spmm_cols(h, dx, dy, n, m, s);
@@ -747,6 +758,7 @@ int spmv(gg_hmat *h, int precision, const double *dx, double *dy, int m, cudaStr
 int spmm_block(gg_hmat *h, int m, const float2 *xb, const double *Bbase, double *ABbase, int64_t ld,
                const int *dcol, cudaStream_t s) {
   if (m < 1 || m > 16) return fail(GG_ERR_ARG, "spmm_block: 1 to 16 columns");
+  GG_TRY(check_precision(h, GG_SPLIT));
   int v = 0;
   GG_TRY(tune_variant(h, 0, m, s, &v));
   return launch_spmm(h, m, v, xb, Bbase, ABbase, ld, dcol, s);
@@ -836,6 +848,7 @@ extern "C" int gg_hmat_tune(gg_hmat *h, int kernel, int m, int *chosen, int *nva
   if (!h || kernel < 0 || kernel > 1 || (kernel == 0 && (m < 1 || m > 16)))
     return fail(GG_ERR_ARG, "gg_hmat_tune: kernel 0 (m = 1..16) or 1");
   if (!h->emt_valid) return fail(GG_ERR_STATE, "gg_hmat_tune: EMT not set");
+  GG_TRY(check_precision(h, GG_SPLIT));
   GG_CUDA(cudaSetDevice(h->ctx->device));
   GG_TRY(refresh_sym_values(h));
   int v = 0;

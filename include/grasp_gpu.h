@@ -194,6 +194,42 @@ int gg_hmat_set_emt(gg_hmat *h, const double *emt);
 /* SPICMV2 (lib9290/spicmv2.f90:2): C = H B for m host vectors [ncf x m]. */
 int gg_spicmv2(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c, int precision);
 
+/* ---- blocks whose matrix stays off the device (SPODMV, DNICMV) -------------
+ * SPODMV (rci90/spodmv.f90:3): rci's product for a block too large to keep in
+ * memory, which re-reads the lower triangle from rci.res for every product
+ * (rci90/maneig.f90:262-279). gg_hmat_create_host keeps such a block in
+ * pinned host memory instead of HBM: its full symmetric matrix is built once
+ * there, in the form the given precision's product reads (GG_FP64: FP64
+ * values and int32 columns, 12 bytes per stored entry of either triangle;
+ * GG_SPLIT: hi + lo FP32 values and 16-bit columns when NCF <= 65536, 10
+ * bytes), and every product reads it over the host link while the vectors
+ * and the diagonal stay on the device. Results are bit for bit those of the
+ * same matrix on the device (gg_hmat_create + gg_hmat_set_emt with the
+ * shifted diagonal).
+ * iendc/irow as gg_hmat_create; emt[nnz]: the block's values as rci writes
+ * them to rci.res (setham_gg.f90:378), diagonal unshifted; the diagonal used
+ * is EMT(IENDC(i)) - eav, SPODMV's DIAG (spodmv.f90:77). The caller's arrays
+ * are not referenced after the call.
+ * The matrix works with gg_spicmv2 and gg_spodmv, gg_maneig (whose
+ * p->precision must be the matrix's; the leading-block stage runs on a device
+ * copy of the leading rows), gg_matvec_timing, gg_spmm_timing and
+ * gg_hmat_tune in its precision; SETHAM, gg_hmat_get_emt/set_emt,
+ * gg_hmat_create_view and gg_maneig_batched refuse it with GG_ERR_ARG.
+ * gg_hmat_host_precision: the precision a host-resident matrix was built for,
+ * -1 for a matrix on the device.
+ * gg_spodmv: C = (H - EAV) B for m host vectors [ncf x m], in the matrix's
+ * precision (GG_ERR_ARG for a matrix on the device).                        */
+int gg_hmat_create_host(gg_ctx *ctx, int ncf, int64_t nnz, const int64_t *iendc, const int32_t *irow,
+                        const double *emt, double eav, int precision, gg_hmat **out);
+int gg_hmat_host_precision(gg_hmat *h);
+int gg_spodmv(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c);
+/* DNICMV (rci90/dnicmv.f90:3): the product with a dense lower triangle packed
+ * by rows, ap[i(i-1)/2 + j - 1] = A(i, j) for 1 <= j <= i <= ncf (the EMT of
+ * hmat_C with IEND = IEND + ICOL, diagonal last in each row). The matrix gets
+ * the sparse structure with every entry present; gg_spicmv2 on it is
+ * DNICMV's C = A B and gg_maneig solves it like any block.                 */
+int gg_hmat_create_packed(gg_ctx *ctx, int ncf, const double *ap, gg_hmat **out);
+
 /* ---- eigen-solve ------------------------------------------------------------
  * MANEIG (rci90/maneig.f90:3 when flavour = 0, rmcdhf90/maneig.f90:3 when
  * flavour = 1): lowest nvec eigenpairs of the block's H - EAV, dominant

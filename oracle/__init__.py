@@ -87,6 +87,8 @@ def lib():
         L.or_shift_eav.restype = C.c_double
         L.or_shift_eav.argtypes = [C.c_int, _i64, _d]
         L.or_spicmv2.argtypes = [C.c_int, C.c_int, _i64, _i32, _d, _d, _d]
+        L.or_spodmv.argtypes = [C.c_int, C.c_int, _i64, _i32, _d, C.c_double, _d, _d]
+        L.or_dnicmv.argtypes = [C.c_int, C.c_int, _d, _d, _d]
         L.or_dspevx.argtypes = [C.c_int, _d, C.c_int, C.c_int, _d, _d]
         L.or_iniest2.argtypes = [C.c_int, C.c_int, C.c_int, _d, _d, _i64, _i32]
         L.or_gdvd.argtypes = [C.c_int, _i64, _i32, _d, _d, C.POINTER(OrDvdParams), _d, C.c_int64,
@@ -234,6 +236,27 @@ def spicmv2(n, iendc, irow, emt, b):
     iendc = np.ascontiguousarray(iendc, np.int64); irow = np.ascontiguousarray(irow, np.int32)
     emt = np.ascontiguousarray(emt, np.float64)
     lib().or_spicmv2(n, m, _p(iendc, _i64), _p(irow, _i32), _p(emt, _d), _p(b, _d), _p(c, _d))
+    return c
+
+
+def spodmv(n, iendc, irow, emt, eav, b):
+    """SPODMV's C = (H - EAV) B from rows with the diagonal unshifted."""
+    b = np.asfortranarray(b.reshape(n, -1), dtype=np.float64)
+    m = b.shape[1]
+    c = np.zeros((n, m), order="F")
+    iendc = np.ascontiguousarray(iendc, np.int64); irow = np.ascontiguousarray(irow, np.int32)
+    emt = np.ascontiguousarray(emt, np.float64)
+    lib().or_spodmv(n, m, _p(iendc, _i64), _p(irow, _i32), _p(emt, _d), float(eav), _p(b, _d), _p(c, _d))
+    return c
+
+
+def dnicmv(n, ap, b):
+    """DNICMV's C = A B, A's lower triangle packed by rows."""
+    b = np.asfortranarray(b.reshape(n, -1), dtype=np.float64)
+    m = b.shape[1]
+    c = np.zeros((n, m), order="F")
+    ap = np.ascontiguousarray(ap, np.float64)
+    lib().or_dnicmv(n, m, _p(ap, _d), _p(b, _d), _p(c, _d))
     return c
 
 

@@ -1173,6 +1173,55 @@ void or_spicmv2(int n, int m, const int64_t *iendc, const int32_t *irow, const d
   spicmv2(n, m, iendc, irow, emt, b, c, 1);
 }
 
+// SPODMV (rci90/spodmv.f90:65-80): the rows as rci.res holds them (NELC
+// entries, the diagonal EMT(NELC) last and unshifted), DIAG = C(ICOL,IV) +
+// (EMT(NELC) - EAV) B(ICOL,IV), then DMERGE (dmerge.f90:35-40) over the
+// other NELC - 1 entries, C(ICOL,IV) = DIAG + DL.
+void or_spodmv(int n, int m, const int64_t *iendc, const int32_t *irow, const double *emt, double eav,
+               const double *b, double *c) {
+  for (int64_t i = 0; i < (int64_t)n * m; ++i) c[i] = 0.0;
+  for (int icol = 1; icol <= n; ++icol) {
+    const int64_t p0 = iendc[icol - 1], nelc = iendc[icol] - p0;
+    const double *e = emt + p0;
+    const int32_t *ir = irow + p0;
+    for (int iv = 0; iv < m; ++iv) {
+      const double *B = b + (size_t)iv * n;
+      double *C = c + (size_t)iv * n;
+      const double diag = C[icol - 1] + (e[nelc - 1] - eav) * B[icol - 1];
+      const double dconst = B[icol - 1];
+      double dsum = 0.0;
+      for (int64_t i = 0; i < nelc - 1; ++i) {
+        dsum = dsum + e[i] * B[ir[i] - 1];
+        C[ir[i] - 1] = C[ir[i] - 1] + dconst * e[i];
+      }
+      C[icol - 1] = diag + dsum;
+    }
+  }
+}
+
+// DNICMV (rci90/dnicmv.f90:52-64) with DMERGE_DNICMV (:100-104): the lower
+// triangle packed by rows, row ICOL = EMT(IBEG..IEND), IEND = IEND + ICOL;
+// DIAG = C(ICOL,IV) + EMT(IEND) B(ICOL,IV), DL = DOT_PRODUCT(EMT(IBEG..IEND-1),
+// B(1..ICOL-1)), C(1..ICOL-1) += B(ICOL) EMT(IBEG..IEND-1), C(ICOL) = DIAG + DL.
+void or_dnicmv(int n, int m, const double *emt, const double *b, double *c) {
+  for (int64_t i = 0; i < (int64_t)n * m; ++i) c[i] = 0.0;
+  int64_t ibeg = 0;
+  for (int icol = 1; icol <= n; ++icol) {
+    const double *e = emt + ibeg;
+    for (int iv = 0; iv < m; ++iv) {
+      const double *B = b + (size_t)iv * n;
+      double *C = c + (size_t)iv * n;
+      const double diag = C[icol - 1] + e[icol - 1] * B[icol - 1];
+      double dsum = 0.0;
+      for (int i = 0; i < icol - 1; ++i) dsum = dsum + e[i] * B[i];
+      const double dconst = B[icol - 1];
+      for (int i = 0; i < icol - 1; ++i) C[i] = C[i] + dconst * e[i];
+      C[icol - 1] = diag + dsum;
+    }
+    ibeg += icol;
+  }
+}
+
 int or_dspevx(int n, const double *ap, int il, int iu, double *w, double *z) {
   return dspevx_lowest(n, ap, il, iu, w, z);
 }
