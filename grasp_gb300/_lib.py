@@ -65,6 +65,7 @@ GPU_SYMBOLS = {
     "gg_hmat_host_precision": (C.c_int, [C.c_void_p]),
     "gg_spodmv": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, _d, _d]),
     "gg_hmat_create_packed": (C.c_int, [C.c_void_p, C.c_int, _d, C.POINTER(C.c_void_p)]),
+    "gg_host_read_timing": (C.c_int, [C.c_void_p, C.c_size_t, C.c_int, C.c_int, _d]),
     "gg_maneig": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.POINTER(GGDvdParams), _d, _d, _int, _int, _int]),
     "gg_maneig_batched": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), _int, C.POINTER(GGDvdParams), _d,
                                     _d, _int, _int, _int]),

@@ -136,6 +136,13 @@ class Context:
         name = lambda v: _lib.gpu().gg_tune_variant_name(2, v).decode()  # noqa: E731
         return dict(chosen=name(ch.value), ms={name(v): float(ms[v]) for v in range(nv.value)})
 
+    def host_read_timing(self, nbytes, mode=0, iters=10):
+        """ms per pass over a pinned host buffer (gg_host_read_timing): mode 0
+        read by a kernel over the host link, 1 copied by cudaMemcpyAsync."""
+        ms = C.c_double()
+        check(_lib.gpu().gg_host_read_timing(self._h, int(nbytes), int(mode), int(iters), C.byref(ms)))
+        return ms.value
+
     def stage_stat(self, which):
         return _lib.gpu().gg_stage_stat(self._h, which)
 

@@ -134,6 +134,27 @@ int build_host_sym(gg_hmat *h, const int64_t *iendc, const int32_t *irow, const 
   return GG_OK;
 }
 
+// streaming read of n float4 from (host) memory, U loads in flight per
+// thread; one sum per block keeps the loads
+__global__ void __launch_bounds__(256) k_stream_read(const float4 *__restrict__ src, int64_t n,
+                                                     float *__restrict__ sink) {
+  constexpr int U = 4;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  float acc = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += U * stride) {
+    float4 v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int64_t j = i + u * stride;
+      v[u] = j < n ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc += v[u].x + v[u].y + v[u].z + v[u].w;
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(sink + blockIdx.x, acc);
+}
+
 }  // namespace
 
 int leading_block_host(gg_hmat *h, int ns, gg_hmat **out) {
@@ -220,6 +241,47 @@ int gg_hmat_host_precision(gg_hmat *h) {
 int gg_spodmv(gg_ctx *ctx, gg_hmat *h, int m, const double *b, double *c) {
   if (!h || h->host_prec < 0) return fail(GG_ERR_ARG, "gg_spodmv: not a host-resident matrix");
   return gg_spicmv2(ctx, h, m, b, c, h->host_prec);
+}
+
+int gg_host_read_timing(gg_ctx *ctx, size_t bytes, int mode, int iters, double *ms_per_pass) {
+  if (!ctx || bytes < 16 || iters < 1 || (mode != 0 && mode != 1) || !ms_per_pass)
+    return fail(GG_ERR_ARG, "gg_host_read_timing: bad arguments");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  bytes &= ~(size_t)15;
+  void *hp = nullptr;
+  GG_CUDA(cudaHostAlloc(&hp, bytes, cudaHostAllocMapped));
+  std::memset(hp, 0, bytes);
+  void *dp = nullptr;
+  int st = GG_OK;
+  if (cudaHostGetDevicePointer(&dp, hp, 0) != cudaSuccess) st = fail(GG_ERR_CUDA, "gg_host_read_timing: mapping");
+  DBuf<float> sink;
+  DBuf<char> dst;
+  const int blocks = 4 * ctx->sms;
+  if (st == GG_OK) st = sink.alloc(blocks);
+  if (st == GG_OK && mode == 1) st = dst.alloc(bytes);
+  auto pass = [&]() -> int {
+    if (mode == 0) {
+      k_stream_read<<<blocks, 256, 0, ctx->stream>>>(static_cast<const float4 *>(dp), (int64_t)(bytes / 16),
+                                                      sink.p);
+      ::gg::note_launch();
+    } else {
+      GG_CUDA(cudaMemcpyAsync(dst.p, hp, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    GG_CUDA(cudaGetLastError());
+    return GG_OK;
+  };
+  if (st == GG_OK && sink.p) st = cudaMemsetAsync(sink.p, 0, blocks * sizeof(float), ctx->stream) == cudaSuccess
+                                      ? GG_OK : fail(GG_ERR_CUDA, "gg_host_read_timing: memset");
+  if (st == GG_OK) st = pass();  // warm-up
+  if (st == GG_OK) st = timer_start(ctx);
+  for (int it = 0; it < iters && st == GG_OK; ++it) st = pass();
+  double ms = 0;
+  if (st == GG_OK) st = timer_stop(ctx, &ms);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFreeHost(hp);
+  if (st != GG_OK) return st;
+  *ms_per_pass = ms / iters;
+  return GG_OK;
 }
 
 int gg_hmat_create_packed(gg_ctx *ctx, int ncf, const double *ap, gg_hmat **out) {

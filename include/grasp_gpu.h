@@ -395,6 +395,11 @@ int gg_event_record(gg_ctx *ctx, int slot);
 int gg_event_elapsed(gg_ctx *ctx, int a, int b, double *ms);
 int gg_matvec_timing(gg_ctx *ctx, gg_hmat *h, int precision, int iters, double *ms_per_launch, double *alg_bytes);
 int gg_spmm_timing(gg_ctx *ctx, gg_hmat *h, int m, int iters, double *ms_per_launch, double *alg_bytes);
+/* The host link's read rate, the bound of a host-resident matrix's product:
+ * ms per pass over a pinned host buffer of `bytes` (rounded down to 16),
+ * mode 0: read by a streaming kernel (16-byte loads, as the matvec's entries
+ * are read), mode 1: copied to the device by cudaMemcpyAsync.             */
+int gg_host_read_timing(gg_ctx *ctx, size_t bytes, int mode, int iters, double *ms_per_pass);
 
 #ifdef __cplusplus
 }
