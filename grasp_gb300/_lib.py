@@ -23,6 +23,13 @@ class GGList(C.Structure):
     _fields_ = [("nlab", C.c_int64), ("lab", _i32), ("start", _i64), ("loc", _i32), ("coeff", _d)]
 
 
+class GGCof(C.Structure):
+    """gg_cof: one orbital's SETCOF lists (include/grasp_gpu.h)."""
+    _fields_ = [("ny", C.c_int), ("nya", C.POINTER(C.c_int32)), ("ya", C.POINTER(C.c_double)),
+                ("nx", C.c_int), ("nxa", C.POINTER(C.c_int32)), ("xa", C.POINTER(C.c_double)),
+                ("nd", C.c_int), ("nda", C.POINTER(C.c_int32)), ("da", C.POINTER(C.c_double))]
+
+
 class GGDvdParams(C.Structure):
     _fields_ = [
         ("flavour", C.c_int), ("precision", C.c_int), ("lim", C.c_int), ("maxiter", C.c_int),
@@ -48,6 +55,9 @@ GPU_SYMBOLS = {
     "gg_slater": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
     "gg_ypot": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _d]),
     "gg_xpot": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _d, _d]),
+    "gg_cofpot": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(GGCof), C.c_int, _i32, _d, C.c_double, _d,
+                            _d, _d]),
+    "gg_setlag": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _int, C.POINTER(GGCof), _d]),
     "gg_slater_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
     "gg_rinti": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _d]),
     "gg_iabint_table": (C.c_int, [C.c_void_p, _d]),

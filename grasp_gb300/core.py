@@ -15,7 +15,7 @@ import ctypes as C
 import numpy as np
 
 from . import _lib
-from ._lib import GGDvdParams, GGList, _d, _i32, _i64, _int, _u8, check, ptr
+from ._lib import GGCof, GGDvdParams, GGList, _d, _i32, _i64, _int, _u8, check, ptr
 
 FP64 = 0
 SPLIT = 1
@@ -117,6 +117,31 @@ class Context:
         check(_lib.gpu().gg_xpot(self._h, nxa.size, ptr(nxa, _i32), ptr(xa, _d), ptr(xp, _d), ptr(xq, _d)))
         return xp, xq
 
+    def cofpot(self, j, ucfj, cof, iecc=(), ecv=(), accy=0.0):
+        """COFPOT after SETCOF (gg_cofpot): YPOT, XPOT, LAGCON, DACON of
+        orbital j from its lists (dict nya/ya/nxa/xa/nda/da); (YP, XP, XQ)."""
+        keep = []
+        c = _mkcof(cof, keep)
+        iecc = np.ascontiguousarray(iecc, np.int32); ecv = np.ascontiguousarray(ecv, np.float64)
+        n = self.n
+        yp, xp, xq = np.zeros(n), np.zeros(n), np.zeros(n)
+        check(_lib.gpu().gg_cofpot(self._h, int(j), float(ucfj), C.byref(c), iecc.size, ptr(iecc, _i32),
+                                   ptr(ecv, _d), float(accy), ptr(yp, _d), ptr(xp, _d), ptr(xq, _d)))
+        return yp, xp, xq
+
+    def setlag(self, iecc, ucf, lfix, cofs):
+        """SETLAG's multipliers (gg_setlag) for the pairs iecc[k] = LI + 215 LJ;
+        cofs[orbital - 1] = that orbital's lists (None for orbitals in no pair)."""
+        keep = []
+        empty = {}
+        arr = (GGCof * len(cofs))(*[_mkcof(c if c is not None else empty, keep) for c in cofs])
+        iecc = np.ascontiguousarray(iecc, np.int32); ucf = np.ascontiguousarray(ucf, np.float64)
+        lfix = np.ascontiguousarray(lfix, np.int32)
+        ecv = np.zeros(iecc.size)
+        check(_lib.gpu().gg_setlag(self._h, iecc.size, ptr(iecc, _i32), ptr(ucf, _d), ptr(lfix, _int), arr,
+                                   ptr(ecv, _d)))
+        return ecv
+
     def rinti(self, j, k, mode=0):
         out = C.c_double()
         check(_lib.gpu().gg_rinti(self._h, j, k, mode, C.byref(out)))
@@ -158,6 +183,16 @@ class Context:
 
     def synchronize(self):
         check(_lib.gpu().gg_ctx_synchronize(self._h))
+
+
+def _mkcof(d, keep):
+    arrs = [np.ascontiguousarray(d.get(k, []), t) for k, t in
+            (("nya", np.int32), ("ya", np.float64), ("nxa", np.int32), ("xa", np.float64),
+             ("nda", np.int32), ("da", np.float64))]
+    keep.extend(arrs)
+    nya, ya, nxa, xa, nda, da = arrs
+    return GGCof(nya.size, ptr(nya, _i32), ptr(ya, _d), nxa.size, ptr(nxa, _i32), ptr(xa, _d),
+                 nda.size, ptr(nda, _i32), ptr(da, _d))
 
 
 def _mklist(d, keep):

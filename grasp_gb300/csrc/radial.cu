@@ -904,32 +904,144 @@ __global__ void k_potential(int mode, int ncof, const int *__restrict__ fidx, co
   }
 }
 
-// DPBDT (lib9290/dpbdt.f90:39-99): 13-point derivative of orbital J (per
-// grid index) into dP, dQ (1-based).
+// DPBDT (lib9290/dpbdt.f90:39-99): 13-point derivative of orbital J at grid
+// index i (1-based): the end rows from the 13 x 13 table, the interior by the
+// antisymmetric 12-neighbour formula.
+__device__ __forceinline__ void dpbdt_point(const double *PF, const double *QF, int ld, int J, const QuadConst &q,
+                                            int i, double &hp, double &hq) {
+  const int N = q.n;
+  hp = 0.0;
+  hq = 0.0;
+  if (i <= 6) {
+    for (int k = 1; k <= 13; ++k) hp = hp + q.A13[i - 1][k - 1] * pf(PF, ld, k, J);
+    for (int k = 1; k <= 13; ++k) hq = hq + q.A13[i - 1][k - 1] * pf(QF, ld, k, J);
+  } else if (i <= N - 6) {
+    const double A1 = q.A13[6][0], A2 = q.A13[6][1], A3 = q.A13[6][2], A4 = q.A13[6][3], A5 = q.A13[6][4],
+                 A6 = q.A13[6][5];
+    hp = A1 * (pf(PF, ld, i - 6, J) - pf(PF, ld, i + 6, J)) + A2 * (pf(PF, ld, i - 5, J) - pf(PF, ld, i + 5, J)) +
+         A3 * (pf(PF, ld, i - 4, J) - pf(PF, ld, i + 4, J)) + A4 * (pf(PF, ld, i - 3, J) - pf(PF, ld, i + 3, J)) +
+         A5 * (pf(PF, ld, i - 2, J) - pf(PF, ld, i + 2, J)) + A6 * (pf(PF, ld, i - 1, J) - pf(PF, ld, i + 1, J));
+    hq = A1 * (pf(QF, ld, i - 6, J) - pf(QF, ld, i + 6, J)) + A2 * (pf(QF, ld, i - 5, J) - pf(QF, ld, i + 5, J)) +
+         A3 * (pf(QF, ld, i - 4, J) - pf(QF, ld, i + 4, J)) + A4 * (pf(QF, ld, i - 3, J) - pf(QF, ld, i + 3, J)) +
+         A5 * (pf(QF, ld, i - 2, J) - pf(QF, ld, i + 2, J)) + A6 * (pf(QF, ld, i - 1, J) - pf(QF, ld, i + 1, J));
+  } else {
+    const int irow = i - N + 13;
+    for (int k = 1; k <= 13; ++k) hp = hp + q.A13[irow - 1][k - 1] * pf(PF, ld, N - 13 + k, J);
+    for (int k = 1; k <= 13; ++k) hq = hq + q.A13[irow - 1][k - 1] * pf(QF, ld, N - 13 + k, J);
+  }
+}
+
+// DPBDT of orbital J at every grid index into dP, dQ (1-based), by the lanes
+// of a warp
 __device__ void dpbdt_warp(const double *PF, const double *QF, int ld, int J, const QuadConst &q, double *dP,
                            double *dQ, int lane) {
-  const int N = q.n;
-  const double A1 = q.A13[6][0], A2 = q.A13[6][1], A3 = q.A13[6][2], A4 = q.A13[6][3], A5 = q.A13[6][4],
-               A6 = q.A13[6][5];
-  for (int i = 1 + lane; i <= N; i += 32) {
-    double hp = 0.0, hq = 0.0;
-    if (i <= 6) {
-      for (int k = 1; k <= 13; ++k) hp = hp + q.A13[i - 1][k - 1] * pf(PF, ld, k, J);
-      for (int k = 1; k <= 13; ++k) hq = hq + q.A13[i - 1][k - 1] * pf(QF, ld, k, J);
-    } else if (i <= N - 6) {
-      hp = A1 * (pf(PF, ld, i - 6, J) - pf(PF, ld, i + 6, J)) + A2 * (pf(PF, ld, i - 5, J) - pf(PF, ld, i + 5, J)) +
-           A3 * (pf(PF, ld, i - 4, J) - pf(PF, ld, i + 4, J)) + A4 * (pf(PF, ld, i - 3, J) - pf(PF, ld, i + 3, J)) +
-           A5 * (pf(PF, ld, i - 2, J) - pf(PF, ld, i + 2, J)) + A6 * (pf(PF, ld, i - 1, J) - pf(PF, ld, i + 1, J));
-      hq = A1 * (pf(QF, ld, i - 6, J) - pf(QF, ld, i + 6, J)) + A2 * (pf(QF, ld, i - 5, J) - pf(QF, ld, i + 5, J)) +
-           A3 * (pf(QF, ld, i - 4, J) - pf(QF, ld, i + 4, J)) + A4 * (pf(QF, ld, i - 3, J) - pf(QF, ld, i + 3, J)) +
-           A5 * (pf(QF, ld, i - 2, J) - pf(QF, ld, i + 2, J)) + A6 * (pf(QF, ld, i - 1, J) - pf(QF, ld, i + 1, J));
-    } else {
-      const int irow = i - N + 13;
-      for (int k = 1; k <= 13; ++k) hp = hp + q.A13[irow - 1][k - 1] * pf(PF, ld, N - 13 + k, J);
-      for (int k = 1; k <= 13; ++k) hq = hq + q.A13[irow - 1][k - 1] * pf(QF, ld, N - 13 + k, J);
-    }
+  for (int i = 1 + lane; i <= q.n; i += 32) {
+    double hp, hq;
+    dpbdt_point(PF, QF, ld, J, q, i, hp, hq);
     dP[i] = hp;
     dQ[i] = hq;
+  }
+}
+
+// LAGCON (rmcdhf90/lagcon.f90:46-55): per multiplier in list order,
+// XP(I) = XP(I) + WARI QF(I,M), XQ(I) = XQ(I) - WARI PF(I,M), WARI = WA R(I),
+// I = 1..MF(M); mo[t] = M and wa[t] = ECV WB of the multipliers the host kept
+// (those of pairs with this orbital, |WA| >= EPS). xp, xq 0-based.
+__global__ void k_lagcon(int n, int nt, const int *__restrict__ mo, const double *__restrict__ wa,
+                         const int *__restrict__ MF, const double *__restrict__ R, const double *__restrict__ PF,
+                         const double *__restrict__ QF, int ld, double *__restrict__ xp, double *__restrict__ xq) {
+  for (int i = 1 + blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+    double p = xp[i - 1], qv = xq[i - 1];
+    for (int t = 0; t < nt; ++t) {
+      const int M = mo[t];
+      if (i > MF[M]) continue;
+      const double wari = wa[t] * R[i];
+      p = p + wari * pf(QF, ld, i, M);
+      qv = qv - wari * pf(PF, ld, i, M);
+    }
+    xp[i - 1] = p;
+    xq[i - 1] = qv;
+  }
+}
+
+// DACON (rmcdhf90/dacon.f90:25-46): per entry of the list in order, with TA,
+// TB = DPBDT(IORB) at the point, for I = 2..MF(IORB):
+//   XP(I) += COEFF (TA RPORII + FK PFI - (2C R(I) + ZBCI) QFI),
+//   XQ(I) += COEFF (TB RPORII - FK QFI + ZBCI PFI),
+// RPORII = 1/(H RPOR(I)), ZBCI = ZZ(I)/C, FK = kappa(IORB). xp, xq 0-based.
+__global__ void k_dacon(int n, int nd, const int *__restrict__ nda, const double *__restrict__ da,
+                        const int *__restrict__ NAK, const int *__restrict__ MF, const double *__restrict__ R,
+                        const double *__restrict__ RPOR, const double *__restrict__ ZZ, const double *__restrict__ PF,
+                        const double *__restrict__ QF, int ld, QuadConst q, double *__restrict__ xp,
+                        double *__restrict__ xq) {
+  const double twoc = q.c + q.c;
+  for (int i = 2 + blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
+    double p = xp[i - 1], qv = xq[i - 1];
+    for (int t = 0; t < nd; ++t) {
+      const int io = nda[t];
+      if (i > MF[io]) continue;
+      double ta, tb;
+      dpbdt_point(PF, QF, ld, io, q, i, ta, tb);
+      const double coeff = da[t], fk = (double)NAK[io];
+      const double rporii = 1.0 / (q.h * RPOR[i]);
+      const double pfi = pf(PF, ld, i, io), qfi = pf(QF, ld, i, io);
+      const double zbci = ZZ[i] / q.c;
+      p = p + coeff * (ta * rporii + fk * pfi - (twoc * R[i] + zbci) * qfi);
+      qv = qv + coeff * (tb * rporii - fk * qfi + zbci * pfi);
+    }
+    xp[i - 1] = p;
+    xq[i - 1] = qv;
+  }
+}
+
+// SETLAG's quadrature (rmcdhf90/setlag.f90:177-219), one block per pair
+// {J, M, case, MTP}: TA(I), I = 2..MTP, from the two orbitals' potentials
+// (pot + 3 n slot: YP, XP, XQ, 0-based), then QUAD by thread 0. case 0: M
+// fixed; 1: J fixed; 2: occupations more than 10 % apart; 3: otherwise.
+__global__ void k_setlag_quad(const int4 *__restrict__ pj, const int2 *__restrict__ slots,
+                              const double *__restrict__ pot, int n, const double *__restrict__ PF,
+                              const double *__restrict__ QF, int ld, const double *__restrict__ R,
+                              const double *__restrict__ RP, const double *__restrict__ RPOR, QuadConst q, int np,
+                              double *__restrict__ TAall, double *__restrict__ result) {
+  const int4 w = pj[blockIdx.x];
+  const int J = w.x, M = w.y, cs = w.z, mtp = w.w;
+  const double *ypj = pot + (size_t)3 * n * slots[blockIdx.x].x, *xpj = ypj + n, *xqj = xpj + n;
+  const double *ypm = pot + (size_t)3 * n * slots[blockIdx.x].y, *xpm = ypm + n, *xqm = xpm + n;
+  double *TA = TAall + (size_t)blockIdx.x * np;
+  const double C = q.c;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) {
+    double v = 0.0;
+    if (i >= 2 && i <= mtp) {
+      const double pj_ = pf(PF, ld, i, J), qj = pf(QF, ld, i, J), pm = pf(PF, ld, i, M), qm = pf(QF, ld, i, M);
+      if (cs == 0)
+        v = RPOR[i] * ((pm * xqj[i - 1] - qm * xpj[i - 1]) * C + (pm * pj_ + qm * qj) * ypj[i - 1]);
+      else if (cs == 1)
+        v = RPOR[i] * ((pj_ * xqm[i - 1] - qj * xpm[i - 1]) * C + (pj_ * pm + qj * qm) * ypm[i - 1]);
+      else if (cs == 2)
+        v = RPOR[i] * ((pm * xqj[i - 1] - qm * xpj[i - 1] - pj_ * xqm[i - 1] + qj * xpm[i - 1]) * C +
+                       (ypj[i - 1] - ypm[i - 1]) * (pm * pj_ + qm * qj));
+      else
+        v = RPOR[i] * ((pm * xqj[i - 1] - qm * xpj[i - 1] + pj_ * xqm[i - 1] - qj * xpm[i - 1]) * C +
+                       (ypj[i - 1] + ypm[i - 1]) * (pm * pj_ + qm * qj));
+    }
+    TA[i] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) result[blockIdx.x] = quad_seq(TA, mtp, R, RP, q);
+}
+
+// ECV from the pair's quadrature and RINTI (setlag.f90:184, 194, 205, 218)
+__global__ void k_setlag_final(int np_, const int4 *__restrict__ pj, const double2 *__restrict__ ucf,
+                               const double *__restrict__ result, const double *__restrict__ rijm,
+                               double *__restrict__ ecv) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= np_) return;
+  const double uj = ucf[t].x, um = ucf[t].y;
+  switch (pj[t].z) {
+    case 0: ecv[t] = (result[t] - rijm[t]) * uj; break;
+    case 1: ecv[t] = (result[t] - rijm[t]) * um; break;
+    case 2: ecv[t] = result[t] / (1.0 / uj - 1.0 / um); break;
+    default: ecv[t] = (result[t] - 2.0 * rijm[t]) / (1.0 / uj + 1.0 / um); break;
   }
 }
 
@@ -1455,31 +1567,41 @@ int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out) {
 }  // extern "C"
 
 
+extern "C" {
+static int run_rinti(gg_ctx *ctx, const std::vector<int2> &jk, int mode, double *dOut, const std::vector<int> *outidx);
+}
+
 // YPOT / XPOT on the device: the list's distinct Y^k_ab (every grid point,
-// YZK's TB), then k_potential.
-static int potential(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const double *co, double *out0,
-                     double *out1) {
-  GG_TRY(ensure_orbitals(ctx));
-  Orbitals &o = ctx->orb;
-  Grid &g = ctx->grid;
+// YZK's TB), then k_potential. A term list of one potential: per entry the
+// index of its Y function, the orbital it multiplies (XPOT) and COEFF.
+struct PotTerms {
+  std::vector<int> fidx, iorb;
+  std::vector<double> coef;
+};
+using YKey = std::map<std::tuple<int, int, int>, int>;
+
+// parses a YPOT (mode 0: NYA = (IOY2 KEY + IOY1) KEY + K) or XPOT (mode 1:
+// NXA = ((IORB KEY + IOY2) KEY + IOY1) KEY + K) list, adding its distinct Y
+// functions to hy (shared by all lists of one call)
+static int parse_terms(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const double *co, YKey &seen,
+                       std::vector<YDesc> &hy, PotTerms &t) {
+  const Orbitals &o = ctx->orb;
+  const Grid &g = ctx->grid;
   const int nw = o.nw;
-  if (ncof < 0 || (ncof > 0 && (!lab || !co)) || !out0 || (mode == 1 && !out1))
-    return fail(GG_ERR_ARG, "gg_ypot/gg_xpot: bad arguments");
-  GG_CUDA(cudaSetDevice(ctx->device));
-  std::vector<YDesc> hy;
-  std::vector<int> fidx(std::max(ncof, 1)), iorb(std::max(ncof, 1), 1);
-  std::vector<double> coef(std::max(ncof, 1));
-  std::map<std::tuple<int, int, int>, int> seen;
-  for (int t = 0; t < ncof; ++t) {
-    int64_t l = lab[t];
+  if (ncof < 0 || (ncof > 0 && (!lab || !co))) return fail(GG_ERR_ARG, "potential: bad coefficient list");
+  t.fidx.assign(ncof, 0);
+  t.iorb.assign(ncof, 1);
+  t.coef.assign(ncof, 0.0);
+  for (int e = 0; e < ncof; ++e) {
+    int64_t l = lab[e];
     const int k = (int)(l % KEYORB);
     l /= KEYORB;
     const int a = (int)(l % KEYORB);
     l /= KEYORB;
     const int b = (int)(mode == 0 ? l : l % KEYORB);
     const int io = (mode == 0) ? 1 : (int)(l / KEYORB);
-    if (lab[t] < 0 || k > KLIMIT || a < 1 || a > nw || b < 1 || b > nw || io < 1 || io > nw)
-      return fail(GG_ERR_ARG, "gg_ypot/gg_xpot: label outside the orbital set or K above 20");
+    if (lab[e] < 0 || k > KLIMIT || a < 1 || a > nw || b < 1 || b > nw || io < 1 || io > nw)
+      return fail(GG_ERR_ARG, "potential: label outside the orbital set or K above 20");
     auto it = seen.find({k, a, b});
     if (it == seen.end()) {
       YDesc y;
@@ -1493,30 +1615,111 @@ static int potential(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const 
       it = seen.emplace(std::make_tuple(k, a, b), (int)hy.size()).first;
       hy.push_back(y);
     }
-    fidx[t] = it->second;
-    iorb[t] = io;
-    coef[t] = (mode == 0) ? co[t] : co[t] / g.c;  // XPOT: COEFF = COEFF/C
+    t.fidx[e] = it->second;
+    t.iorb[e] = io;
+    t.coef[e] = (mode == 0) ? co[e] : co[e] / g.c;  // XPOT: COEFF = COEFF/C
   }
-  const int nf = std::max(1, (int)hy.size());
-  if (hy.empty()) hy.push_back(YDesc{0, 1, 1, 2, 2, 0, 1});  // no terms: the loop below adds none
+  return GG_OK;
+}
+
+// One orbital's potentials on the device: YP, XP, XQ (N each, 0-based) at
+// out, out + n, out + 2 n.
+struct PotJob {
+  PotTerms y, x;
+  std::vector<int> nda;
+  std::vector<double> da;
+  std::vector<int> lag_m;      // LAGCON: the pairs' other orbitals
+  std::vector<double> lag_wa;  // and their weights ECV WB
+};
+
+// the jobs' YPOT, XPOT, then LAGCON and DACON, into dPot (3 n per job): all
+// Y functions of all lists built once
+static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vector<YDesc> &hy,
+                          DBuf<double> &dPot) {
+  Orbitals &o = ctx->orb;
+  Grid &g = ctx->grid;
+  cudaStream_t s = ctx->stream;
+  const int n = g.n, nf = std::max(1, (int)hy.size());
+  if (hy.empty()) hy.push_back(YDesc{0, 1, 1, 2, 2, 0, 1});  // no terms: no function is read
   DBuf<YDesc> dy;
-  DBuf<int> dfi, dio;
-  DBuf<double> dco, dY, scratch, d0, d1;
-  GG_TRY(upload(dy, hy, ctx->stream));
-  GG_TRY(upload(dfi, fidx, ctx->stream));
-  GG_TRY(upload(dio, iorb, ctx->stream));
-  GG_TRY(upload(dco, coef, ctx->stream));
+  DBuf<double> dY, scratch;
+  GG_TRY(upload(dy, hy, s));
   GG_TRY(dY.alloc((size_t)nf * g.np));
-  GG_TRY(d0.alloc(g.n));
-  if (mode == 1) GG_TRY(d1.alloc(g.n));
   GG_TRY(build_y(ctx, dy.p, nf, dY.p, scratch));
-  k_potential<<<(g.n + 127) / 128, 128, 0, ctx->stream>>>(mode, ncof, dfi.p, dco.p, dio.p, dY.p, g.np, g.dZZ.p,
-                                                           o.dPF.p, o.dQF.p, o.ld, g.n, d0.p, d1.p);
-  ::gg::note_launch();
+  GG_TRY(dPot.alloc((size_t)3 * n * std::max<size_t>(1, jobs.size())));
+  // every job's integer and coefficient arrays in one upload each
+  std::vector<int> ih;
+  std::vector<double> dh;
+  struct Off { size_t yf, yc, xf, xi, xc, dn, dd, lm, lw; };
+  std::vector<Off> off(jobs.size());
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const PotJob &J = jobs[j];
+    auto pi = [&](const std::vector<int> &v) { size_t at = ih.size(); ih.insert(ih.end(), v.begin(), v.end()); ih.push_back(0); return at; };
+    auto pd = [&](const std::vector<double> &v) { size_t at = dh.size(); dh.insert(dh.end(), v.begin(), v.end()); dh.push_back(0.0); return at; };
+    off[j] = Off{pi(J.y.fidx), pd(J.y.coef), pi(J.x.fidx), pi(J.x.iorb), pd(J.x.coef), pi(J.nda), pd(J.da),
+                 pi(J.lag_m), pd(J.lag_wa)};
+  }
+  DBuf<int> di;
+  DBuf<double> dd;
+  GG_TRY(upload(di, ih, s));
+  GG_TRY(upload(dd, dh, s));
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const PotJob &J = jobs[j];
+    double *yp = dPot.p + (size_t)3 * n * j, *xp = yp + n, *xq = xp + n;
+    k_potential<<<blocks, 128, 0, s>>>(0, (int)J.y.fidx.size(), di.p + off[j].yf, dd.p + off[j].yc, di.p, dY.p,
+                                       g.np, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, yp, nullptr);
+    k_potential<<<blocks, 128, 0, s>>>(1, (int)J.x.fidx.size(), di.p + off[j].xf, dd.p + off[j].xc,
+                                       di.p + off[j].xi, dY.p, g.np, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, xp, xq);
+    ::gg::note_launch();
+    ::gg::note_launch();
+    if (!J.lag_m.empty()) {
+      k_lagcon<<<blocks, 128, 0, s>>>(n, (int)J.lag_m.size(), di.p + off[j].lm, dd.p + off[j].lw, o.dMF.p, g.dR.p,
+                                      o.dPF.p, o.dQF.p, o.ld, xp, xq);
+      ::gg::note_launch();
+    }
+    if (!J.nda.empty()) {
+      k_dacon<<<blocks, 128, 0, s>>>(n, (int)J.nda.size(), di.p + off[j].dn, dd.p + off[j].dd, o.dNAK.p, o.dMF.p,
+                                     g.dR.p, g.dRPOR.p, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, g.q, xp, xq);
+      ::gg::note_launch();
+    }
+  }
   GG_CUDA(cudaGetLastError());
-  GG_CUDA(cudaMemcpyAsync(out0, d0.p, g.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  if (mode == 1) GG_CUDA(cudaMemcpyAsync(out1, d1.p, g.n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  GG_CUDA(cudaStreamSynchronize(ctx->stream));
+  GG_CUDA(cudaStreamSynchronize(s));  // the uploads and scratch are freed on return
+  return GG_OK;
+}
+
+static int potential(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const double *co, double *out0,
+                     double *out1) {
+  GG_TRY(ensure_orbitals(ctx));
+  if (!out0 || (mode == 1 && !out1)) return fail(GG_ERR_ARG, "gg_ypot/gg_xpot: bad arguments");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  std::vector<YDesc> hy;
+  YKey seen;
+  std::vector<PotJob> jobs(1);
+  GG_TRY(parse_terms(ctx, mode, ncof, lab, co, seen, hy, mode == 0 ? jobs[0].y : jobs[0].x));
+  DBuf<double> pot;
+  GG_TRY(run_potentials(ctx, jobs, hy, pot));
+  const int n = ctx->grid.n;
+  if (mode == 0) {
+    GG_CUDA(cudaMemcpy(out0, pot.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+  } else {
+    GG_CUDA(cudaMemcpy(out0, pot.p + n, n * sizeof(double), cudaMemcpyDeviceToHost));
+    GG_CUDA(cudaMemcpy(out1, pot.p + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return GG_OK;
+}
+
+// one orbital's SETCOF lists as a job (DACON's list checked here)
+static int cof_job(gg_ctx *ctx, const gg_cof *c, YKey &seen, std::vector<YDesc> &hy, PotJob &J) {
+  if (!c) return fail(GG_ERR_ARG, "potential: missing coefficient lists");
+  GG_TRY(parse_terms(ctx, 0, c->ny, c->nya, c->ya, seen, hy, J.y));
+  GG_TRY(parse_terms(ctx, 1, c->nx, c->nxa, c->xa, seen, hy, J.x));
+  if (c->nd < 0 || (c->nd > 0 && (!c->nda || !c->da))) return fail(GG_ERR_ARG, "potential: bad DACON list");
+  J.nda.assign(c->nda, c->nda + std::max(0, c->nd));
+  J.da.assign(c->da, c->da + std::max(0, c->nd));
+  for (int io : J.nda)
+    if (io < 1 || io > ctx->orb.nw) return fail(GG_ERR_ARG, "potential: DACON orbital outside the orbital set");
   return GG_OK;
 }
 
@@ -1530,6 +1733,124 @@ int gg_ypot(gg_ctx *ctx, int ncof, const int32_t *nya, const double *ya, double 
 int gg_xpot(gg_ctx *ctx, int ncof, const int32_t *nxa, const double *xa, double *xp, double *xq) {
   if (!ctx) return fail(GG_ERR_ARG, "gg_xpot: no context");
   return potential(ctx, 1, ncof, nxa, xa, xp, xq);
+}
+
+int gg_cofpot(gg_ctx *ctx, int j, double ucfj, const gg_cof *cof, int nec, const int32_t *iecc, const double *ecv,
+              double accy, double *yp, double *xp, double *xq) {
+  if (!ctx || !cof || !yp || !xp || !xq || nec < 0 || (nec > 0 && (!iecc || !ecv)))
+    return fail(GG_ERR_ARG, "gg_cofpot: bad arguments");
+  GG_TRY(ensure_orbitals(ctx));
+  const int nw = ctx->orb.nw;
+  if (j < 1 || j > nw) return fail(GG_ERR_ARG, "gg_cofpot: orbital outside the orbital set");
+  GG_CUDA(cudaSetDevice(ctx->device));
+  std::vector<YDesc> hy;
+  YKey seen;
+  std::vector<PotJob> jobs(1);
+  GG_TRY(cof_job(ctx, cof, seen, hy, jobs[0]));
+  // LAGCON's host part (lagcon.f90:32-45): the pairs with J and their weights
+  if (nec > 0) {
+    const double eps = (accy > 0 ? accy : std::pow(ctx->grid.h, 6)) * 0.01;
+    const double wb = 1.0 / (ucfj * ctx->grid.c) / 1.0;
+    for (int k = 0; k < nec; ++k) {
+      const int l1 = iecc[k] / KEYORB, l2 = iecc[k] - KEYORB * l1;
+      int m;
+      if (j == l1)
+        m = l2;
+      else if (j == l2)
+        m = l1;
+      else
+        continue;
+      if (m < 1 || m > nw) return fail(GG_ERR_ARG, "gg_cofpot: multiplier pair outside the orbital set");
+      const double wa = ecv[k] * wb;
+      if (std::fabs(wa) < eps) continue;
+      jobs[0].lag_m.push_back(m);
+      jobs[0].lag_wa.push_back(wa);
+    }
+  }
+  DBuf<double> pot;
+  GG_TRY(run_potentials(ctx, jobs, hy, pot));
+  const int n = ctx->grid.n;
+  GG_CUDA(cudaMemcpy(yp, pot.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+  GG_CUDA(cudaMemcpy(xp, pot.p + n, n * sizeof(double), cudaMemcpyDeviceToHost));
+  GG_CUDA(cudaMemcpy(xq, pot.p + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+  return GG_OK;
+}
+
+int gg_setlag(gg_ctx *ctx, int nec, const int32_t *iecc, const double *ucf, const int *lfix, const gg_cof *cof,
+              double *ecv) {
+  if (!ctx || nec < 0 || (nec > 0 && (!iecc || !ucf || !lfix || !cof || !ecv)))
+    return fail(GG_ERR_ARG, "gg_setlag: bad arguments");
+  if (nec == 0) return GG_OK;
+  GG_TRY(ensure_orbitals(ctx));
+  const Orbitals &o = ctx->orb;
+  Grid &g = ctx->grid;
+  const int nw = o.nw;
+  GG_CUDA(cudaSetDevice(ctx->device));
+  // the pairs (setlag.f90:146-149: M = IECC / KEY, J = IECC - KEY M), one
+  // potential job per orbital named in a pair
+  std::vector<int> slot(nw + 1, -1), orbs;
+  std::vector<int4> pj(nec);
+  std::vector<int2> ps(nec);
+  std::vector<double2> uc(nec);
+  std::vector<int2> rjk;
+  std::vector<int> ridx;
+  for (int k = 0; k < nec; ++k) {
+    const int M = iecc[k] / KEYORB, J = iecc[k] - KEYORB * M;
+    if (J < 1 || J > nw || M < 1 || M > nw) return fail(GG_ERR_ARG, "gg_setlag: pair outside the orbital set");
+    if (o.nak[J] != o.nak[M]) return fail(GG_ERR_KAPPA, "gg_setlag: pair with different kappa (RINTI)");
+    for (int x : {J, M})
+      if (slot[x] < 0) {
+        slot[x] = (int)orbs.size();
+        orbs.push_back(x);
+      }
+    const double uj = ucf[J - 1], um = ucf[M - 1];
+    int cs;
+    if (lfix[M - 1]) {
+      cs = 0;
+    } else if (lfix[J - 1]) {
+      cs = 1;
+    } else {
+      const double qdif = std::fabs((uj - um) / std::max(uj, um));
+      cs = (qdif > 1.0e-01) ? 2 : 3;
+    }
+    pj[k] = make_int4(J, M, cs, std::max(o.mf[J], o.mf[M]));
+    ps[k] = make_int2(slot[J], slot[M]);
+    uc[k] = make_double2(uj, um);
+    if (cs != 2) {  // RINTI(M, J, 1), or RINTI(J, M, 1) when J is fixed
+      rjk.push_back(cs == 1 ? make_int2(J, M) : make_int2(M, J));
+      ridx.push_back(k);
+    }
+  }
+  std::vector<YDesc> hy;
+  YKey seen;
+  std::vector<PotJob> jobs(orbs.size());
+  for (size_t i = 0; i < orbs.size(); ++i) GG_TRY(cof_job(ctx, &cof[orbs[i] - 1], seen, hy, jobs[i]));
+  DBuf<double> pot;
+  GG_TRY(run_potentials(ctx, jobs, hy, pot));
+  cudaStream_t s = ctx->stream;
+  DBuf<int4> dpj;
+  DBuf<int2> dps;
+  DBuf<double2> duc;
+  DBuf<double> dTA, dres, drij, decv;
+  GG_TRY(upload(dpj, pj, s));
+  GG_TRY(upload(dps, ps, s));
+  GG_TRY(upload(duc, uc, s));
+  GG_TRY(dTA.alloc((size_t)nec * g.np));
+  GG_TRY(dres.alloc(nec));
+  GG_TRY(drij.alloc(nec));
+  GG_TRY(decv.alloc(nec));
+  GG_CUDA(cudaMemsetAsync(drij.p, 0, nec * sizeof(double), s));
+  k_setlag_quad<<<nec, 128, 0, s>>>(dpj.p, dps.p, pot.p, g.n, o.dPF.p, o.dQF.p, o.ld, g.dR.p, g.dRP.p, g.dRPOR.p,
+                                    g.q, g.np, dTA.p, dres.p);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  if (!rjk.empty()) GG_TRY(run_rinti(ctx, rjk, 1, drij.p, &ridx));
+  k_setlag_final<<<(nec + 127) / 128, 128, 0, s>>>(nec, dpj.p, duc.p, dres.p, drij.p, decv.p);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  GG_CUDA(cudaMemcpyAsync(ecv, decv.p, nec * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  return GG_OK;
 }
 
 }  // extern "C"

@@ -121,6 +121,37 @@ int gg_slater(gg_ctx *ctx, int ia, int ib, int ic, int id, int k, double *out);
  * K > 20 (YZK's KLIMIT).                                                    */
 int gg_ypot(gg_ctx *ctx, int ncof, const int32_t *nya, const double *ya, double *yp);
 int gg_xpot(gg_ctx *ctx, int ncof, const int32_t *nxa, const double *xa, double *xp, double *xq);
+/* The three coefficient lists SETCOF (rmcdhf90/setcof.f90) leaves in scf_C
+ * for one orbital: YPOT's (NYCOF, NYA, YA), XPOT's (NXCOF, NXA, XA) and
+ * DACON's (NDCOF, NDA, DA; NDA = orbital index, 1-based).                  */
+typedef struct {
+  int ny;
+  const int32_t *nya;
+  const double *ya;
+  int nx;
+  const int32_t *nxa;
+  const double *xa;
+  int nd;
+  const int32_t *nda;
+  const double *da;
+} gg_cof;
+/* gg_cofpot: COFPOT (rmcdhf90/cofpot.f90:29-33) after its SETCOF: YPOT,
+ * XPOT, LAGCON (lagcon.f90:32-56, one process) and DACON (dacon.f90:25-46)
+ * for orbital j (1-based) with UCF(J) = ucfj. The Lagrange multipliers are
+ * lagr_C's: nec pairs iecc[k] = LI + 215 LJ with values ecv[k] (nec = 0: no
+ * LAGCON term). accy: def_C's ACCY (<= 0: H^6, its default); LAGCON skips a
+ * multiplier whose weight is below 0.01 ACCY. yp, xp, xq: N doubles each.
+ * gg_setlag: SETLAG's multipliers (rmcdhf90/setlag.f90:127-223) for the nec
+ * pairs of iecc (as above; the orbitals of a pair have the same kappa): each
+ * orbital named in a pair gets its potentials (YPOT, XPOT, DACON) from its
+ * lists cof[orbital - 1] once, then ecv[k] from the pair's quadrature and
+ * RINTI, by the reference's three cases (a fixed orbital, occupation numbers
+ * more than 10 % apart, close occupations). ucf[nw], lfix[nw] (0/1): UCF and
+ * LFIX of every orbital. Entries of cof for orbitals in no pair are not read. */
+int gg_cofpot(gg_ctx *ctx, int j, double ucfj, const gg_cof *cof, int nec, const int32_t *iecc, const double *ecv,
+              double accy, double *yp, double *xp, double *xq);
+int gg_setlag(gg_ctx *ctx, int nec, const int32_t *iecc, const double *ucf, const int *lfix, const gg_cof *cof,
+              double *ecv);
 /* gg_slater without any device allocation. No counterpart in the reference:
  * for callers that cannot allocate device memory at the point where they
  * need an integral (device memory fully handed to a pool or to a large

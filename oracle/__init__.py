@@ -72,6 +72,9 @@ def lib():
         L.or_yzk.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, _d]
         L.or_ypot.argtypes = [C.c_void_p, C.c_int, _i32, _d, _d]
         L.or_xpot.argtypes = [C.c_void_p, C.c_int, _i32, _d, _d, _d]
+        L.or_cofpot.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(OrCof), C.c_int, _i32, _d, C.c_double,
+                                _d, _d, _d]
+        L.or_setlag.argtypes = [C.c_void_p, C.c_int, _i32, _d, _int, C.POINTER(OrCof), _d]
         L.or_slater.restype = C.c_double
         L.or_slater.argtypes = [C.c_void_p] + [C.c_int] * 5
         L.or_rinti.restype = C.c_double
@@ -101,6 +104,22 @@ def lib():
 
 def _p(a, t):
     return a.ctypes.data_as(t)
+
+
+class OrCof(C.Structure):
+    """One orbital's SETCOF lists (YPOT's NYA/YA, XPOT's NXA/XA, DACON's NDA/DA)."""
+    _fields_ = [("ny", C.c_int), ("nya", _i32), ("ya", _d), ("nx", C.c_int), ("nxa", _i32), ("xa", _d),
+                ("nd", C.c_int), ("nda", _i32), ("da", _d)]
+
+
+def _cof(d, keep):
+    arrs = [np.ascontiguousarray(d.get(k, []), t) for k, t in
+            (("nya", np.int32), ("ya", np.float64), ("nxa", np.int32), ("xa", np.float64),
+             ("nda", np.int32), ("da", np.float64))]
+    keep.extend(arrs)
+    nya, ya, nxa, xa, nda, da = arrs
+    return OrCof(nya.size, _p(nya, _i32), _p(ya, _d), nxa.size, _p(nxa, _i32), _p(xa, _d),
+                 nda.size, _p(nda, _i32), _p(da, _d))
 
 
 class Oracle:
@@ -173,6 +192,32 @@ class Oracle:
         if lib().or_xpot(self._h, nxa.size, _p(nxa, _i32), _p(xa, _d), _p(xp, _d), _p(xq, _d)) != 0:
             raise ValueError("xpot: label outside the orbital set")
         return xp, xq
+
+    def cofpot(self, j, ucfj, cof, iecc=(), ecv=(), accy=None):
+        """COFPOT after SETCOF (rmcdhf90/cofpot.f90:30-33): YPOT, XPOT, LAGCON,
+        DACON of orbital j from its lists (dict nya/ya/nxa/xa/nda/da);
+        returns YP, XP, XQ."""
+        keep = []
+        c = _cof(cof, keep)
+        iecc = np.ascontiguousarray(iecc, np.int32); ecv = np.ascontiguousarray(ecv, np.float64)
+        accy = self.h ** 6 if accy is None else accy
+        yp, xp, xq = np.zeros(self.n), np.zeros(self.n), np.zeros(self.n)
+        if lib().or_cofpot(self._h, j, ucfj, C.byref(c), iecc.size, _p(iecc, _i32), _p(ecv, _d), accy,
+                           _p(yp, _d), _p(xp, _d), _p(xq, _d)) != 0:
+            raise ValueError("cofpot: label outside the orbital set")
+        return yp, xp, xq
+
+    def setlag(self, iecc, ucf, lfix, cofs):
+        """SETLAG (rmcdhf90/setlag.f90:140-223): ECV of each pair iecc[k] =
+        LI + 215 LJ; cofs[orbital - 1] = that orbital's lists."""
+        keep = []
+        arr = (OrCof * len(cofs))(*[_cof(c, keep) for c in cofs])
+        iecc = np.ascontiguousarray(iecc, np.int32); ucf = np.ascontiguousarray(ucf, np.float64)
+        lfix = np.ascontiguousarray(lfix, np.int32)
+        ecv = np.zeros(iecc.size)
+        if lib().or_setlag(self._h, iecc.size, _p(iecc, _i32), _p(ucf, _d), _p(lfix, _int), arr, _p(ecv, _d)) != 0:
+            raise ValueError("setlag: bad list or pair")
+        return ecv
 
     def slater(self, a, b, c, d, k):
         return lib().or_slater(self._h, a, b, c, d, k)

@@ -936,6 +936,162 @@ int or_xpot(or_ctx *g, int ncof, const int32_t *nxa, const double *xa, double *x
   return 0;
 }
 
+// LAGCON (rmcdhf90/lagcon.f90:32-56, NPROCS = 1): XP, XQ 1-based.
+static void lagcon(const or_ctx *g, int J, double ucfj, int nec, const int32_t *iecc, const double *ecv, double accy,
+                   double *XP, double *XQ) {
+  const int KEY = 215;
+  if (nec == 0) return;
+  const double EPS = accy * 0.01;
+  const double WB = 1.0 / (ucfj * g->c) / 1.0;
+  for (int k = 0; k < nec; ++k) {
+    const int L1 = iecc[k] / KEY, L2 = iecc[k] - KEY * L1;
+    int M;
+    if (J == L1)
+      M = L2;
+    else if (J == L2)
+      M = L1;
+    else
+      continue;
+    const double WA = ecv[k] * WB;
+    if (std::fabs(WA) < EPS) continue;
+    for (int i = 1; i <= g->MF[M]; ++i) {
+      const double WARI = WA * g->R[i];
+      XP[i] = XP[i] + WARI * g->qf(i, M);
+      XQ[i] = XQ[i] - WARI * g->pf(i, M);
+    }
+  }
+}
+
+// DACON (rmcdhf90/dacon.f90:25-46): XP, XQ 1-based.
+static void dacon(const or_ctx *g, int nd, const int32_t *nda, const double *da, double *XP, double *XQ) {
+  const double TWOC = g->c + g->c;
+  std::vector<double> TA(g->nn1(), 0.0), TB(g->nn1(), 0.0);
+  for (int k = 0; k < nd; ++k) {
+    const int IORB = nda[k];
+    dpbdt(g, IORB, TA.data(), TB.data());
+    const int MFI = g->MF[IORB];
+    const double COEFF = da[k], FK = (double)g->NAK[IORB];
+    for (int i = 2; i <= MFI; ++i) {
+      const double RPORII = 1.0 / (g->h * g->RPOR[i]);
+      const double PFI = g->pf(i, IORB), QFI = g->qf(i, IORB);
+      const double ZBCI = g->ZZ[i] / g->c;
+      XP[i] = XP[i] + COEFF * (TA[i] * RPORII + FK * PFI - (TWOC * g->R[i] + ZBCI) * QFI);
+      XQ[i] = XQ[i] + COEFF * (TB[i] * RPORII - FK * QFI + ZBCI * PFI);
+    }
+  }
+}
+
+// one orbital's lists as SETCOF leaves them in scf_C
+struct or_cof {
+  int ny;
+  const int32_t *nya;
+  const double *ya;
+  int nx;
+  const int32_t *nxa;
+  const double *xa;
+  int nd;
+  const int32_t *nda;
+  const double *da;
+};
+
+// YPOT, XPOT, [LAGCON], DACON for orbital J: YP, XP, XQ 1-based (nn1 each)
+static int potentials(or_ctx *g, const or_cof *c, bool lag, int J, double ucfj, int nec, const int32_t *iecc,
+                      const double *ecv, double accy, std::vector<double> &YP, std::vector<double> &XP,
+                      std::vector<double> &XQ) {
+  const int N = g->n;
+  std::vector<double> yp(N), xp(N), xq(N);
+  if (or_ypot(g, c->ny, c->nya, c->ya, yp.data()) || or_xpot(g, c->nx, c->nxa, c->xa, xp.data(), xq.data()))
+    return -1;
+  YP.assign(g->nn1(), 0.0);
+  XP.assign(g->nn1(), 0.0);
+  XQ.assign(g->nn1(), 0.0);
+  for (int i = 1; i <= N; ++i) {
+    YP[i] = yp[i - 1];
+    XP[i] = xp[i - 1];
+    XQ[i] = xq[i - 1];
+  }
+  if (lag) lagcon(g, J, ucfj, nec, iecc, ecv, accy, XP.data(), XQ.data());
+  dacon(g, c->nd, c->nda, c->da, XP.data(), XQ.data());
+  return 0;
+}
+
+// COFPOT (rmcdhf90/cofpot.f90:29-33) after SETCOF: YPOT, XPOT, LAGCON, DACON.
+int or_cofpot(or_ctx *g, int j, double ucfj, const or_cof *cof, int nec, const int32_t *iecc, const double *ecv,
+              double accy, double *yp, double *xp, double *xq) {
+  std::vector<double> YP, XP, XQ;
+  if (potentials(g, cof, true, j, ucfj, nec, iecc, ecv, accy, YP, XP, XQ)) return -1;
+  for (int i = 1; i <= g->n; ++i) {
+    yp[i - 1] = YP[i];
+    xp[i - 1] = XP[i];
+    xq[i - 1] = XQ[i];
+  }
+  return 0;
+}
+
+// SETLAG (rmcdhf90/setlag.f90:140-223): ECV of each pair, in pair order, the
+// potentials of J and M recomputed when they change (JLAST, MLAST).
+int or_setlag(or_ctx *g, int nec, const int32_t *iecc, const double *ucf, const int *lfix, const or_cof *cof,
+              double *ecv) {
+  const int KEY = 215;
+  const double P001 = 1.0e-01;
+  const double C = g->c;
+  std::vector<double> YPJ, XPJ, XQJ, YPM, XPM, XQM;
+  std::vector<double> TA(g->nn1(), 0.0), T1(g->nn1(), 0.0), T2(g->nn1(), 0.0);
+  int JLAST = 0, MLAST = 0;
+  for (int li = 0; li < nec; ++li) {
+    const int M = iecc[li] / KEY, J = iecc[li] - KEY * M;
+    if (J != JLAST) {
+      if (potentials(g, &cof[J - 1], false, J, 0.0, 0, nullptr, nullptr, 0.0, YPJ, XPJ, XQJ)) return -1;
+      JLAST = J;
+    }
+    if (M != MLAST) {
+      if (potentials(g, &cof[M - 1], false, M, 0.0, 0, nullptr, nullptr, 0.0, YPM, XPM, XQM)) return -1;
+      MLAST = M;
+    }
+    const double UCFJ = ucf[J - 1], UCFM = ucf[M - 1];
+    const int MTP = std::max(g->MF[J], g->MF[M]);
+    int err = 0;
+    auto pm = [&](int i) { return g->pf(i, M); };
+    auto qm = [&](int i) { return g->qf(i, M); };
+    auto pj = [&](int i) { return g->pf(i, J); };
+    auto qj = [&](int i) { return g->qf(i, J); };
+    std::fill(TA.begin(), TA.end(), 0.0);
+    if (lfix[M - 1]) {
+      for (int i = 2; i <= MTP; ++i)
+        TA[i] = g->RPOR[i] * ((pm(i) * XQJ[i] - qm(i) * XPJ[i]) * C + (pm(i) * pj(i) + qm(i) * qj(i)) * YPJ[i]);
+      const double RESULT = quad(g, MTP, TA.data());
+      const double RIJM = rinti(g, M, J, 1, T1.data(), T2.data(), &err);
+      ecv[li] = (RESULT - RIJM) * UCFJ;
+    } else if (lfix[J - 1]) {
+      for (int i = 2; i <= MTP; ++i)
+        TA[i] = g->RPOR[i] * ((pj(i) * XQM[i] - qj(i) * XPM[i]) * C + (pj(i) * pm(i) + qj(i) * qm(i)) * YPM[i]);
+      const double RESULT = quad(g, MTP, TA.data());
+      const double RIJM = rinti(g, J, M, 1, T1.data(), T2.data(), &err);
+      ecv[li] = (RESULT - RIJM) * UCFM;
+    } else {
+      const double QDIF = std::fabs((UCFJ - UCFM) / std::max(UCFJ, UCFM));
+      if (QDIF > P001) {
+        const double OBQDIF = 1.0 / UCFJ - 1.0 / UCFM;
+        for (int i = 2; i <= MTP; ++i)
+          TA[i] = g->RPOR[i] * ((pm(i) * XQJ[i] - qm(i) * XPJ[i] - pj(i) * XQM[i] + qj(i) * XPM[i]) * C +
+                                (YPJ[i] - YPM[i]) * (pm(i) * pj(i) + qm(i) * qj(i)));
+        const double RESULT = quad(g, MTP, TA.data());
+        ecv[li] = RESULT / OBQDIF;
+      } else {
+        const double OBQSUM = 1.0 / UCFJ + 1.0 / UCFM;
+        for (int i = 2; i <= MTP; ++i)
+          TA[i] = g->RPOR[i] * ((pm(i) * XQJ[i] - qm(i) * XPJ[i] + pj(i) * XQM[i] - qj(i) * XPM[i]) * C +
+                                (YPJ[i] + YPM[i]) * (pm(i) * pj(i) + qm(i) * qj(i)));
+        const double RESULT = quad(g, MTP, TA.data());
+        const double RIJM = rinti(g, M, J, 1, T1.data(), T2.data(), &err);
+        ecv[li] = (RESULT - 2.0 * RIJM) / OBQSUM;
+      }
+    }
+    if (err) return -2;
+  }
+  return 0;
+}
+
 double or_rinti(or_ctx *g, int j, int k, int mode, int *err) {
   std::vector<double> TA(g->nn1(), 0.0), TB(g->nn1(), 0.0);
   return rinti(g, j, k, mode, TA.data(), TB.data(), err);

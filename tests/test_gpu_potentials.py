@@ -37,3 +37,67 @@ def test_potentials_match_oracle(gpu_ready, oracle_mod, run):
         ctx.ypot(np.array([(1 * KEY + (nw + 1)) * KEY], np.int32), np.ones(1))
     with pytest.raises(GGError):
         ctx.xpot(np.array([((1 * KEY + 1) * KEY + 1) * KEY + 21], np.int32), np.ones(1))  # K above 20
+
+
+def _ctx_oracle(run, oracle_mod):
+    from grasp_gb300 import Context
+    d = G.load(run, oracle_mod)
+    ctx = Context(0)
+    ctx.set_grid(d["n"], d["rnt"], d["h"], d["c"], d["zz"])
+    ctx.set_orbitals(d["nak"], d["mf"], d["pf"], d["qf"])
+    o = oracle_mod.Oracle(n=d["n"], rnt=d["rnt"], h=d["h"], c=d["c"], zz=d["zz"])
+    o.set_orbitals(d["nak"], d["mf"], d["pf"], d["qf"])
+    return d, ctx, o
+
+
+@pytest.mark.parametrize("run", ["He", "Ge"])
+def test_cofpot_matches_oracle(gpu_ready, oracle_mod, run):
+    """COFPOT's device part (YPOT, XPOT, LAGCON, DACON) against the oracle's."""
+    from tests.test_lagrange import _cofs, same_kappa_pairs
+    d, ctx, o = _ctx_oracle(run, oracle_mod)
+    nw = len(d["nak"])
+    cofs = _cofs(nw, 21)
+    iecc = same_kappa_pairs(d["nak"], 10, 3)
+    ecv = np.random.default_rng(8).normal(size=iecc.size)
+    for j in sorted({int(c) % KEY for c in iecc} | {1}):
+        yp, xp, xq = ctx.cofpot(j, 1.25, cofs[j - 1], iecc, ecv)
+        yp0, xp0, xq0 = o.cofpot(j, 1.25, cofs[j - 1], iecc, ecv)
+        for a, b in ((yp, yp0), (xp, xp0), (xq, xq0)):
+            assert np.abs(a - b).max() <= 1e-14 * np.abs(b).max(), (j, np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.mark.parametrize("run", ["He", "Ge"])
+def test_setlag_matches_oracle(gpu_ready, oracle_mod, run):
+    """SETLAG's multipliers (every case: M fixed, J fixed, occupations apart,
+    close occupations) against the oracle's, which follows the reference's
+    loop over pairs."""
+    from grasp_gb300 import GGError
+    from tests.test_lagrange import _cofs, same_kappa_pairs
+    d, ctx, o = _ctx_oracle(run, oracle_mod)
+    nw = len(d["nak"])
+    cofs = _cofs(nw, 31)
+    iecc = same_kappa_pairs(d["nak"], 16, 4)
+    rng = np.random.default_rng(6)
+    cases = set()
+    for trial in range(3):
+        ucf = rng.uniform(0.5, 2.0, nw)
+        if trial == 2:
+            ucf[:] = 1.0 + rng.uniform(0, 0.05, nw)  # every pair within 10 %
+        lfix = (rng.random(nw) < (0.0 if trial else 0.3)).astype(np.int32)
+        ecv = ctx.setlag(iecc, ucf, lfix, cofs)
+        ecv0 = o.setlag(iecc, ucf, lfix, cofs)
+        scale = max(1.0, np.abs(ecv0).max())
+        assert np.abs(ecv - ecv0).max() <= 1e-12 * scale, (trial, np.abs(ecv - ecv0).max() / scale)
+        for c in iecc:
+            m, j = int(c) // KEY, int(c) % KEY
+            if lfix[m - 1]:
+                cases.add(0)
+            elif lfix[j - 1]:
+                cases.add(1)
+            else:
+                cases.add(2 if abs(ucf[j - 1] - ucf[m - 1]) / max(ucf[j - 1], ucf[m - 1]) > 0.1 else 3)
+    assert cases == {0, 1, 2, 3}, cases
+    # a pair of orbitals with different kappa: RINTI's error
+    bad = [(i, j) for j in range(2, nw + 1) for i in range(1, j) if d["nak"][i - 1] != d["nak"][j - 1]][0]
+    with pytest.raises(GGError):
+        ctx.setlag(np.array([bad[0] + KEY * bad[1]], np.int32), np.ones(nw), np.zeros(nw, np.int32), cofs)
