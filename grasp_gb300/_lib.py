@@ -58,6 +58,10 @@ GPU_SYMBOLS = {
     "gg_cofpot": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.POINTER(GGCof), C.c_int, _i32, _d, C.c_double, _d,
                             _d, _d]),
     "gg_setlag": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _int, C.POINTER(GGCof), _d]),
+    "gg_genintbreit": (C.c_int, [C.c_void_p, C.c_int, C.c_double, _d, C.c_double, _i64, _int]),
+    "gg_get_breit_table": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _i32]),
+    "gg_brint": (C.c_int, [C.c_void_p] + [C.c_int] * 6 + [_d]),
+    "gg_brintf": (C.c_int, [C.c_void_p, C.c_int, _i32, C.c_double, _d, C.c_double, _d]),
     "gg_slater_noalloc": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _d]),
     "gg_rinti": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, _d]),
     "gg_iabint_table": (C.c_int, [C.c_void_p, _d]),

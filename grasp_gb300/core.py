@@ -142,6 +142,32 @@ class Context:
                                    ptr(ecv, _d)))
         return ecv
 
+    def genintbreit(self, itype, wfact, e, accy=0.0):
+        """GENINTBREIT1/2 on the device (gg_genintbreit): (INDTP, VALTP,
+        KSTARTBREIT, J2MAX) of the type-1 or type-2 table."""
+        e = np.ascontiguousarray(e, np.float64)
+        nb = C.c_int64(); j2 = C.c_int()
+        check(_lib.gpu().gg_genintbreit(self._h, int(itype), float(wfact), ptr(e, _d), float(accy), C.byref(nb),
+                                        C.byref(j2)))
+        ind = np.zeros(nb.value, np.int32); val = np.zeros(nb.value); kst = np.zeros(j2.value + 2, np.int32)
+        check(_lib.gpu().gg_get_breit_table(self._h, int(itype), ptr(ind, _i32), ptr(val, _d), ptr(kst, _i32)))
+        return ind, val, kst, j2.value
+
+    def brint(self, itype, a, b, c, d, k):
+        """BRINT1/BRINT2: a value of the context's table (gg_brint)."""
+        v = C.c_double()
+        check(_lib.gpu().gg_brint(self._h, int(itype), a, b, c, d, k, C.byref(v)))
+        return v.value
+
+    def brintf(self, items, wfact, e, accy=0.0):
+        """BRINTF for rows (type, ia, ib, ic, id, k) of items (gg_brintf)."""
+        it = np.ascontiguousarray(np.asarray(items, np.int32).reshape(-1, 6))
+        e = np.ascontiguousarray(e, np.float64)
+        out = np.zeros(it.shape[0])
+        check(_lib.gpu().gg_brintf(self._h, it.shape[0], ptr(it, _i32), float(wfact), ptr(e, _d), float(accy),
+                                   ptr(out, _d)))
+        return out
+
     def rinti(self, j, k, mode=0):
         out = C.c_double()
         check(_lib.gpu().gg_rinti(self._h, j, k, mode, C.byref(out)))

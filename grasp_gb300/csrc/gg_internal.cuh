@@ -139,6 +139,16 @@ struct Orbitals {
   DBuf<int> dMF, dNAK;                  // 1-based
 };
 
+// GENINTBREIT1/2's tables (breit.cu): type 1 and type 2
+struct BreitTable {
+  bool valid = false;
+  int j2max = 0;
+  int64_t n = 0;
+  std::vector<int32_t> kstart;          // KSTARTBREIT(0:j2max+1), 1-based positions
+  std::vector<int32_t> hInd;            // INDTP
+  std::vector<double> hVal;             // VALTP
+};
+
 struct RkCache;  // radial.cu: GENINTRK's orbital-set structure, reused between calls
 void rk_cache_free(RkCache *c);
 
@@ -199,6 +209,7 @@ struct gg_ctx {
   double btune_ms[6] = {};      // tuner's times of its variants (ms)
   cudaStream_t aux = nullptr;   // second blocking stream: uploads that overlap work on `stream`
   cudaEvent_t aux_done = nullptr;
+  gg::BreitTable breit[2];      // GENINTBREIT1, GENINTBREIT2
 };
 
 struct gg_hmat {

@@ -152,6 +152,32 @@ int gg_cofpot(gg_ctx *ctx, int j, double ucfj, const gg_cof *cof, int nec, const
               double accy, double *yp, double *xp, double *xq);
 int gg_setlag(gg_ctx *ctx, int nec, const int32_t *iecc, const double *ucf, const int *lfix, const gg_cof *cof,
               double *ecv);
+/* ---- Breit (transverse photon) integrals -----------------------------------
+ * gg_genintbreit: GENINTBREIT1 / GENINTBREIT2 (rci90/genintbreit1.f90:3,
+ * genintbreit2.f90:3) on the device: BRINTF(type, ia, ib, ic, id, k)
+ * (rci90/brintf.f90:3) for every k = 0..J2MAX and orbitals ia, ib, ic, id
+ * (1..NW) that TRIANGBREIT1 / TRIANGBREIT2 admits, in the reference's loop
+ * order (k, then ia, ib, ic, id). The photon frequencies are W = wfact
+ * |E(a) - E(b)| / C (bessel.f90:88) from the orbital energies e[nw] (orb_C's
+ * E) and WFACT (bess_C; 1 is rci's default, 0 the zero-frequency limit);
+ * accy: ACCY (<= 0: H^6). *nb_out = NB, *j2max_out = J2MAX. The table stays
+ * with the context (one per type).
+ * BRINTF is evaluated from its arguments alone: where the reference skips a
+ * BESSEL call for two equal orbitals and reads its slot's earlier content
+ * (brintf.f90:47-48), the zero-frequency function (zero) is used.
+ * gg_get_breit_table: INDTP = ((ia KEY + ib) KEY + ic) KEY + id (KEY = NW +
+ * 1), VALTP and KSTARTBREIT(0:J2MAX+1) (1-based); any pointer may be NULL.
+ * gg_brint: BRINT1 / BRINT2 (rci90/brint1.f90:3, brint2.f90:3), a value of
+ * the context's table of that type; GG_ERR_NOTFOUND where the reference
+ * STOPs.
+ * gg_brintf: BRINTF for n integrals of any type 1..6 (those BRINT3-6
+ * evaluate on demand and cache, brint3.f90:111-153, in one call):
+ * items[6 t .. 6 t + 5] = type, ia, ib, ic, id, k; out[n].                  */
+int gg_genintbreit(gg_ctx *ctx, int type, double wfact, const double *e, double accy, int64_t *nb_out,
+                   int *j2max_out);
+int gg_get_breit_table(gg_ctx *ctx, int type, int32_t *indtp, double *valtp, int32_t *kstart);
+int gg_brint(gg_ctx *ctx, int type, int ia, int ib, int ic, int id, int k, double *tegral);
+int gg_brintf(gg_ctx *ctx, int n, const int32_t *items, double wfact, const double *e, double accy, double *out);
 /* gg_slater without any device allocation. No counterpart in the reference:
  * for callers that cannot allocate device memory at the point where they
  * need an integral (device memory fully handed to a pool or to a large
@@ -354,7 +380,7 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * assembly plan built by the last gg_setham_upload (0 when it built none),
  * 30 block passes of the last split gg_maneig whose second Gram-Schmidt
  * pass was skipped (the first kept at least half of every new column's
- * squared norm).                                                            */
+ * squared norm), 31 device and host ms of the last gg_genintbreit.                                                            */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors

@@ -75,6 +75,10 @@ def lib():
         L.or_cofpot.argtypes = [C.c_void_p, C.c_int, C.c_double, C.POINTER(OrCof), C.c_int, _i32, _d, C.c_double,
                                 _d, _d, _d]
         L.or_setlag.argtypes = [C.c_void_p, C.c_int, _i32, _d, _int, C.POINTER(OrCof), _d]
+        L.or_brintf.restype = C.c_double
+        L.or_brintf.argtypes = [C.c_void_p] + [C.c_int] * 6 + [C.c_double, _d, C.c_double]
+        L.or_genintbreit.restype = C.c_int64
+        L.or_genintbreit.argtypes = [C.c_void_p, C.c_int, C.c_double, _d, C.c_double, _i32, _d, _i32, _int, C.c_int]
         L.or_slater.restype = C.c_double
         L.or_slater.argtypes = [C.c_void_p] + [C.c_int] * 5
         L.or_rinti.restype = C.c_double
@@ -221,6 +225,27 @@ class Oracle:
 
     def slater(self, a, b, c, d, k):
         return lib().or_slater(self._h, a, b, c, d, k)
+
+    def brintf(self, itype, a, b, c, d, k, wfact, e, accy=None):
+        """BRINTF (rci90/brintf.f90): one Breit integral of type 1..6; e = the
+        orbital energies, wfact = the frequency scale (bess_C WFACT)."""
+        e = np.ascontiguousarray(e, np.float64)
+        accy = self.h ** 6 if accy is None else accy
+        return lib().or_brintf(self._h, itype, a, b, c, d, k, wfact, _p(e, _d), accy)
+
+    def genintbreit(self, itype, wfact, e, accy=None, nthreads=1):
+        """GENINTBREIT1/2 (rci90/genintbreit1.f90, genintbreit2.f90): INDTP,
+        VALTP, KSTARTBREIT and J2MAX of the type-1 or type-2 table."""
+        e = np.ascontiguousarray(e, np.float64)
+        accy = self.h ** 6 if accy is None else accy
+        j2 = C.c_int(0)
+        kst = np.zeros(64, np.int32)
+        nb = lib().or_genintbreit(self._h, itype, wfact, _p(e, _d), accy, None, None, _p(kst, _i32), C.byref(j2),
+                                  nthreads)
+        ind = np.zeros(nb, np.int32); val = np.zeros(nb)
+        lib().or_genintbreit(self._h, itype, wfact, _p(e, _d), accy, _p(ind, _i32), _p(val, _d), _p(kst, _i32),
+                             C.byref(j2), nthreads)
+        return ind, val, kst[:j2.value + 2].copy(), j2.value
 
     def rinti(self, j, k, mode=0):
         err = C.c_int(0)

@@ -8,6 +8,7 @@
 #include "oracle.h"
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <chrono>
 #include <cmath>
@@ -1090,6 +1091,299 @@ int or_setlag(or_ctx *g, int nec, const int32_t *iecc, const double *ucf, const 
     if (err) return -2;
   }
   return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Breit integrals: BESSEL, ZKF, RKINT, SKINT, BRRA, BRINTF, TRIANGBREIT1/2,
+// GENINTBREIT1/2 (rci90). BRINTF is restated as a function of its arguments:
+// the reference keeps the Bessel functions of the last pairs in four slots
+// (bess_C KEEP) and skips BESSEL calls whose slot already holds the
+// function; here each needed slot is evaluated. The results agree wherever
+// the reference's slot holds the function it reads (slot 1: pair (IA,IB),
+// slot 2: pair (IC,ID)); where it skips a call for two equal orbitals
+// (zero frequency, brintf.f90:47-48) it reads the slot's earlier content.
+// ---------------------------------------------------------------------------
+struct or_bess {
+  std::vector<double> J, N;  // 1-based
+  double w = 0.0;
+};
+
+// BESSEL (rci90/bessel.f90:85-205): (j_nn(wr) series and asymptotic forms)
+static void bessel(const or_ctx *g, double wfact, const double *E, double accy, int ia, int ib, int nn, or_bess &b) {
+  const int N = g->n;
+  b.J.assign(g->nn1(), 0.0);
+  b.N.assign(g->nn1(), 0.0);
+  const double EPSI = std::sqrt(0.1 * accy);
+  const double W = wfact * std::fabs(E[ia - 1] - E[ib - 1]) / g->c;
+  b.w = W;
+  if (W < EPSI * EPSI) return;
+  int JCHAN = N + 1;
+  for (int j = 2; j <= N; ++j) {
+    const double WA = -0.5 * ((g->R[j] * W) * (g->R[j] * W));
+    double X1 = 1.0, X2 = 1.0, S1 = 0.0, S2 = 0.0;
+    bool done = false;
+    for (int i = 1; i <= 4; ++i) {
+      X1 = X1 * WA / (double)(i * (2 * (nn + i) + 1));
+      X2 = X2 * WA / (double)(i * (2 * (i - nn) - 1));
+      S1 = S1 + X1;
+      S2 = S2 + X2;
+      if (std::fabs(X1) >= std::fabs(S1) * EPSI || std::fabs(X2) >= std::fabs(S2) * EPSI) continue;
+      b.J[j] = S1;
+      b.N[j] = S2;
+      done = true;
+      break;
+    }
+    if (!done) {
+      JCHAN = j;
+      break;
+    }
+  }
+  if (JCHAN > N) return;
+  double DFNM, DFN;
+  if (nn == 0) {
+    DFNM = 1.0;
+    DFN = 1.0;
+  } else {
+    DFNM = 1.0;
+    for (int i = 3; i <= 2 * nn - 1; i += 2) DFNM = DFNM * (double)i;
+    DFN = DFNM * (double)(2 * nn + 1);
+  }
+  DFNM = 1.0 / DFNM;
+  const int IREM = nn % 4;  // MOD: the sign of nn
+  double SSN, SCN;
+  int ISWAP;
+  switch (IREM) {
+    case 1: SSN = -1.0; SCN = 1.0; ISWAP = 1; break;
+    case 2: SSN = -1.0; SCN = -1.0; ISWAP = 0; break;
+    case 3: SSN = 1.0; SCN = -1.0; ISWAP = 1; break;
+    default: SSN = 1.0; SCN = 1.0; ISWAP = 0; break;
+  }
+  for (int j = JCHAN; j <= N; ++j) {
+    const double WA = W * g->R[j];
+    double SN, CN;
+    if (ISWAP == 0) {
+      SN = SSN * std::sin(WA);
+      CN = SCN * std::cos(WA);
+    } else {
+      SN = SSN * std::cos(WA);
+      CN = SCN * std::sin(WA);
+    }
+    const double OBWA = 1.0 / WA;
+    double B = OBWA;
+    double S1 = B * SN, S2 = B * CN;
+    for (int i = 1; i <= nn; ++i) {
+      const double SKEEP = SN;
+      SN = CN;
+      CN = -SKEEP;
+      B = B * OBWA * (double)((nn + i) * (nn - i + 1)) / (double)(2 * i);
+      S1 = S1 + B * SN;
+      S2 = S2 + B * CN;
+    }
+    S1 = S1 * DFN / powi(WA, nn) - 1.0;
+    S2 = S2 * powi(WA, nn + 1) * DFNM - 1.0;
+    b.J[j] = S1;
+    b.N[j] = S2;
+  }
+}
+
+// ZKF (rci90/zkf.f90:32-75): ZK from TA(2:MTP), 1-based; R**K for K < 0 is
+// 1/R**|K| (the reference fills its power array only for K > 0).
+static void zkf(const or_ctx *g, int K, int MTP, const double *TA, double *ZK) {
+  const int N = g->n;
+  std::vector<double> RTTK(g->nn1(), 0.0), RHOP(g->nn1(), 0.0), TEMP(g->nn1(), 0.0);
+  if (K != 0)
+    for (int i = 2; i <= N; ++i) RTTK[i] = powi(g->R[i], K);
+  const int MTPP1 = MTP + 1, MTPP3 = MTP + 3, MTPP4 = MTP + 4;
+  for (int i = 2; i <= MTP; ++i) RHOP[i] = g->RP[i] * TA[i];
+  TEMP[1] = 0.0;
+  for (int i = 2; i <= MTP; ++i) TEMP[i] = (K == 0) ? RHOP[i] : RTTK[i] * RHOP[i];
+  for (int i = MTPP1; i <= MTPP4; ++i) TEMP[i] = 0.0;
+  ZK[1] = 0.0;
+  for (int ii = 2; ii <= 4; ++ii) {
+    double SUM = 0.0;
+    for (int kk = 2; kk <= 5; ++kk) SUM = SUM + g->CNC5C[kk][ii] * TEMP[kk];
+    ZK[ii] = SUM;
+  }
+  for (int ii = 5; ii <= MTPP3; ++ii)
+    ZK[ii] = ZK[ii - 4] + g->C1 * (TEMP[ii - 4] + TEMP[ii]) + g->C2 * (TEMP[ii - 3] + TEMP[ii - 1]) +
+             g->C3 * TEMP[ii - 2];
+  const double ZKLIM = ZK[MTPP3];
+  if (K == 0) {
+    for (int i = MTPP4; i <= N; ++i) ZK[i] = ZKLIM;
+  } else {
+    for (int i = 2; i <= MTPP3; ++i) ZK[i] = ZK[i] / RTTK[i];
+    for (int i = MTPP4; i <= N; ++i) ZK[i] = ZKLIM / RTTK[i];
+  }
+}
+
+// RKINT (rci90/rkint.f90:40-60): bj, bn = slot IW's BESSJ(1,IW), BESSN(1,IW)
+// (null for IW = 0)
+static double rkint(const or_ctx *g, const double *RAC, int IA, int IC, const double *RBD, int IB, int ID, int K,
+                    const double *bj, const double *bn) {
+  const int MXRBD = std::min(g->MF[IB], g->MF[ID]), MXRAC = std::min(g->MF[IA], g->MF[IC]);
+  std::vector<double> TA(g->nn1(), 0.0), TB(g->nn1(), 0.0);
+  for (int i = 1; i <= MXRAC; ++i) TA[i] = bj ? RAC[i] * (1.0 + bj[i]) : RAC[i];
+  int MTP = MXRAC;
+  zkf(g, K, MTP, TA.data(), TB.data());
+  MTP = std::min(MTP, MXRBD);
+  TA[1] = 0.0;
+  for (int i = 2; i <= MTP; ++i) TA[i] = bn ? RBD[i] * (1.0 + bn[i]) * TB[i] * g->RPOR[i] : RBD[i] * TB[i] * g->RPOR[i];
+  return quad(g, MTP, TA.data());
+}
+
+// SKINT (rci90/skint.f90:43-85): slot IW's BESSJ(1..2,IW), BESSN(1..2,IW)
+// and WIJ(IW)
+static double skint(const or_ctx *g, const double *RAC, int IA, int IC, const double *RBD, int IB, int ID, int K,
+                    const or_bess &b1, const or_bess &b2) {
+  const double EPSI = 1.0e-10;
+  const double W = b1.w;
+  const double WK = (double)(K + K + 1);
+  const int MXRAC = std::min(g->MF[IA], g->MF[IC]), MXRBD = std::min(g->MF[IB], g->MF[ID]);
+  std::vector<double> TA(g->nn1(), 0.0), TB(g->nn1(), 0.0), TKEEP(g->nn1(), 0.0);
+  for (int i = 1; i <= MXRAC; ++i) TA[i] = RAC[i];
+  int MTP = MXRAC;
+  zkf(g, K - 1, MTP, TA.data(), TB.data());
+  double SK;
+  if (std::fabs(W) < EPSI) {
+    for (int i = 1; i <= MTP; ++i) TKEEP[i] = TB[i];
+    zkf(g, K + 1, MTP, TA.data(), TB.data());
+    MTP = std::min(MTP, MXRBD);
+    TA[1] = 0.0;
+    for (int i = 2; i <= MTP; ++i) TA[i] = RBD[i] * g->RPOR[i] * (TB[i] - TKEEP[i]);
+    const double VALU = quad(g, MTP, TA.data());
+    SK = WK * VALU * 0.5;
+  } else {
+    for (int i = 1; i <= MTP; ++i) TKEEP[i] = TB[i];
+    for (int i = 1; i <= MTP; ++i) TA[i] = -TA[i] * b1.J[i];
+    zkf(g, K - 1, MTP, TA.data(), TB.data());
+    MTP = std::min(MTP, MXRBD);
+    TA[1] = 0.0;
+    for (int i = 2; i <= MTP; ++i)
+      TA[i] = ((1.0 + b2.N[i]) * TB[i] - TKEEP[i] * b2.N[i]) * RBD[i] / powi(g->R[i], 2) * g->RPOR[i];
+    double VALU = quad(g, MTP, TA.data());
+    SK = powi(WK / W, 2) * VALU;
+    for (int i = 1; i <= MXRBD; ++i) TA[i] = RBD[i] * (1.0 + b2.J[i]);
+    MTP = MXRBD;
+    zkf(g, K + 1, MTP, TA.data(), TB.data());
+    MTP = std::min(MTP, MXRAC);
+    TA[1] = 0.0;
+    for (int i = 2; i <= MTP; ++i) TA[i] = RAC[i] * (1.0 + b1.N[i]) * TB[i] * g->R[i] * g->RP[i];
+    VALU = quad(g, MTP, TA.data());
+    SK = SK - VALU * W * W / (double)((2 * K + 3) * (2 * K - 1));
+  }
+  return SK;
+}
+
+// BRRA (rci90/brra.f90:36-118) with BRINTF's argument order (IA, IB, IC, ID)
+// = BRRA's (IA, IC, IB, ID); s[iw][ik]: the Bessel slots
+static double brra(const or_ctx *g, int ITYPE, int IA, int IC, int IB, int ID, int K, or_bess s[3][3]) {
+  const double HALF = 0.5, TWO = 2.0;
+  const int MXRAC = std::min(g->MF[IA], g->MF[IC]), MXRBD = std::min(g->MF[IB], g->MF[ID]);
+  std::vector<double> RAC(g->nn1(), 0.0), RBD(g->nn1(), 0.0);
+  for (int i = 1; i <= MXRAC; ++i) RAC[i] = g->pf(i, IA) * g->qf(i, IC);
+  for (int i = 1; i <= MXRBD; ++i) RBD[i] = g->pf(i, IB) * g->qf(i, ID);
+  auto R = [&](bool rac, int iw) {
+    const double *bj = iw ? s[iw][1].J.data() : nullptr, *bn = iw ? s[iw][1].N.data() : nullptr;
+    return rac ? rkint(g, RAC.data(), IA, IC, RBD.data(), IB, ID, K, bj, bn)
+               : rkint(g, RBD.data(), IB, ID, RAC.data(), IA, IC, K, bj, bn);
+  };
+  auto S = [&](int iw) { return skint(g, RAC.data(), IA, IC, RBD.data(), IB, ID, K, s[iw][1], s[iw][2]); };
+  switch (ITYPE) {
+    case 1:
+      if (IA == IB && IC == ID) return TWO * R(true, 1);
+      if (IA == ID && IC == IB) return R(true, 1) + R(false, 1);
+      return (R(true, 1) + R(true, 2) + R(false, 1) + R(false, 2)) * HALF;
+    case 2:
+      if ((IA == IB && IC == ID) || (IA == ID && IC == IB)) return S(1);
+      return (S(1) + S(2)) * HALF;
+    case 3:
+      if (IA == IC) {
+        for (int i = 1; i <= MXRBD; ++i) RBD[i] = RBD[i] + g->pf(i, ID) * g->qf(i, IB);
+        return (R(true, 0) + R(false, 0) + R(true, 2) + R(false, 2)) * HALF;
+      }
+      for (int i = 1; i <= MXRAC; ++i) RAC[i] = RAC[i] + g->pf(i, IC) * g->qf(i, IA);
+      return (R(true, 1) + R(false, 1) + R(true, 0) + R(false, 0)) * HALF;
+    case 4:
+      return R(true, 0) + R(false, 0);
+    case 5:
+      if (IA == ID && IC == IB) return R(true, 1) + R(false, 1);
+      return TWO * R(true, 1);
+    default:
+      return S(1);
+  }
+}
+
+// BRINTF (rci90/brintf.f90:34-69): slot 1 = pair (IA, IB), slot 2 = pair
+// (IC, ID); order K (types 1, 3, 5) or K - 1 and K + 1 (types 2, 6)
+double brintf(const or_ctx *g, int ITYPE, int IA, int IB, int IC, int ID, int K, double wfact, const double *E,
+              double accy) {
+  or_bess s[3][3];
+  if (ITYPE == 1 || ITYPE == 3 || ITYPE == 5) {
+    bessel(g, wfact, E, accy, IA, IB, K, s[1][1]);
+    if (ITYPE != 5) bessel(g, wfact, E, accy, IC, ID, K, s[2][1]);
+  } else if (ITYPE == 2 || ITYPE == 6) {
+    bessel(g, wfact, E, accy, IA, IB, K - 1, s[1][1]);
+    bessel(g, wfact, E, accy, IA, IB, K + 1, s[1][2]);
+    if (ITYPE == 2) {
+      bessel(g, wfact, E, accy, IC, ID, K - 1, s[2][1]);
+      bessel(g, wfact, E, accy, IC, ID, K + 1, s[2][2]);
+    }
+  }
+  return brra(g, ITYPE, IA, IB, IC, ID, K, s);
+}
+
+// TRIANGBREIT1 (rci90/triangbreit1.f90:27-46), TRIANGBREIT2 (triangbreit2.f90:27-42)
+static bool triangbreit(const or_ctx *g, int type, int IA, int IB, int IC, int ID, int K) {
+  const int LA = g->NKL[IA], LB = g->NKL[IB], LC = g->NKL[IC], LD = g->NKL[ID];
+  const int JA = g->NKJ[IA], JB = g->NKJ[IB], JC = g->NKJ[IC], JD = g->NKJ[ID];
+  auto side = [&](int par, int l, int x, int la, int lb, int ja, int jb) {
+    return ((l + x + la + lb) % 2 == par) && std::abs(ja - jb) <= 2 * x && std::abs(ja + jb) >= 2 * x;
+  };
+  if (type == 1) {
+    for (int L = K - 1; L <= K + 1; ++L)
+      if (side(1, K - L, L, LA, LB, JA, JB) && side(1, K - L, L, LC, LD, JC, JD)) return true;
+    return false;
+  }
+  return side(0, 0, K, LA, LB, JA, JB) && side(0, 0, K, LC, LD, JC, JD);
+}
+
+double or_brintf(or_ctx *g, int type, int ia, int ib, int ic, int id, int k, double wfact, const double *E,
+                 double accy) {
+  return brintf(g, type, ia, ib, ic, id, k, wfact, E, accy);
+}
+
+// GENINTBREIT1 / GENINTBREIT2 (rci90/genintbreit1.f90:50-100,
+// genintbreit2.f90:50-100): NB, INDTP ((IA*KEY+IB)*KEY+IC)*KEY+ID with KEY =
+// NW + 1, VALTP = BRINTF(type, ...), KSTARTBREIT(0:J2MAX+1). With ind null
+// only NB and kstart are returned. nthreads host threads share the values.
+int64_t or_genintbreit(or_ctx *g, int type, double wfact, const double *E, double accy, int32_t *ind, double *val,
+                       int32_t *kstart, int *j2max_out, int nthreads) {
+  const int NW = g->nw, KEY = NW + 1;
+  int J2MAX = g->NKJ[1];
+  for (int i = 2; i <= NW; ++i) J2MAX = std::max(J2MAX, g->NKJ[i]);
+  if (j2max_out) *j2max_out = J2MAX;
+  std::vector<std::array<int, 5>> items;
+  int64_t NB = 0;
+  if (kstart) kstart[0] = 1;
+  for (int K = 0; K <= J2MAX; ++K) {
+    for (int IA = 1; IA <= NW; ++IA)
+      for (int IB = 1; IB <= NW; ++IB)
+        for (int IC = 1; IC <= NW; ++IC)
+          for (int ID = 1; ID <= NW; ++ID)
+            if (triangbreit(g, type, IA, IB, IC, ID, K)) {
+              ++NB;
+              if (ind) items.push_back({K, IA, IB, IC, ID});
+            }
+    if (kstart) kstart[K + 1] = (int32_t)(NB + 1);
+  }
+  if (ind) {
+    parallel_for((int64_t)items.size(), nthreads, [&](int64_t i, int) {
+      const auto &t = items[i];
+      ind[i] = ((t[1] * KEY + t[2]) * KEY + t[3]) * KEY + t[4];
+      val[i] = brintf(g, type, t[1], t[2], t[3], t[4], t[0], wfact, E, accy);
+    });
+  }
+  return NB;
 }
 
 double or_rinti(or_ctx *g, int j, int k, int mode, int *err) {

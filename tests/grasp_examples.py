@@ -206,4 +206,5 @@ def load(run, oracle_mod):
                 m -= 1
             mf[l] = m
     return dict(n=n, rnt=rnt, h=h, c=c, z=z, zz=zz, nak=nak, np=np.array([p for p, _ in wanted], np.int32), mf=mf,
-                pf=pf, qf=qf, labels=labels, ncore=ncore, levels=sm["levels"], summary=sm)
+                pf=pf, qf=qf, labels=labels, ncore=ncore, levels=sm["levels"], summary=sm,
+                e=np.array([stored[key].e for key in wanted]))
