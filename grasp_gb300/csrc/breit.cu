@@ -30,9 +30,8 @@
 // orbitals (zero frequency, brintf.f90:47-48) its slot keeps earlier
 // content; here that slot is the zero-frequency function (zero).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
-#include <map>
-#include <tuple>
 #include <vector>
 
 #include "gg_internal.cuh"
@@ -391,7 +390,8 @@ struct Planner {
   const gg_ctx *ctx;
   double wfact, epsi;
   std::vector<double> e;
-  std::map<std::tuple<int, int, int>, int> bidx;
+  int nw = 0;
+  std::vector<int> bidx;  // [pair (x <= y)][order + 1]: function index, -2 not yet seen
   std::vector<BessDesc> bess;
   std::vector<BrJob> jobs;
   std::vector<BrInt> ints;
@@ -400,15 +400,16 @@ struct Planner {
   double w(int x, int y) const { return wfact * std::fabs(e[x - 1] - e[y - 1]) / ctx->grid.c; }
   // the Bessel function of pair (x, y), order nn; -1 when it is zero
   int bessel(int x, int y, int nn) {
+    int &slot = bidx[((size_t)(std::min(x, y) - 1) * nw + (std::max(x, y) - 1)) * (KLIM + 3) + (nn + 1)];
+    if (slot != -2) return slot;
     const double W = w(x, y);
-    if (W < epsi * epsi) return -1;
-    const auto key = std::make_tuple(std::min(x, y), std::max(x, y), nn);
-    auto it = bidx.find(key);
-    if (it != bidx.end()) return it->second;
-    const int id = (int)bess.size();
-    bess.push_back(BessDesc{W, nn});
-    bidx.emplace(key, id);
-    return id;
+    if (W < epsi * epsi) {
+      slot = -1;
+    } else {
+      slot = (int)bess.size();
+      bess.push_back(BessDesc{W, nn});
+    }
+    return slot;
   }
   void job(int form, int k, int sx, int sy, bool saug, int px, int py, bool paug, int bj, int bn) {
     BrJob j;
@@ -540,8 +541,9 @@ template <class T> int upload_vec(DBuf<T> &b, const std::vector<T> &h, cudaStrea
   return GG_OK;
 }
 
-// the planned integrals on the device, values into out (host, ints order)
-int run_plan(gg_ctx *ctx, Planner &P, double *out) {
+// the planned integrals on the device, values into out (host, ints order);
+// *kernel_ms: device time of the kernels
+int run_plan(gg_ctx *ctx, Planner &P, double *out, double *kernel_ms = nullptr) {
   GG_TRY(P.err);
   const Grid &g = ctx->grid;
   const Orbitals &o = ctx->orb;
@@ -563,6 +565,12 @@ int run_plan(gg_ctx *ctx, Planner &P, double *out) {
   const int64_t nj = (int64_t)P.jobs.size(), ni = (int64_t)P.ints.size();
   GG_TRY(dv.alloc(std::max<int64_t>(1, nj)));
   GG_TRY(dout.alloc(std::max<int64_t>(1, ni)));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (kernel_ms) {
+    GG_CUDA(cudaEventCreate(&e0));
+    GG_CUDA(cudaEventCreate(&e1));
+    GG_CUDA(cudaEventRecord(e0, s));
+  }
   if (nj > 0) {
     k_breit_jobs<<<(unsigned)((nj + 127) / 128), 128, 0, s>>>(djobs.p, nj, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p,
                                                                g.dRP.p, g.dRPOR.p, g.dPow.p, g.np, g.q, dBJ.p,
@@ -574,8 +582,16 @@ int run_plan(gg_ctx *ctx, Planner &P, double *out) {
     ::gg::note_launch();
   }
   GG_CUDA(cudaGetLastError());
+  if (kernel_ms) GG_CUDA(cudaEventRecord(e1, s));
   if (ni > 0) GG_CUDA(cudaMemcpyAsync(out, dout.p, ni * sizeof(double), cudaMemcpyDeviceToHost, s));
   GG_CUDA(cudaStreamSynchronize(s));
+  if (kernel_ms) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    *kernel_ms = ms;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+  }
   return GG_OK;
 }
 
@@ -588,6 +604,8 @@ int make_planner(gg_ctx *ctx, double wfact, const double *e, double accy, Planne
   P.wfact = wfact;
   P.epsi = std::sqrt(0.1 * (accy > 0 ? accy : std::pow(ctx->grid.h, 6)));
   P.e.assign(e, e + o.nw);
+  P.nw = o.nw;
+  P.bidx.assign((size_t)o.nw * o.nw * (KLIM + 3), -2);
   return GG_OK;
 }
 
@@ -609,6 +627,7 @@ int gg_genintbreit(gg_ctx *ctx, int type, double wfact, const double *e, double 
   const int nw = o.nw, KEY = nw + 1;
   int j2max = o.nkj[1];
   for (int i = 2; i <= nw; ++i) j2max = std::max(j2max, o.nkj[i]);
+  const auto th0 = std::chrono::steady_clock::now();
   BreitTable &T = ctx->breit[type - 1];
   T.valid = false;
   T.j2max = j2max;
@@ -627,8 +646,9 @@ int gg_genintbreit(gg_ctx *ctx, int type, double wfact, const double *e, double 
     GG_TRY(P.err);
   }
   T.n = (int64_t)T.hInd.size();
+  ctx->stats[32] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - th0).count();
   T.hVal.assign(std::max<int64_t>(1, T.n), 0.0);
-  GG_TRY(run_plan(ctx, P, T.hVal.data()));
+  GG_TRY(run_plan(ctx, P, T.hVal.data(), &ctx->stats[33]));
   T.hVal.resize(T.n);
   T.valid = true;
   double ms = 0;

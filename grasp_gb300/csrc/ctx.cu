@@ -310,7 +310,7 @@ int gg_set_orbitals(gg_ctx *ctx, int nw, int ld, const int *nak, const int *mf, 
 }
 
 double gg_stage_stat(gg_ctx *ctx, int which) {
-  if (!ctx || which < 0 || which >= 32) return -1.0;
+  if (!ctx || which < 0 || which >= 34) return -1.0;
   return ctx->stats[which];
 }
 

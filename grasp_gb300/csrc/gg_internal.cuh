@@ -200,7 +200,7 @@ struct gg_ctx {
   gg::RkTable rk;
   gg::DBuf<double> dIab;                // [nw * nw]
   bool iab_valid = false;
-  double stats[32] = {};
+  double stats[40] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev_mid = nullptr;  // a point inside a timed call (gg_maneig: after its structures)
   cudaEvent_t marks[8] = {};  // gg_event_record slots

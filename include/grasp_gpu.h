@@ -380,7 +380,9 @@ int gg_maneig_batched(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nv
  * assembly plan built by the last gg_setham_upload (0 when it built none),
  * 30 block passes of the last split gg_maneig whose second Gram-Schmidt
  * pass was skipped (the first kept at least half of every new column's
- * squared norm), 31 device and host ms of the last gg_genintbreit.                                                            */
+ * squared norm), 31 device and host ms of the last gg_genintbreit, 32 / 33
+ * its host ms enumerating the integrals and their terms / its device ms of
+ * the Bessel, term and combination kernels.                                                            */
 double gg_stage_stat(gg_ctx *ctx, int which);
 
 /* gg_projected_eig: DVDSON's projected eigenproblem, CALL DSPEVX('Vectors
