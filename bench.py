@@ -530,6 +530,58 @@ def host_resident_leg(ctx, H, w, ev_ref, vec_ref, steps):
     return out
 
 
+def breit_leg(local, w, steps, cpu=True):
+    """rci's Breit integral tables (GENINTBREIT1/2, rci90/genintbreit1.f90:3,
+    genintbreit2.f90:3) for the Fe XV orbital set (34 subshells) with the
+    orbitals' Dirac energies and rci's default WFACT = 1 (frequency-dependent
+    transverse photon). Device ms per table (planning on the host, then the
+    Bessel, term and combination kernels); the oracle's BRINTF on a sample of
+    the type-1 table gives the single-core CPU time per integral and the
+    largest difference."""
+    import numpy as np
+
+    from grasp_gb300 import Context
+    ctx = Context(local)
+    ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
+    ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    e = np.asarray(w.orb.e, np.float64)
+    out = {"orbitals": int(len(w.orb.nak)), "wfact": 1.0}
+    tables = {}
+    for itype in (1, 2):
+        ctx.genintbreit(itype, 1.0, e)  # warm
+        tot, plan, kern = [], [], []
+        for _ in range(max(1, min(steps, 5))):
+            ind, val, kst, j2 = ctx.genintbreit(itype, 1.0, e)
+            tot.append(ctx.stage_stat(31))
+            plan.append(ctx.stage_stat(32))
+            kern.append(ctx.stage_stat(33))
+        tables[itype] = (ind, val, kst)
+        out[f"type{itype}"] = {"integrals": int(ind.size), "ms": statistics.median(tot),
+                               "host_plan_ms": statistics.median(plan), "kernels_ms": statistics.median(kern)}
+    if cpu:
+        import oracle
+        o = oracle.Oracle(n=w.n, rnt=w.rnt, h=w.h, c=w.c, zz=w.zz)
+        o.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+        ind, val, kst = tables[1]
+        key = len(w.orb.nak) + 1
+        pos = np.random.default_rng(0).choice(ind.size, 300, replace=False)
+        t0 = time.perf_counter()
+        err = 0.0
+        for p in pos:
+            k = int(np.searchsorted(kst, p + 1, side="right") - 1)
+            x = int(ind[p])
+            d = x % key; x //= key
+            c = x % key; x //= key
+            b = x % key; a = x // key
+            err = max(err, abs(o.brintf(1, a, b, c, d, k, 1.0, e) - val[p]))
+        per = (time.perf_counter() - t0) / pos.size
+        out["cpu_oracle"] = {"us_per_type1_integral": per * 1e6, "type1_table_s_1core": per * ind.size,
+                             "sample": "300 random entries of the type-1 table, 1 core",
+                             "max_abs_diff_rel": err / float(np.abs(val).max())}
+    ctx.close()
+    return out
+
+
 def run_ours(a):
     ws, rank, local, pg = _dist()
     import numpy as np
@@ -636,6 +688,7 @@ def run_ours(a):
                 e2e_parts.append(parts)
     t_e2e = _max_over_ranks(pg, statistics.median(e2e_times)) if e2e_times else None
     host_res = host_resident_leg(ctx, H, w, ev, vec, a.steps) if not a.no_extra else None
+    breit = breit_leg(local, w, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
     batched = batched_leg(local, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
     rk = rk_leg(local) if not a.no_extra else None
     large = large_leg(local, cpu=(rank == 0 and not a.no_cpu_baseline)) if not (a.no_extra or a.no_large) else None
@@ -684,6 +737,7 @@ def run_ours(a):
         "clocks": clk,
         "cpu_baseline": cpu,
         "host_resident_block": host_res,
+        "breit_tables_fe15_orbitals": breit,
         "batched_310_blocks": batched,
         "rk_table_40_orbitals": rk,
         "large_300k_csf": large,
