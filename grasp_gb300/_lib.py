@@ -59,6 +59,10 @@ GPU_SYMBOLS = {
                             _d, _d]),
     "gg_setlag": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _int, C.POINTER(GGCof), _d]),
     "gg_genintbreit": (C.c_int, [C.c_void_p, C.c_int, C.c_double, _d, C.c_double, _i64, _int]),
+    "gg_setcof_prepare": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p), _int, C.POINTER(_d),
+                                    C.POINTER(_d), C.c_int]),
+    "gg_setcof": (C.c_int, [C.c_void_p, C.c_int, C.c_double, C.c_int, _int, _i32, _d, _int, _i32, _d, _int, _i32,
+                            _d]),
     "gg_get_breit_table": (C.c_int, [C.c_void_p, C.c_int, _i32, _d, _i32]),
     "gg_brint": (C.c_int, [C.c_void_p] + [C.c_int] * 6 + [_d]),
     "gg_brintf": (C.c_int, [C.c_void_p, C.c_int, _i32, C.c_double, _d, C.c_double, _d]),

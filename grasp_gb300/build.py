@@ -21,8 +21,8 @@ GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = GENCODE + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INC]
 # files whose FP64 arithmetic restates the reference step by step: no
 # contraction of a*b + c into one fused rounding
-NO_FMAD = {"radial.cu", "setham.cu", "spmv.cu", "davidson.cu", "breit.cu"}  # exact FP64 sums; error-free double-float steps
-CU_SOURCES = ["ctx.cu", "radial.cu", "setham.cu", "spmv.cu", "davidson.cu", "bdvd.cu", "hostmat.cu", "breit.cu"]
+NO_FMAD = {"radial.cu", "setham.cu", "spmv.cu", "davidson.cu", "breit.cu", "setcof.cu"}  # exact FP64 sums; error-free double-float steps
+CU_SOURCES = ["ctx.cu", "radial.cu", "setham.cu", "spmv.cu", "davidson.cu", "bdvd.cu", "hostmat.cu", "breit.cu", "setcof.cu"]
 CPP_SOURCES = ["hosteig.cpp"]
 ANGULAR_SOURCES = ["angular.cpp"]
 

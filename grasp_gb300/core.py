@@ -142,6 +142,44 @@ class Context:
                                    ptr(ecv, _d)))
         return ecv
 
+    def setcof_prepare(self, hmats, wt, evec=None, eol=True):
+        """SETCOF's sums for every orbital (gg_setcof_prepare): hmats in
+        rmcdhf's block order (lists uploaded); eol: evec[b] (NCF_b x nev_b) and
+        wt[b] (nev_b level weights); else wt[b] = the NCF_b CSF weights."""
+        nb = len(hmats)
+        keep = []
+        hs = (C.c_void_p * nb)(*[h._h for h in hmats])
+        wts = [np.ascontiguousarray(w, np.float64) for w in wt]
+        keep += wts
+        wp = (_d * nb)(*[ptr(w, _d) for w in wts])
+        if eol:
+            evs = [np.asfortranarray(np.asarray(v, np.float64).reshape(h.ncf, -1)) for v, h in zip(evec, hmats)]
+            keep += evs
+            ep = (_d * nb)(*[ptr(v, _d) for v in evs])
+            nev = np.array([v.shape[1] for v in evs], np.int32)
+        else:
+            ep = (_d * nb)()
+            nev = np.zeros(nb, np.int32)
+        check(_lib.gpu().gg_setcof_prepare(self._h, nb, hs, ptr(nev, _int), ep, wp, int(bool(eol))))
+
+    def setcof(self, j, ucfj):
+        """SETCOF(EOL, J)'s lists (gg_setcof) from the prepared sums: a dict
+        nya/ya, nxa/xa, nda/da (gg_cofpot's and cofpot's input)."""
+        cap = 1024
+        while True:
+            ny, nx, nd = C.c_int(), C.c_int(), C.c_int()
+            nya = np.zeros(cap, np.int32); ya = np.zeros(cap); nxa = np.zeros(cap, np.int32); xa = np.zeros(cap)
+            nda = np.zeros(cap, np.int32); da = np.zeros(cap)
+            st = _lib.gpu().gg_setcof(self._h, int(j), float(ucfj), cap, C.byref(ny), ptr(nya, _i32), ptr(ya, _d),
+                                      C.byref(nx), ptr(nxa, _i32), ptr(xa, _d), C.byref(nd), ptr(nda, _i32),
+                                      ptr(da, _d))
+            if st == _lib_status("GG_ERR_RANGE"):
+                cap = max(ny.value, nx.value, nd.value)
+                continue
+            check(st)
+            return dict(nya=nya[:ny.value].copy(), ya=ya[:ny.value].copy(), nxa=nxa[:nx.value].copy(),
+                        xa=xa[:nx.value].copy(), nda=nda[:nd.value].copy(), da=da[:nd.value].copy())
+
     def genintbreit(self, itype, wfact, e, accy=0.0):
         """GENINTBREIT1/2 on the device (gg_genintbreit): (INDTP, VALTP,
         KSTARTBREIT, J2MAX) of the type-1 or type-2 table."""
@@ -450,7 +488,7 @@ def projected_eig(s, m, mvec=None):
 
 
 def _lib_status(name):
-    return {"GG_ERR_CONVERGE": -7}[name]
+    return {"GG_ERR_CONVERGE": -7, "GG_ERR_RANGE": -5}[name]
 
 
 def launch_count():

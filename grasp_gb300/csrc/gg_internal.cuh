@@ -210,6 +210,7 @@ struct gg_ctx {
   cudaStream_t aux = nullptr;   // second blocking stream: uploads that overlap work on `stream`
   cudaEvent_t aux_done = nullptr;
   gg::BreitTable breit[2];      // GENINTBREIT1, GENINTBREIT2
+  std::shared_ptr<void> setcof; // setcof.cu: the sums of the last gg_setcof_prepare
 };
 
 struct gg_hmat {
@@ -280,6 +281,8 @@ int timer_start(gg_ctx *ctx);
 int timer_stop(gg_ctx *ctx, double *ms);
 // spmv.cu
 int build_sym(gg_hmat *h);
+// setham.cu: CLRX (lib9290/clrx.f90) on the host
+double clrx_host(int kappaa, int k, int kappab);
 // hostmat.cu: the leading ns x ns block of a host-resident matrix as a
 // device matrix
 int leading_block_host(gg_hmat *h, int ns, gg_hmat **out);

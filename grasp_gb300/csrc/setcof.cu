@@ -1,0 +1,389 @@
+// setcof.cu - SETCOF (rmcdhf90/setcof.f90) on the device: the coefficient
+// lists of the direct (YPOT), exchange (XPOT) and one-body (DACON)
+// potentials of an orbital, from the blocks' T/V lists and the mixing
+// coefficients.
+//
+// The reference reads mcp.30/31/32+k from disk once per orbital and SCF
+// iteration and, for each label that involves the orbital, adds its
+// contributions' DSUBRS(IR, IC) COEFF (dsubrs.f90: the generalized weight of
+// the CSF pair). Those label sums do not depend on the orbital except
+// through the final 1/UCF(J), so here one pass computes them for every label
+// of every block (one thread per label, contributions added in list order,
+// as the reference does), together with the diagonal FCO/GCO sums of every
+// (J, IB, K) (one thread each, CSFs in block and row order). A call for
+// orbital J then only filters and merges the labels on the host, in the
+// reference's order (FCO, GCO, the T list by block, the V^k lists by k and
+// block), so its lists are the reference's entry for entry.
+#include <algorithm>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "gg_internal.cuh"
+
+namespace gg {
+
+// the prepared sums of the last gg_setcof_prepare
+struct SetcofState {
+  int nblocks = 0, eol = 0;
+  int kmaxf = -1;                             // largest over the blocks
+  std::vector<int> bkmaxf;                    // per block
+  std::vector<std::vector<int64_t>> lab0;     // per block: first label of each list (T, V0..)
+  std::vector<std::vector<int32_t>> labs;     // per block: the labels of all its lists
+  std::vector<std::vector<double>> sums;      // per block: each label's sum of DSUBRS COEFF (x2 off the diagonal)
+  std::vector<double> fco, gco;               // [J][IB][K] diagonal sums (index below)
+  int kdim = 0;
+  size_t idx(int j, int ib, int k) const { return ((size_t)(j - 1) * nw + (ib - 1)) * kdim + k; }
+  int nw = 0;
+};
+
+namespace {
+
+// DSUBRS (rmcdhf90/dsubrs.f90:20-33): EOL, sum over the block's levels of
+// EVEC(I) EVEC(J) WT(level); otherwise WT(I) on the diagonal, 0 elsewhere
+__device__ __forceinline__ double dsubrs(int eol, int i, int j, int ncf, int nev, const double *evec,
+                                         const double *wt) {
+  if (eol) {
+    double d = 0.0;
+    for (int k = 0; k < nev; ++k) d = d + evec[(size_t)k * ncf + (i - 1)] * evec[(size_t)k * ncf + (j - 1)] * wt[k];
+    return d;
+  }
+  return i == j ? wt[i - 1] : 0.0;
+}
+
+// the column owning each EMT position (ICLMN of the mcp records, 1-based)
+__global__ void k_owner(const int64_t *__restrict__ iendc, int ncf, int32_t *__restrict__ owner) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= ncf) return;
+  for (int64_t p = iendc[w] + lane; p < iendc[w + 1]; p += 32) owner[p] = w + 1;
+}
+
+// SUM over a label's contributions (setcof.f90:242-251 for the T list,
+// :302-311 for the V lists): CONTR = DSUBRS(IR, IC) COEFF, doubled when
+// IR != IC, added in list order; IR = IROW(INDX), IC = ICLMN
+__global__ void k_label_sums(int64_t nlab, const int64_t *__restrict__ start, const int32_t *__restrict__ loc,
+                             const double *__restrict__ coeff, const int32_t *__restrict__ irow,
+                             const int32_t *__restrict__ owner, int eol, int ncf, int nev,
+                             const double *__restrict__ evec, const double *__restrict__ wt,
+                             double *__restrict__ out) {
+  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (l >= nlab) return;
+  double sum = 0.0;
+  for (int64_t i = start[l]; i < start[l + 1]; ++i) {
+    const int p = loc[i] - 1;
+    const int ir = irow[p], ic = owner[p];
+    double contr = dsubrs(eol, ir, ic, ncf, nev, evec, wt) * coeff[i];
+    if (ir != ic) contr = contr + contr;
+    sum = sum + contr;
+  }
+  out[l] = sum;
+}
+
+// one block's CSFs for the diagonal sums
+struct DiagBlock {
+  int ncf, nev;
+  const double *evec, *wt;
+  const uint8_t *iq;      // [nconf][nw]
+  const int32_t *conf;    // [ncf]
+};
+
+// one diagonal sum: kind 0 FCO(K, IR, J, IB) (fco.f90), 1 GCO(K, IR, J, IB)
+// (gco.f90); c = CLRX of the item
+struct DiagItem {
+  int kind, j, ib, k;
+  int fullj, fullb;  // 2j + 1 of J and IB (a full subshell)
+  double c;
+};
+
+// SUMR = sum over blocks and CSFs of DSUBRS(IR, IR) FCO/GCO (setcof.f90:82-90,
+// 121-129), CSFs in block and row order
+__global__ void k_diag_sums(const DiagItem *__restrict__ items, int nitems, const DiagBlock *__restrict__ blocks,
+                            int nblocks, int nw, int eol, double *__restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nitems) return;
+  const DiagItem it = items[t];
+  double sumr = 0.0;
+  for (int b = 0; b < nblocks; ++b) {
+    const DiagBlock B = blocks[b];
+    for (int ir = 1; ir <= B.ncf; ++ir) {
+      const uint8_t *q = B.iq + (size_t)B.conf[ir - 1] * nw;
+      const int qa = q[it.j - 1], qb = q[it.ib - 1];
+      double f = 0.0;
+      if (it.kind == 0) {
+        if (it.j == it.ib) {
+          if (it.k == 0) {
+            f = (double)((qa * (qa - 1)) / 2);
+          } else if (qa == it.fullj) {
+            const double fac = it.c * (double)qa;
+            f = -0.5 * fac * fac;
+          }
+        } else if (it.k == 0) {
+          f = (double)(qa * qb);
+        }
+      } else if (qa == it.fullj || qb == it.fullb) {
+        f = -(double)(qa * qb) * it.c * it.c;
+      }
+      sumr = sumr + dsubrs(eol, ir, ir, B.ncf, B.nev, B.evec, B.wt) * f;
+    }
+  }
+  out[t] = sumr;
+}
+
+template <class T> int upv(DBuf<T> &b, const std::vector<T> &h, cudaStream_t s) {
+  GG_TRY(b.alloc(std::max<size_t>(1, h.size())));
+  if (!h.empty()) GG_CUDA(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  return GG_OK;
+}
+
+// appends (label, value) or, when merge and the label is already listed,
+// adds to its value (the reference's "check it against the previously
+// recorded" search: the first entry with that label)
+void put(std::vector<int32_t> &lab, std::vector<double> &val, int32_t l, double v, bool merge) {
+  if (merge)
+    for (size_t i = 0; i < lab.size(); ++i)
+      if (lab[i] == l) {
+        val[i] = val[i] + v;
+        return;
+      }
+  lab.push_back(l);
+  val.push_back(v);
+}
+
+}  // namespace
+}  // namespace gg
+
+using namespace gg;
+
+extern "C" {
+
+int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nev, const double *const *evec,
+                      const double *const *wt, int eol) {
+  if (!ctx || nblocks < 1 || !h || !wt || (eol && (!nev || !evec)))
+    return fail(GG_ERR_ARG, "gg_setcof_prepare: bad arguments");
+  GG_TRY(ensure_orbitals(ctx));
+  GG_CUDA(cudaSetDevice(ctx->device));
+  const Orbitals &o = ctx->orb;
+  const int nw = o.nw;
+  cudaStream_t s = ctx->stream;
+  auto st = std::make_shared<SetcofState>();
+  st->nblocks = nblocks;
+  st->eol = eol ? 1 : 0;
+  st->nw = nw;
+  std::vector<DBuf<double>> devec(nblocks), dwt(nblocks);
+  std::vector<DiagBlock> hb(nblocks);
+  for (int b = 0; b < nblocks; ++b) {
+    gg_hmat *m = h[b];
+    if (!m || m->ctx->device != ctx->device) return fail(GG_ERR_ARG, "gg_setcof_prepare: bad block");
+    Lists &L = *m->lists;
+    if (!L.valid) return fail(GG_ERR_STATE, "gg_setcof_prepare: a block has no lists (gg_setham_upload)");
+    if (m->host_prec >= 0) return fail(GG_ERR_ARG, "gg_setcof_prepare: a host-resident block has no lists");
+    const int ncf = m->ncf, ne = eol ? nev[b] : 0;
+    if (eol && (ne < 1 || !evec[b] || !wt[b])) return fail(GG_ERR_ARG, "gg_setcof_prepare: missing levels");
+    if (!eol && !wt[b]) return fail(GG_ERR_ARG, "gg_setcof_prepare: missing CSF weights");
+    if (eol) {
+      GG_TRY(devec[b].alloc((size_t)ncf * ne));
+      GG_CUDA(cudaMemcpyAsync(devec[b].p, evec[b], (size_t)ncf * ne * sizeof(double), cudaMemcpyHostToDevice, s));
+      GG_TRY(dwt[b].alloc(ne));
+      GG_CUDA(cudaMemcpyAsync(dwt[b].p, wt[b], ne * sizeof(double), cudaMemcpyHostToDevice, s));
+    } else {
+      GG_TRY(dwt[b].alloc(ncf));
+      GG_CUDA(cudaMemcpyAsync(dwt[b].p, wt[b], ncf * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    // every label's sum
+    DBuf<int32_t> owner;
+    DBuf<double> dsum;
+    GG_TRY(owner.alloc(std::max<int64_t>(1, m->nnz)));
+    k_owner<<<(unsigned)(((int64_t)ncf * 32 + 255) / 256), 256, 0, s>>>(m->dIendc.p, ncf, owner.p);
+    ::gg::note_launch();
+    GG_TRY(dsum.alloc(std::max<int64_t>(1, L.nlab)));
+    if (L.nlab > 0) {
+      k_label_sums<<<(unsigned)((L.nlab + 127) / 128), 128, 0, s>>>(L.nlab, L.dStart.p, L.dLoc.p, L.dCoeff.p,
+                                                                   m->dIrow.p, owner.p, st->eol, ncf, ne,
+                                                                   devec[b].p, dwt[b].p, dsum.p);
+      ::gg::note_launch();
+    }
+    GG_CUDA(cudaGetLastError());
+    st->labs.emplace_back(L.nlab);
+    st->sums.emplace_back(L.nlab);
+    if (L.nlab > 0) {
+      GG_CUDA(cudaMemcpyAsync(st->labs.back().data(), L.dLab.p, L.nlab * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+      GG_CUDA(cudaMemcpyAsync(st->sums.back().data(), dsum.p, L.nlab * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    GG_CUDA(cudaStreamSynchronize(s));  // owner and dsum are freed here
+    st->lab0.push_back(L.list_lab0);
+    st->bkmaxf.push_back(L.kmaxf);
+    st->kmaxf = std::max(st->kmaxf, L.kmaxf);
+    hb[b] = DiagBlock{ncf, ne, eol ? devec[b].p : nullptr, dwt[b].p, L.dIq.p, L.dConf.p};
+  }
+  // the diagonal sums of every (J, IB, K) SETCOF asks for
+  int jmax = 0;
+  for (int a = 1; a <= nw; ++a) jmax = std::max(jmax, o.nkj[a]);
+  st->kdim = jmax + 2;
+  std::vector<DiagItem> items;
+  std::vector<size_t> where;
+  for (int j = 1; j <= nw; ++j)
+    for (int ib = 1; ib <= nw; ++ib) {
+      const int kmax = (ib == j) ? o.nkj[j] - 1 : 0;
+      for (int k = 0; k <= kmax; k += 2) {
+        items.push_back(DiagItem{0, j, ib, k, o.nkj[j] + 1, o.nkj[ib] + 1, k > 0 ? clrx_host(o.nak[j], k, o.nak[j]) : 0.0});
+        where.push_back(st->idx(j, ib, k) * 2);
+      }
+      if (ib == j) continue;
+      const int kmin = (o.nak[j] * o.nak[ib] > 0) ? std::abs((o.nkj[j] - o.nkj[ib]) / 2)
+                                                   : std::abs((o.nkj[j] - o.nkj[ib]) / 2) + 1;
+      for (int k = kmin; k <= (o.nkj[j] + o.nkj[ib]) / 2; k += 2) {
+        items.push_back(DiagItem{1, j, ib, k, o.nkj[j] + 1, o.nkj[ib] + 1, clrx_host(o.nak[j], k, o.nak[ib])});
+        where.push_back(st->idx(j, ib, k) * 2 + 1);
+      }
+    }
+  DBuf<DiagItem> ditems;
+  DBuf<DiagBlock> dblocks;
+  DBuf<double> dout;
+  GG_TRY(upv(ditems, items, s));
+  GG_TRY(upv(dblocks, hb, s));
+  GG_TRY(dout.alloc(std::max<size_t>(1, items.size())));
+  if (!items.empty()) {
+    k_diag_sums<<<(unsigned)((items.size() + 63) / 64), 64, 0, s>>>(ditems.p, (int)items.size(), dblocks.p, nblocks,
+                                                                   nw, st->eol, dout.p);
+    ::gg::note_launch();
+  }
+  GG_CUDA(cudaGetLastError());
+  std::vector<double> hv(items.size());
+  if (!items.empty()) GG_CUDA(cudaMemcpyAsync(hv.data(), dout.p, hv.size() * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  st->fco.assign((size_t)nw * nw * st->kdim, 0.0);
+  st->gco.assign((size_t)nw * nw * st->kdim, 0.0);
+  for (size_t t = 0; t < items.size(); ++t) (where[t] % 2 ? st->gco : st->fco)[where[t] / 2] = hv[t];
+  ctx->setcof = st;
+  return GG_OK;
+}
+
+int gg_setcof(gg_ctx *ctx, int j, double ucfj, int cap, int *ny, int32_t *nya, double *ya, int *nx, int32_t *nxa,
+              double *xa, int *nd, int32_t *nda, double *da) {
+  if (!ctx || !ny || !nx || !nd || cap < 0 || (cap > 0 && (!nya || !ya || !nxa || !xa || !nda || !da)))
+    return fail(GG_ERR_ARG, "gg_setcof: bad arguments");
+  const auto st = std::static_pointer_cast<SetcofState>(ctx->setcof);
+  if (!st) return fail(GG_ERR_STATE, "gg_setcof: call gg_setcof_prepare first");
+  const Orbitals &o = ctx->orb;
+  const int nw = st->nw, KEY = KEYORB;
+  if (j < 1 || j > nw || o.nw != nw) return fail(GG_ERR_ARG, "gg_setcof: orbital outside the orbital set");
+  std::vector<int32_t> ly, lx, ld;
+  std::vector<double> vy, vx, vd;
+  // Y from FCO (setcof.f90:73-105): NYA = K + IB KEY (KEY + 1)
+  {
+    int64_t ilabel = 0;
+    const int64_t nwterm = (int64_t)KEY * (KEY + 1);
+    for (int ib = 1; ib <= nw; ++ib) {
+      ilabel += nwterm;
+      const int kmax = (ib == j) ? o.nkj[j] - 1 : 0;
+      for (int k = 0; k <= kmax; k += 2) {
+        const double sumr = st->fco[st->idx(j, ib, k)];
+        const double ykab = (ib == j) ? 2.0 * sumr / ucfj : sumr / ucfj;
+        ly.push_back((int32_t)(k + ilabel));
+        vy.push_back(ykab);
+      }
+    }
+  }
+  // X from GCO (:107-147): NXA = K + KEY J + IB KEY^2 (KEY + 1)
+  {
+    int64_t ilabel = (int64_t)KEY * j;
+    const int64_t nwterm = (int64_t)KEY * KEY * (KEY + 1);
+    for (int ib = 1; ib <= nw; ++ib) {
+      ilabel += nwterm;
+      if (ib == j) continue;
+      const int kmin = (o.nak[j] * o.nak[ib] > 0) ? std::abs((o.nkj[j] - o.nkj[ib]) / 2)
+                                                   : std::abs((o.nkj[j] - o.nkj[ib]) / 2) + 1;
+      for (int k = kmin; k <= (o.nkj[j] + o.nkj[ib]) / 2; k += 2) {
+        lx.push_back((int32_t)(k + ilabel));
+        vx.push_back(st->gco[st->idx(j, ib, k)] / ucfj);
+      }
+    }
+  }
+  // DA from the T lists, block by block (:188-285)
+  for (int b = 0; b < st->nblocks; ++b) {
+    const int64_t l0 = st->lab0[b][0], l1 = st->lab0[b][1];
+    for (int64_t l = l0; l < l1; ++l) {
+      const int32_t lab = st->labs[b][l];
+      const int ia = lab % KEY, ibb = lab / KEY;
+      if (ia != j && ibb != j) continue;
+      const double sum = 0.5 * st->sums[b][l] / ucfj;
+      put(ld, vd, ia == j ? ibb : ia, sum, b > 0);
+    }
+  }
+  // the V^k lists, k by k and block by block (:287-515)
+  for (int k = 0; k <= st->kmaxf; ++k)
+    for (int b = 0; b < st->nblocks; ++b) {
+      if (k > st->bkmaxf[b]) continue;
+      const int64_t l0 = st->lab0[b][k + 1], l1 = st->lab0[b][k + 2];
+      const bool merge = b > 0;
+      for (int64_t l = l0; l < l1; ++l) {
+        int32_t lab = st->labs[b][l];
+        int ix[4];
+        ix[3] = lab % KEY;
+        lab /= KEY;
+        ix[1] = lab % KEY;
+        lab /= KEY;
+        ix[2] = lab % KEY;
+        ix[0] = lab / KEY;
+        int irank = 0;
+        for (int t = 0; t < 4; ++t) irank += (ix[t] == j);
+        if (irank == 0) continue;
+        const double sum = 0.5 * st->sums[b][l] / ucfj;
+        auto at = [&](int p) { return ix[(p - 1) % 4]; };  // INDEXS(IL), IL wrapped into 1..4
+        if (irank == 1) {
+          int ithis = 0;
+          for (int iind = 1; iind <= 4; ++iind) {
+            if (ix[iind - 1] != j) continue;
+            ithis = ((at(iind + 2) * KEY + at(iind + 3)) * KEY + at(iind + 1)) * KEY + k;
+            break;
+          }
+          put(lx, vx, ithis, sum, merge);
+        } else if (irank == 2) {
+          int loc1 = 0, loc2 = 0, found = 0;
+          for (int iind = 1; iind <= 4; ++iind) {
+            if (ix[iind - 1] != j) continue;
+            if (found == 0) {
+              loc1 = iind;
+              found = 1;
+            } else {
+              loc2 = iind;
+              break;
+            }
+          }
+          if (loc2 - loc1 == 2) {
+            const int ithis = (at(loc1 + 3) * KEY + at(loc1 + 1)) * KEY + k;
+            put(ly, vy, ithis, sum + sum, merge);
+          } else {
+            const int ithis = ((at(loc1 + 2) * KEY + at(loc1 + 3)) * KEY + at(loc1 + 1)) * KEY + k;
+            put(lx, vx, ithis, sum + sum, merge);
+          }
+        } else if (irank == 3) {
+          int ithis = 0, ithis2 = 0;
+          for (int iind = 1; iind <= 4; ++iind) {
+            if (ix[iind - 1] == j) continue;
+            const int other = ix[iind - 1];
+            ithis = (other * KEY + j) * KEY + k;
+            ithis2 = ((other * KEY + j) * KEY + j) * KEY + k;
+          }
+          put(ly, vy, ithis, sum + sum, merge);
+          put(lx, vx, ithis2, sum, merge);
+        } else {
+          put(ly, vy, (j * KEY + j) * KEY + k, 4.0 * sum, merge);
+        }
+      }
+    }
+  *ny = (int)ly.size();
+  *nx = (int)lx.size();
+  *nd = (int)ld.size();
+  if ((int)ly.size() > cap || (int)lx.size() > cap || (int)ld.size() > cap)
+    return fail(GG_ERR_RANGE, "gg_setcof: a list is longer than cap (the counts are set)");
+  std::copy(ly.begin(), ly.end(), nya);
+  std::copy(vy.begin(), vy.end(), ya);
+  std::copy(lx.begin(), lx.end(), nxa);
+  std::copy(vx.begin(), vx.end(), xa);
+  std::copy(ld.begin(), ld.end(), nda);
+  std::copy(vd.begin(), vd.end(), da);
+  return GG_OK;
+}
+
+}  // extern "C"

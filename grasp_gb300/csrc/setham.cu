@@ -424,6 +424,9 @@ long long host_rk_pos(const RkTable &rk, int nw, int ia, int ib, int ic, int id,
 }
 
 }  // namespace
+
+double clrx_host(int kappaa, int k, int kappab) { return clrx(kappaa, k, kappab); }
+
 }  // namespace gg
 
 using namespace gg;

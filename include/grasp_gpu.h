@@ -148,6 +148,26 @@ typedef struct {
  * RINTI, by the reference's three cases (a fixed orbital, occupation numbers
  * more than 10 % apart, close occupations). ucf[nw], lfix[nw] (0/1): UCF and
  * LFIX of every orbital. Entries of cof for orbitals in no pair are not read. */
+/* SETCOF (rmcdhf90/setcof.f90:3) from the blocks' T/V lists on the device.
+ * gg_setcof_prepare: the sums SETCOF forms from the mixing coefficients, for
+ * every orbital at once: each label's sum over its contributions of
+ * DSUBRS(IR, IC) COEFF, doubled off the diagonal (setcof.f90:242-251,
+ * 302-311), and every diagonal FCO/GCO sum over the CSFs (:82-90, :121-129).
+ * h[nblocks]: the blocks in rmcdhf's order, their lists uploaded with
+ * gg_setham_upload (which also gave their IQ). eol != 0 (EOL): DSUBRS from
+ * the levels (dsubrs.f90:20-28), evec[b] the block's nev[b] eigenvectors
+ * (NCF_b x nev[b], column-major) and wt[b] their weights; eol = 0: wt[b] the
+ * NCF_b weights DSUBRS(IR, IR) = WT(IR) reads, evec and nev unused. The sums
+ * stay with the context until the next call.
+ * gg_setcof: SETCOF(EOL, J)'s lists for orbital j with UCF(J) = ucfj, from
+ * the prepared sums: YPOT's (*ny, nya, ya), XPOT's (*nx, nxa, xa) and
+ * DACON's (*nd, nda, da), entry for entry the reference's (its order and
+ * its merging of repeated labels across blocks). Each output array holds
+ * cap entries; GG_ERR_RANGE (with the counts set) when a list is longer.   */
+int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *nev, const double *const *evec,
+                      const double *const *wt, int eol);
+int gg_setcof(gg_ctx *ctx, int j, double ucfj, int cap, int *ny, int32_t *nya, double *ya, int *nx, int32_t *nxa,
+              double *xa, int *nd, int32_t *nda, double *da);
 int gg_cofpot(gg_ctx *ctx, int j, double ucfj, const gg_cof *cof, int nec, const int32_t *iecc, const double *ecv,
               double accy, double *yp, double *xp, double *xq);
 int gg_setlag(gg_ctx *ctx, int nec, const int32_t *iecc, const double *ucf, const int *lfix, const gg_cof *cof,

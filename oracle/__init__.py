@@ -47,6 +47,12 @@ class OrList(C.Structure):
     ]
 
 
+class OrBlock(C.Structure):
+    _fields_ = [("ncf", C.c_int), ("iendc", _i64), ("irow", _i32), ("iq", C.POINTER(C.c_uint8)),
+                ("tlist", OrList), ("kmaxf", C.c_int), ("vlists", C.POINTER(OrList)), ("nev", C.c_int),
+                ("evec", _d), ("wt", _d)]
+
+
 class OrDvdParams(C.Structure):
     _fields_ = [
         ("lim", C.c_int), ("ilow", C.c_int), ("ihigh", C.c_int), ("niv", C.c_int),
@@ -91,6 +97,8 @@ def lib():
         L.or_clrx.argtypes = [C.c_int] * 3
         L.or_setham.argtypes = [C.c_void_p, C.c_int, C.c_int64, _i64, C.POINTER(C.c_uint8),
                                 C.POINTER(OrList), C.c_int, C.POINTER(OrList), _d]
+        L.or_setcof.argtypes = [C.c_void_p, C.c_int, C.POINTER(OrBlock), C.c_int, C.c_int, C.c_double, C.c_int,
+                                _int, _i32, _d, _int, _i32, _d, _int, _i32, _d]
         L.or_shift_eav.restype = C.c_double
         L.or_shift_eav.argtypes = [C.c_int, _i64, _d]
         L.or_spicmv2.argtypes = [C.c_int, C.c_int, _i64, _i32, _d, _d, _d]
@@ -271,6 +279,48 @@ class Oracle:
         if rc != 0:
             raise KeyError("Rkintc Integral not found")
         return out.value
+
+    def setcof(self, blocks, eol, j, ucfj):
+        """SETCOF (rmcdhf90/setcof.f90) for orbital j. blocks: dicts with ncf,
+        iendc, irow, iq ([ncf x nw] bytes), tlist, vlists (dicts of lab,
+        start, loc, coeff), and the mixing data: evec ([ncf x nev]) and wt
+        (nev level weights) when eol, else wt = the ncf CSF weights."""
+        keep = []
+
+        def mk(d):
+            lab = np.ascontiguousarray(d["lab"], np.int32); st = np.ascontiguousarray(d["start"], np.int64)
+            loc = np.ascontiguousarray(d["loc"], np.int32); co = np.ascontiguousarray(d["coeff"], np.float64)
+            keep.extend([lab, st, loc, co])
+            return OrList(lab.size, _p(lab, _i32), _p(st, _i64), _p(loc, _i32), _p(co, _d))
+
+        obs = []
+        for b in blocks:
+            iendc = np.ascontiguousarray(b["iendc"], np.int64); irow = np.ascontiguousarray(b["irow"], np.int32)
+            iq = np.ascontiguousarray(b["iq"], np.uint8); wt = np.ascontiguousarray(b["wt"], np.float64)
+            vl = (OrList * max(1, len(b["vlists"])))(*[mk(v) for v in b["vlists"]])
+            keep.extend([iendc, irow, iq, wt, vl])
+            if eol:
+                ev = np.asfortranarray(np.asarray(b["evec"], np.float64).reshape(b["ncf"], -1))
+                keep.append(ev)
+                evp, nev = _p(ev, _d), ev.shape[1]
+            else:
+                evp, nev = None, 0
+            obs.append(OrBlock(b["ncf"], _p(iendc, _i64), _p(irow, _i32), iq.ctypes.data_as(C.POINTER(C.c_uint8)),
+                               mk(b["tlist"]), len(b["vlists"]) - 1, vl, nev, evp, _p(wt, _d)))
+        arr = (OrBlock * len(obs))(*obs)
+        cap = 4096
+        while True:
+            ny, nx, nd = C.c_int(), C.c_int(), C.c_int()
+            nya = np.zeros(cap, np.int32); ya = np.zeros(cap); nxa = np.zeros(cap, np.int32); xa = np.zeros(cap)
+            nda = np.zeros(cap, np.int32); da = np.zeros(cap)
+            rc = lib().or_setcof(self._h, len(obs), arr, int(bool(eol)), j, ucfj, cap, C.byref(ny), _p(nya, _i32),
+                                 _p(ya, _d), C.byref(nx), _p(nxa, _i32), _p(xa, _d), C.byref(nd), _p(nda, _i32),
+                                 _p(da, _d))
+            if rc == -2:
+                cap = max(ny.value, nx.value, nd.value)
+                continue
+            return dict(nya=nya[:ny.value].copy(), ya=ya[:ny.value].copy(), nxa=nxa[:nx.value].copy(),
+                        xa=xa[:nx.value].copy(), nda=nda[:nd.value].copy(), da=da[:nd.value].copy())
 
     def setham(self, ncf, nelmnt, iendc, iq, tlist, vlists):
         """tlist / vlists: dicts with 'lab', 'start', 'loc', 'coeff' numpy arrays."""

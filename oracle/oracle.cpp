@@ -1610,6 +1610,182 @@ int or_setham(or_ctx *g, int ncf, int64_t nelmnt, const int64_t *iendc, const ui
   return 0;
 }
 
+// DSUBRS (rmcdhf90/dsubrs.f90:20-33), block-local CSF indices
+static double dsubrs(int eol, int I, int J, const or_block &B) {
+  if (eol) {
+    double d = 0.0;
+    for (int k = 1; k <= B.nev; ++k)
+      d = d + B.evec[(size_t)(k - 1) * B.ncf + (I - 1)] * B.evec[(size_t)(k - 1) * B.ncf + (J - 1)] * B.wt[k - 1];
+    return d;
+  }
+  return I == J ? B.wt[I - 1] : 0.0;
+}
+
+// SETCOF (rmcdhf90/setcof.f90:48-524): the reference's loops, lists in the
+// order it builds them, a repeated label of a later block merged into the
+// first entry with that label
+int or_setcof(or_ctx *g, int nblocks, const or_block *blocks, int eol, int J, double UCFJ, int cap, int *ny,
+              int32_t *nya, double *ya, int *nx, int32_t *nxa, double *xa, int *nd, int32_t *nda, double *da) {
+  const int KEY = 215, NW = g->nw;
+  std::vector<int32_t> NYA, NXA, NDA;
+  std::vector<double> YA, XA, DA;
+  auto merge = [](std::vector<int32_t> &lab, std::vector<double> &val, int32_t l, double v, bool search) {
+    if (search)
+      for (size_t i = 0; i < lab.size(); ++i)
+        if (lab[i] == l) {
+          val[i] = val[i] + v;
+          return;
+        }
+    lab.push_back(l);
+    val.push_back(v);
+  };
+  const int NAKJ = g->NAK[J], NKJJ = g->NKJ[J];
+  // :73-105
+  int64_t ILABEL = 0;
+  int64_t NWTERM = (int64_t)KEY * (KEY + 1);
+  for (int IB = 1; IB <= NW; ++IB) {
+    ILABEL = ILABEL + NWTERM;
+    const int KMAX = (IB == J) ? NKJJ - 1 : 0;
+    for (int K = 0; K <= KMAX; K += 2) {
+      double SUMR = 0.0;
+      for (int nb = 0; nb < nblocks; ++nb) {
+        const or_block &B = blocks[nb];
+        for (int IR = 1; IR <= B.ncf; ++IR)
+          SUMR = SUMR + dsubrs(eol, IR, IR, B) * fco(g, K, B.iq + (size_t)(IR - 1) * NW, J, IB);
+      }
+      const double YKAB = (IB == J) ? 2.0 * SUMR / UCFJ : SUMR / UCFJ;
+      NYA.push_back((int32_t)(K + ILABEL));
+      YA.push_back(YKAB);
+    }
+  }
+  // :107-147
+  ILABEL = (int64_t)KEY * J;
+  NWTERM = (int64_t)KEY * KEY * (KEY + 1);
+  for (int IB = 1; IB <= NW; ++IB) {
+    ILABEL = ILABEL + NWTERM;
+    if (IB == J) continue;
+    const int NKJIB = g->NKJ[IB];
+    const int KMIN = (NAKJ * g->NAK[IB] > 0) ? std::abs((NKJJ - NKJIB) / 2) : std::abs((NKJJ - NKJIB) / 2) + 1;
+    const int KMAX = (NKJJ + NKJIB) / 2;
+    for (int K = KMIN; K <= KMAX; K += 2) {
+      double SUMR = 0.0;
+      for (int nb = 0; nb < nblocks; ++nb) {
+        const or_block &B = blocks[nb];
+        for (int IR = 1; IR <= B.ncf; ++IR)
+          SUMR = SUMR + dsubrs(eol, IR, IR, B) * gco(g, K, B.iq + (size_t)(IR - 1) * NW, J, IB);
+      }
+      NXA.push_back((int32_t)(K + ILABEL));
+      XA.push_back(SUMR / UCFJ);
+    }
+  }
+  // the column (ICLMN) owning each position of a block
+  auto owners = [](const or_block &B) {
+    std::vector<int32_t> own((size_t)B.iendc[B.ncf]);
+    for (int c = 1; c <= B.ncf; ++c)
+      for (int64_t p = B.iendc[c - 1]; p < B.iendc[c]; ++p) own[p] = c;
+    return own;
+  };
+  auto label_sum = [&](const or_block &B, const std::vector<int32_t> &own, const or_list &L, int64_t l) {
+    double SUM = 0.0;
+    for (int64_t i = L.start[l]; i < L.start[l + 1]; ++i) {
+      const int IR = B.irow[L.loc[i] - 1], IC = own[L.loc[i] - 1];
+      double CONTR = dsubrs(eol, IR, IC, B) * L.coeff[i];
+      if (IR != IC) CONTR = CONTR + CONTR;
+      SUM = SUM + CONTR;
+    }
+    return 0.5 * SUM / UCFJ;
+  };
+  // :188-285, the T list of each block
+  for (int nb = 0; nb < nblocks; ++nb) {
+    const or_block &B = blocks[nb];
+    const std::vector<int32_t> own = owners(B);
+    for (int64_t l = 0; l < B.tlist.nlab; ++l) {
+      const int LAB = B.tlist.lab[l];
+      const int IA = LAB % KEY, IB = LAB / KEY;
+      if (IA != J && IB != J) continue;
+      const double SUM = label_sum(B, own, B.tlist, l);
+      merge(NDA, DA, IA == J ? IB : IA, SUM, nb > 0);
+    }
+  }
+  // :287-515, the V^k lists, k by k, block by block
+  int KMAXF = -1;
+  for (int nb = 0; nb < nblocks; ++nb) KMAXF = std::max(KMAXF, blocks[nb].kmaxf);
+  for (int K = 0; K <= KMAXF; ++K)
+    for (int nb = 0; nb < nblocks; ++nb) {
+      const or_block &B = blocks[nb];
+      if (K > B.kmaxf) continue;
+      const std::vector<int32_t> own = owners(B);
+      const or_list &L = B.vlists[K];
+      for (int64_t l = 0; l < L.nlab; ++l) {
+        int LAB = L.lab[l];
+        int INDEXS[5];
+        INDEXS[4] = LAB % KEY;
+        LAB = LAB / KEY;
+        INDEXS[2] = LAB % KEY;
+        LAB = LAB / KEY;
+        INDEXS[3] = LAB % KEY;
+        INDEXS[1] = LAB / KEY;
+        int IRANK = 0;
+        for (int t = 1; t <= 4; ++t) IRANK += (INDEXS[t] == J);
+        if (IRANK == 0) continue;
+        const double SUM = label_sum(B, own, L, l);
+        auto wrap = [](int il) { return il > 4 ? il - 4 : il; };
+        if (IRANK == 1) {
+          int ITHIS = -911;
+          for (int IIND = 1; IIND <= 4; ++IIND) {
+            if (INDEXS[IIND] != J) continue;
+            const int IORB = INDEXS[wrap(IIND + 2)], IYO1 = INDEXS[wrap(IIND + 1)], IYO2 = INDEXS[wrap(IIND + 3)];
+            ITHIS = ((IORB * KEY + IYO2) * KEY + IYO1) * KEY + K;
+            break;
+          }
+          merge(NXA, XA, ITHIS, SUM, nb > 0);
+        } else if (IRANK == 2) {
+          int IFOUND = 0, LOC1 = 0, LOC2 = 0;
+          for (int IIND = 1; IIND <= 4; ++IIND) {
+            if (INDEXS[IIND] != J) continue;
+            if (IFOUND == 0) {
+              LOC1 = IIND;
+              IFOUND = IFOUND + 1;
+            } else if (IFOUND == 1) {
+              LOC2 = IIND;
+              break;
+            }
+          }
+          if (LOC2 - LOC1 == 2) {
+            const int IYO2 = INDEXS[wrap(LOC1 + 3)], IYO1 = INDEXS[wrap(LOC1 + 1)];
+            merge(NYA, YA, (IYO2 * KEY + IYO1) * KEY + K, SUM + SUM, nb > 0);
+          } else {
+            const int IORB = INDEXS[wrap(LOC1 + 2)], IYO1 = INDEXS[wrap(LOC1 + 1)], IYO2 = INDEXS[wrap(LOC1 + 3)];
+            merge(NXA, XA, ((IORB * KEY + IYO2) * KEY + IYO1) * KEY + K, SUM + SUM, nb > 0);
+          }
+        } else if (IRANK == 3) {
+          int ITHIS = -911, ITHIS2 = -911;
+          for (int IIND = 1; IIND <= 4; ++IIND) {
+            if (INDEXS[IIND] == J) continue;
+            const int INDIND = INDEXS[IIND];
+            ITHIS = (INDIND * KEY + J) * KEY + K;
+            ITHIS2 = ((INDIND * KEY + J) * KEY + J) * KEY + K;
+          }
+          merge(NYA, YA, ITHIS, SUM + SUM, nb > 0);
+          merge(NXA, XA, ITHIS2, SUM, nb > 0);
+        } else {
+          merge(NYA, YA, (J * KEY + J) * KEY + K, 4.0 * SUM, nb > 0);
+        }
+      }
+    }
+  *ny = (int)NYA.size();
+  *nx = (int)NXA.size();
+  *nd = (int)NDA.size();
+  if (*ny > cap || *nx > cap || *nd > cap) return -2;
+  std::copy(NYA.begin(), NYA.end(), nya);
+  std::copy(YA.begin(), YA.end(), ya);
+  std::copy(NXA.begin(), NXA.end(), nxa);
+  std::copy(XA.begin(), XA.end(), xa);
+  std::copy(NDA.begin(), NDA.end(), nda);
+  std::copy(DA.begin(), DA.end(), da);
+  return 0;
+}
+
 double or_shift_eav(int ncf, const int64_t *iendc, double *emt) {
   double eav = 0.0;
   for (int ir = 1; ir <= ncf; ++ir) eav = eav + emt[iendc[ir] - 1];

@@ -92,6 +92,27 @@ int or_setham(or_ctx *, int ncf, int64_t nelmnt, const int64_t *iendc,
               const uint8_t *iq, const or_list *tlist, int kmaxf,
               const or_list *vlists, double *emt);
 
+/* SETCOF (rmcdhf90/setcof.f90:48-524) for orbital j: one block's data as
+ * SETCOF reads it (its mcp.30 structure, its T/V lists, its IQ) and the
+ * mixing coefficients DSUBRS reads (dsubrs.f90): eol != 0: nev levels,
+ * evec [ncf x nev] column-major, wt[nev]; eol == 0: wt[ncf] CSF weights. */
+typedef struct {
+  int ncf;
+  const int64_t *iendc;
+  const int32_t *irow;
+  const uint8_t *iq;
+  or_list tlist;
+  int kmaxf;
+  const or_list *vlists;
+  int nev;
+  const double *evec;
+  const double *wt;
+} or_block;
+/* the lists (NYA/YA, NXA/XA, NDA/DA), cap entries each; -2 when a list is
+ * longer (counts set) */
+int or_setcof(or_ctx *, int nblocks, const or_block *blocks, int eol, int j, double ucfj, int cap, int *ny,
+              int32_t *nya, double *ya, int *nx, int32_t *nxa, double *xa, int *nd, int32_t *nda, double *da);
+
 /* EAV and its subtraction from the diagonal (rmcdhf90/matrix.f90:178-203). */
 double or_shift_eav(int ncf, const int64_t *iendc, double *emt);
 
