@@ -17,6 +17,8 @@
 #include <algorithm>
 #include <cstring>
 #include <memory>
+#include <tuple>
+#include <utility>
 #include <vector>
 
 #include "gg_internal.cuh"
@@ -35,20 +37,42 @@ struct SetcofState {
   int kdim = 0;
   size_t idx(int j, int ib, int k) const { return ((size_t)(j - 1) * nw + (ib - 1)) * kdim + k; }
   int nw = 0;
+  // per orbital, the labels that name it: T labels as (block, label), V
+  // labels as (k, block, label), each in the order SETCOF visits them
+  std::vector<std::vector<std::pair<int, int64_t>>> tref;
+  std::vector<std::vector<std::tuple<int, int, int64_t>>> vref;
 };
 
 namespace {
 
 // DSUBRS (rmcdhf90/dsubrs.f90:20-33): EOL, sum over the block's levels of
-// EVEC(I) EVEC(J) WT(level); otherwise WT(I) on the diagonal, 0 elsewhere
-__device__ __forceinline__ double dsubrs(int eol, int i, int j, int ncf, int nev, const double *evec,
-                                         const double *wt) {
+// EVEC(I) EVEC(J) WT(level); otherwise WT(I) on the diagonal, 0 elsewhere.
+// ev holds the levels' coefficients by CSF ([ncf][nev]: one CSF's nev
+// values contiguous), the same products in the same order.
+__device__ __forceinline__ double dsubrs(int eol, int i, int j, int nev, const double *ev, const double *wt) {
   if (eol) {
+    const double *a = ev + (size_t)(i - 1) * nev, *b = ev + (size_t)(j - 1) * nev;
     double d = 0.0;
-    for (int k = 0; k < nev; ++k) d = d + evec[(size_t)k * ncf + (i - 1)] * evec[(size_t)k * ncf + (j - 1)] * wt[k];
+    for (int k = 0; k < nev; ++k) d = d + a[k] * b[k] * wt[k];
     return d;
   }
   return i == j ? wt[i - 1] : 0.0;
+}
+
+// the levels' coefficients by CSF: evr[r][k] = evec[k][r]
+__global__ void k_by_csf(const double *__restrict__ evec, int ncf, int nev, double *__restrict__ evr) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < (int64_t)ncf * nev;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int r = (int)(e / nev), k = (int)(e % nev);
+    evr[e] = evec[(size_t)k * ncf + r];
+  }
+}
+
+// DSUBRS(IR, IR) of every CSF
+__global__ void k_dsubrs_diag(int eol, int ncf, int nev, const double *__restrict__ ev, const double *__restrict__ wt,
+                              double *__restrict__ d) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < ncf) d[r] = dsubrs(eol, r + 1, r + 1, nev, ev, wt);
 }
 
 // the column owning each EMT position (ICLMN of the mcp records, 1-based)
@@ -60,29 +84,48 @@ __global__ void k_owner(const int64_t *__restrict__ iendc, int ncf, int32_t *__r
 
 // SUM over a label's contributions (setcof.f90:242-251 for the T list,
 // :302-311 for the V lists): CONTR = DSUBRS(IR, IC) COEFF, doubled when
-// IR != IC, added in list order; IR = IROW(INDX), IC = ICLMN
-__global__ void k_label_sums(int64_t nlab, const int64_t *__restrict__ start, const int32_t *__restrict__ loc,
-                             const double *__restrict__ coeff, const int32_t *__restrict__ irow,
-                             const int32_t *__restrict__ owner, int eol, int ncf, int nev,
-                             const double *__restrict__ evec, const double *__restrict__ wt,
-                             double *__restrict__ out) {
-  const int64_t l = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// IR != IC, added in list order; IR = IROW(INDX), IC = ICLMN. One warp per
+// label: the lanes form 32 consecutive CONTR at a time (their gathers in
+// flight together) into shared memory, lane 0 adds them in order.
+constexpr int LS_WARPS = 4;
+__global__ void __launch_bounds__(LS_WARPS * 32) k_label_sums(int64_t nlab, const int64_t *__restrict__ start,
+                                                              const int32_t *__restrict__ loc,
+                                                              const double *__restrict__ coeff,
+                                                              const int32_t *__restrict__ irow,
+                                                              const int32_t *__restrict__ owner, int eol, int nev,
+                                                              const double *__restrict__ ev,
+                                                              const double *__restrict__ wt,
+                                                              double *__restrict__ out) {
+  __shared__ double cs[LS_WARPS][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t l = blockIdx.x * (int64_t)LS_WARPS + w;
   if (l >= nlab) return;
   double sum = 0.0;
-  for (int64_t i = start[l]; i < start[l + 1]; ++i) {
-    const int p = loc[i] - 1;
-    const int ir = irow[p], ic = owner[p];
-    double contr = dsubrs(eol, ir, ic, ncf, nev, evec, wt) * coeff[i];
-    if (ir != ic) contr = contr + contr;
-    sum = sum + contr;
+  const int64_t i0 = start[l], i1 = start[l + 1];
+  for (int64_t c = i0; c < i1; c += 32) {
+    const int64_t i = c + lane;
+    double contr = 0.0;
+    if (i < i1) {
+      const int p = loc[i] - 1;
+      const int ir = irow[p], ic = owner[p];
+      contr = dsubrs(eol, ir, ic, nev, ev, wt) * coeff[i];
+      if (ir != ic) contr = contr + contr;
+    }
+    cs[w][lane] = contr;
+    __syncwarp();
+    if (lane == 0) {
+      const int n = (int)min((int64_t)32, i1 - c);
+      for (int t = 0; t < n; ++t) sum = sum + cs[w][t];
+    }
+    __syncwarp();
   }
-  out[l] = sum;
+  if (lane == 0) out[l] = sum;
 }
 
 // one block's CSFs for the diagonal sums
 struct DiagBlock {
-  int ncf, nev;
-  const double *evec, *wt;
+  int ncf;
+  const double *d;        // DSUBRS(IR, IR)
   const uint8_t *iq;      // [nconf][nw]
   const int32_t *conf;    // [ncf]
 };
@@ -96,16 +139,23 @@ struct DiagItem {
 };
 
 // SUMR = sum over blocks and CSFs of DSUBRS(IR, IR) FCO/GCO (setcof.f90:82-90,
-// 121-129), CSFs in block and row order
-__global__ void k_diag_sums(const DiagItem *__restrict__ items, int nitems, const DiagBlock *__restrict__ blocks,
-                            int nblocks, int nw, int eol, double *__restrict__ out) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+// 121-129), CSFs in block and row order. One warp per sum: the lanes form
+// 32 consecutive terms, lane 0 adds them in order.
+__global__ void __launch_bounds__(LS_WARPS * 32) k_diag_sums(const DiagItem *__restrict__ items, int nitems,
+                                                             const DiagBlock *__restrict__ blocks, int nblocks,
+                                                             int nw, double *__restrict__ out) {
+  __shared__ double cs[LS_WARPS][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x * LS_WARPS + w;
   if (t >= nitems) return;
   const DiagItem it = items[t];
   double sumr = 0.0;
   for (int b = 0; b < nblocks; ++b) {
     const DiagBlock B = blocks[b];
-    for (int ir = 1; ir <= B.ncf; ++ir) {
+    for (int r0 = 1; r0 <= B.ncf; r0 += 32) {
+      const int ir = r0 + lane;
+      double term = 0.0;
+      if (ir <= B.ncf) {
       const uint8_t *q = B.iq + (size_t)B.conf[ir - 1] * nw;
       const int qa = q[it.j - 1], qb = q[it.ib - 1];
       double f = 0.0;
@@ -123,10 +173,18 @@ __global__ void k_diag_sums(const DiagItem *__restrict__ items, int nitems, cons
       } else if (qa == it.fullj || qb == it.fullb) {
         f = -(double)(qa * qb) * it.c * it.c;
       }
-      sumr = sumr + dsubrs(eol, ir, ir, B.ncf, B.nev, B.evec, B.wt) * f;
+      term = B.d[ir - 1] * f;
+      }
+      cs[w][lane] = term;
+      __syncwarp();
+      if (lane == 0) {
+        const int n = min(32, B.ncf - r0 + 1);
+        for (int u = 0; u < n; ++u) sumr = sumr + cs[w][u];
+      }
+      __syncwarp();
     }
   }
-  out[t] = sumr;
+  if (lane == 0) out[t] = sumr;
 }
 
 template <class T> int upv(DBuf<T> &b, const std::vector<T> &h, cudaStream_t s) {
@@ -169,7 +227,7 @@ int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *ne
   st->nblocks = nblocks;
   st->eol = eol ? 1 : 0;
   st->nw = nw;
-  std::vector<DBuf<double>> devec(nblocks), dwt(nblocks);
+  std::vector<DBuf<double>> devec(nblocks), dwt(nblocks), ddiag(nblocks);
   std::vector<DiagBlock> hb(nblocks);
   for (int b = 0; b < nblocks; ++b) {
     gg_hmat *m = h[b];
@@ -181,8 +239,14 @@ int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *ne
     if (eol && (ne < 1 || !evec[b] || !wt[b])) return fail(GG_ERR_ARG, "gg_setcof_prepare: missing levels");
     if (!eol && !wt[b]) return fail(GG_ERR_ARG, "gg_setcof_prepare: missing CSF weights");
     if (eol) {
+      DBuf<double> tmp;
+      GG_TRY(tmp.alloc((size_t)ncf * ne));
       GG_TRY(devec[b].alloc((size_t)ncf * ne));
-      GG_CUDA(cudaMemcpyAsync(devec[b].p, evec[b], (size_t)ncf * ne * sizeof(double), cudaMemcpyHostToDevice, s));
+      GG_CUDA(cudaMemcpyAsync(tmp.p, evec[b], (size_t)ncf * ne * sizeof(double), cudaMemcpyHostToDevice, s));
+      k_by_csf<<<std::max(1, std::min(4 * ctx->sms, (int)(((int64_t)ncf * ne + 255) / 256))), 256, 0, s>>>(
+          tmp.p, ncf, ne, devec[b].p);
+      ::gg::note_launch();
+      GG_CUDA(cudaStreamSynchronize(s));  // tmp is freed here
       GG_TRY(dwt[b].alloc(ne));
       GG_CUDA(cudaMemcpyAsync(dwt[b].p, wt[b], ne * sizeof(double), cudaMemcpyHostToDevice, s));
     } else {
@@ -197,9 +261,10 @@ int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *ne
     ::gg::note_launch();
     GG_TRY(dsum.alloc(std::max<int64_t>(1, L.nlab)));
     if (L.nlab > 0) {
-      k_label_sums<<<(unsigned)((L.nlab + 127) / 128), 128, 0, s>>>(L.nlab, L.dStart.p, L.dLoc.p, L.dCoeff.p,
-                                                                   m->dIrow.p, owner.p, st->eol, ncf, ne,
-                                                                   devec[b].p, dwt[b].p, dsum.p);
+      k_label_sums<<<(unsigned)((L.nlab + LS_WARPS - 1) / LS_WARPS), LS_WARPS * 32, 0, s>>>(
+          L.nlab, L.dStart.p, L.dLoc.p, L.dCoeff.p,
+                                                                   m->dIrow.p, owner.p, st->eol, ne, devec[b].p,
+                                                                   dwt[b].p, dsum.p);
       ::gg::note_launch();
     }
     GG_CUDA(cudaGetLastError());
@@ -213,7 +278,10 @@ int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *ne
     st->lab0.push_back(L.list_lab0);
     st->bkmaxf.push_back(L.kmaxf);
     st->kmaxf = std::max(st->kmaxf, L.kmaxf);
-    hb[b] = DiagBlock{ncf, ne, eol ? devec[b].p : nullptr, dwt[b].p, L.dIq.p, L.dConf.p};
+    GG_TRY(ddiag[b].alloc(ncf));
+    k_dsubrs_diag<<<(ncf + 255) / 256, 256, 0, s>>>(st->eol, ncf, ne, devec[b].p, dwt[b].p, ddiag[b].p);
+    ::gg::note_launch();
+    hb[b] = DiagBlock{ncf, ddiag[b].p, L.dIq.p, L.dConf.p};
   }
   // the diagonal sums of every (J, IB, K) SETCOF asks for
   int jmax = 0;
@@ -243,8 +311,8 @@ int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *ne
   GG_TRY(upv(dblocks, hb, s));
   GG_TRY(dout.alloc(std::max<size_t>(1, items.size())));
   if (!items.empty()) {
-    k_diag_sums<<<(unsigned)((items.size() + 63) / 64), 64, 0, s>>>(ditems.p, (int)items.size(), dblocks.p, nblocks,
-                                                                   nw, st->eol, dout.p);
+    k_diag_sums<<<(unsigned)((items.size() + LS_WARPS - 1) / LS_WARPS), LS_WARPS * 32, 0, s>>>(
+        ditems.p, (int)items.size(), dblocks.p, nblocks, nw, dout.p);
     ::gg::note_launch();
   }
   GG_CUDA(cudaGetLastError());
@@ -254,6 +322,33 @@ int gg_setcof_prepare(gg_ctx *ctx, int nblocks, gg_hmat *const *h, const int *ne
   st->fco.assign((size_t)nw * nw * st->kdim, 0.0);
   st->gco.assign((size_t)nw * nw * st->kdim, 0.0);
   for (size_t t = 0; t < items.size(); ++t) (where[t] % 2 ? st->gco : st->fco)[where[t] / 2] = hv[t];
+  // the labels of each orbital, in visiting order
+  st->tref.assign(nw + 1, {});
+  st->vref.assign(nw + 1, {});
+  for (int b = 0; b < nblocks; ++b)
+    for (int64_t l = st->lab0[b][0]; l < st->lab0[b][1]; ++l) {
+      const int32_t lab = st->labs[b][l];
+      const int ia = lab % KEYORB, ib = lab / KEYORB;
+      if (ia >= 1 && ia <= nw) st->tref[ia].push_back({b, l});
+      if (ib != ia && ib >= 1 && ib <= nw) st->tref[ib].push_back({b, l});
+    }
+  for (int k = 0; k <= st->kmaxf; ++k)
+    for (int b = 0; b < nblocks; ++b) {
+      if (k > st->bkmaxf[b]) continue;
+      for (int64_t l = st->lab0[b][k + 1]; l < st->lab0[b][k + 2]; ++l) {
+        int32_t lab = st->labs[b][l];
+        int ix[4];
+        for (int t = 0; t < 4; ++t) {
+          ix[t] = lab % KEYORB;
+          lab /= KEYORB;
+        }
+        for (int t = 0; t < 4; ++t) {
+          bool seen = false;
+          for (int u = 0; u < t; ++u) seen = seen || ix[u] == ix[t];
+          if (!seen && ix[t] >= 1 && ix[t] <= nw) st->vref[ix[t]].push_back(std::make_tuple(k, b, l));
+        }
+      }
+    }
   ctx->setcof = st;
   return GG_OK;
 }
@@ -300,23 +395,20 @@ int gg_setcof(gg_ctx *ctx, int j, double ucfj, int cap, int *ny, int32_t *nya, d
     }
   }
   // DA from the T lists, block by block (:188-285)
-  for (int b = 0; b < st->nblocks; ++b) {
-    const int64_t l0 = st->lab0[b][0], l1 = st->lab0[b][1];
-    for (int64_t l = l0; l < l1; ++l) {
-      const int32_t lab = st->labs[b][l];
-      const int ia = lab % KEY, ibb = lab / KEY;
-      if (ia != j && ibb != j) continue;
-      const double sum = 0.5 * st->sums[b][l] / ucfj;
-      put(ld, vd, ia == j ? ibb : ia, sum, b > 0);
-    }
+  for (const auto &r : st->tref[j]) {
+    const int b = r.first;
+    const int64_t l = r.second;
+    const int32_t lab = st->labs[b][l];
+    const int ia = lab % KEY, ibb = lab / KEY;
+    const double sum = 0.5 * st->sums[b][l] / ucfj;
+    put(ld, vd, ia == j ? ibb : ia, sum, b > 0);
   }
   // the V^k lists, k by k and block by block (:287-515)
-  for (int k = 0; k <= st->kmaxf; ++k)
-    for (int b = 0; b < st->nblocks; ++b) {
-      if (k > st->bkmaxf[b]) continue;
-      const int64_t l0 = st->lab0[b][k + 1], l1 = st->lab0[b][k + 2];
+  for (const auto &r : st->vref[j]) {
+      const int k = std::get<0>(r), b = std::get<1>(r);
       const bool merge = b > 0;
-      for (int64_t l = l0; l < l1; ++l) {
+      {
+        const int64_t l = std::get<2>(r);
         int32_t lab = st->labs[b][l];
         int ix[4];
         ix[3] = lab % KEY;
