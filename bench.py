@@ -582,6 +582,43 @@ def breit_leg(local, w, steps, cpu=True):
     return out
 
 
+def setcof_leg(ctx, H, w, vec, cpu=True):
+    """rmcdhf's SETCOF (rmcdhf90/setcof.f90:3) for the Fe XV block's lists
+    and its 10 eigenvectors (EOL, equal level weights): the device pass over
+    all labels and diagonal sums, then every orbital's three lists; the
+    oracle's SETCOF for one orbital (it re-reads every list per orbital, as
+    the reference does) on one core."""
+    import numpy as np
+
+    b = w.block
+    nw = len(w.orb.nak)
+    wt = np.full(vec.shape[1], 1.0 / vec.shape[1])
+    ctx.setcof_prepare([H], [wt], [vec], eol=True)  # warm
+    prep, lists = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        ctx.setcof_prepare([H], [wt], [vec], eol=True)
+        t1 = time.perf_counter()
+        got = [ctx.setcof(j, 2.0) for j in range(1, nw + 1)]
+        t2 = time.perf_counter()
+        prep.append(t1 - t0)
+        lists.append(t2 - t1)
+    out = {"contributions": int(sum(int(np.asarray(x["start"])[-1]) for x in [b.tlist] + list(b.vlists))),
+           "orbitals": nw, "prepare_ms": statistics.median(prep) * 1e3,
+           "all_orbitals_lists_ms": statistics.median(lists) * 1e3}
+    if cpu:
+        import oracle
+        o = oracle.Oracle(n=w.n, rnt=w.rnt, h=w.h, c=w.c, zz=w.zz)
+        o.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+        blk = [dict(ncf=b.ncf, iendc=b.iendc, irow=b.irow, iq=b.iq, tlist=b.tlist, vlists=b.vlists, evec=vec, wt=wt)]
+        t0 = time.perf_counter()
+        ref = o.setcof(blk, True, 5, 2.0)
+        dt = time.perf_counter() - t0
+        same = all(np.array_equal(got[4][k], ref[k]) for k in ref)
+        out["cpu_oracle"] = {"one_orbital_s": dt, "all_orbitals_s_1core": dt * nw, "identical_lists": bool(same)}
+    return out
+
+
 def run_ours(a):
     ws, rank, local, pg = _dist()
     import numpy as np
@@ -689,6 +726,7 @@ def run_ours(a):
     t_e2e = _max_over_ranks(pg, statistics.median(e2e_times)) if e2e_times else None
     host_res = host_resident_leg(ctx, H, w, ev, vec, a.steps) if not a.no_extra else None
     breit = breit_leg(local, w, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
+    setcof = setcof_leg(ctx, H, w, vec, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
     batched = batched_leg(local, a.steps, cpu=(rank == 0 and not a.no_cpu_baseline)) if not a.no_extra else None
     rk = rk_leg(local) if not a.no_extra else None
     large = large_leg(local, cpu=(rank == 0 and not a.no_cpu_baseline)) if not (a.no_extra or a.no_large) else None
@@ -738,6 +776,7 @@ def run_ours(a):
         "cpu_baseline": cpu,
         "host_resident_block": host_res,
         "breit_tables_fe15_orbitals": breit,
+        "setcof_fe15": setcof,
         "batched_310_blocks": batched,
         "rk_table_40_orbitals": rk,
         "large_300k_csf": large,
