@@ -11,6 +11,8 @@ kernel family it is named for, a few times:
   python -m inputs.profile_targets rk_split # the same on the tensor cores (fp16 Ozaki digits, tcgen05)
   python -m inputs.profile_targets batch    # two batched solves of the 310-block workload (split)
   python -m inputs.profile_targets batch8   # the same for 8 ions (80 blocks), for detailed captures
+  python -m inputs.profile_targets breit    # the type-1 Breit table of the Ne VII orbital set (16 subshells)
+  python -m inputs.profile_targets setcof   # SETCOF's device pass over the Fe XV block's lists
 """
 from __future__ import annotations
 
@@ -94,6 +96,34 @@ def batch(zs=None):
     print("blocks", len(hs), "iterations", ctx.stage_stat(21), "ms", ctx.stage_stat(3))
 
 
+def breit():
+    """The type-1 Breit table of the Ne VII orbital set (n <= 4, l <= 3:
+    16 subshells), WFACT 1 with the orbitals' Dirac energies, twice."""
+    from grasp_gb300 import Context
+    from . import workloads
+    w = workloads.ne7()
+    ctx = Context(0)
+    ctx.set_grid(w.n, w.rnt, w.h, w.c, w.zz)
+    ctx.set_orbitals(w.orb.nak, w.orb.mf, w.orb.pf, w.orb.qf)
+    for _ in range(2):
+        ind, val, kst, j2 = ctx.genintbreit(1, 1.0, w.orb.e)
+    print("integrals", ind.size, "ms", ctx.stage_stat(31), "kernels ms", ctx.stage_stat(33))
+
+
+def setcof():
+    """SETCOF's device pass over the Fe XV block's lists with its 10
+    eigenvectors (EOL, equal weights), twice."""
+    import numpy as np
+
+    from grasp_gb300 import SPLIT
+    w, ctx, H = _fe15_context()
+    ev, vec, info = H.maneig(w.nroots, flavour=0, precision=SPLIT, mblock=w.nroots)
+    wt = np.full(w.nroots, 1.0 / w.nroots)
+    for _ in range(2):
+        ctx.setcof_prepare([H], [wt], [vec], eol=True)
+    print("lists of orbital 5:", {k: len(v) for k, v in ctx.setcof(5, 2.0).items()})
+
+
 if __name__ == "__main__":
     {"spmv": spmv, "spmm": spmm, "solve": solve, "solve2": solve2, "rk": rk, "rk_split": rk_split, "batch": batch,
-     "batch8": lambda: batch(zs=tuple(range(10, 18)))}[sys.argv[1]]()
+     "batch8": lambda: batch(zs=tuple(range(10, 18))), "breit": breit, "setcof": setcof}[sys.argv[1]]()
