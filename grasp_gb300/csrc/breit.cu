@@ -520,21 +520,6 @@ struct Planner {
   }
 };
 
-// TRIANGBREIT1 (rci90/triangbreit1.f90:27-46), TRIANGBREIT2 (triangbreit2.f90:27-42)
-bool triangbreit(const Orbitals &o, int type, int a, int b, int c, int d, int K) {
-  const int la = o.nkl[a], lb = o.nkl[b], lc = o.nkl[c], ld = o.nkl[d];
-  const int ja = o.nkj[a], jb = o.nkj[b], jc = o.nkj[c], jd = o.nkj[d];
-  if (type == 1) {
-    for (int L = K - 1; L <= K + 1; ++L)
-      if ((K + la + lb) % 2 == 1 && std::abs(ja - jb) <= 2 * L && std::abs(ja + jb) >= 2 * L &&
-          (K + lc + ld) % 2 == 1 && std::abs(jc - jd) <= 2 * L && std::abs(jc + jd) >= 2 * L)
-        return true;
-    return false;
-  }
-  return (K + la + lb) % 2 == 0 && std::abs(ja - jb) <= 2 * K && std::abs(ja + jb) >= 2 * K &&
-         (K + lc + ld) % 2 == 0 && std::abs(jc - jd) <= 2 * K && std::abs(jc + jd) >= 2 * K;
-}
-
 template <class T> int upload_vec(DBuf<T> &b, const std::vector<T> &h, cudaStream_t s) {
   GG_TRY(b.alloc(std::max<size_t>(1, h.size())));
   if (!h.empty()) GG_CUDA(cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s));
@@ -633,15 +618,37 @@ int gg_genintbreit(gg_ctx *ctx, int type, double wfact, const double *e, double 
   T.j2max = j2max;
   T.kstart.assign(j2max + 2, 1);
   T.hInd.clear();
+  // TRIANGBREIT1 (rci90/triangbreit1.f90:27-46) and TRIANGBREIT2
+  // (triangbreit2.f90:27-42) factor into one condition per pair: type 1 admits
+  // (a, b, c, d) when some L in K-1..K+1 admits both pairs, type 2 when both
+  // pairs are admitted at L = K. mask[pair] holds those bits (per L).
+  std::vector<unsigned char> mask((size_t)(nw + 1) * (nw + 1));
   for (int K = 0; K <= j2max; ++K) {
     for (int a = 1; a <= nw; ++a)
-      for (int b = 1; b <= nw; ++b)
+      for (int b = 1; b <= nw; ++b) {
+        unsigned char m = 0;
+        const int la = o.nkl[a], lb = o.nkl[b], ja = o.nkj[a], jb = o.nkj[b];
+        if (type == 1) {
+          for (int t = 0; t < 3; ++t) {
+            const int L = K - 1 + t;
+            if ((K + la + lb) % 2 == 1 && std::abs(ja - jb) <= 2 * L && std::abs(ja + jb) >= 2 * L) m |= 1 << t;
+          }
+        } else if ((K + la + lb) % 2 == 0 && std::abs(ja - jb) <= 2 * K && std::abs(ja + jb) >= 2 * K) {
+          m = 1;
+        }
+        mask[(size_t)a * (nw + 1) + b] = m;
+      }
+    for (int a = 1; a <= nw; ++a)
+      for (int b = 1; b <= nw; ++b) {
+        const unsigned char mab = mask[(size_t)a * (nw + 1) + b];
+        if (!mab) continue;
         for (int c = 1; c <= nw; ++c)
           for (int d = 1; d <= nw; ++d)
-            if (triangbreit(o, type, a, b, c, d, K)) {
+            if (mab & mask[(size_t)c * (nw + 1) + d]) {
               T.hInd.push_back(((a * KEY + b) * KEY + c) * KEY + d);
               P.add(type, a, b, c, d, K);
             }
+      }
     T.kstart[K + 1] = (int32_t)(T.hInd.size() + 1);
     GG_TRY(P.err);
   }
