@@ -606,6 +606,25 @@ def setcof_leg(ctx, H, w, vec, cpu=True):
     out = {"contributions": int(sum(int(np.asarray(x["start"])[-1]) for x in [b.tlist] + list(b.vlists))),
            "orbitals": nw, "prepare_ms": statistics.median(prep) * 1e3,
            "all_orbitals_lists_ms": statistics.median(lists) * 1e3}
+    # the rest of rmcdhf's potential chain from those lists: COFPOT (YPOT,
+    # XPOT, DACON) for every orbital, SETLAG over the same-kappa pairs
+    nak = np.asarray(w.orb.nak)
+    ucf = 1.0 + 0.05 * np.arange(nw)
+    lfix = np.zeros(nw, np.int32)
+    pairs = np.array([i + 215 * j for j in range(2, nw + 1) for i in range(1, j) if nak[i - 1] == nak[j - 1]],
+                     np.int32)
+    cof_ms, lag_ms = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        for j in range(1, nw + 1):
+            ctx.cofpot(j, ucf[j - 1], got[j - 1])
+        t1 = time.perf_counter()
+        ecv = ctx.setlag(pairs, ucf, lfix, got)
+        t2 = time.perf_counter()
+        cof_ms.append((t1 - t0) * 1e3)
+        lag_ms.append((t2 - t1) * 1e3)
+    out["cofpot_all_orbitals_ms"] = statistics.median(cof_ms)
+    out["setlag"] = {"pairs": int(pairs.size), "ms": statistics.median(lag_ms)}
     if cpu:
         import oracle
         o = oracle.Oracle(n=w.n, rnt=w.rnt, h=w.h, c=w.c, zz=w.zz)
@@ -616,6 +635,17 @@ def setcof_leg(ctx, H, w, vec, cpu=True):
         dt = time.perf_counter() - t0
         same = all(np.array_equal(got[4][k], ref[k]) for k in ref)
         out["cpu_oracle"] = {"one_orbital_s": dt, "all_orbitals_s_1core": dt * nw, "identical_lists": bool(same)}
+        t0 = time.perf_counter()
+        yp0, xp0, xq0 = o.cofpot(5, ucf[4], got[4])
+        out["cpu_oracle"]["cofpot_one_orbital_s"] = time.perf_counter() - t0
+        yp, xp, xq = ctx.cofpot(5, ucf[4], got[4])
+        out["cpu_oracle"]["cofpot_max_rel_diff"] = float(max(np.abs(yp - yp0).max() / np.abs(yp0).max(),
+                                                             np.abs(xp - xp0).max() / np.abs(xp0).max()))
+        if pairs.size:
+            t0 = time.perf_counter()
+            ecv0 = o.setlag(pairs[:4], ucf, lfix, got)
+            out["cpu_oracle"]["setlag_s_per_pair"] = (time.perf_counter() - t0) / min(4, pairs.size)
+            out["cpu_oracle"]["setlag_max_abs_diff"] = float(np.abs(ecv[:4] - ecv0).max())
     return out
 
 
