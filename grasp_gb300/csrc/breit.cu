@@ -9,6 +9,10 @@
 // stride-4 Newton-Cotes chain), the frequency-dependent terms weighted by
 // spherical Bessel factors (bessel.f90). On the device:
 //
+//  0. k_plan_table / k_plan_items: the integrals and their terms. A table
+//     row (k, a, b) holds the (c, d) whose TRIANGBREIT pair masks share a
+//     bit, in the reference's order; one pass counts each row's integrals
+//     and terms, the host scans the counts, a second pass writes them.
 //  1. k_bessel: every Bessel function the integrals need, (pair, order) with
 //     W = WFACT |E(a) - E(b)| / C, one block each: the series where it
 //     converges in four terms, the asymptotic form from the first point where
@@ -384,141 +388,183 @@ __global__ void k_breit_combine(const BrInt *__restrict__ ints, int64_t n, const
 }
 
 // ---------------------------------------------------------------------------
-// host: the terms of each integral (brintf.f90:34-69, brra.f90:36-118)
+// the terms of each integral (brintf.f90:34-69, brra.f90:36-118), planned on
+// the device: one thread per integral (or per (k, a, b) row of a table)
+// counts its terms, the counts are scanned, the same thread writes them.
 // ---------------------------------------------------------------------------
-struct Planner {
-  const gg_ctx *ctx;
-  double wfact, epsi;
-  std::vector<double> e;
-  int nw = 0;
-  std::vector<int> bidx;  // [pair (x <= y)][order + 1]: function index, -2 not yet seen
-  std::vector<BessDesc> bess;
-  std::vector<BrJob> jobs;
-  std::vector<BrInt> ints;
-  int err = GG_OK;
-
-  double w(int x, int y) const { return wfact * std::fabs(e[x - 1] - e[y - 1]) / ctx->grid.c; }
-  // the Bessel function of pair (x, y), order nn; -1 when it is zero
-  int bessel(int x, int y, int nn) {
-    int &slot = bidx[((size_t)(std::min(x, y) - 1) * nw + (std::max(x, y) - 1)) * (KLIM + 3) + (nn + 1)];
-    if (slot != -2) return slot;
-    const double W = w(x, y);
-    if (W < epsi * epsi) {
-      slot = -1;
-    } else {
-      slot = (int)bess.size();
-      bess.push_back(BessDesc{W, nn});
-    }
-    return slot;
-  }
-  void job(int form, int k, int sx, int sy, bool saug, int px, int py, bool paug, int bj, int bn) {
-    BrJob j;
-    j.form = (unsigned char)form;
-    j.sx = (unsigned char)sx;
-    j.sy = (unsigned char)sy;
-    j.px = (unsigned char)px;
-    j.py = (unsigned char)py;
-    j.flags = (unsigned char)((saug ? 1 : 0) | (paug ? 2 : 0));
-    j.k = (signed char)k;
-    j.pad = 0;
-    j.bj = bj;
-    j.bn = bn;
-    jobs.push_back(j);
-  }
-  // BRINTF(type, a, b, c, d, k): RAC = P_a Q_b, RBD = P_c Q_d; Bessel slot 1
-  // pair (a, b), slot 2 pair (c, d)
-  void add(int type, int a, int b, int c, int d, int K) {
-    if (K + 1 > KLIM || K < 0) {
-      err = fail(GG_ERR_ARG, "Breit integrals: k outside 0..19");
-      return;
-    }
-    BrInt bi;
-    bi.q0 = (int)jobs.size();
-    bi.k = (short)K;
-    bi.w1 = w(a, b);
-    bi.w2 = w(c, d);
-    auto R = [&](bool rac, int iw, bool augac, bool augbd) {
-      const int f = iw == 0 ? -1 : (iw == 1 ? bessel(a, b, K) : bessel(c, d, K));
-      if (rac)
-        job(0, K, a, b, augac, c, d, augbd, f, f);
-      else
-        job(0, K, c, d, augbd, a, b, augac, f, f);
-    };
-    auto S = [&](int iw) {
-      const int x = iw == 1 ? a : c, y = iw == 1 ? b : d;
-      const double W = w(x, y);
-      if (std::fabs(W) < 1.0e-10) {
-        job(1, K, a, b, false, c, d, false, -1, -1);
-      } else {
-        const int f1 = bessel(x, y, K - 1), f2 = bessel(x, y, K + 1);
-        job(2, K, a, b, false, c, d, false, f1, f2);
-        job(3, K, c, d, false, a, b, false, f2, f1);
-      }
-    };
-    switch (type) {
-      case 1:
-        if (a == c && b == d) {
-          bi.code = 0;
-          R(true, 1, false, false);
-        } else if (a == d && b == c) {
-          bi.code = 1;
-          R(true, 1, false, false);
-          R(false, 1, false, false);
-        } else {
-          bi.code = 2;
-          R(true, 1, false, false);
-          R(true, 2, false, false);
-          R(false, 1, false, false);
-          R(false, 2, false, false);
-        }
-        break;
-      case 2:
-        if ((a == c && b == d) || (a == d && b == c)) {
-          bi.code = 3;
-          S(1);
-        } else {
-          bi.code = 4;
-          S(1);
-          S(2);
-        }
-        break;
-      case 3:
-        bi.code = 2;
-        if (a == b) {
-          R(true, 0, false, true);
-          R(false, 0, false, true);
-          R(true, 2, false, true);
-          R(false, 2, false, true);
-        } else {
-          R(true, 1, true, false);
-          R(false, 1, true, false);
-          R(true, 0, true, false);
-          R(false, 0, true, false);
-        }
-        break;
-      case 4:
-        bi.code = 1;
-        R(true, 0, false, false);
-        R(false, 0, false, false);
-        break;
-      case 5:
-        if (a == d && b == c) {
-          bi.code = 1;
-          R(true, 1, false, false);
-          R(false, 1, false, false);
-        } else {
-          bi.code = 0;
-          R(true, 1, false, false);
-        }
-        break;
-      default:
-        bi.code = 3;
-        S(1);
-        break;
-    }
-    ints.push_back(bi);
-  }
+struct PlanTabs {
+  const double *W;   // [a][b]: W = WFACT |E(a) - E(b)| / C
+  const int *bid;    // [order + 1][min(a,b)][max(a,b)]: Bessel function, -1 zero
+  int nw;
 };
+
+__device__ __forceinline__ int bes_id(const PlanTabs &T, int x, int y, int nn) {
+  const int lo = min(x, y), hi = max(x, y);
+  return T.bid[((size_t)(nn + 1) * T.nw + (lo - 1)) * T.nw + (hi - 1)];
+}
+
+// BRINTF(type, a, b, c, d, k): RAC = P_a Q_b, RBD = P_c Q_d; Bessel slot 1
+// pair (a, b), slot 2 pair (c, d). Returns the number of terms; with bi and
+// jb set, writes the integral's record (first term q0) and its terms.
+__device__ int plan_one(int type, int a, int b, int c, int d, int K, const PlanTabs &T, int q0, BrInt *bi,
+                        BrJob *jb) {
+  auto w = [&](int x, int y) { return T.W[(size_t)(x - 1) * T.nw + (y - 1)]; };
+  int n = 0;
+  auto job = [&](int form, int sx, int sy, bool saug, int px, int py, bool paug, int bj, int bn) {
+    if (jb) {
+      BrJob j;
+      j.form = (unsigned char)form;
+      j.sx = (unsigned char)sx;
+      j.sy = (unsigned char)sy;
+      j.px = (unsigned char)px;
+      j.py = (unsigned char)py;
+      j.flags = (unsigned char)((saug ? 1 : 0) | (paug ? 2 : 0));
+      j.k = (signed char)K;
+      j.pad = 0;
+      j.bj = bj;
+      j.bn = bn;
+      jb[n] = j;
+    }
+    ++n;
+  };
+  auto R = [&](bool rac, int iw, bool augac, bool augbd) {
+    const int f = iw == 0 ? -1 : (iw == 1 ? bes_id(T, a, b, K) : bes_id(T, c, d, K));
+    if (rac)
+      job(0, a, b, augac, c, d, augbd, f, f);
+    else
+      job(0, c, d, augbd, a, b, augac, f, f);
+  };
+  auto S = [&](int iw) {
+    const int x = iw == 1 ? a : c, y = iw == 1 ? b : d;
+    if (fabs(w(x, y)) < 1.0e-10) {
+      job(1, a, b, false, c, d, false, -1, -1);
+    } else {
+      const int f1 = bes_id(T, x, y, K - 1), f2 = bes_id(T, x, y, K + 1);
+      job(2, a, b, false, c, d, false, f1, f2);
+      job(3, c, d, false, a, b, false, f2, f1);
+    }
+  };
+  int code;
+  switch (type) {
+    case 1:
+      if (a == c && b == d) {
+        code = 0;
+        R(true, 1, false, false);
+      } else if (a == d && b == c) {
+        code = 1;
+        R(true, 1, false, false);
+        R(false, 1, false, false);
+      } else {
+        code = 2;
+        R(true, 1, false, false);
+        R(true, 2, false, false);
+        R(false, 1, false, false);
+        R(false, 2, false, false);
+      }
+      break;
+    case 2:
+      if ((a == c && b == d) || (a == d && b == c)) {
+        code = 3;
+        S(1);
+      } else {
+        code = 4;
+        S(1);
+        S(2);
+      }
+      break;
+    case 3:
+      code = 2;
+      if (a == b) {
+        R(true, 0, false, true);
+        R(false, 0, false, true);
+        R(true, 2, false, true);
+        R(false, 2, false, true);
+      } else {
+        R(true, 1, true, false);
+        R(false, 1, true, false);
+        R(true, 0, true, false);
+        R(false, 0, true, false);
+      }
+      break;
+    case 4:
+      code = 1;
+      R(true, 0, false, false);
+      R(false, 0, false, false);
+      break;
+    case 5:
+      if (a == d && b == c) {
+        code = 1;
+        R(true, 1, false, false);
+        R(false, 1, false, false);
+      } else {
+        code = 0;
+        R(true, 1, false, false);
+      }
+      break;
+    default:
+      code = 3;
+      S(1);
+      break;
+  }
+  if (bi) {
+    BrInt r;
+    r.q0 = q0;
+    r.code = (short)code;
+    r.k = (short)K;
+    r.w1 = w(a, b);
+    r.w2 = w(c, d);
+    *bi = r;
+  }
+  return n;
+}
+
+// a table row: the (c, d) that TRIANGBREIT admits with (k, a, b) (pair
+// masks share a bit), in the reference's order; pass 0 counts integrals and
+// terms, pass 1 writes them from the scanned offsets
+__global__ void k_plan_table(int type, int nw, int kmax, const unsigned char *__restrict__ mask, PlanTabs T,
+                             int pass, int *__restrict__ cnt_i, int *__restrict__ cnt_j,
+                             const int64_t *__restrict__ off_i, const int64_t *__restrict__ off_j,
+                             int32_t *__restrict__ ind, BrInt *__restrict__ ints, BrJob *__restrict__ jobs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (kmax + 1) * nw * nw) return;
+  const int K = t / (nw * nw), a = (t / nw) % nw + 1, b = t % nw + 1;
+  const int KEY = nw + 1;
+  const unsigned char *mk = mask + (size_t)K * (nw + 1) * (nw + 1);
+  const unsigned char mab = mk[a * (nw + 1) + b];
+  int ni = 0, nj = 0;
+  if (mab) {
+    int64_t pi = pass ? off_i[t] : 0, pj = pass ? off_j[t] : 0;
+    for (int c = 1; c <= nw; ++c)
+      for (int d = 1; d <= nw; ++d)
+        if (mab & mk[c * (nw + 1) + d]) {
+          if (pass) {
+            ind[pi] = ((a * KEY + b) * KEY + c) * KEY + d;
+            const int q = plan_one(type, a, b, c, d, K, T, (int)pj, ints + pi, jobs + pj);
+            ++pi;
+            pj += q;
+          } else {
+            ++ni;
+            nj += plan_one(type, a, b, c, d, K, T, 0, nullptr, nullptr);
+          }
+        }
+  }
+  if (!pass) {
+    cnt_i[t] = ni;
+    cnt_j[t] = nj;
+  }
+}
+
+// a list of integrals (items[6 t ..] = type, a, b, c, d, k)
+__global__ void k_plan_items(const int32_t *__restrict__ items, int n, PlanTabs T, int pass, int *__restrict__ cnt_j,
+                             const int64_t *__restrict__ off_j, BrInt *__restrict__ ints, BrJob *__restrict__ jobs) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int32_t *it = items + 6 * (size_t)t;
+  if (pass)
+    plan_one(it[0], it[1], it[2], it[3], it[4], it[5], T, (int)off_j[t], ints + t, jobs + off_j[t]);
+  else
+    cnt_j[t] = plan_one(it[0], it[1], it[2], it[3], it[4], it[5], T, 0, nullptr, nullptr);
+}
 
 template <class T> int upload_vec(DBuf<T> &b, const std::vector<T> &h, cudaStream_t s) {
   GG_TRY(b.alloc(std::max<size_t>(1, h.size())));
@@ -526,28 +572,74 @@ template <class T> int upload_vec(DBuf<T> &b, const std::vector<T> &h, cudaStrea
   return GG_OK;
 }
 
-// the planned integrals on the device, values into out (host, ints order);
-// *kernel_ms: device time of the kernels
-int run_plan(gg_ctx *ctx, Planner &P, double *out, double *kernel_ms = nullptr) {
-  GG_TRY(P.err);
+// the host side of a plan: the frequencies, the Bessel functions the
+// integrals read (pair, order) with their ids, on the device
+struct Plan {
+  gg_ctx *ctx = nullptr;
+  int nw = 0;
+  double wfact = 0, epsi = 0;
+  std::vector<double> e, W;
+  std::vector<int> bid;  // [order + 1][lo][hi]
+  std::vector<BessDesc> bess;
+  DBuf<double> dW;
+  DBuf<int> dbid;
+  int norders() const { return KLIM + 3; }
+  int &slot(int x, int y, int nn) {
+    const int lo = std::min(x, y), hi = std::max(x, y);
+    return bid[((size_t)(nn + 1) * nw + (lo - 1)) * nw + (hi - 1)];
+  }
+  void need(int x, int y, int nn) {
+    int &s = slot(x, y, nn);
+    if (s != -2) return;
+    const double w = W[(size_t)(x - 1) * nw + (y - 1)];
+    if (w < epsi * epsi) {
+      s = -1;
+    } else {
+      s = (int)bess.size();
+      bess.push_back(BessDesc{w, nn});
+    }
+  }
+  int upload(cudaStream_t s) {
+    for (int &v : bid)
+      if (v == -2) v = -1;
+    GG_TRY(upload_vec(dW, W, s));
+    GG_TRY(upload_vec(dbid, bid, s));
+    return GG_OK;
+  }
+  PlanTabs tabs() const { return PlanTabs{dW.p, dbid.p, nw}; }
+};
+
+int make_plan(gg_ctx *ctx, double wfact, const double *e, double accy, Plan &P) {
+  GG_TRY(ensure_orbitals(ctx));
+  const Orbitals &o = ctx->orb;
+  if (!e) return fail(GG_ERR_ARG, "Breit integrals: orbital energies required");
+  if (o.nw > 214) return fail(GG_ERR_ARG, "Breit integrals: more than 214 orbitals");
+  P.ctx = ctx;
+  P.nw = o.nw;
+  P.wfact = wfact;
+  P.epsi = std::sqrt(0.1 * (accy > 0 ? accy : std::pow(ctx->grid.h, 6)));
+  P.e.assign(e, e + o.nw);
+  P.W.assign((size_t)o.nw * o.nw, 0.0);
+  for (int x = 1; x <= o.nw; ++x)
+    for (int y = 1; y <= o.nw; ++y)
+      P.W[(size_t)(x - 1) * o.nw + (y - 1)] = wfact * std::fabs(e[x - 1] - e[y - 1]) / ctx->grid.c;
+  P.bid.assign((size_t)P.norders() * o.nw * o.nw, -2);
+  return GG_OK;
+}
+
+// the Bessel functions, the terms and the combinations; values into out
+// (host, ni integrals); *kernel_ms: device time of these kernels
+int run_terms(gg_ctx *ctx, const Plan &P, const BrJob *djobs, int64_t nj, const BrInt *dints, int64_t ni,
+              double *out, double *kernel_ms = nullptr) {
   const Grid &g = ctx->grid;
   const Orbitals &o = ctx->orb;
   cudaStream_t s = ctx->stream;
   const int nb = (int)P.bess.size();
   DBuf<BessDesc> dbd;
   DBuf<double> dBJ, dBN, dv, dout;
-  DBuf<BrJob> djobs;
-  DBuf<BrInt> dints;
   GG_TRY(upload_vec(dbd, P.bess, s));
   GG_TRY(dBJ.alloc((size_t)std::max(1, nb) * g.np));
   GG_TRY(dBN.alloc((size_t)std::max(1, nb) * g.np));
-  if (nb > 0) {
-    k_bessel<<<nb, 128, 0, s>>>(dbd.p, g.dR.p, g.n, g.np, P.epsi, dBJ.p, dBN.p);
-    ::gg::note_launch();
-  }
-  GG_TRY(upload_vec(djobs, P.jobs, s));
-  GG_TRY(upload_vec(dints, P.ints, s));
-  const int64_t nj = (int64_t)P.jobs.size(), ni = (int64_t)P.ints.size();
   GG_TRY(dv.alloc(std::max<int64_t>(1, nj)));
   GG_TRY(dout.alloc(std::max<int64_t>(1, ni)));
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -556,14 +648,18 @@ int run_plan(gg_ctx *ctx, Planner &P, double *out, double *kernel_ms = nullptr) 
     GG_CUDA(cudaEventCreate(&e1));
     GG_CUDA(cudaEventRecord(e0, s));
   }
+  if (nb > 0) {
+    k_bessel<<<nb, 128, 0, s>>>(dbd.p, g.dR.p, g.n, g.np, P.epsi, dBJ.p, dBN.p);
+    ::gg::note_launch();
+  }
   if (nj > 0) {
-    k_breit_jobs<<<(unsigned)((nj + 127) / 128), 128, 0, s>>>(djobs.p, nj, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p,
+    k_breit_jobs<<<(unsigned)((nj + 127) / 128), 128, 0, s>>>(djobs, nj, o.dPF.p, o.dQF.p, o.ld, o.dMF.p, g.dR.p,
                                                                g.dRP.p, g.dRPOR.p, g.dPow.p, g.np, g.q, dBJ.p,
                                                                dBN.p, dv.p);
     ::gg::note_launch();
   }
   if (ni > 0) {
-    k_breit_combine<<<(unsigned)((ni + 255) / 256), 256, 0, s>>>(dints.p, ni, dv.p, dout.p);
+    k_breit_combine<<<(unsigned)((ni + 255) / 256), 256, 0, s>>>(dints, ni, dv.p, dout.p);
     ::gg::note_launch();
   }
   GG_CUDA(cudaGetLastError());
@@ -580,18 +676,15 @@ int run_plan(gg_ctx *ctx, Planner &P, double *out, double *kernel_ms = nullptr) 
   return GG_OK;
 }
 
-int make_planner(gg_ctx *ctx, double wfact, const double *e, double accy, Planner &P) {
-  GG_TRY(ensure_orbitals(ctx));
-  const Orbitals &o = ctx->orb;
-  if (!e) return fail(GG_ERR_ARG, "Breit integrals: orbital energies required");
-  if (o.nw > 214) return fail(GG_ERR_ARG, "Breit integrals: more than 214 orbitals");
-  P.ctx = ctx;
-  P.wfact = wfact;
-  P.epsi = std::sqrt(0.1 * (accy > 0 ? accy : std::pow(ctx->grid.h, 6)));
-  P.e.assign(e, e + o.nw);
-  P.nw = o.nw;
-  P.bidx.assign((size_t)o.nw * o.nw * (KLIM + 3), -2);
-  return GG_OK;
+// exclusive scan of counts into int64 offsets; returns the total
+int64_t scan(const std::vector<int> &cnt, std::vector<int64_t> &off) {
+  off.resize(cnt.size());
+  int64_t t = 0;
+  for (size_t i = 0; i < cnt.size(); ++i) {
+    off[i] = t;
+    t += cnt[i];
+  }
+  return t;
 }
 
 }  // namespace
@@ -605,25 +698,28 @@ int gg_genintbreit(gg_ctx *ctx, int type, double wfact, const double *e, double 
                    int *j2max_out) {
   if (!ctx || (type != 1 && type != 2)) return fail(GG_ERR_ARG, "gg_genintbreit: type 1 or 2");
   GG_CUDA(cudaSetDevice(ctx->device));
-  Planner P;
-  GG_TRY(make_planner(ctx, wfact, e, accy, P));
+  Plan P;
+  GG_TRY(make_plan(ctx, wfact, e, accy, P));
   GG_TRY(timer_start(ctx));
+  const auto th0 = std::chrono::steady_clock::now();
   const Orbitals &o = ctx->orb;
-  const int nw = o.nw, KEY = nw + 1;
+  const int nw = o.nw;
   int j2max = o.nkj[1];
   for (int i = 2; i <= nw; ++i) j2max = std::max(j2max, o.nkj[i]);
-  const auto th0 = std::chrono::steady_clock::now();
+  if (j2max + 1 > KLIM) return fail(GG_ERR_ARG, "gg_genintbreit: 2j above 19");
   BreitTable &T = ctx->breit[type - 1];
   T.valid = false;
   T.j2max = j2max;
-  T.kstart.assign(j2max + 2, 1);
-  T.hInd.clear();
+  cudaStream_t s = ctx->stream;
   // TRIANGBREIT1 (rci90/triangbreit1.f90:27-46) and TRIANGBREIT2
-  // (triangbreit2.f90:27-42) factor into one condition per pair: type 1 admits
-  // (a, b, c, d) when some L in K-1..K+1 admits both pairs, type 2 when both
-  // pairs are admitted at L = K. mask[pair] holds those bits (per L).
-  std::vector<unsigned char> mask((size_t)(nw + 1) * (nw + 1));
-  for (int K = 0; K <= j2max; ++K) {
+  // (triangbreit2.f90:27-42) factor into one condition per pair: type 1
+  // admits (a, b, c, d) when some L in K-1..K+1 admits both pairs, type 2
+  // when both pairs are admitted at L = K. mask[k][pair] holds those bits
+  // (per L); the Bessel functions the admitted integrals read are those of
+  // the pairs with a mask bit, at order k (type 1) or k -+ 1 (type 2).
+  const size_t msz = (size_t)(nw + 1) * (nw + 1);
+  std::vector<unsigned char> mask((size_t)(j2max + 1) * msz, 0);
+  for (int K = 0; K <= j2max; ++K)
     for (int a = 1; a <= nw; ++a)
       for (int b = 1; b <= nw; ++b) {
         unsigned char m = 0;
@@ -633,30 +729,54 @@ int gg_genintbreit(gg_ctx *ctx, int type, double wfact, const double *e, double 
             const int L = K - 1 + t;
             if ((K + la + lb) % 2 == 1 && std::abs(ja - jb) <= 2 * L && std::abs(ja + jb) >= 2 * L) m |= 1 << t;
           }
+          if (m) P.need(a, b, K);
         } else if ((K + la + lb) % 2 == 0 && std::abs(ja - jb) <= 2 * K && std::abs(ja + jb) >= 2 * K) {
           m = 1;
+          P.need(a, b, K - 1);
+          P.need(a, b, K + 1);
         }
-        mask[(size_t)a * (nw + 1) + b] = m;
+        mask[(size_t)K * msz + (size_t)a * (nw + 1) + b] = m;
       }
-    for (int a = 1; a <= nw; ++a)
-      for (int b = 1; b <= nw; ++b) {
-        const unsigned char mab = mask[(size_t)a * (nw + 1) + b];
-        if (!mab) continue;
-        for (int c = 1; c <= nw; ++c)
-          for (int d = 1; d <= nw; ++d)
-            if (mab & mask[(size_t)c * (nw + 1) + d]) {
-              T.hInd.push_back(((a * KEY + b) * KEY + c) * KEY + d);
-              P.add(type, a, b, c, d, K);
-            }
-      }
-    T.kstart[K + 1] = (int32_t)(T.hInd.size() + 1);
-    GG_TRY(P.err);
-  }
-  T.n = (int64_t)T.hInd.size();
+  GG_TRY(P.upload(s));
+  DBuf<unsigned char> dmask;
+  GG_TRY(upload_vec(dmask, mask, s));
+  const int rows = (j2max + 1) * nw * nw;
+  DBuf<int> dci, dcj;
+  GG_TRY(dci.alloc(rows));
+  GG_TRY(dcj.alloc(rows));
+  k_plan_table<<<(rows + 127) / 128, 128, 0, s>>>(type, nw, j2max, dmask.p, P.tabs(), 0, dci.p, dcj.p, nullptr,
+                                                  nullptr, nullptr, nullptr, nullptr);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  std::vector<int> ci(rows), cj(rows);
+  GG_CUDA(cudaMemcpyAsync(ci.data(), dci.p, rows * sizeof(int), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaMemcpyAsync(cj.data(), dcj.p, rows * sizeof(int), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  std::vector<int64_t> oi, oj;
+  const int64_t ni = scan(ci, oi), nj = scan(cj, oj);
+  if (ni > INT32_MAX || nj > INT32_MAX) return fail(GG_ERR_RANGE, "gg_genintbreit: table too large");
+  T.kstart.assign(j2max + 2, 1);
+  for (int K = 0; K <= j2max; ++K) T.kstart[K + 1] = (int32_t)((K + 1 <= j2max ? oi[(size_t)(K + 1) * nw * nw] : ni) + 1);
+  DBuf<int64_t> doi, doj;
+  DBuf<int32_t> dind;
+  DBuf<BrInt> dints;
+  DBuf<BrJob> djobs;
+  GG_TRY(upload_vec(doi, oi, s));
+  GG_TRY(upload_vec(doj, oj, s));
+  GG_TRY(dind.alloc(std::max<int64_t>(1, ni)));
+  GG_TRY(dints.alloc(std::max<int64_t>(1, ni)));
+  GG_TRY(djobs.alloc(std::max<int64_t>(1, nj)));
+  k_plan_table<<<(rows + 127) / 128, 128, 0, s>>>(type, nw, j2max, dmask.p, P.tabs(), 1, nullptr, nullptr, doi.p,
+                                                  doj.p, dind.p, dints.p, djobs.p);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  T.n = ni;
+  T.hInd.resize(ni);
+  if (ni > 0) GG_CUDA(cudaMemcpyAsync(T.hInd.data(), dind.p, ni * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   ctx->stats[32] = 1e3 * std::chrono::duration<double>(std::chrono::steady_clock::now() - th0).count();
-  T.hVal.assign(std::max<int64_t>(1, T.n), 0.0);
-  GG_TRY(run_plan(ctx, P, T.hVal.data(), &ctx->stats[33]));
-  T.hVal.resize(T.n);
+  T.hVal.assign(std::max<int64_t>(1, ni), 0.0);
+  GG_TRY(run_terms(ctx, P, djobs.p, nj, dints.p, ni, T.hVal.data(), &ctx->stats[33]));
+  T.hVal.resize(ni);
   T.valid = true;
   double ms = 0;
   GG_TRY(timer_stop(ctx, &ms));
@@ -696,18 +816,50 @@ int gg_brintf(gg_ctx *ctx, int n, const int32_t *items, double wfact, const doub
   if (!ctx || n < 0 || (n > 0 && (!items || !out))) return fail(GG_ERR_ARG, "gg_brintf: bad arguments");
   if (n == 0) return GG_OK;
   GG_CUDA(cudaSetDevice(ctx->device));
-  Planner P;
-  GG_TRY(make_planner(ctx, wfact, e, accy, P));
+  Plan P;
+  GG_TRY(make_plan(ctx, wfact, e, accy, P));
   const int nw = ctx->orb.nw;
+  // the Bessel functions the integrals read (brintf.f90:34-69)
   for (int t = 0; t < n; ++t) {
     const int32_t *it = items + 6 * (size_t)t;
     if (it[0] < 1 || it[0] > 6) return fail(GG_ERR_ARG, "gg_brintf: type outside 1..6");
     for (int j = 1; j <= 4; ++j)
       if (it[j] < 1 || it[j] > nw) return fail(GG_ERR_ARG, "gg_brintf: orbital outside the orbital set");
-    P.add(it[0], it[1], it[2], it[3], it[4], it[5]);
-    GG_TRY(P.err);
+    const int K = it[5];
+    if (K < 0 || K + 1 > KLIM) return fail(GG_ERR_ARG, "gg_brintf: k outside 0..19");
+    switch (it[0]) {
+      case 1: case 3: P.need(it[1], it[2], K); P.need(it[3], it[4], K); break;
+      case 5: P.need(it[1], it[2], K); break;
+      case 2: P.need(it[3], it[4], K - 1); P.need(it[3], it[4], K + 1);  // fall through
+      case 6: P.need(it[1], it[2], K - 1); P.need(it[1], it[2], K + 1); break;
+      default: break;
+    }
   }
-  return run_plan(ctx, P, out);
+  cudaStream_t s = ctx->stream;
+  GG_TRY(P.upload(s));
+  DBuf<int32_t> ditems;
+  DBuf<int> dcj;
+  GG_TRY(ditems.alloc((size_t)6 * n));
+  GG_CUDA(cudaMemcpyAsync(ditems.p, items, (size_t)6 * n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  GG_TRY(dcj.alloc(n));
+  k_plan_items<<<(n + 127) / 128, 128, 0, s>>>(ditems.p, n, P.tabs(), 0, dcj.p, nullptr, nullptr, nullptr);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  std::vector<int> cj(n);
+  GG_CUDA(cudaMemcpyAsync(cj.data(), dcj.p, n * sizeof(int), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  std::vector<int64_t> oj;
+  const int64_t nj = scan(cj, oj);
+  DBuf<int64_t> doj;
+  DBuf<BrInt> dints;
+  DBuf<BrJob> djobs;
+  GG_TRY(upload_vec(doj, oj, s));
+  GG_TRY(dints.alloc(n));
+  GG_TRY(djobs.alloc(std::max<int64_t>(1, nj)));
+  k_plan_items<<<(n + 127) / 128, 128, 0, s>>>(ditems.p, n, P.tabs(), 1, nullptr, doj.p, dints.p, djobs.p);
+  ::gg::note_launch();
+  GG_CUDA(cudaGetLastError());
+  return run_terms(ctx, P, djobs.p, nj, dints.p, n, out);
 }
 
 }  // extern "C"
