@@ -904,6 +904,57 @@ __global__ void k_potential(int mode, int ncof, const int *__restrict__ fidx, co
   }
 }
 
+// XPOT in two passes for long lists: the products of terms t0 .. t0+nt at
+// every grid point (CTB = COEFF TB, CTB QF and CTB PF) by all SMs, then per
+// grid point the sums XP = XP + CTB QF, XQ = XQ - CTB PF in list order (the
+// same operations as k_potential; only the additions stay sequential)
+__global__ void k_xprod(int nt, const int *__restrict__ fidx, const double *__restrict__ coef,
+                        const int *__restrict__ iorb, const double *__restrict__ Y, int np,
+                        const double *__restrict__ PF, const double *__restrict__ QF, int ld, int n,
+                        double *__restrict__ P1, double *__restrict__ P2) {
+  const int tot = nt * n;  // the caller keeps nt * n below 2^22
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
+    const int t = e / n, i = e % n + 1;
+    const double ctb = coef[t] * Y[(size_t)fidx[t] * np + i];
+    P1[e] = ctb * pf(QF, ld, i, iorb[t]);
+    P2[e] = ctb * pf(PF, ld, i, iorb[t]);
+  }
+}
+// k_xsum: 32 grid points per block; blockIdx.y = 0 sums XP = XP + P1,
+// blockIdx.y = 1 sums XQ = XQ - P2. The loads run XSUM_AHEAD terms ahead of
+// the additions (register double buffer) so that the chain of dependent
+// FP64 additions, not the load latency, sets the time.
+constexpr int XSUM_AHEAD = 16;
+template <bool SUB>
+__device__ __forceinline__ double xsum_chain(double acc, const double *__restrict__ P, int nt, int n) {
+  double cur[XSUM_AHEAD], nxt[XSUM_AHEAD];
+  int t = 0;
+#pragma unroll
+  for (int u = 0; u < XSUM_AHEAD; ++u) cur[u] = (u < nt) ? P[(size_t)u * n] : 0.0;
+  for (; t + XSUM_AHEAD <= nt; t += XSUM_AHEAD) {
+    const int t1 = t + XSUM_AHEAD;
+#pragma unroll
+    for (int u = 0; u < XSUM_AHEAD; ++u) nxt[u] = (t1 + u < nt) ? P[(size_t)(t1 + u) * n] : 0.0;
+#pragma unroll
+    for (int u = 0; u < XSUM_AHEAD; ++u) acc = SUB ? acc - cur[u] : acc + cur[u];
+#pragma unroll
+    for (int u = 0; u < XSUM_AHEAD; ++u) cur[u] = nxt[u];
+  }
+#pragma unroll
+  for (int u = 0; u < XSUM_AHEAD; ++u)
+    if (t + u < nt) acc = SUB ? acc - cur[u] : acc + cur[u];
+  return acc;
+}
+__global__ void k_xsum(int nt, int n, const double *__restrict__ P1, const double *__restrict__ P2,
+                       double *__restrict__ xp, double *__restrict__ xq) {
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  if (i >= n) return;
+  if (blockIdx.y == 0)
+    xp[i] = xsum_chain<false>(xp[i], P1 + i, nt, n);
+  else
+    xq[i] = xsum_chain<true>(xq[i], P2 + i, nt, n);
+}
+
 // DPBDT (lib9290/dpbdt.f90:39-99): 13-point derivative of orbital J at grid
 // index i (1-based): the end rows from the 13 x 13 table, the interior by the
 // antisymmetric 12-neighbour formula.
@@ -1578,7 +1629,19 @@ struct PotTerms {
   std::vector<int> fidx, iorb;
   std::vector<double> coef;
 };
-using YKey = std::map<std::tuple<int, int, int>, int>;
+// the distinct (K, a, b) of one call's lists: a dense table over
+// K <= KLIMIT and the orbital pairs, holding function index + 1 (0: none)
+struct YKey {
+  std::vector<int> at;
+  int nw = 0;
+  int &slot(int k, int a, int b, int nw_) {
+    if (at.empty()) {
+      nw = nw_;
+      at.assign((size_t)(KLIMIT + 1) * nw * nw, 0);
+    }
+    return at[((size_t)k * nw + (a - 1)) * nw + (b - 1)];
+  }
+};
 
 // parses a YPOT (mode 0: NYA = (IOY2 KEY + IOY1) KEY + K) or XPOT (mode 1:
 // NXA = ((IORB KEY + IOY2) KEY + IOY1) KEY + K) list, adding its distinct Y
@@ -1602,8 +1665,8 @@ static int parse_terms(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, cons
     const int io = (mode == 0) ? 1 : (int)(l / KEYORB);
     if (lab[e] < 0 || k > KLIMIT || a < 1 || a > nw || b < 1 || b > nw || io < 1 || io > nw)
       return fail(GG_ERR_ARG, "potential: label outside the orbital set or K above 20");
-    auto it = seen.find({k, a, b});
-    if (it == seen.end()) {
+    int &f = seen.slot(k, a, b, nw);
+    if (f == 0) {
       YDesc y;
       y.k = k;
       y.b = a;
@@ -1612,15 +1675,19 @@ static int parse_terms(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, cons
       y.mtpb = g.n;  // the whole function: the potentials use TB(1:N)
       y.cs = 0;
       y.nd = 1;
-      it = seen.emplace(std::make_tuple(k, a, b), (int)hy.size()).first;
       hy.push_back(y);
+      f = (int)hy.size();
     }
-    t.fidx[e] = it->second;
+    t.fidx[e] = f - 1;
     t.iorb[e] = io;
     t.coef[e] = (mode == 0) ? co[e] : co[e] / g.c;  // XPOT: COEFF = COEFF/C
   }
   return GG_OK;
 }
+
+// XPOT lists at least this long take the two-pass form (products by all
+// SMs, then the per-point sums)
+constexpr int XPOT_SPLIT = 512;
 
 // One orbital's potentials on the device: YP, XP, XQ (N each, 0-based) at
 // out, out + n, out + 2 n.
@@ -1660,7 +1727,7 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
                  pi(J.lag_m), pd(J.lag_wa)};
   }
   DBuf<int> di;
-  DBuf<double> dd;
+  DBuf<double> dd, prod;
   GG_TRY(upload(di, ih, s));
   GG_TRY(upload(dd, dh, s));
   const unsigned blocks = (unsigned)((n + 127) / 128);
@@ -1669,9 +1736,26 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
     double *yp = dPot.p + (size_t)3 * n * j, *xp = yp + n, *xq = xp + n;
     k_potential<<<blocks, 128, 0, s>>>(0, (int)J.y.fidx.size(), di.p + off[j].yf, dd.p + off[j].yc, di.p, dY.p,
                                        g.np, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, yp, nullptr);
-    k_potential<<<blocks, 128, 0, s>>>(1, (int)J.x.fidx.size(), di.p + off[j].xf, dd.p + off[j].xc,
-                                       di.p + off[j].xi, dY.p, g.np, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, xp, xq);
-    ::gg::note_launch();
+    const int nx = (int)J.x.fidx.size();
+    if (nx < XPOT_SPLIT) {
+      k_potential<<<blocks, 128, 0, s>>>(1, nx, di.p + off[j].xf, dd.p + off[j].xc, di.p + off[j].xi, dY.p, g.np,
+                                         g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, xp, xq);
+      ::gg::note_launch();
+    } else {
+      // long lists: the products by all SMs, chunk by chunk, then the sums
+      GG_CUDA(cudaMemsetAsync(xp, 0, 2 * (size_t)n * sizeof(double), s));
+      const int chunk = std::max(1, (int)((64ll << 20) / ((int64_t)n * 16)));
+      GG_TRY(prod.alloc((size_t)2 * std::min(nx, chunk) * n));
+      for (int t0 = 0; t0 < nx; t0 += chunk) {
+        const int nt = std::min(chunk, nx - t0);
+        const double *c0 = dd.p + off[j].xc + t0;
+        k_xprod<<<4 * ctx->sms, 256, 0, s>>>(nt, di.p + off[j].xf + t0, c0, di.p + off[j].xi + t0, dY.p, g.np,
+                                              o.dPF.p, o.dQF.p, o.ld, n, prod.p, prod.p + (size_t)nt * n);
+        k_xsum<<<dim3((n + 31) / 32, 2), 32, 0, s>>>(nt, n, prod.p, prod.p + (size_t)nt * n, xp, xq);
+        ::gg::note_launch();
+        ::gg::note_launch();
+      }
+    }
     ::gg::note_launch();
     if (!J.lag_m.empty()) {
       k_lagcon<<<blocks, 128, 0, s>>>(n, (int)J.lag_m.size(), di.p + off[j].lm, dd.p + off[j].lw, o.dMF.p, g.dR.p,

@@ -24,8 +24,10 @@ def test_potentials_match_oracle(gpu_ready, oracle_mod, run):
     o = oracle_mod.Oracle(n=d["n"], rnt=d["rnt"], h=d["h"], c=d["c"], zz=d["zz"])
     o.set_orbitals(d["nak"], d["mf"], d["pf"], d["qf"])
     nw = len(d["nak"])
-    for seed in (4, 5):
-        k, a, b, io, nya, nxa, co = _lists(nw, n=60, seed=seed)
+    # 1500 terms take XPOT's two-pass form (products by all SMs, then the
+    # per-point sums in list order)
+    for seed, nt in ((4, 60), (5, 60), (6, 1500)):
+        k, a, b, io, nya, nxa, co = _lists(nw, n=nt, seed=seed)
         yp, yp0 = ctx.ypot(nya, co), o.ypot(nya, co)
         assert np.abs(yp - yp0).max() <= 1e-14 * np.abs(yp0).max(), np.abs(yp - yp0).max()
         (xp, xq), (xp0, xq0) = ctx.xpot(nxa, co), o.xpot(nxa, co)
