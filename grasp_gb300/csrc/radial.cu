@@ -1168,20 +1168,198 @@ bool triangrk(int la, int k, int lb) {  // rci90/triangrk.f90:27-37
   return true;
 }
 
+// The same YZK part 2 in three passes for many functions. Each step of
+// k_ychain's recurrences adds an increment that does not depend on the
+// chain, so the increments are formed by all SMs (k_yincr), the chains run
+// only the dependent additions (k_ychain_sum), and Y = Z r^-k + W r^(k+1)
+// is assembled per point (k_yassemble). The operations and their order are
+// k_ychain's: the functions come out identical.
+//   RZ(i) = C1 (T(i-4) + T(i)) + C2 (T(i-3) + T(i-1)) + C3 T(i-2), i >= 5,
+//     added to Z as one term (Z = Z + RTMP);
+//   RW(i) = the three terms C1 (TW(i) + TW(i+4)), C2 (TW(i+1) + TW(i+3)),
+//     C3 TW(i+2), 2 <= i <= MTP, added to W one after the other
+//     (WK = ((WK + t1) + t2) + t3, k_ychain's left-to-right sum).
+__global__ void k_yincr(const YDesc *__restrict__ yd, int nf, const double *__restrict__ TZ,
+                        const double *__restrict__ TW, int np, QuadConst q, double *__restrict__ RZ,
+                        double *__restrict__ RW) {
+  const int f = blockIdx.y;
+  if (f >= nf) return;
+  const int MTP = yd[f].mtp;
+  const double *T = TZ + (size_t)f * np, *Tw = TW + (size_t)f * np;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    double rz = 0.0, w1 = 0.0, w2 = 0.0, w3 = 0.0;
+    if (i >= 5) rz = q.C1 * (T[i - 4] + T[i]) + q.C2 * (T[i - 3] + T[i - 1]) + q.C3 * T[i - 2];
+    if (i >= 2 && i <= MTP) {
+      w1 = q.C1 * (Tw[i] + Tw[i + 4]);
+      w2 = q.C2 * (Tw[i + 1] + Tw[i + 3]);
+      w3 = q.C3 * Tw[i + 2];
+    }
+    RZ[(size_t)f * np + i] = rz;
+    double *rw = RW + ((size_t)f * np + i) * 3;
+    rw[0] = w1;
+    rw[1] = w2;
+    rw[2] = w3;
+  }
+}
+
+// acc = acc + P(o_j, 0) + ... + P(o_j, NT-1) (left to right), O(o_j) = acc
+// for j = 0 .. cnt-1 in order, o_j = start + step j, P holding NT terms per
+// point; the loads of group g + 1 are issued before the additions of group g
+template <int NT, int A>
+__device__ __forceinline__ double ychain_run(double acc, const double *__restrict__ P, double *__restrict__ O,
+                                             int start, int step, int cnt) {
+  double cur[A][NT], nxt[A][NT];
+#pragma unroll
+  for (int u = 0; u < A; ++u)
+#pragma unroll
+    for (int v = 0; v < NT; ++v) cur[u][v] = (u < cnt) ? P[(size_t)(start + step * u) * NT + v] : 0.0;
+  int j = 0;
+  for (; j + A <= cnt; j += A) {
+    const int j1 = j + A;
+#pragma unroll
+    for (int u = 0; u < A; ++u)
+#pragma unroll
+      for (int v = 0; v < NT; ++v) nxt[u][v] = (j1 + u < cnt) ? P[(size_t)(start + step * (j1 + u)) * NT + v] : 0.0;
+#pragma unroll
+    for (int u = 0; u < A; ++u) {
+#pragma unroll
+      for (int v = 0; v < NT; ++v) acc = acc + cur[u][v];
+      O[start + step * (j + u)] = acc;
+    }
+#pragma unroll
+    for (int u = 0; u < A; ++u)
+#pragma unroll
+      for (int v = 0; v < NT; ++v) cur[u][v] = nxt[u][v];
+  }
+#pragma unroll
+  for (int u = 0; u < A; ++u)
+    if (j + u < cnt) {
+#pragma unroll
+      for (int v = 0; v < NT; ++v) acc = acc + cur[u][v];
+      O[start + step * (j + u)] = acc;
+    }
+  return acc;
+}
+// the chains' additions (Z: 16 points loaded ahead, W: 8); writes Z into Y,
+// W into W, each chain's K = 0 correction DIF and the function's asymptotic
+// value ZKLIM
+__global__ void k_ychain_sum(const YDesc *__restrict__ yd, int nf, const double *__restrict__ TZ,
+                             const double *__restrict__ RZ, const double *__restrict__ RW, int np, QuadConst q,
+                             double *__restrict__ Y, double *__restrict__ W, double *__restrict__ dif_out,
+                             double *__restrict__ zk_out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int f = t >> 2, c = t & 3;
+  const bool active = f < nf;
+  const YDesc y = active ? yd[f] : yd[0];
+  const int K = y.k, MTP = y.mtp, MTPP3 = MTP + 3, N = q.n;
+  const size_t base = (size_t)(active ? f : 0) * np;
+  const double *T = TZ + base, *Rz = RZ + base, *Rw = RW + 3 * base;
+  double *Yf = Y + base, *Wf = W + base;
+  const int s = c + 2;  // chain start: 2, 3, 4, 5
+  double z = 0.0;
+  if (active) {
+    if (s <= 4) {
+      double sum = 0.0;
+      for (int kk = 2; kk <= 5; ++kk) sum = sum + q.CNC5C[kk - 2][s - 2] * T[kk];
+      z = sum;
+    } else {  // ZK(5) = ZK(1) + RTMP(5), ZK(1) = 0
+      z = 0.0 + Rz[5];
+    }
+    Yf[s] = z;
+    // the points s + 4, s + 8, ... <= MTP + 3
+    const int cnt = (MTPP3 >= s + 4) ? (MTPP3 - s - 4) / 4 + 1 : 0;
+    z = ychain_run<1, 16>(z, Rz, Yf, s + 4, 4, cnt);
+  }
+  const int owner = (MTPP3 - 2) & 3;
+  const double z_top = __shfl_sync(0xffffffffu, z, (threadIdx.x & ~3) + owner);
+  if (!active) return;
+  double zklim, dif = 0.0;
+  if (K == 0) {
+    zklim = (y.b == y.d) ? 1.0 : 0.0;
+    const double d0 = z - zklim;
+    if (fabs(d0) > q.accy) dif = d0;
+  } else {
+    zklim = z_top;
+  }
+  dif_out[(size_t)f * 4 + c] = dif;
+  if (c == 0) zk_out[f] = zklim;
+  // W from the top of this chain's points with i <= min(N, MTP) down to s
+  const int lim = min(N, MTP);
+  if (lim < s) return;
+  const int cnt = (lim - s) / 4 + 1;  // the points s + 4 (cnt - 1), ..., s + 4, s
+  ychain_run<3, 8>(0.0, Rw, Wf, s + 4 * (cnt - 1), -4, cnt);
+}
+
+__global__ void k_yassemble(const YDesc *__restrict__ yd, int nf, const double *__restrict__ R,
+                            const double *__restrict__ pw, int np, QuadConst q, const double *__restrict__ dif,
+                            const double *__restrict__ zk, const double *__restrict__ W, double *__restrict__ Y) {
+  const int f = blockIdx.y;
+  if (f >= nf) return;
+  const YDesc y = yd[f];
+  const int K = y.k, MTP = y.mtp, MTPP3 = MTP + 3, N = q.n;
+  const double zklim = zk[f];
+  const double *RTTKM = pw + (size_t)(1 * (KLIMIT + 1) + K) * np;
+  const double *RTTK1 = pw + (size_t)(2 * (KLIMIT + 1) + K) * np;
+  const double *Wf = W + (size_t)f * np;
+  double *Yf = Y + (size_t)f * np;
+  for (int i = 2 + blockIdx.x * blockDim.x + threadIdx.x; i < np; i += gridDim.x * blockDim.x) {
+    double yv = 0.0;
+    if (i <= N) {
+      double zf;
+      if (K == 0) {
+        if (i <= MTPP3) {
+          const double d = dif[(size_t)f * 4 + ((i - 2) & 3)];
+          zf = (d != 0.0) ? Yf[i] - d : Yf[i];
+        } else {
+          zf = zklim;
+        }
+      } else {
+        zf = (i <= MTPP3) ? Yf[i] * RTTKM[i] : zklim * RTTKM[i];
+      }
+      double wkf = 0.0;
+      if (i <= MTP) {
+        const double wk = Wf[i];
+        wkf = (K == 0) ? wk * R[i] : wk * RTTK1[i];
+      }
+      yv = zf + wkf;
+      if (i > y.mtpb) yv = 0.0;
+    }
+    Yf[i] = yv;
+  }
+}
+
+// build_y takes the three-pass form from this many functions on
+constexpr int YSPLIT_MIN = 32;
+
 // Builds Y functions for the descriptor list on the device: TZ/TW scratch
 // then the chains. Y must hold nf * np doubles.
 int build_y(gg_ctx *ctx, const YDesc *d_yd, int nf, double *dY, DBuf<double> &scratch) {
   Grid &g = ctx->grid;
   Orbitals &o = ctx->orb;
   const int np = g.np;
-  GG_TRY(scratch.alloc((size_t)2 * nf * np));
+  const bool split = nf >= YSPLIT_MIN;
+  GG_TRY(scratch.alloc(split ? (size_t)6 * nf * np + (size_t)5 * nf : (size_t)2 * nf * np));
   double *TZ = scratch.p, *TW = scratch.p + (size_t)nf * np;
   dim3 grid1((np + 127) / 128, nf);
   k_ytemp<<<grid1, 128, 0, ctx->stream>>>(d_yd, nf, o.dPF.p, o.dQF.p, o.ld, g.dRP.p, g.dPow.p, np, TZ, TW); ::gg::note_launch();
   GG_CUDA(cudaGetLastError());
   GG_CUDA(cudaMemsetAsync(dY, 0, (size_t)nf * np * sizeof(double), ctx->stream));
   const int nthr = nf * 4;
-  k_ychain<<<(nthr + 127) / 128, 128, 0, ctx->stream>>>(d_yd, nf, TZ, TW, g.dR.p, g.dPow.p, np, g.q, dY); ::gg::note_launch();
+  if (!split) {
+    k_ychain<<<(nthr + 127) / 128, 128, 0, ctx->stream>>>(d_yd, nf, TZ, TW, g.dR.p, g.dPow.p, np, g.q, dY);
+    ::gg::note_launch();
+  } else {
+    // RZ: one term per point; RW: three terms per point; DIF per chain; ZKLIM
+    double *RZ = TW + (size_t)nf * np, *RW = RZ + (size_t)nf * np, *dif = RW + (size_t)3 * nf * np;
+    double *zk = dif + 4 * nf;
+    k_yincr<<<grid1, 128, 0, ctx->stream>>>(d_yd, nf, TZ, TW, np, g.q, RZ, RW);
+    // W goes where TW was: k_yincr was its last reader
+    k_ychain_sum<<<(nthr + 127) / 128, 128, 0, ctx->stream>>>(d_yd, nf, TZ, RZ, RW, np, g.q, dY, TW, dif, zk);
+    k_yassemble<<<grid1, 128, 0, ctx->stream>>>(d_yd, nf, g.dR.p, g.dPow.p, np, g.q, dif, zk, TW, dY);
+    ::gg::note_launch();
+    ::gg::note_launch();
+    ::gg::note_launch();
+  }
   GG_CUDA(cudaGetLastError());
   return GG_OK;
 }
