@@ -904,24 +904,32 @@ __global__ void k_potential(int mode, int ncof, const int *__restrict__ fidx, co
   }
 }
 
-// XPOT in two passes for long lists: the products of terms t0 .. t0+nt at
+// XPOT in two passes for long lists: the products of a segment of terms at
 // every grid point (CTB = COEFF TB, CTB QF and CTB PF) by all SMs, then per
 // grid point the sums XP = XP + CTB QF, XQ = XQ - CTB PF in list order (the
-// same operations as k_potential; only the additions stay sequential)
-__global__ void k_xprod(int nt, const int *__restrict__ fidx, const double *__restrict__ coef,
-                        const int *__restrict__ iorb, const double *__restrict__ Y, int np,
-                        const double *__restrict__ PF, const double *__restrict__ QF, int ld, int n,
-                        double *__restrict__ P1, double *__restrict__ P2) {
-  const int tot = nt * n;  // the caller keeps nt * n below 2^22
+// same operations as k_potential; only the additions stay sequential). A
+// segment is terms t0 .. t0+nt of one job's list; one launch takes the
+// segments of several jobs (blockIdx.y / blockIdx.z).
+struct XSeg {
+  const int *fidx, *iorb;
+  const double *coef;
+  double *P1, *P2;  // nt * n products each
+  double *xp, *xq;
+  int nt;
+};
+__global__ void k_xprod(const XSeg *__restrict__ segs, const double *__restrict__ Y, int np,
+                        const double *__restrict__ PF, const double *__restrict__ QF, int ld, int n) {
+  const XSeg g = segs[blockIdx.y];
+  const int tot = g.nt * n;  // the caller keeps nt * n below 2^26
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < tot; e += gridDim.x * blockDim.x) {
     const int t = e / n, i = e % n + 1;
-    const double ctb = coef[t] * Y[(size_t)fidx[t] * np + i];
-    P1[e] = ctb * pf(QF, ld, i, iorb[t]);
-    P2[e] = ctb * pf(PF, ld, i, iorb[t]);
+    const double ctb = g.coef[t] * Y[(size_t)g.fidx[t] * np + i];
+    g.P1[e] = ctb * pf(QF, ld, i, g.iorb[t]);
+    g.P2[e] = ctb * pf(PF, ld, i, g.iorb[t]);
   }
 }
-// k_xsum: 32 grid points per block; blockIdx.y = 0 sums XP = XP + P1,
-// blockIdx.y = 1 sums XQ = XQ - P2. The loads run XSUM_AHEAD terms ahead of
+// k_xsum: 32 grid points of segment blockIdx.z per block; blockIdx.y = 0
+// sums XP = XP + P1, blockIdx.y = 1 sums XQ = XQ - P2. The loads run XSUM_AHEAD terms ahead of
 // the additions (register double buffer) so that the chain of dependent
 // FP64 additions, not the load latency, sets the time.
 constexpr int XSUM_AHEAD = 16;
@@ -945,14 +953,14 @@ __device__ __forceinline__ double xsum_chain(double acc, const double *__restric
     if (t + u < nt) acc = SUB ? acc - cur[u] : acc + cur[u];
   return acc;
 }
-__global__ void k_xsum(int nt, int n, const double *__restrict__ P1, const double *__restrict__ P2,
-                       double *__restrict__ xp, double *__restrict__ xq) {
+__global__ void k_xsum(const XSeg *__restrict__ segs, int n) {
+  const XSeg g = segs[blockIdx.z];
   const int i = blockIdx.x * 32 + threadIdx.x;
   if (i >= n) return;
   if (blockIdx.y == 0)
-    xp[i] = xsum_chain<false>(xp[i], P1 + i, nt, n);
+    g.xp[i] = xsum_chain<false>(g.xp[i], g.P1 + i, g.nt, n);
   else
-    xq[i] = xsum_chain<true>(xq[i], P2 + i, nt, n);
+    g.xq[i] = xsum_chain<true>(g.xq[i], g.P2 + i, g.nt, n);
 }
 
 // DPBDT (lib9290/dpbdt.f90:39-99): 13-point derivative of orbital J at grid
@@ -1864,7 +1872,7 @@ static int parse_terms(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, cons
 }
 
 // XPOT lists at least this long take the two-pass form (products by all
-// SMs, then the per-point sums)
+// SMs, then the per-point sums, all such lists of one call together)
 constexpr int XPOT_SPLIT = 512;
 
 // One orbital's potentials on the device: YP, XP, XQ (N each, 0-based) at
@@ -1909,32 +1917,70 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
   GG_TRY(upload(di, ih, s));
   GG_TRY(upload(dd, dh, s));
   const unsigned blocks = (unsigned)((n + 127) / 128);
+  GG_CUDA(cudaMemsetAsync(dPot.p, 0, (size_t)3 * n * jobs.size() * sizeof(double), s));
+  std::vector<int> longj;  // jobs whose XPOT takes the two-pass form
   for (size_t j = 0; j < jobs.size(); ++j) {
     const PotJob &J = jobs[j];
     double *yp = dPot.p + (size_t)3 * n * j, *xp = yp + n, *xq = xp + n;
     k_potential<<<blocks, 128, 0, s>>>(0, (int)J.y.fidx.size(), di.p + off[j].yf, dd.p + off[j].yc, di.p, dY.p,
                                        g.np, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, yp, nullptr);
-    const int nx = (int)J.x.fidx.size();
-    if (nx < XPOT_SPLIT) {
-      k_potential<<<blocks, 128, 0, s>>>(1, nx, di.p + off[j].xf, dd.p + off[j].xc, di.p + off[j].xi, dY.p, g.np,
-                                         g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, xp, xq);
-      ::gg::note_launch();
-    } else {
-      // long lists: the products by all SMs, chunk by chunk, then the sums
-      GG_CUDA(cudaMemsetAsync(xp, 0, 2 * (size_t)n * sizeof(double), s));
-      const int chunk = std::max(1, (int)((64ll << 20) / ((int64_t)n * 16)));
-      GG_TRY(prod.alloc((size_t)2 * std::min(nx, chunk) * n));
-      for (int t0 = 0; t0 < nx; t0 += chunk) {
-        const int nt = std::min(chunk, nx - t0);
-        const double *c0 = dd.p + off[j].xc + t0;
-        k_xprod<<<4 * ctx->sms, 256, 0, s>>>(nt, di.p + off[j].xf + t0, c0, di.p + off[j].xi + t0, dY.p, g.np,
-                                              o.dPF.p, o.dQF.p, o.ld, n, prod.p, prod.p + (size_t)nt * n);
-        k_xsum<<<dim3((n + 31) / 32, 2), 32, 0, s>>>(nt, n, prod.p, prod.p + (size_t)nt * n, xp, xq);
-        ::gg::note_launch();
-        ::gg::note_launch();
-      }
-    }
     ::gg::note_launch();
+    const int nx = (int)J.x.fidx.size();
+    if (nx >= XPOT_SPLIT) {
+      longj.push_back((int)j);
+      continue;
+    }
+    k_potential<<<blocks, 128, 0, s>>>(1, nx, di.p + off[j].xf, dd.p + off[j].xc, di.p + off[j].xi, dY.p, g.np,
+                                       g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, xp, xq);
+    ::gg::note_launch();
+  }
+  // the long lists of all jobs together, in rounds of at most `per` terms of
+  // each job (a job's rounds run in its list's order), each round one
+  // product launch and one sum launch over its segments
+  DBuf<XSeg> dseg;
+  std::vector<size_t> rstart;
+  if (!longj.empty()) {
+    const int64_t round_terms = std::max<int64_t>(1, (512ll << 20) / (16ll * n));
+    const int per = (int)std::max<int64_t>(1, std::min<int64_t>(round_terms / (int64_t)longj.size(), (1 << 26) / n));
+    std::vector<XSeg> hs;
+    std::vector<size_t> poff;
+    size_t maxprod = 0;
+    for (int t0 = 0;; t0 += per) {
+      const size_t r0 = hs.size();
+      size_t po = 0;
+      for (int j : longj) {
+        const int nx = (int)jobs[j].x.fidx.size();
+        if (t0 >= nx) continue;
+        const int nt = std::min(per, nx - t0);
+        double *yp = dPot.p + (size_t)3 * n * j;
+        hs.push_back(XSeg{di.p + off[j].xf + t0, di.p + off[j].xi + t0, dd.p + off[j].xc + t0, nullptr, nullptr,
+                          yp + n, yp + 2 * n, nt});
+        poff.push_back(po);
+        po += (size_t)2 * nt * n;
+      }
+      if (hs.size() == r0) break;
+      rstart.push_back(r0);
+      maxprod = std::max(maxprod, po);
+    }
+    rstart.push_back(hs.size());
+    GG_TRY(prod.alloc(maxprod));
+    for (size_t e = 0; e < hs.size(); ++e) {
+      hs[e].P1 = prod.p + poff[e];
+      hs[e].P2 = hs[e].P1 + (size_t)hs[e].nt * n;
+    }
+    GG_TRY(upload(dseg, hs, s));
+    for (size_t r = 0; r + 1 < rstart.size(); ++r) {
+      const unsigned nseg = (unsigned)(rstart[r + 1] - rstart[r]);
+      const unsigned bx = std::max(1u, (unsigned)(4 * ctx->sms) / nseg);
+      k_xprod<<<dim3(bx, nseg), 256, 0, s>>>(dseg.p + rstart[r], dY.p, g.np, o.dPF.p, o.dQF.p, o.ld, n);
+      k_xsum<<<dim3((n + 31) / 32, 2, nseg), 32, 0, s>>>(dseg.p + rstart[r], n);
+      ::gg::note_launch();
+      ::gg::note_launch();
+    }
+  }
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const PotJob &J = jobs[j];
+    double *xp = dPot.p + (size_t)3 * n * j + n, *xq = xp + n;
     if (!J.lag_m.empty()) {
       k_lagcon<<<blocks, 128, 0, s>>>(n, (int)J.lag_m.size(), di.p + off[j].lm, dd.p + off[j].lw, o.dMF.p, g.dR.p,
                                       o.dPF.p, o.dQF.p, o.ld, xp, xq);
