@@ -880,28 +880,67 @@ __global__ void k_quad_table(const QuadItem *__restrict__ items, const int *__re
 // YPOT / XPOT (rmcdhf90/ypot.f90:35-49, xpot.f90:31-54): one thread per grid
 // point combines the list's Y functions in the list's order (the reference's
 // per-point operations: YP = YP - COEFF*TB; CTB = COEFF*TB, XP += CTB*QF,
-// XQ -= CTB*PF, with COEFF = XA/C formed on the host).
-__global__ void k_potential(int mode, int ncof, const int *__restrict__ fidx, const double *__restrict__ coef,
-                            const int *__restrict__ iorb, const double *__restrict__ Y, int np,
+// XQ -= CTB*PF, with COEFF = XA/C formed on the host). One launch takes the
+// lists of several jobs (blockIdx.y); each thread loads the next POT_AHEAD
+// terms (index, coefficient, Y value, orbital values) before it combines
+// the current ones, so the loads do not wait on the chain.
+struct PotSeg {
+  const int *fidx, *iorb;
+  const double *coef;
+  double *out0, *out1;
+  int ncof;
+};
+constexpr int POT_AHEAD = 8;
+template <int MODE>
+__global__ void k_potential(const PotSeg *__restrict__ segs, const double *__restrict__ Y, int np,
                             const double *__restrict__ ZZ, const double *__restrict__ PF,
-                            const double *__restrict__ QF, int ld, int n, double *__restrict__ out0,
-                            double *__restrict__ out1) {
-  for (int i = 1 + blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
-    if (mode == 0) {
-      double yp = ZZ[i];
-      for (int t = 0; t < ncof; ++t) yp = yp - coef[t] * Y[(size_t)fidx[t] * np + i];
-      out0[i - 1] = yp;
-    } else {
-      double xp = 0.0, xq = 0.0;
-      for (int t = 0; t < ncof; ++t) {
-        const double ctb = coef[t] * Y[(size_t)fidx[t] * np + i];
-        xp = xp + ctb * pf(QF, ld, i, iorb[t]);
-        xq = xq - ctb * pf(PF, ld, i, iorb[t]);
+                            const double *__restrict__ QF, int ld, int n) {
+  const PotSeg g = segs[blockIdx.y];
+  const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  double cy[POT_AHEAD], cc[POT_AHEAD], cq[POT_AHEAD], cp[POT_AHEAD];
+  double ny[POT_AHEAD], nc[POT_AHEAD], nq[POT_AHEAD], npf[POT_AHEAD];
+  auto load = [&](int t0, double *y, double *c, double *qv, double *pv) {
+#pragma unroll
+    for (int u = 0; u < POT_AHEAD; ++u) {
+      const int t = t0 + u;
+      y[u] = c[u] = qv[u] = pv[u] = 0.0;
+      if (t < g.ncof) {
+        c[u] = g.coef[t];
+        y[u] = Y[(size_t)g.fidx[t] * np + i];
+        if (MODE == 1) {
+          const int io = g.iorb[t];
+          qv[u] = pf(QF, ld, i, io);
+          pv[u] = pf(PF, ld, i, io);
+        }
       }
-      out0[i - 1] = xp;
-      out1[i - 1] = xq;
+    }
+  };
+  double a0 = (MODE == 0) ? ZZ[i] : 0.0, a1 = 0.0;
+  load(0, cy, cc, cq, cp);
+  for (int t0 = 0; t0 < g.ncof; t0 += POT_AHEAD) {
+    load(t0 + POT_AHEAD, ny, nc, nq, npf);
+#pragma unroll
+    for (int u = 0; u < POT_AHEAD; ++u)
+      if (t0 + u < g.ncof) {
+        if (MODE == 0) {
+          a0 = a0 - cc[u] * cy[u];
+        } else {
+          const double ctb = cc[u] * cy[u];
+          a0 = a0 + ctb * cq[u];
+          a1 = a1 - ctb * cp[u];
+        }
+      }
+#pragma unroll
+    for (int u = 0; u < POT_AHEAD; ++u) {
+      cy[u] = ny[u];
+      cc[u] = nc[u];
+      cq[u] = nq[u];
+      cp[u] = npf[u];
     }
   }
+  g.out0[i - 1] = a0;
+  if (MODE == 1) g.out1[i - 1] = a1;
 }
 
 // XPOT in two passes for long lists: the products of a segment of terms at
@@ -1006,9 +1045,21 @@ __device__ void dpbdt_warp(const double *PF, const double *QF, int ld, int J, co
 // XP(I) = XP(I) + WARI QF(I,M), XQ(I) = XQ(I) - WARI PF(I,M), WARI = WA R(I),
 // I = 1..MF(M); mo[t] = M and wa[t] = ECV WB of the multipliers the host kept
 // (those of pairs with this orbital, |WA| >= EPS). xp, xq 0-based.
-__global__ void k_lagcon(int n, int nt, const int *__restrict__ mo, const double *__restrict__ wa,
-                         const int *__restrict__ MF, const double *__restrict__ R, const double *__restrict__ PF,
-                         const double *__restrict__ QF, int ld, double *__restrict__ xp, double *__restrict__ xq) {
+// One job's LAGCON or DACON list (blockIdx.y selects the job): the entries'
+// orbitals and weights, and the job's XP, XQ.
+struct TermSeg {
+  const int *idx;
+  const double *w;
+  double *xp, *xq;
+  int nt;
+};
+__global__ void k_lagcon(const TermSeg *__restrict__ segs, int n, const int *__restrict__ MF,
+                         const double *__restrict__ R, const double *__restrict__ PF, const double *__restrict__ QF,
+                         int ld) {
+  const TermSeg g = segs[blockIdx.y];
+  const int nt = g.nt, *mo = g.idx;
+  const double *wa = g.w;
+  double *xp = g.xp, *xq = g.xq;
   for (int i = 1 + blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
     double p = xp[i - 1], qv = xq[i - 1];
     for (int t = 0; t < nt; ++t) {
@@ -1028,11 +1079,14 @@ __global__ void k_lagcon(int n, int nt, const int *__restrict__ mo, const double
 //   XP(I) += COEFF (TA RPORII + FK PFI - (2C R(I) + ZBCI) QFI),
 //   XQ(I) += COEFF (TB RPORII - FK QFI + ZBCI PFI),
 // RPORII = 1/(H RPOR(I)), ZBCI = ZZ(I)/C, FK = kappa(IORB). xp, xq 0-based.
-__global__ void k_dacon(int n, int nd, const int *__restrict__ nda, const double *__restrict__ da,
-                        const int *__restrict__ NAK, const int *__restrict__ MF, const double *__restrict__ R,
-                        const double *__restrict__ RPOR, const double *__restrict__ ZZ, const double *__restrict__ PF,
-                        const double *__restrict__ QF, int ld, QuadConst q, double *__restrict__ xp,
-                        double *__restrict__ xq) {
+__global__ void k_dacon(const TermSeg *__restrict__ segs, int n, const int *__restrict__ NAK,
+                        const int *__restrict__ MF, const double *__restrict__ R, const double *__restrict__ RPOR,
+                        const double *__restrict__ ZZ, const double *__restrict__ PF, const double *__restrict__ QF,
+                        int ld, QuadConst q) {
+  const TermSeg g = segs[blockIdx.y];
+  const int nd = g.nt, *nda = g.idx;
+  const double *da = g.w;
+  double *xp = g.xp, *xq = g.xq;
   const double twoc = q.c + q.c;
   for (int i = 2 + blockIdx.x * blockDim.x + threadIdx.x; i <= n; i += gridDim.x * blockDim.x) {
     double p = xp[i - 1], qv = xq[i - 1];
@@ -1893,12 +1947,13 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
   Grid &g = ctx->grid;
   cudaStream_t s = ctx->stream;
   const int n = g.n, nf = std::max(1, (int)hy.size());
-  if (hy.empty()) hy.push_back(YDesc{0, 1, 1, 2, 2, 0, 1});  // no terms: no function is read
   DBuf<YDesc> dy;
   DBuf<double> dY, scratch;
-  GG_TRY(upload(dy, hy, s));
   GG_TRY(dY.alloc((size_t)nf * g.np));
-  GG_TRY(build_y(ctx, dy.p, nf, dY.p, scratch));
+  if (!hy.empty()) {  // no terms: no function is read
+    GG_TRY(upload(dy, hy, s));
+    GG_TRY(build_y(ctx, dy.p, nf, dY.p, scratch));
+  }
   GG_TRY(dPot.alloc((size_t)3 * n * std::max<size_t>(1, jobs.size())));
   // every job's integer and coefficient arrays in one upload each
   std::vector<int> ih;
@@ -1918,21 +1973,40 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
   GG_TRY(upload(dd, dh, s));
   const unsigned blocks = (unsigned)((n + 127) / 128);
   GG_CUDA(cudaMemsetAsync(dPot.p, 0, (size_t)3 * n * jobs.size() * sizeof(double), s));
+  // YPOT of every job and the short XPOT lists: one launch each
   std::vector<int> longj;  // jobs whose XPOT takes the two-pass form
+  std::vector<PotSeg> hp;
   for (size_t j = 0; j < jobs.size(); ++j) {
-    const PotJob &J = jobs[j];
-    double *yp = dPot.p + (size_t)3 * n * j, *xp = yp + n, *xq = xp + n;
-    k_potential<<<blocks, 128, 0, s>>>(0, (int)J.y.fidx.size(), di.p + off[j].yf, dd.p + off[j].yc, di.p, dY.p,
-                                       g.np, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, yp, nullptr);
-    ::gg::note_launch();
-    const int nx = (int)J.x.fidx.size();
-    if (nx >= XPOT_SPLIT) {
+    double *yp = dPot.p + (size_t)3 * n * j;
+    hp.push_back(PotSeg{di.p + off[j].yf, nullptr, dd.p + off[j].yc, yp, nullptr, (int)jobs[j].y.fidx.size()});
+  }
+  const size_t nyseg = hp.size();
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const int nx = (int)jobs[j].x.fidx.size();
+    double *xp = dPot.p + (size_t)3 * n * j + n;
+    if (nx >= XPOT_SPLIT)
       longj.push_back((int)j);
-      continue;
+    else
+      hp.push_back(PotSeg{di.p + off[j].xf, di.p + off[j].xi, dd.p + off[j].xc, xp, xp + n, nx});
+  }
+  DBuf<PotSeg> dpseg;
+  if (!hp.empty()) {
+    GG_TRY(upload(dpseg, hp, s));
+    for (size_t a = 0; a < hp.size(); a += 65535) {  // gridDim.y limit
+      const size_t b = std::min(hp.size(), a + 65535);
+      if (a < nyseg) {
+        const size_t e = std::min(b, nyseg);
+        k_potential<0><<<dim3(blocks, (unsigned)(e - a)), 128, 0, s>>>(dpseg.p + a, dY.p, g.np, g.dZZ.p, o.dPF.p,
+                                                                        o.dQF.p, o.ld, n);
+        ::gg::note_launch();
+      }
+      if (b > nyseg) {
+        const size_t a1 = std::max(a, nyseg);
+        k_potential<1><<<dim3(blocks, (unsigned)(b - a1)), 128, 0, s>>>(dpseg.p + a1, dY.p, g.np, g.dZZ.p, o.dPF.p,
+                                                                         o.dQF.p, o.ld, n);
+        ::gg::note_launch();
+      }
     }
-    k_potential<<<blocks, 128, 0, s>>>(1, nx, di.p + off[j].xf, dd.p + off[j].xc, di.p + off[j].xi, dY.p, g.np,
-                                       g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, n, xp, xq);
-    ::gg::note_launch();
   }
   // the long lists of all jobs together, in rounds of at most `per` terms of
   // each job (a job's rounds run in its list's order), each round one
@@ -1978,17 +2052,33 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
       ::gg::note_launch();
     }
   }
-  for (size_t j = 0; j < jobs.size(); ++j) {
-    const PotJob &J = jobs[j];
-    double *xp = dPot.p + (size_t)3 * n * j + n, *xq = xp + n;
-    if (!J.lag_m.empty()) {
-      k_lagcon<<<blocks, 128, 0, s>>>(n, (int)J.lag_m.size(), di.p + off[j].lm, dd.p + off[j].lw, o.dMF.p, g.dR.p,
-                                      o.dPF.p, o.dQF.p, o.ld, xp, xq);
+  // then every job's LAGCON terms (one launch) and DACON terms (one launch),
+  // in that order per job as in COFPOT
+  std::vector<TermSeg> ht;
+  size_t nlag = 0;
+  for (int pass = 0; pass < 2; ++pass) {
+    for (size_t j = 0; j < jobs.size(); ++j) {
+      const PotJob &J = jobs[j];
+      double *xp = dPot.p + (size_t)3 * n * j + n;
+      if (pass == 0 && !J.lag_m.empty())
+        ht.push_back(TermSeg{di.p + off[j].lm, dd.p + off[j].lw, xp, xp + n, (int)J.lag_m.size()});
+      if (pass == 1 && !J.nda.empty())
+        ht.push_back(TermSeg{di.p + off[j].dn, dd.p + off[j].dd, xp, xp + n, (int)J.nda.size()});
+    }
+    if (pass == 0) nlag = ht.size();
+  }
+  DBuf<TermSeg> dtseg;
+  if (!ht.empty()) {
+    GG_TRY(upload(dtseg, ht, s));
+    for (size_t a = 0; a < nlag; a += 65535) {  // gridDim.y limit
+      const unsigned c = (unsigned)std::min<size_t>(65535, nlag - a);
+      k_lagcon<<<dim3(blocks, c), 128, 0, s>>>(dtseg.p + a, n, o.dMF.p, g.dR.p, o.dPF.p, o.dQF.p, o.ld);
       ::gg::note_launch();
     }
-    if (!J.nda.empty()) {
-      k_dacon<<<blocks, 128, 0, s>>>(n, (int)J.nda.size(), di.p + off[j].dn, dd.p + off[j].dd, o.dNAK.p, o.dMF.p,
-                                     g.dR.p, g.dRPOR.p, g.dZZ.p, o.dPF.p, o.dQF.p, o.ld, g.q, xp, xq);
+    for (size_t a = nlag; a < ht.size(); a += 65535) {
+      const unsigned c = (unsigned)std::min<size_t>(65535, ht.size() - a);
+      k_dacon<<<dim3(blocks, c), 128, 0, s>>>(dtseg.p + a, n, o.dNAK.p, o.dMF.p, g.dR.p, g.dRPOR.p, g.dZZ.p, o.dPF.p,
+                                              o.dQF.p, o.ld, g.q);
       ::gg::note_launch();
     }
   }
@@ -2078,9 +2168,11 @@ int gg_cofpot(gg_ctx *ctx, int j, double ucfj, const gg_cof *cof, int nec, const
   DBuf<double> pot;
   GG_TRY(run_potentials(ctx, jobs, hy, pot));
   const int n = ctx->grid.n;
-  GG_CUDA(cudaMemcpy(yp, pot.p, n * sizeof(double), cudaMemcpyDeviceToHost));
-  GG_CUDA(cudaMemcpy(xp, pot.p + n, n * sizeof(double), cudaMemcpyDeviceToHost));
-  GG_CUDA(cudaMemcpy(xq, pot.p + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+  std::vector<double> h((size_t)3 * n);  // one read-back of YP, XP, XQ
+  GG_CUDA(cudaMemcpy(h.data(), pot.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
+  std::copy(h.begin(), h.begin() + n, yp);
+  std::copy(h.begin() + n, h.begin() + 2 * n, xp);
+  std::copy(h.begin() + 2 * n, h.end(), xq);
   return GG_OK;
 }
 

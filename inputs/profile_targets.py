@@ -13,6 +13,8 @@ kernel family it is named for, a few times:
   python -m inputs.profile_targets batch8   # the same for 8 ions (80 blocks), for detailed captures
   python -m inputs.profile_targets breit    # the type-1 Breit table of the Ne VII orbital set (16 subshells)
   python -m inputs.profile_targets setcof   # SETCOF's device pass over the Fe XV block's lists
+  python -m inputs.profile_targets potentials  # from those lists: COFPOT of orbital 5, SETLAG over the
+                                            # 55 same-kappa pairs (twice each)
 """
 from __future__ import annotations
 
@@ -124,6 +126,29 @@ def setcof():
     print("lists of orbital 5:", {k: len(v) for k, v in ctx.setcof(5, 2.0).items()})
 
 
+def potentials():
+    """COFPOT of orbital 5 (136 / 6,587 / 4 YPOT / XPOT / DACON terms) and
+    SETLAG over the Fe XV orbitals' 55 same-kappa pairs, from the device
+    SETCOF lists of the block's 10 eigenvectors; twice each."""
+    import numpy as np
+
+    from grasp_gb300 import SPLIT
+    w, ctx, H = _fe15_context()
+    ev, vec, info = H.maneig(w.nroots, flavour=0, precision=SPLIT, mblock=w.nroots)
+    nw = len(w.orb.nak)
+    ctx.setcof_prepare([H], [np.full(w.nroots, 1.0 / w.nroots)], [vec], eol=True)
+    lists = [ctx.setcof(j, 2.0) for j in range(1, nw + 1)]
+    nak = np.asarray(w.orb.nak)
+    pairs = np.array([i + 215 * j for j in range(2, nw + 1) for i in range(1, j) if nak[i - 1] == nak[j - 1]],
+                     np.int32)
+    ucf = 1.0 + 0.05 * np.arange(nw)
+    for _ in range(2):
+        ctx.cofpot(5, ucf[4], lists[4])
+        ctx.setlag(pairs, ucf, np.zeros(nw, np.int32), lists)
+    print("XPOT terms of orbital 5:", len(lists[4]["nxa"]), "pairs:", pairs.size)
+
+
 if __name__ == "__main__":
     {"spmv": spmv, "spmm": spmm, "solve": solve, "solve2": solve2, "rk": rk, "rk_split": rk_split, "batch": batch,
-     "batch8": lambda: batch(zs=tuple(range(10, 18))), "breit": breit, "setcof": setcof}[sys.argv[1]]()
+     "batch8": lambda: batch(zs=tuple(range(10, 18))), "breit": breit, "setcof": setcof,
+     "potentials": potentials}[sys.argv[1]]()
