@@ -103,3 +103,38 @@ def test_setlag_matches_oracle(gpu_ready, oracle_mod, run):
     bad = [(i, j) for j in range(2, nw + 1) for i in range(1, j) if d["nak"][i - 1] != d["nak"][j - 1]][0]
     with pytest.raises(GGError):
         ctx.setlag(np.array([bad[0] + KEY * bad[1]], np.int32), np.ones(nw), np.zeros(nw, np.int32), cofs)
+
+
+def test_setlag_long_and_short_lists_match_oracle(gpu_ready, oracle_mod):
+    """SETLAG where some orbitals' XPOT lists are long (600 to 1,100 terms:
+    the joint two-pass rounds over several orbitals) and the others short
+    (one joint launch), with YPOT lists of every length modulo the
+    prefetch depth, and DACON terms on every orbital: the multipliers equal
+    the oracle's (bar 1e-12 of the largest)."""
+    from tests.test_lagrange import same_kappa_pairs
+    d, ctx, o = _ctx_oracle("Ge", oracle_mod)
+    nw = len(d["nak"])
+    cofs = []
+    for j in range(1, nw + 1):
+        nx = 600 + 37 * j if j % 3 == 0 else 5 + j
+        ny = 3 + 5 * j
+        _, _, _, _, _, nxa, cx = _lists(nw, n=nx, seed=200 + j)
+        _, _, _, _, nya, _, cy = _lists(nw, n=ny, seed=300 + j)
+        rng = np.random.default_rng(400 + j)
+        cofs.append(dict(nya=nya, ya=cy, nxa=nxa, xa=cx, nda=rng.integers(1, nw + 1, 2),
+                         da=rng.normal(size=2) * 0.1))
+    assert sum(len(c["nxa"]) >= 512 for c in cofs) >= 2
+    iecc = same_kappa_pairs(d["nak"], 12, 9)
+    ucf = np.random.default_rng(10).uniform(0.5, 2.0, nw)
+    lfix = np.zeros(nw, np.int32)
+    ecv = ctx.setlag(iecc, ucf, lfix, cofs)
+    ecv0 = o.setlag(iecc, ucf, lfix, cofs)
+    scale = max(1.0, np.abs(ecv0).max())
+    assert np.abs(ecv - ecv0).max() <= 1e-12 * scale, np.abs(ecv - ecv0).max() / scale
+    # COFPOT of a long-list orbital with LAGCON terms through the same path
+    j = 3
+    ecv1 = np.random.default_rng(11).normal(size=iecc.size)
+    got = ctx.cofpot(j, 1.25, cofs[j - 1], iecc, ecv1)
+    ref = o.cofpot(j, 1.25, cofs[j - 1], iecc, ecv1)
+    for a, b in zip(got, ref):
+        assert np.abs(a - b).max() <= 1e-14 * max(1e-300, np.abs(b).max())
