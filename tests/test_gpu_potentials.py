@@ -138,3 +138,25 @@ def test_setlag_long_and_short_lists_match_oracle(gpu_ready, oracle_mod):
     ref = o.cofpot(j, 1.25, cofs[j - 1], iecc, ecv1)
     for a, b in zip(got, ref):
         assert np.abs(a - b).max() <= 1e-14 * max(1e-300, np.abs(b).max())
+
+
+@pytest.mark.parametrize("run", ["He", "Ge"])
+def test_three_pass_y_build_equals_one_pass(gpu_ready, oracle_mod, run):
+    """The Y functions of the three-pass build (k_yincr, k_ychain_sum,
+    k_yassemble: lists of 32 or more distinct functions) equal the one-pass
+    k_ychain's (a single function) to the bit: YPOT over 48 distinct
+    functions whose coefficients are zero but one equals YPOT of that one
+    term alone, for functions with k = 0 (b = d: the asymptote 1; b != d)
+    and k > 0."""
+    d, ctx, o = _ctx_oracle(run, oracle_mod)
+    nw = len(d["nak"])
+    rng = np.random.default_rng(12)
+    keys = {(0, 1, 1), (0, 2, 2), (0, 1, 2), (2, 1, 3), (5, 2, nw)}
+    while len(keys) < 48:
+        keys.add((int(rng.integers(0, 6)), int(rng.integers(1, nw + 1)), int(rng.integers(1, nw + 1))))
+    keys = sorted(keys)
+    nya = np.array([(b * KEY + a) * KEY + k for k, a, b in keys], np.int32)
+    for t in [keys.index(x) for x in ((0, 1, 1), (0, 2, 2), (0, 1, 2), (2, 1, 3), (5, 2, nw))] + [7, 30, 47]:
+        co = np.zeros(len(keys))
+        co[t] = 1.7
+        np.testing.assert_array_equal(ctx.ypot(nya, co), ctx.ypot(nya[t:t + 1], co[t:t + 1]), err_msg=str(keys[t]))
