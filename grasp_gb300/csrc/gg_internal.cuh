@@ -211,6 +211,8 @@ struct gg_ctx {
   cudaEvent_t aux_done = nullptr;
   gg::BreitTable breit[2];      // GENINTBREIT1, GENINTBREIT2
   std::shared_ptr<void> setcof; // setcof.cu: the sums of the last gg_setcof_prepare
+  std::shared_ptr<void> pot_stage;  // radial.cu: pinned staging of the potentials' coefficient lists
+  size_t pot_stage_bytes = 0;
 };
 
 struct gg_hmat {

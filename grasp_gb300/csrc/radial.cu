@@ -1002,6 +1002,72 @@ __global__ void k_xsum(const XSeg *__restrict__ segs, int n) {
     g.xq[i] = xsum_chain<true>(g.xq[i], g.P2 + i, g.nt, n);
 }
 
+// The lists' labels decoded on the device, one thread per term (mode 0:
+// YPOT labels, 1: XPOT labels): the term's (K, a, b) key into a dense table
+// over K <= KLIMIT and the orbital pairs, marked present; the orbital it
+// multiplies (XPOT) and COEFF (XPOT: XA/C, as the reference forms it). A
+// label outside the orbital set or with K above KLIMIT sets *err.
+__global__ void k_parse_terms(int mode, int64_t nt, const int32_t *__restrict__ lab, const double *__restrict__ co,
+                              int nw, double c, int *__restrict__ tab, int *__restrict__ key,
+                              int *__restrict__ iorb, double *__restrict__ coef, int *__restrict__ err) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t l0 = lab[e];
+    int64_t l = l0;
+    const int k = (int)(l % KEYORB);
+    l /= KEYORB;
+    const int a = (int)(l % KEYORB);
+    l /= KEYORB;
+    const int64_t b = mode == 0 ? l : l % KEYORB;
+    const int64_t io = mode == 0 ? 1 : l / KEYORB;
+    if (l0 < 0 || k > KLIMIT || a < 1 || a > nw || b < 1 || b > nw || io < 1 || io > nw) {
+      atomicOr(err, 1);
+      key[e] = 0;
+      iorb[e] = 1;
+      coef[e] = 0.0;
+      continue;
+    }
+    const int kk = (k * nw + (a - 1)) * nw + (int)(b - 1);
+    tab[kk] = 1;
+    key[e] = kk;
+    iorb[e] = (int)io;
+    coef[e] = mode == 0 ? co[e] : co[e] / c;
+  }
+}
+
+// numbers the table's present (K, a, b) in table order (one block): the
+// entry becomes its function index + 1, the function's YZK descriptor is
+// written there, info[0] = the number of functions
+__global__ void __launch_bounds__(1024) k_number_functions(int *__restrict__ tab, int size, int nw,
+                                                            const int *__restrict__ MF, int n,
+                                                            YDesc *__restrict__ yd, int *__restrict__ info) {
+  __shared__ int part[1024];
+  const int per = (size + 1023) / 1024, lo = threadIdx.x * per, hi = min(size, lo + per);
+  int cnt = 0;
+  for (int e = lo; e < hi; ++e) cnt += tab[e] != 0;
+  part[threadIdx.x] = cnt;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {  // inclusive scan of the counts
+    const int v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
+    __syncthreads();
+    part[threadIdx.x] += v;
+    __syncthreads();
+  }
+  int f = part[threadIdx.x] - cnt;
+  for (int e = lo; e < hi; ++e)
+    if (tab[e]) {
+      const int k = e / (nw * nw), a = (e / nw) % nw + 1, b = e % nw + 1;
+      yd[f] = YDesc{k, a, b, min(MF[a], MF[b]), n, 0, 1};
+      tab[e] = ++f;
+    }
+  if (threadIdx.x == 1023) info[0] = part[1023];
+}
+
+__global__ void k_term_functions(int64_t nt, const int *__restrict__ key, const int *__restrict__ tab,
+                                 int *__restrict__ fidx) {
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nt; e += (int64_t)gridDim.x * blockDim.x)
+    fidx[e] = tab[key[e]] - 1;
+}
+
 // DPBDT (lib9290/dpbdt.f90:39-99): 13-point derivative of orbital J at grid
 // index i (1-based): the end rows from the 13 x 13 table, the interior by the
 // antisymmetric 12-neighbour formula.
@@ -1863,65 +1929,18 @@ static int run_rinti(gg_ctx *ctx, const std::vector<int2> &jk, int mode, double 
 }
 
 // YPOT / XPOT on the device: the list's distinct Y^k_ab (every grid point,
-// YZK's TB), then k_potential. A term list of one potential: per entry the
-// index of its Y function, the orbital it multiplies (XPOT) and COEFF.
-struct PotTerms {
-  std::vector<int> fidx, iorb;
-  std::vector<double> coef;
-};
-// the distinct (K, a, b) of one call's lists: a dense table over
-// K <= KLIMIT and the orbital pairs, holding function index + 1 (0: none)
-struct YKey {
-  std::vector<int> at;
-  int nw = 0;
-  int &slot(int k, int a, int b, int nw_) {
-    if (at.empty()) {
-      nw = nw_;
-      at.assign((size_t)(KLIMIT + 1) * nw * nw, 0);
-    }
-    return at[((size_t)k * nw + (a - 1)) * nw + (b - 1)];
-  }
+// YZK's TB), then k_potential. A list as the caller passed it: YPOT labels
+// NYA = (IOY2 KEY + IOY1) KEY + K, XPOT labels NXA = ((IORB KEY + IOY2) KEY +
+// IOY1) KEY + K, and their coefficients.
+struct RawList {
+  const int32_t *lab = nullptr;
+  const double *co = nullptr;
+  int n = 0;
 };
 
-// parses a YPOT (mode 0: NYA = (IOY2 KEY + IOY1) KEY + K) or XPOT (mode 1:
-// NXA = ((IORB KEY + IOY2) KEY + IOY1) KEY + K) list, adding its distinct Y
-// functions to hy (shared by all lists of one call)
-static int parse_terms(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const double *co, YKey &seen,
-                       std::vector<YDesc> &hy, PotTerms &t) {
-  const Orbitals &o = ctx->orb;
-  const Grid &g = ctx->grid;
-  const int nw = o.nw;
+static int raw_list(int ncof, const int32_t *lab, const double *co, RawList &r) {
   if (ncof < 0 || (ncof > 0 && (!lab || !co))) return fail(GG_ERR_ARG, "potential: bad coefficient list");
-  t.fidx.assign(ncof, 0);
-  t.iorb.assign(ncof, 1);
-  t.coef.assign(ncof, 0.0);
-  for (int e = 0; e < ncof; ++e) {
-    int64_t l = lab[e];
-    const int k = (int)(l % KEYORB);
-    l /= KEYORB;
-    const int a = (int)(l % KEYORB);
-    l /= KEYORB;
-    const int b = (int)(mode == 0 ? l : l % KEYORB);
-    const int io = (mode == 0) ? 1 : (int)(l / KEYORB);
-    if (lab[e] < 0 || k > KLIMIT || a < 1 || a > nw || b < 1 || b > nw || io < 1 || io > nw)
-      return fail(GG_ERR_ARG, "potential: label outside the orbital set or K above 20");
-    int &f = seen.slot(k, a, b, nw);
-    if (f == 0) {
-      YDesc y;
-      y.k = k;
-      y.b = a;
-      y.d = b;
-      y.mtp = std::min(o.mf[a], o.mf[b]);
-      y.mtpb = g.n;  // the whole function: the potentials use TB(1:N)
-      y.cs = 0;
-      y.nd = 1;
-      hy.push_back(y);
-      f = (int)hy.size();
-    }
-    t.fidx[e] = f - 1;
-    t.iorb[e] = io;
-    t.coef[e] = (mode == 0) ? co[e] : co[e] / g.c;  // XPOT: COEFF = COEFF/C
-  }
+  r = RawList{lab, co, ncof};
   return GG_OK;
 }
 
@@ -1932,7 +1951,7 @@ constexpr int XPOT_SPLIT = 512;
 // One orbital's potentials on the device: YP, XP, XQ (N each, 0-based) at
 // out, out + n, out + 2 n.
 struct PotJob {
-  PotTerms y, x;
+  RawList y, x;
   std::vector<int> nda;
   std::vector<double> da;
   std::vector<int> lag_m;      // LAGCON: the pairs' other orbitals
@@ -1941,31 +1960,88 @@ struct PotJob {
 
 // the jobs' YPOT, XPOT, then LAGCON and DACON, into dPot (3 n per job): all
 // Y functions of all lists built once
-static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vector<YDesc> &hy,
-                          DBuf<double> &dPot) {
+static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, DBuf<double> &dPot) {
   Orbitals &o = ctx->orb;
   Grid &g = ctx->grid;
   cudaStream_t s = ctx->stream;
-  const int n = g.n, nf = std::max(1, (int)hy.size());
+  const int n = g.n, nw = o.nw;
+  // every job's YPOT list, then every job's XPOT list, as the caller passed
+  // them, staged in pinned memory and copied to the device in one transfer
+  std::vector<size_t> oy(jobs.size()), ox(jobs.size());
+  size_t T = 0;
+  for (size_t j = 0; j < jobs.size(); ++j) oy[j] = T, T += (size_t)jobs[j].y.n;
+  const size_t TY = T;
+  for (size_t j = 0; j < jobs.size(); ++j) ox[j] = T, T += (size_t)jobs[j].x.n;
+  const size_t lab_bytes = (T * sizeof(int32_t) + 15) / 16 * 16, need = lab_bytes + T * sizeof(double);
+  if (need > ctx->pot_stage_bytes) {
+    void *hp = nullptr;
+    GG_CUDA(cudaHostAlloc(&hp, need + need / 4, cudaHostAllocDefault));
+    note_alloc();
+    ctx->pot_stage = std::shared_ptr<void>(hp, [](void *q) { cudaFreeHost(q); });
+    ctx->pot_stage_bytes = need + need / 4;
+  }
+  char *stage = static_cast<char *>(ctx->pot_stage.get());
+  int32_t *hlab = reinterpret_cast<int32_t *>(stage);
+  double *hco = reinterpret_cast<double *>(stage + lab_bytes);
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const RawList *L[2] = {&jobs[j].y, &jobs[j].x};
+    const size_t at[2] = {oy[j], ox[j]};
+    for (int m = 0; m < 2; ++m)
+      if (L[m]->n > 0) {
+        std::memcpy(hlab + at[m], L[m]->lab, (size_t)L[m]->n * sizeof(int32_t));
+        std::memcpy(hco + at[m], L[m]->co, (size_t)L[m]->n * sizeof(double));
+      }
+  }
+  const size_t tsize = (size_t)(KLIMIT + 1) * nw * nw;
+  DBuf<char> draw;
+  DBuf<int> dterm, dtab, dinfo;  // dterm: key, orbital, function index per term
+  DBuf<double> dcoef;
   DBuf<YDesc> dy;
+  GG_TRY(draw.alloc(std::max<size_t>(need, 16)));
+  GG_TRY(dterm.alloc(3 * std::max<size_t>(T, 1)));
+  GG_TRY(dcoef.alloc(std::max<size_t>(T, 1)));
+  GG_TRY(dtab.alloc(tsize));
+  GG_TRY(dinfo.alloc(2));
+  GG_TRY(dy.alloc(std::max<size_t>(1, std::min(T, tsize))));
+  int *dkey = dterm.p, *diorb = dkey + std::max<size_t>(T, 1), *dfidx = diorb + std::max<size_t>(T, 1);
+  const int32_t *dlab = reinterpret_cast<const int32_t *>(draw.p);
+  const double *dco = reinterpret_cast<const double *>(draw.p + lab_bytes);
+  if (T > 0) GG_CUDA(cudaMemcpyAsync(draw.p, stage, need, cudaMemcpyHostToDevice, s));
+  GG_CUDA(cudaMemsetAsync(dtab.p, 0, tsize * sizeof(int), s));
+  GG_CUDA(cudaMemsetAsync(dinfo.p, 0, 2 * sizeof(int), s));
+  const unsigned pgrid = (unsigned)std::max<size_t>(1, std::min<size_t>((T + 255) / 256, (size_t)8 * ctx->sms));
+  for (int m = 0; m < 2; ++m) {
+    const size_t a = m == 0 ? 0 : TY, cnt = m == 0 ? TY : T - TY;
+    if (cnt == 0) continue;
+    k_parse_terms<<<pgrid, 256, 0, s>>>(m, (int64_t)cnt, dlab + a, dco + a, nw, g.c, dtab.p, dkey + a, diorb + a,
+                                        dcoef.p + a, dinfo.p + 1);
+    ::gg::note_launch();
+  }
+  k_number_functions<<<1, 1024, 0, s>>>(dtab.p, (int)tsize, nw, o.dMF.p, n, dy.p, dinfo.p);
+  ::gg::note_launch();
+  int info[2] = {0, 0};
+  GG_CUDA(cudaMemcpyAsync(info, dinfo.p, sizeof(info), cudaMemcpyDeviceToHost, s));
+  GG_CUDA(cudaStreamSynchronize(s));
+  if (info[1]) return fail(GG_ERR_ARG, "potential: label outside the orbital set or K above 20");
+  if (T > 0) {
+    k_term_functions<<<pgrid, 256, 0, s>>>((int64_t)T, dkey, dtab.p, dfidx);
+    ::gg::note_launch();
+  }
+  const int nf = std::max(1, info[0]);
   DBuf<double> dY, scratch;
   GG_TRY(dY.alloc((size_t)nf * g.np));
-  if (!hy.empty()) {  // no terms: no function is read
-    GG_TRY(upload(dy, hy, s));
-    GG_TRY(build_y(ctx, dy.p, nf, dY.p, scratch));
-  }
+  if (info[0] > 0) GG_TRY(build_y(ctx, dy.p, nf, dY.p, scratch));  // no terms: no function is read
   GG_TRY(dPot.alloc((size_t)3 * n * std::max<size_t>(1, jobs.size())));
-  // every job's integer and coefficient arrays in one upload each
+  // the DACON and LAGCON lists (a few entries per job) in one upload each
   std::vector<int> ih;
   std::vector<double> dh;
-  struct Off { size_t yf, yc, xf, xi, xc, dn, dd, lm, lw; };
+  struct Off { size_t dn, dd, lm, lw; };
   std::vector<Off> off(jobs.size());
   for (size_t j = 0; j < jobs.size(); ++j) {
     const PotJob &J = jobs[j];
     auto pi = [&](const std::vector<int> &v) { size_t at = ih.size(); ih.insert(ih.end(), v.begin(), v.end()); ih.push_back(0); return at; };
     auto pd = [&](const std::vector<double> &v) { size_t at = dh.size(); dh.insert(dh.end(), v.begin(), v.end()); dh.push_back(0.0); return at; };
-    off[j] = Off{pi(J.y.fidx), pd(J.y.coef), pi(J.x.fidx), pi(J.x.iorb), pd(J.x.coef), pi(J.nda), pd(J.da),
-                 pi(J.lag_m), pd(J.lag_wa)};
+    off[j] = Off{pi(J.nda), pd(J.da), pi(J.lag_m), pd(J.lag_wa)};
   }
   DBuf<int> di;
   DBuf<double> dd, prod;
@@ -1978,16 +2054,16 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
   std::vector<PotSeg> hp;
   for (size_t j = 0; j < jobs.size(); ++j) {
     double *yp = dPot.p + (size_t)3 * n * j;
-    hp.push_back(PotSeg{di.p + off[j].yf, nullptr, dd.p + off[j].yc, yp, nullptr, (int)jobs[j].y.fidx.size()});
+    hp.push_back(PotSeg{dfidx + oy[j], nullptr, dcoef.p + oy[j], yp, nullptr, jobs[j].y.n});
   }
   const size_t nyseg = hp.size();
   for (size_t j = 0; j < jobs.size(); ++j) {
-    const int nx = (int)jobs[j].x.fidx.size();
+    const int nx = jobs[j].x.n;
     double *xp = dPot.p + (size_t)3 * n * j + n;
     if (nx >= XPOT_SPLIT)
       longj.push_back((int)j);
     else
-      hp.push_back(PotSeg{di.p + off[j].xf, di.p + off[j].xi, dd.p + off[j].xc, xp, xp + n, nx});
+      hp.push_back(PotSeg{dfidx + ox[j], diorb + ox[j], dcoef.p + ox[j], xp, xp + n, nx});
   }
   DBuf<PotSeg> dpseg;
   if (!hp.empty()) {
@@ -2023,12 +2099,12 @@ static int run_potentials(gg_ctx *ctx, const std::vector<PotJob> &jobs, std::vec
       const size_t r0 = hs.size();
       size_t po = 0;
       for (int j : longj) {
-        const int nx = (int)jobs[j].x.fidx.size();
+        const int nx = jobs[j].x.n;
         if (t0 >= nx) continue;
         const int nt = std::min(per, nx - t0);
         double *yp = dPot.p + (size_t)3 * n * j;
-        hs.push_back(XSeg{di.p + off[j].xf + t0, di.p + off[j].xi + t0, dd.p + off[j].xc + t0, nullptr, nullptr,
-                          yp + n, yp + 2 * n, nt});
+        hs.push_back(XSeg{dfidx + ox[j] + t0, diorb + ox[j] + t0, dcoef.p + ox[j] + t0, nullptr, nullptr, yp + n,
+                          yp + 2 * n, nt});
         poff.push_back(po);
         po += (size_t)2 * nt * n;
       }
@@ -2092,12 +2168,10 @@ static int potential(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const 
   GG_TRY(ensure_orbitals(ctx));
   if (!out0 || (mode == 1 && !out1)) return fail(GG_ERR_ARG, "gg_ypot/gg_xpot: bad arguments");
   GG_CUDA(cudaSetDevice(ctx->device));
-  std::vector<YDesc> hy;
-  YKey seen;
   std::vector<PotJob> jobs(1);
-  GG_TRY(parse_terms(ctx, mode, ncof, lab, co, seen, hy, mode == 0 ? jobs[0].y : jobs[0].x));
+  GG_TRY(raw_list(ncof, lab, co, mode == 0 ? jobs[0].y : jobs[0].x));
   DBuf<double> pot;
-  GG_TRY(run_potentials(ctx, jobs, hy, pot));
+  GG_TRY(run_potentials(ctx, jobs, pot));
   const int n = ctx->grid.n;
   if (mode == 0) {
     GG_CUDA(cudaMemcpy(out0, pot.p, n * sizeof(double), cudaMemcpyDeviceToHost));
@@ -2109,10 +2183,10 @@ static int potential(gg_ctx *ctx, int mode, int ncof, const int32_t *lab, const 
 }
 
 // one orbital's SETCOF lists as a job (DACON's list checked here)
-static int cof_job(gg_ctx *ctx, const gg_cof *c, YKey &seen, std::vector<YDesc> &hy, PotJob &J) {
+static int cof_job(gg_ctx *ctx, const gg_cof *c, PotJob &J) {
   if (!c) return fail(GG_ERR_ARG, "potential: missing coefficient lists");
-  GG_TRY(parse_terms(ctx, 0, c->ny, c->nya, c->ya, seen, hy, J.y));
-  GG_TRY(parse_terms(ctx, 1, c->nx, c->nxa, c->xa, seen, hy, J.x));
+  GG_TRY(raw_list(c->ny, c->nya, c->ya, J.y));
+  GG_TRY(raw_list(c->nx, c->nxa, c->xa, J.x));
   if (c->nd < 0 || (c->nd > 0 && (!c->nda || !c->da))) return fail(GG_ERR_ARG, "potential: bad DACON list");
   J.nda.assign(c->nda, c->nda + std::max(0, c->nd));
   J.da.assign(c->da, c->da + std::max(0, c->nd));
@@ -2141,10 +2215,8 @@ int gg_cofpot(gg_ctx *ctx, int j, double ucfj, const gg_cof *cof, int nec, const
   const int nw = ctx->orb.nw;
   if (j < 1 || j > nw) return fail(GG_ERR_ARG, "gg_cofpot: orbital outside the orbital set");
   GG_CUDA(cudaSetDevice(ctx->device));
-  std::vector<YDesc> hy;
-  YKey seen;
   std::vector<PotJob> jobs(1);
-  GG_TRY(cof_job(ctx, cof, seen, hy, jobs[0]));
+  GG_TRY(cof_job(ctx, cof, jobs[0]));
   // LAGCON's host part (lagcon.f90:32-45): the pairs with J and their weights
   if (nec > 0) {
     const double eps = (accy > 0 ? accy : std::pow(ctx->grid.h, 6)) * 0.01;
@@ -2166,7 +2238,7 @@ int gg_cofpot(gg_ctx *ctx, int j, double ucfj, const gg_cof *cof, int nec, const
     }
   }
   DBuf<double> pot;
-  GG_TRY(run_potentials(ctx, jobs, hy, pot));
+  GG_TRY(run_potentials(ctx, jobs, pot));
   const int n = ctx->grid.n;
   std::vector<double> h((size_t)3 * n);  // one read-back of YP, XP, XQ
   GG_CUDA(cudaMemcpy(h.data(), pot.p, h.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -2221,12 +2293,10 @@ int gg_setlag(gg_ctx *ctx, int nec, const int32_t *iecc, const double *ucf, cons
       ridx.push_back(k);
     }
   }
-  std::vector<YDesc> hy;
-  YKey seen;
   std::vector<PotJob> jobs(orbs.size());
-  for (size_t i = 0; i < orbs.size(); ++i) GG_TRY(cof_job(ctx, &cof[orbs[i] - 1], seen, hy, jobs[i]));
+  for (size_t i = 0; i < orbs.size(); ++i) GG_TRY(cof_job(ctx, &cof[orbs[i] - 1], jobs[i]));
   DBuf<double> pot;
-  GG_TRY(run_potentials(ctx, jobs, hy, pot));
+  GG_TRY(run_potentials(ctx, jobs, pot));
   cudaStream_t s = ctx->stream;
   DBuf<int4> dpj;
   DBuf<int2> dps;
