@@ -971,25 +971,38 @@ __global__ void k_xprod(const XSeg *__restrict__ segs, const double *__restrict_
 // sums XP = XP + P1, blockIdx.y = 1 sums XQ = XQ - P2. The loads run XSUM_AHEAD terms ahead of
 // the additions (register double buffer) so that the chain of dependent
 // FP64 additions, not the load latency, sets the time.
-constexpr int XSUM_AHEAD = 16;
+constexpr int XSUM_AHEAD = 32;
 template <bool SUB>
 __device__ __forceinline__ double xsum_chain(double acc, const double *__restrict__ P, int nt, int n) {
-  double cur[XSUM_AHEAD], nxt[XSUM_AHEAD];
+  constexpr int A = XSUM_AHEAD;
+  double cur[A], nxt[A];
+#pragma unroll
+  for (int u = 0; u < A; ++u) cur[u] = (u < nt) ? P[(size_t)u * n] : 0.0;
   int t = 0;
+  // while the next group is complete its loads need no bounds test
+  for (; t + 2 * A <= nt; t += A) {
+    const double *q = P + (size_t)(t + A) * n;
 #pragma unroll
-  for (int u = 0; u < XSUM_AHEAD; ++u) cur[u] = (u < nt) ? P[(size_t)u * n] : 0.0;
-  for (; t + XSUM_AHEAD <= nt; t += XSUM_AHEAD) {
-    const int t1 = t + XSUM_AHEAD;
+    for (int u = 0; u < A; ++u) nxt[u] = q[(size_t)u * n];
 #pragma unroll
-    for (int u = 0; u < XSUM_AHEAD; ++u) nxt[u] = (t1 + u < nt) ? P[(size_t)(t1 + u) * n] : 0.0;
+    for (int u = 0; u < A; ++u) acc = SUB ? acc - cur[u] : acc + cur[u];
 #pragma unroll
-    for (int u = 0; u < XSUM_AHEAD; ++u) acc = SUB ? acc - cur[u] : acc + cur[u];
-#pragma unroll
-    for (int u = 0; u < XSUM_AHEAD; ++u) cur[u] = nxt[u];
+    for (int u = 0; u < A; ++u) cur[u] = nxt[u];
   }
+  if (t + A <= nt) {  // cur is a complete group; fewer than A terms follow it
+    const int t1 = t + A;
 #pragma unroll
-  for (int u = 0; u < XSUM_AHEAD; ++u)
-    if (t + u < nt) acc = SUB ? acc - cur[u] : acc + cur[u];
+    for (int u = 0; u < A; ++u) nxt[u] = (t1 + u < nt) ? P[(size_t)(t1 + u) * n] : 0.0;
+#pragma unroll
+    for (int u = 0; u < A; ++u) acc = SUB ? acc - cur[u] : acc + cur[u];
+#pragma unroll
+    for (int u = 0; u < A; ++u)
+      if (t1 + u < nt) acc = SUB ? acc - nxt[u] : acc + nxt[u];
+  } else {  // fewer than A terms in all
+#pragma unroll
+    for (int u = 0; u < A; ++u)
+      if (t + u < nt) acc = SUB ? acc - cur[u] : acc + cur[u];
+  }
   return acc;
 }
 __global__ void k_xsum(const XSeg *__restrict__ segs, int n) {
