@@ -971,7 +971,7 @@ __global__ void k_xprod(const XSeg *__restrict__ segs, const double *__restrict_
 // sums XP = XP + P1, blockIdx.y = 1 sums XQ = XQ - P2. The loads run XSUM_AHEAD terms ahead of
 // the additions (register double buffer) so that the chain of dependent
 // FP64 additions, not the load latency, sets the time.
-constexpr int XSUM_AHEAD = 32;
+constexpr int XSUM_AHEAD = 48;
 template <bool SUB>
 __device__ __forceinline__ double xsum_chain(double acc, const double *__restrict__ P, int nt, int n) {
   constexpr int A = XSUM_AHEAD;
