@@ -880,32 +880,34 @@ __global__ void k_quad_table(const QuadItem *__restrict__ items, const int *__re
 // YPOT / XPOT (rmcdhf90/ypot.f90:35-49, xpot.f90:31-54): one thread per grid
 // point combines the list's Y functions in the list's order (the reference's
 // per-point operations: YP = YP - COEFF*TB; CTB = COEFF*TB, XP += CTB*QF,
-// XQ -= CTB*PF, with COEFF = XA/C formed on the host). One launch takes the
-// lists of several jobs (blockIdx.y); each thread loads the next POT_AHEAD
-// terms (index, coefficient, Y value, orbital values) before it combines
-// the current ones, so the loads do not wait on the chain.
+// XQ -= CTB*PF, with COEFF = XA/C). One launch takes the lists of several
+// jobs (blockIdx.y); each thread loads the next group of terms (index,
+// coefficient, Y value, orbital values; 16 for YPOT, 8 for XPOT) before it
+// combines the current ones, so the loads do not wait on the chain.
 struct PotSeg {
   const int *fidx, *iorb;
   const double *coef;
   double *out0, *out1;
   int ncof;
 };
-constexpr int POT_AHEAD = 8;
 template <int MODE>
 __global__ void k_potential(const PotSeg *__restrict__ segs, const double *__restrict__ Y, int np,
                             const double *__restrict__ ZZ, const double *__restrict__ PF,
                             const double *__restrict__ QF, int ld, int n) {
+  constexpr int A = MODE == 0 ? 16 : 8;  // terms loaded ahead
   const PotSeg g = segs[blockIdx.y];
   const int i = 1 + blockIdx.x * blockDim.x + threadIdx.x;
   if (i > n) return;
-  double cy[POT_AHEAD], cc[POT_AHEAD], cq[POT_AHEAD], cp[POT_AHEAD];
-  double ny[POT_AHEAD], nc[POT_AHEAD], nq[POT_AHEAD], npf[POT_AHEAD];
-  auto load = [&](int t0, double *y, double *c, double *qv, double *pv) {
+  const int nc = g.ncof;
+  double cy[A], cc[A], cq[A], cp[A];
+  double ny[A], nc_[A], nq[A], npf[A];
+  // terms t0 .. t0 + A - 1 (those below nc when `guard`)
+  auto load = [&](int t0, bool guard, double *y, double *c, double *qv, double *pv) {
 #pragma unroll
-    for (int u = 0; u < POT_AHEAD; ++u) {
+    for (int u = 0; u < A; ++u) {
       const int t = t0 + u;
       y[u] = c[u] = qv[u] = pv[u] = 0.0;
-      if (t < g.ncof) {
+      if (!guard || t < nc) {
         c[u] = g.coef[t];
         y[u] = Y[(size_t)g.fidx[t] * np + i];
         if (MODE == 1) {
@@ -917,27 +919,39 @@ __global__ void k_potential(const PotSeg *__restrict__ segs, const double *__res
     }
   };
   double a0 = (MODE == 0) ? ZZ[i] : 0.0, a1 = 0.0;
-  load(0, cy, cc, cq, cp);
-  for (int t0 = 0; t0 < g.ncof; t0 += POT_AHEAD) {
-    load(t0 + POT_AHEAD, ny, nc, nq, npf);
+  auto combine = [&](int t0, const double *y, const double *c, const double *qv, const double *pv) {
 #pragma unroll
-    for (int u = 0; u < POT_AHEAD; ++u)
-      if (t0 + u < g.ncof) {
+    for (int u = 0; u < A; ++u)
+      if (t0 + u < nc) {
         if (MODE == 0) {
-          a0 = a0 - cc[u] * cy[u];
+          a0 = a0 - c[u] * y[u];
         } else {
-          const double ctb = cc[u] * cy[u];
-          a0 = a0 + ctb * cq[u];
-          a1 = a1 - ctb * cp[u];
+          const double ctb = c[u] * y[u];
+          a0 = a0 + ctb * qv[u];
+          a1 = a1 - ctb * pv[u];
         }
       }
+  };
+  load(0, true, cy, cc, cq, cp);
+  int t = 0;
+  // while the next group is complete its loads need no bounds test
+  for (; t + 2 * A <= nc; t += A) {
+    load(t + A, false, ny, nc_, nq, npf);
+    combine(t, cy, cc, cq, cp);
 #pragma unroll
-    for (int u = 0; u < POT_AHEAD; ++u) {
+    for (int u = 0; u < A; ++u) {
       cy[u] = ny[u];
-      cc[u] = nc[u];
+      cc[u] = nc_[u];
       cq[u] = nq[u];
       cp[u] = npf[u];
     }
+  }
+  if (t + A <= nc) {  // cur is complete; fewer than A terms follow it
+    load(t + A, true, ny, nc_, nq, npf);
+    combine(t, cy, cc, cq, cp);
+    combine(t + A, ny, nc_, nq, npf);
+  } else {
+    combine(t, cy, cc, cq, cp);
   }
   g.out0[i - 1] = a0;
   if (MODE == 1) g.out1[i - 1] = a1;
